@@ -1,0 +1,132 @@
+/*
+ * mmo_gpu.h -- C ABI of the GB300 UFF scoring library (libmmo_gpu.so).
+ *
+ * Drop-in for the force-field scoring calls of UnixJunkie/MMO (paths inside
+ * that project).  MMO scores a ligand through OCaml closures of type
+ * Mol.t -> float:
+ *   ene_inter = Mol.ene_inter_UFF_shifted_bst prot_bst prot   (src/lds.ml:1952-1955)
+ *   ene_intra = Mol.ene_intra_UFFNB_brute                      (src/lds.ml:702-712)
+ * called once per Monte Carlo frame (src/lds.ml:900-905), per NLopt objective
+ * evaluation (src/lds.ml:1246-1251) and 2(6 + n) more times per numerical
+ * gradient (src/lds.ml:1118-1136).  The functions below replace those calls:
+ * the plain ones one call for one call, the batched one many poses (and the
+ * analytic gradient) per call.
+ *
+ * Conventions: every function returns MMO_OK (0) or a negative MMO_E* code;
+ * mmo_last_error() gives a message.  Host pointers unless the name ends in
+ * _device.  Energies are kcal/mol in FP64; coordinates in Angstrom.  A context
+ * owns one GPU and one CUDA stream and is not thread-safe; create it after any
+ * fork() (MMO forks its workers, src/lds.ml:2009,2050).
+ */
+#ifndef MMO_GPU_H
+#define MMO_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define MMO_OK 0
+#define MMO_EINVAL (-1)       /* bad argument (size, pointer, flag)             */
+#define MMO_ECUDA (-2)        /* CUDA runtime error                              */
+#define MMO_ENOMEM (-3)       /* device or pinned allocation failed              */
+#define MMO_ESTATE (-4)       /* protein or ligand not set                       */
+#define MMO_EELEMENT (-5)     /* atomic number not in the UFF table (UFF.ml:10-22) */
+#define MMO_ETIMEOUT (-6)     /* a bounded device-side wait gave up              */
+
+/* ---- physics switches (mmo_set_physics) ---------------------------------- */
+#define MMO_DIEL_CONST 0      /* eps = 4: K q_i q_j / r, K = 332.0637/4 (UFF.ml:25) */
+#define MMO_DIEL_DIST 1       /* eps = 4 r: K q_i q_j / r^2                       */
+#define MMO_MIX_GEOMEAN 0     /* x_ij = sqrt(x_i x_j), D_ij = sqrt(D_i D_j) (UFF.ml:47-48) */
+#define MMO_MIX_LB 1          /* x_ij = (x_i + x_j)/2, D_ij = sqrt(D_i D_j)       */
+#define MMO_INTER_SHIFTED 0   /* (1-(r/12)^2)^2 switch, 12 A cut: -ff BrL / Bst (mol.ml:822-849, 928-960) */
+#define MMO_INTER_GLOBAL 1    /* no switch, no cut: -ff BrG (mol.ml:796-818)      */
+#define MMO_INTRA_PLAIN 0     /* no switch, no cut (mol.ml:881-903)               */
+#define MMO_INTRA_SHIFTED 1   /* switch + 12 A cut (mol.ml:853-877)               */
+
+/* ---- mmo_score_poses flags ------------------------------------------------ */
+#define MMO_F_INTER 1         /* add the ligand-protein energy                    */
+#define MMO_F_INTRA 2         /* add the intra-ligand energy                      */
+#define MMO_F_GRAD 4          /* also dE/d[x, y, z, a, b, g, tau_0 ..]            */
+#define MMO_F_RECENTER 8      /* MC pose map (mol.ml:705-710) instead of Optim.apply_config (optim.ml:64-80) */
+
+/* ---- per-pose status bits ------------------------------------------------- */
+#define MMO_S_TOO_LONG 1      /* enclosing radius > 12 A: Mol.Too_long (mol.ml:587-591) */
+#define MMO_S_NONFINITE 2     /* energy is not finite                             */
+
+typedef struct mmo_ctx mmo_ctx;
+
+/* Last error message of ctx (or of the last failed mmo_ctx_create when ctx is NULL). */
+const char* mmo_last_error(const mmo_ctx* ctx);
+
+/* Open a context on CUDA device `device`.  Replaces nothing in MMO: it holds
+ * what the partial applications of src/lds.ml:1952-1979 close over. */
+int mmo_ctx_create(int device, mmo_ctx** out);
+int mmo_ctx_destroy(mmo_ctx* ctx);
+
+/* Physics switches; the default (all 0) is the reference's behaviour. */
+int mmo_set_physics(mmo_ctx* ctx, int dielectric, int mixing, int inter_form, int intra_form);
+
+/* Upload the rigid protein once: Mol.receptor_of_pqrs_file (mol.ml:412-417)
+ * plus the partial application `ff0 prot` (lds.ml:1967).  anum = atomic
+ * numbers (Mol.t.elt_a). */
+int mmo_set_protein(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
+                    const double* q, const int* anum);
+
+/* Upload the ligand once: the fields of Mol.t that a .pqrs ligand carries
+ * (pqrs.ml:41-87, mol.ml:384-402).  xs/ys/zs: centred reference conformer;
+ * interacting: n*n bytes, 1 where the topological distance is >= 3
+ * (mol.ml:203-208); bond_lr: 2*nrb (left, right) atoms of each rotatable bond;
+ * group_offsets[nrb+1] / group_atoms: each bond's rotation group with its right
+ * end excluded (pqrs.ml:343-351).  Replaces the per-ligand set-up of
+ * ene_intra_builder (lds.ml:702-712).  n <= 128, nrb <= 32. */
+int mmo_set_ligand(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
+                   const double* q, const int* anum, const uint8_t* interacting, int nrb,
+                   const int* bond_lr, const int* group_offsets, const int* group_atoms);
+
+/* Plain drop-in for Mol.ene_inter_UFF_shifted_bst / _shifted_brute /
+ * _global_brute (mol.ml:796-849, 928-960) on the protein of mmo_set_protein:
+ * one ligand (any n <= 128 atoms) per call, energy into *out. */
+int mmo_ene_inter(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
+                  const double* q, const int* anum, double* out);
+
+/* Plain drop-in for Mol.ene_intra_UFFNB_brute (mol.ml:881-903) on the ligand
+ * of mmo_set_ligand, at the given coordinates. */
+int mmo_ene_intra(mmo_ctx* ctx, const double* xs, const double* ys, const double* zs,
+                  double* out);
+
+/* Score B poses of the ligand of mmo_set_ligand.  dofs: B x (6 + nrb) floats,
+ * the config vector [x, y, z, a, b, g, tau_0 ..] of optim.ml:19-22 rebuilt by
+ * Optim.apply_config (optim.ml:64-80) or, with MMO_F_RECENTER, by the MC map
+ * centre-rotate-translate (mol.ml:705-710) with R = r_xyz(a, b, g).
+ * E_out[B] (FP64): E_inter and/or E_intra as flags select.  grad_out (null
+ * unless MMO_F_GRAD): B x (6 + nrb) floats, the analytic gradient replacing
+ * approx_local_gradient (lds.ml:1118-1136).  status_out[B] (nullable):
+ * MMO_S_* bits.  B = 1 runs the one-pose-per-launch plain path. */
+int mmo_score_poses(mmo_ctx* ctx, int B, const float* dofs, int flags, double* E_out,
+                    float* grad_out, int* status_out);
+
+/* As mmo_score_poses with device pointers, queued on `stream` (a
+ * cudaStream_t, or NULL for the context's stream) without synchronising;
+ * mmo_sync() waits and reports device-side errors. */
+int mmo_score_poses_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E,
+                           float* d_grad, int* d_status, void* stream);
+
+/* Wait for the context's work on `stream` (NULL: its own) and report any
+ * device-side error flag (MMO_ETIMEOUT). */
+int mmo_sync(mmo_ctx* ctx, void* stream);
+
+/* Tile shape of the batched pair kernel: poses per lane (1, 2, 4), threads
+ * per CTA (256, 512) and protein chunks per pose (0: automatic).  Setting 0
+ * for all restores the automatic choice. */
+int mmo_set_tiles(mmo_ctx* ctx, int poses_per_lane, int threads, int chunks);
+
+/* Number of SMs of the context's device (for callers that size batches). */
+int mmo_device_sms(const mmo_ctx* ctx, int* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,779 @@
+// capi.cu -- the extern "C" boundary of libmmo_gpu.so (include/mmo_gpu.h):
+// context, uploads of the protein and the ligand into their HBM layouts,
+// the plain drop-in calls and the batched pose scorer.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/mmo_diag.h"
+#include "../../include/mmo_gpu.h"
+#include "mmo_internal.cuh"
+
+using namespace mmo;
+
+namespace {
+
+// src/UFF.ml:10-22: (anum, x_i, D_i); index in this table = device type index
+struct UffRow {
+  int anum;
+  double xi, di;
+};
+constexpr UffRow kUff[kNTypes] = {{0, 0.0, 0.0},      {1, 2.886, 0.044},  {6, 3.851, 0.105},
+                                  {7, 3.660, 0.069},  {8, 3.500, 0.060},  {9, 3.364, 0.050},
+                                  {12, 3.021, 0.111}, {15, 4.147, 0.305}, {16, 4.035, 0.274},
+                                  {17, 3.947, 0.227}, {35, 4.189, 0.251}, {53, 4.500, 0.339}};
+constexpr double kElec = 332.0637 / 4.0;  // UFF.ml:25, const.ml:18
+
+int type_of(int anum) {
+  for (int t = 0; t < kNTypes; ++t)
+    if (kUff[t].anum == anum) return t;
+  return -1;
+}
+
+// (x_ij^2, D_ij) in double, rounded once
+void pair_xd(int mixing, int t1, int t2, double* x2, double* d) {
+  const double x1 = kUff[t1].xi, xb = kUff[t2].xi;
+  if (mixing == MMO_MIX_LB) {
+    const double x = 0.5 * (x1 + xb);
+    *x2 = x * x;
+  } else {
+    *x2 = x1 * xb;  // (sqrt(x_i x_j))^2, UFF.ml:47
+  }
+  *d = std::sqrt(kUff[t1].di * kUff[t2].di);  // UFF.ml:48
+}
+
+char g_create_err[256] = "";
+
+// next 16-byte aligned offset of a block of `bytes`
+size_t take(size_t& off, size_t bytes) {
+  const size_t o = (off + 15) & ~size_t(15);
+  off = o + bytes;
+  return o;
+}
+
+// pointer into `base` (or null while only sizing) for `count` T's
+template <class T>
+T* align_ptr(char* base, size_t& off, size_t count) {
+  const size_t o = take(off, sizeof(T) * count);
+  return base ? reinterpret_cast<T*>(base + o) : nullptr;
+}
+
+}  // namespace
+
+struct mmo_ctx {
+  int device = 0;
+  int sms = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  Physics ph{0, 0, 0, 0};
+  PairTable tab{};
+  int tile_kp = 0, tile_threads = 0, tile_chunks = 0;
+  // last launch plan and the inputs it was made for
+  PairPlan plan{};
+  long plan_key[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+
+  // protein
+  DevProtein prot{};
+  void* d_prot = nullptr;
+  double origin[3] = {0, 0, 0};
+  float origin_f[3] = {0, 0, 0};
+
+  // ligand (host copies kept for physics changes)
+  DevLigand lig{};
+  void* d_lig = nullptr;
+  bool has_lig = false;
+  std::vector<double> lx, ly, lz, lq;
+  std::vector<int> ltype, lbonds, lgoff, lgatoms;
+  std::vector<uint8_t> linter;
+
+  // scratch
+  Scratch scr{};
+  size_t capX = 0, capE = 0, capG = 0, capI = 0;
+  int* d_err = nullptr;
+
+  // stage timing (mmo_set_profiling)
+  bool profiling = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  bool ev_valid = false;
+
+  // host-API staging
+  char* h_in = nullptr;
+  char* h_out = nullptr;
+  char* d_in = nullptr;
+  char* d_out = nullptr;
+  size_t cap_in = 0, cap_out = 0;
+};
+
+namespace {
+
+int fail(mmo_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+int cuda_fail(mmo_ctx* c, cudaError_t e, const char* what) {
+  return fail(c, e == cudaErrorMemoryAllocation ? MMO_ENOMEM : MMO_ECUDA, "%s: %s", what,
+              cudaGetErrorString(e));
+}
+
+#define MMO_CK(call, what)                                \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+  } while (0)
+
+void rebuild_table(mmo_ctx* ctx) {
+  for (int a = 0; a < kNTypes; ++a)
+    for (int b = 0; b < kNTypes; ++b) {
+      double x2, d;
+      pair_xd(ctx->ph.mixing, a, b, &x2, &d);
+      ctx->tab.xd[a * kNTypes + b] = make_float2((float)x2, (float)d);
+    }
+}
+
+int grow(mmo_ctx* ctx, void** p, size_t* cap, size_t bytes, const char* what) {
+  if (bytes <= *cap) return MMO_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  bytes = std::max<size_t>(bytes, 256);
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, what);
+  *cap = bytes;
+  return MMO_OK;
+}
+
+int grow_host(mmo_ctx* ctx, char** h, char** d, size_t* cap, size_t bytes) {
+  if (bytes <= *cap) return MMO_OK;
+  if (*h) cudaFreeHost(*h);
+  if (*d) cudaFree(*d);
+  *h = *d = nullptr;
+  *cap = 0;
+  bytes = std::max<size_t>(bytes, 4096);
+  MMO_CK(cudaHostAlloc((void**)h, bytes, cudaHostAllocDefault), "pinned staging");
+  MMO_CK(cudaMalloc((void**)d, bytes), "device staging");
+  *cap = bytes;
+  return MMO_OK;
+}
+
+int ensure_scratch(mmo_ctx* ctx, int B, int L, int C, bool grad) {
+  int r;
+  const size_t n = (size_t)B * C * L;
+  if ((r = grow(ctx, (void**)&ctx->scr.X, &ctx->capX, sizeof(float4) * (size_t)B * L, "X")))
+    return r;
+  if ((r = grow(ctx, (void**)&ctx->scr.Epart, &ctx->capE, sizeof(double) * n, "Epart"))) return r;
+  if (grad && (r = grow(ctx, (void**)&ctx->scr.Gpart, &ctx->capG, sizeof(float4) * n, "Gpart")))
+    return r;
+  if ((r = grow(ctx, (void**)&ctx->scr.Eintra, &ctx->capI, sizeof(double) * (size_t)B,
+                "Eintra")))
+    return r;
+  ctx->scr.C = C;
+  return MMO_OK;
+}
+
+int upload_ligand(mmo_ctx* ctx) {
+  const int n = (int)ctx->lx.size(), nrb = (int)ctx->lbonds.size() / 2;
+  // interacting pairs (mol.ml:203-208), i < j, in the reference's loop order
+  std::vector<int2> pij;
+  std::vector<float4> ppar;
+  std::vector<std::vector<std::pair<int, float4>>> nb(n);
+  for (int i = 0; i < n - 1; ++i)
+    for (int j = i + 1; j < n; ++j) {
+      if (!ctx->linter[(size_t)i * n + j]) continue;
+      double x2, d;
+      pair_xd(ctx->ph.mixing, ctx->ltype[i], ctx->ltype[j], &x2, &d);
+      const float4 par = make_float4((float)x2, (float)d, (float)(kElec * ctx->lq[i] * ctx->lq[j]), 0.f);
+      pij.push_back(make_int2(i, j));
+      ppar.push_back(par);
+      nb[i].push_back({j, par});
+      nb[j].push_back({i, par});
+    }
+  std::vector<int> nb_off(n + 1, 0), nb_idx;
+  std::vector<float4> nb_par;
+  for (int i = 0; i < n; ++i) {
+    nb_off[i + 1] = nb_off[i] + (int)nb[i].size();
+    for (auto& e : nb[i]) {
+      nb_idx.push_back(e.first);
+      nb_par.push_back(e.second);
+    }
+  }
+  std::vector<float4> ref(n);
+  for (int i = 0; i < n; ++i)
+    ref[i] = make_float4((float)ctx->lx[i], (float)ctx->ly[i], (float)ctx->lz[i], (float)ctx->lq[i]);
+  std::vector<uint32_t> gmask((size_t)std::max(nrb, 1) * kSlots, 0u);
+  for (int t = 0; t < nrb; ++t)
+    for (int k = ctx->lgoff[t]; k < ctx->lgoff[t + 1]; ++k) {
+      const int a = ctx->lgatoms[k];
+      gmask[(size_t)t * kSlots + (a >> 5)] |= 1u << (a & 31);
+    }
+  std::vector<int2> bonds(std::max(nrb, 1));
+  for (int t = 0; t < nrb; ++t) bonds[t] = make_int2(ctx->lbonds[2 * t], ctx->lbonds[2 * t + 1]);
+  const int np = (int)pij.size();
+  // one blob: sizes first, then copy
+  size_t off = 0;
+  char* base = nullptr;
+  auto layout = [&](char* b) {
+    off = 0;
+    DevLigand L{};
+    L.L = n;
+    L.nrb = nrb;
+    L.npairs = np;
+    L.ref = align_ptr<float4>(b, off, n);
+    L.type = align_ptr<int>(b, off, n);
+    L.q = align_ptr<float>(b, off, n);
+    L.bonds = align_ptr<int2>(b, off, bonds.size());
+    L.gmask = align_ptr<uint32_t>(b, off, gmask.size());
+    L.pair_ij = align_ptr<int2>(b, off, std::max(np, 1));
+    L.pair_par = align_ptr<float4>(b, off, std::max(np, 1));
+    L.nb_off = align_ptr<int>(b, off, n + 1);
+    L.nb_idx = align_ptr<int>(b, off, std::max((int)nb_idx.size(), 1));
+    L.nb_par = align_ptr<float4>(b, off, std::max((int)nb_par.size(), 1));
+    return L;
+  };
+  layout(nullptr);
+  const size_t bytes = off;
+  std::vector<char> host(bytes, 0);
+  DevLigand H = layout(host.data());
+  memcpy((void*)H.ref, ref.data(), sizeof(float4) * n);
+  memcpy((void*)H.type, ctx->ltype.data(), sizeof(int) * n);
+  for (int i = 0; i < n; ++i) const_cast<float*>(H.q)[i] = (float)ctx->lq[i];
+  memcpy((void*)H.bonds, bonds.data(), sizeof(int2) * bonds.size());
+  memcpy((void*)H.gmask, gmask.data(), sizeof(uint32_t) * gmask.size());
+  if (np) {
+    memcpy((void*)H.pair_ij, pij.data(), sizeof(int2) * np);
+    memcpy((void*)H.pair_par, ppar.data(), sizeof(float4) * np);
+    memcpy((void*)H.nb_idx, nb_idx.data(), sizeof(int) * nb_idx.size());
+    memcpy((void*)H.nb_par, nb_par.data(), sizeof(float4) * nb_par.size());
+  }
+  memcpy((void*)H.nb_off, nb_off.data(), sizeof(int) * (n + 1));
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before ligand upload");
+  if (ctx->d_lig) cudaFree(ctx->d_lig);
+  ctx->d_lig = nullptr;
+  MMO_CK(cudaMalloc(&ctx->d_lig, bytes), "ligand blob");
+  MMO_CK(cudaMemcpy(ctx->d_lig, host.data(), bytes, cudaMemcpyHostToDevice), "ligand upload");
+  base = reinterpret_cast<char*>(ctx->d_lig);
+  ctx->lig = layout(base);
+  ctx->has_lig = true;
+  return MMO_OK;
+}
+
+PairPlan make_plan(mmo_ctx* ctx, int B, bool grad);
+
+// automatic tile plan for the batched pair kernel, cached per input shape
+PairPlan plan_for(mmo_ctx* ctx, int B, bool grad) {
+  const long key[8] = {B, grad, ctx->prot.P, ctx->lig.L, ctx->tile_kp, ctx->tile_threads,
+                       ctx->tile_chunks, ctx->ph.dielectric * 2 + ctx->ph.inter_form};
+  if (!std::equal(key, key + 8, ctx->plan_key)) {
+    ctx->plan = make_plan(ctx, B, grad);
+    std::copy(key, key + 8, ctx->plan_key);
+  }
+  return ctx->plan;
+}
+
+PairPlan make_plan(mmo_ctx* ctx, int B, bool grad) {
+  PairPlan p{};
+  p.kp = ctx->tile_kp ? ctx->tile_kp : (B >= 4096 ? 4 : (B >= 256 ? 2 : 1));
+  p.threads = ctx->tile_threads ? ctx->tile_threads : 512;
+  const int P = ctx->prot.P, L = ctx->lig.L;
+  const int nslices = (P + kSliceAtoms - 1) / kSliceAtoms;
+  const int slice_len = (P + nslices - 1) / nslices;
+  const int smem = slice_len * 16;
+  int bps = pairs_batched_max_blocks(p.kp, p.threads, grad, ctx->ph, smem);
+  if (bps < 1) bps = 1;
+  p.blocks = ctx->sms * bps;
+  const long W = (long)p.blocks * (p.threads / 32);
+  const long npb = (B + 32L * p.kp - 1) / (32L * p.kp);
+  int best = 1;
+  if (ctx->tile_chunks) {
+    best = std::max(1, ctx->tile_chunks / nslices);
+  } else {
+    double best_cost = 1e300;
+    for (int c = 1; c <= 64; ++c) {
+      const long items = npb * L * c;
+      const long waves = (items + W - 1) / W;
+      const long len = (slice_len + c - 1) / c;
+      const double cost = (double)waves * (double)(len + 48);
+      if (cost < best_cost - 1e-9) {
+        best_cost = cost;
+        best = c;
+      }
+    }
+  }
+  p.C = best * nslices;
+  const long items = npb * L * best;
+  const long need = (items + p.threads / 32 - 1) / (p.threads / 32);
+  if (need < p.blocks) p.blocks = (int)std::max(1L, need);
+  return p;
+}
+
+int check_dev_err(mmo_ctx* ctx, int flag) {
+  if (flag & kErrTimeout)
+    return fail(ctx, MMO_ETIMEOUT, "a bounded device-side wait (protein staging) gave up");
+  return MMO_OK;
+}
+
+int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E,
+                 float* d_grad, int* d_status, int* d_err, int zero_err, cudaStream_t st) {
+  if (!ctx->has_lig) return fail(ctx, MMO_ESTATE, "no ligand: call mmo_set_ligand first");
+  if ((flags & MMO_F_INTER) && ctx->prot.P <= 0)
+    return fail(ctx, MMO_ESTATE, "no protein: call mmo_set_protein first");
+  if (B < 0 || (B > 0 && (!d_dofs || !d_E || !d_status)))
+    return fail(ctx, MMO_EINVAL, "bad batch arguments");
+  if ((flags & MMO_F_GRAD) && !d_grad) return fail(ctx, MMO_EINVAL, "MMO_F_GRAD needs grad_out");
+  if (B == 0) return MMO_OK;
+  const bool grad = flags & MMO_F_GRAD;
+  const bool inter = (flags & MMO_F_INTER) && ctx->prot.P > 0;
+  const int L = ctx->lig.L;
+  PairPlan plan{};
+  int C = 1;
+  if (inter) {
+    if (B == 1) {
+      C = std::max(1, (ctx->prot.P + 255) / 256);
+    } else {
+      plan = plan_for(ctx, B, grad);
+      C = plan.C;
+    }
+  }
+  int r = ensure_scratch(ctx, B, L, C, grad);
+  if (r) return r;
+  PoseIO io{};
+  io.dofs = d_dofs;
+  io.E = d_E;
+  io.grad = grad ? d_grad : nullptr;
+  io.status = d_status;
+  io.err = d_err;
+  io.zero_err = zero_err;
+  io.B = B;
+  io.ox = ctx->origin_f[0];
+  io.oy = ctx->origin_f[1];
+  io.oz = ctx->origin_f[2];
+  int fl = flags & (kFlagInter | kFlagIntra | kFlagGrad | kFlagRecenter);
+  if (!inter) fl &= ~kFlagInter;
+  const bool prof = ctx->profiling;
+  if (prof) MMO_CK(cudaEventRecord(ctx->ev[0], st), "event");
+  MMO_CK(launch_rebuild(ctx->lig, io, ctx->scr, fl, ctx->ph.intra_form, ctx->ph.dielectric, st),
+         "rebuild kernel");
+  if (prof) MMO_CK(cudaEventRecord(ctx->ev[1], st), "event");
+  if (inter) {
+    if (B == 1) {
+      MMO_CK(launch_pairs_plain(ctx->prot, ctx->tab, ctx->scr.X, ctx->lig.q, ctx->lig.type, L, C,
+                                ctx->scr.Epart, ctx->scr.Gpart, grad, ctx->ph, st),
+             "plain pair kernel");
+    } else {
+      MMO_CK(launch_pairs_batched(ctx->prot, ctx->tab, ctx->lig, ctx->scr, B, fl, ctx->ph, plan,
+                                  d_err, st),
+             "batched pair kernel");
+    }
+  }
+  if (prof) MMO_CK(cudaEventRecord(ctx->ev[2], st), "event");
+  MMO_CK(launch_finish(ctx->lig, io, ctx->scr, fl, ctx->ph, st), "finish kernel");
+  if (prof) {
+    MMO_CK(cudaEventRecord(ctx->ev[3], st), "event");
+    ctx->ev_valid = true;
+  }
+  return MMO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mmo_last_error(const mmo_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_err; }
+
+int mmo_ctx_create(int device, mmo_ctx** out) {
+  if (!out) return MMO_EINVAL;
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || device < 0 || device >= ndev) {
+    snprintf(g_create_err, sizeof g_create_err, "no CUDA device %d (%s)", device,
+             e != cudaSuccess ? cudaGetErrorString(e) : "out of range");
+    return e != cudaSuccess ? MMO_ECUDA : MMO_EINVAL;
+  }
+  mmo_ctx* ctx = new (std::nothrow) mmo_ctx();
+  if (!ctx) return MMO_ENOMEM;
+  ctx->device = device;
+  if ((e = cudaSetDevice(device)) != cudaSuccess ||
+      (e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device)) !=
+          cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaMalloc((void**)&ctx->d_err, sizeof(int))) != cudaSuccess ||
+      (e = cudaMemset(ctx->d_err, 0, sizeof(int))) != cudaSuccess) {
+    snprintf(g_create_err, sizeof g_create_err, "context set-up: %s", cudaGetErrorString(e));
+    delete ctx;
+    return e == cudaErrorMemoryAllocation ? MMO_ENOMEM : MMO_ECUDA;
+  }
+  rebuild_table(ctx);
+  *out = ctx;
+  return MMO_OK;
+}
+
+int mmo_ctx_destroy(mmo_ctx* ctx) {
+  if (!ctx) return MMO_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  cudaFree(ctx->d_prot);
+  cudaFree(ctx->d_lig);
+  cudaFree(ctx->scr.X);
+  cudaFree(ctx->scr.Epart);
+  cudaFree(ctx->scr.Gpart);
+  cudaFree(ctx->scr.Eintra);
+  for (auto& e : ctx->ev)
+    if (e) cudaEventDestroy(e);
+  cudaFree(ctx->d_err);
+  cudaFree(ctx->d_in);
+  cudaFree(ctx->d_out);
+  if (ctx->h_in) cudaFreeHost(ctx->h_in);
+  if (ctx->h_out) cudaFreeHost(ctx->h_out);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return MMO_OK;
+}
+
+int mmo_set_physics(mmo_ctx* ctx, int dielectric, int mixing, int inter_form, int intra_form) {
+  if (!ctx) return MMO_EINVAL;
+  if ((dielectric | mixing | inter_form | intra_form) & ~1)
+    return fail(ctx, MMO_EINVAL, "physics switches are 0 or 1");
+  ctx->ph = Physics{dielectric, mixing, inter_form, intra_form};
+  rebuild_table(ctx);
+  if (ctx->has_lig) return upload_ligand(ctx);
+  return MMO_OK;
+}
+
+int mmo_set_tiles(mmo_ctx* ctx, int kp, int threads, int chunks) {
+  if (!ctx) return MMO_EINVAL;
+  if (!(kp == 0 || kp == 1 || kp == 2 || kp == 4) ||
+      !(threads == 0 || threads == 256 || threads == 512) || chunks < 0 || chunks > 4096)
+    return fail(ctx, MMO_EINVAL, "tiles: poses_per_lane in {0,1,2,4}, threads in {0,256,512}");
+  ctx->tile_kp = kp;
+  ctx->tile_threads = threads;
+  ctx->tile_chunks = chunks;
+  return MMO_OK;
+}
+
+int mmo_device_sms(const mmo_ctx* ctx, int* out) {
+  if (!ctx || !out) return MMO_EINVAL;
+  *out = ctx->sms;
+  return MMO_OK;
+}
+
+int mmo_set_protein(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
+                    const double* q, const int* anum) {
+  if (!ctx) return MMO_EINVAL;
+  if (n < 0 || (n > 0 && (!xs || !ys || !zs || !q || !anum)))
+    return fail(ctx, MMO_EINVAL, "mmo_set_protein: bad arguments");
+  std::vector<int> type(n);
+  double o[3] = {0, 0, 0};
+  for (int i = 0; i < n; ++i) {
+    type[i] = type_of(anum[i]);
+    if (type[i] < 0)
+      return fail(ctx, MMO_EELEMENT, "protein atom %d: element %d not in the UFF table", i, anum[i]);
+    if (!std::isfinite(xs[i]) || !std::isfinite(ys[i]) || !std::isfinite(zs[i]) ||
+        !std::isfinite(q[i]))
+      return fail(ctx, MMO_EINVAL, "protein atom %d: non-finite coordinate or charge", i);
+    o[0] += xs[i];
+    o[1] += ys[i];
+    o[2] += zs[i];
+  }
+  if (n > 0)
+    for (int d = 0; d < 3; ++d) o[d] /= n;
+  float of[3] = {(float)o[0], (float)o[1], (float)o[2]};
+  // stable sort by type: runs of constant pair parameters
+  std::vector<int> idx(n);
+  std::iota(idx.begin(), idx.end(), 0);
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return type[a] < type[b]; });
+  std::vector<float4> atoms(std::max(n, 1));
+  std::vector<uint8_t> ptype(std::max(n, 16), 0);
+  std::vector<int> rstart, rtype;
+  DevProtein P{};
+  P.P = n;
+  for (int k = 0; k < n; ++k) {
+    const int i = idx[k];
+    atoms[k] = make_float4((float)(xs[i] - (double)of[0]), (float)(ys[i] - (double)of[1]),
+                           (float)(zs[i] - (double)of[2]), (float)(kElec * q[i]));
+    ptype[k] = (uint8_t)type[i];
+    if (k == 0 || type[i] != type[idx[k - 1]]) {
+      rstart.push_back(k);
+      rtype.push_back(type[i]);
+    }
+  }
+  P.nruns = (int)rtype.size();
+  rstart.push_back(n);
+  std::vector<int> runs(2 * kNTypes + 1, 0);
+  std::copy(rstart.begin(), rstart.end(), runs.begin());
+  std::copy(rtype.begin(), rtype.end(), runs.begin() + P.nruns + 1);
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before protein upload");
+  if (ctx->d_prot) cudaFree(ctx->d_prot);
+  ctx->d_prot = nullptr;
+  size_t off = 0;
+  const size_t o_atoms = take(off, sizeof(float4) * atoms.size());
+  const size_t o_type = take(off, ptype.size());
+  const size_t o_runs = take(off, sizeof(int) * runs.size());
+  std::vector<char> blob(off, 0);
+  memcpy(blob.data() + o_atoms, atoms.data(), sizeof(float4) * atoms.size());
+  memcpy(blob.data() + o_type, ptype.data(), ptype.size());
+  memcpy(blob.data() + o_runs, runs.data(), sizeof(int) * runs.size());
+  MMO_CK(cudaMalloc(&ctx->d_prot, off), "protein");
+  MMO_CK(cudaMemcpy(ctx->d_prot, blob.data(), off, cudaMemcpyHostToDevice), "protein upload");
+  P.atoms = reinterpret_cast<const float4*>((char*)ctx->d_prot + o_atoms);
+  P.type = reinterpret_cast<const uint8_t*>((char*)ctx->d_prot + o_type);
+  P.runs = reinterpret_cast<const int*>((char*)ctx->d_prot + o_runs);
+  ctx->prot = P;
+  for (int d = 0; d < 3; ++d) {
+    ctx->origin[d] = (double)of[d];
+    ctx->origin_f[d] = of[d];
+  }
+  return MMO_OK;
+}
+
+int mmo_set_ligand(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
+                   const double* q, const int* anum, const uint8_t* interacting, int nrb,
+                   const int* bond_lr, const int* group_offsets, const int* group_atoms) {
+  if (!ctx) return MMO_EINVAL;
+  if (n < 1 || n > kMaxLig)
+    return fail(ctx, MMO_EINVAL, "mmo_set_ligand: n = %d outside 1..%d", n, kMaxLig);
+  if (nrb < 0 || nrb > kMaxTors)
+    return fail(ctx, MMO_EINVAL, "mmo_set_ligand: nrb = %d outside 0..%d", nrb, kMaxTors);
+  if (!xs || !ys || !zs || !q || !anum || !interacting ||
+      (nrb > 0 && (!bond_lr || !group_offsets || !group_atoms)))
+    return fail(ctx, MMO_EINVAL, "mmo_set_ligand: null array");
+  std::vector<int> type(n);
+  for (int i = 0; i < n; ++i) {
+    type[i] = type_of(anum[i]);
+    if (type[i] < 0)
+      return fail(ctx, MMO_EELEMENT, "ligand atom %d: element %d not in the UFF table", i, anum[i]);
+    if (!std::isfinite(xs[i]) || !std::isfinite(ys[i]) || !std::isfinite(zs[i]) ||
+        !std::isfinite(q[i]))
+      return fail(ctx, MMO_EINVAL, "ligand atom %d: non-finite coordinate or charge", i);
+  }
+  std::vector<int> goff, gat, bonds;
+  if (nrb > 0) {
+    goff.assign(group_offsets, group_offsets + nrb + 1);
+    if (goff[0] != 0) return fail(ctx, MMO_EINVAL, "group_offsets[0] must be 0");
+    for (int t = 0; t < nrb; ++t) {
+      const int l = bond_lr[2 * t], r = bond_lr[2 * t + 1];
+      if (l < 0 || l >= n || r < 0 || r >= n || l == r)
+        return fail(ctx, MMO_EINVAL, "rotatable bond %d: bad atoms (%d, %d)", t, l, r);
+      if (goff[t + 1] < goff[t]) return fail(ctx, MMO_EINVAL, "group_offsets not monotone");
+      for (int k = goff[t]; k < goff[t + 1]; ++k) {
+        const int a = group_atoms[k];
+        if (a < 0 || a >= n || a == r || a == l)
+          return fail(ctx, MMO_EINVAL, "rotation group %d: bad atom %d", t, a);
+      }
+      bonds.push_back(l);
+      bonds.push_back(r);
+    }
+    gat.assign(group_atoms, group_atoms + goff[nrb]);
+  }
+  ctx->lx.assign(xs, xs + n);
+  ctx->ly.assign(ys, ys + n);
+  ctx->lz.assign(zs, zs + n);
+  ctx->lq.assign(q, q + n);
+  ctx->ltype = type;
+  ctx->lbonds = bonds;
+  ctx->lgoff = nrb > 0 ? goff : std::vector<int>{0};
+  ctx->lgatoms = gat;
+  ctx->linter.assign(interacting, interacting + (size_t)n * n);
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  return upload_ligand(ctx);
+}
+
+int mmo_ene_inter(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
+                  const double* q, const int* anum, double* out) {
+  if (!ctx) return MMO_EINVAL;
+  if (n < 0 || n > kMaxLig || !out || (n > 0 && (!xs || !ys || !zs || !q || !anum)))
+    return fail(ctx, MMO_EINVAL, "mmo_ene_inter: bad arguments (n <= %d)", kMaxLig);
+  if (n == 0 || ctx->prot.P == 0) {
+    *out = 0.0;
+    return MMO_OK;
+  }
+  // staging: X[n] float4 | q[n] float | type[n] int ; output: C*n doubles | E
+  const int C = std::max(1, (ctx->prot.P + 255) / 256);
+  size_t off = 0;
+  const size_t oX = take(off, sizeof(float4) * n);
+  const size_t oq = take(off, sizeof(float) * n);
+  const size_t ot = take(off, sizeof(int) * n);
+  const size_t in_bytes = off;
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  int r = grow_host(ctx, &ctx->h_in, &ctx->d_in, &ctx->cap_in, in_bytes);
+  if (r) return r;
+  r = grow_host(ctx, &ctx->h_out, &ctx->d_out, &ctx->cap_out, sizeof(double) * ((size_t)C * n + 1));
+  if (r) return r;
+  float4* hX = reinterpret_cast<float4*>(ctx->h_in + oX);
+  float* hq = reinterpret_cast<float*>(ctx->h_in + oq);
+  int* ht = reinterpret_cast<int*>(ctx->h_in + ot);
+  for (int i = 0; i < n; ++i) {
+    const int t = type_of(anum[i]);
+    if (t < 0) return fail(ctx, MMO_EELEMENT, "ligand atom %d: element %d not in the UFF table", i, anum[i]);
+    hX[i] = make_float4((float)(xs[i] - ctx->origin[0]), (float)(ys[i] - ctx->origin[1]),
+                        (float)(zs[i] - ctx->origin[2]), 0.f);
+    hq[i] = (float)q[i];
+    ht[i] = t;
+  }
+  const float4* dX = reinterpret_cast<const float4*>(ctx->d_in + oX);
+  const float* dq = reinterpret_cast<const float*>(ctx->d_in + oq);
+  const int* dt = reinterpret_cast<const int*>(ctx->d_in + ot);
+  double* dEp = reinterpret_cast<double*>(ctx->d_out);
+  double* dE = dEp + (size_t)C * n;
+  MMO_CK(cudaMemcpyAsync(ctx->d_in, ctx->h_in, in_bytes, cudaMemcpyHostToDevice, ctx->stream),
+         "H2D");
+  MMO_CK(launch_pairs_plain(ctx->prot, ctx->tab, dX, dq, dt, n, C, dEp, nullptr, 0, ctx->ph,
+                            ctx->stream),
+         "plain pair kernel");
+  MMO_CK(launch_reduce_plain(dEp, C * n, dE, ctx->stream), "reduce kernel");
+  MMO_CK(cudaMemcpyAsync(ctx->h_out, dE, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+         "D2H");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync");
+  memcpy(out, ctx->h_out, sizeof(double));
+  return MMO_OK;
+}
+
+int mmo_ene_intra(mmo_ctx* ctx, const double* xs, const double* ys, const double* zs,
+                  double* out) {
+  if (!ctx) return MMO_EINVAL;
+  if (!ctx->has_lig) return fail(ctx, MMO_ESTATE, "no ligand: call mmo_set_ligand first");
+  if (!xs || !ys || !zs || !out) return fail(ctx, MMO_EINVAL, "mmo_ene_intra: null pointer");
+  const int n = ctx->lig.L;
+  int r = grow_host(ctx, &ctx->h_in, &ctx->d_in, &ctx->cap_in, sizeof(float4) * n);
+  if (r) return r;
+  r = grow_host(ctx, &ctx->h_out, &ctx->d_out, &ctx->cap_out, sizeof(double));
+  if (r) return r;
+  float4* hX = reinterpret_cast<float4*>(ctx->h_in);
+  // the intra term is translation-invariant: centre on atom 0 before rounding
+  for (int i = 0; i < n; ++i)
+    hX[i] = make_float4((float)(xs[i] - xs[0]), (float)(ys[i] - ys[0]), (float)(zs[i] - zs[0]), 0.f);
+  MMO_CK(cudaMemcpyAsync(ctx->d_in, ctx->h_in, sizeof(float4) * n, cudaMemcpyHostToDevice,
+                         ctx->stream),
+         "H2D");
+  MMO_CK(launch_intra_plain(ctx->lig, reinterpret_cast<const float4*>(ctx->d_in),
+                            ctx->ph.intra_form, ctx->ph.dielectric,
+                            reinterpret_cast<double*>(ctx->d_out), ctx->stream),
+         "intra kernel");
+  MMO_CK(cudaMemcpyAsync(ctx->h_out, ctx->d_out, sizeof(double), cudaMemcpyDeviceToHost,
+                         ctx->stream),
+         "D2H");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync");
+  memcpy(out, ctx->h_out, sizeof(double));
+  return MMO_OK;
+}
+
+int mmo_score_poses(mmo_ctx* ctx, int B, const float* dofs, int flags, double* E_out,
+                    float* grad_out, int* status_out) {
+  if (!ctx) return MMO_EINVAL;
+  if (!ctx->has_lig) return fail(ctx, MMO_ESTATE, "no ligand: call mmo_set_ligand first");
+  if (B < 0 || (B > 0 && (!dofs || !E_out)) || ((flags & MMO_F_GRAD) && !grad_out))
+    return fail(ctx, MMO_EINVAL, "mmo_score_poses: bad arguments");
+  if (B == 0) return MMO_OK;
+  const int nd = 6 + ctx->lig.nrb;
+  const bool grad = flags & MMO_F_GRAD;
+  // output block: E[B] | grad[B][nd] | status[B] | err
+  size_t off = 0;
+  take(off, sizeof(double) * B);
+  const size_t o_grad = take(off, grad ? sizeof(float) * (size_t)B * nd : 0);
+  const size_t o_st = take(off, sizeof(int) * B);
+  const size_t o_err = take(off, sizeof(int));
+  const size_t out_bytes = off;
+  const size_t in_bytes = sizeof(float) * (size_t)B * nd;
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  int r = grow_host(ctx, &ctx->h_in, &ctx->d_in, &ctx->cap_in, in_bytes);
+  if (r) return r;
+  r = grow_host(ctx, &ctx->h_out, &ctx->d_out, &ctx->cap_out, out_bytes);
+  if (r) return r;
+  memcpy(ctx->h_in, dofs, in_bytes);
+  MMO_CK(cudaMemcpyAsync(ctx->d_in, ctx->h_in, in_bytes, cudaMemcpyHostToDevice, ctx->stream),
+         "H2D");
+  r = score_device(ctx, B, reinterpret_cast<const float*>(ctx->d_in), flags,
+                   reinterpret_cast<double*>(ctx->d_out),
+                   grad ? reinterpret_cast<float*>(ctx->d_out + o_grad) : nullptr,
+                   reinterpret_cast<int*>(ctx->d_out + o_st),
+                   reinterpret_cast<int*>(ctx->d_out + o_err), 1, ctx->stream);
+  if (r) return r;
+  MMO_CK(cudaMemcpyAsync(ctx->h_out, ctx->d_out, out_bytes, cudaMemcpyDeviceToHost, ctx->stream),
+         "D2H");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync");
+  memcpy(E_out, ctx->h_out, sizeof(double) * B);
+  if (grad) memcpy(grad_out, ctx->h_out + o_grad, sizeof(float) * (size_t)B * nd);
+  if (status_out) memcpy(status_out, ctx->h_out + o_st, sizeof(int) * B);
+  return check_dev_err(ctx, *reinterpret_cast<int*>(ctx->h_out + o_err));
+}
+
+int mmo_score_poses_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E,
+                           float* d_grad, int* d_status, void* stream) {
+  if (!ctx) return MMO_EINVAL;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : ctx->stream;
+  return score_device(ctx, B, d_dofs, flags, d_E, d_grad, d_status, ctx->d_err, 0, st);
+}
+
+int mmo_sync(mmo_ctx* ctx, void* stream) {
+  if (!ctx) return MMO_EINVAL;
+  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : ctx->stream;
+  MMO_CK(cudaStreamSynchronize(st), "sync");
+  int flag = 0;
+  MMO_CK(cudaMemcpy(&flag, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+  if (flag) MMO_CK(cudaMemset(ctx->d_err, 0, sizeof(int)), "clear error flag");
+  return check_dev_err(ctx, flag);
+}
+
+int mmo_set_profiling(mmo_ctx* ctx, int on) {
+  if (!ctx) return MMO_EINVAL;
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  if (on && !ctx->ev[0])
+    for (auto& e : ctx->ev) MMO_CK(cudaEventCreate(&e), "event create");
+  ctx->profiling = on != 0;
+  ctx->ev_valid = false;
+  return MMO_OK;
+}
+
+int mmo_stage_times(mmo_ctx* ctx, float* ms) {
+  if (!ctx || !ms) return MMO_EINVAL;
+  if (!ctx->ev_valid) return fail(ctx, MMO_ESTATE, "no profiled scoring call yet");
+  MMO_CK(cudaEventSynchronize(ctx->ev[3]), "event sync");
+  for (int k = 0; k < 3; ++k)
+    MMO_CK(cudaEventElapsedTime(&ms[k], ctx->ev[k], ctx->ev[k + 1]), "elapsed");
+  return MMO_OK;
+}
+
+int mmo_fp32_fma_peak(mmo_ctx* ctx, double* tflops, double* ms_out) {
+  if (!ctx || !tflops) return MMO_EINVAL;
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  float* d = nullptr;
+  MMO_CK(cudaMalloc(&d, sizeof(float)), "probe buffer");
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  double flops = 0.0, best = 0.0, best_ms = 0.0;
+  cudaError_t e = cudaSuccess;
+  for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {
+    cudaEventRecord(a, ctx->stream);
+    e = launch_fma_peak(ctx->sms, 8192, d, ctx->stream, &flops);
+    cudaEventRecord(b, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    if (e == cudaSuccess && rep > 0 && flops / (ms * 1e-3) > best) {
+      best = flops / (ms * 1e-3);
+      best_ms = ms;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "fma probe");
+  *tflops = best * 1e-12;
+  if (ms_out) *ms_out = best_ms;
+  return MMO_OK;
+}
+
+}  // extern "C"

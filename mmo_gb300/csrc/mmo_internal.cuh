@@ -1,0 +1,207 @@
+// mmo_internal.cuh -- device data layout, launch plans and shared helpers of
+// the GB300 (sm_103a) UFF scoring library.  Not part of the public C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mmo {
+
+constexpr int kMaxLig = 128;    // ligand atoms per system (4 per lane in a warp)
+constexpr int kSlots = kMaxLig / 32;
+constexpr int kMaxTors = 32;    // rotatable bonds per ligand
+constexpr int kNTypes = 12;     // UFF elements of src/UFF.ml:10-22
+constexpr int kSliceAtoms = 12288;  // protein atoms resident in shared memory per launch
+constexpr float kCut2 = 144.0f;     // 12 A cutoff, squared (const.ml:12-14)
+constexpr float kMinR2 = 1e-4f;     // (0.01 A)^2, Math.non_zero_dist (math.ml:58-62)
+
+// Protein in HBM: atoms sorted by UFF type so that the pair parameters are
+// constant over each run; (x, y, z) are relative to the frame origin and w is
+// K * q with K = 332.0637 / 4.
+struct DevProtein {
+  const float4* atoms;    // [P]
+  const uint8_t* type;    // [P] type index, for the plain kernel
+  const int* runs;        // [2 * kNTypes + 1]: run_start[nruns + 1], then run_type[nruns]
+  int P;
+  int nruns;
+};
+
+// Pair parameters (x_ij^2, D_ij) for every type pair, passed by value so that
+// warp-uniform lookups hit the constant bank.
+struct PairTable {
+  float2 xd[kNTypes * kNTypes];
+};
+
+// Ligand topology and reference conformer in HBM.
+struct DevLigand {
+  int L, nrb, npairs;
+  const float4* ref;        // [L] (x, y, z, q) centred conformer
+  const int* type;          // [L] type index
+  const float* q;           // [L] partial charge
+  const int2* bonds;        // [nrb] (left, right) rotation axis
+  const uint32_t* gmask;    // [nrb][kSlots] group bitmask, bit (a & 31) of word (a >> 5)
+  const int2* pair_ij;      // [npairs] interacting pairs i < j (mol.ml:203-208)
+  const float4* pair_par;   // [npairs] (x^2, D, K q_i q_j, 0)
+  const int* nb_off;        // [L + 1] both-direction CSR of the same pairs
+  const int* nb_idx;        // partner atom
+  const float4* nb_par;     // (x^2, D, K q_i q_j, 0)
+};
+
+// Per-pose work buffers, pose-major so the warp-per-pose kernels read them
+// contiguously.  C = protein chunks per pose.
+struct Scratch {
+  float4* X;       // [B][L] posed coordinates in the device frame
+  double* Epart;   // [B][C][L] inter energy partial per chunk and ligand atom
+  float4* Gpart;   // [B][C][L] dE/dX partial per chunk and ligand atom
+  double* Eintra;  // [B]
+  int C;
+};
+
+struct PoseIO {
+  const float* dofs;  // [B][6 + nrb] optimiser layout (optim.ml:19-22)
+  double* E;          // [B]
+  float* grad;        // [B][6 + nrb] or null
+  int* status;        // [B]
+  int* err;           // device-side error flag (kErr* bits)
+  int zero_err;       // the rebuild kernel clears *err first
+  int B;
+  float ox, oy, oz;   // frame origin subtracted from the translation
+};
+
+enum : int { kFlagInter = 1, kFlagIntra = 2, kFlagGrad = 4, kFlagRecenter = 8 };
+enum : int { kStatusTooLong = 1, kStatusNonFinite = 2 };
+enum : int { kErrTimeout = 1 };
+
+struct Physics {
+  int dielectric;  // 0: eps = 4; 1: eps = 4 r
+  int mixing;      // 0: geometric mean; 1: Lorentz-Berthelot
+  int inter_form;  // 0: shifted 12 A; 1: global
+  int intra_form;  // 0: plain; 1: shifted 12 A
+};
+
+// Launch plan of the batched pair kernel (chosen by the tuner).
+struct PairPlan {
+  int kp;        // poses per lane: 1, 2 or 4
+  int threads;   // threads per CTA: 256 or 512
+  int C;         // protein chunks per pose
+  int blocks;    // persistent grid size
+};
+
+// ---- launchers (defined in the .cu files) --------------------------------
+cudaError_t launch_rebuild(const DevLigand& lig, const PoseIO& io, const Scratch& s,
+                           int flags, int intra_form, int dielectric, cudaStream_t st);
+cudaError_t launch_pairs_batched(const DevProtein& prot, const PairTable& tab,
+                                 const DevLigand& lig, const Scratch& s, int B, int flags,
+                                 const Physics& ph, const PairPlan& plan, int* d_err,
+                                 cudaStream_t st);
+cudaError_t launch_pairs_plain(const DevProtein& prot, const PairTable& tab, const float4* X,
+                               const float* lig_q, const int* lig_type, int L, int C,
+                               double* Epart, float4* Gpart, int grad, const Physics& ph,
+                               cudaStream_t st);
+cudaError_t launch_finish(const DevLigand& lig, const PoseIO& io, const Scratch& s, int flags,
+                          const Physics& ph, cudaStream_t st);
+cudaError_t launch_reduce_plain(const double* Epart, int n, double* out, cudaStream_t st);
+cudaError_t launch_intra_plain(const DevLigand& lig, const float4* X, int form, int dielectric,
+                               double* out, cudaStream_t st);
+int pairs_batched_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_bytes);
+cudaError_t launch_fma_peak(int sms, int iters, float* out, cudaStream_t st, double* flops);
+
+// ---- device helpers ------------------------------------------------------
+#ifdef __CUDACC__
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// One UFF nonbonded pair, FP32.  d = ligand - partner.  FORM 0: shifted by
+// (1 - (r/12)^2)^2 and cut at 12 A (mol.ml:836-845); FORM 1: unshifted
+// (mol.ml:811-815, 894-900).  DIEL 0: K qq / r; DIEL 1: K qq / r^2.  The
+// distance is clamped at 0.01 A (math.ml:58-62), where the derivative is 0.
+// acc += E_pair; with GRAD, g += dE_pair/dd.
+template <bool GRAD, int DIEL, int FORM>
+__device__ __forceinline__ void uff_pair(float dx, float dy, float dz, float x2, float D,
+                                         float qq, float& acc, float& gx, float& gy,
+                                         float& gz) {
+  const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  const float r2c = fmaxf(r2, kMinR2);
+  const float ir = rsqrtf(r2c);
+  const float ir2 = ir * ir;
+  const float p2 = x2 * ir2;
+  const float p6 = p2 * p2 * p2;
+  const float Dp6 = D * p6;
+  const float lj = Dp6 * (p6 - 2.0f);
+  const float el = DIEL == 0 ? qq * ir : qq * ir2;
+  const float e = lj + el;
+  float s = 1.0f, w = 1.0f;
+  if (FORM == 0) {
+    s = fmaxf(fmaf(r2c, -1.0f / 144.0f, 1.0f), 0.0f);
+    w = s * s;
+  }
+  acc = fmaf(w, e, acc);
+  if (GRAD) {
+    // 2 dE/dr2: w (2 dLJ/dr2 + 2 dEl/dr2) + 2 dw/dr2 * e
+    const float t = fmaf(-12.0f, Dp6 * (p6 - 1.0f), DIEL == 0 ? -el : -2.0f * el);
+    float g = w * t * ir2;
+    if (FORM == 0) g = fmaf(s * (-1.0f / 36.0f), e, g);
+    g = r2 < kMinR2 ? 0.0f : g;
+    gx = fmaf(g, dx, gx);
+    gy = fmaf(g, dy, gy);
+    gz = fmaf(g, dz, gz);
+  }
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// 1-D bulk copy global -> shared through the TMA engine; 16-byte aligned
+// addresses and a size that is a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// Bounded wait on an mbarrier phase: returns false after max_iter polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t max_iter) {
+  for (uint32_t it = 0; it < max_iter; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+#endif
+
+}  // namespace mmo

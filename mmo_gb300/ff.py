@@ -1,0 +1,239 @@
+"""Host-side mirror of MMO's force-field scoring interface over the CUDA library.
+
+MMO (src/lds.ml) scores a ligand with two closures of type Mol.t -> float:
+
+* ``ene_inter``: ``Mol.ene_inter_UFF_global_brute`` / ``_shifted_brute`` /
+  ``_shifted_bst prot_bst`` applied to the protein (src/lds.ml:1952-1955,
+  1965-1967, selected by ``-ff BrG|BrL|Bst``);
+* ``ene_intra``: ``Mol.ene_intra_UFFNB_brute`` (src/lds.ml:702-712).
+
+:func:`ene_inter_builder` and :func:`ene_intra_builder` return the same
+closures backed by the GPU; :class:`UFFScorer` adds the batched pose scorer
+with the analytic gradient that replaces ``approx_local_gradient``
+(src/lds.ml:1118-1136).  Errors follow the reference: an enclosing radius
+above 12 A raises :class:`TooLong` (Mol.Too_long, src/mol.ml:587-591) where the
+reference raises it (Optim.apply_config, src/optim.ml:75).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import lib as _L
+from .topology import Mol
+
+
+class TooLong(Exception):
+    """Mol.Too_long: the conformer's enclosing radius exceeds 12 A."""
+
+
+@dataclass(frozen=True)
+class Physics:
+    """Physics switches; the defaults are the reference's behaviour."""
+
+    dielectric: int = _L.DIEL_CONST
+    mixing: int = _L.MIX_GEOMEAN
+    inter_form: int = _L.INTER_SHIFTED
+    intra_form: int = _L.INTRA_PLAIN
+
+
+FF_STYLES = {"BrG": _L.INTER_GLOBAL, "BrL": _L.INTER_SHIFTED, "Bst": _L.INTER_SHIFTED}
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, np.float64)
+
+
+class UFFScorer:
+    """One GPU context holding a protein and a ligand (libmmo_gpu.so)."""
+
+    def __init__(self, device: int = 0, physics: Physics = Physics()):
+        self._lib = _L.load()
+        h = C.c_void_p()
+        _L.check(self._lib.mmo_ctx_create(device, C.byref(h)), None)
+        self._h = h
+        self.device = device
+        self.physics = physics
+        self.protein: Mol | None = None
+        self.ligand: Mol | None = None
+        if physics != Physics():
+            self.set_physics(physics)
+
+    # -- lifetime --------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.mmo_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, code: int) -> None:
+        _L.check(code, self._h)
+
+    # -- set-up ----------------------------------------------------------
+    def set_physics(self, ph: Physics) -> None:
+        self._check(self._lib.mmo_set_physics(self._h, ph.dielectric, ph.mixing, ph.inter_form,
+                                              ph.intra_form))
+        self.physics = ph
+
+    def set_tiles(self, poses_per_lane=0, threads=0, chunks=0) -> None:
+        self._check(self._lib.mmo_set_tiles(self._h, poses_per_lane, threads, chunks))
+
+    def sms(self) -> int:
+        out = C.c_int()
+        self._check(self._lib.mmo_device_sms(self._h, C.byref(out)))
+        return out.value
+
+    def set_protein(self, prot: Mol) -> None:
+        x, y, z, q = (_f64(v) for v in (prot.x, prot.y, prot.z, prot.q))
+        an = np.ascontiguousarray(prot.anum, np.int32)
+        self._check(self._lib.mmo_set_protein(self._h, prot.n, _dp(x), _dp(y), _dp(z), _dp(q),
+                                              _ip(an)))
+        self.protein = prot
+
+    def set_ligand(self, lig: Mol) -> None:
+        """``lig`` is the centred reference conformer (the ``centered_lig`` of
+        src/lds.ml), with its rotatable bonds and rotation groups."""
+        x, y, z, q = (_f64(v) for v in (lig.x, lig.y, lig.z, lig.q))
+        an = np.ascontiguousarray(lig.anum, np.int32)
+        inter = np.ascontiguousarray(lig.interacting, np.uint8)
+        bonds = np.ascontiguousarray(lig.rbonds.reshape(-1), np.int32)
+        off, atoms = lig.group_arrays()
+        off = np.ascontiguousarray(off, np.int32)
+        atoms = np.ascontiguousarray(atoms if atoms.size else np.zeros(1, np.int32), np.int32)
+        if not bonds.size:
+            bonds = np.zeros(2, np.int32)
+        self._check(self._lib.mmo_set_ligand(
+            self._h, lig.n, _dp(x), _dp(y), _dp(z), _dp(q), _ip(an),
+            inter.ctypes.data_as(C.POINTER(C.c_uint8)), lig.nrb, _ip(bonds), _ip(off),
+            _ip(atoms)))
+        self.ligand = lig
+
+    # -- plain drop-ins (one call per Mol.t, like the reference closures) --
+    def ene_inter(self, lig: Mol) -> float:
+        """Mol.ene_inter_UFF_shifted_bst prot_bst prot lig (src/mol.ml:958-960)."""
+        x, y, z, q = (_f64(v) for v in (lig.x, lig.y, lig.z, lig.q))
+        an = np.ascontiguousarray(lig.anum, np.int32)
+        out = C.c_double()
+        self._check(self._lib.mmo_ene_inter(self._h, lig.n, _dp(x), _dp(y), _dp(z), _dp(q),
+                                            _ip(an), C.byref(out)))
+        return out.value
+
+    def ene_intra(self, lig: Mol) -> float:
+        """Mol.ene_intra_UFFNB_brute lig (src/mol.ml:881-903) for the ligand of
+        set_ligand at lig's coordinates."""
+        x, y, z = (_f64(v) for v in (lig.x, lig.y, lig.z))
+        out = C.c_double()
+        self._check(self._lib.mmo_ene_intra(self._h, _dp(x), _dp(y), _dp(z), C.byref(out)))
+        return out.value
+
+    # -- batched poses -----------------------------------------------------
+    def score_poses(self, dofs, inter=True, intra=True, grad=False, recenter=False):
+        """E (float64 [B]), grad (float32 [B, 6+nrb] or None), status (int32 [B]).
+
+        dofs: float32 [B, 6 + nrb] in the Optim.config layout
+        [x, y, z, a, b, g, tau_0 ...] (src/optim.ml:19-22)."""
+        dofs = np.ascontiguousarray(dofs, np.float32)
+        if dofs.ndim == 1:
+            dofs = dofs[None, :]
+        B, nd = dofs.shape
+        if self.ligand is None or nd != 6 + self.ligand.nrb:
+            raise ValueError("dofs must be [B, 6 + nrb] for the ligand of set_ligand")
+        flags = ((_L.F_INTER if inter else 0) | (_L.F_INTRA if intra else 0) |
+                 (_L.F_GRAD if grad else 0) | (_L.F_RECENTER if recenter else 0))
+        E = np.zeros(B, np.float64)
+        G = np.zeros((B, nd), np.float32) if grad else None
+        st = np.zeros(B, np.int32)
+        self._check(self._lib.mmo_score_poses(
+            self._h, B, dofs.ctypes.data_as(C.POINTER(C.c_float)), flags, _dp(E),
+            G.ctypes.data_as(C.POINTER(C.c_float)) if G is not None else None, _ip(st)))
+        return E, G, st
+
+    def score_config(self, conf, recenter=False) -> float:
+        """E_inter + E_intra of one Optim.config, raising TooLong as
+        Optim.apply_config does (src/optim.ml:75)."""
+        E, _, st = self.score_poses(np.asarray(conf, np.float32)[None, :], recenter=recenter)
+        if st[0] & _L.S_TOO_LONG:
+            raise TooLong()
+        return float(E[0])
+
+    def score_poses_device(self, d_dofs: int, B: int, d_E: int, d_grad: int | None,
+                           d_status: int, flags: int, stream: int | None = None) -> None:
+        """Raw device-pointer entry point (integers are device addresses)."""
+        self._check(self._lib.mmo_score_poses_device(self._h, B, d_dofs, flags, d_E,
+                                                     d_grad or None, d_status, stream))
+
+    def sync(self, stream: int | None = None) -> None:
+        self._check(self._lib.mmo_sync(self._h, stream))
+
+    # -- measurement ------------------------------------------------------
+    def set_profiling(self, on: bool) -> None:
+        self._check(self._lib.mmo_set_profiling(self._h, int(on)))
+
+    def stage_times(self):
+        """(rebuild, pair sweep, finish) device ms of the last scoring call."""
+        ms = (C.c_float * 3)()
+        self._check(self._lib.mmo_stage_times(self._h, ms))
+        return tuple(float(v) for v in ms)
+
+    def fp32_peak_tflops(self) -> float:
+        t, ms = C.c_double(), C.c_double()
+        self._check(self._lib.mmo_fp32_fma_peak(self._h, C.byref(t), C.byref(ms)))
+        return t.value
+
+
+def ene_inter_builder(prot: Mol, ff_style: str = "Bst", device: int = 0,
+                      physics: Physics = Physics()):
+    """``ff0 prot`` of src/lds.ml:1952-1967 on the GPU: Mol -> float."""
+    ph = Physics(physics.dielectric, physics.mixing, FF_STYLES[ff_style], physics.intra_form)
+    s = UFFScorer(device, ph)
+    s.set_protein(prot)
+
+    def ene_inter(lig: Mol) -> float:
+        return s.ene_inter(lig)
+
+    ene_inter.scorer = s
+    return ene_inter
+
+
+def ene_intra_builder(centered_lig: Mol, tweak_rbonds: bool = True, device: int = 0,
+                      physics: Physics = Physics()):
+    """``ene_intra_builder UFF_NB`` of src/lds.ml:702-712 on the GPU: for a
+    rigid ligand (or no rotatable bond) the constant E_intra of the start
+    conformer, else Mol -> E_intra."""
+    s = UFFScorer(device, physics)
+    s.set_ligand(centered_lig)
+    if tweak_rbonds and centered_lig.nrb > 0:
+        def ene_intra(lig: Mol) -> float:
+            return s.ene_intra(lig)
+    else:
+        const = s.ene_intra(centered_lig)
+
+        def ene_intra(_lig: Mol) -> float:
+            return const
+    ene_intra.scorer = s
+    return ene_intra

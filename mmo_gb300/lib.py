@@ -1,0 +1,74 @@
+"""ctypes binding of libmmo_gpu.so (include/mmo_gpu.h).
+
+The library is built in-tree (mmo_gb300/build.py).  There is no fallback: if
+the shared library is missing or fails to load, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmmo_gpu.so")
+
+OK, EINVAL, ECUDA, ENOMEM, ESTATE, EELEMENT, ETIMEOUT = 0, -1, -2, -3, -4, -5, -6
+DIEL_CONST, DIEL_DIST = 0, 1
+MIX_GEOMEAN, MIX_LB = 0, 1
+INTER_SHIFTED, INTER_GLOBAL = 0, 1
+INTRA_PLAIN, INTRA_SHIFTED = 0, 1
+F_INTER, F_INTRA, F_GRAD, F_RECENTER = 1, 2, 4, 8
+S_TOO_LONG, S_NONFINITE = 1, 2
+
+# every symbol the header declares, with its ctypes signature
+_P = C.POINTER
+_d, _i, _vp, _cp = C.c_double, C.c_int, C.c_void_p, C.c_char_p
+SIGNATURES = {
+    "mmo_last_error": (_cp, [_vp]),
+    "mmo_ctx_create": (_i, [_i, _P(_vp)]),
+    "mmo_ctx_destroy": (_i, [_vp]),
+    "mmo_set_physics": (_i, [_vp, _i, _i, _i, _i]),
+    "mmo_set_protein": (_i, [_vp, _i, _P(_d), _P(_d), _P(_d), _P(_d), _P(_i)]),
+    "mmo_set_ligand": (_i, [_vp, _i, _P(_d), _P(_d), _P(_d), _P(_d), _P(_i), _P(C.c_uint8), _i,
+                            _P(_i), _P(_i), _P(_i)]),
+    "mmo_ene_inter": (_i, [_vp, _i, _P(_d), _P(_d), _P(_d), _P(_d), _P(_i), _P(_d)]),
+    "mmo_ene_intra": (_i, [_vp, _P(_d), _P(_d), _P(_d), _P(_d)]),
+    "mmo_score_poses": (_i, [_vp, _i, _P(C.c_float), _i, _P(_d), _P(C.c_float), _P(_i)]),
+    "mmo_score_poses_device": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp, _vp]),
+    "mmo_sync": (_i, [_vp, _vp]),
+    "mmo_set_tiles": (_i, [_vp, _i, _i, _i]),
+    "mmo_device_sms": (_i, [_vp, _P(_i)]),
+    "mmo_set_profiling": (_i, [_vp, _i]),
+    "mmo_stage_times": (_i, [_vp, _P(C.c_float)]),
+    "mmo_fp32_fma_peak": (_i, [_vp, _P(_d), _P(_d)]),
+}
+
+
+class MMOError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s (code %d)" % (msg, code))
+        self.code = code
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the CUDA library once; raise if it is not built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError("libmmo_gpu.so is not built: run mmo_gb300.build.build() "
+                               "(nvcc, sm_103a); there is no CPU fallback")
+        lib = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def check(code: int, ctx=None) -> None:
+    if code != OK:
+        msg = load().mmo_last_error(ctx)
+        raise MMOError(code, msg.decode() if msg else "error")

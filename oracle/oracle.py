@@ -1,0 +1,255 @@
+"""ctypes front end of the FP64 C oracle (uff_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
+and by bench.py's CPU-baseline leg, never by the mmo_gb300 package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+
+F_INTER, F_INTRA, F_RECENTER = 1, 2, 8
+S_TOO_LONG, S_NONFINITE = 1, 2
+
+
+class Physics(C.Structure):
+    _fields_ = [("dielectric", C.c_int), ("mixing", C.c_int), ("inter_form", C.c_int),
+                ("intra_form", C.c_int)]
+
+
+class CMol(C.Structure):
+    _fields_ = [("n", C.c_int), ("x", C.POINTER(C.c_double)), ("y", C.POINTER(C.c_double)),
+                ("z", C.POINTER(C.c_double)), ("q", C.POINTER(C.c_double)),
+                ("anum", C.POINTER(C.c_int))]
+
+
+class CLigand(C.Structure):
+    _fields_ = [("m", CMol), ("interacting", C.POINTER(C.c_uint8)), ("nrb", C.c_int),
+                ("bond_lr", C.POINTER(C.c_int)), ("grp_off", C.POINTER(C.c_int)),
+                ("grp_atoms", C.POINTER(C.c_int))]
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(
+                os.path.join(HERE, "uff_oracle.c")):
+            build()
+        L = C.CDLL(LIB)
+        P = C.POINTER
+        d, i, v = C.c_double, C.c_int, None
+        sig = {
+            "orc_elec_weight": (d, []),
+            "orc_uff_params": (i, [i, P(d), P(d)]),
+            "orc_pair_params": (v, [P(Physics), i, i, P(d), P(d)]),
+            "orc_shift_12A": (d, [d]),
+            "orc_non_zero_dist": (d, [d]),
+            "orc_dihedral": (d, [P(d), P(d), P(d), P(d)]),
+            "orc_rot_xyz": (v, [d, d, d, P(d)]),
+            "orc_rot_axis_angle": (v, [P(d), d, P(d)]),
+            "orc_rotate_bond": (v, [i, P(d), P(d), P(d), i, i, P(i), i, d]),
+            "orc_ene_inter": (d, [P(Physics), P(CMol), P(CMol)]),
+            "orc_ene_inter_parts": (v, [P(Physics), P(CMol), P(CMol), P(d)]),
+            "orc_ene_intra": (d, [P(Physics), P(CMol), P(C.c_uint8)]),
+            "orc_cells_build": (C.c_void_p, [P(CMol)]),
+            "orc_cells_free": (v, [C.c_void_p]),
+            "orc_ene_inter_cells": (d, [P(Physics), C.c_void_p, P(CMol)]),
+            "orc_apply_config": (i, [P(CLigand), P(d), i, P(d), P(d), P(d)]),
+            "orc_score_conf": (d, [P(Physics), P(CMol), C.c_void_p, P(CLigand), P(d), i, P(i)]),
+            "orc_grad_fd": (v, [P(Physics), P(CMol), C.c_void_p, P(CLigand), P(d), i, P(d),
+                                P(d)]),
+            "orc_grad_analytic": (d, [P(Physics), P(CMol), P(CLigand), P(d), i, P(d), P(d),
+                                      P(i)]),
+            "orc_score_batch": (v, [P(Physics), P(CMol), P(CLigand), i, P(C.c_float), i, i,
+                                    P(d), i, i, P(d), P(d), P(i)]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def physics(dielectric=0, mixing=0, inter_form=0, intra_form=0) -> Physics:
+    return Physics(dielectric, mixing, inter_form, intra_form)
+
+
+REF = physics()
+
+
+class OMol:
+    """Keeps the numpy buffers of a CMol alive."""
+
+    def __init__(self, x, y, z, q, anum):
+        self.arrs = [np.ascontiguousarray(a, np.float64) for a in (x, y, z, q)]
+        self.anum = np.ascontiguousarray(anum, np.int32)
+        self.c = CMol(len(self.anum), *(_dp(a) for a in self.arrs), _ip(self.anum))
+
+    @classmethod
+    def of(cls, m, xyz=None):
+        if xyz is None:
+            return cls(m.x, m.y, m.z, m.q, m.anum)
+        xyz = np.asarray(xyz, np.float64)
+        return cls(xyz[:, 0], xyz[:, 1], xyz[:, 2], m.q, m.anum)
+
+
+class OLigand:
+    def __init__(self, m):
+        self.mol = OMol.of(m)
+        self.inter = np.ascontiguousarray(m.interacting, np.uint8)
+        self.bonds = np.ascontiguousarray(m.rbonds.reshape(-1), np.int32)
+        off, atoms = m.group_arrays()
+        self.off = np.ascontiguousarray(off, np.int32)
+        self.atoms = np.ascontiguousarray(atoms if atoms.size else np.zeros(1, np.int32), np.int32)
+        self.nrb = m.nrb
+        self.c = CLigand(self.mol.c, self.inter.ctypes.data_as(C.POINTER(C.c_uint8)), m.nrb,
+                         _ip(self.bonds if self.bonds.size else np.zeros(1, np.int32)),
+                         _ip(self.off), _ip(self.atoms))
+        self._keep = [self.bonds]
+
+
+def elec_weight() -> float:
+    return lib().orc_elec_weight()
+
+
+def pair_params(a1, a2, ph=REF):
+    xo, do = C.c_double(), C.c_double()
+    lib().orc_pair_params(C.byref(ph), a1, a2, C.byref(xo), C.byref(do))
+    return xo.value, do.value
+
+
+def shift_12A(d):
+    return lib().orc_shift_12A(d)
+
+
+def non_zero_dist(d):
+    return lib().orc_non_zero_dist(d)
+
+
+def dihedral(i, j, k, l):
+    arrs = [np.ascontiguousarray(v, np.float64) for v in (i, j, k, l)]
+    return lib().orc_dihedral(*(_dp(a) for a in arrs))
+
+
+def rot_xyz(a, b, g):
+    R = np.zeros(9)
+    lib().orc_rot_xyz(a, b, g, _dp(R))
+    return R.reshape(3, 3)
+
+
+def rotate_bond(xyz, left, right, group, alpha):
+    xyz = np.asarray(xyz, np.float64)
+    x, y, z = (np.ascontiguousarray(xyz[:, d]) for d in range(3))
+    g = np.ascontiguousarray(group, np.int32)
+    lib().orc_rotate_bond(len(x), _dp(x), _dp(y), _dp(z), left, right,
+                          _ip(g if g.size else np.zeros(1, np.int32)), len(g), alpha)
+    return np.stack([x, y, z], axis=1)
+
+
+def ene_inter(prot, lig, xyz=None, ph=REF):
+    p, l = OMol.of(prot), OMol.of(lig, xyz)
+    return lib().orc_ene_inter(C.byref(ph), C.byref(p.c), C.byref(l.c))
+
+
+def ene_inter_parts(prot, lig, xyz=None, ph=REF):
+    p, l = OMol.of(prot), OMol.of(lig, xyz)
+    out = np.zeros(2)
+    lib().orc_ene_inter_parts(C.byref(ph), C.byref(p.c), C.byref(l.c), _dp(out))
+    return out
+
+
+def ene_inter_cells(prot, lig, xyz=None, ph=REF):
+    p, l = OMol.of(prot), OMol.of(lig, xyz)
+    cells = lib().orc_cells_build(C.byref(p.c))
+    try:
+        return lib().orc_ene_inter_cells(C.byref(ph), cells, C.byref(l.c))
+    finally:
+        lib().orc_cells_free(cells)
+
+
+def ene_intra(lig, xyz=None, ph=REF):
+    l = OMol.of(lig, xyz)
+    inter = np.ascontiguousarray(lig.interacting, np.uint8)
+    return lib().orc_ene_intra(C.byref(ph), C.byref(l.c),
+                               inter.ctypes.data_as(C.POINTER(C.c_uint8)))
+
+
+def apply_config(lig, conf, flags=0):
+    L = OLigand(lig)
+    conf = np.ascontiguousarray(conf, np.float64)
+    x, y, z = np.zeros(lig.n), np.zeros(lig.n), np.zeros(lig.n)
+    st = lib().orc_apply_config(C.byref(L.c), _dp(conf), flags, _dp(x), _dp(y), _dp(z))
+    return np.stack([x, y, z], axis=1), st
+
+
+def score_conf(prot, lig, conf, flags=F_INTER | F_INTRA, ph=REF):
+    p, L = OMol.of(prot), OLigand(lig)
+    conf = np.ascontiguousarray(conf, np.float64)
+    st = C.c_int()
+    e = lib().orc_score_conf(C.byref(ph), C.byref(p.c), None, C.byref(L.c), _dp(conf), flags,
+                             C.byref(st))
+    return e, st.value
+
+
+def grad_fd(prot, lig, conf, eps, flags=F_INTER | F_INTRA, ph=REF):
+    p, L = OMol.of(prot), OLigand(lig)
+    conf = np.ascontiguousarray(conf, np.float64)
+    eps = np.ascontiguousarray(np.broadcast_to(eps, conf.shape), np.float64)
+    g = np.zeros_like(conf)
+    lib().orc_grad_fd(C.byref(ph), C.byref(p.c), None, C.byref(L.c), _dp(conf), flags, _dp(eps),
+                      _dp(g))
+    return g
+
+
+def grad_analytic(prot, lig, conf, flags=F_INTER | F_INTRA, ph=REF, want_xyz=False):
+    p, L = OMol.of(prot), OLigand(lig)
+    conf = np.ascontiguousarray(conf, np.float64)
+    g = np.zeros_like(conf)
+    gx = np.zeros(3 * lig.n)
+    st = C.c_int()
+    e = lib().orc_grad_analytic(C.byref(ph), C.byref(p.c), C.byref(L.c), _dp(conf), flags,
+                                _dp(g), _dp(gx), C.byref(st))
+    if want_xyz:
+        return e, g, gx.reshape(-1, 3), st.value
+    return e, g, st.value
+
+
+def score_batch(prot, lig, dofs, flags=F_INTER | F_INTRA, mode=0, eps=None, use_cells=False,
+                nthreads=1, ph=REF):
+    """mode 0: energy; 1: + analytic gradient; 2: + central differences."""
+    p, L = OMol.of(prot), OLigand(lig)
+    dofs = np.ascontiguousarray(dofs, np.float32)
+    B, nd = dofs.shape
+    E = np.zeros(B)
+    G = np.zeros((B, nd)) if mode else None
+    st = np.zeros(B, np.int32)
+    eps_a = np.ascontiguousarray(np.broadcast_to(eps if eps is not None else 1e-4, (nd,)),
+                                 np.float64)
+    lib().orc_score_batch(C.byref(ph), C.byref(p.c), C.byref(L.c), B,
+                          dofs.ctypes.data_as(C.POINTER(C.c_float)), flags, mode, _dp(eps_a),
+                          int(use_cells), nthreads, _dp(E), _dp(G) if G is not None else None,
+                          _ip(st))
+    return E, G, st

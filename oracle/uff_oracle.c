@@ -1,0 +1,685 @@
+/*
+ * uff_oracle.c -- FP64 CPU oracle for the MMO UFF scoring hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path and the CPU baseline
+ * timed by bench.py.  The shipped library never links or calls this file.
+ * Each function cites the reference OCaml it restates (paths inside
+ * UnixJunkie/MMO).  Parity against the reference itself is unpinned (no golden
+ * energies ship with it); see uff_oracle.h for what pins this oracle.
+ */
+#include "uff_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* const.ml:12-18 and UFF.ml:25 */
+static const double CUTOFF = 12.0;
+static const double EPS_PROT = 4.0;
+double orc_elec_weight(void) { return 332.0637 / EPS_PROT; }
+
+/* UFF.ml:10-22: (anum, x_i, D_i); anum 0 is a virtual element with no vdW */
+static const struct { int anum; double xi, di; } UFF_TABLE[] = {
+    {0, 0.0, 0.0},     {1, 2.886, 0.044},  {6, 3.851, 0.105},  {7, 3.660, 0.069},
+    {8, 3.500, 0.060}, {9, 3.364, 0.050},  {12, 3.021, 0.111}, {15, 4.147, 0.305},
+    {16, 4.035, 0.274}, {17, 3.947, 0.227}, {35, 4.189, 0.251}, {53, 4.500, 0.339}};
+
+int orc_uff_params(int anum, double *xi, double *di) {
+  for (unsigned k = 0; k < sizeof(UFF_TABLE) / sizeof(UFF_TABLE[0]); ++k)
+    if (UFF_TABLE[k].anum == anum) {
+      *xi = UFF_TABLE[k].xi;
+      *di = UFF_TABLE[k].di;
+      return 1;
+    }
+  return 0;
+}
+
+/* UFF.ml:43-51 (FF.geo_mean for both); the table holds NaN for unsupported
+ * elements (UFF.ml:37), which the NaN returned here reproduces. */
+void orc_pair_params(const orc_physics *ph, int a1, int a2, double *x_ij, double *d_ij) {
+  double x1, d1, x2, d2;
+  if (!orc_uff_params(a1, &x1, &d1) || !orc_uff_params(a2, &x2, &d2)) {
+    *x_ij = NAN;
+    *d_ij = NAN;
+    return;
+  }
+  *x_ij = ph->mixing == 1 ? 0.5 * (x1 + x2) : sqrt(x1 * x2);
+  *d_ij = sqrt(d1 * d2);
+}
+
+/* FF.ml:17-20 */
+double orc_shift_12A(double d) {
+  if (d < 12.0) {
+    double s = 1.0 - (d / 12.0) * (d / 12.0);
+    return s * s;
+  }
+  return 0.0;
+}
+
+/* math.ml:58-62 */
+double orc_non_zero_dist(double d) { return d < 0.01 ? 0.01 : d; }
+
+/* FF.ml:5-12: pow6 x = pow3 (x * x) */
+static double pow6(double x) {
+  double x2 = x * x;
+  return x2 * x2 * x2;
+}
+
+static void cross(const double a[3], const double b[3], double c[3]) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+static double dot(const double a[3], const double b[3]) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+/* math.ml:48-56: atan2((u1 |u2|) . (u2 x u3), (u1 x u2) . (u2 x u3)) */
+double orc_dihedral(const double i[3], const double j[3], const double k[3], const double l[3]) {
+  double u1[3], u2[3], u3[3], u2u3[3], u1u2[3], u1m[3];
+  for (int d = 0; d < 3; ++d) {
+    u1[d] = j[d] - i[d];
+    u2[d] = k[d] - j[d];
+    u3[d] = l[d] - k[d];
+  }
+  cross(u2, u3, u2u3);
+  double m2 = sqrt(dot(u2, u2));
+  for (int d = 0; d < 3; ++d) u1m[d] = u1[d] * m2;
+  cross(u1, u2, u1u2);
+  return atan2(dot(u1m, u2u3), dot(u1u2, u2u3));
+}
+
+/* rot.ml:52-66: R = Rz(g) Ry(b) Rx(a), row-major a..i */
+void orc_rot_xyz(double al, double be, double ga, double R[9]) {
+  double ca = cos(al), sa = sin(al), cb = cos(be), sb = sin(be), cg = cos(ga), sg = sin(ga);
+  R[0] = cb * cg;
+  R[1] = cg * sa * sb - ca * sg;
+  R[2] = sa * sg + ca * cg * sb;
+  R[3] = cb * sg;
+  R[4] = ca * cg + sa * sb * sg;
+  R[5] = ca * sb * sg - cg * sa;
+  R[6] = -sb;
+  R[7] = cb * sa;
+  R[8] = ca * cb;
+}
+
+/* d R / d(a, b, g), entry by entry from the closed form above */
+static void rot_xyz_derivs(double al, double be, double ga, double dA[9], double dB[9],
+                           double dG[9]) {
+  double ca = cos(al), sa = sin(al), cb = cos(be), sb = sin(be), cg = cos(ga), sg = sin(ga);
+  dA[0] = 0.0;
+  dA[1] = cg * ca * sb + sa * sg;
+  dA[2] = ca * sg - sa * cg * sb;
+  dA[3] = 0.0;
+  dA[4] = -sa * cg + ca * sb * sg;
+  dA[5] = -sa * sb * sg - cg * ca;
+  dA[6] = 0.0;
+  dA[7] = cb * ca;
+  dA[8] = -sa * cb;
+
+  dB[0] = -sb * cg;
+  dB[1] = cg * sa * cb;
+  dB[2] = ca * cg * cb;
+  dB[3] = -sb * sg;
+  dB[4] = sa * cb * sg;
+  dB[5] = ca * cb * sg;
+  dB[6] = -cb;
+  dB[7] = -sb * sa;
+  dB[8] = -ca * sb;
+
+  dG[0] = -cb * sg;
+  dG[1] = -sg * sa * sb - ca * cg;
+  dG[2] = sa * cg - ca * sg * sb;
+  dG[3] = cb * cg;
+  dG[4] = -ca * sg + sa * sb * cg;
+  dG[5] = ca * sb * cg + sg * sa;
+  dG[6] = 0.0;
+  dG[7] = 0.0;
+  dG[8] = 0.0;
+}
+
+/* rot.ml:136-146 */
+void orc_rot_axis_angle(const double u[3], double theta, double R[9]) {
+  double c = cos(theta), s = sin(theta), o = 1.0 - c;
+  double x = u[0], y = u[1], z = u[2];
+  R[0] = c + x * x * o;
+  R[1] = x * y * o - z * s;
+  R[2] = x * z * o + y * s;
+  R[3] = x * y * o + z * s;
+  R[4] = c + y * y * o;
+  R[5] = y * z * o - x * s;
+  R[6] = x * z * o - y * s;
+  R[7] = y * z * o + x * s;
+  R[8] = c + z * z * o;
+}
+
+static void matvec(const double R[9], const double v[3], double o[3]) {
+  o[0] = R[0] * v[0] + R[1] * v[1] + R[2] * v[2];
+  o[1] = R[3] * v[0] + R[4] * v[1] + R[5] * v[2];
+  o[2] = R[6] * v[0] + R[7] * v[1] + R[8] * v[2];
+}
+static void matTvec(const double R[9], const double v[3], double o[3]) {
+  o[0] = R[0] * v[0] + R[3] * v[1] + R[6] * v[2];
+  o[1] = R[1] * v[0] + R[4] * v[1] + R[7] * v[2];
+  o[2] = R[2] * v[0] + R[5] * v[1] + R[8] * v[2];
+}
+
+/* bond axis of mol.ml:615-619: normalize (p_right - p_left) */
+static void bond_axis(const double *x, const double *y, const double *z, int left, int right,
+                      double c[3], double a[3], double u[3], double *alen) {
+  c[0] = x[right];
+  c[1] = y[right];
+  c[2] = z[right];
+  a[0] = c[0] - x[left];
+  a[1] = c[1] - y[left];
+  a[2] = c[2] - z[left];
+  *alen = sqrt(dot(a, a));
+  u[0] = a[0] / *alen;
+  u[1] = a[1] / *alen;
+  u[2] = a[2] / *alen;
+}
+
+/* mol.ml:610-631 */
+void orc_rotate_bond(int n, double *x, double *y, double *z, int left, int right,
+                     const int *grp, int ng, double alpha) {
+  (void)n;
+  double c[3], a[3], u[3], alen, R[9];
+  bond_axis(x, y, z, left, right, c, a, u, &alen);
+  orc_rot_axis_angle(u, alpha, R);
+  for (int k = 0; k < ng; ++k) {
+    int i = grp[k];
+    double v[3] = {x[i] - c[0], y[i] - c[1], z[i] - c[2]}, w[3];
+    matvec(R, v, w);
+    x[i] = w[0] + c[0];
+    y[i] = w[1] + c[1];
+    z[i] = w[2] + c[2];
+  }
+}
+
+static void centroid(int n, const double *x, const double *y, const double *z, double c[3]) {
+  double sx = 0, sy = 0, sz = 0;
+  for (int i = 0; i < n; ++i) {
+    sx += x[i];
+    sy += y[i];
+    sz += z[i];
+  }
+  c[0] = sx / n;
+  c[1] = sy / n;
+  c[2] = sz / n;
+}
+
+/* mol.ml:576-591: radius = max_i (0.01 + |center - x_i|); Too_long above 12 A */
+static int too_long(int n, const double *x, const double *y, const double *z) {
+  if (n == 0) return 0;
+  double c[3], r = 0.0;
+  centroid(n, x, y, z, c);
+  for (int i = 0; i < n; ++i) {
+    double dx = c[0] - x[i], dy = c[1] - y[i], dz = c[2] - z[i];
+    double d = 0.01 + sqrt(dx * dx + dy * dy + dz * dz);
+    if (d > r) r = d;
+  }
+  return r > CUTOFF;
+}
+
+/* torsions of optim.ml:68-71 applied in bond order; returns Too_long status */
+static int apply_torsions(const orc_ligand *lig, const double *tau, double *x, double *y,
+                          double *z) {
+  int n = lig->m.n;
+  memcpy(x, lig->m.x, sizeof(double) * n);
+  memcpy(y, lig->m.y, sizeof(double) * n);
+  memcpy(z, lig->m.z, sizeof(double) * n);
+  for (int t = 0; t < lig->nrb; ++t)
+    orc_rotate_bond(n, x, y, z, lig->bond_lr[2 * t], lig->bond_lr[2 * t + 1],
+                    lig->grp_atoms + lig->grp_off[t], lig->grp_off[t + 1] - lig->grp_off[t],
+                    tau[t]);
+  return too_long(n, x, y, z) ? ORC_S_TOO_LONG : 0;
+}
+
+/* optim.ml:64-80 (flags without RECENTER) or mol.ml:705-710 (RECENTER) */
+int orc_apply_config(const orc_ligand *lig, const double *conf, int flags, double *x,
+                     double *y, double *z) {
+  int n = lig->m.n;
+  int st = apply_torsions(lig, conf + 6, x, y, z);
+  double R[9], c[3] = {0, 0, 0};
+  orc_rot_xyz(conf[3], conf[4], conf[5], R);
+  if (flags & ORC_F_RECENTER) centroid(n, x, y, z, c);
+  for (int i = 0; i < n; ++i) {
+    double v[3] = {x[i] - c[0], y[i] - c[1], z[i] - c[2]}, w[3];
+    matvec(R, v, w);
+    x[i] = w[0] + conf[0];
+    y[i] = w[1] + conf[1];
+    z[i] = w[2] + conf[2];
+  }
+  return st;
+}
+
+/* one pair term before the elec weight: elec part and vdW part, FP64, in the
+ * operation order of mol.ml:840-845 */
+static inline void pair_terms(int dielectric, double r, double q_i, double q_j, double x_ij,
+                              double d_ij, double w, double *el, double *vdw) {
+  double p6 = pow6(x_ij / r);
+  double qq = q_i * q_j;
+  *el = w * (dielectric == 1 ? qq / (r * r) : qq / r);
+  *vdw = w * (d_ij * ((-2.0 * p6) + (p6 * p6)));
+}
+
+/* mol.ml:796-818 (global) and mol.ml:822-849 (shifted); protein-major order */
+void orc_ene_inter_parts(const orc_physics *ph, const orc_mol *prot, const orc_mol *lig,
+                         double parts[2]) {
+  double se = 0.0, sv = 0.0;
+  for (int i = 0; i < prot->n; ++i) {
+    for (int j = 0; j < lig->n; ++j) {
+      double dx = prot->x[i] - lig->x[j], dy = prot->y[i] - lig->y[j],
+             dz = prot->z[i] - lig->z[j];
+      double r2 = dx * dx + dy * dy + dz * dz;
+      double w = 1.0, r;
+      if (ph->inter_form == 0) {
+        if (!(r2 < 144.0)) continue;
+        r = orc_non_zero_dist(sqrt(r2));
+        w = orc_shift_12A(r);
+      } else {
+        r = orc_non_zero_dist(sqrt(r2));
+      }
+      double x_ij, d_ij, el, vdw;
+      orc_pair_params(ph, prot->anum[i], lig->anum[j], &x_ij, &d_ij);
+      pair_terms(ph->dielectric, r, prot->q[i], lig->q[j], x_ij, d_ij, w, &el, &vdw);
+      se += el;
+      sv += vdw;
+    }
+  }
+  parts[0] = orc_elec_weight() * se;
+  parts[1] = sv;
+}
+
+double orc_ene_inter(const orc_physics *ph, const orc_mol *prot, const orc_mol *lig) {
+  double p[2];
+  orc_ene_inter_parts(ph, prot, lig, p);
+  return p[0] + p[1];
+}
+
+/* mol.ml:881-903 (plain) and mol.ml:853-877 (shifted, 12 A) */
+double orc_ene_intra(const orc_physics *ph, const orc_mol *lig, const uint8_t *interacting) {
+  int n = lig->n;
+  double se = 0.0, sv = 0.0;
+  for (int i = 0; i < n - 1; ++i) {
+    for (int j = i + 1; j < n; ++j) {
+      if (!interacting[i * n + j]) continue;
+      double dx = lig->x[i] - lig->x[j], dy = lig->y[i] - lig->y[j], dz = lig->z[i] - lig->z[j];
+      double r = orc_non_zero_dist(sqrt(dx * dx + dy * dy + dz * dz));
+      double w = 1.0;
+      if (ph->intra_form == 1) {
+        if (!(r < 12.0)) continue;
+        w = orc_shift_12A(r);
+      }
+      double x_ij, d_ij, el, vdw;
+      orc_pair_params(ph, lig->anum[i], lig->anum[j], &x_ij, &d_ij);
+      pair_terms(ph->dielectric, r, lig->q[i], lig->q[j], x_ij, d_ij, w, &el, &vdw);
+      se += el;
+      sv += vdw;
+    }
+  }
+  return orc_elec_weight() * se + sv;
+}
+
+/* ---- cell grid: the 12 A neighbour query of mol.ml:939 -------------------- */
+struct orc_cells {
+  orc_mol prot;
+  double lo[3];
+  int dim[3];
+  int *start; /* dim0*dim1*dim2 + 1 */
+  int *idx;   /* protein atoms sorted by cell */
+};
+
+static int cell_coord(double v, double lo, int dim) {
+  int c = (int)floor((v - lo) / CUTOFF);
+  if (c < 0) c = 0;
+  if (c >= dim) c = dim - 1;
+  return c;
+}
+
+orc_cells *orc_cells_build(const orc_mol *prot) {
+  orc_cells *c = (orc_cells *)calloc(1, sizeof(orc_cells));
+  c->prot = *prot;
+  double hi[3] = {-1e300, -1e300, -1e300};
+  c->lo[0] = c->lo[1] = c->lo[2] = 1e300;
+  const double *xyz[3] = {prot->x, prot->y, prot->z};
+  for (int i = 0; i < prot->n; ++i)
+    for (int d = 0; d < 3; ++d) {
+      if (xyz[d][i] < c->lo[d]) c->lo[d] = xyz[d][i];
+      if (xyz[d][i] > hi[d]) hi[d] = xyz[d][i];
+    }
+  if (prot->n == 0) c->lo[0] = c->lo[1] = c->lo[2] = hi[0] = hi[1] = hi[2] = 0.0;
+  for (int d = 0; d < 3; ++d) c->dim[d] = (int)floor((hi[d] - c->lo[d]) / CUTOFF) + 1;
+  int ncell = c->dim[0] * c->dim[1] * c->dim[2];
+  c->start = (int *)calloc((size_t)(ncell > 0 ? ncell : 1) + 1, sizeof(int));
+  c->idx = (int *)malloc(sizeof(int) * (prot->n > 0 ? prot->n : 1));
+  int *cid = (int *)malloc(sizeof(int) * (prot->n > 0 ? prot->n : 1));
+  for (int i = 0; i < prot->n; ++i) {
+    int cx = cell_coord(prot->x[i], c->lo[0], c->dim[0]);
+    int cy = cell_coord(prot->y[i], c->lo[1], c->dim[1]);
+    int cz = cell_coord(prot->z[i], c->lo[2], c->dim[2]);
+    cid[i] = (cz * c->dim[1] + cy) * c->dim[0] + cx;
+    c->start[cid[i] + 1]++;
+  }
+  for (int k = 0; k < ncell; ++k) c->start[k + 1] += c->start[k];
+  int *fill = (int *)calloc((size_t)(ncell > 0 ? ncell : 1), sizeof(int));
+  for (int i = 0; i < prot->n; ++i) c->idx[c->start[cid[i]] + fill[cid[i]]++] = i;
+  free(fill);
+  free(cid);
+  return c;
+}
+
+void orc_cells_free(orc_cells *c) {
+  if (!c) return;
+  free(c->start);
+  free(c->idx);
+  free(c);
+}
+
+/* mol.ml:928-960: ligand-major; protein atoms within 12 A of each ligand atom.
+ * The shifted weight is 0 at 12 A, so this equals the brute shifted sum up to
+ * summation order. */
+double orc_ene_inter_cells(const orc_physics *ph, const orc_cells *c, const orc_mol *lig) {
+  const orc_mol *prot = &c->prot;
+  double se = 0.0, sv = 0.0;
+  for (int j = 0; j < lig->n; ++j) {
+    int cx = (int)floor((lig->x[j] - c->lo[0]) / CUTOFF);
+    int cy = (int)floor((lig->y[j] - c->lo[1]) / CUTOFF);
+    int cz = (int)floor((lig->z[j] - c->lo[2]) / CUTOFF);
+    for (int gz = cz - 1; gz <= cz + 1; ++gz) {
+      if (gz < 0 || gz >= c->dim[2]) continue;
+      for (int gy = cy - 1; gy <= cy + 1; ++gy) {
+        if (gy < 0 || gy >= c->dim[1]) continue;
+        for (int gx = cx - 1; gx <= cx + 1; ++gx) {
+          if (gx < 0 || gx >= c->dim[0]) continue;
+          int cell = (gz * c->dim[1] + gy) * c->dim[0] + gx;
+          for (int k = c->start[cell]; k < c->start[cell + 1]; ++k) {
+            int i = c->idx[k];
+            double dx = prot->x[i] - lig->x[j], dy = prot->y[i] - lig->y[j],
+                   dz = prot->z[i] - lig->z[j];
+            double r2 = dx * dx + dy * dy + dz * dz;
+            if (!(r2 < 144.0)) continue;
+            double r = orc_non_zero_dist(sqrt(r2));
+            double w = orc_shift_12A(r);
+            double x_ij, d_ij, el, vdw;
+            orc_pair_params(ph, lig->anum[j], prot->anum[i], &x_ij, &d_ij);
+            pair_terms(ph->dielectric, r, prot->q[i], lig->q[j], x_ij, d_ij, w, &el, &vdw);
+            se += el;
+            sv += vdw;
+          }
+        }
+      }
+    }
+  }
+  return orc_elec_weight() * se + sv;
+}
+
+double orc_score_conf(const orc_physics *ph, const orc_mol *prot, const orc_cells *cells,
+                      const orc_ligand *lig, const double *conf, int flags, int *status) {
+  int n = lig->m.n;
+  double *buf = (double *)malloc(sizeof(double) * 3 * (n > 0 ? n : 1));
+  double *x = buf, *y = buf + n, *z = buf + 2 * n;
+  int st = orc_apply_config(lig, conf, flags, x, y, z);
+  orc_mol m = lig->m;
+  m.x = x;
+  m.y = y;
+  m.z = z;
+  double E = 0.0;
+  if (flags & ORC_F_INTER)
+    E += (cells && ph->inter_form == 0) ? orc_ene_inter_cells(ph, cells, &m)
+                                        : orc_ene_inter(ph, prot, &m);
+  if (flags & ORC_F_INTRA) E += orc_ene_intra(ph, &m, lig->interacting);
+  if (!isfinite(E)) st |= ORC_S_NONFINITE;
+  if (status) *status = st;
+  free(buf);
+  return E;
+}
+
+/* lds.ml:1118-1136 */
+void orc_grad_fd(const orc_physics *ph, const orc_mol *prot, const orc_cells *cells,
+                 const orc_ligand *lig, const double *conf, int flags, const double *eps,
+                 double *grad) {
+  int nd = 6 + lig->nrb;
+  double *c = (double *)malloc(sizeof(double) * nd);
+  memcpy(c, conf, sizeof(double) * nd);
+  for (int k = 0; k < nd; ++k) {
+    c[k] = conf[k] - eps[k];
+    double before = orc_score_conf(ph, prot, cells, lig, c, flags, NULL);
+    c[k] = conf[k] + eps[k];
+    double after = orc_score_conf(ph, prot, cells, lig, c, flags, NULL);
+    c[k] = conf[k];
+    grad[k] = (after - before) / (2.0 * eps[k]);
+  }
+  free(c);
+}
+
+/* d(pair energy)/d(r2) * 2 for one pair with the switch weight; the pair
+ * energy is w(r) * (D p6 (p6 - 2) + K qq / r^m), r = max(|d|, 0.01).  Below
+ * 0.01 A the distance is clamped, so the derivative there is zero. */
+static double pair_energy_grad(int dielectric, int shifted, double r2, double qqK, double x_ij,
+                               double d_ij, double *e_out) {
+  double r = sqrt(r2);
+  int clamped = r < 0.01;
+  if (clamped) r = 0.01;
+  double s = 1.0, w = 1.0, dw = 0.0; /* dw = dw/dr */
+  if (shifted) {
+    double t = r / 12.0;
+    s = 1.0 - t * t;
+    w = s * s;
+    dw = 2.0 * s * (-2.0 * r / 144.0);
+  }
+  double p6 = pow6(x_ij / r);
+  double lj = d_ij * (p6 * p6 - 2.0 * p6);
+  double dlj = d_ij * (2.0 * p6 * (-6.0 * p6 / r) - 2.0 * (-6.0 * p6 / r)); /* d/dr */
+  double el, del;
+  if (dielectric == 1) {
+    el = qqK / (r * r);
+    del = -2.0 * qqK / (r * r * r);
+  } else {
+    el = qqK / r;
+    del = -qqK / (r * r);
+  }
+  double e = lj + el;
+  *e_out = w * e;
+  if (clamped) return 0.0;
+  double dEdr = dw * e + w * (dlj + del);
+  return dEdr / r; /* dE/dd = (dE/dr) d / r */
+}
+
+/* analytic reverse-mode gradient; see uff_oracle.h */
+double orc_grad_analytic(const orc_physics *ph, const orc_mol *prot, const orc_ligand *lig,
+                         const double *conf, int flags, double *grad, double *gxyz,
+                         int *status) {
+  int n = lig->m.n, nrb = lig->nrb;
+  double K = orc_elec_weight();
+  /* forward with snapshots of every stage of the torsion chain */
+  double *snap = (double *)malloc(sizeof(double) * 3 * n * (nrb + 1) + 1);
+  double *Zx = snap, *Zy = snap + n, *Zz = snap + 2 * n;
+  memcpy(Zx, lig->m.x, sizeof(double) * n);
+  memcpy(Zy, lig->m.y, sizeof(double) * n);
+  memcpy(Zz, lig->m.z, sizeof(double) * n);
+  for (int t = 0; t < nrb; ++t) {
+    double *px = snap + 3 * n * t, *nx = snap + 3 * n * (t + 1);
+    memcpy(nx, px, sizeof(double) * 3 * n);
+    orc_rotate_bond(n, nx, nx + n, nx + 2 * n, lig->bond_lr[2 * t], lig->bond_lr[2 * t + 1],
+                    lig->grp_atoms + lig->grp_off[t], lig->grp_off[t + 1] - lig->grp_off[t],
+                    conf[6 + t]);
+  }
+  double *Y = snap + 3 * n * nrb;
+  int st = too_long(n, Y, Y + n, Y + 2 * n) ? ORC_S_TOO_LONG : 0;
+  double R[9], ctr[3] = {0, 0, 0};
+  orc_rot_xyz(conf[3], conf[4], conf[5], R);
+  if (flags & ORC_F_RECENTER) centroid(n, Y, Y + n, Y + 2 * n, ctr);
+  double *X = (double *)malloc(sizeof(double) * 3 * n + 1);
+  double *Yc = (double *)malloc(sizeof(double) * 3 * n + 1);
+  double *G = (double *)calloc(3 * n + 1, sizeof(double));
+  for (int i = 0; i < n; ++i) {
+    double v[3] = {Y[i] - ctr[0], Y[n + i] - ctr[1], Y[2 * n + i] - ctr[2]}, w[3];
+    Yc[3 * i] = v[0];
+    Yc[3 * i + 1] = v[1];
+    Yc[3 * i + 2] = v[2];
+    matvec(R, v, w);
+    for (int d = 0; d < 3; ++d) X[3 * i + d] = w[d] + conf[d];
+  }
+  /* energy and dE/dX */
+  double E = 0.0;
+  if (flags & ORC_F_INTER) {
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < prot->n; ++i) {
+        double d[3] = {X[3 * j] - prot->x[i], X[3 * j + 1] - prot->y[i],
+                       X[3 * j + 2] - prot->z[i]};
+        double r2 = dot(d, d);
+        if (ph->inter_form == 0 && !(r2 < 144.0)) continue;
+        double x_ij, d_ij, e;
+        orc_pair_params(ph, prot->anum[i], lig->m.anum[j], &x_ij, &d_ij);
+        double g = pair_energy_grad(ph->dielectric, ph->inter_form == 0, r2,
+                                    K * prot->q[i] * lig->m.q[j], x_ij, d_ij, &e);
+        E += e;
+        for (int k = 0; k < 3; ++k) G[3 * j + k] += g * d[k];
+      }
+  }
+  if (flags & ORC_F_INTRA) {
+    for (int i = 0; i < n - 1; ++i)
+      for (int j = i + 1; j < n; ++j) {
+        if (!lig->interacting[i * n + j]) continue;
+        double d[3] = {X[3 * i] - X[3 * j], X[3 * i + 1] - X[3 * j + 1],
+                       X[3 * i + 2] - X[3 * j + 2]};
+        double r2 = dot(d, d);
+        int shifted = ph->intra_form == 1;
+        if (shifted && !(orc_non_zero_dist(sqrt(r2)) < 12.0)) continue;
+        double x_ij, d_ij, e;
+        orc_pair_params(ph, lig->m.anum[i], lig->m.anum[j], &x_ij, &d_ij);
+        double g = pair_energy_grad(ph->dielectric, shifted, r2, K * lig->m.q[i] * lig->m.q[j],
+                                    x_ij, d_ij, &e);
+        E += e;
+        for (int k = 0; k < 3; ++k) {
+          G[3 * i + k] += g * d[k];
+          G[3 * j + k] -= g * d[k];
+        }
+      }
+  }
+  if (gxyz) memcpy(gxyz, G, sizeof(double) * 3 * n);
+  /* rigid part */
+  double dA[9], dB[9], dG[9], M[9] = {0};
+  rot_xyz_derivs(conf[3], conf[4], conf[5], dA, dB, dG);
+  grad[0] = grad[1] = grad[2] = 0.0;
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) {
+      grad[k] += G[3 * i + k];
+      for (int l = 0; l < 3; ++l) M[3 * k + l] += G[3 * i + k] * Yc[3 * i + l];
+    }
+  grad[3] = grad[4] = grad[5] = 0.0;
+  for (int e = 0; e < 9; ++e) {
+    grad[3] += M[e] * dA[e];
+    grad[4] += M[e] * dB[e];
+    grad[5] += M[e] * dG[e];
+  }
+  /* adjoint of Y */
+  double *A = (double *)malloc(sizeof(double) * 3 * n + 1);
+  double mean[3] = {0, 0, 0};
+  for (int i = 0; i < n; ++i) {
+    matTvec(R, G + 3 * i, A + 3 * i);
+    for (int k = 0; k < 3; ++k) mean[k] += A[3 * i + k];
+  }
+  if (flags & ORC_F_RECENTER)
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < 3; ++k) A[3 * i + k] -= mean[k] / n;
+  /* reverse through the torsions */
+  for (int t = nrb - 1; t >= 0; --t) {
+    const double *pre = snap + 3 * n * t, *post = snap + 3 * n * (t + 1);
+    int left = lig->bond_lr[2 * t], right = lig->bond_lr[2 * t + 1];
+    double c[3], a[3], u[3], alen, Rt[9];
+    bond_axis(pre, pre + n, pre + 2 * n, left, right, c, a, u, &alen);
+    double th = conf[6 + t], ct = cos(th), stt = sin(th);
+    orc_rot_axis_angle(u, th, Rt);
+    double dth = 0.0, dU[3] = {0, 0, 0}, dC[3] = {0, 0, 0};
+    for (int k = lig->grp_off[t]; k < lig->grp_off[t + 1]; ++k) {
+      int i = lig->grp_atoms[k];
+      double vp[3] = {post[i] - c[0], post[n + i] - c[1], post[2 * n + i] - c[2]};
+      double v[3] = {pre[i] - c[0], pre[n + i] - c[1], pre[2 * n + i] - c[2]};
+      double *Ai = A + 3 * i, uxv[3], vxA[3], RtA[3];
+      cross(u, vp, uxv);
+      dth += dot(Ai, uxv);
+      cross(v, Ai, vxA);
+      double uv = dot(u, v), Au = dot(Ai, u);
+      for (int d = 0; d < 3; ++d) dU[d] += stt * vxA[d] + (1.0 - ct) * (uv * Ai[d] + Au * v[d]);
+      matTvec(Rt, Ai, RtA);
+      for (int d = 0; d < 3; ++d) {
+        dC[d] += Ai[d] - RtA[d];
+        Ai[d] = RtA[d];
+      }
+    }
+    grad[6 + t] = dth;
+    double uu = dot(u, dU), da[3];
+    for (int d = 0; d < 3; ++d) da[d] = (dU[d] - u[d] * uu) / alen;
+    for (int d = 0; d < 3; ++d) {
+      A[3 * right + d] += da[d] + dC[d];
+      A[3 * left + d] -= da[d];
+    }
+  }
+  if (!isfinite(E)) st |= ORC_S_NONFINITE;
+  if (status) *status = st;
+  free(A);
+  free(G);
+  free(Yc);
+  free(X);
+  free(snap);
+  return E;
+}
+
+/* ---- batch over poses on host threads ------------------------------------ */
+typedef struct {
+  const orc_physics *ph;
+  const orc_mol *prot;
+  const orc_cells *cells;
+  const orc_ligand *lig;
+  const float *dofs;
+  int flags, mode, b0, b1, nd;
+  const double *eps;
+  double *E, *grad;
+  int *status;
+} batch_job;
+
+static void *batch_worker(void *arg) {
+  batch_job *j = (batch_job *)arg;
+  double conf[64 + 6];
+  for (int b = j->b0; b < j->b1; ++b) {
+    for (int k = 0; k < j->nd; ++k) conf[k] = (double)j->dofs[(size_t)b * j->nd + k];
+    int st = 0;
+    double *g = j->grad ? j->grad + (size_t)b * j->nd : NULL;
+    if (j->mode == 1 && g) {
+      j->E[b] = orc_grad_analytic(j->ph, j->prot, j->lig, conf, j->flags, g, NULL, &st);
+    } else {
+      j->E[b] = orc_score_conf(j->ph, j->prot, j->cells, j->lig, conf, j->flags, &st);
+      if (j->mode == 2 && g) orc_grad_fd(j->ph, j->prot, j->cells, j->lig, conf, j->flags, j->eps, g);
+    }
+    if (j->status) j->status[b] = st;
+  }
+  return NULL;
+}
+
+void orc_score_batch(const orc_physics *ph, const orc_mol *prot, const orc_ligand *lig, int B,
+                     const float *dofs, int flags, int mode, const double *eps, int use_cells,
+                     int nthreads, double *E, double *grad, int *status) {
+  orc_cells *cells = (use_cells && ph->inter_form == 0) ? orc_cells_build(prot) : NULL;
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > B) nthreads = B > 0 ? B : 1;
+  pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+  batch_job *jobs = (batch_job *)malloc(sizeof(batch_job) * nthreads);
+  for (int t = 0; t < nthreads; ++t) {
+    batch_job j = {ph, prot, cells, lig, dofs, flags, mode,
+                   (int)((long)B * t / nthreads), (int)((long)B * (t + 1) / nthreads),
+                   6 + lig->nrb, eps, E, grad, status};
+    jobs[t] = j;
+    if (nthreads == 1)
+      batch_worker(&jobs[t]);
+    else
+      pthread_create(&th[t], NULL, batch_worker, &jobs[t]);
+  }
+  if (nthreads > 1)
+    for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+  free(jobs);
+  free(th);
+  orc_cells_free(cells);
+}

@@ -1,0 +1,301 @@
+"""Parity of the CUDA path (through the C ABI) with the FP64 oracle.
+
+Tolerances (stated by the scoring contract): energies within 1e-5 of the FP64
+oracle, relative to max(|E64|, sum of |pair energies|); gradients within 1e-4
+of the FP64 analytic gradient, relative to its largest component."""
+import numpy as np
+import pytest
+
+from mmo_gb300 import synth
+from mmo_gb300.topology import Mol
+
+pytestmark = pytest.mark.gpu
+
+E_TOL = 1e-5
+G_TOL = 1e-4
+
+
+def _posed(oracle, lig, conf, recenter=False):
+    xyz, st = oracle.apply_config(lig, np.asarray(conf, np.float64),
+                                  oracle.F_RECENTER if recenter else 0)
+    return xyz, st
+
+
+def ref_batch(oracle, system, dofs, grad=False, recenter=False, inter=True, intra=True, ph=None):
+    """FP64 energies (and analytic gradients) plus the conditioning scale."""
+    from oracle import np_twin as T
+
+    flags = (oracle.F_INTER if inter else 0) | (oracle.F_INTRA if intra else 0)
+    flags |= oracle.F_RECENTER if recenter else 0
+    E, G, st = oracle.score_batch(system.pocket, system.ligand, dofs, flags=flags,
+                                  mode=1 if grad else 0, nthreads=16,
+                                  ph=ph if ph is not None else oracle.REF)
+    scale = np.zeros(len(dofs))
+    lig, p = system.ligand, system.pocket
+    shifted = ph is None or ph.inter_form == 0
+    diel = 0 if ph is None else ph.dielectric
+    for b, conf in enumerate(dofs):
+        xyz, _ = _posed(oracle, lig, conf, recenter)
+        if inter and p.n:
+            scale[b] += T.ene_inter(p.xyz(), p.q, p.anum, xyz, lig.q, lig.anum, shifted=shifted,
+                                    dielectric=diel, absolute=True)
+        if intra:
+            scale[b] += T.ene_intra(xyz, lig.q, lig.anum, lig.interacting, dielectric=diel,
+                                    absolute=True)
+    return E, G, st, scale
+
+
+def assert_energy(E, E64, scale, tol=E_TOL):
+    err = np.abs(E - E64) / np.maximum(np.maximum(np.abs(E64), scale), 1e-300)
+    assert err.max() <= tol, (err.max(), int(err.argmax()))
+
+
+def assert_grad(G, G64, tol=G_TOL):
+    for b in range(G64.shape[0]):
+        s = np.abs(G64[b]).max()
+        if s == 0:
+            assert np.abs(G[b]).max() == 0
+            continue
+        err = np.abs(G[b].astype(np.float64) - G64[b]).max() / s
+        assert err <= tol, (b, err)
+
+
+@pytest.fixture(scope="module")
+def small():
+    return synth.single_pose(seed=0)
+
+
+@pytest.fixture(scope="module")
+def batch():
+    return synth.pose_batch(n_poses=256, seed=1)
+
+
+# -- plain drop-ins (Mol.t -> float) ----------------------------------------------
+
+@pytest.mark.parametrize("phys", [(0, 0, 0, 0), (0, 0, 1, 0), (1, 0, 0, 0), (0, 1, 0, 1),
+                                  (1, 1, 1, 1)])
+def test_plain_ene_inter_and_intra(oracle, scorer_factory, small, phys):
+    from mmo_gb300.ff import Physics
+    from oracle import np_twin as T
+
+    ph = oracle.physics(*phys)
+    s = scorer_factory(small.pocket, small.ligand, Physics(*phys))
+    xyz, _ = _posed(oracle, small.ligand, small.poses[0])
+    lig = small.ligand.with_xyz(xyz)
+    e = s.ene_inter(lig)
+    e64 = oracle.ene_inter(small.pocket, small.ligand, xyz, ph=ph)
+    scale = T.ene_inter(small.pocket.xyz(), small.pocket.q, small.pocket.anum, xyz, lig.q,
+                        lig.anum, shifted=phys[2] == 0, dielectric=phys[0], absolute=True)
+    assert_energy(np.array([e]), np.array([e64]), np.array([scale]))
+    ei = s.ene_intra(lig)
+    ei64 = oracle.ene_intra(small.ligand, xyz, ph=ph)
+    si = T.ene_intra(xyz, lig.q, lig.anum, lig.interacting, dielectric=phys[0], absolute=True)
+    assert_energy(np.array([ei]), np.array([ei64]), np.array([si]))
+
+
+def test_plain_closures_match_reference_call_shape(oracle, gpu_lib, small):
+    from mmo_gb300.ff import ene_inter_builder, ene_intra_builder
+
+    xyz, _ = _posed(oracle, small.ligand, small.poses[0])
+    lig = small.ligand.with_xyz(xyz)
+    ene_inter = ene_inter_builder(small.pocket, "Bst")
+    ene_intra = ene_intra_builder(small.ligand)
+    e = ene_inter(lig) + ene_intra(lig)
+    e64 = oracle.ene_inter(small.pocket, small.ligand, xyz) + oracle.ene_intra(small.ligand, xyz)
+    assert abs(e - e64) <= E_TOL * abs(e64)
+    rigid = ene_intra_builder(small.ligand, tweak_rbonds=False)
+    assert rigid(lig) == pytest.approx(oracle.ene_intra(small.ligand), rel=1e-5)
+    ene_inter.scorer.close()
+    ene_intra.scorer.close()
+    rigid.scorer.close()
+
+
+# -- one pose per launch (plain path of mmo_score_poses) ---------------------------
+
+@pytest.mark.parametrize("recenter", [False, True])
+def test_single_pose_energy_gradient(oracle, scorer_factory, small, recenter):
+    s = scorer_factory(small.pocket, small.ligand)
+    E, G, st = s.score_poses(small.poses, grad=True, recenter=recenter)
+    E64, G64, st64, scale = ref_batch(oracle, small, small.poses, grad=True, recenter=recenter)
+    assert_energy(E, E64, scale)
+    assert_grad(G, G64)
+    assert np.array_equal(st, st64)
+
+
+# -- batched ------------------------------------------------------------------------
+
+def test_batched_energy(oracle, scorer_factory, batch):
+    s = scorer_factory(batch.pocket, batch.ligand)
+    E, _, st = s.score_poses(batch.poses)
+    E64, _, st64, scale = ref_batch(oracle, batch, batch.poses)
+    assert_energy(E, E64, scale)
+    assert np.array_equal(st, st64)
+
+
+@pytest.mark.parametrize("recenter", [False, True])
+def test_batched_energy_gradient(oracle, scorer_factory, batch, recenter):
+    s = scorer_factory(batch.pocket, batch.ligand)
+    d = batch.poses[:128]
+    E, G, st = s.score_poses(d, grad=True, recenter=recenter)
+    E64, G64, st64, scale = ref_batch(oracle, batch, d, grad=True, recenter=recenter)
+    assert_energy(E, E64, scale)
+    assert_grad(G, G64)
+
+
+@pytest.mark.parametrize("inter,intra", [(True, False), (False, True)])
+def test_batched_terms_separately(oracle, scorer_factory, batch, inter, intra):
+    s = scorer_factory(batch.pocket, batch.ligand)
+    d = batch.poses[:64]
+    E, G, _ = s.score_poses(d, inter=inter, intra=intra, grad=True)
+    E64, G64, _, scale = ref_batch(oracle, batch, d, grad=True, inter=inter, intra=intra)
+    assert_energy(E, E64, scale)
+    assert_grad(G, G64)
+
+
+@pytest.mark.parametrize("phys", [(1, 0, 0, 0), (0, 1, 1, 1), (1, 1, 1, 0)])
+def test_batched_physics_variants(oracle, scorer_factory, batch, phys):
+    from mmo_gb300.ff import Physics
+
+    s = scorer_factory(batch.pocket, batch.ligand, Physics(*phys))
+    d = batch.poses[:64]
+    E, G, _ = s.score_poses(d, grad=True)
+    E64, G64, _, scale = ref_batch(oracle, batch, d, grad=True, ph=oracle.physics(*phys))
+    assert_energy(E, E64, scale)
+    assert_grad(G, G64)
+
+
+@pytest.mark.parametrize("kp,threads,chunks", [(1, 256, 0), (2, 512, 3), (4, 512, 1),
+                                               (4, 256, 17), (2, 256, 64)])
+def test_tile_shapes_agree(scorer_factory, batch, kp, threads, chunks):
+    s = scorer_factory(batch.pocket, batch.ligand)
+    d = batch.poses[:200]
+    E0, G0, _ = s.score_poses(d, grad=True)
+    s.set_tiles(kp, threads, chunks)
+    E1, G1, _ = s.score_poses(d, grad=True)
+    assert np.abs(E1 - E0).max() <= 1e-6 * np.abs(E0).max()
+    assert np.abs(G1 - G0).max() <= 1e-5 * np.abs(G0).max()
+
+
+def test_deterministic(scorer_factory, batch):
+    s = scorer_factory(batch.pocket, batch.ligand)
+    a = s.score_poses(batch.poses, grad=True)
+    b = s.score_poses(batch.poses, grad=True)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_plain_and_batched_agree(scorer_factory, batch):
+    s = scorer_factory(batch.pocket, batch.ligand)
+    d = batch.poses[:40]
+    Eb, Gb, _ = s.score_poses(d, grad=True)
+    for b in range(0, 40, 7):
+        E1, G1, _ = s.score_poses(d[b:b + 1], grad=True)
+        assert abs(E1[0] - Eb[b]) <= 1e-6 * abs(Eb[b])
+        assert np.abs(G1[0] - Gb[b]).max() <= 1e-5 * np.abs(Gb[b]).max()
+
+
+# -- edge cases ---------------------------------------------------------------------
+
+def test_edge_single_atom_ligand(oracle, scorer_factory, small):
+    lig = Mol("one", np.zeros(1), np.zeros(1), np.zeros(1), np.array([0.4]),
+              np.array([8], np.int32), None, np.zeros((1, 1), np.int32))
+    s = scorer_factory(small.pocket, lig)
+    d = np.array([[0.5, -1.0, 2.0, 0.1, 0.2, 0.3], [30.0, 0, 0, 0, 0, 0]], np.float32)
+    E, G, st = s.score_poses(d, grad=True)
+    sysm = synth.System("one", small.pocket, lig, d)
+    E64, G64, _, scale = ref_batch(oracle, sysm, d, grad=True)
+    assert_energy(E[:1], E64[:1], scale[:1])
+    assert_grad(G[:1], G64[:1])
+    assert E[1] == 0.0 and np.all(G[1] == 0.0)  # beyond the 12 A cutoff
+
+
+def test_edge_max_ligand_and_two_slices(oracle, scorer_factory):
+    rng = np.random.default_rng(4)
+    lig = synth.random_ligand(rng, 128, 32)
+    pocket = synth.random_pocket(rng, 13000, 23.0)  # above one shared-memory slice
+    d = synth.random_poses(rng, 40, lig.nrb, 4.0)
+    sysm = synth.System("big", pocket, lig, d)
+    s = scorer_factory(pocket, lig)
+    E, G, st = s.score_poses(d, grad=True)
+    E64, G64, st64, scale = ref_batch(oracle, sysm, d, grad=True)
+    assert_energy(E, E64, scale)
+    assert_grad(G, G64)
+    assert np.array_equal(st, st64)
+
+
+def test_edge_rigid_ligand_and_tiny_pocket(oracle, scorer_factory):
+    rng = np.random.default_rng(5)
+    lig = synth.random_ligand(rng, 20, 0)
+    pocket = synth.random_pocket(rng, 1, 1.0)
+    d = synth.random_poses(rng, 33, 0, 2.0)
+    sysm = synth.System("rigid", pocket, lig, d)
+    s = scorer_factory(pocket, lig)
+    E, G, _ = s.score_poses(d, grad=True)
+    E64, G64, _, scale = ref_batch(oracle, sysm, d, grad=True)
+    assert_energy(E, E64, scale)
+    assert_grad(G, G64)
+
+
+def test_edge_too_long_status(oracle, scorer_factory, small):
+    from mmo_gb300.ff import TooLong
+
+    n = 22
+    xyz = np.array([[i * 1.22, 0.8 * (i % 2), 0.0] for i in range(n)])
+    from mmo_gb300.topology import build_ligand
+
+    lig = build_ligand("chain", xyz - xyz.mean(0), np.zeros(n), np.full(n, 6, np.int32),
+                       [(i, i + 1) for i in range(n - 1)])
+    s = scorer_factory(small.pocket, lig)
+    d = np.zeros((3, 6 + lig.nrb), np.float32)
+    d[1, 6:] = np.pi / 2  # folded: not too long
+    E, _, st = s.score_poses(d)
+    _, st64 = oracle.apply_config(lig, d[0].astype(np.float64))
+    assert st[0] == st64 == 1
+    assert [int(v) for v in st] == [int(oracle.apply_config(lig, c.astype(np.float64))[1])
+                                    for c in d]
+    with pytest.raises(TooLong):
+        s.score_config(d[0])
+
+
+def test_edge_close_contact_clamp(oracle, scorer_factory):
+    # a ligand atom on top of a protein atom: r clamped to 0.01 A, finite energy
+    prot = Mol("p", np.array([0.0, 5.0]), np.zeros(2), np.zeros(2), np.array([0.3, -0.2]),
+               np.array([6, 8], np.int32))
+    lig = Mol("l", np.zeros(1), np.zeros(1), np.zeros(1), np.array([0.1]),
+              np.array([7], np.int32), None, np.zeros((1, 1), np.int32))
+    s = scorer_factory(prot, lig)
+    d = np.array([[0.0, 0.0, 0.004, 0, 0, 0], [0.0, 0.0, 0.5, 0, 0, 0]], np.float32)
+    E, G, st = s.score_poses(d, grad=True)
+    sysm = synth.System("clamp", prot, lig, d)
+    E64, G64, _, scale = ref_batch(oracle, sysm, d, grad=True)
+    assert np.all(np.isfinite(E)) and not np.any(st & 2)
+    assert_energy(E, E64, scale)
+    assert_grad(G, G64)
+
+
+def test_ragged_batch_sizes(oracle, scorer_factory, batch):
+    s = scorer_factory(batch.pocket, batch.ligand)
+    for B in (2, 31, 33, 129, 255):
+        d = batch.poses[:B]
+        E, _, _ = s.score_poses(d)
+        E64, _, _, scale = ref_batch(oracle, batch, d) if B <= 33 else (None, None, None, None)
+        if E64 is not None:
+            assert_energy(E, E64, scale)
+        Efull, _, _ = s.score_poses(batch.poses)
+        assert np.abs(E - Efull[:B]).max() <= 1e-6 * np.abs(Efull[:B]).max()
+
+
+# -- full-size workload through size-independent properties ------------------------
+
+def test_full_size_energy_batch(oracle, scorer_factory):
+    """65,536 poses: a sample against the oracle, and the batch against its
+    own poses re-scored one by one and in another order."""
+    big = synth.pose_batch(n_poses=65536, seed=1)
+    s = scorer_factory(big.pocket, big.ligand)
+    E, _, st = s.score_poses(big.poses)
+    assert np.all(np.isfinite(E))
+    idx = np.random.default_rng(0).choice(len(E), 48, replace=False)
+    E64, _, st64, scale = ref_batch(oracle, big, big.poses[idx])
+    assert_energy(E[idx], E64, scale)
+    perm = np.random.default_rng(1).permutation(len(E))
+    Ep, _, _ = s.score_poses(big.poses[perm])
+    assert np.abs(Ep - E[perm]).max() <= 1e-6 * np.abs(E).max()

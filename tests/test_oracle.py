@@ -1,0 +1,227 @@
+"""The FP64 oracle against known answers, the reference's own test vectors and
+an independent NumPy restatement (CPU only)."""
+import math
+
+import numpy as np
+import pytest
+
+from mmo_gb300 import synth
+from mmo_gb300.topology import Mol, build_ligand
+
+K = 332.0637 / 4.0
+
+
+def two_atoms(a1, q1, a2, q2, r):
+    prot = Mol("p", np.array([0.0]), np.array([0.0]), np.array([0.0]), np.array([q1]),
+               np.array([a1], np.int32))
+    lig = Mol("l", np.array([r]), np.array([0.0]), np.array([0.0]), np.array([q2]),
+              np.array([a2], np.int32))
+    return prot, lig
+
+
+def chain(n, bond=1.5):
+    """zig-zag chain of n carbons with all internal bonds rotatable"""
+    xyz = []
+    for i in range(n):
+        xyz.append([i * bond * math.sin(math.radians(54.75)), 0.8 * (i % 2), 0.0])
+    bonds = [(i, i + 1) for i in range(n - 1)]
+    return build_ligand("chain%d" % n, np.array(xyz), np.zeros(n), np.full(n, 6, np.int32), bonds)
+
+
+# -- known answers from the formulas -------------------------------------------
+
+def test_elec_weight(oracle):
+    assert oracle.elec_weight() == pytest.approx(83.015925, abs=1e-12)
+
+
+def test_shift_values(oracle):
+    # FF.ml:17-20
+    assert oracle.shift_12A(0.0) == 1.0
+    assert oracle.shift_12A(6.0) == pytest.approx(0.5625, abs=1e-15)
+    assert oracle.shift_12A(12.0) == 0.0
+    assert oracle.shift_12A(13.0) == 0.0
+    assert oracle.non_zero_dist(0.001) == 0.01
+    assert oracle.non_zero_dist(0.5) == 0.5
+
+
+def test_pair_table(oracle):
+    # UFF.ml:43-51: geometric means; unsupported elements give NaN
+    x, d = oracle.pair_params(6, 8)
+    assert x == pytest.approx(math.sqrt(3.851 * 3.500), rel=1e-15)
+    assert d == pytest.approx(math.sqrt(0.105 * 0.060), rel=1e-15)
+    x, d = oracle.pair_params(6, 8, oracle.physics(mixing=1))
+    assert x == pytest.approx(0.5 * (3.851 + 3.500), rel=1e-15)
+    x, d = oracle.pair_params(6, 2)
+    assert math.isnan(x) and math.isnan(d)
+
+
+@pytest.mark.parametrize("anum,xi,di", [(1, 2.886, 0.044), (6, 3.851, 0.105), (7, 3.660, 0.069),
+                                        (8, 3.500, 0.060), (16, 4.035, 0.274), (53, 4.5, 0.339)])
+def test_lj_minimum(oracle, anum, xi, di):
+    # at r = x_ij the LJ 12-6 term is -D_ij; global form has no switch
+    prot, lig = two_atoms(anum, 0.0, anum, 0.0, xi)
+    g = oracle.physics(inter_form=1)
+    assert oracle.ene_inter(prot, lig, ph=g) == pytest.approx(-di, rel=1e-12)
+    w = (1.0 - (xi / 12.0) ** 2) ** 2
+    assert oracle.ene_inter(prot, lig) == pytest.approx(-di * w, rel=1e-12)
+
+
+def test_coulomb_pair(oracle):
+    # virtual element 0 has no vdW: only K q1 q2 / r (times the switch)
+    prot, lig = two_atoms(0, 0.5, 0, -0.3, 5.0)
+    w = (1.0 - (5.0 / 12.0) ** 2) ** 2
+    assert oracle.ene_inter(prot, lig) == pytest.approx(K * -0.15 / 5.0 * w, rel=1e-13)
+    assert oracle.ene_inter(prot, lig, ph=oracle.physics(inter_form=1)) == pytest.approx(
+        K * -0.15 / 5.0, rel=1e-13)
+    assert oracle.ene_inter(prot, lig, ph=oracle.physics(dielectric=1, inter_form=1)) == \
+        pytest.approx(K * -0.15 / 25.0, rel=1e-13)
+
+
+def test_cutoff_and_clamp(oracle):
+    prot, lig = two_atoms(6, 0.5, 6, 0.5, 12.0)
+    assert oracle.ene_inter(prot, lig) == 0.0
+    prot, lig = two_atoms(0, 1.0, 0, 1.0, 0.001)  # clamped to 0.01 A
+    assert oracle.ene_inter(prot, lig, ph=oracle.physics(inter_form=1)) == pytest.approx(
+        K / 0.01, rel=1e-13)
+
+
+def test_intra_exclusions(oracle):
+    # 1-2 and 1-3 pairs are excluded; 1-4 counts fully (mol.ml:203-208, 891-894)
+    lig3 = chain(3)
+    assert lig3.interacting.sum() == 0
+    assert oracle.ene_intra(lig3) == 0.0
+    lig4 = chain(4)
+    assert lig4.interacting[0, 3] == 1 and lig4.interacting.sum() == 2
+    r = np.linalg.norm(lig4.xyz()[0] - lig4.xyz()[3])
+    p6 = (3.851 / r) ** 6
+    assert oracle.ene_intra(lig4) == pytest.approx(0.105 * (p6 * p6 - 2 * p6), rel=1e-12)
+
+
+# -- the reference's own numeric test vectors (src/tests.ml:10-54) --------------
+
+def test_dihedral_vectors_from_reference(oracle):
+    c = math.cos(0.25 * math.pi)
+    i, j, k = [0., 0., 0.], [0., 1., 0.], [1., 1., 0.]
+    ls = [[1, 2, 0], [1, 1 + c, c], [1, 1, 1], [1, 1 - c, c], [1, 0, 0], [1, 1 - c, -c],
+          [1, 1, -1], [1, 1 + c, -c]]
+    want = [1.0, -0.75, -0.5, -0.25, 0.0, 0.25, 0.5, 0.75]
+    for l, w in zip(ls, want):
+        assert abs(oracle.dihedral(i, j, k, l) - w * math.pi) <= 0.001
+
+
+def test_rotate_bond_turns_dihedral(oracle, rng):
+    # rotate_bond (mol.ml:610-631) about (j, k) by theta moves dihedral i-j-k-l by +theta,
+    # pinned through the dihedral function of the reference's test above
+    xyz = np.array([[0, 0, 0], [0, 1, 0], [1, 1, 0], [1, 2, 0.]])
+    d0 = oracle.dihedral(*xyz)
+    for th in rng.uniform(-math.pi, math.pi, 8):
+        x2 = oracle.rotate_bond(xyz, 1, 2, [3], th)
+        d1 = oracle.dihedral(*x2)
+        assert abs((d1 - d0 - th + math.pi) % (2 * math.pi) - math.pi) < 1e-12
+        back = oracle.rotate_bond(x2, 1, 2, [3], -th)
+        assert np.abs(back - xyz).max() < 1e-14
+
+
+# -- C oracle vs the independent NumPy twin --------------------------------------
+
+@pytest.mark.parametrize("ph", [dict(), dict(inter_form=1), dict(dielectric=1), dict(mixing=1)])
+def test_c_vs_numpy_inter(oracle, ph):
+    from oracle import np_twin as T
+
+    s = synth.single_pose(seed=7)
+    conf = s.poses[0].astype(np.float64)
+    xyz, st = oracle.apply_config(s.ligand, conf)
+    p, l = s.pocket, s.ligand
+    e_c = oracle.ene_inter(p, l, xyz, ph=oracle.physics(**ph))
+    e_n = T.ene_inter(p.xyz(), p.q, p.anum, xyz, l.q, l.anum, shifted=ph.get("inter_form", 0) == 0,
+                      mixing=ph.get("mixing", 0), dielectric=ph.get("dielectric", 0))
+    assert e_c == pytest.approx(e_n, rel=1e-12)
+    if ph.get("inter_form", 0) == 0:
+        assert oracle.ene_inter_cells(p, l, xyz, ph=oracle.physics(**ph)) == pytest.approx(
+            e_c, rel=1e-12)
+
+
+def test_c_vs_numpy_intra_and_pose(oracle, rng):
+    from oracle import np_twin as T
+
+    for seed in range(4):
+        r = np.random.default_rng(seed)
+        lig = synth.random_ligand(r, int(r.integers(8, 60)), int(r.integers(0, 12)))
+        conf = np.concatenate([r.uniform(-3, 3, 3), r.uniform(-np.pi, np.pi, 3 + lig.nrb)])
+        for flags in (0, oracle.F_RECENTER):
+            x_c, _ = oracle.apply_config(lig, conf, flags)
+            x_n = T.apply_config(lig.xyz(), lig.rbonds, lig.rgroups, conf, recenter=bool(flags))
+            assert np.abs(x_c - x_n).max() < 1e-12
+        assert oracle.ene_intra(lig, x_c) == pytest.approx(
+            T.ene_intra(x_c, lig.q, lig.anum, lig.interacting), rel=1e-12, abs=1e-12)
+
+
+# -- analytic FP64 gradient vs central differences (h = 1e-4) --------------------
+
+@pytest.mark.parametrize("flags", [3, 3 | 8, 1, 2])
+def test_gradient_vs_fd(oracle, flags):
+    # dense pocket: clash energies up to 1e16, so a small step (1e-6) keeps the
+    # central-difference truncation error below the check
+    s = synth.pose_batch(n_poses=4, seed=5, n_atoms=20, n_rot=4, n_pocket=400, radius=10.0,
+                         half_box=6.0)
+    for conf in s.poses.astype(np.float64):
+        E, g, st = oracle.grad_analytic(s.pocket, s.ligand, conf, flags)
+        Es, _ = oracle.score_conf(s.pocket, s.ligand, conf, flags)
+        assert E == pytest.approx(Es, rel=1e-12)
+        gf = oracle.grad_fd(s.pocket, s.ligand, conf, 1e-6, flags)
+        scale = np.abs(g).max()
+        assert np.abs(g - gf).max() <= 1e-6 * scale + 1e-9
+
+
+def test_gradient_vs_fd_h1e4(oracle):
+    # sparse pocket (moderate energies): central differences with h = 1e-4 A/rad
+    s = synth.pose_batch(n_poses=4, seed=8, n_atoms=24, n_rot=5, n_pocket=150, radius=14.0,
+                         half_box=3.0)
+    for conf in s.poses.astype(np.float64):
+        E, g, _ = oracle.grad_analytic(s.pocket, s.ligand, conf)
+        gf = oracle.grad_fd(s.pocket, s.ligand, conf, 1e-4)
+        assert np.abs(g - gf).max() <= 1e-4 * np.abs(g).max()
+
+
+def test_gradient_physics_variants(oracle):
+    s = synth.pose_batch(n_poses=2, seed=9, n_atoms=16, n_rot=3, n_pocket=300, radius=9.0)
+    for ph in (oracle.physics(1, 1, 1, 1), oracle.physics(0, 0, 1, 0), oracle.physics(1, 0, 0, 1)):
+        for conf in s.poses.astype(np.float64):
+            E, g, _ = oracle.grad_analytic(s.pocket, s.ligand, conf, ph=ph)
+            gf = oracle.grad_fd(s.pocket, s.ligand, conf, 1e-4, ph=ph)
+            assert np.abs(g - gf).max() <= 1e-5 * np.abs(g).max() + 1e-9
+
+
+# -- invariances and statuses ---------------------------------------------------
+
+def test_invariances(oracle, rng):
+    s = synth.single_pose(seed=3)
+    xyz, _ = oracle.apply_config(s.ligand, s.poses[0].astype(np.float64))
+    e0 = oracle.ene_inter(s.pocket, s.ligand, xyz)
+    perm = rng.permutation(s.pocket.n)
+    p = s.pocket
+    pp = Mol("pp", p.x[perm], p.y[perm], p.z[perm], p.q[perm], p.anum[perm])
+    assert oracle.ene_inter(pp, s.ligand, xyz) == pytest.approx(e0, rel=1e-12)
+    t = np.array([3.0, -7.0, 11.0])
+    pt = Mol("pt", p.x + t[0], p.y + t[1], p.z + t[2], p.q, p.anum)
+    assert oracle.ene_inter(pt, s.ligand, xyz + t) == pytest.approx(e0, rel=1e-11)
+
+
+def test_too_long_status(oracle):
+    lig = chain(22)  # about 29 A end to end
+    lig = lig.centered()
+    _, st = oracle.apply_config(lig, np.zeros(6 + lig.nrb))
+    assert st == oracle.S_TOO_LONG
+    short = chain(6).centered()
+    _, st = oracle.apply_config(short, np.zeros(6 + short.nrb))
+    assert st == 0
+
+
+def test_batch_matches_single(oracle):
+    s = synth.pose_batch(n_poses=6, seed=2, n_atoms=12, n_rot=3, n_pocket=200, radius=8.0)
+    E, G, st = oracle.score_batch(s.pocket, s.ligand, s.poses, mode=1, nthreads=3)
+    Ec, _, _ = oracle.score_batch(s.pocket, s.ligand, s.poses, mode=0, use_cells=True)
+    for b, conf in enumerate(s.poses.astype(np.float64)):
+        e, g, _ = oracle.grad_analytic(s.pocket, s.ligand, conf)
+        assert E[b] == e and np.array_equal(G[b], g)
+        assert Ec[b] == pytest.approx(e, rel=1e-12)
