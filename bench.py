@@ -48,8 +48,8 @@ POSES = 4096
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--poses", type=int, default=POSES)
     ap.add_argument("--cpu-sample", type=int, default=0,
@@ -161,7 +161,9 @@ def run_reference(args):
         return 0
     nthreads = os.cpu_count() or 1
     s = system_for_rank(0, args.poses)
-    sample = args.cpu_sample or calibrate_sample(s, nthreads, target_s=8.0)
+    # about two minutes of CPU work over all the timed steps
+    budget = 120.0 / max(args.steps, 1)
+    sample = args.cpu_sample or min(args.poses, calibrate_sample(s, nthreads, target_s=budget))
     times = []
     for _ in range(max(args.warmup, 0) and 1):
         cpu_baseline(s, min(sample, nthreads), nthreads)
@@ -219,7 +221,8 @@ def main():
     d_G = torch.empty((B, nd), dtype=torch.float32, device=dev)
     d_st = torch.empty(B, dtype=torch.int32, device=dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > L2
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     sp = stream.cuda_stream
 
     def step():

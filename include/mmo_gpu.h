@@ -109,13 +109,15 @@ int mmo_score_poses(mmo_ctx* ctx, int B, const float* dofs, int flags, double* E
                     float* grad_out, int* status_out);
 
 /* As mmo_score_poses with device pointers, queued on `stream` (a
- * cudaStream_t, or NULL for the context's stream) without synchronising;
- * mmo_sync() waits and reports device-side errors. */
+ * cudaStream_t; NULL is the legacy default stream) without synchronising;
+ * mmo_sync() waits and reports device-side errors.  Calls on one context
+ * share its scratch buffers, so they must all go to one stream. */
 int mmo_score_poses_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E,
                            float* d_grad, int* d_status, void* stream);
 
-/* Wait for the context's work on `stream` (NULL: its own) and report any
- * device-side error flag (MMO_ETIMEOUT). */
+/* Wait for `stream` (a cudaStream_t; NULL is the legacy default stream) and
+ * report, then clear, the device-side error flag of the device-pointer calls
+ * (MMO_ETIMEOUT). */
 int mmo_sync(mmo_ctx* ctx, void* stream);
 
 /* Tile shape of the batched pair kernel: poses per lane (1, 2, 4), threads

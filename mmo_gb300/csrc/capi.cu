@@ -50,6 +50,14 @@ void pair_xd(int mixing, int t1, int t2, double* x2, double* d) {
 
 char g_create_err[256] = "";
 
+// (x, y, z) as hi/lo float pairs: dst[0] = (hi..., w), dst[1] = (lo..., 0)
+void split_store(float4* dst, double x, double y, double z, float w) {
+  const float xh = (float)x, yh = (float)y, zh = (float)z;
+  dst[0] = make_float4(xh, yh, zh, w);
+  dst[1] = make_float4((float)(x - (double)xh), (float)(y - (double)yh), (float)(z - (double)zh),
+                       0.f);
+}
+
 // next 16-byte aligned offset of a block of `bytes`
 size_t take(size_t& off, size_t bytes) {
   const size_t o = (off + 15) & ~size_t(15);
@@ -170,7 +178,7 @@ int grow_host(mmo_ctx* ctx, char** h, char** d, size_t* cap, size_t bytes) {
 int ensure_scratch(mmo_ctx* ctx, int B, int L, int C, bool grad) {
   int r;
   const size_t n = (size_t)B * C * L;
-  if ((r = grow(ctx, (void**)&ctx->scr.X, &ctx->capX, sizeof(float4) * (size_t)B * L, "X")))
+  if ((r = grow(ctx, (void**)&ctx->scr.X, &ctx->capX, sizeof(float4) * 2 * (size_t)B * L, "X")))
     return r;
   if ((r = grow(ctx, (void**)&ctx->scr.Epart, &ctx->capE, sizeof(double) * n, "Epart"))) return r;
   if (grad && (r = grow(ctx, (void**)&ctx->scr.Gpart, &ctx->capG, sizeof(float4) * n, "Gpart")))
@@ -230,6 +238,7 @@ int upload_ligand(mmo_ctx* ctx) {
     L.nrb = nrb;
     L.npairs = np;
     L.ref = align_ptr<float4>(b, off, n);
+    L.ref64 = align_ptr<double>(b, off, 3 * (size_t)n);
     L.type = align_ptr<int>(b, off, n);
     L.q = align_ptr<float>(b, off, n);
     L.bonds = align_ptr<int2>(b, off, bonds.size());
@@ -246,6 +255,12 @@ int upload_ligand(mmo_ctx* ctx) {
   std::vector<char> host(bytes, 0);
   DevLigand H = layout(host.data());
   memcpy((void*)H.ref, ref.data(), sizeof(float4) * n);
+  for (int i = 0; i < n; ++i) {
+    double* r64 = const_cast<double*>(H.ref64) + 3 * i;
+    r64[0] = ctx->lx[i];
+    r64[1] = ctx->ly[i];
+    r64[2] = ctx->lz[i];
+  }
   memcpy((void*)H.type, ctx->ltype.data(), sizeof(int) * n);
   for (int i = 0; i < n; ++i) const_cast<float*>(H.q)[i] = (float)ctx->lq[i];
   memcpy((void*)H.bonds, bonds.data(), sizeof(int2) * bonds.size());
@@ -288,7 +303,7 @@ PairPlan make_plan(mmo_ctx* ctx, int B, bool grad) {
   const int P = ctx->prot.P, L = ctx->lig.L;
   const int nslices = (P + kSliceAtoms - 1) / kSliceAtoms;
   const int slice_len = (P + nslices - 1) / nslices;
-  const int smem = slice_len * 16;
+  const int smem = slice_len * 32;
   int bps = pairs_batched_max_blocks(p.kp, p.threads, grad, ctx->ph, smem);
   if (bps < 1) bps = 1;
   p.blocks = ctx->sms * bps;
@@ -493,15 +508,15 @@ int mmo_set_protein(mmo_ctx* ctx, int n, const double* xs, const double* ys, con
   std::vector<int> idx(n);
   std::iota(idx.begin(), idx.end(), 0);
   std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return type[a] < type[b]; });
-  std::vector<float4> atoms(std::max(n, 1));
+  std::vector<float4> atoms(2 * (size_t)std::max(n, 1));
   std::vector<uint8_t> ptype(std::max(n, 16), 0);
   std::vector<int> rstart, rtype;
   DevProtein P{};
   P.P = n;
   for (int k = 0; k < n; ++k) {
     const int i = idx[k];
-    atoms[k] = make_float4((float)(xs[i] - (double)of[0]), (float)(ys[i] - (double)of[1]),
-                           (float)(zs[i] - (double)of[2]), (float)(kElec * q[i]));
+    split_store(&atoms[2 * (size_t)k], xs[i] - (double)of[0], ys[i] - (double)of[1],
+                zs[i] - (double)of[2], (float)(kElec * q[i]));
     ptype[k] = (uint8_t)type[i];
     if (k == 0 || type[i] != type[idx[k - 1]]) {
       rstart.push_back(k);
@@ -602,7 +617,7 @@ int mmo_ene_inter(mmo_ctx* ctx, int n, const double* xs, const double* ys, const
   // staging: X[n] float4 | q[n] float | type[n] int ; output: C*n doubles | E
   const int C = std::max(1, (ctx->prot.P + 255) / 256);
   size_t off = 0;
-  const size_t oX = take(off, sizeof(float4) * n);
+  const size_t oX = take(off, sizeof(float4) * 2 * n);
   const size_t oq = take(off, sizeof(float) * n);
   const size_t ot = take(off, sizeof(int) * n);
   const size_t in_bytes = off;
@@ -617,8 +632,8 @@ int mmo_ene_inter(mmo_ctx* ctx, int n, const double* xs, const double* ys, const
   for (int i = 0; i < n; ++i) {
     const int t = type_of(anum[i]);
     if (t < 0) return fail(ctx, MMO_EELEMENT, "ligand atom %d: element %d not in the UFF table", i, anum[i]);
-    hX[i] = make_float4((float)(xs[i] - ctx->origin[0]), (float)(ys[i] - ctx->origin[1]),
-                        (float)(zs[i] - ctx->origin[2]), 0.f);
+    split_store(&hX[2 * i], xs[i] - ctx->origin[0], ys[i] - ctx->origin[1],
+                zs[i] - ctx->origin[2], 0.f);
     hq[i] = (float)q[i];
     ht[i] = t;
   }
@@ -646,15 +661,15 @@ int mmo_ene_intra(mmo_ctx* ctx, const double* xs, const double* ys, const double
   if (!ctx->has_lig) return fail(ctx, MMO_ESTATE, "no ligand: call mmo_set_ligand first");
   if (!xs || !ys || !zs || !out) return fail(ctx, MMO_EINVAL, "mmo_ene_intra: null pointer");
   const int n = ctx->lig.L;
-  int r = grow_host(ctx, &ctx->h_in, &ctx->d_in, &ctx->cap_in, sizeof(float4) * n);
+  int r = grow_host(ctx, &ctx->h_in, &ctx->d_in, &ctx->cap_in, sizeof(float4) * 2 * n);
   if (r) return r;
   r = grow_host(ctx, &ctx->h_out, &ctx->d_out, &ctx->cap_out, sizeof(double));
   if (r) return r;
   float4* hX = reinterpret_cast<float4*>(ctx->h_in);
   // the intra term is translation-invariant: centre on atom 0 before rounding
   for (int i = 0; i < n; ++i)
-    hX[i] = make_float4((float)(xs[i] - xs[0]), (float)(ys[i] - ys[0]), (float)(zs[i] - zs[0]), 0.f);
-  MMO_CK(cudaMemcpyAsync(ctx->d_in, ctx->h_in, sizeof(float4) * n, cudaMemcpyHostToDevice,
+    split_store(&hX[2 * i], xs[i] - xs[0], ys[i] - ys[0], zs[i] - zs[0], 0.f);
+  MMO_CK(cudaMemcpyAsync(ctx->d_in, ctx->h_in, sizeof(float4) * 2 * n, cudaMemcpyHostToDevice,
                          ctx->stream),
          "H2D");
   MMO_CK(launch_intra_plain(ctx->lig, reinterpret_cast<const float4*>(ctx->d_in),
@@ -712,13 +727,14 @@ int mmo_score_poses(mmo_ctx* ctx, int B, const float* dofs, int flags, double* E
 int mmo_score_poses_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E,
                            float* d_grad, int* d_status, void* stream) {
   if (!ctx) return MMO_EINVAL;
-  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : ctx->stream;
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   return score_device(ctx, B, d_dofs, flags, d_E, d_grad, d_status, ctx->d_err, 0, st);
 }
 
 int mmo_sync(mmo_ctx* ctx, void* stream) {
   if (!ctx) return MMO_EINVAL;
-  cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : ctx->stream;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   MMO_CK(cudaStreamSynchronize(st), "sync");
   int flag = 0;
   MMO_CK(cudaMemcpy(&flag, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");

@@ -31,13 +31,13 @@ __global__ void __launch_bounds__(512)
   if (threadIdx.x < 2 * prot.nruns + 1) s_runs[threadIdx.x] = prot.runs[threadIdx.x];
   if (threadIdx.x == 0) {
     mbar_init(&bar, 1);
-    const uint32_t bytes = (uint32_t)slice_len * 16u;
+    const uint32_t bytes = (uint32_t)slice_len * 32u;
     mbar_expect_tx(&bar, bytes);
     constexpr uint32_t kPiece = 32768u;
     for (uint32_t off = 0; off < bytes; off += kPiece) {
       const uint32_t n = bytes - off < kPiece ? bytes - off : kPiece;
       bulk_g2s(reinterpret_cast<char*>(sp) + off,
-               reinterpret_cast<const char*>(prot.atoms + slice0) + off, n, &bar);
+               reinterpret_cast<const char*>(prot.atoms + 2 * (size_t)slice0) + off, n, &bar);
     }
   }
   __syncthreads();
@@ -65,16 +65,22 @@ __global__ void __launch_bounds__(512)
     const int ltype = lig.type[j];
     const float qj = lig.ref[j].w;
 
-    float px[KP], py[KP], pz[KP], ae[KP], gx[KP], gy[KP], gz[KP];
+    float px[KP], py[KP], pz[KP], lx[KP], ly[KP], lz[KP], ae[KP], gx[KP], gy[KP], gz[KP];
     double ad[KP];
 #pragma unroll
     for (int k = 0; k < KP; ++k) {
       const int b = pb * 32 * KP + k * 32 + lane;
-      float4 x = make_float4(1e4f, 1e4f, 1e4f, 0.f);
-      if (b < B) x = scr.X[(size_t)b * L + j];
-      px[k] = x.x;
-      py[k] = x.y;
-      pz[k] = x.z;
+      float4 xh = make_float4(1e4f, 1e4f, 1e4f, 0.f), xl = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (b < B) {
+        xh = scr.X[((size_t)b * L + j) * 2];
+        xl = scr.X[((size_t)b * L + j) * 2 + 1];
+      }
+      px[k] = xh.x;
+      py[k] = xh.y;
+      pz[k] = xh.z;
+      lx[k] = xl.x;
+      ly[k] = xl.y;
+      lz[k] = xl.z;
       ae[k] = gx[k] = gy[k] = gz[k] = 0.f;
       ad[k] = 0.0;
     }
@@ -87,11 +93,14 @@ __global__ void __launch_bounds__(512)
         const int i1 = min(i0 + kFlush, hi);
 #pragma unroll 4
         for (int i = i0 - slice0; i < i1 - slice0; ++i) {
-          const float4 p = sp[i];
+          const float4 p = sp[2 * i];
+          const float4 pl = sp[2 * i + 1];
           const float qq = p.w * qj;
 #pragma unroll
           for (int k = 0; k < KP; ++k)
-            uff_pair<GRAD, DIEL, FORM>(px[k] - p.x, py[k] - p.y, pz[k] - p.z, xd.x, xd.y, qq,
+            uff_pair<GRAD, DIEL, FORM>(split_diff(px[k], lx[k], p.x, pl.x),
+                                       split_diff(py[k], ly[k], p.y, pl.y),
+                                       split_diff(pz[k], lz[k], p.z, pl.z), xd.x, xd.y, qq,
                                        ae[k], gx[k], gy[k], gz[k]);
         }
 #pragma unroll
@@ -127,14 +136,15 @@ __global__ void __launch_bounds__(256)
   if (item >= C * L) return;
   const int j = item % L, c = item / L;
   const int c0 = c * chunk_len, c1 = min(c0 + chunk_len, prot.P);
-  const float4 xj = X[j];
+  const float4 xh = X[2 * j], xl = X[2 * j + 1];
   const float qj = lig_q[j];
   const int lt = lig_type[j];
   float ae = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
   for (int i = c0 + lane; i < c1; i += 32) {
-    const float4 p = prot.atoms[i];
+    const float4 p = prot.atoms[2 * i], pl = prot.atoms[2 * i + 1];
     const float2 xd = stab[prot.type[i] * kNTypes + lt];
-    uff_pair<GRAD, DIEL, FORM>(xj.x - p.x, xj.y - p.y, xj.z - p.z, xd.x, xd.y, p.w * qj, ae, gx,
+    uff_pair<GRAD, DIEL, FORM>(split_diff(xh.x, xl.x, p.x, pl.x), split_diff(xh.y, xl.y, p.y, pl.y),
+                               split_diff(xh.z, xl.z, p.z, pl.z), xd.x, xd.y, p.w * qj, ae, gx,
                                gy, gz);
   }
   const double e = warp_sum((double)ae);
@@ -196,7 +206,7 @@ cudaError_t launch_pairs_batched(const DevProtein& prot, const PairTable& tab,
     const int s0 = sl * slice_len, s1 = min(s0 + slice_len, prot.P);
     if (s0 >= s1) break;
     const int chunk_len = (s1 - s0 + C_slice - 1) / C_slice;
-    const int smem = (s1 - s0) * 16;
+    const int smem = (s1 - s0) * 32;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     fn<<<plan.blocks, plan.threads, smem, st>>>(prot, tab, lig, s, B, s0, s1, sl * C_slice,

@@ -124,56 +124,149 @@ __device__ __forceinline__ float3 centroid(const DevLigand& lig, int lane, const
   return make_float3(warp_sum(sx) * inv, warp_sum(sy) * inv, warp_sum(sz) * inv);
 }
 
-// mol.ml:576-591: max_i (0.01 + |c - y_i|) > 12
-__device__ __forceinline__ bool too_long(const DevLigand& lig, int lane, float3 c,
-                                         const float (&zx)[kSlots], const float (&zy)[kSlots],
-                                         const float (&zz)[kSlots]) {
-  float r = 0.f;
+// ---- FP64 pose map (k_rebuild) --------------------------------------------
+__device__ __forceinline__ double pickd(const double (&v)[kSlots], int slot) {
+  double r = v[0];
 #pragma unroll
-  for (int s = 0; s < kSlots; ++s)
-    if (lane + 32 * s < lig.L) {
-      const float dx = c.x - zx[s], dy = c.y - zy[s], dz = c.z - zz[s];
-      r = fmaxf(r, 0.01f + sqrtf(dx * dx + dy * dy + dz * dz));
-    }
-  return warp_max(r) > 12.0f;
+  for (int s = 1; s < kSlots; ++s)
+    if (slot == s) r = v[s];
+  return r;
+}
+
+__device__ __forceinline__ double3 fetchd(const double (&x)[kSlots], const double (&y)[kSlots],
+                                          const double (&z)[kSlots], int idx) {
+  const int owner = idx & 31, slot = idx >> 5;
+  return make_double3(__shfl_sync(kFull, pickd(x, slot), owner),
+                      __shfl_sync(kFull, pickd(y, slot), owner),
+                      __shfl_sync(kFull, pickd(z, slot), owner));
+}
+
+__device__ __forceinline__ double warp_maxd(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
+
+// sine and cosine of angle k of the pose ([a, b, g, tau_0 ...]), computed
+// once by lane (k & 31) in round (k >> 5) and read back by every lane
+struct AngleTable {
+  double s0, c0, s1, c1;
+  __device__ __forceinline__ void get(int k, double& s, double& c) const {
+    const int owner = k & 31;
+    const bool hi = k >= 32;
+    s = __shfl_sync(kFull, hi ? s1 : s0, owner);
+    c = __shfl_sync(kFull, hi ? c1 : c0, owner);
+  }
+};
+
+__device__ __forceinline__ AngleTable angle_table(const float* dof, int nrb, int lane) {
+  AngleTable t{0.0, 1.0, 0.0, 1.0};
+  const int n = 3 + nrb;
+  if (lane < n) sincos((double)dof[3 + lane], &t.s0, &t.c0);
+  if (lane + 32 < n) sincos((double)dof[3 + lane + 32], &t.s1, &t.c1);
+  return t;
+}
+
+__device__ __forceinline__ void store_split(float4* X, double x, double y, double z) {
+  const float xh = __double2float_rn(x), yh = __double2float_rn(y), zh = __double2float_rn(z);
+  X[0] = make_float4(xh, yh, zh, 0.f);
+  X[1] = make_float4(__double2float_rn(x - (double)xh), __double2float_rn(y - (double)yh),
+                     __double2float_rn(z - (double)zh), 0.f);
 }
 
 // ---------------------------------------------------------------------------
-// k_rebuild: posed coordinates X[b][a] (device frame) and, optionally, the
-// intra-ligand energy of mol.ml:881-903 (IFORM 1) or 853-877 (IFORM 0).
+// k_rebuild: posed coordinates X[b][a] (device frame, hi/lo floats) computed
+// in FP64 and, optionally, the intra-ligand energy of mol.ml:881-903 (IFORM 1)
+// or 853-877 (IFORM 0).
 // ---------------------------------------------------------------------------
 template <bool RECENTER, int DIEL, int IFORM>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     k_rebuild(DevLigand lig, PoseIO io, Scratch scr, int with_intra) {
-  __shared__ float4 sx[kWarpsPerBlock][kMaxLig];
+  __shared__ float4 sxh[kWarpsPerBlock][kMaxLig];
+  __shared__ float4 sxl[kWarpsPerBlock][kMaxLig];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int b = blockIdx.x * kWarpsPerBlock + wib;
   if (b >= io.B) return;
-  const int L = lig.L, nd = 6 + lig.nrb;
+  const int L = lig.L, nrb = lig.nrb, nd = 6 + nrb;
   const float* dof = io.dofs + (size_t)b * nd;
-  float zx[kSlots], zy[kSlots], zz[kSlots];
-  load_ref(lig, lane, zx, zy, zz);
-  torsion_chain<false>(lig, dof + 6, lane, zx, zy, zz, nullptr);
-  const float3 c = centroid(lig, lane, zx, zy, zz);
-  const int status = too_long(lig, lane, c, zx, zy, zz) ? kStatusTooLong : 0;
-  float R[9], cs[6];
-  rot_xyz(dof, R, cs);
-  const float tx = dof[0] - io.ox, ty = dof[1] - io.oy, tz = dof[2] - io.oz;
+  const AngleTable ang = angle_table(dof, nrb, lane);
+  double zx[kSlots], zy[kSlots], zz[kSlots];
+#pragma unroll
+  for (int s = 0; s < kSlots; ++s) {
+    const int a = lane + 32 * s;
+    zx[s] = a < L ? lig.ref64[3 * a] : 0.0;
+    zy[s] = a < L ? lig.ref64[3 * a + 1] : 0.0;
+    zz[s] = a < L ? lig.ref64[3 * a + 2] : 0.0;
+  }
+  // torsions in bond order (optim.ml:68-71, mol.ml:610-631)
+  for (int t = 0; t < nrb; ++t) {
+    const int2 bd = lig.bonds[t];
+    const double3 pl = fetchd(zx, zy, zz, bd.x);
+    const double3 pr = fetchd(zx, zy, zz, bd.y);
+    const double ax = pr.x - pl.x, ay = pr.y - pl.y, az = pr.z - pl.z;
+    const double len = sqrt(ax * ax + ay * ay + az * az);
+    const double ux = ax / len, uy = ay / len, uz = az / len;
+    double sn, cs;
+    ang.get(3 + t, sn, cs);
+    const double o = 1.0 - cs;
+    const double R0 = cs + ux * ux * o, R1 = ux * uy * o - uz * sn, R2 = ux * uz * o + uy * sn;
+    const double R3 = ux * uy * o + uz * sn, R4 = cs + uy * uy * o, R5 = uy * uz * o - ux * sn;
+    const double R6 = ux * uz * o - uy * sn, R7 = uy * uz * o + ux * sn, R8 = cs + uz * uz * o;
+#pragma unroll
+    for (int s = 0; s < kSlots; ++s) {
+      if ((lig.gmask[t * kSlots + s] >> lane) & 1u) {
+        const double vx = zx[s] - pr.x, vy = zy[s] - pr.y, vz = zz[s] - pr.z;
+        zx[s] = R0 * vx + R1 * vy + R2 * vz + pr.x;
+        zy[s] = R3 * vx + R4 * vy + R5 * vz + pr.y;
+        zz[s] = R6 * vx + R7 * vy + R8 * vz + pr.z;
+      }
+    }
+  }
+  // centroid and enclosing radius (mol.ml:576-591)
+  double cx = 0.0, cy = 0.0, cz = 0.0;
+#pragma unroll
+  for (int s = 0; s < kSlots; ++s)
+    if (lane + 32 * s < L) {
+      cx += zx[s];
+      cy += zy[s];
+      cz += zz[s];
+    }
+  cx = warp_sum(cx) / L;
+  cy = warp_sum(cy) / L;
+  cz = warp_sum(cz) / L;
+  double rad = 0.0;
+#pragma unroll
+  for (int s = 0; s < kSlots; ++s)
+    if (lane + 32 * s < L) {
+      const double dx = cx - zx[s], dy = cy - zy[s], dz = cz - zz[s];
+      rad = fmax(rad, 0.01 + sqrt(dx * dx + dy * dy + dz * dz));
+    }
+  const int status = warp_maxd(rad) > 12.0 ? kStatusTooLong : 0;
+  // rigid map: Rz(g) Ry(b) Rx(a) (rot.ml:52-66), then + t
+  double sa, ca, sb, cb, sg, cg;
+  ang.get(0, sa, ca);
+  ang.get(1, sb, cb);
+  ang.get(2, sg, cg);
+  const double R0 = cb * cg, R1 = cg * sa * sb - ca * sg, R2 = sa * sg + ca * cg * sb;
+  const double R3 = cb * sg, R4 = ca * cg + sa * sb * sg, R5 = ca * sb * sg - cg * sa;
+  const double R6 = -sb, R7 = cb * sa, R8 = ca * cb;
+  const double tx = (double)dof[0] - (double)io.ox, ty = (double)dof[1] - (double)io.oy,
+               tz = (double)dof[2] - (double)io.oz;
 #pragma unroll
   for (int s = 0; s < kSlots; ++s) {
     const int a = lane + 32 * s;
     if (a < L) {
-      float vx = zx[s], vy = zy[s], vz = zz[s];
+      double vx = zx[s], vy = zy[s], vz = zz[s];
       if (RECENTER) {
-        vx -= c.x;
-        vy -= c.y;
-        vz -= c.z;
+        vx -= cx;
+        vy -= cy;
+        vz -= cz;
       }
-      const float4 p = make_float4(R[0] * vx + R[1] * vy + R[2] * vz + tx,
-                                   R[3] * vx + R[4] * vy + R[5] * vz + ty,
-                                   R[6] * vx + R[7] * vy + R[8] * vz + tz, 0.f);
-      scr.X[(size_t)b * L + a] = p;
-      sx[wib][a] = p;
+      float4* out = scr.X + ((size_t)b * L + a) * 2;
+      store_split(out, R0 * vx + R1 * vy + R2 * vz + tx, R3 * vx + R4 * vy + R5 * vz + ty,
+                  R6 * vx + R7 * vy + R8 * vz + tz);
+      sxh[wib][a] = out[0];
+      sxl[wib][a] = out[1];
     }
   }
   double e_intra = 0.0;
@@ -183,9 +276,12 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     for (int p = lane; p < lig.npairs; p += 32) {
       const int2 ij = lig.pair_ij[p];
       const float4 par = lig.pair_par[p];
-      const float4 pi = sx[wib][ij.x], pj = sx[wib][ij.y];
-      uff_pair<false, DIEL, IFORM>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, par.x, par.y, par.z,
-                                   acc, d0, d1, d2);
+      const float4 ih = sxh[wib][ij.x], il = sxl[wib][ij.x];
+      const float4 jh = sxh[wib][ij.y], jl = sxl[wib][ij.y];
+      uff_pair<false, DIEL, IFORM>(split_diff(ih.x, il.x, jh.x, jl.x),
+                                   split_diff(ih.y, il.y, jh.y, jl.y),
+                                   split_diff(ih.z, il.z, jh.z, jl.z), par.x, par.y, par.z, acc,
+                                   d0, d1, d2);
     }
     e_intra = warp_sum((double)acc);
   }
@@ -203,7 +299,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 template <bool GRAD, bool RECENTER, int DIEL, int IFORM>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     k_finish(DevLigand lig, PoseIO io, Scratch scr, int flags) {
-  __shared__ float4 sx[kWarpsPerBlock][kMaxLig];
+  __shared__ float4 sxh[kWarpsPerBlock][kMaxLig];
+  __shared__ float4 sxl[kWarpsPerBlock][kMaxLig];
   __shared__ TorsRec srec[kWarpsPerBlock][kMaxTors];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int b = blockIdx.x * kWarpsPerBlock + wib;
@@ -250,15 +347,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
   float R[9], cs[6];
   rot_xyz(dof, R, cs);
   if (flags & kFlagIntra) {
-    // posed coordinates (frame-free: the intra term is rigid-invariant)
+    // intra-ligand gradient at the stored hi/lo posed coordinates
 #pragma unroll
     for (int s = 0; s < kSlots; ++s) {
       const int a = lane + 32 * s;
       if (a < L) {
-        const float vx = zx[s] - c.x, vy = zy[s] - c.y, vz = zz[s] - c.z;
-        sx[wib][a] = make_float4(R[0] * vx + R[1] * vy + R[2] * vz,
-                                 R[3] * vx + R[4] * vy + R[5] * vz,
-                                 R[6] * vx + R[7] * vy + R[8] * vz, 0.f);
+        sxh[wib][a] = scr.X[((size_t)b * L + a) * 2];
+        sxl[wib][a] = scr.X[((size_t)b * L + a) * 2 + 1];
       }
     }
     __syncwarp();
@@ -266,13 +361,16 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     for (int s = 0; s < kSlots; ++s) {
       const int a = lane + 32 * s;
       if (a < L) {
-        const float4 pa = sx[wib][a];
+        const float4 ah = sxh[wib][a], al = sxl[wib][a];
         float acc = 0.f;
         for (int k = lig.nb_off[a]; k < lig.nb_off[a + 1]; ++k) {
-          const float4 pb = sx[wib][lig.nb_idx[k]];
+          const int j = lig.nb_idx[k];
+          const float4 bh = sxh[wib][j], bl = sxl[wib][j];
           const float4 par = lig.nb_par[k];
-          uff_pair<true, DIEL, IFORM>(pa.x - pb.x, pa.y - pb.y, pa.z - pb.z, par.x, par.y,
-                                      par.z, acc, gx[s], gy[s], gz[s]);
+          uff_pair<true, DIEL, IFORM>(split_diff(ah.x, al.x, bh.x, bl.x),
+                                      split_diff(ah.y, al.y, bh.y, bl.y),
+                                      split_diff(ah.z, al.z, bh.z, bl.z), par.x, par.y, par.z,
+                                      acc, gx[s], gy[s], gz[s]);
         }
       }
     }
@@ -437,16 +535,19 @@ __global__ void k_reduce_plain(const double* Epart, int n, double* out) {
   if (threadIdx.x == 0) out[0] = e;
 }
 
-// one warp: intra-ligand energy of one set of coordinates (mol.ml:881-903)
+// one warp: intra-ligand energy of one set of hi/lo coordinates X[L][2]
+// (mol.ml:881-903)
 template <int DIEL, int IFORM>
 __global__ void k_intra_plain(DevLigand lig, const float4* X, double* out) {
   float acc = 0.f, d0 = 0.f, d1 = 0.f, d2 = 0.f;
   for (int p = threadIdx.x; p < lig.npairs; p += 32) {
     const int2 ij = lig.pair_ij[p];
     const float4 par = lig.pair_par[p];
-    const float4 pi = X[ij.x], pj = X[ij.y];
-    uff_pair<false, DIEL, IFORM>(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, par.x, par.y, par.z,
-                                 acc, d0, d1, d2);
+    const float4 ih = X[2 * ij.x], il = X[2 * ij.x + 1], jh = X[2 * ij.y], jl = X[2 * ij.y + 1];
+    uff_pair<false, DIEL, IFORM>(split_diff(ih.x, il.x, jh.x, jl.x),
+                                 split_diff(ih.y, il.y, jh.y, jl.y),
+                                 split_diff(ih.z, il.z, jh.z, jl.z), par.x, par.y, par.z, acc,
+                                 d0, d1, d2);
   }
   const double e = warp_sum((double)acc);
   if (threadIdx.x == 0) out[0] = e;

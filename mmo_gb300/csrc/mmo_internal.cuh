@@ -11,15 +11,22 @@ constexpr int kMaxLig = 128;    // ligand atoms per system (4 per lane in a warp
 constexpr int kSlots = kMaxLig / 32;
 constexpr int kMaxTors = 32;    // rotatable bonds per ligand
 constexpr int kNTypes = 12;     // UFF elements of src/UFF.ml:10-22
-constexpr int kSliceAtoms = 12288;  // protein atoms resident in shared memory per launch
+constexpr int kSliceAtoms = 6912;   // protein atoms resident in shared memory per launch (32 B each)
 constexpr float kCut2 = 144.0f;     // 12 A cutoff, squared (const.ml:12-14)
 constexpr float kMinR2 = 1e-4f;     // (0.01 A)^2, Math.non_zero_dist (math.ml:58-62)
 
+// Coordinates are carried as unevaluated float pairs hi + lo (hi = fl(v),
+// lo = fl(v - hi)), so a pair difference (x_hi - p_hi) + (x_lo - p_lo) is
+// accurate to about one float ulp of |d| however close the atoms are: the
+// r^-12 term turns a coordinate error delta into a relative energy error of
+// about 12 delta / r, which plain floats (delta ~ 1e-6 A at 16 A) cannot keep
+// below 1e-5 for clashing contacts.
+//
 // Protein in HBM: atoms sorted by UFF type so that the pair parameters are
 // constant over each run; (x, y, z) are relative to the frame origin and w is
 // K * q with K = 332.0637 / 4.
 struct DevProtein {
-  const float4* atoms;    // [P]
+  const float4* atoms;    // [P][2]: (x_hi, y_hi, z_hi, K q), (x_lo, y_lo, z_lo, 0)
   const uint8_t* type;    // [P] type index, for the plain kernel
   const int* runs;        // [2 * kNTypes + 1]: run_start[nruns + 1], then run_type[nruns]
   int P;
@@ -35,7 +42,8 @@ struct PairTable {
 // Ligand topology and reference conformer in HBM.
 struct DevLigand {
   int L, nrb, npairs;
-  const float4* ref;        // [L] (x, y, z, q) centred conformer
+  const float4* ref;        // [L] (x, y, z, q) centred conformer, rounded to float
+  const double* ref64;      // [L][3] the same conformer in double
   const int* type;          // [L] type index
   const float* q;           // [L] partial charge
   const int2* bonds;        // [nrb] (left, right) rotation axis
@@ -50,7 +58,7 @@ struct DevLigand {
 // Per-pose work buffers, pose-major so the warp-per-pose kernels read them
 // contiguously.  C = protein chunks per pose.
 struct Scratch {
-  float4* X;       // [B][L] posed coordinates in the device frame
+  float4* X;       // [B][L][2] posed coordinates in the device frame, hi then lo
   double* Epart;   // [B][C][L] inter energy partial per chunk and ligand atom
   float4* Gpart;   // [B][C][L] dE/dX partial per chunk and ligand atom
   double* Eintra;  // [B]
@@ -122,6 +130,11 @@ __device__ __forceinline__ float warp_max(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
+}
+
+// pair difference a - b of two hi/lo coordinate pairs
+__device__ __forceinline__ float split_diff(float ah, float al, float bh, float bl) {
+  return (ah - bh) + (al - bl);
 }
 
 // One UFF nonbonded pair, FP32.  d = ligand - partner.  FORM 0: shifted by
