@@ -227,6 +227,33 @@ int upload_ligand(mmo_ctx* ctx) {
     }
   std::vector<int2> bonds(std::max(nrb, 1));
   for (int t = 0; t < nrb; ++t) bonds[t] = make_int2(ctx->lbonds[2 * t], ctx->lbonds[2 * t + 1]);
+  // nested groups: every two groups nested or disjoint; the axis of an inner
+  // group inside its outer group or on the outer axis; no axis atom of one of
+  // two disjoint groups inside the other
+  auto in = [&](int t, int a) { return (gmask[(size_t)t * kSlots + (a >> 5)] >> (a & 31)) & 1u; };
+  auto subset = [&](int t, int u) {  // G_t subset of G_u
+    for (int w = 0; w < kSlots; ++w)
+      if (gmask[(size_t)t * kSlots + w] & ~gmask[(size_t)u * kSlots + w]) return false;
+    return true;
+  };
+  auto disjoint = [&](int t, int u) {
+    for (int w = 0; w < kSlots; ++w)
+      if (gmask[(size_t)t * kSlots + w] & gmask[(size_t)u * kSlots + w]) return false;
+    return true;
+  };
+  bool nested = true;
+  for (int t = 0; t < nrb && nested; ++t)
+    for (int u = 0; u < nrb && nested; ++u) {
+      if (t == u) continue;
+      const int ul = bonds[u].x, ur = bonds[u].y, tl = bonds[t].x, tr = bonds[t].y;
+      if (disjoint(t, u)) {
+        nested = !in(t, ul) && !in(t, ur);
+      } else if (subset(u, t)) {
+        nested = (in(t, ul) || ul == tl || ul == tr) && (in(t, ur) || ur == tl || ur == tr);
+      } else if (!subset(t, u)) {
+        nested = false;
+      }
+    }
   const int np = (int)pij.size();
   // one blob: sizes first, then copy
   size_t off = 0;
@@ -237,6 +264,7 @@ int upload_ligand(mmo_ctx* ctx) {
     L.L = n;
     L.nrb = nrb;
     L.npairs = np;
+    L.nested = nested ? 1 : 0;
     L.ref = align_ptr<float4>(b, off, n);
     L.ref64 = align_ptr<double>(b, off, 3 * (size_t)n);
     L.type = align_ptr<int>(b, off, n);

@@ -204,8 +204,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     const double3 pl = fetchd(zx, zy, zz, bd.x);
     const double3 pr = fetchd(zx, zy, zz, bd.y);
     const double ax = pr.x - pl.x, ay = pr.y - pl.y, az = pr.z - pl.z;
-    const double len = sqrt(ax * ax + ay * ay + az * az);
-    const double ux = ax / len, uy = ay / len, uz = az / len;
+    const double inv = rnorm3d(ax, ay, az);
+    const double ux = ax * inv, uy = ay * inv, uz = az * inv;
     double sn, cs;
     ang.get(3 + t, sn, cs);
     const double o = 1.0 - cs;
@@ -302,6 +302,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
   __shared__ float4 sxh[kWarpsPerBlock][kMaxLig];
   __shared__ float4 sxl[kWarpsPerBlock][kMaxLig];
   __shared__ TorsRec srec[kWarpsPerBlock][kMaxTors];
+  __shared__ float4 saxis[kWarpsPerBlock][2 * kMaxTors];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int b = blockIdx.x * kWarpsPerBlock + wib;
   if (b >= io.B) return;
@@ -346,7 +347,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
   const float3 c = RECENTER ? centroid(lig, lane, zx, zy, zz) : make_float3(0.f, 0.f, 0.f);
   float R[9], cs[6];
   rot_xyz(dof, R, cs);
-  if (flags & kFlagIntra) {
+  const bool intra = flags & kFlagIntra;
+  if (intra) {
     // intra-ligand gradient at the stored hi/lo posed coordinates
 #pragma unroll
     for (int s = 0; s < kSlots; ++s) {
@@ -357,6 +359,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       }
     }
     __syncwarp();
+  }
+  if (intra && !lig.nested) {
+    // general groups: intra forces per atom, through the full reverse pass
 #pragma unroll
     for (int s = 0; s < kSlots; ++s) {
       const int a = lane + 32 * s;
@@ -374,6 +379,57 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         }
       }
     }
+  }
+  // nested groups: dE_intra/dtau_t = sum over interacting pairs with exactly
+  // one atom in group t of (dE/dX_moving) . (w_t x (X_moving - C_t)), w_t and
+  // C_t the final axis of bond t; the term adds nothing to the rigid DOFs.
+  // Keeping the large, cancelling intra forces out of the per-atom sums keeps
+  // the FP32 reverse pass accurate.
+  float dti[kMaxTors];
+#pragma unroll
+  for (int t = 0; t < kMaxTors; ++t) dti[t] = 0.f;
+  if (intra && lig.nested && lig.nrb > 0) {
+    if (lane < lig.nrb) {
+      const int2 bd = lig.bonds[lane];
+      const float4 rh = sxh[wib][bd.y], rl = sxl[wib][bd.y];
+      const float4 lh = sxh[wib][bd.x], ll = sxl[wib][bd.x];
+      const float ax = split_diff(rh.x, rl.x, lh.x, ll.x), ay = split_diff(rh.y, rl.y, lh.y, ll.y),
+                  az = split_diff(rh.z, rl.z, lh.z, ll.z);
+      const float inv = rsqrtf(ax * ax + ay * ay + az * az);
+      saxis[wib][lane] = make_float4(ax * inv, ay * inv, az * inv, 0.f);
+      saxis[wib][kMaxTors + lane] = rh;
+    }
+    __syncwarp();
+    for (int p = lane; p < lig.npairs; p += 32) {
+      const int2 ij = lig.pair_ij[p];
+      const float4 par = lig.pair_par[p];
+      const float4 ih = sxh[wib][ij.x], il = sxl[wib][ij.x];
+      const float4 jh = sxh[wib][ij.y], jl = sxl[wib][ij.y];
+      const float dx = split_diff(ih.x, il.x, jh.x, jl.x);
+      const float dy = split_diff(ih.y, il.y, jh.y, jl.y);
+      const float dz = split_diff(ih.z, il.z, jh.z, jl.z);
+      const float g = uff_pair_g<DIEL, IFORM>(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), par.x, par.y,
+                                              par.z);
+#pragma unroll
+      for (int t = 0; t < kMaxTors; ++t) {
+        if (t < lig.nrb) {
+          const bool in_i = (lig.gmask[t * kSlots + (ij.x >> 5)] >> (ij.x & 31)) & 1u;
+          const bool in_j = (lig.gmask[t * kSlots + (ij.y >> 5)] >> (ij.y & 31)) & 1u;
+          if (in_i != in_j) {
+            const float4 w = saxis[wib][t], cc = saxis[wib][kMaxTors + t];
+            const float4 m = in_i ? ih : jh;
+            const float lx = m.x - cc.x, ly = m.y - cc.y, lz = m.z - cc.z;
+            // d . (w x l)
+            const float v = dx * (w.y * lz - w.z * ly) + dy * (w.z * lx - w.x * lz) +
+                            dz * (w.x * ly - w.y * lx);
+            dti[t] = fmaf(in_i ? g : -g, v, dti[t]);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < kMaxTors; ++t)
+      if (t < lig.nrb) dti[t] = warp_sum(dti[t]);
   }
   // rigid map: dE/dt = sum G; dE/dR_kl = sum_i G_ik Yc_il
   float red[12];
@@ -523,7 +579,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
           az[s] -= daz;
         }
     }
-    if (lane == 0) grad[6 + t] = q[0];
+    if (lane == 0) {
+      float intra_t = 0.f;
+#pragma unroll
+      for (int k = 0; k < kMaxTors; ++k)
+        if (k == t) intra_t = dti[k];
+      grad[6 + t] = q[0] + intra_t;
+    }
   }
 }
 

@@ -42,6 +42,13 @@ struct PairTable {
 // Ligand topology and reference conformer in HBM.
 struct DevLigand {
   int L, nrb, npairs;
+  // 1 when the rotation groups are nested or disjoint with each axis moving
+  // rigidly with the groups that contain it (rotatable bonds that are
+  // bridges, groups on one side: mol_graph.ml:126-192).  Then a torsion turns
+  // its group rigidly about its final axis, and the intra-ligand term (which
+  // is rigid-invariant) enters the gradient only through pairs that straddle
+  // a group boundary.
+  int nested;
   const float4* ref;        // [L] (x, y, z, q) centred conformer, rounded to float
   const double* ref64;      // [L][3] the same conformer in double
   const int* type;          // [L] type index
@@ -172,6 +179,28 @@ __device__ __forceinline__ void uff_pair(float dx, float dy, float dz, float x2,
     gy = fmaf(g, dy, gy);
     gz = fmaf(g, dz, gz);
   }
+}
+
+// The scalar g of one pair's gradient, dE_pair/dd = g d (same terms as uff_pair).
+template <int DIEL, int FORM>
+__device__ __forceinline__ float uff_pair_g(float r2, float x2, float D, float qq) {
+  const float r2c = fmaxf(r2, kMinR2);
+  const float ir = rsqrtf(r2c);
+  const float ir2 = ir * ir;
+  const float p2 = x2 * ir2;
+  const float p6 = p2 * p2 * p2;
+  const float Dp6 = D * p6;
+  const float el = DIEL == 0 ? qq * ir : qq * ir2;
+  const float e = Dp6 * (p6 - 2.0f) + el;
+  float s = 1.0f, w = 1.0f;
+  if (FORM == 0) {
+    s = fmaxf(fmaf(r2c, -1.0f / 144.0f, 1.0f), 0.0f);
+    w = s * s;
+  }
+  const float t = fmaf(-12.0f, Dp6 * (p6 - 1.0f), DIEL == 0 ? -el : -2.0f * el);
+  float g = w * t * ir2;
+  if (FORM == 0) g = fmaf(s * (-1.0f / 36.0f), e, g);
+  return r2 < kMinR2 ? 0.0f : g;
 }
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
