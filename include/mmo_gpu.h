@@ -115,6 +115,26 @@ int mmo_score_poses(mmo_ctx* ctx, int B, const float* dofs, int flags, double* E
 int mmo_score_poses_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E,
                            float* d_grad, int* d_status, void* stream);
 
+/* Allocation-free variant of mmo_score_poses_device (no counterpart in the
+ * reference).  For callers that cannot allocate device memory while they
+ * score: code that runs inside a CUDA stream capture, real-time loops that may
+ * not stall on the allocator, and hosts whose device memory is owned by
+ * another allocator (a framework's caching allocator or a fixed arena).  The
+ * caller passes every input and output as device pointers; the call's work
+ * buffers come from a static 32 MiB device array that every GPU loading this
+ * library holds until the process exits, so this function calls no cudaMalloc
+ * or cudaFree.  A call needs 32*B*L + 8*B bytes plus 8*B*L (24*B*L with
+ * MMO_F_GRAD) per protein chunk; a batch that does not fit with one chunk
+ * per shared-memory slice of the protein is rejected with MMO_EINVAL and a
+ * message naming the sizes (4,096 poses of a 48-atom ligand fit, with the
+ * gradient).  The first call on a device looks up the array's device address
+ * with that device current; make that first call before any stream capture.
+ * All calls share the one array, so calls that overlap on the GPU (other
+ * streams, other contexts on the same device) race: serialise them on one
+ * stream.  Device-side wait timeouts are reported by mmo_sync. */
+int mmo_score_poses_noalloc(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E,
+                            float* d_grad, int* d_status, void* stream);
+
 /* Wait for `stream` (a cudaStream_t; NULL is the legacy default stream) and
  * report, then clear, the device-side error flag of the device-pointer calls
  * (MMO_ETIMEOUT). */

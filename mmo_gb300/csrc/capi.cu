@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <numeric>
 #include <string>
@@ -821,3 +822,122 @@ int mmo_fp32_fma_peak(mmo_ctx* ctx, double* tflops, double* ms_out) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free batched scoring (mmo_score_poses_noalloc).
+//
+// The work buffers of a call (posed coordinates, per-chunk energy and
+// gradient partials, intra-ligand energies) live in one file-scope device
+// array of kNoAllocBytes instead of buffers that grow with cudaMalloc.  Every
+// GPU that loads this library holds the array until the process exits.  In
+// host code the name g_noalloc_scratch is only a host-side stand-in for the
+// array, not a device address, so the kernels get the address that
+// cudaGetSymbolAddress returns for the current device.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocBytes = size_t(32) << 20;  // 32 MiB per GPU
+constexpr int kNoAllocDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kNoAllocDevices] = {};
+
+// Device address of the static scratch on `device`, looked up once per device
+// with that device current.
+int noalloc_scratch(mmo_ctx* ctx, int device, unsigned char** out) {
+  if (device < 0 || device >= kNoAllocDevices)
+    return fail(ctx, MMO_EINVAL, "mmo_score_poses_noalloc: device %d above %d", device,
+                kNoAllocDevices - 1);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void* p = nullptr;
+    MMO_CK(cudaSetDevice(device), "set device");
+    MMO_CK(cudaGetSymbolAddress(&p, g_noalloc_scratch), "static scratch address");
+    g_noalloc_ptr[device] = p;
+  }
+  *out = static_cast<unsigned char*>(g_noalloc_ptr[device]);
+  return MMO_OK;
+}
+
+}  // namespace
+
+extern "C" int mmo_score_poses_noalloc(mmo_ctx* ctx, int B, const float* d_dofs, int flags,
+                                       double* d_E, float* d_grad, int* d_status, void* stream) {
+  if (!ctx) return MMO_EINVAL;
+  if (!ctx->has_lig) return fail(ctx, MMO_ESTATE, "no ligand: call mmo_set_ligand first");
+  if ((flags & MMO_F_INTER) && ctx->prot.P <= 0)
+    return fail(ctx, MMO_ESTATE, "no protein: call mmo_set_protein first");
+  if (B < 0 || (B > 0 && (!d_dofs || !d_E || !d_status)))
+    return fail(ctx, MMO_EINVAL, "mmo_score_poses_noalloc: bad batch arguments");
+  if ((flags & MMO_F_GRAD) && !d_grad)
+    return fail(ctx, MMO_EINVAL, "mmo_score_poses_noalloc: MMO_F_GRAD needs grad_out");
+  if (B == 0) return MMO_OK;
+  const bool grad = flags & MMO_F_GRAD;
+  const bool inter = (flags & MMO_F_INTER) && ctx->prot.P > 0;
+  const int L = ctx->lig.L;
+  // scratch layout: X[B][L][2] float4 | Eintra[B] | Epart[B][C][L] | Gpart[B][C][L]
+  const size_t fixed = 256 * 4 + sizeof(float4) * 2 * (size_t)B * L + sizeof(double) * (size_t)B;
+  const size_t per_chunk = (sizeof(double) + (grad ? sizeof(float4) : 0)) * (size_t)B * L;
+  const int nslices = inter ? (ctx->prot.P + kSliceAtoms - 1) / kSliceAtoms : 1;
+  const long c_fit = fixed < kNoAllocBytes ? (long)((kNoAllocBytes - fixed) / per_chunk) : 0;
+  if (c_fit < nslices) {
+    const size_t need = fixed + per_chunk * nslices;
+    return fail(ctx, MMO_EINVAL,
+                "mmo_score_poses_noalloc: %d poses of %d atoms need %zu bytes of scratch, above "
+                "the %zu-byte static scratch; score fewer poses per call",
+                B, L, need, kNoAllocBytes);
+  }
+  unsigned char* base = nullptr;
+  int r = noalloc_scratch(ctx, ctx->device, &base);
+  if (r) return r;
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  PairPlan plan{};
+  int C = 1;
+  if (inter) {
+    plan = plan_for(ctx, B, grad);
+    const int c_slice = std::max(1, std::min(plan.C / nslices, (int)(c_fit / nslices)));
+    C = c_slice * nslices;
+    const long npb = (B + 32L * plan.kp - 1) / (32L * plan.kp);
+    const long need = (npb * L * c_slice + plan.threads / 32 - 1) / (plan.threads / 32);
+    plan.C = C;
+    plan.blocks = (int)std::max(1L, std::min((long)plan.blocks, need));
+  }
+  size_t off = 0;
+  Scratch s{};
+  s.X = reinterpret_cast<float4*>(base + take(off, sizeof(float4) * 2 * (size_t)B * L));
+  off = (off + 255) & ~size_t(255);
+  s.Eintra = reinterpret_cast<double*>(base + take(off, sizeof(double) * (size_t)B));
+  off = (off + 255) & ~size_t(255);
+  s.Epart = reinterpret_cast<double*>(base + take(off, sizeof(double) * (size_t)B * C * L));
+  off = (off + 255) & ~size_t(255);
+  s.Gpart = grad ? reinterpret_cast<float4*>(base + take(off, sizeof(float4) * (size_t)B * C * L))
+                 : nullptr;
+  s.C = C;
+  if (off > kNoAllocBytes) return fail(ctx, MMO_EINVAL, "mmo_score_poses_noalloc: layout overflow");
+  PoseIO io{};
+  io.dofs = d_dofs;
+  io.E = d_E;
+  io.grad = grad ? d_grad : nullptr;
+  io.status = d_status;
+  io.err = ctx->d_err;
+  io.zero_err = 0;
+  io.B = B;
+  io.ox = ctx->origin_f[0];
+  io.oy = ctx->origin_f[1];
+  io.oz = ctx->origin_f[2];
+  int fl = flags & (kFlagInter | kFlagIntra | kFlagGrad | kFlagRecenter);
+  if (!inter) fl &= ~kFlagInter;
+  // every region a kernel reads is written first in this call: X and Eintra
+  // by the rebuild, each (pose, chunk, atom) partial by the pair sweep
+  MMO_CK(launch_rebuild(ctx->lig, io, s, fl, ctx->ph.intra_form, ctx->ph.dielectric, st),
+         "rebuild kernel");
+  if (inter)
+    MMO_CK(launch_pairs_batched(ctx->prot, ctx->tab, ctx->lig, s, B, fl, ctx->ph, plan,
+                                ctx->d_err, st),
+           "batched pair kernel");
+  MMO_CK(launch_finish(ctx->lig, io, s, fl, ctx->ph, st), "finish kernel");
+  return MMO_OK;
+}
