@@ -82,6 +82,7 @@ struct mmo_ctx {
   std::string err;
   Physics ph{0, 0, 0, 0};
   PairTable tab{};
+  PairTable4 tab4{};
   int tile_kp = 0, tile_threads = 0, tile_chunks = 0;
   // last launch plan and the inputs it was made for
   PairPlan plan{};
@@ -103,7 +104,7 @@ struct mmo_ctx {
 
   // scratch
   Scratch scr{};
-  size_t capX = 0, capE = 0, capG = 0, capI = 0;
+  size_t capX = 0, capE = 0, capG = 0, capI = 0, capY = 0, capR = 0;
   int* d_err = nullptr;
 
   // stage timing (mmo_set_profiling)
@@ -148,6 +149,9 @@ void rebuild_table(mmo_ctx* ctx) {
       double x2, d;
       pair_xd(ctx->ph.mixing, a, b, &x2, &d);
       ctx->tab.xd[a * kNTypes + b] = make_float2((float)x2, (float)d);
+      // packed sweep: (X / r^2)^3 = D (x / r)^6 with X = D^(1/3) x^2
+      ctx->tab4.v[a * kNTypes + b] = make_float4(
+          (float)(std::cbrt(d) * x2), d > 0.0 ? (float)(1.0 / d) : 0.f, (float)x2, (float)d);
     }
 }
 
@@ -184,9 +188,16 @@ int ensure_scratch(mmo_ctx* ctx, int B, int L, int C, bool grad) {
   if ((r = grow(ctx, (void**)&ctx->scr.Epart, &ctx->capE, sizeof(double) * n, "Epart"))) return r;
   if (grad && (r = grow(ctx, (void**)&ctx->scr.Gpart, &ctx->capG, sizeof(float4) * n, "Gpart")))
     return r;
-  if ((r = grow(ctx, (void**)&ctx->scr.Eintra, &ctx->capI, sizeof(double) * (size_t)B,
-                "Eintra")))
-    return r;
+  if (grad) {
+    const size_t nrb = std::max(1, ctx->lig.nrb);
+    if ((r = grow(ctx, (void**)&ctx->scr.Y, &ctx->capY, sizeof(float4) * (size_t)B * L, "Y")))
+      return r;
+    if ((r = grow(ctx, (void**)&ctx->scr.rec, &ctx->capR, sizeof(float4) * 3 * (size_t)B * nrb,
+                  "torsion records")))
+      return r;
+    if ((r = grow(ctx, (void**)&ctx->scr.cen, &ctx->capI, sizeof(float4) * (size_t)B, "centroids")))
+      return r;
+  }
   ctx->scr.C = C;
   return MMO_OK;
 }
@@ -274,6 +285,9 @@ int upload_ligand(mmo_ctx* ctx) {
     L.gmask = align_ptr<uint32_t>(b, off, gmask.size());
     L.pair_ij = align_ptr<int2>(b, off, std::max(np, 1));
     L.pair_par = align_ptr<float4>(b, off, std::max(np, 1));
+    L.amask = align_ptr<uint32_t>(b, off, n);
+    L.grp_off = align_ptr<int>(b, off, nrb + 1);
+    L.grp_atoms = align_ptr<int>(b, off, std::max((int)ctx->lgatoms.size(), 1));
     L.nb_off = align_ptr<int>(b, off, n + 1);
     L.nb_idx = align_ptr<int>(b, off, std::max((int)nb_idx.size(), 1));
     L.nb_par = align_ptr<float4>(b, off, std::max((int)nb_par.size(), 1));
@@ -283,6 +297,12 @@ int upload_ligand(mmo_ctx* ctx) {
   const size_t bytes = off;
   std::vector<char> host(bytes, 0);
   DevLigand H = layout(host.data());
+  for (int t = 0; t < nrb; ++t)
+    for (int k = ctx->lgoff[t]; k < ctx->lgoff[t + 1]; ++k)
+      const_cast<uint32_t*>(H.amask)[ctx->lgatoms[k]] |= 1u << t;
+  memcpy((void*)H.grp_off, ctx->lgoff.data(), sizeof(int) * (nrb + 1));
+  if (!ctx->lgatoms.empty())
+    memcpy((void*)H.grp_atoms, ctx->lgatoms.data(), sizeof(int) * ctx->lgatoms.size());
   memcpy((void*)H.ref, ref.data(), sizeof(float4) * n);
   for (int i = 0; i < n; ++i) {
     double* r64 = const_cast<double*>(H.ref64) + 3 * i;
@@ -327,12 +347,13 @@ PairPlan plan_for(mmo_ctx* ctx, int B, bool grad) {
 
 PairPlan make_plan(mmo_ctx* ctx, int B, bool grad) {
   PairPlan p{};
-  p.kp = ctx->tile_kp ? ctx->tile_kp : (B >= 4096 ? 4 : (B >= 256 ? 2 : 1));
+  p.kp = ctx->tile_kp ? ctx->tile_kp : (B >= 4096 ? 4 : 2);
   p.threads = ctx->tile_threads ? ctx->tile_threads : 512;
+  if (p.kp >= 8) p.threads = 256;  // 8 poses per lane need the register budget of 256 threads
   const int P = ctx->prot.P, L = ctx->lig.L;
   const int nslices = (P + kSliceAtoms - 1) / kSliceAtoms;
   const int slice_len = (P + nslices - 1) / nslices;
-  const int smem = slice_len * 32;
+  const int smem = slice_len * 64;
   int bps = pairs_batched_max_blocks(p.kp, p.threads, grad, ctx->ph, smem);
   if (bps < 1) bps = 1;
   p.blocks = ctx->sms * bps;
@@ -406,8 +427,7 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
   if (!inter) fl &= ~kFlagInter;
   const bool prof = ctx->profiling;
   if (prof) MMO_CK(cudaEventRecord(ctx->ev[0], st), "event");
-  MMO_CK(launch_rebuild(ctx->lig, io, ctx->scr, fl, ctx->ph.intra_form, ctx->ph.dielectric, st),
-         "rebuild kernel");
+  MMO_CK(launch_rebuild(ctx->lig, io, ctx->scr, fl, st), "rebuild kernel");
   if (prof) MMO_CK(cudaEventRecord(ctx->ev[1], st), "event");
   if (inter) {
     if (B == 1) {
@@ -415,7 +435,7 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
                                 ctx->scr.Epart, ctx->scr.Gpart, grad, ctx->ph, st),
              "plain pair kernel");
     } else {
-      MMO_CK(launch_pairs_batched(ctx->prot, ctx->tab, ctx->lig, ctx->scr, B, fl, ctx->ph, plan,
+      MMO_CK(launch_pairs_batched(ctx->prot, ctx->tab4, ctx->lig, ctx->scr, B, fl, ctx->ph, plan,
                                   d_err, st),
              "batched pair kernel");
     }
@@ -472,7 +492,9 @@ int mmo_ctx_destroy(mmo_ctx* ctx) {
   cudaFree(ctx->scr.X);
   cudaFree(ctx->scr.Epart);
   cudaFree(ctx->scr.Gpart);
-  cudaFree(ctx->scr.Eintra);
+  cudaFree(ctx->scr.Y);
+  cudaFree(ctx->scr.rec);
+  cudaFree(ctx->scr.cen);
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
   cudaFree(ctx->d_err);
@@ -497,9 +519,9 @@ int mmo_set_physics(mmo_ctx* ctx, int dielectric, int mixing, int inter_form, in
 
 int mmo_set_tiles(mmo_ctx* ctx, int kp, int threads, int chunks) {
   if (!ctx) return MMO_EINVAL;
-  if (!(kp == 0 || kp == 1 || kp == 2 || kp == 4) ||
+  if (!(kp == 0 || kp == 2 || kp == 4 || kp == 8) ||
       !(threads == 0 || threads == 256 || threads == 512) || chunks < 0 || chunks > 4096)
-    return fail(ctx, MMO_EINVAL, "tiles: poses_per_lane in {0,1,2,4}, threads in {0,256,512}");
+    return fail(ctx, MMO_EINVAL, "tiles: poses_per_lane in {0,2,4,8}, threads in {0,256,512}");
   ctx->tile_kp = kp;
   ctx->tile_threads = threads;
   ctx->tile_chunks = chunks;
@@ -537,7 +559,7 @@ int mmo_set_protein(mmo_ctx* ctx, int n, const double* xs, const double* ys, con
   std::vector<int> idx(n);
   std::iota(idx.begin(), idx.end(), 0);
   std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return type[a] < type[b]; });
-  std::vector<float4> atoms(2 * (size_t)std::max(n, 1));
+  std::vector<float4> atoms(2 * (size_t)std::max(n, 1)), atoms4(4 * (size_t)std::max(n, 1));
   std::vector<uint8_t> ptype(std::max(n, 16), 0);
   std::vector<int> rstart, rtype;
   DevProtein P{};
@@ -546,6 +568,11 @@ int mmo_set_protein(mmo_ctx* ctx, int n, const double* xs, const double* ys, con
     const int i = idx[k];
     split_store(&atoms[2 * (size_t)k], xs[i] - (double)of[0], ys[i] - (double)of[1],
                 zs[i] - (double)of[2], (float)(kElec * q[i]));
+    const float4 h = atoms[2 * (size_t)k], l = atoms[2 * (size_t)k + 1];
+    atoms4[4 * (size_t)k] = make_float4(-h.x, -h.x, -h.y, -h.y);
+    atoms4[4 * (size_t)k + 1] = make_float4(-h.z, -h.z, h.w, h.w);
+    atoms4[4 * (size_t)k + 2] = make_float4(-l.x, -l.x, -l.y, -l.y);
+    atoms4[4 * (size_t)k + 3] = make_float4(-l.z, -l.z, 0.f, 0.f);
     ptype[k] = (uint8_t)type[i];
     if (k == 0 || type[i] != type[idx[k - 1]]) {
       rstart.push_back(k);
@@ -563,15 +590,18 @@ int mmo_set_protein(mmo_ctx* ctx, int n, const double* xs, const double* ys, con
   ctx->d_prot = nullptr;
   size_t off = 0;
   const size_t o_atoms = take(off, sizeof(float4) * atoms.size());
+  const size_t o_atoms4 = take(off, sizeof(float4) * atoms4.size());
   const size_t o_type = take(off, ptype.size());
   const size_t o_runs = take(off, sizeof(int) * runs.size());
   std::vector<char> blob(off, 0);
   memcpy(blob.data() + o_atoms, atoms.data(), sizeof(float4) * atoms.size());
+  memcpy(blob.data() + o_atoms4, atoms4.data(), sizeof(float4) * atoms4.size());
   memcpy(blob.data() + o_type, ptype.data(), ptype.size());
   memcpy(blob.data() + o_runs, runs.data(), sizeof(int) * runs.size());
   MMO_CK(cudaMalloc(&ctx->d_prot, off), "protein");
   MMO_CK(cudaMemcpy(ctx->d_prot, blob.data(), off, cudaMemcpyHostToDevice), "protein upload");
   P.atoms = reinterpret_cast<const float4*>((char*)ctx->d_prot + o_atoms);
+  P.atoms4 = reinterpret_cast<const float4*>((char*)ctx->d_prot + o_atoms4);
   P.type = reinterpret_cast<const uint8_t*>((char*)ctx->d_prot + o_type);
   P.runs = reinterpret_cast<const int*>((char*)ctx->d_prot + o_runs);
   ctx->prot = P;
@@ -877,8 +907,11 @@ extern "C" int mmo_score_poses_noalloc(mmo_ctx* ctx, int B, const float* d_dofs,
   const bool grad = flags & MMO_F_GRAD;
   const bool inter = (flags & MMO_F_INTER) && ctx->prot.P > 0;
   const int L = ctx->lig.L;
-  // scratch layout: X[B][L][2] float4 | Eintra[B] | Epart[B][C][L] | Gpart[B][C][L]
-  const size_t fixed = 256 * 4 + sizeof(float4) * 2 * (size_t)B * L + sizeof(double) * (size_t)B;
+  // scratch layout: X[B][L][2] | (gradient: Y[B][L] | rec[B][nrb][3] | cen[B]) |
+  // Epart[B][C][L] | (gradient: Gpart[B][C][L])
+  const size_t nrb = std::max(1, ctx->lig.nrb);
+  const size_t fixed = 256 * 6 + sizeof(float4) * 2 * (size_t)B * L +
+                       (grad ? sizeof(float4) * ((size_t)B * L + 3 * (size_t)B * nrb + B) : 0);
   const size_t per_chunk = (sizeof(double) + (grad ? sizeof(float4) : 0)) * (size_t)B * L;
   const int nslices = inter ? (ctx->prot.P + kSliceAtoms - 1) / kSliceAtoms : 1;
   const long c_fit = fixed < kNoAllocBytes ? (long)((kNoAllocBytes - fixed) / per_chunk) : 0;
@@ -909,8 +942,14 @@ extern "C" int mmo_score_poses_noalloc(mmo_ctx* ctx, int B, const float* d_dofs,
   Scratch s{};
   s.X = reinterpret_cast<float4*>(base + take(off, sizeof(float4) * 2 * (size_t)B * L));
   off = (off + 255) & ~size_t(255);
-  s.Eintra = reinterpret_cast<double*>(base + take(off, sizeof(double) * (size_t)B));
-  off = (off + 255) & ~size_t(255);
+  if (grad) {
+    s.Y = reinterpret_cast<float4*>(base + take(off, sizeof(float4) * (size_t)B * L));
+    off = (off + 255) & ~size_t(255);
+    s.rec = reinterpret_cast<float4*>(base + take(off, sizeof(float4) * 3 * (size_t)B * nrb));
+    off = (off + 255) & ~size_t(255);
+    s.cen = reinterpret_cast<float4*>(base + take(off, sizeof(float4) * (size_t)B));
+    off = (off + 255) & ~size_t(255);
+  }
   s.Epart = reinterpret_cast<double*>(base + take(off, sizeof(double) * (size_t)B * C * L));
   off = (off + 255) & ~size_t(255);
   s.Gpart = grad ? reinterpret_cast<float4*>(base + take(off, sizeof(float4) * (size_t)B * C * L))
@@ -930,12 +969,12 @@ extern "C" int mmo_score_poses_noalloc(mmo_ctx* ctx, int B, const float* d_dofs,
   io.oz = ctx->origin_f[2];
   int fl = flags & (kFlagInter | kFlagIntra | kFlagGrad | kFlagRecenter);
   if (!inter) fl &= ~kFlagInter;
-  // every region a kernel reads is written first in this call: X and Eintra
-  // by the rebuild, each (pose, chunk, atom) partial by the pair sweep
-  MMO_CK(launch_rebuild(ctx->lig, io, s, fl, ctx->ph.intra_form, ctx->ph.dielectric, st),
-         "rebuild kernel");
+  // every region a kernel reads is written first in this call: X, Y, the
+  // torsion records and the centroids by the rebuild, each (pose, chunk,
+  // atom) partial by the pair sweep
+  MMO_CK(launch_rebuild(ctx->lig, io, s, fl, st), "rebuild kernel");
   if (inter)
-    MMO_CK(launch_pairs_batched(ctx->prot, ctx->tab, ctx->lig, s, B, fl, ctx->ph, plan,
+    MMO_CK(launch_pairs_batched(ctx->prot, ctx->tab4, ctx->lig, s, B, fl, ctx->ph, plan,
                                 ctx->d_err, st),
            "batched pair kernel");
   MMO_CK(launch_finish(ctx->lig, io, s, fl, ctx->ph, st), "finish kernel");

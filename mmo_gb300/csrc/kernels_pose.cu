@@ -1,42 +1,126 @@
-// kernels_pose.cu -- warp-per-pose kernels: pose rebuild (+ intra-ligand
-// energy) before the pair sweep, and the finishing pass after it (energy
-// reduction, intra-ligand gradient, reverse pass through the rigid map and
-// the torsion chain).
+// kernels_pose.cu -- the per-pose kernels around the pair sweep.
 //
-// Pose map (UnixJunkie/MMO): torsions applied in bond order, each rotating its
-// group about the current (left, right) axis (src/optim.ml:68-71,
-// src/mol.ml:610-631); enclosing-radius check (src/mol.ml:576-591); then
-// x = Rz(g) Ry(b) Rx(a) y + t (src/optim.ml:77-80, src/rot.ml:52-66), or with
-// the centroid removed first for the Monte Carlo map (src/mol.ml:705-710).
+// k_rebuild (one thread per pose, FP64): the pose map of UnixJunkie/MMO --
+// torsions applied in bond order, each rotating its group about the current
+// (left, right) axis (src/optim.ml:68-71, src/mol.ml:610-631), the
+// enclosing-radius check (src/mol.ml:576-591), then x = Rz(g) Ry(b) Rx(a) y + t
+// (src/optim.ml:77-80, src/rot.ml:52-66), or with the centroid removed first
+// for the Monte Carlo map (src/mol.ml:705-710).  All poses of a block share the
+// ligand, so the threads of a warp walk the same atom indices in lockstep and
+// keep their coordinates in shared memory laid out [atom][thread].
+//
+// k_finish (one warp per pose, lanes over atoms): the FP64 energy of the pose
+// (inter partials + the intra-ligand term of src/mol.ml:881-903) and, with the
+// gradient, the reverse pass through the rigid map and the torsion chain.
 #include "mmo_internal.cuh"
 
 namespace mmo {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kWarpsPerBlock = 4;
+constexpr int kRebuildThreads = 32;   // poses per rebuild block
+constexpr int kWarpsPerBlock = 4;     // poses per finish block
 
-struct TorsRec {
-  float cx, cy, cz, ux, uy, uz, ilen, ct, st;
-};
-
-__device__ __forceinline__ float pick(const float (&v)[kSlots], int slot) {
-  float r = v[0];
-#pragma unroll
-  for (int s = 1; s < kSlots; ++s)
-    if (slot == s) r = v[s];
-  return r;
+// ---------------------------------------------------------------------------
+// k_rebuild
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void store_split(float4* X, double x, double y, double z) {
+  const float xh = __double2float_rn(x), yh = __double2float_rn(y), zh = __double2float_rn(z);
+  X[0] = make_float4(xh, yh, zh, 0.f);
+  X[1] = make_float4(__double2float_rn(x - (double)xh), __double2float_rn(y - (double)yh),
+                     __double2float_rn(z - (double)zh), 0.f);
 }
 
-// coordinates of atom idx, read from the lane that owns it
-__device__ __forceinline__ float3 fetch(const float (&x)[kSlots], const float (&y)[kSlots],
-                                        const float (&z)[kSlots], int idx) {
-  const int owner = idx & 31, slot = idx >> 5;
-  return make_float3(__shfl_sync(kFull, pick(x, slot), owner),
-                     __shfl_sync(kFull, pick(y, slot), owner),
-                     __shfl_sync(kFull, pick(z, slot), owner));
+template <bool RECENTER, bool RECORD>
+__global__ void __launch_bounds__(kRebuildThreads) k_rebuild(DevLigand lig, PoseIO io, Scratch scr) {
+  extern __shared__ double sz[];  // [3][L][kRebuildThreads]
+  const int tid = threadIdx.x;
+  const int b = blockIdx.x * kRebuildThreads + tid;
+  const int L = lig.L, nrb = lig.nrb, nd = 6 + nrb;
+  double* X = sz;
+  double* Yc = sz + L * kRebuildThreads;
+  double* Zc = sz + 2 * L * kRebuildThreads;
+#define AT(arr, a) arr[(a) * kRebuildThreads + tid]
+  const bool live = b < io.B;
+  const float* dof = io.dofs + (size_t)(live ? b : 0) * nd;
+  for (int a = 0; a < L; ++a) {
+    AT(X, a) = lig.ref64[3 * a];
+    AT(Yc, a) = lig.ref64[3 * a + 1];
+    AT(Zc, a) = lig.ref64[3 * a + 2];
+  }
+  for (int t = 0; t < nrb; ++t) {
+    const int2 bd = lig.bonds[t];
+    const double cx = AT(X, bd.y), cy = AT(Yc, bd.y), cz = AT(Zc, bd.y);
+    const double ax = cx - AT(X, bd.x), ay = cy - AT(Yc, bd.x), az = cz - AT(Zc, bd.x);
+    const double inv = rnorm3d(ax, ay, az);
+    const double ux = ax * inv, uy = ay * inv, uz = az * inv;
+    double sn, cs;
+    sincos((double)dof[6 + t], &sn, &cs);
+    // Rodrigues matrix of rot.ml:136-146
+    const double o = 1.0 - cs;
+    const double R0 = cs + ux * ux * o, R1 = ux * uy * o - uz * sn, R2 = ux * uz * o + uy * sn;
+    const double R3 = ux * uy * o + uz * sn, R4 = cs + uy * uy * o, R5 = uy * uz * o - ux * sn;
+    const double R6 = ux * uz * o - uy * sn, R7 = uy * uz * o + ux * sn, R8 = cs + uz * uz * o;
+    for (int k = lig.grp_off[t]; k < lig.grp_off[t + 1]; ++k) {
+      const int i = lig.grp_atoms[k];
+      const double vx = AT(X, i) - cx, vy = AT(Yc, i) - cy, vz = AT(Zc, i) - cz;
+      AT(X, i) = R0 * vx + R1 * vy + R2 * vz + cx;
+      AT(Yc, i) = R3 * vx + R4 * vy + R5 * vz + cy;
+      AT(Zc, i) = R6 * vx + R7 * vy + R8 * vz + cz;
+    }
+    if (RECORD && live) {
+      float4* r = scr.rec + ((size_t)b * nrb + t) * 3;
+      r[0] = make_float4((float)cx, (float)cy, (float)cz, (float)cs);
+      r[1] = make_float4((float)ux, (float)uy, (float)uz, (float)sn);
+      r[2] = make_float4((float)inv, 0.f, 0.f, 0.f);
+    }
+  }
+  // centroid and enclosing radius, max_i (0.01 + |c - y_i|) > 12 (mol.ml:576-591)
+  double mx = 0.0, my = 0.0, mz = 0.0;
+  for (int a = 0; a < L; ++a) {
+    mx += AT(X, a);
+    my += AT(Yc, a);
+    mz += AT(Zc, a);
+  }
+  mx /= L;
+  my /= L;
+  mz /= L;
+  double d2max = 0.0;
+  for (int a = 0; a < L; ++a) {
+    const double dx = mx - AT(X, a), dy = my - AT(Yc, a), dz = mz - AT(Zc, a);
+    d2max = fmax(d2max, dx * dx + dy * dy + dz * dz);
+  }
+  const int status = 0.01 + sqrt(d2max) > 12.0 ? kStatusTooLong : 0;
+  // rigid map
+  double sa, ca, sb, cb, sg, cg;
+  sincos((double)dof[3], &sa, &ca);
+  sincos((double)dof[4], &sb, &cb);
+  sincos((double)dof[5], &sg, &cg);
+  const double R0 = cb * cg, R1 = cg * sa * sb - ca * sg, R2 = sa * sg + ca * cg * sb;
+  const double R3 = cb * sg, R4 = ca * cg + sa * sb * sg, R5 = ca * sb * sg - cg * sa;
+  const double R6 = -sb, R7 = cb * sa, R8 = ca * cb;
+  const double tx = (double)dof[0] - (double)io.ox, ty = (double)dof[1] - (double)io.oy,
+               tz = (double)dof[2] - (double)io.oz;
+  const double ox = RECENTER ? mx : 0.0, oy = RECENTER ? my : 0.0, oz = RECENTER ? mz : 0.0;
+  if (live) {
+    for (int a = 0; a < L; ++a) {
+      const double vx = AT(X, a) - ox, vy = AT(Yc, a) - oy, vz = AT(Zc, a) - oz;
+      store_split(scr.X + ((size_t)b * L + a) * 2, R0 * vx + R1 * vy + R2 * vz + tx,
+                  R3 * vx + R4 * vy + R5 * vz + ty, R6 * vx + R7 * vy + R8 * vz + tz);
+      if (RECORD)
+        scr.Y[(size_t)b * L + a] = make_float4((float)AT(X, a), (float)AT(Yc, a),
+                                                (float)AT(Zc, a), 0.f);
+    }
+    if (RECORD) scr.cen[b] = make_float4((float)mx, (float)my, (float)mz, 0.f);
+    io.status[b] = status;
+    if (b == 0 && io.zero_err) *io.err = 0;
+  }
+#undef AT
 }
 
+// ---------------------------------------------------------------------------
+// k_finish
+// ---------------------------------------------------------------------------
 // Rodrigues matrix of rot.ml:136-146, row-major
 __device__ __forceinline__ void axis_angle(float ux, float uy, float uz, float c, float s,
                                            float (&R)[9]) {
@@ -52,279 +136,101 @@ __device__ __forceinline__ void axis_angle(float ux, float uy, float uz, float c
   R[8] = c + uz * uz * o;
 }
 
-// Rz(g) Ry(b) Rx(a) of rot.ml:52-66
-__device__ __forceinline__ void rot_xyz(const float* dof, float (&R)[9], float (&cs)[6]) {
-  float sa, ca, sb, cb, sg, cg;
-  sincosf(dof[3], &sa, &ca);
-  sincosf(dof[4], &sb, &cb);
-  sincosf(dof[5], &sg, &cg);
-  R[0] = cb * cg;
-  R[1] = cg * sa * sb - ca * sg;
-  R[2] = sa * sg + ca * cg * sb;
-  R[3] = cb * sg;
-  R[4] = ca * cg + sa * sb * sg;
-  R[5] = ca * sb * sg - cg * sa;
-  R[6] = -sb;
-  R[7] = cb * sa;
-  R[8] = ca * cb;
-  cs[0] = ca; cs[1] = sa; cs[2] = cb; cs[3] = sb; cs[4] = cg; cs[5] = sg;
+template <int DIEL, int IFORM>
+__device__ __forceinline__ float intra_pair_g(const float4* sh, const float4* sl, int i, int j,
+                                              float4 par, float& e, float& dx, float& dy,
+                                              float& dz) {
+  const float4 ih = sh[i], il = sl[i], jh = sh[j], jl = sl[j];
+  dx = split_diff(ih.x, il.x, jh.x, jl.x);
+  dy = split_diff(ih.y, il.y, jh.y, jl.y);
+  dz = split_diff(ih.z, il.z, jh.z, jl.z);
+  float g0 = 0.f, g1 = 0.f, g2 = 0.f, acc = 0.f;
+  uff_pair<false, DIEL, IFORM>(dx, dy, dz, par.x, par.y, par.z, acc, g0, g1, g2);
+  e = acc;
+  return uff_pair_g<DIEL, IFORM>(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), par.x, par.y, par.z);
 }
 
-template <bool RECORD>
-__device__ __forceinline__ void torsion_chain(const DevLigand& lig, const float* tau, int lane,
-                                              float (&zx)[kSlots], float (&zy)[kSlots],
-                                              float (&zz)[kSlots], TorsRec* rec) {
-  for (int t = 0; t < lig.nrb; ++t) {
-    const int2 bd = lig.bonds[t];
-    const float3 pl = fetch(zx, zy, zz, bd.x);
-    const float3 pr = fetch(zx, zy, zz, bd.y);
-    const float ax = pr.x - pl.x, ay = pr.y - pl.y, az = pr.z - pl.z;
-    const float len = sqrtf(ax * ax + ay * ay + az * az);
-    const float ux = ax / len, uy = ay / len, uz = az / len;
-    float sn, cs;
-    sincosf(tau[t], &sn, &cs);
-    float R[9];
-    axis_angle(ux, uy, uz, cs, sn, R);
-#pragma unroll
-    for (int s = 0; s < kSlots; ++s) {
-      if ((lig.gmask[t * kSlots + s] >> lane) & 1u) {
-        const float vx = zx[s] - pr.x, vy = zy[s] - pr.y, vz = zz[s] - pr.z;
-        zx[s] = R[0] * vx + R[1] * vy + R[2] * vz + pr.x;
-        zy[s] = R[3] * vx + R[4] * vy + R[5] * vz + pr.y;
-        zz[s] = R[6] * vx + R[7] * vy + R[8] * vz + pr.z;
-      }
-    }
-    if (RECORD && lane == 0) rec[t] = TorsRec{pr.x, pr.y, pr.z, ux, uy, uz, 1.0f / len, cs, sn};
-  }
-}
-
-__device__ __forceinline__ void load_ref(const DevLigand& lig, int lane, float (&zx)[kSlots],
-                                         float (&zy)[kSlots], float (&zz)[kSlots]) {
-#pragma unroll
-  for (int s = 0; s < kSlots; ++s) {
-    const int a = lane + 32 * s;
-    float4 r = a < lig.L ? lig.ref[a] : make_float4(0.f, 0.f, 0.f, 0.f);
-    zx[s] = r.x;
-    zy[s] = r.y;
-    zz[s] = r.z;
-  }
-}
-
-__device__ __forceinline__ float3 centroid(const DevLigand& lig, int lane, const float (&zx)[kSlots],
-                                           const float (&zy)[kSlots], const float (&zz)[kSlots]) {
-  float sx = 0.f, sy = 0.f, sz = 0.f;
-#pragma unroll
-  for (int s = 0; s < kSlots; ++s)
-    if (lane + 32 * s < lig.L) {
-      sx += zx[s];
-      sy += zy[s];
-      sz += zz[s];
-    }
-  const float inv = 1.0f / (float)lig.L;
-  return make_float3(warp_sum(sx) * inv, warp_sum(sy) * inv, warp_sum(sz) * inv);
-}
-
-// ---- FP64 pose map (k_rebuild) --------------------------------------------
-__device__ __forceinline__ double pickd(const double (&v)[kSlots], int slot) {
-  double r = v[0];
-#pragma unroll
-  for (int s = 1; s < kSlots; ++s)
-    if (slot == s) r = v[s];
-  return r;
-}
-
-__device__ __forceinline__ double3 fetchd(const double (&x)[kSlots], const double (&y)[kSlots],
-                                          const double (&z)[kSlots], int idx) {
-  const int owner = idx & 31, slot = idx >> 5;
-  return make_double3(__shfl_sync(kFull, pickd(x, slot), owner),
-                      __shfl_sync(kFull, pickd(y, slot), owner),
-                      __shfl_sync(kFull, pickd(z, slot), owner));
-}
-
-__device__ __forceinline__ double warp_maxd(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(kFull, v, o));
-  return v;
-}
-
-// sine and cosine of angle k of the pose ([a, b, g, tau_0 ...]), computed
-// once by lane (k & 31) in round (k >> 5) and read back by every lane
-struct AngleTable {
-  double s0, c0, s1, c1;
-  __device__ __forceinline__ void get(int k, double& s, double& c) const {
-    const int owner = k & 31;
-    const bool hi = k >= 32;
-    s = __shfl_sync(kFull, hi ? s1 : s0, owner);
-    c = __shfl_sync(kFull, hi ? c1 : c0, owner);
-  }
-};
-
-__device__ __forceinline__ AngleTable angle_table(const float* dof, int nrb, int lane) {
-  AngleTable t{0.0, 1.0, 0.0, 1.0};
-  const int n = 3 + nrb;
-  if (lane < n) sincos((double)dof[3 + lane], &t.s0, &t.c0);
-  if (lane + 32 < n) sincos((double)dof[3 + lane + 32], &t.s1, &t.c1);
-  return t;
-}
-
-__device__ __forceinline__ void store_split(float4* X, double x, double y, double z) {
-  const float xh = __double2float_rn(x), yh = __double2float_rn(y), zh = __double2float_rn(z);
-  X[0] = make_float4(xh, yh, zh, 0.f);
-  X[1] = make_float4(__double2float_rn(x - (double)xh), __double2float_rn(y - (double)yh),
-                     __double2float_rn(z - (double)zh), 0.f);
-}
-
-// ---------------------------------------------------------------------------
-// k_rebuild: posed coordinates X[b][a] (device frame, hi/lo floats) computed
-// in FP64 and, optionally, the intra-ligand energy of mol.ml:881-903 (IFORM 1)
-// or 853-877 (IFORM 0).
-// ---------------------------------------------------------------------------
-template <bool RECENTER, int DIEL, int IFORM>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
-    k_rebuild(DevLigand lig, PoseIO io, Scratch scr, int with_intra) {
-  __shared__ float4 sxh[kWarpsPerBlock][kMaxLig];
-  __shared__ float4 sxl[kWarpsPerBlock][kMaxLig];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int b = blockIdx.x * kWarpsPerBlock + wib;
-  if (b >= io.B) return;
-  const int L = lig.L, nrb = lig.nrb, nd = 6 + nrb;
-  const float* dof = io.dofs + (size_t)b * nd;
-  const AngleTable ang = angle_table(dof, nrb, lane);
-  double zx[kSlots], zy[kSlots], zz[kSlots];
-#pragma unroll
-  for (int s = 0; s < kSlots; ++s) {
-    const int a = lane + 32 * s;
-    zx[s] = a < L ? lig.ref64[3 * a] : 0.0;
-    zy[s] = a < L ? lig.ref64[3 * a + 1] : 0.0;
-    zz[s] = a < L ? lig.ref64[3 * a + 2] : 0.0;
-  }
-  // torsions in bond order (optim.ml:68-71, mol.ml:610-631)
-  for (int t = 0; t < nrb; ++t) {
-    const int2 bd = lig.bonds[t];
-    const double3 pl = fetchd(zx, zy, zz, bd.x);
-    const double3 pr = fetchd(zx, zy, zz, bd.y);
-    const double ax = pr.x - pl.x, ay = pr.y - pl.y, az = pr.z - pl.z;
-    const double inv = rnorm3d(ax, ay, az);
-    const double ux = ax * inv, uy = ay * inv, uz = az * inv;
-    double sn, cs;
-    ang.get(3 + t, sn, cs);
-    const double o = 1.0 - cs;
-    const double R0 = cs + ux * ux * o, R1 = ux * uy * o - uz * sn, R2 = ux * uz * o + uy * sn;
-    const double R3 = ux * uy * o + uz * sn, R4 = cs + uy * uy * o, R5 = uy * uz * o - ux * sn;
-    const double R6 = ux * uz * o - uy * sn, R7 = uy * uz * o + ux * sn, R8 = cs + uz * uz * o;
-#pragma unroll
-    for (int s = 0; s < kSlots; ++s) {
-      if ((lig.gmask[t * kSlots + s] >> lane) & 1u) {
-        const double vx = zx[s] - pr.x, vy = zy[s] - pr.y, vz = zz[s] - pr.z;
-        zx[s] = R0 * vx + R1 * vy + R2 * vz + pr.x;
-        zy[s] = R3 * vx + R4 * vy + R5 * vz + pr.y;
-        zz[s] = R6 * vx + R7 * vy + R8 * vz + pr.z;
-      }
-    }
-  }
-  // centroid and enclosing radius (mol.ml:576-591)
-  double cx = 0.0, cy = 0.0, cz = 0.0;
-#pragma unroll
-  for (int s = 0; s < kSlots; ++s)
-    if (lane + 32 * s < L) {
-      cx += zx[s];
-      cy += zy[s];
-      cz += zz[s];
-    }
-  cx = warp_sum(cx) / L;
-  cy = warp_sum(cy) / L;
-  cz = warp_sum(cz) / L;
-  double rad = 0.0;
-#pragma unroll
-  for (int s = 0; s < kSlots; ++s)
-    if (lane + 32 * s < L) {
-      const double dx = cx - zx[s], dy = cy - zy[s], dz = cz - zz[s];
-      rad = fmax(rad, 0.01 + sqrt(dx * dx + dy * dy + dz * dz));
-    }
-  const int status = warp_maxd(rad) > 12.0 ? kStatusTooLong : 0;
-  // rigid map: Rz(g) Ry(b) Rx(a) (rot.ml:52-66), then + t
-  double sa, ca, sb, cb, sg, cg;
-  ang.get(0, sa, ca);
-  ang.get(1, sb, cb);
-  ang.get(2, sg, cg);
-  const double R0 = cb * cg, R1 = cg * sa * sb - ca * sg, R2 = sa * sg + ca * cg * sb;
-  const double R3 = cb * sg, R4 = ca * cg + sa * sb * sg, R5 = ca * sb * sg - cg * sa;
-  const double R6 = -sb, R7 = cb * sa, R8 = ca * cb;
-  const double tx = (double)dof[0] - (double)io.ox, ty = (double)dof[1] - (double)io.oy,
-               tz = (double)dof[2] - (double)io.oz;
-#pragma unroll
-  for (int s = 0; s < kSlots; ++s) {
-    const int a = lane + 32 * s;
-    if (a < L) {
-      double vx = zx[s], vy = zy[s], vz = zz[s];
-      if (RECENTER) {
-        vx -= cx;
-        vy -= cy;
-        vz -= cz;
-      }
-      float4* out = scr.X + ((size_t)b * L + a) * 2;
-      store_split(out, R0 * vx + R1 * vy + R2 * vz + tx, R3 * vx + R4 * vy + R5 * vz + ty,
-                  R6 * vx + R7 * vy + R8 * vz + tz);
-      sxh[wib][a] = out[0];
-      sxl[wib][a] = out[1];
-    }
-  }
-  double e_intra = 0.0;
-  if (with_intra) {
-    __syncwarp();
-    float acc = 0.f, d0 = 0.f, d1 = 0.f, d2 = 0.f;
-    for (int p = lane; p < lig.npairs; p += 32) {
-      const int2 ij = lig.pair_ij[p];
-      const float4 par = lig.pair_par[p];
-      const float4 ih = sxh[wib][ij.x], il = sxl[wib][ij.x];
-      const float4 jh = sxh[wib][ij.y], jl = sxl[wib][ij.y];
-      uff_pair<false, DIEL, IFORM>(split_diff(ih.x, il.x, jh.x, jl.x),
-                                   split_diff(ih.y, il.y, jh.y, jl.y),
-                                   split_diff(ih.z, il.z, jh.z, jl.z), par.x, par.y, par.z, acc,
-                                   d0, d1, d2);
-    }
-    e_intra = warp_sum((double)acc);
-  }
-  if (lane == 0) {
-    io.status[b] = status;
-    if (with_intra) scr.Eintra[b] = e_intra;
-    if (b == 0 && io.zero_err) *io.err = 0;
-  }
-}
-
-// ---------------------------------------------------------------------------
-// k_finish: E[b] = sum of inter partials (FP64) + E_intra; with GRAD the
-// intra-ligand gradient and the reverse pass to dE/d[x, y, z, a, b, g, tau].
-// ---------------------------------------------------------------------------
 template <bool GRAD, bool RECENTER, int DIEL, int IFORM>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     k_finish(DevLigand lig, PoseIO io, Scratch scr, int flags) {
   __shared__ float4 sxh[kWarpsPerBlock][kMaxLig];
   __shared__ float4 sxl[kWarpsPerBlock][kMaxLig];
-  __shared__ TorsRec srec[kWarpsPerBlock][kMaxTors];
   __shared__ float4 saxis[kWarpsPerBlock][2 * kMaxTors];
+  __shared__ float sdti[kWarpsPerBlock][kMaxTors][33];  // per-lane torsion partials
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int b = blockIdx.x * kWarpsPerBlock + wib;
   if (b >= io.B) return;
-  const int L = lig.L, C = scr.C, nd = 6 + lig.nrb;
+  const int L = lig.L, C = scr.C, nrb = lig.nrb, nd = 6 + nrb;
+  const bool intra = flags & kFlagIntra, inter = flags & kFlagInter;
   double e = 0.0;
-  if (flags & kFlagInter) {
+  if (inter) {
     const double* ep = scr.Epart + (size_t)b * C * L;
     for (int k = lane; k < C * L; k += 32) e += ep[k];
-    e = warp_sum(e);
   }
-  if (flags & kFlagIntra) e += scr.Eintra[b];
+  if (intra) {
+    for (int a = lane; a < L; a += 32) {
+      sxh[wib][a] = scr.X[((size_t)b * L + a) * 2];
+      sxl[wib][a] = scr.X[((size_t)b * L + a) * 2 + 1];
+    }
+    __syncwarp();
+  }
+  const bool crossing = GRAD && intra && lig.nested && nrb > 0;
+  if (crossing) {
+    // final axis w_t and centre C_t of every torsion, from the posed coordinates
+    if (lane < nrb) {
+      const int2 bd = lig.bonds[lane];
+      const float4 rh = sxh[wib][bd.y], rl = sxl[wib][bd.y];
+      const float4 lh = sxh[wib][bd.x], ll = sxl[wib][bd.x];
+      const float ax = split_diff(rh.x, rl.x, lh.x, ll.x), ay = split_diff(rh.y, rl.y, lh.y, ll.y),
+                  az = split_diff(rh.z, rl.z, lh.z, ll.z);
+      const float inv = rsqrtf(ax * ax + ay * ay + az * az);
+      saxis[wib][lane] = make_float4(ax * inv, ay * inv, az * inv, 0.f);
+      saxis[wib][kMaxTors + lane] = rh;
+    }
+    for (int t = 0; t < nrb; ++t) sdti[wib][t][lane] = 0.f;
+    __syncwarp();
+  }
+  if (intra) {
+    // interacting pairs i < j: the energy, and for nested groups the torsion
+    // terms (dE/dX_moving) . (w_t x (X_moving - C_t)) of every torsion whose
+    // group holds exactly one of the two atoms
+    float acc = 0.f;
+    for (int p = lane; p < lig.npairs; p += 32) {
+      const int2 ij = lig.pair_ij[p];
+      const float4 par = lig.pair_par[p];
+      float ep, dx, dy, dz;
+      const float g = intra_pair_g<DIEL, IFORM>(sxh[wib], sxl[wib], ij.x, ij.y, par, ep, dx, dy, dz);
+      acc += ep;
+      if (crossing) {
+        const uint32_t mi = lig.amask[ij.x], mj = lig.amask[ij.y];
+        uint32_t x = mi ^ mj;
+        while (x) {
+          const int t = __ffs(x) - 1;
+          x &= x - 1;
+          const bool in_i = (mi >> t) & 1u;
+          const float4 w = saxis[wib][t], cc = saxis[wib][kMaxTors + t];
+          const float4 m = sxh[wib][in_i ? ij.x : ij.y];
+          const float lx = m.x - cc.x, ly = m.y - cc.y, lz = m.z - cc.z;
+          const float v = dx * (w.y * lz - w.z * ly) + dy * (w.z * lx - w.x * lz) +
+                          dz * (w.x * ly - w.y * lx);
+          sdti[wib][t][lane] = fmaf(in_i ? g : -g, v, sdti[wib][t][lane]);
+        }
+      }
+    }
+    e += (double)acc;
+  }
+  e = warp_sum(e);
   if (lane == 0) {
     io.E[b] = e;
     if (!isfinite(e)) io.status[b] |= kStatusNonFinite;
   }
   if (!GRAD) return;
 
-  // dE/dX from the pair sweep
+  // dE/dX from the pair sweep (and the intra forces for general groups)
   float gx[kSlots], gy[kSlots], gz[kSlots];
 #pragma unroll
   for (int s = 0; s < kSlots; ++s) gx[s] = gy[s] = gz[s] = 0.f;
-  if (flags & kFlagInter) {
+  if (inter) {
     const float4* gp = scr.Gpart + (size_t)b * C * L;
     for (int c = 0; c < C; ++c) {
 #pragma unroll
@@ -339,29 +245,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       }
     }
   }
-  // forward again, recording each torsion's axis
-  const float* dof = io.dofs + (size_t)b * nd;
-  float zx[kSlots], zy[kSlots], zz[kSlots];
-  load_ref(lig, lane, zx, zy, zz);
-  torsion_chain<true>(lig, dof + 6, lane, zx, zy, zz, srec[wib]);
-  const float3 c = RECENTER ? centroid(lig, lane, zx, zy, zz) : make_float3(0.f, 0.f, 0.f);
-  float R[9], cs[6];
-  rot_xyz(dof, R, cs);
-  const bool intra = flags & kFlagIntra;
-  if (intra) {
-    // intra-ligand gradient at the stored hi/lo posed coordinates
-#pragma unroll
-    for (int s = 0; s < kSlots; ++s) {
-      const int a = lane + 32 * s;
-      if (a < L) {
-        sxh[wib][a] = scr.X[((size_t)b * L + a) * 2];
-        sxl[wib][a] = scr.X[((size_t)b * L + a) * 2 + 1];
-      }
-    }
-    __syncwarp();
-  }
   if (intra && !lig.nested) {
-    // general groups: intra forces per atom, through the full reverse pass
 #pragma unroll
     for (int s = 0; s < kSlots; ++s) {
       const int a = lane + 32 * s;
@@ -380,57 +264,25 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       }
     }
   }
-  // nested groups: dE_intra/dtau_t = sum over interacting pairs with exactly
-  // one atom in group t of (dE/dX_moving) . (w_t x (X_moving - C_t)), w_t and
-  // C_t the final axis of bond t; the term adds nothing to the rigid DOFs.
-  // Keeping the large, cancelling intra forces out of the per-atom sums keeps
-  // the FP32 reverse pass accurate.
-  float dti[kMaxTors];
+  // coordinates after the torsions (recorded by k_rebuild)
+  float zx[kSlots], zy[kSlots], zz[kSlots];
 #pragma unroll
-  for (int t = 0; t < kMaxTors; ++t) dti[t] = 0.f;
-  if (intra && lig.nested && lig.nrb > 0) {
-    if (lane < lig.nrb) {
-      const int2 bd = lig.bonds[lane];
-      const float4 rh = sxh[wib][bd.y], rl = sxl[wib][bd.y];
-      const float4 lh = sxh[wib][bd.x], ll = sxl[wib][bd.x];
-      const float ax = split_diff(rh.x, rl.x, lh.x, ll.x), ay = split_diff(rh.y, rl.y, lh.y, ll.y),
-                  az = split_diff(rh.z, rl.z, lh.z, ll.z);
-      const float inv = rsqrtf(ax * ax + ay * ay + az * az);
-      saxis[wib][lane] = make_float4(ax * inv, ay * inv, az * inv, 0.f);
-      saxis[wib][kMaxTors + lane] = rh;
-    }
-    __syncwarp();
-    for (int p = lane; p < lig.npairs; p += 32) {
-      const int2 ij = lig.pair_ij[p];
-      const float4 par = lig.pair_par[p];
-      const float4 ih = sxh[wib][ij.x], il = sxl[wib][ij.x];
-      const float4 jh = sxh[wib][ij.y], jl = sxl[wib][ij.y];
-      const float dx = split_diff(ih.x, il.x, jh.x, jl.x);
-      const float dy = split_diff(ih.y, il.y, jh.y, jl.y);
-      const float dz = split_diff(ih.z, il.z, jh.z, jl.z);
-      const float g = uff_pair_g<DIEL, IFORM>(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), par.x, par.y,
-                                              par.z);
-#pragma unroll
-      for (int t = 0; t < kMaxTors; ++t) {
-        if (t < lig.nrb) {
-          const bool in_i = (lig.gmask[t * kSlots + (ij.x >> 5)] >> (ij.x & 31)) & 1u;
-          const bool in_j = (lig.gmask[t * kSlots + (ij.y >> 5)] >> (ij.y & 31)) & 1u;
-          if (in_i != in_j) {
-            const float4 w = saxis[wib][t], cc = saxis[wib][kMaxTors + t];
-            const float4 m = in_i ? ih : jh;
-            const float lx = m.x - cc.x, ly = m.y - cc.y, lz = m.z - cc.z;
-            // d . (w x l)
-            const float v = dx * (w.y * lz - w.z * ly) + dy * (w.z * lx - w.x * lz) +
-                            dz * (w.x * ly - w.y * lx);
-            dti[t] = fmaf(in_i ? g : -g, v, dti[t]);
-          }
-        }
-      }
-    }
-#pragma unroll
-    for (int t = 0; t < kMaxTors; ++t)
-      if (t < lig.nrb) dti[t] = warp_sum(dti[t]);
+  for (int s = 0; s < kSlots; ++s) {
+    const int a = lane + 32 * s;
+    const float4 y = a < L ? scr.Y[(size_t)b * L + a] : make_float4(0.f, 0.f, 0.f, 0.f);
+    zx[s] = y.x;
+    zy[s] = y.y;
+    zz[s] = y.z;
   }
+  const float4 cen = RECENTER ? scr.cen[b] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float* dof = io.dofs + (size_t)b * nd;
+  float sa, ca, sb, cb, sg, cg;
+  sincosf(dof[3], &sa, &ca);
+  sincosf(dof[4], &sb, &cb);
+  sincosf(dof[5], &sg, &cg);
+  const float R[9] = {cb * cg, cg * sa * sb - ca * sg, sa * sg + ca * cg * sb,
+                      cb * sg, ca * cg + sa * sb * sg, ca * sb * sg - cg * sa,
+                      -sb,     cb * sa,                 ca * cb};
   // rigid map: dE/dt = sum G; dE/dR_kl = sum_i G_ik Yc_il
   float red[12];
 #pragma unroll
@@ -438,7 +290,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 #pragma unroll
   for (int s = 0; s < kSlots; ++s) {
     if (lane + 32 * s < L) {
-      const float yx = zx[s] - c.x, yy = zy[s] - c.y, yz = zz[s] - c.z;
+      const float yx = zx[s] - cen.x, yy = zy[s] - cen.y, yz = zz[s] - cen.z;
       red[0] += gx[s];
       red[1] += gy[s];
       red[2] += gz[s];
@@ -451,7 +303,6 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
   for (int k = 0; k < 12; ++k) red[k] = warp_sum(red[k]);
   float* grad = io.grad + (size_t)b * nd;
   if (lane == 0) {
-    const float ca = cs[0], sa = cs[1], cb = cs[2], sb = cs[3], cg = cs[4], sg = cs[5];
     const float* M = red + 3;
     // d R / d a, d b, d g of rot.ml:52-66, entry by entry
     const float dA[9] = {0.f, cg * ca * sb + sa * sg, ca * sg - sa * cg * sb,
@@ -506,32 +357,40 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       az[s] -= mz;
     }
   }
-  __syncwarp();
+  // intra torsion terms of nested groups, each summed in lane order
+  float dti_mine = 0.f;
+  if (crossing) {
+    __syncwarp();
+    if (lane < nrb)
+      for (int k = 0; k < 32; ++k) dti_mine += sdti[wib][lane][k];
+  }
   // reverse through the torsions, undoing each rotation on the way back
-  for (int t = lig.nrb - 1; t >= 0; --t) {
-    const TorsRec rc = srec[wib][t];
+  const float4* recb = scr.rec + (size_t)b * nrb * 3;
+  for (int t = nrb - 1; t >= 0; --t) {
+    const float4 r0 = recb[3 * t], r1 = recb[3 * t + 1];
+    const float ilen = recb[3 * t + 2].x;
     float Rt[9];
-    axis_angle(rc.ux, rc.uy, rc.uz, rc.ct, rc.st, Rt);
+    axis_angle(r1.x, r1.y, r1.z, r0.w, r1.w, Rt);
     float q[10];
 #pragma unroll
     for (int k = 0; k < 10; ++k) q[k] = 0.f;
 #pragma unroll
     for (int s = 0; s < kSlots; ++s) {
       if ((lig.gmask[t * kSlots + s] >> lane) & 1u) {
-        const float px = zx[s] - rc.cx, py = zy[s] - rc.cy, pz = zz[s] - rc.cz;  // v'
-        const float vx = Rt[0] * px + Rt[3] * py + Rt[6] * pz;                  // v = R^T v'
+        const float px = zx[s] - r0.x, py = zy[s] - r0.y, pz = zz[s] - r0.z;  // v'
+        const float vx = Rt[0] * px + Rt[3] * py + Rt[6] * pz;                // v = R^T v'
         const float vy = Rt[1] * px + Rt[4] * py + Rt[7] * pz;
         const float vz = Rt[2] * px + Rt[5] * py + Rt[8] * pz;
         const float Ax = ax[s], Ay = ay[s], Az = az[s];
         // dtheta += A . (u x v')
-        q[0] += Ax * (rc.uy * pz - rc.uz * py) + Ay * (rc.uz * px - rc.ux * pz) +
-                Az * (rc.ux * py - rc.uy * px);
+        q[0] += Ax * (r1.y * pz - r1.z * py) + Ay * (r1.z * px - r1.x * pz) +
+                Az * (r1.x * py - r1.y * px);
         // v x A
         q[1] += vy * Az - vz * Ay;
         q[2] += vz * Ax - vx * Az;
         q[3] += vx * Ay - vy * Ax;
-        const float uv = rc.ux * vx + rc.uy * vy + rc.uz * vz;
-        const float Au = Ax * rc.ux + Ay * rc.uy + Az * rc.uz;
+        const float uv = r1.x * vx + r1.y * vy + r1.z * vz;
+        const float Au = Ax * r1.x + Ay * r1.y + Az * r1.z;
         q[4] += uv * Ax + Au * vx;
         q[5] += uv * Ay + Au * vy;
         q[6] += uv * Az + Au * vz;
@@ -541,26 +400,27 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         ax[s] = Rt[0] * Ax + Rt[3] * Ay + Rt[6] * Az;
         ay[s] = Rt[1] * Ax + Rt[4] * Ay + Rt[7] * Az;
         az[s] = Rt[2] * Ax + Rt[5] * Ay + Rt[8] * Az;
-        zx[s] = vx + rc.cx;
-        zy[s] = vy + rc.cy;
-        zz[s] = vz + rc.cz;
+        zx[s] = vx + r0.x;
+        zy[s] = vy + r0.y;
+        zz[s] = vz + r0.z;
       }
     }
 #pragma unroll
     for (int k = 0; k < 10; ++k) q[k] = warp_sum(q[k]);
-    const float omc = 1.0f - rc.ct;
-    const float dUx = rc.st * q[1] + omc * q[4];
-    const float dUy = rc.st * q[2] + omc * q[5];
-    const float dUz = rc.st * q[3] + omc * q[6];
-    const float uu = rc.ux * dUx + rc.uy * dUy + rc.uz * dUz;
-    const float dax = (dUx - rc.ux * uu) * rc.ilen;
-    const float day = (dUy - rc.uy * uu) * rc.ilen;
-    const float daz = (dUz - rc.uz * uu) * rc.ilen;
+    // dE/du (Rodrigues form), projected on the sphere and moved to the axis atoms
+    const float omc = 1.0f - r0.w;
+    const float dUx = r1.w * q[1] + omc * q[4];
+    const float dUy = r1.w * q[2] + omc * q[5];
+    const float dUz = r1.w * q[3] + omc * q[6];
+    const float uu = r1.x * dUx + r1.y * dUy + r1.z * dUz;
+    const int2 bd = lig.bonds[t];
+    const float dax = (dUx - r1.x * uu) * ilen;
+    const float day = (dUy - r1.y * uu) * ilen;
+    const float daz = (dUz - r1.z * uu) * ilen;
     // dE/dc = sum A - R^T sum A
     const float dCx = q[7] - (Rt[0] * q[7] + Rt[3] * q[8] + Rt[6] * q[9]);
     const float dCy = q[8] - (Rt[1] * q[7] + Rt[4] * q[8] + Rt[7] * q[9]);
     const float dCz = q[9] - (Rt[2] * q[7] + Rt[5] * q[8] + Rt[8] * q[9]);
-    const int2 bd = lig.bonds[t];
     if (lane == (bd.y & 31)) {
 #pragma unroll
       for (int s = 0; s < kSlots; ++s)
@@ -579,13 +439,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
           az[s] -= daz;
         }
     }
-    if (lane == 0) {
-      float intra_t = 0.f;
-#pragma unroll
-      for (int k = 0; k < kMaxTors; ++k)
-        if (k == t) intra_t = dti[k];
-      grad[6 + t] = q[0] + intra_t;
-    }
+    const float intra_t = __shfl_sync(kFull, dti_mine, t & 31);
+    if (lane == 0) grad[6 + t] = q[0] + intra_t;
   }
 }
 
@@ -615,11 +470,15 @@ __global__ void k_intra_plain(DevLigand lig, const float4* X, double* out) {
   if (threadIdx.x == 0) out[0] = e;
 }
 
-template <bool RC, int DIEL, int IFORM>
-cudaError_t rebuild_t(const DevLigand& lig, const PoseIO& io, const Scratch& s, int intra,
-                      cudaStream_t st) {
-  const int blocks = (io.B + kWarpsPerBlock - 1) / kWarpsPerBlock;
-  k_rebuild<RC, DIEL, IFORM><<<blocks, kWarpsPerBlock * 32, 0, st>>>(lig, io, s, intra);
+template <bool RC, bool REC>
+cudaError_t rebuild_t(const DevLigand& lig, const PoseIO& io, const Scratch& s, cudaStream_t st) {
+  const int blocks = (io.B + kRebuildThreads - 1) / kRebuildThreads;
+  const size_t smem = sizeof(double) * 3 * (size_t)lig.L * kRebuildThreads;
+  cudaError_t e =
+      cudaFuncSetAttribute(k_rebuild<RC, REC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem);
+  if (e != cudaSuccess) return e;
+  k_rebuild<RC, REC><<<blocks, kRebuildThreads, smem, st>>>(lig, io, s);
   return cudaGetLastError();
 }
 
@@ -633,24 +492,16 @@ cudaError_t finish_t(const DevLigand& lig, const PoseIO& io, const Scratch& s, i
 
 }  // namespace
 
-// intra_form: 0 plain (IFORM 1), 1 shifted (IFORM 0)
 cudaError_t launch_rebuild(const DevLigand& lig, const PoseIO& io, const Scratch& s, int flags,
-                           int intra_form, int dielectric, cudaStream_t st) {
+                           cudaStream_t st) {
   if (io.B <= 0) return cudaSuccess;
   const bool rc = flags & kFlagRecenter;
-  const int intra = (flags & kFlagIntra) ? 1 : 0;
-  const int d = dielectric ? 1 : 0, f = intra_form ? 0 : 1;
-#define MMO_RB(RC, D, F) return rebuild_t<RC, D, F>(lig, io, s, intra, st)
-  if (rc) {
-    if (d == 0) { if (f) MMO_RB(true, 0, 1); else MMO_RB(true, 0, 0); }
-    else { if (f) MMO_RB(true, 1, 1); else MMO_RB(true, 1, 0); }
-  } else {
-    if (d == 0) { if (f) MMO_RB(false, 0, 1); else MMO_RB(false, 0, 0); }
-    else { if (f) MMO_RB(false, 1, 1); else MMO_RB(false, 1, 0); }
-  }
-#undef MMO_RB
+  const bool rec = (flags & kFlagGrad) && io.grad;
+  if (rc) return rec ? rebuild_t<true, true>(lig, io, s, st) : rebuild_t<true, false>(lig, io, s, st);
+  return rec ? rebuild_t<false, true>(lig, io, s, st) : rebuild_t<false, false>(lig, io, s, st);
 }
 
+// intra_form: 0 plain (IFORM 1), 1 shifted (IFORM 0)
 cudaError_t launch_finish(const DevLigand& lig, const PoseIO& io, const Scratch& s, int flags,
                           const Physics& ph, cudaStream_t st) {
   if (io.B <= 0) return cudaSuccess;
@@ -658,11 +509,11 @@ cudaError_t launch_finish(const DevLigand& lig, const PoseIO& io, const Scratch&
   const bool rc = flags & kFlagRecenter;
   const int d = ph.dielectric ? 1 : 0, f = ph.intra_form ? 0 : 1;
 #define MMO_FN(G, RC, D, F) return finish_t<G, RC, D, F>(lig, io, s, flags, st)
-#define MMO_FN_D(G, RC)                                              \
+#define MMO_FN_D(G, RC)                                                   \
   if (d == 0) { if (f) MMO_FN(G, RC, 0, 1); else MMO_FN(G, RC, 0, 0); } \
   else { if (f) MMO_FN(G, RC, 1, 1); else MMO_FN(G, RC, 1, 0); }
   if (!g) {
-    MMO_FN(false, false, 0, 1);  // reduction only: physics-independent
+    MMO_FN_D(false, false)
   }
   if (rc) {
     MMO_FN_D(true, true)

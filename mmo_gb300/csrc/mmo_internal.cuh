@@ -11,7 +11,7 @@ constexpr int kMaxLig = 128;    // ligand atoms per system (4 per lane in a warp
 constexpr int kSlots = kMaxLig / 32;
 constexpr int kMaxTors = 32;    // rotatable bonds per ligand
 constexpr int kNTypes = 12;     // UFF elements of src/UFF.ml:10-22
-constexpr int kSliceAtoms = 6912;   // protein atoms resident in shared memory per launch (32 B each)
+constexpr int kSliceAtoms = 3456;   // protein atoms resident in shared memory per launch (64 B each)
 constexpr float kCut2 = 144.0f;     // 12 A cutoff, squared (const.ml:12-14)
 constexpr float kMinR2 = 1e-4f;     // (0.01 A)^2, Math.non_zero_dist (math.ml:58-62)
 
@@ -27,6 +27,10 @@ constexpr float kMinR2 = 1e-4f;     // (0.01 A)^2, Math.non_zero_dist (math.ml:5
 // K * q with K = 332.0637 / 4.
 struct DevProtein {
   const float4* atoms;    // [P][2]: (x_hi, y_hi, z_hi, K q), (x_lo, y_lo, z_lo, 0)
+  // [P][4] the same atoms for the packed FP32x2 sweep, every value doubled and
+  // the coordinates negated: (-x_hi, -x_hi, -y_hi, -y_hi), (-z_hi, -z_hi, Kq, Kq),
+  // (-x_lo, -x_lo, -y_lo, -y_lo), (-z_lo, -z_lo, 0, 0)
+  const float4* atoms4;
   const uint8_t* type;    // [P] type index, for the plain kernel
   const int* runs;        // [2 * kNTypes + 1]: run_start[nruns + 1], then run_type[nruns]
   int P;
@@ -37,6 +41,12 @@ struct DevProtein {
 // warp-uniform lookups hit the constant bank.
 struct PairTable {
   float2 xd[kNTypes * kNTypes];
+};
+
+// The same pairs for the packed sweep: (X = D^(1/3) x^2, 1/D (0 when D = 0),
+// x^2, D).
+struct PairTable4 {
+  float4 v[kNTypes * kNTypes];
 };
 
 // Ligand topology and reference conformer in HBM.
@@ -57,6 +67,9 @@ struct DevLigand {
   const uint32_t* gmask;    // [nrb][kSlots] group bitmask, bit (a & 31) of word (a >> 5)
   const int2* pair_ij;      // [npairs] interacting pairs i < j (mol.ml:203-208)
   const float4* pair_par;   // [npairs] (x^2, D, K q_i q_j, 0)
+  const uint32_t* amask;    // [L] bit t set when the atom is in rotation group t
+  const int* grp_off;       // [nrb + 1] rotation groups as CSR
+  const int* grp_atoms;
   const int* nb_off;        // [L + 1] both-direction CSR of the same pairs
   const int* nb_idx;        // partner atom
   const float4* nb_par;     // (x^2, D, K q_i q_j, 0)
@@ -68,7 +81,9 @@ struct Scratch {
   float4* X;       // [B][L][2] posed coordinates in the device frame, hi then lo
   double* Epart;   // [B][C][L] inter energy partial per chunk and ligand atom
   float4* Gpart;   // [B][C][L] dE/dX partial per chunk and ligand atom
-  double* Eintra;  // [B]
+  float4* Y;       // [B][L] coordinates after the torsions, before the rigid map (gradient only)
+  float4* rec;     // [B][nrb][3] torsion records (c, cos), (u, sin), (1/|a|) (gradient only)
+  float4* cen;     // [B] centroid of Y (gradient only)
   int C;
 };
 
@@ -96,16 +111,16 @@ struct Physics {
 
 // Launch plan of the batched pair kernel (chosen by the tuner).
 struct PairPlan {
-  int kp;        // poses per lane: 1, 2 or 4
+  int kp;        // poses per lane: 2, 4 or 8
   int threads;   // threads per CTA: 256 or 512
   int C;         // protein chunks per pose
   int blocks;    // persistent grid size
 };
 
 // ---- launchers (defined in the .cu files) --------------------------------
-cudaError_t launch_rebuild(const DevLigand& lig, const PoseIO& io, const Scratch& s,
-                           int flags, int intra_form, int dielectric, cudaStream_t st);
-cudaError_t launch_pairs_batched(const DevProtein& prot, const PairTable& tab,
+cudaError_t launch_rebuild(const DevLigand& lig, const PoseIO& io, const Scratch& s, int flags,
+                           cudaStream_t st);
+cudaError_t launch_pairs_batched(const DevProtein& prot, const PairTable4& tab,
                                  const DevLigand& lig, const Scratch& s, int B, int flags,
                                  const Physics& ph, const PairPlan& plan, int* d_err,
                                  cudaStream_t st);
