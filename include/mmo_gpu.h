@@ -140,7 +140,7 @@ int mmo_score_poses_noalloc(mmo_ctx* ctx, int B, const float* d_dofs, int flags,
  * (MMO_ETIMEOUT). */
 int mmo_sync(mmo_ctx* ctx, void* stream);
 
-/* Tile shape of the batched pair kernel: poses per lane (2, 4, 8), threads
+/* Tile shape of the batched pair kernel: poses per lane (1, 2, 4), threads
  * per CTA (256, 512) and protein chunks per pose (0: automatic).  Setting 0
  * for all restores the automatic choice. */
 int mmo_set_tiles(mmo_ctx* ctx, int poses_per_lane, int threads, int chunks);

@@ -347,13 +347,12 @@ PairPlan plan_for(mmo_ctx* ctx, int B, bool grad) {
 
 PairPlan make_plan(mmo_ctx* ctx, int B, bool grad) {
   PairPlan p{};
-  p.kp = ctx->tile_kp ? ctx->tile_kp : (B >= 4096 ? 4 : 2);
+  p.kp = ctx->tile_kp ? ctx->tile_kp : (B >= 4096 ? 4 : (B >= 256 ? 2 : 1));
   p.threads = ctx->tile_threads ? ctx->tile_threads : 512;
-  if (p.kp >= 8) p.threads = 256;  // 8 poses per lane need the register budget of 256 threads
   const int P = ctx->prot.P, L = ctx->lig.L;
   const int nslices = (P + kSliceAtoms - 1) / kSliceAtoms;
   const int slice_len = (P + nslices - 1) / nslices;
-  const int smem = slice_len * 64;
+  const int smem = slice_len * 32;
   int bps = pairs_batched_max_blocks(p.kp, p.threads, grad, ctx->ph, smem);
   if (bps < 1) bps = 1;
   p.blocks = ctx->sms * bps;
@@ -519,9 +518,9 @@ int mmo_set_physics(mmo_ctx* ctx, int dielectric, int mixing, int inter_form, in
 
 int mmo_set_tiles(mmo_ctx* ctx, int kp, int threads, int chunks) {
   if (!ctx) return MMO_EINVAL;
-  if (!(kp == 0 || kp == 2 || kp == 4 || kp == 8) ||
+  if (!(kp == 0 || kp == 1 || kp == 2 || kp == 4) ||
       !(threads == 0 || threads == 256 || threads == 512) || chunks < 0 || chunks > 4096)
-    return fail(ctx, MMO_EINVAL, "tiles: poses_per_lane in {0,2,4,8}, threads in {0,256,512}");
+    return fail(ctx, MMO_EINVAL, "tiles: poses_per_lane in {0,1,2,4}, threads in {0,256,512}");
   ctx->tile_kp = kp;
   ctx->tile_threads = threads;
   ctx->tile_chunks = chunks;
@@ -559,7 +558,7 @@ int mmo_set_protein(mmo_ctx* ctx, int n, const double* xs, const double* ys, con
   std::vector<int> idx(n);
   std::iota(idx.begin(), idx.end(), 0);
   std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return type[a] < type[b]; });
-  std::vector<float4> atoms(2 * (size_t)std::max(n, 1)), atoms4(4 * (size_t)std::max(n, 1));
+  std::vector<float4> atoms(2 * (size_t)std::max(n, 1));
   std::vector<uint8_t> ptype(std::max(n, 16), 0);
   std::vector<int> rstart, rtype;
   DevProtein P{};
@@ -568,11 +567,6 @@ int mmo_set_protein(mmo_ctx* ctx, int n, const double* xs, const double* ys, con
     const int i = idx[k];
     split_store(&atoms[2 * (size_t)k], xs[i] - (double)of[0], ys[i] - (double)of[1],
                 zs[i] - (double)of[2], (float)(kElec * q[i]));
-    const float4 h = atoms[2 * (size_t)k], l = atoms[2 * (size_t)k + 1];
-    atoms4[4 * (size_t)k] = make_float4(-h.x, -h.x, -h.y, -h.y);
-    atoms4[4 * (size_t)k + 1] = make_float4(-h.z, -h.z, h.w, h.w);
-    atoms4[4 * (size_t)k + 2] = make_float4(-l.x, -l.x, -l.y, -l.y);
-    atoms4[4 * (size_t)k + 3] = make_float4(-l.z, -l.z, 0.f, 0.f);
     ptype[k] = (uint8_t)type[i];
     if (k == 0 || type[i] != type[idx[k - 1]]) {
       rstart.push_back(k);
@@ -590,18 +584,15 @@ int mmo_set_protein(mmo_ctx* ctx, int n, const double* xs, const double* ys, con
   ctx->d_prot = nullptr;
   size_t off = 0;
   const size_t o_atoms = take(off, sizeof(float4) * atoms.size());
-  const size_t o_atoms4 = take(off, sizeof(float4) * atoms4.size());
   const size_t o_type = take(off, ptype.size());
   const size_t o_runs = take(off, sizeof(int) * runs.size());
   std::vector<char> blob(off, 0);
   memcpy(blob.data() + o_atoms, atoms.data(), sizeof(float4) * atoms.size());
-  memcpy(blob.data() + o_atoms4, atoms4.data(), sizeof(float4) * atoms4.size());
   memcpy(blob.data() + o_type, ptype.data(), ptype.size());
   memcpy(blob.data() + o_runs, runs.data(), sizeof(int) * runs.size());
   MMO_CK(cudaMalloc(&ctx->d_prot, off), "protein");
   MMO_CK(cudaMemcpy(ctx->d_prot, blob.data(), off, cudaMemcpyHostToDevice), "protein upload");
   P.atoms = reinterpret_cast<const float4*>((char*)ctx->d_prot + o_atoms);
-  P.atoms4 = reinterpret_cast<const float4*>((char*)ctx->d_prot + o_atoms4);
   P.type = reinterpret_cast<const uint8_t*>((char*)ctx->d_prot + o_type);
   P.runs = reinterpret_cast<const int*>((char*)ctx->d_prot + o_runs);
   ctx->prot = P;

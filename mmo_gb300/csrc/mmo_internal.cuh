@@ -11,7 +11,7 @@ constexpr int kMaxLig = 128;    // ligand atoms per system (4 per lane in a warp
 constexpr int kSlots = kMaxLig / 32;
 constexpr int kMaxTors = 32;    // rotatable bonds per ligand
 constexpr int kNTypes = 12;     // UFF elements of src/UFF.ml:10-22
-constexpr int kSliceAtoms = 3456;   // protein atoms resident in shared memory per launch (64 B each)
+constexpr int kSliceAtoms = 6912;   // protein atoms resident in shared memory per launch (32 B each)
 constexpr float kCut2 = 144.0f;     // 12 A cutoff, squared (const.ml:12-14)
 constexpr float kMinR2 = 1e-4f;     // (0.01 A)^2, Math.non_zero_dist (math.ml:58-62)
 
@@ -27,10 +27,6 @@ constexpr float kMinR2 = 1e-4f;     // (0.01 A)^2, Math.non_zero_dist (math.ml:5
 // K * q with K = 332.0637 / 4.
 struct DevProtein {
   const float4* atoms;    // [P][2]: (x_hi, y_hi, z_hi, K q), (x_lo, y_lo, z_lo, 0)
-  // [P][4] the same atoms for the packed FP32x2 sweep, every value doubled and
-  // the coordinates negated: (-x_hi, -x_hi, -y_hi, -y_hi), (-z_hi, -z_hi, Kq, Kq),
-  // (-x_lo, -x_lo, -y_lo, -y_lo), (-z_lo, -z_lo, 0, 0)
-  const float4* atoms4;
   const uint8_t* type;    // [P] type index, for the plain kernel
   const int* runs;        // [2 * kNTypes + 1]: run_start[nruns + 1], then run_type[nruns]
   int P;
@@ -43,7 +39,7 @@ struct PairTable {
   float2 xd[kNTypes * kNTypes];
 };
 
-// The same pairs for the packed sweep: (X = D^(1/3) x^2, 1/D (0 when D = 0),
+// The same pairs for the batched sweep: (X = D^(1/3) x^2, 1/D (0 when D = 0),
 // x^2, D).
 struct PairTable4 {
   float4 v[kNTypes * kNTypes];
@@ -111,7 +107,7 @@ struct Physics {
 
 // Launch plan of the batched pair kernel (chosen by the tuner).
 struct PairPlan {
-  int kp;        // poses per lane: 2, 4 or 8
+  int kp;        // poses per lane: 1, 2 or 4
   int threads;   // threads per CTA: 256 or 512
   int C;         // protein chunks per pose
   int blocks;    // persistent grid size

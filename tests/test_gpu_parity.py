@@ -164,8 +164,8 @@ def test_batched_physics_variants(oracle, scorer_factory, batch, phys):
     assert_grad(G, G64)
 
 
-@pytest.mark.parametrize("kp,threads,chunks", [(2, 256, 0), (2, 512, 3), (4, 512, 1),
-                                               (4, 256, 17), (8, 256, 5), (2, 256, 64)])
+@pytest.mark.parametrize("kp,threads,chunks", [(1, 256, 0), (2, 512, 3), (4, 512, 1),
+                                               (4, 256, 17), (2, 256, 64)])
 def test_tile_shapes_agree(scorer_factory, batch, kp, threads, chunks):
     s = scorer_factory(batch.pocket, batch.ligand)
     d = batch.poses[:200]
