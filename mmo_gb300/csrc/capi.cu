@@ -83,6 +83,7 @@ struct mmo_ctx {
   Physics ph{0, 0, 0, 0};
   PairTable tab{};
   PairTable4 tab4{};
+  float4* d_tab4 = nullptr;  // device copy of tab4
   int tile_kp = 0, tile_threads = 0, tile_chunks = 0;
   // last launch plan and the inputs it was made for
   PairPlan plan{};
@@ -153,6 +154,15 @@ void rebuild_table(mmo_ctx* ctx) {
       ctx->tab4.v[a * kNTypes + b] = make_float4(
           (float)(std::cbrt(d) * x2), d > 0.0 ? (float)(1.0 / d) : 0.f, (float)x2, (float)d);
     }
+}
+
+// copy the packed pair table to the device (after in-flight work on the
+// context's stream)
+int upload_table(mmo_ctx* ctx) {
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before table upload");
+  MMO_CK(cudaMemcpy(ctx->d_tab4, ctx->tab4.v, sizeof(ctx->tab4.v), cudaMemcpyHostToDevice),
+         "pair table upload");
+  return MMO_OK;
 }
 
 int grow(mmo_ctx* ctx, void** p, size_t* cap, size_t bytes, const char* what) {
@@ -434,7 +444,7 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
                                 ctx->scr.Epart, ctx->scr.Gpart, grad, ctx->ph, st),
              "plain pair kernel");
     } else {
-      MMO_CK(launch_pairs_batched(ctx->prot, ctx->tab4, ctx->lig, ctx->scr, B, fl, ctx->ph, plan,
+      MMO_CK(launch_pairs_batched(ctx->prot, ctx->d_tab4, ctx->lig, ctx->scr, B, fl, ctx->ph, plan,
                                   d_err, st),
              "batched pair kernel");
     }
@@ -472,12 +482,18 @@ int mmo_ctx_create(int device, mmo_ctx** out) {
           cudaSuccess ||
       (e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaMalloc((void**)&ctx->d_err, sizeof(int))) != cudaSuccess ||
-      (e = cudaMemset(ctx->d_err, 0, sizeof(int))) != cudaSuccess) {
+      (e = cudaMemset(ctx->d_err, 0, sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc((void**)&ctx->d_tab4, sizeof(ctx->tab4.v))) != cudaSuccess) {
     snprintf(g_create_err, sizeof g_create_err, "context set-up: %s", cudaGetErrorString(e));
     delete ctx;
     return e == cudaErrorMemoryAllocation ? MMO_ENOMEM : MMO_ECUDA;
   }
   rebuild_table(ctx);
+  if (upload_table(ctx) != MMO_OK) {
+    snprintf(g_create_err, sizeof g_create_err, "context set-up: %s", ctx->err.c_str());
+    mmo_ctx_destroy(ctx);
+    return MMO_ECUDA;
+  }
   *out = ctx;
   return MMO_OK;
 }
@@ -497,6 +513,7 @@ int mmo_ctx_destroy(mmo_ctx* ctx) {
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
   cudaFree(ctx->d_err);
+  cudaFree(ctx->d_tab4);
   cudaFree(ctx->d_in);
   cudaFree(ctx->d_out);
   if (ctx->h_in) cudaFreeHost(ctx->h_in);
@@ -512,6 +529,7 @@ int mmo_set_physics(mmo_ctx* ctx, int dielectric, int mixing, int inter_form, in
     return fail(ctx, MMO_EINVAL, "physics switches are 0 or 1");
   ctx->ph = Physics{dielectric, mixing, inter_form, intra_form};
   rebuild_table(ctx);
+  if (int r = upload_table(ctx)) return r;
   if (ctx->has_lig) return upload_ligand(ctx);
   return MMO_OK;
 }
@@ -965,7 +983,7 @@ extern "C" int mmo_score_poses_noalloc(mmo_ctx* ctx, int B, const float* d_dofs,
   // atom) partial by the pair sweep
   MMO_CK(launch_rebuild(ctx->lig, io, s, fl, st), "rebuild kernel");
   if (inter)
-    MMO_CK(launch_pairs_batched(ctx->prot, ctx->tab4, ctx->lig, s, B, fl, ctx->ph, plan,
+    MMO_CK(launch_pairs_batched(ctx->prot, ctx->d_tab4, ctx->lig, s, B, fl, ctx->ph, plan,
                                 ctx->d_err, st),
            "batched pair kernel");
   MMO_CK(launch_finish(ctx->lig, io, s, fl, ctx->ph, st), "finish kernel");

@@ -65,10 +65,32 @@ __device__ __forceinline__ void pair_step(float xh, float yh, float zh, float xl
   }
 }
 
+// dE/dX of one pose for the protein atoms [c0, c1) with the per-pair test
+// of the 0.01 A clamp (rarely needed, so kept out of the main loop's registers)
+template <int DIEL, int FORM>
+__device__ __noinline__ float3 exact_grad(const float4* sp, int slice0, int c0, int c1,
+                                          const int* s_runs, int nruns, const float4* tabv,
+                                          int ltype, float qj, float xh, float yh, float zh,
+                                          float xl, float yl, float zl) {
+  float e = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+  for (int r = 0; r < nruns; ++r) {
+    const int lo = max(c0, s_runs[r]);
+    const int hi = min(c1, s_runs[r + 1]);
+    if (lo >= hi) continue;
+    const float4 pv = tabv[s_runs[nruns + 1 + r] * kNTypes + ltype];
+    for (int i = lo - slice0; i < hi - slice0; ++i) {
+      const float4 p = sp[2 * i], pl = sp[2 * i + 1];
+      uff_pair<true, DIEL, FORM>((xh - p.x) + (xl - pl.x), (yh - p.y) + (yl - pl.y),
+                                 (zh - p.z) + (zl - pl.z), pv.z, pv.w, p.w * qj, e, gx, gy, gz);
+    }
+  }
+  return make_float3(gx, gy, gz);
+}
+
 template <int KP, bool GRAD, int DIEL, int FORM>
 __global__ void __launch_bounds__(512)
-    k_pairs(DevProtein prot, PairTable4 tab, DevLigand lig, Scratch scr, int B, int slice0,
-            int slice1, int chunk0, int C_slice, int chunk_len, int* err) {
+    k_pairs(DevProtein prot, const float4* __restrict__ tabv, DevLigand lig, Scratch scr, int B,
+            int slice0, int slice1, int chunk0, int C_slice, int chunk_len, int* err) {
   extern __shared__ __align__(16) float4 sp[];  // [slice][2]
   __shared__ __align__(8) uint64_t bar;
   __shared__ int s_runs[2 * kNTypes + 1];
@@ -134,7 +156,7 @@ __global__ void __launch_bounds__(512)
       const int lo = max(c0, s_runs[r]);
       const int hi = min(c1, s_runs[r + 1]);
       if (lo >= hi) continue;
-      const float4 pv = tab.v[s_runs[prot.nruns + 1 + r] * kNTypes + ltype];
+      const float4 pv = tabv[s_runs[prot.nruns + 1 + r] * kNTypes + ltype];
       const float c1v = (DIEL == 0 ? 11.0f : 5.0f) * pv.y;
       const float c0v = DIEL == 0 ? -10.0f : -4.0f;
       for (int i0 = lo; i0 < hi; i0 += kFlush) {
@@ -162,20 +184,11 @@ __global__ void __launch_bounds__(512)
       gs = 1.0f;
 #pragma unroll
       for (int k = 0; k < KP; ++k) {
-        float e0 = 0.f;
-        gx[k] = gy[k] = gz[k] = 0.f;
-        for (int r = 0; r < prot.nruns; ++r) {
-          const int lo = max(c0, s_runs[r]);
-          const int hi = min(c1, s_runs[r + 1]);
-          if (lo >= hi) continue;
-          const float4 pv = tab.v[s_runs[prot.nruns + 1 + r] * kNTypes + ltype];
-          for (int i = lo - slice0; i < hi - slice0; ++i) {
-            const float4 p = sp[2 * i], pl = sp[2 * i + 1];
-            uff_pair<true, DIEL, FORM>((xh[k] - p.x) + (xl[k] - pl.x), (yh[k] - p.y) + (yl[k] - pl.y),
-                                       (zh[k] - p.z) + (zl[k] - pl.z), pv.z, pv.w, p.w * qj, e0,
-                                       gx[k], gy[k], gz[k]);
-          }
-        }
+        const float3 g = exact_grad<DIEL, FORM>(sp, slice0, c0, c1, s_runs, prot.nruns, tabv, ltype,
+                                                qj, xh[k], yh[k], zh[k], xl[k], yl[k], zl[k]);
+        gx[k] = g.x;
+        gy[k] = g.y;
+        gz[k] = g.z;
       }
     }
     const int cg = chunk0 + cl;
@@ -227,8 +240,8 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-using PairsFn = void (*)(DevProtein, PairTable4, DevLigand, Scratch, int, int, int, int, int, int,
-                         int*);
+using PairsFn = void (*)(DevProtein, const float4*, DevLigand, Scratch, int, int, int, int, int,
+                         int, int*);
 
 template <int KP>
 PairsFn pick_batched(bool grad, int diel, int form) {
@@ -260,7 +273,7 @@ int pairs_batched_max_blocks(int kp, int threads, int grad, const Physics& ph, i
   return nb;
 }
 
-cudaError_t launch_pairs_batched(const DevProtein& prot, const PairTable4& tab,
+cudaError_t launch_pairs_batched(const DevProtein& prot, const float4* tab,
                                  const DevLigand& lig, const Scratch& s, int B, int flags,
                                  const Physics& ph, const PairPlan& plan, int* d_err,
                                  cudaStream_t st) {

@@ -18,7 +18,7 @@ namespace mmo {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kRebuildThreads = 32;   // poses per rebuild block
+constexpr int kRebuildThreads = 128;  // threads per rebuild block
 constexpr int kWarpsPerBlock = 4;     // poses per finish block
 
 // ---------------------------------------------------------------------------
@@ -31,71 +31,87 @@ __device__ __forceinline__ void store_split(float4* X, double x, double y, doubl
                      __double2float_rn(z - (double)zh), 0.f);
 }
 
-template <bool RECENTER, bool RECORD>
+// TPP threads share one pose: each rotates its share of the atoms while the
+// per-torsion axis and matrix are recomputed by all of them, and the sines and
+// cosines of the pose's angles are computed once, split over the TPP threads.
+// Small batches use many threads per pose (the one-pose path uses a whole
+// warp), large batches one thread per pose.
+template <bool RECENTER, bool RECORD, int TPP>
 __global__ void __launch_bounds__(kRebuildThreads) k_rebuild(DevLigand lig, PoseIO io, Scratch scr) {
-  extern __shared__ double sz[];  // [3][L][kRebuildThreads]
-  const int tid = threadIdx.x;
-  const int b = blockIdx.x * kRebuildThreads + tid;
+  constexpr int PPB = kRebuildThreads / TPP;  // poses per block
+  constexpr int NANG = 3 + kMaxTors;
+  extern __shared__ double sz[];  // [3][L][PPB] coordinates, then [PPB][NANG][2] sin, cos
+  const int tid = threadIdx.x, p = tid / TPP, sub = tid % TPP;
+  const int b = blockIdx.x * PPB + p;
   const int L = lig.L, nrb = lig.nrb, nd = 6 + nrb;
   double* X = sz;
-  double* Yc = sz + L * kRebuildThreads;
-  double* Zc = sz + 2 * L * kRebuildThreads;
-#define AT(arr, a) arr[(a) * kRebuildThreads + tid]
+  double* Yc = sz + L * PPB;
+  double* Zc = sz + 2 * L * PPB;
+  double* SC = sz + 3 * L * PPB + p * NANG * 2;
+#define AT(arr, a) arr[(a) * PPB + p]
   const bool live = b < io.B;
   const float* dof = io.dofs + (size_t)(live ? b : 0) * nd;
-  for (int a = 0; a < L; ++a) {
+  for (int a = sub; a < L; a += TPP) {
     AT(X, a) = lig.ref64[3 * a];
     AT(Yc, a) = lig.ref64[3 * a + 1];
     AT(Zc, a) = lig.ref64[3 * a + 2];
   }
+  for (int k = sub; k < 3 + nrb; k += TPP) sincos((double)dof[3 + k], &SC[2 * k], &SC[2 * k + 1]);
+  __syncwarp();
   for (int t = 0; t < nrb; ++t) {
     const int2 bd = lig.bonds[t];
     const double cx = AT(X, bd.y), cy = AT(Yc, bd.y), cz = AT(Zc, bd.y);
     const double ax = cx - AT(X, bd.x), ay = cy - AT(Yc, bd.x), az = cz - AT(Zc, bd.x);
     const double inv = rnorm3d(ax, ay, az);
     const double ux = ax * inv, uy = ay * inv, uz = az * inv;
-    double sn, cs;
-    sincos((double)dof[6 + t], &sn, &cs);
+    const double sn = SC[2 * (3 + t)], cs = SC[2 * (3 + t) + 1];
     // Rodrigues matrix of rot.ml:136-146
     const double o = 1.0 - cs;
     const double R0 = cs + ux * ux * o, R1 = ux * uy * o - uz * sn, R2 = ux * uz * o + uy * sn;
     const double R3 = ux * uy * o + uz * sn, R4 = cs + uy * uy * o, R5 = uy * uz * o - ux * sn;
     const double R6 = ux * uz * o - uy * sn, R7 = uy * uz * o + ux * sn, R8 = cs + uz * uz * o;
-    for (int k = lig.grp_off[t]; k < lig.grp_off[t + 1]; ++k) {
+    __syncwarp();  // every thread of the pose has read the axis
+    for (int k = lig.grp_off[t] + sub; k < lig.grp_off[t + 1]; k += TPP) {
       const int i = lig.grp_atoms[k];
       const double vx = AT(X, i) - cx, vy = AT(Yc, i) - cy, vz = AT(Zc, i) - cz;
       AT(X, i) = R0 * vx + R1 * vy + R2 * vz + cx;
       AT(Yc, i) = R3 * vx + R4 * vy + R5 * vz + cy;
       AT(Zc, i) = R6 * vx + R7 * vy + R8 * vz + cz;
     }
-    if (RECORD && live) {
+    if (RECORD && live && sub == 0) {
       float4* r = scr.rec + ((size_t)b * nrb + t) * 3;
       r[0] = make_float4((float)cx, (float)cy, (float)cz, (float)cs);
       r[1] = make_float4((float)ux, (float)uy, (float)uz, (float)sn);
       r[2] = make_float4((float)inv, 0.f, 0.f, 0.f);
     }
+    __syncwarp();  // the rotated group is visible before the next axis is read
   }
   // centroid and enclosing radius, max_i (0.01 + |c - y_i|) > 12 (mol.ml:576-591)
   double mx = 0.0, my = 0.0, mz = 0.0;
-  for (int a = 0; a < L; ++a) {
+  for (int a = sub; a < L; a += TPP) {
     mx += AT(X, a);
     my += AT(Yc, a);
     mz += AT(Zc, a);
+  }
+#pragma unroll
+  for (int o = TPP / 2; o > 0; o >>= 1) {
+    mx += __shfl_xor_sync(kFull, mx, o);
+    my += __shfl_xor_sync(kFull, my, o);
+    mz += __shfl_xor_sync(kFull, mz, o);
   }
   mx /= L;
   my /= L;
   mz /= L;
   double d2max = 0.0;
-  for (int a = 0; a < L; ++a) {
+  for (int a = sub; a < L; a += TPP) {
     const double dx = mx - AT(X, a), dy = my - AT(Yc, a), dz = mz - AT(Zc, a);
     d2max = fmax(d2max, dx * dx + dy * dy + dz * dz);
   }
+#pragma unroll
+  for (int o = TPP / 2; o > 0; o >>= 1) d2max = fmax(d2max, __shfl_xor_sync(kFull, d2max, o));
   const int status = 0.01 + sqrt(d2max) > 12.0 ? kStatusTooLong : 0;
   // rigid map
-  double sa, ca, sb, cb, sg, cg;
-  sincos((double)dof[3], &sa, &ca);
-  sincos((double)dof[4], &sb, &cb);
-  sincos((double)dof[5], &sg, &cg);
+  const double sa = SC[0], ca = SC[1], sb = SC[2], cb = SC[3], sg = SC[4], cg = SC[5];
   const double R0 = cb * cg, R1 = cg * sa * sb - ca * sg, R2 = sa * sg + ca * cg * sb;
   const double R3 = cb * sg, R4 = ca * cg + sa * sb * sg, R5 = ca * sb * sg - cg * sa;
   const double R6 = -sb, R7 = cb * sa, R8 = ca * cb;
@@ -103,7 +119,7 @@ __global__ void __launch_bounds__(kRebuildThreads) k_rebuild(DevLigand lig, Pose
                tz = (double)dof[2] - (double)io.oz;
   const double ox = RECENTER ? mx : 0.0, oy = RECENTER ? my : 0.0, oz = RECENTER ? mz : 0.0;
   if (live) {
-    for (int a = 0; a < L; ++a) {
+    for (int a = sub; a < L; a += TPP) {
       const double vx = AT(X, a) - ox, vy = AT(Yc, a) - oy, vz = AT(Zc, a) - oz;
       store_split(scr.X + ((size_t)b * L + a) * 2, R0 * vx + R1 * vy + R2 * vz + tx,
                   R3 * vx + R4 * vy + R5 * vz + ty, R6 * vx + R7 * vy + R8 * vz + tz);
@@ -111,9 +127,11 @@ __global__ void __launch_bounds__(kRebuildThreads) k_rebuild(DevLigand lig, Pose
         scr.Y[(size_t)b * L + a] = make_float4((float)AT(X, a), (float)AT(Yc, a),
                                                 (float)AT(Zc, a), 0.f);
     }
-    if (RECORD) scr.cen[b] = make_float4((float)mx, (float)my, (float)mz, 0.f);
-    io.status[b] = status;
-    if (b == 0 && io.zero_err) *io.err = 0;
+    if (sub == 0) {
+      if (RECORD) scr.cen[b] = make_float4((float)mx, (float)my, (float)mz, 0.f);
+      io.status[b] = status;
+      if (b == 0 && io.zero_err) *io.err = 0;
+    }
   }
 #undef AT
 }
@@ -144,10 +162,9 @@ __device__ __forceinline__ float intra_pair_g(const float4* sh, const float4* sl
   dx = split_diff(ih.x, il.x, jh.x, jl.x);
   dy = split_diff(ih.y, il.y, jh.y, jl.y);
   dz = split_diff(ih.z, il.z, jh.z, jl.z);
-  float g0 = 0.f, g1 = 0.f, g2 = 0.f, acc = 0.f;
-  uff_pair<false, DIEL, IFORM>(dx, dy, dz, par.x, par.y, par.z, acc, g0, g1, g2);
-  e = acc;
-  return uff_pair_g<DIEL, IFORM>(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), par.x, par.y, par.z);
+  float g;
+  uff_pair_eg<DIEL, IFORM>(dx, dy, dz, par.x, par.y, par.z, e, g);
+  return g;
 }
 
 template <bool GRAD, bool RECENTER, int DIEL, int IFORM>
@@ -376,6 +393,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     for (int k = 0; k < 10; ++k) q[k] = 0.f;
 #pragma unroll
     for (int s = 0; s < kSlots; ++s) {
+      if (32 * s >= L) break;  // uniform: no atoms in this slot
       if ((lig.gmask[t * kSlots + s] >> lane) & 1u) {
         const float px = zx[s] - r0.x, py = zy[s] - r0.y, pz = zz[s] - r0.z;  // v'
         const float vx = Rt[0] * px + Rt[3] * py + Rt[6] * pz;                // v = R^T v'
@@ -470,16 +488,29 @@ __global__ void k_intra_plain(DevLigand lig, const float4* X, double* out) {
   if (threadIdx.x == 0) out[0] = e;
 }
 
-template <bool RC, bool REC>
+template <bool RC, bool REC, int TPP>
 cudaError_t rebuild_t(const DevLigand& lig, const PoseIO& io, const Scratch& s, cudaStream_t st) {
-  const int blocks = (io.B + kRebuildThreads - 1) / kRebuildThreads;
-  const size_t smem = sizeof(double) * 3 * (size_t)lig.L * kRebuildThreads;
-  cudaError_t e =
-      cudaFuncSetAttribute(k_rebuild<RC, REC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem);
+  constexpr int PPB = kRebuildThreads / TPP;
+  const int blocks = (io.B + PPB - 1) / PPB;
+  const size_t smem = sizeof(double) * ((size_t)3 * lig.L * PPB + (size_t)PPB * (3 + kMaxTors) * 2);
+  cudaError_t e = cudaFuncSetAttribute(k_rebuild<RC, REC, TPP>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_rebuild<RC, REC><<<blocks, kRebuildThreads, smem, st>>>(lig, io, s);
+  k_rebuild<RC, REC, TPP><<<blocks, kRebuildThreads, smem, st>>>(lig, io, s);
   return cudaGetLastError();
+}
+
+template <bool RC, bool REC>
+cudaError_t rebuild_tpp(int tpp, const DevLigand& lig, const PoseIO& io, const Scratch& s,
+                        cudaStream_t st) {
+  switch (tpp) {
+    case 1: return rebuild_t<RC, REC, 1>(lig, io, s, st);
+    case 2: return rebuild_t<RC, REC, 2>(lig, io, s, st);
+    case 4: return rebuild_t<RC, REC, 4>(lig, io, s, st);
+    case 8: return rebuild_t<RC, REC, 8>(lig, io, s, st);
+    case 16: return rebuild_t<RC, REC, 16>(lig, io, s, st);
+    default: return rebuild_t<RC, REC, 32>(lig, io, s, st);
+  }
 }
 
 template <bool G, bool RC, int DIEL, int IFORM>
@@ -497,8 +528,17 @@ cudaError_t launch_rebuild(const DevLigand& lig, const PoseIO& io, const Scratch
   if (io.B <= 0) return cudaSuccess;
   const bool rc = flags & kFlagRecenter;
   const bool rec = (flags & kFlagGrad) && io.grad;
-  if (rc) return rec ? rebuild_t<true, true>(lig, io, s, st) : rebuild_t<true, false>(lig, io, s, st);
-  return rec ? rebuild_t<false, true>(lig, io, s, st) : rebuild_t<false, false>(lig, io, s, st);
+  // threads per pose: enough threads in flight to hide FP64 latency (about
+  // 20,000, two 128-thread blocks per SM), within 200 KB of shared memory
+  int tpp = 32;
+  while (tpp > 1 && (long)io.B * (tpp / 2) >= 20000) tpp /= 2;
+  while (tpp < 32 && sizeof(double) * (3.0 * lig.L + 2.0 * (3 + kMaxTors)) *
+                             (kRebuildThreads / tpp) > 200.0 * 1024)
+    tpp *= 2;
+  if (rc) return rec ? rebuild_tpp<true, true>(tpp, lig, io, s, st)
+                     : rebuild_tpp<true, false>(tpp, lig, io, s, st);
+  return rec ? rebuild_tpp<false, true>(tpp, lig, io, s, st)
+             : rebuild_tpp<false, false>(tpp, lig, io, s, st);
 }
 
 // intra_form: 0 plain (IFORM 1), 1 shifted (IFORM 0)

@@ -116,7 +116,7 @@ struct PairPlan {
 // ---- launchers (defined in the .cu files) --------------------------------
 cudaError_t launch_rebuild(const DevLigand& lig, const PoseIO& io, const Scratch& s, int flags,
                            cudaStream_t st);
-cudaError_t launch_pairs_batched(const DevProtein& prot, const PairTable4& tab,
+cudaError_t launch_pairs_batched(const DevProtein& prot, const float4* tab,
                                  const DevLigand& lig, const Scratch& s, int B, int flags,
                                  const Physics& ph, const PairPlan& plan, int* d_err,
                                  cudaStream_t st);
@@ -192,9 +192,12 @@ __device__ __forceinline__ void uff_pair(float dx, float dy, float dz, float x2,
   }
 }
 
-// The scalar g of one pair's gradient, dE_pair/dd = g d (same terms as uff_pair).
+// Energy e and the scalar g of one pair's gradient, dE_pair/dd = g d (the
+// terms of uff_pair, from one reciprocal square root).
 template <int DIEL, int FORM>
-__device__ __forceinline__ float uff_pair_g(float r2, float x2, float D, float qq) {
+__device__ __forceinline__ void uff_pair_eg(float dx, float dy, float dz, float x2, float D,
+                                            float qq, float& e_out, float& g_out) {
+  const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
   const float r2c = fmaxf(r2, kMinR2);
   const float ir = rsqrtf(r2c);
   const float ir2 = ir * ir;
@@ -211,7 +214,8 @@ __device__ __forceinline__ float uff_pair_g(float r2, float x2, float D, float q
   const float t = fmaf(-12.0f, Dp6 * (p6 - 1.0f), DIEL == 0 ? -el : -2.0f * el);
   float g = w * t * ir2;
   if (FORM == 0) g = fmaf(s * (-1.0f / 36.0f), e, g);
-  return r2 < kMinR2 ? 0.0f : g;
+  e_out = w * e;
+  g_out = r2 < kMinR2 ? 0.0f : g;
 }
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
