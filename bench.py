@@ -258,6 +258,8 @@ def main():
     clk = clocks.stop()
     sc.set_profiling(False)
     sc.sync(sp)
+    launches = sc.last_launches()
+    pairs_ev, pairs_all = sc.pair_count()
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     tot_ms = float(sum(step_ms))
     if dist:
@@ -312,8 +314,9 @@ def main():
     # ---- roofline of the pair sweep -----------------------------------------
     peak = sc.fp32_peak_tflops()
     pair_avg = float(np.mean(pair_ms))
-    flops = FLOPS_PAIR_GRAD * L_atoms * P * B
+    flops = FLOPS_PAIR_GRAD * pairs_ev
     achieved = flops / (pair_avg * 1e-3) * 1e-12
+    culled = pairs_ev < pairs_all
 
     line = {
         "metric": METRIC, "value": value, "unit": "poses/s", "n_gpus": world,
@@ -327,16 +330,20 @@ def main():
                    "parallelism": "dp%d (poses sharded, no collective)" % world},
         "e2e": {"value": e2e_val, "unit": "poses/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
-        "gpu_launches": 3 * args.steps,
+        "gpu_launches": launches * args.steps,
         "plain": {"value": plain_v, "e2e": plain_e2e, "unit": "poses/s", "sample": n_plain,
                   "launches_per_pose": 3},
         "batched_vs_plain": value / world / plain_v,
         "batched_vs_plain_e2e": e2e_val / world / plain_e2e,
-        "roofline": {"bound": "fp32", "kernel": "k_pairs (pair sweep, energy+gradient)",
+        "roofline": {"bound": "fp32",
+                     "kernel": ("k_pairs_cull (cut-off pair sweep, energy+gradient)" if culled
+                                else "k_pairs (pair sweep, energy+gradient)"),
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,
                      "peak_source": "measured FP32 FMA probe on this GPU (mmo_fp32_fma_peak)",
-                     "flops_per_launch": flops, "ms_per_launch": pair_avg},
+                     "flops_per_pair": FLOPS_PAIR_GRAD, "pairs_evaluated": pairs_ev,
+                     "pairs_all": pairs_all, "flops_per_launch": flops,
+                     "ms_per_launch": pair_avg},
         "clocks": clk,
         "wall_s_timed": wall,
         "status_bits_set": int(np.count_nonzero(st)),

@@ -19,10 +19,21 @@ extern "C" {
  * stream) when on != 0. */
 int mmo_set_profiling(mmo_ctx* ctx, int on);
 
-/* Device milliseconds of the last scoring call's stages: ms[0] pose rebuild
- * (+ intra energy), ms[1] pair sweep (all launches), ms[2] finishing pass
- * (reduction, intra gradient, reverse kinematics).  Waits for those events. */
+/* Device milliseconds of the last scoring call's stages, ms[4]: ms[0] pose
+ * rebuild, ms[1] pair sweep (its kernel launches only), ms[2] finishing
+ * (piece reduction, intra energy and gradient, reverse kinematics), ms[3]
+ * entry sort of the cut-off sweep (0 without it).  Waits for those events. */
 int mmo_stage_times(mmo_ctx* ctx, float* ms);
+
+/* Pair evaluations of the last batched scoring call: *evaluated counts the
+ * (entry, protein atom) pairs the sweep computed (the cut-off sweep computes
+ * 32 * entries_per_lane pairs for each protein atom a warp visits), *all the
+ * pairs of the batch (poses x ligand atoms x protein atoms).  Waits for the
+ * device. */
+int mmo_pair_count(mmo_ctx* ctx, double* evaluated, double* all);
+
+/* Kernels (this library's own) that the last scoring call launched. */
+int mmo_last_launches(const mmo_ctx* ctx, int* kernels);
 
 /* FP32 FMA throughput of the device: a grid of independent FMA chains timed
  * with CUDA events; *tflops = 2 * FMAs / time. */

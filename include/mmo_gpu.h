@@ -145,6 +145,17 @@ int mmo_sync(mmo_ctx* ctx, void* stream);
  * for all restores the automatic choice. */
 int mmo_set_tiles(mmo_ctx* ctx, int poses_per_lane, int threads, int chunks);
 
+/* Cut-off sweep of the shifted form for batches (the counterpart of
+ * Mol.ene_inter_UFF_shifted_bst, UnixJunkie/MMO src/mol.ml:928-962, which
+ * visits only the protein atoms within 12 A of each ligand atom).  mode 0:
+ * automatic, used for batches of 2 or more poses under the shifted form when
+ * the protein and its row index fit in shared memory; mode 1: off, every pair
+ * is evaluated.  row_spacing: (y, z) spacing of the protein's row index in A
+ * (<= 0: 2; a change rebuilds the index); piece_atoms: protein atoms per
+ * work item (0: 256); entries_per_lane: 1, 2, 4 (0: 2). */
+int mmo_set_cull(mmo_ctx* ctx, int mode, double row_spacing, int piece_atoms,
+                 int entries_per_lane);
+
 /* Number of SMs of the context's device (for callers that size batches). */
 int mmo_device_sms(const mmo_ctx* ctx, int* out);
 

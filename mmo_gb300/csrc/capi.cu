@@ -94,6 +94,33 @@ struct mmo_ctx {
   void* d_prot = nullptr;
   double origin[3] = {0, 0, 0};
   float origin_f[3] = {0, 0, 0};
+  // host copy in the device frame, for rebuilding the row index
+  std::vector<double> pxs, pys, pzs;
+  std::vector<float> pkq;
+  std::vector<int> ptypes;
+
+  // cut-off sweep of the shifted form (mmo_set_cull)
+  int cull_mode = 0;        // 0: automatic, 1: off
+  double cull_h = 2.0;      // row spacing of the protein index, A
+  int cull_piece = 0;       // protein atoms per piece, 0: automatic
+  int cull_kp = 0;          // entries per lane, 0: automatic
+  bool cull_ok = false;     // row index built and resident in shared memory
+  long cull_version = 0;    // bumped by every rebuild of the row index
+  DevCull cull{};
+  void* d_cull = nullptr;
+  std::vector<int> cull_rows;  // host copy of row_start
+  int smem_optin = 0;
+  CullScratch cs{};
+  CullSegs segs{};
+  CullPlan cplan{};
+  long cplan_key[10] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+  int* d_piece = nullptr;
+  size_t capPiece = 0, capHist = 0, capBin = 0, capRank = 0, capXs = 0, capOrd = 0, capEp = 0,
+         capGp = 0;
+  unsigned* d_queue = nullptr;  // [0] work counter, [2..3] pair evaluations (u64)
+  bool last_cull = false;       // the last call's inter term used the cut-off sweep
+  double last_pairs = 0;        // poses x ligand atoms x protein atoms of the last call
+  int last_launches = 0;        // kernels of the last scoring call
 
   // ligand (host copies kept for physics changes)
   DevLigand lig{};
@@ -102,15 +129,17 @@ struct mmo_ctx {
   std::vector<double> lx, ly, lz, lq;
   std::vector<int> ltype, lbonds, lgoff, lgatoms;
   std::vector<uint8_t> linter;
+  std::vector<int> lseg_type, lseg_count;  // ligand types present, atoms of each
+  long lig_version = 0, prot_version = 0;  // bumped by every upload
 
   // scratch
   Scratch scr{};
   size_t capX = 0, capE = 0, capG = 0, capI = 0, capY = 0, capR = 0;
   int* d_err = nullptr;
 
-  // stage timing (mmo_set_profiling)
+  // stage timing (mmo_set_profiling): start, rebuilt, sorted, swept, finished
   bool profiling = false;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   bool ev_valid = false;
 
   // host-API staging
@@ -301,6 +330,7 @@ int upload_ligand(mmo_ctx* ctx) {
     L.nb_off = align_ptr<int>(b, off, n + 1);
     L.nb_idx = align_ptr<int>(b, off, std::max((int)nb_idx.size(), 1));
     L.nb_par = align_ptr<float4>(b, off, std::max((int)nb_par.size(), 1));
+    L.seg_of_atom = align_ptr<int>(b, off, n);
     return L;
   };
   layout(nullptr);
@@ -331,6 +361,17 @@ int upload_ligand(mmo_ctx* ctx) {
     memcpy((void*)H.nb_par, nb_par.data(), sizeof(float4) * nb_par.size());
   }
   memcpy((void*)H.nb_off, nb_off.data(), sizeof(int) * (n + 1));
+  // type segments of the cut-off sweep: the ligand's types in ascending order
+  ctx->lseg_type.clear();
+  ctx->lseg_count.clear();
+  for (int t = 0; t < kNTypes; ++t) {
+    const int c = (int)std::count(ctx->ltype.begin(), ctx->ltype.end(), t);
+    if (!c) continue;
+    for (int i = 0; i < n; ++i)
+      if (ctx->ltype[i] == t) const_cast<int*>(H.seg_of_atom)[i] = (int)ctx->lseg_type.size();
+    ctx->lseg_type.push_back(t);
+    ctx->lseg_count.push_back(c);
+  }
   MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before ligand upload");
   if (ctx->d_lig) cudaFree(ctx->d_lig);
   ctx->d_lig = nullptr;
@@ -339,6 +380,115 @@ int upload_ligand(mmo_ctx* ctx) {
   base = reinterpret_cast<char*>(ctx->d_lig);
   ctx->lig = layout(base);
   ctx->has_lig = true;
+  ++ctx->lig_version;
+  return MMO_OK;
+}
+
+// Row index of the protein for the cut-off sweep: rows of a (y, z) grid of
+// spacing h in (iz, iy) order, empty rows dropped, each row sorted by x; a
+// flush point after the row where 256 atoms have accumulated.
+int build_cull(mmo_ctx* ctx) {
+  ctx->cull_ok = false;
+  ctx->cull_rows.clear();
+  if (ctx->d_cull) {
+    MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before row index upload");
+    cudaFree(ctx->d_cull);
+  }
+  ctx->d_cull = nullptr;
+  const int n = (int)ctx->pxs.size();
+  if (n <= 0) return MMO_OK;
+  std::vector<float> fx(n), fy(n), fz(n);
+  float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+  for (int i = 0; i < n; ++i) {
+    fx[i] = (float)ctx->pxs[i];
+    fy[i] = (float)ctx->pys[i];
+    fz[i] = (float)ctx->pzs[i];
+    const float v[3] = {fx[i], fy[i], fz[i]};
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = std::min(lo[d], v[d]);
+      hi[d] = std::max(hi[d], v[d]);
+    }
+  }
+  double h = ctx->cull_h > 0 ? ctx->cull_h : 2.0;
+  long ny = 0, nz = 0;
+  for (;;) {
+    ny = (long)std::floor((hi[1] - lo[1]) / h) + 1;
+    nz = (long)std::floor((hi[2] - lo[2]) / h) + 1;
+    if (ny * nz <= (1L << 20)) break;
+    h *= 1.5;
+  }
+  std::vector<long> key(n);
+  for (int i = 0; i < n; ++i) {
+    const long iy = std::min(ny - 1, (long)std::floor((fy[i] - lo[1]) / h));
+    const long iz = std::min(nz - 1, (long)std::floor((fz[i] - lo[2]) / h));
+    key[i] = iz * ny + iy;
+  }
+  std::vector<int> idx(n);
+  std::iota(idx.begin(), idx.end(), 0);
+  std::sort(idx.begin(), idx.end(), [&](int a, int b) {
+    if (key[a] != key[b]) return key[a] < key[b];
+    if (fx[a] != fx[b]) return fx[a] < fx[b];
+    return a < b;
+  });
+  std::vector<float4> atoms(2 * (size_t)n);
+  std::vector<int> rs;
+  std::vector<float4> rbox;
+  std::vector<int> rflush;
+  int since = 0;
+  for (int k = 0; k < n; ++k) {
+    const int i = idx[k];
+    split_store(&atoms[2 * (size_t)k], ctx->pxs[i], ctx->pys[i], ctx->pzs[i], ctx->pkq[i]);
+    const int tb = ctx->ptypes[i] * kNTypes;
+    memcpy(&atoms[2 * (size_t)k + 1].w, &tb, sizeof tb);
+    if (k == 0 || key[i] != key[idx[k - 1]]) {
+      if (k) {
+        since += k - rs.back();
+        rflush.push_back(since >= kCullFlush);
+        if (since >= kCullFlush) since = 0;
+      }
+      rs.push_back(k);
+      rbox.push_back(make_float4(1e30f, -1e30f, 1e30f, -1e30f));
+    }
+    float4& b = rbox.back();
+    b.x = std::min(b.x, fy[i]);
+    b.y = std::max(b.y, fy[i]);
+    b.z = std::min(b.z, fz[i]);
+    b.w = std::max(b.w, fz[i]);
+  }
+  rflush.push_back(1);
+  rs.push_back(n);
+  const int nrows = (int)rbox.size();
+  size_t off = 0;
+  const size_t o_atoms = take(off, sizeof(float4) * atoms.size());
+  const size_t o_rs = take(off, sizeof(int) * rs.size());
+  const size_t o_box = take(off, sizeof(float4) * rbox.size());
+  const size_t o_fl = take(off, sizeof(int) * rflush.size());
+  std::vector<char> blob(off, 0);
+  memcpy(blob.data() + o_atoms, atoms.data(), sizeof(float4) * atoms.size());
+  memcpy(blob.data() + o_rs, rs.data(), sizeof(int) * rs.size());
+  memcpy(blob.data() + o_box, rbox.data(), sizeof(float4) * rbox.size());
+  memcpy(blob.data() + o_fl, rflush.data(), sizeof(int) * rflush.size());
+  MMO_CK(cudaMalloc(&ctx->d_cull, off), "protein row index");
+  MMO_CK(cudaMemcpy(ctx->d_cull, blob.data(), off, cudaMemcpyHostToDevice), "row index upload");
+  DevCull c{};
+  char* base = reinterpret_cast<char*>(ctx->d_cull);
+  c.atoms = reinterpret_cast<const float4*>(base + o_atoms);
+  c.row_start = reinterpret_cast<const int*>(base + o_rs);
+  c.row_box = reinterpret_cast<const float4*>(base + o_box);
+  c.row_flush = reinterpret_cast<const int*>(base + o_fl);
+  c.P = n;
+  c.nrows = nrows;
+  // entry binning: a cube about the protein's box, 2 A beyond it
+  float side = 0.f;
+  for (int d = 0; d < 3; ++d) side = std::max(side, hi[d] - lo[d]);
+  side += 4.0f;
+  for (int d = 0; d < 3; ++d) c.glo[d] = 0.5f * (lo[d] + hi[d]) - 0.5f * side;
+  c.ginv = (float)kCullGrid / side;
+  ctx->cull = c;
+  ctx->cull_rows = rs;
+  ++ctx->cull_version;
+  // the sweep keeps the whole protein and its index in shared memory
+  ctx->cull_ok = cull_smem_bytes(n, nrows, nrows) <= ctx->smem_optin;
   return MMO_OK;
 }
 
@@ -391,6 +541,92 @@ PairPlan make_plan(mmo_ctx* ctx, int B, bool grad) {
   return p;
 }
 
+// the cut-off sweep serves the shifted form when the protein's row index fits
+// in shared memory
+bool use_cull(const mmo_ctx* ctx, int B) {
+  return ctx->cull_mode == 0 && ctx->cull_ok && ctx->ph.inter_form == 0 && B >= 2 &&
+         !ctx->lseg_type.empty();
+}
+
+// plan of the cut-off sweep (pieces, type segments, grid), cached per input
+int cull_plan_for(mmo_ctx* ctx, int B, bool grad) {
+  const long key[10] = {B, grad, ctx->prot_version, ctx->lig_version, ctx->cull_kp,
+                        ctx->cull_piece, ctx->tile_threads, ctx->ph.dielectric,
+                        ctx->cull_version, ctx->prot.P};
+  if (std::equal(key, key + 10, ctx->cplan_key)) return MMO_OK;
+  CullPlan p{};
+  p.kp = ctx->cull_kp ? ctx->cull_kp : 2;
+  p.threads = ctx->tile_threads ? ctx->tile_threads : 512;
+  p.piece_atoms = ctx->cull_piece ? ctx->cull_piece : 256;
+  const std::vector<int>& rs = ctx->cull_rows;
+  const int nrows = (int)rs.size() - 1;
+  // pieces: consecutive rows of about piece_atoms atoms
+  std::vector<int> pr{0};
+  int acc = 0;
+  for (int r = 0; r < nrows; ++r) {
+    acc += rs[r + 1] - rs[r];
+    if (acc >= p.piece_atoms && r + 1 < nrows) {
+      pr.push_back(r + 1);
+      acc = 0;
+    }
+  }
+  pr.push_back(nrows);
+  const int npieces = (int)pr.size() - 1;
+  int r = grow(ctx, (void**)&ctx->d_piece, &ctx->capPiece, sizeof(int) * pr.size(), "piece table");
+  if (r) return r;
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before piece table upload");
+  MMO_CK(cudaMemcpy(ctx->d_piece, pr.data(), sizeof(int) * pr.size(), cudaMemcpyHostToDevice),
+         "piece table upload");
+  CullSegs sg{};
+  sg.nseg = (int)ctx->lseg_type.size();
+  sg.G = 32 * p.kp;
+  sg.off[0] = 0;
+  for (int t = 0; t < sg.nseg; ++t) {
+    sg.n[t] = B * ctx->lseg_count[t];
+    sg.type[t] = ctx->lseg_type[t];
+    sg.off[t + 1] = sg.off[t] + (sg.n[t] + sg.G - 1) / sg.G * sg.G;
+  }
+  p.smem = cull_smem_bytes(ctx->cull.P, ctx->cull.nrows, npieces);
+  const int bps = std::max(1, cull_max_blocks(p.kp, p.threads, grad, ctx->ph, p.smem));
+  p.blocks = ctx->sms * bps;
+  const long items = (long)sg.off[sg.nseg] / sg.G * npieces;
+  const long need = (items + p.threads / 32 - 1) / (p.threads / 32);
+  if (need < p.blocks) p.blocks = (int)std::max(1L, need);
+  ctx->cplan = p;
+  ctx->segs = sg;
+  ctx->cs.npieces = npieces;
+  std::copy(key, key + 10, ctx->cplan_key);
+  return MMO_OK;
+}
+
+int ensure_cull_scratch(mmo_ctx* ctx, int B, int L, bool grad) {
+  int r;
+  const CullSegs& sg = ctx->segs;
+  const size_t slots = sg.off[sg.nseg], np = ctx->cs.npieces;
+  CullScratch& c = ctx->cs;
+  if ((r = grow(ctx, (void**)&c.hist, &ctx->capHist, sizeof(unsigned) * sg.nseg * kCullBins,
+                "entry bins")))
+    return r;
+  if ((r = grow(ctx, (void**)&c.bin, &ctx->capBin, sizeof(int) * (size_t)B * L, "entry bin")))
+    return r;
+  if ((r = grow(ctx, (void**)&c.rank, &ctx->capRank, sizeof(int) * (size_t)B * L, "entry rank")))
+    return r;
+  if ((r = grow(ctx, (void**)&c.Xs, &ctx->capXs, sizeof(float4) * 2 * slots, "sorted entries")))
+    return r;
+  if ((r = grow(ctx, (void**)&c.order, &ctx->capOrd, sizeof(int) * slots, "slot order"))) return r;
+  if ((r = grow(ctx, (void**)&c.Ep, &ctx->capEp, sizeof(double) * np * slots, "piece energies")))
+    return r;
+  if (grad &&
+      (r = grow(ctx, (void**)&c.Gp, &ctx->capGp, sizeof(float4) * np * slots, "piece gradients")))
+    return r;
+  c.queue = ctx->d_queue;
+  c.pairs = reinterpret_cast<unsigned long long*>(ctx->d_queue + 2);
+  c.seg_of_atom = ctx->lig.seg_of_atom;
+  c.piece_row = ctx->d_piece;
+  c.slots = (int)slots;
+  return MMO_OK;
+}
+
 int check_dev_err(mmo_ctx* ctx, int flag) {
   if (flag & kErrTimeout)
     return fail(ctx, MMO_ETIMEOUT, "a bounded device-side wait (protein staging) gave up");
@@ -409,18 +645,26 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
   const bool grad = flags & MMO_F_GRAD;
   const bool inter = (flags & MMO_F_INTER) && ctx->prot.P > 0;
   const int L = ctx->lig.L;
+  const bool cull = inter && use_cull(ctx, B);
+  ctx->last_cull = cull;
+  ctx->last_pairs = inter ? (double)B * L * ctx->prot.P : 0.0;
+  // rebuild + finish, and the sweep: entry bin, scan, scatter, sweep, piece sum
+  ctx->last_launches = 2 + (cull ? 5 : (inter ? 1 : 0));
   PairPlan plan{};
   int C = 1;
+  int r;
   if (inter) {
     if (B == 1) {
       C = std::max(1, (ctx->prot.P + 255) / 256);
+    } else if (cull) {
+      if ((r = cull_plan_for(ctx, B, grad))) return r;
     } else {
       plan = plan_for(ctx, B, grad);
       C = plan.C;
     }
   }
-  int r = ensure_scratch(ctx, B, L, C, grad);
-  if (r) return r;
+  if ((r = ensure_scratch(ctx, B, L, C, grad))) return r;
+  if (cull && (r = ensure_cull_scratch(ctx, B, L, grad))) return r;
   PoseIO io{};
   io.dofs = d_dofs;
   io.E = d_E;
@@ -435,24 +679,40 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
   int fl = flags & (kFlagInter | kFlagIntra | kFlagGrad | kFlagRecenter);
   if (!inter) fl &= ~kFlagInter;
   const bool prof = ctx->profiling;
-  if (prof) MMO_CK(cudaEventRecord(ctx->ev[0], st), "event");
+  auto mark = [&](int k) { return prof ? cudaEventRecord(ctx->ev[k], st) : cudaSuccess; };
+  MMO_CK(mark(0), "event");
   MMO_CK(launch_rebuild(ctx->lig, io, ctx->scr, fl, st), "rebuild kernel");
-  if (prof) MMO_CK(cudaEventRecord(ctx->ev[1], st), "event");
-  if (inter) {
-    if (B == 1) {
-      MMO_CK(launch_pairs_plain(ctx->prot, ctx->tab, ctx->scr.X, ctx->lig.q, ctx->lig.type, L, C,
-                                ctx->scr.Epart, ctx->scr.Gpart, grad, ctx->ph, st),
-             "plain pair kernel");
-    } else {
-      MMO_CK(launch_pairs_batched(ctx->prot, ctx->d_tab4, ctx->lig, ctx->scr, B, fl, ctx->ph, plan,
-                                  d_err, st),
-             "batched pair kernel");
+  MMO_CK(mark(1), "event");
+  if (cull) {
+    const CullSegs& sg = ctx->segs;
+    MMO_CK(cudaMemsetAsync(ctx->cs.hist, 0, sizeof(unsigned) * sg.nseg * kCullBins, st),
+           "entry bin reset");
+    MMO_CK(launch_cull_sort(ctx->cull, ctx->scr, ctx->lig.q, B, L, sg, ctx->cs, st),
+           "entry sort kernels");
+    MMO_CK(mark(2), "event");
+    MMO_CK(launch_pairs_cull(ctx->cull, ctx->d_tab4, sg, ctx->cs, fl, ctx->ph, ctx->cplan, d_err,
+                             st),
+           "cut-off pair kernel");
+    MMO_CK(mark(3), "event");
+    MMO_CK(launch_cull_reduce(sg, ctx->cs, ctx->scr, grad, st), "piece reduction kernel");
+  } else {
+    MMO_CK(mark(2), "event");
+    if (inter) {
+      if (B == 1) {
+        MMO_CK(launch_pairs_plain(ctx->prot, ctx->tab, ctx->scr.X, ctx->lig.q, ctx->lig.type, L,
+                                  C, ctx->scr.Epart, ctx->scr.Gpart, grad, ctx->ph, st),
+               "plain pair kernel");
+      } else {
+        MMO_CK(launch_pairs_batched(ctx->prot, ctx->d_tab4, ctx->lig, ctx->scr, B, fl, ctx->ph,
+                                    plan, d_err, st),
+               "batched pair kernel");
+      }
     }
+    MMO_CK(mark(3), "event");
   }
-  if (prof) MMO_CK(cudaEventRecord(ctx->ev[2], st), "event");
   MMO_CK(launch_finish(ctx->lig, io, ctx->scr, fl, ctx->ph, st), "finish kernel");
   if (prof) {
-    MMO_CK(cudaEventRecord(ctx->ev[3], st), "event");
+    MMO_CK(mark(4), "event");
     ctx->ev_valid = true;
   }
   return MMO_OK;
@@ -483,7 +743,10 @@ int mmo_ctx_create(int device, mmo_ctx** out) {
       (e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaMalloc((void**)&ctx->d_err, sizeof(int))) != cudaSuccess ||
       (e = cudaMemset(ctx->d_err, 0, sizeof(int))) != cudaSuccess ||
-      (e = cudaMalloc((void**)&ctx->d_tab4, sizeof(ctx->tab4.v))) != cudaSuccess) {
+      (e = cudaMalloc((void**)&ctx->d_tab4, sizeof(ctx->tab4.v))) != cudaSuccess ||
+      (e = cudaMalloc((void**)&ctx->d_queue, 16)) != cudaSuccess ||
+      (e = cudaDeviceGetAttribute(&ctx->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                                  device)) != cudaSuccess) {
     snprintf(g_create_err, sizeof g_create_err, "context set-up: %s", cudaGetErrorString(e));
     delete ctx;
     return e == cudaErrorMemoryAllocation ? MMO_ENOMEM : MMO_ECUDA;
@@ -514,6 +777,16 @@ int mmo_ctx_destroy(mmo_ctx* ctx) {
     if (e) cudaEventDestroy(e);
   cudaFree(ctx->d_err);
   cudaFree(ctx->d_tab4);
+  cudaFree(ctx->d_queue);
+  cudaFree(ctx->d_cull);
+  cudaFree(ctx->d_piece);
+  cudaFree(ctx->cs.hist);
+  cudaFree(ctx->cs.bin);
+  cudaFree(ctx->cs.rank);
+  cudaFree(ctx->cs.Xs);
+  cudaFree(ctx->cs.order);
+  cudaFree(ctx->cs.Ep);
+  cudaFree(ctx->cs.Gp);
   cudaFree(ctx->d_in);
   cudaFree(ctx->d_out);
   if (ctx->h_in) cudaFreeHost(ctx->h_in);
@@ -542,6 +815,28 @@ int mmo_set_tiles(mmo_ctx* ctx, int kp, int threads, int chunks) {
   ctx->tile_kp = kp;
   ctx->tile_threads = threads;
   ctx->tile_chunks = chunks;
+  return MMO_OK;
+}
+
+int mmo_set_cull(mmo_ctx* ctx, int mode, double row_spacing, int piece_atoms,
+                 int entries_per_lane) {
+  if (!ctx) return MMO_EINVAL;
+  if ((mode != 0 && mode != 1) || piece_atoms < 0 || piece_atoms > (1 << 20) ||
+      !(entries_per_lane == 0 || entries_per_lane == 1 || entries_per_lane == 2 ||
+        entries_per_lane == 4) ||
+      !std::isfinite(row_spacing) || (row_spacing > 0 && (row_spacing < 0.25 || row_spacing > 64)))
+    return fail(ctx, MMO_EINVAL,
+                "cull: mode 0 or 1, row spacing in [0.25, 64] A (<= 0: default), piece atoms "
+                ">= 0, entries per lane in {0,1,2,4}");
+  ctx->cull_mode = mode;
+  ctx->cull_piece = piece_atoms;
+  ctx->cull_kp = entries_per_lane;
+  const double h = row_spacing > 0 ? row_spacing : 2.0;
+  if (h != ctx->cull_h) {
+    ctx->cull_h = h;
+    MMO_CK(cudaSetDevice(ctx->device), "set device");
+    return build_cull(ctx);
+  }
   return MMO_OK;
 }
 
@@ -618,7 +913,20 @@ int mmo_set_protein(mmo_ctx* ctx, int n, const double* xs, const double* ys, con
     ctx->origin[d] = (double)of[d];
     ctx->origin_f[d] = of[d];
   }
-  return MMO_OK;
+  ctx->pxs.resize(n);
+  ctx->pys.resize(n);
+  ctx->pzs.resize(n);
+  ctx->pkq.resize(n);
+  ctx->ptypes.resize(n);
+  for (int i = 0; i < n; ++i) {
+    ctx->pxs[i] = xs[i] - (double)of[0];
+    ctx->pys[i] = ys[i] - (double)of[1];
+    ctx->pzs[i] = zs[i] - (double)of[2];
+    ctx->pkq[i] = (float)(kElec * q[i]);
+    ctx->ptypes[i] = type[i];
+  }
+  ++ctx->prot_version;
+  return build_cull(ctx);
 }
 
 int mmo_set_ligand(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
@@ -823,9 +1131,31 @@ int mmo_set_profiling(mmo_ctx* ctx, int on) {
 int mmo_stage_times(mmo_ctx* ctx, float* ms) {
   if (!ctx || !ms) return MMO_EINVAL;
   if (!ctx->ev_valid) return fail(ctx, MMO_ESTATE, "no profiled scoring call yet");
-  MMO_CK(cudaEventSynchronize(ctx->ev[3]), "event sync");
-  for (int k = 0; k < 3; ++k)
-    MMO_CK(cudaEventElapsedTime(&ms[k], ctx->ev[k], ctx->ev[k + 1]), "elapsed");
+  MMO_CK(cudaEventSynchronize(ctx->ev[4]), "event sync");
+  MMO_CK(cudaEventElapsedTime(&ms[0], ctx->ev[0], ctx->ev[1]), "elapsed");
+  MMO_CK(cudaEventElapsedTime(&ms[1], ctx->ev[2], ctx->ev[3]), "elapsed");
+  MMO_CK(cudaEventElapsedTime(&ms[2], ctx->ev[3], ctx->ev[4]), "elapsed");
+  MMO_CK(cudaEventElapsedTime(&ms[3], ctx->ev[1], ctx->ev[2]), "elapsed");
+  return MMO_OK;
+}
+
+int mmo_last_launches(const mmo_ctx* ctx, int* kernels) {
+  if (!ctx || !kernels) return MMO_EINVAL;
+  *kernels = ctx->last_launches;
+  return MMO_OK;
+}
+
+int mmo_pair_count(mmo_ctx* ctx, double* evaluated, double* all) {
+  if (!ctx || !evaluated || !all) return MMO_EINVAL;
+  *all = ctx->last_pairs;
+  *evaluated = ctx->last_pairs;
+  if (ctx->last_cull) {
+    unsigned long long n = 0;
+    MMO_CK(cudaSetDevice(ctx->device), "set device");
+    MMO_CK(cudaDeviceSynchronize(), "device sync");
+    MMO_CK(cudaMemcpy(&n, ctx->d_queue + 2, sizeof n, cudaMemcpyDeviceToHost), "pair count");
+    *evaluated = (double)n;
+  }
   return MMO_OK;
 }
 

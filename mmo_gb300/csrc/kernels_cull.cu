@@ -1,0 +1,389 @@
+// kernels_cull.cu -- the cut-off sweep of the shifted form
+// (Mol.ene_inter_UFF_shifted_bst, UnixJunkie/MMO src/mol.ml:928-962: the
+// reference visits, for each ligand atom, only the protein atoms that its
+// bisector-tree neighbour query returns within 12 A).  Here the query is made for a
+// group of 32 * KP (pose, ligand atom) entries at once:
+//
+//   k_cull_bin      entry -> (ligand type segment, Morton cell of its position)
+//   k_cull_scan     bin counts -> first slot of each bin (one CTA per segment)
+//   k_cull_scatter  entries copied into slot order
+//   k_pairs_cull    persistent CTAs, protein resident in shared memory (TMA
+//                   bulk copy); a warp takes (group, protein piece) items from
+//                   a work counter, bounds its group by a box and sweeps the
+//                   rows of the piece that come within 12 A of the box
+//   k_cull_reduce   sums the pieces of each entry in piece order
+//
+// Slot order only decides which entries share a warp.  Skipped pairs add
+// exact zeros and the FP32 partials are flushed at fixed rows, so the result
+// of an entry is the same whichever entries share its group.
+#include "mmo_internal.cuh"
+
+namespace mmo {
+namespace {
+
+constexpr uint32_t kWaitPolls = 1u << 22;
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {  // 5 bits -> every third bit
+  v &= 0x1fu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+__device__ __forceinline__ int grid_cell(float v, float lo, float inv) {
+  // NaN converts to 0; the clamp keeps infinities and far entries on the grid
+  return min(max(__float2int_rd((v - lo) * inv), 0), kCullGrid - 1);
+}
+
+__global__ void k_cull_bin(const float4* __restrict__ X, int n, int L,
+                           const int* __restrict__ seg_of_atom, DevCull cull, unsigned* hist,
+                           int* bin, int* rank) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const float4 h = X[2 * (size_t)e];
+  const uint32_t cx = grid_cell(h.x, cull.glo[0], cull.ginv);
+  const uint32_t cy = grid_cell(h.y, cull.glo[1], cull.ginv);
+  const uint32_t cz = grid_cell(h.z, cull.glo[2], cull.ginv);
+  const int b = seg_of_atom[e % L] * kCullBins +
+                (int)(spread3(cx) | (spread3(cy) << 1) | (spread3(cz) << 2));
+  bin[e] = b;
+  rank[e] = (int)atomicAdd(&hist[b], 1u);
+}
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanPer = kCullBins / kScanThreads;
+
+__global__ void __launch_bounds__(kScanThreads) k_cull_scan(unsigned* hist, CullSegs seg,
+                                                             unsigned* queue) {
+  __shared__ unsigned wsum[kScanThreads / 32];
+  unsigned* h = hist + (size_t)blockIdx.x * kCullBins + threadIdx.x * kScanPer;
+  unsigned loc[kScanPer];
+  unsigned s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    loc[k] = h[k];
+    s += loc[k];
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned inc = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned v = __shfl_up_sync(kFull, inc, o);
+    if (lane >= o) inc += v;
+  }
+  if (lane == 31) wsum[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    unsigned v = wsum[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned u = __shfl_up_sync(kFull, v, o);
+      if (lane >= o) v += u;
+    }
+    wsum[lane] = v;  // inclusive over warps
+  }
+  __syncthreads();
+  unsigned run = (unsigned)seg.off[blockIdx.x] + (w ? wsum[w - 1] : 0u) + inc - s;
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    h[k] = run;
+    run += loc[k];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    queue[0] = 0u;
+    *reinterpret_cast<unsigned long long*>(queue + 2) = 0ull;
+  }
+}
+
+__global__ void k_cull_scatter(const float4* __restrict__ X, int n, int L,
+                               const float* __restrict__ lig_q, const unsigned* __restrict__ hist,
+                               const int* __restrict__ bin, const int* __restrict__ rank,
+                               float4* Xs, int* order) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const int slot = (int)hist[bin[e]] + rank[e];
+  const float4 h = X[2 * (size_t)e], l = X[2 * (size_t)e + 1];
+  Xs[2 * (size_t)slot] = make_float4(h.x, h.y, h.z, lig_q[e % L]);
+  Xs[2 * (size_t)slot + 1] = make_float4(l.x, l.y, l.z, 0.f);
+  order[slot] = e;
+}
+
+// dE/dX of one entry over the protein atoms [a0, a1) with the per-pair test
+// of the 0.01 A clamp; the same arithmetic in the same order as the sweep, so
+// entries without a clamped pair get the sweep's value bit for bit.
+template <int DIEL>
+__device__ __noinline__ float3 cull_exact_grad(const float4* sp, const float4* trow, int a0, int a1,
+                                               float q, float xh, float yh, float zh, float xl,
+                                               float yl, float zl) {
+  constexpr float c0 = DIEL == 0 ? -10.0f : -4.0f;
+  float acc = 0.f, gx = 0.f, gy = 0.f, gz = 0.f, mn = 1e30f;
+  for (int i = a0; i < a1; ++i) {
+    const float4 p = sp[2 * i], pl = sp[2 * i + 1];
+    const float4 pv = trow[__float_as_int(pl.w)];
+    pair_step<true, DIEL, 0, true>(xh, yh, zh, xl, yl, zl, p, pl, p.w * q, pv.x, pv.y, pv.z, c0,
+                                   acc, gx, gy, gz, mn);
+  }
+  return make_float3(gx, gy, gz);
+}
+
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
+__device__ __forceinline__ float warp_maxf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
+
+template <int KP, bool GRAD, int DIEL>
+__global__ void __launch_bounds__(512)
+    k_pairs_cull(DevCull cull, const float4* __restrict__ tabv, CullSegs seg, CullScratch cs,
+                 int* err) {
+  extern __shared__ __align__(16) float4 sp[];  // [P][2], then the tables below
+  __shared__ __align__(8) uint64_t bar;
+  const int P = cull.P, nrows = cull.nrows, npieces = cs.npieces;
+  float4* s_rbox = sp + 2 * P;
+  float4* s_tab = s_rbox + nrows;                       // [ptype][ltype] (X, 1/D, c1, 0)
+  int* s_rs = reinterpret_cast<int*>(s_tab + kNTypes * kNTypes);
+  int* s_flush = s_rs + nrows + 1;
+  int* s_piece = s_flush + nrows;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    const uint32_t bytes = (uint32_t)P * 32u;
+    mbar_expect_tx(&bar, bytes);
+    constexpr uint32_t kPiece = 32768u;
+    for (uint32_t off = 0; off < bytes; off += kPiece) {
+      const uint32_t n = bytes - off < kPiece ? bytes - off : kPiece;
+      bulk_g2s(reinterpret_cast<char*>(sp) + off, reinterpret_cast<const char*>(cull.atoms) + off,
+               n, &bar);
+    }
+  }
+  for (int k = threadIdx.x; k < nrows; k += blockDim.x) {
+    s_rbox[k] = cull.row_box[k];
+    s_flush[k] = cull.row_flush[k];
+  }
+  for (int k = threadIdx.x; k <= nrows; k += blockDim.x) s_rs[k] = cull.row_start[k];
+  for (int k = threadIdx.x; k <= npieces; k += blockDim.x) s_piece[k] = cs.piece_row[k];
+  for (int k = threadIdx.x; k < kNTypes * kNTypes; k += blockDim.x) {
+    const float4 v = tabv[k];
+    s_tab[k] = make_float4(v.x, v.y, (DIEL == 0 ? 11.0f : 5.0f) * v.y, 0.f);
+  }
+  __syncthreads();
+  if (!mbar_wait(&bar, 0, kWaitPolls)) {
+    if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
+    mbar_wait(&bar, 0, kWaitPolls);
+    return;
+  }
+
+  constexpr float c0v = DIEL == 0 ? -10.0f : -4.0f;
+  constexpr int G = 32 * KP;
+  const int lane = threadIdx.x & 31;
+  const int nitems = seg.off[seg.nseg] / G * npieces;
+  for (;;) {
+    int item = 0;
+    if (lane == 0) item = (int)atomicAdd(cs.queue, 1u);
+    item = __shfl_sync(kFull, item, 0);
+    if (item >= nitems) break;
+    const int g = item / npieces;
+    const int pc = item - g * npieces;
+    const int slot0 = g * G;
+    int t = 0;
+    while (t + 1 < seg.nseg && slot0 >= seg.off[t + 1]) ++t;
+    const int s_end = seg.off[t] + seg.n[t];
+    const float4* trow = s_tab + seg.type[t];  // + ptype * kNTypes (stored in the atom)
+
+    float xh[KP], yh[KP], zh[KP], xl[KP], yl[KP], zl[KP], q[KP];
+    float acc[KP], gx[KP], gy[KP], gz[KP];
+    double ad[KP];
+    float blx = 1e30f, bly = 1e30f, blz = 1e30f, bhx = -1e30f, bhy = -1e30f, bhz = -1e30f;
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
+      const int s = min(slot0 + k * 32 + lane, s_end - 1);
+      const float4 h = cs.Xs[2 * (size_t)s], l = cs.Xs[2 * (size_t)s + 1];
+      xh[k] = h.x;
+      yh[k] = h.y;
+      zh[k] = h.z;
+      q[k] = h.w;
+      xl[k] = l.x;
+      yl[k] = l.y;
+      zl[k] = l.z;
+      acc[k] = gx[k] = gy[k] = gz[k] = 0.f;
+      ad[k] = 0.0;
+      blx = fminf(blx, h.x);
+      bly = fminf(bly, h.y);
+      blz = fminf(blz, h.z);
+      bhx = fmaxf(bhx, h.x);
+      bhy = fmaxf(bhy, h.y);
+      bhz = fmaxf(bhz, h.z);
+    }
+    blx = warp_min(blx);
+    bly = warp_min(bly);
+    blz = warp_min(blz);
+    bhx = warp_maxf(bhx);
+    bhy = warp_maxf(bhy);
+    bhz = warp_maxf(bhz);
+
+    float mn = 1e30f;
+    int visited = 0;
+    const int r0 = s_piece[pc], r1 = s_piece[pc + 1];
+    for (int r = r0; r < r1; ++r) {
+      const float4 rb = s_rbox[r];
+      const float dy = fmaxf(fmaxf(rb.x - bhy, bly - rb.y), 0.f);
+      const float dz = fmaxf(fmaxf(rb.z - bhz, blz - rb.w), 0.f);
+      const float d2 = fmaf(dy, dy, dz * dz);
+      if (d2 < kCullR2) {
+        const float w = sqrtf(kCullR2 - d2);
+        const float xlo = blx - w, xhi = bhx + w;
+        const int a = s_rs[r], b = s_rs[r + 1];
+        int nlo = 0, nhi = 0;
+        for (int i0 = a; i0 < b; i0 += 32) {
+          const int i = i0 + lane;
+          const float x = i < b ? sp[2 * i].x : 3.0e38f;
+          nlo += __popc(__ballot_sync(kFull, x < xlo));
+          nhi += __popc(__ballot_sync(kFull, x <= xhi));
+        }
+        visited += nhi - nlo;
+#pragma unroll 2
+        for (int i = a + nlo; i < a + nhi; ++i) {
+          const float4 p = sp[2 * i], pl = sp[2 * i + 1];
+          const float4 pv = trow[__float_as_int(pl.w)];
+#pragma unroll
+          for (int k = 0; k < KP; ++k)
+            pair_step<GRAD, DIEL, 0>(xh[k], yh[k], zh[k], xl[k], yl[k], zl[k], p, pl, p.w * q[k],
+                                     pv.x, pv.y, pv.z, c0v, acc[k], gx[k], gy[k], gz[k], mn);
+        }
+      }
+      if (s_flush[r]) {
+#pragma unroll
+        for (int k = 0; k < KP; ++k) {
+          ad[k] += (double)acc[k];
+          acc[k] = 0.f;
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < KP; ++k) ad[k] += (double)acc[k];
+    if (GRAD && __any_sync(kFull, mn < kMinR2)) {
+      // a pair closer than 0.01 A, where the clamped distance makes the
+      // derivative 0: redo the gradient over the piece with the per-pair test
+      const int a0 = s_rs[r0], a1 = s_rs[r1];
+#pragma unroll
+      for (int k = 0; k < KP; ++k) {
+        const float3 gg = cull_exact_grad<DIEL>(sp, trow, a0, a1, q[k], xh[k], yh[k], zh[k], xl[k],
+                                                yl[k], zl[k]);
+        gx[k] = gg.x;
+        gy[k] = gg.y;
+        gz[k] = gg.z;
+      }
+    }
+    if (lane == 0 && visited) atomicAdd(cs.pairs, (unsigned long long)visited * G);
+    constexpr float gs = DIEL == 0 ? -1.0f : -2.0f;
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
+      const int s = slot0 + k * 32 + lane;
+      if (s < s_end) {
+        const size_t o = (size_t)pc * cs.slots + s;
+        cs.Ep[o] = ad[k];
+        if (GRAD) cs.Gp[o] = make_float4(gs * gx[k], gs * gy[k], gs * gz[k], 0.f);
+      }
+    }
+  }
+}
+
+__global__ void k_cull_reduce(CullSegs seg, CullScratch cs, double* Epart, float4* Gpart,
+                              int grad) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= seg.off[seg.nseg]) return;
+  int t = 0;
+  while (t + 1 < seg.nseg && s >= seg.off[t + 1]) ++t;
+  if (s >= seg.off[t] + seg.n[t]) return;  // padding slot
+  const int e = cs.order[s];
+  double E = 0.0;
+  float gx = 0.f, gy = 0.f, gz = 0.f;
+  for (int pc = 0; pc < cs.npieces; ++pc) {
+    const size_t o = (size_t)pc * cs.slots + s;
+    E += cs.Ep[o];
+    if (grad) {
+      const float4 g = cs.Gp[o];
+      gx += g.x;
+      gy += g.y;
+      gz += g.z;
+    }
+  }
+  // an entry at a non-finite position can fall in a group far from the protein
+  const float4 h = cs.Xs[2 * (size_t)s];
+  if (!isfinite(h.x) || !isfinite(h.y) || !isfinite(h.z)) E = __longlong_as_double(0x7ff8000000000000ll);
+  Epart[e] = E;
+  if (grad) Gpart[e] = make_float4(gx, gy, gz, 0.f);
+}
+
+using CullFn = void (*)(DevCull, const float4*, CullSegs, CullScratch, int*);
+
+template <int KP>
+CullFn pick_kp(bool grad, int diel) {
+  if (grad) return diel ? k_pairs_cull<KP, true, 1> : k_pairs_cull<KP, true, 0>;
+  return diel ? k_pairs_cull<KP, false, 1> : k_pairs_cull<KP, false, 0>;
+}
+
+CullFn pick_cull(int kp, bool grad, const Physics& ph) {
+  const int d = ph.dielectric ? 1 : 0;
+  switch (kp) {
+    case 1: return pick_kp<1>(grad, d);
+    case 2: return pick_kp<2>(grad, d);
+    default: return pick_kp<4>(grad, d);
+  }
+}
+
+}  // namespace
+
+int cull_smem_bytes(int P, int nrows, int npieces) {
+  const long b = 32L * P + 16L * nrows + 16L * kNTypes * kNTypes + 4L * (nrows + 1) + 4L * nrows +
+                 4L * (npieces + 1);
+  return (int)((b + 15) / 16 * 16);
+}
+
+int cull_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_bytes) {
+  CullFn fn = pick_cull(kp, grad != 0, ph);
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes) !=
+      cudaSuccess)
+    return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, smem_bytes) != cudaSuccess)
+    return 0;
+  return nb;
+}
+
+cudaError_t launch_cull_sort(const DevCull& cull, const Scratch& s, const float* lig_q, int B,
+                             int L, const CullSegs& seg, const CullScratch& cs, cudaStream_t st) {
+  const int n = B * L;
+  if (n <= 0) return cudaSuccess;
+  const int tb = 256, nb = (n + tb - 1) / tb;
+  k_cull_bin<<<nb, tb, 0, st>>>(s.X, n, L, cs.seg_of_atom, cull, cs.hist, cs.bin, cs.rank);
+  k_cull_scan<<<seg.nseg, kScanThreads, 0, st>>>(cs.hist, seg, cs.queue);
+  k_cull_scatter<<<nb, tb, 0, st>>>(s.X, n, L, lig_q, cs.hist, cs.bin, cs.rank, cs.Xs, cs.order);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pairs_cull(const DevCull& cull, const float4* tab, const CullSegs& seg,
+                              const CullScratch& cs, int flags, const Physics& ph,
+                              const CullPlan& plan, int* d_err, cudaStream_t st) {
+  CullFn fn = pick_cull(plan.kp, (flags & kFlagGrad) != 0, ph);
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, plan.smem);
+  if (e != cudaSuccess) return e;
+  fn<<<plan.blocks, plan.threads, plan.smem, st>>>(cull, tab, seg, cs, d_err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cull_reduce(const CullSegs& seg, const CullScratch& cs, const Scratch& s,
+                               int grad, cudaStream_t st) {
+  const int n = seg.off[seg.nseg];
+  if (n <= 0) return cudaSuccess;
+  k_cull_reduce<<<(n + 255) / 256, 256, 0, st>>>(seg, cs, s.Epart, s.Gpart, grad);
+  return cudaGetLastError();
+}
+
+}  // namespace mmo

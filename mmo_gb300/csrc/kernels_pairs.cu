@@ -22,49 +22,6 @@ namespace {
 constexpr int kFlush = 256;  // protein atoms per FP32 partial before the FP64 add
 constexpr uint32_t kWaitPolls = 1u << 22;
 
-// One pair: ligand atom (hi/lo) against protein atom p (hi, K q) / pl (lo).
-// With Dp6 = (X / r^2)^3 = D p6 (X = D^(1/3) x^2) and p6 = Dp6 / D:
-//   lj = Dp6 (Dp6 / D - 2),  e = lj + el,
-//   -(2 dE/dr2 unswitched) r2     = e - Dp6 (10 - 11 p6)        (eps = 4)
-//   -(2 dE/dr2 unswitched) r2 / 2 = e - Dp6 (4 - 5 p6)          (eps = 4 r)
-// so nt below is -t (eps 4) or -t/2 (eps 4r) and g accumulates -dE/dd or
-// -dE/dd / 2 (the caller rescales); (c1, c0) = (11/D, -10) or (5/D, -4).
-// mn tracks the smallest r2 for the 0.01 A clamp check.
-template <bool GRAD, int DIEL, int FORM>
-__device__ __forceinline__ void pair_step(float xh, float yh, float zh, float xl, float yl,
-                                          float zl, float4 p, float4 pl, float qq, float X,
-                                          float invD, float c1, float c0, float& acc, float& gx,
-                                          float& gy, float& gz, float& mn) {
-  const float dx = (xh - p.x) + (xl - pl.x);
-  const float dy = (yh - p.y) + (yl - pl.y);
-  const float dz = (zh - p.z) + (zl - pl.z);
-  const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-  const float r2c = fmaxf(r2, kMinR2);
-  const float ir = rsqrtf(r2c);
-  const float ir2 = ir * ir;
-  const float P = X * ir2;
-  const float Dp6 = (P * P) * P;
-  const float lj = Dp6 * fmaf(Dp6, invD, -2.0f);
-  const float e = fmaf(qq, DIEL == 0 ? ir : ir2, lj);
-  float s = 1.0f;
-  if (FORM == 0) {
-    s = fmaxf(fmaf(r2c, -1.0f / 144.0f, 1.0f), 0.0f);
-    acc = fmaf(s * s, e, acc);
-  } else {
-    acc += e;
-  }
-  if (GRAD) {
-    const float nt = fmaf(Dp6, fmaf(Dp6, c1, c0), e);
-    const float na = nt * ir2;
-    float g = na;
-    if (FORM == 0) g = s * fmaf(s, na, e * (DIEL == 0 ? 1.0f / 36.0f : 1.0f / 72.0f));
-    mn = fminf(mn, r2);
-    gx = fmaf(g, dx, gx);
-    gy = fmaf(g, dy, gy);
-    gz = fmaf(g, dz, gz);
-  }
-}
-
 // dE/dX of one pose for the protein atoms [c0, c1) with the per-pair test
 // of the 0.01 A clamp (rarely needed, so kept out of the main loop's registers)
 template <int DIEL, int FORM>

@@ -69,6 +69,7 @@ struct DevLigand {
   const int* nb_off;        // [L + 1] both-direction CSR of the same pairs
   const int* nb_idx;        // partner atom
   const float4* nb_par;     // (x^2, D, K q_i q_j, 0)
+  const int* seg_of_atom;   // [L] rank of the atom's type among the ligand's types
 };
 
 // Per-pose work buffers, pose-major so the warp-per-pose kernels read them
@@ -113,6 +114,65 @@ struct PairPlan {
   int blocks;    // persistent grid size
 };
 
+// ---- cut-off sweep (shifted form) ----------------------------------------
+// The shifted form is exactly 0 beyond 12 A (s = max(1 - r^2/144, 0)), and
+// in a pocket most ligand-protein pairs lie beyond it.  The cut-off sweep
+// groups the (pose, ligand atom) entries of a batch by ligand type and by
+// position, bounds each group of 32 * KP entries by a box, and visits only the
+// protein atoms within 12 A of the box, found through a row index of the
+// protein.  Pairs it skips have r^2 > kCullR2, where the switched term and its
+// derivative are exactly 0 in FP32, and it accumulates in a fixed order over
+// fixed pieces of the protein, so an entry's result does not depend on which
+// entries share its group.
+constexpr int kCullGrid = 32;                                   // entry binning cells per axis
+constexpr int kCullBins = kCullGrid * kCullGrid * kCullGrid;    // Morton-ordered cells
+constexpr float kCullR2 = 145.0f;  // visit radius^2: 1 - r^2/144 < 0 in FP32 beyond it
+constexpr int kCullFlush = 256;    // protein atoms per FP32 partial before the FP64 add
+
+// The protein ordered in rows of a (y, z) grid of spacing h: row order (iz, iy)
+// with empty rows dropped, atoms in a row sorted by x.
+struct DevCull {
+  const float4* atoms;       // [P][2]: (x_hi, y_hi, z_hi, K q), (x_lo, y_lo, z_lo, type * kNTypes as int bits)
+  const int* row_start;      // [nrows + 1]
+  const float4* row_box;     // [nrows] (y_min, y_max, z_min, z_max) of the row's atoms
+  const int* row_flush;      // [nrows] 1: add the FP32 partial to the FP64 sum after this row
+  int P, nrows;
+  float glo[3];              // entry binning grid origin and cells per A
+  float ginv;
+};
+
+// Per-call description of the entry groups: the entries of ligand type
+// segment t fill slots [off[t], off[t] + n[t]), the segment padded to a
+// multiple of the group size G = 32 * kp.
+struct CullSegs {
+  int nseg;
+  int G;
+  int off[kNTypes + 1];
+  int n[kNTypes];
+  int type[kNTypes];
+};
+
+struct CullScratch {
+  unsigned* hist;        // [nseg * kCullBins] counts, then slot cursors
+  int* bin;              // [B * L] entry -> bin
+  int* rank;             // [B * L] entry -> rank in its bin
+  float4* Xs;            // [slots][2] entries in slot order: (x, y, z hi, q), (x, y, z lo, 0)
+  int* order;            // [slots] slot -> entry b * L + j
+  double* Ep;            // [npieces][slots] energy per protein piece
+  float4* Gp;            // [npieces][slots] -dE/dX (scaled) per protein piece
+  unsigned* queue;       // work counter of the sweep
+  unsigned long long* pairs;  // pair evaluations of the sweep (32 * KP per visited atom)
+  const int* seg_of_atom;  // [L] ligand atom -> type segment
+  const int* piece_row;  // [npieces + 1] first row of each protein piece
+  int slots, npieces;
+};
+
+struct CullPlan {
+  int kp, threads, blocks;
+  int piece_atoms;
+  int smem;              // dynamic shared memory of the sweep
+};
+
 // ---- launchers (defined in the .cu files) --------------------------------
 cudaError_t launch_rebuild(const DevLigand& lig, const PoseIO& io, const Scratch& s, int flags,
                            cudaStream_t st);
@@ -130,6 +190,17 @@ cudaError_t launch_reduce_plain(const double* Epart, int n, double* out, cudaStr
 cudaError_t launch_intra_plain(const DevLigand& lig, const float4* X, int form, int dielectric,
                                double* out, cudaStream_t st);
 int pairs_batched_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_bytes);
+// entry sort of the cut-off sweep: bin, scan, scatter (hist must be zeroed)
+cudaError_t launch_cull_sort(const DevCull& cull, const Scratch& s, const float* lig_q, int B,
+                             int L, const CullSegs& seg, const CullScratch& cs, cudaStream_t st);
+cudaError_t launch_pairs_cull(const DevCull& cull, const float4* tab, const CullSegs& seg,
+                              const CullScratch& cs, int flags, const Physics& ph,
+                              const CullPlan& plan, int* d_err, cudaStream_t st);
+// sums the pieces of each slot into Epart / Gpart (one chunk) of its entry
+cudaError_t launch_cull_reduce(const CullSegs& seg, const CullScratch& cs, const Scratch& s,
+                               int grad, cudaStream_t st);
+int cull_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_bytes);
+int cull_smem_bytes(int P, int nrows, int npieces);
 cudaError_t launch_fma_peak(int sms, int iters, float* out, cudaStream_t st, double* flops);
 
 // ---- device helpers ------------------------------------------------------
@@ -216,6 +287,50 @@ __device__ __forceinline__ void uff_pair_eg(float dx, float dy, float dz, float 
   if (FORM == 0) g = fmaf(s * (-1.0f / 36.0f), e, g);
   e_out = w * e;
   g_out = r2 < kMinR2 ? 0.0f : g;
+}
+
+// One pair: ligand atom (hi/lo) against protein atom p (hi, K q) / pl (lo).
+// With Dp6 = (X / r^2)^3 = D p6 (X = D^(1/3) x^2) and p6 = Dp6 / D:
+//   lj = Dp6 (Dp6 / D - 2),  e = lj + el,
+//   -(2 dE/dr2 unswitched) r2     = e - Dp6 (10 - 11 p6)        (eps = 4)
+//   -(2 dE/dr2 unswitched) r2 / 2 = e - Dp6 (4 - 5 p6)          (eps = 4 r)
+// so nt below is -t (eps 4) or -t/2 (eps 4r) and g accumulates -dE/dd or
+// -dE/dd / 2 (the caller rescales); (c1, c0) = (11/D, -10) or (5/D, -4).
+// mn tracks the smallest r2 for the 0.01 A clamp check.
+template <bool GRAD, int DIEL, int FORM, bool MASK = false>
+__device__ __forceinline__ void pair_step(float xh, float yh, float zh, float xl, float yl,
+                                          float zl, float4 p, float4 pl, float qq, float X,
+                                          float invD, float c1, float c0, float& acc, float& gx,
+                                          float& gy, float& gz, float& mn) {
+  const float dx = (xh - p.x) + (xl - pl.x);
+  const float dy = (yh - p.y) + (yl - pl.y);
+  const float dz = (zh - p.z) + (zl - pl.z);
+  const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+  const float r2c = fmaxf(r2, kMinR2);
+  const float ir = rsqrtf(r2c);
+  const float ir2 = ir * ir;
+  const float P = X * ir2;
+  const float Dp6 = (P * P) * P;
+  const float lj = Dp6 * fmaf(Dp6, invD, -2.0f);
+  const float e = fmaf(qq, DIEL == 0 ? ir : ir2, lj);
+  float s = 1.0f;
+  if (FORM == 0) {
+    s = fmaxf(fmaf(r2c, -1.0f / 144.0f, 1.0f), 0.0f);
+    acc = fmaf(s * s, e, acc);
+  } else {
+    acc += e;
+  }
+  if (GRAD) {
+    const float nt = fmaf(Dp6, fmaf(Dp6, c1, c0), e);
+    const float na = nt * ir2;
+    float g = na;
+    if (FORM == 0) g = s * fmaf(s, na, e * (DIEL == 0 ? 1.0f / 36.0f : 1.0f / 72.0f));
+    if (MASK) g = r2 < kMinR2 ? 0.0f : g;  // clamped distance: derivative 0
+    mn = fminf(mn, r2);
+    gx = fmaf(g, dx, gx);
+    gy = fmaf(g, dy, gy);
+    gz = fmaf(g, dz, gz);
+  }
 }
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {

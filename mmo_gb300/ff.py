@@ -103,6 +103,11 @@ class UFFScorer:
     def set_tiles(self, poses_per_lane=0, threads=0, chunks=0) -> None:
         self._check(self._lib.mmo_set_tiles(self._h, poses_per_lane, threads, chunks))
 
+    def set_cull(self, mode=0, row_spacing=0.0, piece_atoms=0, entries_per_lane=0) -> None:
+        """Cut-off sweep of the shifted form: mode 0 automatic, 1 off."""
+        self._check(self._lib.mmo_set_cull(self._h, mode, float(row_spacing), piece_atoms,
+                                           entries_per_lane))
+
     def sms(self) -> int:
         out = C.c_int()
         self._check(self._lib.mmo_device_sms(self._h, C.byref(out)))
@@ -195,10 +200,23 @@ class UFFScorer:
         self._check(self._lib.mmo_set_profiling(self._h, int(on)))
 
     def stage_times(self):
-        """(rebuild, pair sweep, finish) device ms of the last scoring call."""
-        ms = (C.c_float * 3)()
+        """(rebuild, pair sweep, finish, entry sort) device ms of the last
+        scoring call."""
+        ms = (C.c_float * 4)()
         self._check(self._lib.mmo_stage_times(self._h, ms))
         return tuple(float(v) for v in ms)
+
+    def pair_count(self):
+        """(pairs evaluated, all pairs) of the last batched scoring call."""
+        ev, al = C.c_double(), C.c_double()
+        self._check(self._lib.mmo_pair_count(self._h, C.byref(ev), C.byref(al)))
+        return ev.value, al.value
+
+    def last_launches(self) -> int:
+        """Kernels the last scoring call launched."""
+        n = C.c_int()
+        self._check(self._lib.mmo_last_launches(self._h, C.byref(n)))
+        return n.value
 
     def fp32_peak_tflops(self) -> float:
         t, ms = C.c_double(), C.c_double()

@@ -37,9 +37,12 @@ SIGNATURES = {
     "mmo_score_poses_noalloc": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp, _vp]),
     "mmo_sync": (_i, [_vp, _vp]),
     "mmo_set_tiles": (_i, [_vp, _i, _i, _i]),
+    "mmo_set_cull": (_i, [_vp, _i, C.c_double, _i, _i]),
     "mmo_device_sms": (_i, [_vp, _P(_i)]),
     "mmo_set_profiling": (_i, [_vp, _i]),
     "mmo_stage_times": (_i, [_vp, _P(C.c_float)]),
+    "mmo_pair_count": (_i, [_vp, _P(C.c_double), _P(C.c_double)]),
+    "mmo_last_launches": (_i, [_vp, _P(C.c_int)]),
     "mmo_fp32_fma_peak": (_i, [_vp, _P(_d), _P(_d)]),
 }
 

@@ -168,12 +168,72 @@ def test_batched_physics_variants(oracle, scorer_factory, batch, phys):
                                                (4, 256, 17), (2, 256, 64)])
 def test_tile_shapes_agree(scorer_factory, batch, kp, threads, chunks):
     s = scorer_factory(batch.pocket, batch.ligand)
+    s.set_cull(mode=1)  # the full sweep, whose tiles these are
     d = batch.poses[:200]
     E0, G0, _ = s.score_poses(d, grad=True)
     s.set_tiles(kp, threads, chunks)
     E1, G1, _ = s.score_poses(d, grad=True)
     assert np.abs(E1 - E0).max() <= 1e-6 * np.abs(E0).max()
     assert np.abs(G1 - G0).max() <= 1e-5 * np.abs(G0).max()
+
+
+# -- cut-off sweep of the shifted form ----------------------------------------------
+
+@pytest.mark.parametrize("diel", [0, 1])
+def test_cull_matches_full_sweep(scorer_factory, batch, diel):
+    from mmo_gb300.ff import Physics
+
+    s = scorer_factory(batch.pocket, batch.ligand, Physics(diel, 0, 0, 0))
+    d = batch.poses
+    E0, G0, st0 = s.score_poses(d, grad=True)
+    s.set_cull(mode=1)
+    E1, G1, st1 = s.score_poses(d, grad=True)
+    assert np.array_equal(st0, st1)
+    assert np.abs(E1 - E0).max() <= 1e-6 * np.abs(E0).max()
+    err = np.abs(G1 - G0).max(axis=1) / np.abs(G0).max(axis=1)
+    assert err.max() <= 1e-5
+
+
+@pytest.mark.parametrize("h,piece,kp", [(1.0, 256, 4), (2.0, 1024, 2), (3.0, 0, 1),
+                                        (0.5, 64, 4), (1.5, 100000, 2)])
+def test_cull_parameters_agree(oracle, scorer_factory, batch, h, piece, kp):
+    s = scorer_factory(batch.pocket, batch.ligand)
+    d = batch.poses[:96]
+    E0, G0, _ = s.score_poses(d, grad=True)
+    s.set_cull(0, h, piece, kp)
+    E1, G1, _ = s.score_poses(d, grad=True)
+    assert np.abs(E1 - E0).max() <= 1e-6 * np.abs(E0).max()
+    assert (np.abs(G1 - G0).max(axis=1) / np.abs(G0).max(axis=1)).max() <= 1e-5
+    E64, G64, _, scale = ref_batch(oracle, batch, d[:24], grad=True)
+    assert_energy(E1[:24], E64, scale)
+    assert_grad(G1[:24], G64)
+
+
+def test_cull_result_independent_of_grouping(scorer_factory, batch):
+    """A pose's energy and gradient do not depend on the other poses of the
+    batch: the cut-off sweep groups entries by position, and a reordered or
+    smaller batch forms other groups, but skipped pairs add exact zeros and the
+    partial sums break at fixed protein rows."""
+    s = scorer_factory(batch.pocket, batch.ligand)
+    d = batch.poses
+    E, G, _ = s.score_poses(d, grad=True)
+    perm = np.random.default_rng(5).permutation(len(d))
+    Ep, Gp, _ = s.score_poses(d[perm], grad=True)
+    assert np.array_equal(Ep, E[perm]) and np.array_equal(Gp, G[perm])
+    Es, Gs, _ = s.score_poses(d[17:50], grad=True)
+    assert np.array_equal(Es, E[17:50]) and np.array_equal(Gs, G[17:50])
+
+
+def test_cull_non_finite_pose(scorer_factory, batch):
+    s = scorer_factory(batch.pocket, batch.ligand)
+    d = batch.poses[:64].copy()
+    E0, G0, _ = s.score_poses(d, grad=True)
+    d[5, 0] = np.nan
+    E, G, st = s.score_poses(d, grad=True, inter=True, intra=False)
+    assert np.isnan(E[5]) and (st[5] & 2)
+    E1, _, _ = s.score_poses(batch.poses[:64], grad=True, inter=True, intra=False)
+    keep = np.arange(64) != 5
+    assert np.array_equal(E[keep], E1[keep])
 
 
 def test_deterministic(scorer_factory, batch):
