@@ -229,6 +229,10 @@ def main():
         sc.score_poses_device(d_dofs.data_ptr(), B, d_E.data_ptr(), d_G.data_ptr(),
                               d_st.data_ptr(), flags, sp)
 
+    # launch plan from the autotuner (times the candidate plans on this batch)
+    tune_ms = sc.tune_device(d_dofs.data_ptr(), B, d_E.data_ptr(), d_G.data_ptr(),
+                             d_st.data_ptr(), flags, sp)
+    plan = sc.plan()
     # warm-up (also builds the launch plan and scratch)
     for _ in range(max(args.warmup, 3)):
         flush.zero_()
@@ -327,7 +331,8 @@ def main():
                    "torsions": nrb, "pocket_atoms": P,
                    "precision": "fp32 pair terms, fp64 per-pose sums",
                    "l2": "flushed before every timed step (256 MiB write), not timed",
-                   "parallelism": "dp%d (poses sharded, no collective)" % world},
+                   "parallelism": "dp%d (poses sharded, no collective)" % world,
+                   "plan": dict(plan, tuned_ms=tune_ms)},
         "e2e": {"value": e2e_val, "unit": "poses/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": launches * args.steps,

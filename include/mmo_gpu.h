@@ -140,8 +140,10 @@ int mmo_score_poses_noalloc(mmo_ctx* ctx, int B, const float* d_dofs, int flags,
  * (MMO_ETIMEOUT). */
 int mmo_sync(mmo_ctx* ctx, void* stream);
 
-/* Tile shape of the batched pair kernel: poses per lane (1, 2, 4), threads
- * per CTA (256, 512) and protein chunks per pose (0: automatic).  Setting 0
+/* Tile shape of the batched pair kernels: poses per lane (1, 2, 4) and
+ * protein chunks per pose (0: automatic) of the full sweep, and threads per
+ * CTA (256, 512, 768, 1024; the full sweep runs at most 512, the cut-off
+ * sweep at most 1024, 768 or 512 for 1, 2 or 4 entries per lane).  Setting 0
  * for all restores the automatic choice. */
 int mmo_set_tiles(mmo_ctx* ctx, int poses_per_lane, int threads, int chunks);
 
@@ -155,6 +157,31 @@ int mmo_set_tiles(mmo_ctx* ctx, int poses_per_lane, int threads, int chunks);
  * work item (0: 256); entries_per_lane: 1, 2, 4 (0: 2). */
 int mmo_set_cull(mmo_ctx* ctx, int mode, double row_spacing, int piece_atoms,
                  int entries_per_lane);
+
+/* Autotuner of the batched pair sweep (no counterpart in the reference).
+ * Times launch plans on this batch and keeps the fastest as the context's
+ * settings (mmo_set_cull, mmo_set_tiles): under the shifted form the cut-off
+ * sweep's row spacing (1.5, 2, 3 A), entries per lane (1, 2, 4) and piece
+ * size (256, 512 atoms) against the full sweep's poses per lane (1, 2, 4) and
+ * protein chunks (4 to 24); under the global form the full sweep's plans.
+ * Arguments as mmo_score_poses_device, whose outputs it leaves as computed by
+ * the chosen plan.  With a cache file (mmo_set_tune_cache) a plan recorded
+ * there for the same shape (poses, ligand atoms, torsions, protein atoms,
+ * physics, gradient) is applied without timing (*ms = -1) and a timed one is
+ * appended.  Each candidate runs 4 times; the call synchronises the stream.
+ * Refused inside a stream capture (MMO_ESTATE).  *ms (may be NULL): device
+ * milliseconds of one call with the chosen plan. */
+int mmo_tune(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E, float* d_grad,
+             int* d_status, void* stream, double* ms);
+
+/* File of tuned plans for mmo_tune, one line per shape; NULL or "" for none. */
+int mmo_set_tune_cache(mmo_ctx* ctx, const char* path);
+
+/* Plan of the last batched call: *path 1 for the cut-off sweep, 0 for the
+ * full sweep; entries (or poses) per lane; threads per CTA; piece atoms (or
+ * protein chunks per pose); the row spacing of the protein index. */
+int mmo_get_plan(const mmo_ctx* ctx, int* path, int* per_lane, int* threads,
+                 int* piece_or_chunks, double* row_spacing);
 
 /* Number of SMs of the context's device (for callers that size batches). */
 int mmo_device_sms(const mmo_ctx* ctx, int* out);

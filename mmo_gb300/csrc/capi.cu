@@ -116,7 +116,8 @@ struct mmo_ctx {
   long cplan_key[10] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
   int* d_piece = nullptr;
   size_t capPiece = 0, capHist = 0, capBin = 0, capRank = 0, capXs = 0, capOrd = 0, capEp = 0,
-         capGp = 0;
+         capGp = 0, capArr = 0, capVis = 0;
+  std::string tune_cache;        // file of tuned plans (mmo_set_tune_cache)
   unsigned* d_queue = nullptr;  // [0] work counter, [2..3] pair evaluations (u64)
   bool last_cull = false;       // the last call's inter term used the cut-off sweep
   double last_pairs = 0;        // poses x ligand atoms x protein atoms of the last call
@@ -438,7 +439,7 @@ int build_cull(mmo_ctx* ctx) {
   for (int k = 0; k < n; ++k) {
     const int i = idx[k];
     split_store(&atoms[2 * (size_t)k], ctx->pxs[i], ctx->pys[i], ctx->pzs[i], ctx->pkq[i]);
-    const int tb = ctx->ptypes[i] * kNTypes;
+    const int tb = ctx->ptypes[i] * kNTypes * (int)sizeof(float4);
     memcpy(&atoms[2 * (size_t)k + 1].w, &tb, sizeof tb);
     if (k == 0 || key[i] != key[idx[k - 1]]) {
       if (k) {
@@ -508,7 +509,7 @@ PairPlan plan_for(mmo_ctx* ctx, int B, bool grad) {
 PairPlan make_plan(mmo_ctx* ctx, int B, bool grad) {
   PairPlan p{};
   p.kp = ctx->tile_kp ? ctx->tile_kp : (B >= 4096 ? 4 : (B >= 256 ? 2 : 1));
-  p.threads = ctx->tile_threads ? ctx->tile_threads : 512;
+  p.threads = std::min(ctx->tile_threads ? ctx->tile_threads : 512, 512);
   const int P = ctx->prot.P, L = ctx->lig.L;
   const int nslices = (P + kSliceAtoms - 1) / kSliceAtoms;
   const int slice_len = (P + nslices - 1) / nslices;
@@ -556,7 +557,7 @@ int cull_plan_for(mmo_ctx* ctx, int B, bool grad) {
   if (std::equal(key, key + 10, ctx->cplan_key)) return MMO_OK;
   CullPlan p{};
   p.kp = ctx->cull_kp ? ctx->cull_kp : 2;
-  p.threads = ctx->tile_threads ? ctx->tile_threads : 512;
+  p.threads = std::min(ctx->tile_threads ? ctx->tile_threads : 1024, cull_max_threads(p.kp));
   p.piece_atoms = ctx->cull_piece ? ctx->cull_piece : 256;
   const std::vector<int>& rs = ctx->cull_rows;
   const int nrows = (int)rs.size() - 1;
@@ -619,6 +620,12 @@ int ensure_cull_scratch(mmo_ctx* ctx, int B, int L, bool grad) {
   if (grad &&
       (r = grow(ctx, (void**)&c.Gp, &ctx->capGp, sizeof(float4) * np * slots, "piece gradients")))
     return r;
+  const size_t groups = slots / sg.G;
+  if ((r = grow(ctx, (void**)&c.arrive, &ctx->capArr, sizeof(int) * groups, "group arrivals")))
+    return r;
+  if ((r = grow(ctx, (void**)&c.vis, &ctx->capVis, groups * np, "piece flags"))) return r;
+  c.Eout = ctx->scr.Epart;
+  c.Gout = ctx->scr.Gpart;
   c.queue = ctx->d_queue;
   c.pairs = reinterpret_cast<unsigned long long*>(ctx->d_queue + 2);
   c.seg_of_atom = ctx->lig.seg_of_atom;
@@ -648,8 +655,8 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
   const bool cull = inter && use_cull(ctx, B);
   ctx->last_cull = cull;
   ctx->last_pairs = inter ? (double)B * L * ctx->prot.P : 0.0;
-  // rebuild + finish, and the sweep: entry bin, scan, scatter, sweep, piece sum
-  ctx->last_launches = 2 + (cull ? 5 : (inter ? 1 : 0));
+  // rebuild + finish, and the sweep: entry bin, scan, scatter, sweep
+  ctx->last_launches = 2 + (cull ? 4 : (inter ? 1 : 0));
   PairPlan plan{};
   int C = 1;
   int r;
@@ -694,7 +701,6 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
                              st),
            "cut-off pair kernel");
     MMO_CK(mark(3), "event");
-    MMO_CK(launch_cull_reduce(sg, ctx->cs, ctx->scr, grad, st), "piece reduction kernel");
   } else {
     MMO_CK(mark(2), "event");
     if (inter) {
@@ -787,6 +793,8 @@ int mmo_ctx_destroy(mmo_ctx* ctx) {
   cudaFree(ctx->cs.order);
   cudaFree(ctx->cs.Ep);
   cudaFree(ctx->cs.Gp);
+  cudaFree(ctx->cs.arrive);
+  cudaFree(ctx->cs.vis);
   cudaFree(ctx->d_in);
   cudaFree(ctx->d_out);
   if (ctx->h_in) cudaFreeHost(ctx->h_in);
@@ -810,8 +818,10 @@ int mmo_set_physics(mmo_ctx* ctx, int dielectric, int mixing, int inter_form, in
 int mmo_set_tiles(mmo_ctx* ctx, int kp, int threads, int chunks) {
   if (!ctx) return MMO_EINVAL;
   if (!(kp == 0 || kp == 1 || kp == 2 || kp == 4) ||
-      !(threads == 0 || threads == 256 || threads == 512) || chunks < 0 || chunks > 4096)
-    return fail(ctx, MMO_EINVAL, "tiles: poses_per_lane in {0,1,2,4}, threads in {0,256,512}");
+      !(threads == 0 || threads == 256 || threads == 512 || threads == 768 || threads == 1024) ||
+      chunks < 0 || chunks > 4096)
+    return fail(ctx, MMO_EINVAL,
+                "tiles: poses_per_lane in {0,1,2,4}, threads in {0,256,512,768,1024}");
   ctx->tile_kp = kp;
   ctx->tile_threads = threads;
   ctx->tile_chunks = chunks;
@@ -1106,6 +1116,160 @@ int mmo_score_poses_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, 
   MMO_CK(cudaSetDevice(ctx->device), "set device");
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   return score_device(ctx, B, d_dofs, flags, d_E, d_grad, d_status, ctx->d_err, 0, st);
+}
+
+namespace {
+
+// One launch plan of the batched pair sweep as the tuner sets it.
+struct TunePlan {
+  int cull;       // 1: cut-off sweep, 0: full sweep
+  double h;       // row spacing (cut-off)
+  int kp;         // entries per lane (cut-off) or poses per lane (full)
+  int piece;      // protein atoms per piece (cut-off)
+  int threads;
+  int chunks;     // protein chunks per pose (full)
+};
+
+void apply_plan(mmo_ctx* ctx, const TunePlan& p, int* r) {
+  ctx->cull_mode = p.cull ? 0 : 1;
+  ctx->cull_kp = p.cull ? p.kp : 0;
+  ctx->cull_piece = p.cull ? p.piece : 0;
+  ctx->tile_kp = p.cull ? 0 : p.kp;
+  ctx->tile_chunks = p.cull ? 0 : p.chunks;
+  ctx->tile_threads = p.threads;
+  *r = MMO_OK;
+  if (p.cull && p.h != ctx->cull_h) {
+    ctx->cull_h = p.h;
+    *r = build_cull(ctx);
+  }
+}
+
+std::string tune_key(const mmo_ctx* ctx, int B, bool grad) {
+  char k[160];
+  snprintf(k, sizeof k, "%d %d %d %d %d %d %d %d %d", B, ctx->lig.L, ctx->lig.nrb, ctx->prot.P,
+           ctx->ph.dielectric, ctx->ph.mixing, ctx->ph.inter_form, ctx->ph.intra_form,
+           grad ? 1 : 0);
+  return k;
+}
+
+bool tune_lookup(const std::string& path, const std::string& key, TunePlan* p) {
+  FILE* f = fopen(path.c_str(), "r");
+  if (!f) return false;
+  char line[512];
+  bool found = false;
+  while (fgets(line, sizeof line, f)) {
+    const char* colon = strchr(line, ':');
+    if (line[0] == '#' || !colon) continue;
+    std::string k(line, colon - line);
+    while (!k.empty() && k.back() == ' ') k.pop_back();
+    TunePlan q{};
+    double ms;
+    if (k == key && sscanf(colon + 1, "%d %lf %d %d %d %d %lf", &q.cull, &q.h, &q.kp, &q.piece,
+                           &q.threads, &q.chunks, &ms) == 7) {
+      *p = q;  // the last line for a key wins
+      found = true;
+    }
+  }
+  fclose(f);
+  return found;
+}
+
+}  // namespace
+
+int mmo_set_tune_cache(mmo_ctx* ctx, const char* path) {
+  if (!ctx) return MMO_EINVAL;
+  ctx->tune_cache = path ? path : "";
+  return MMO_OK;
+}
+
+int mmo_get_plan(const mmo_ctx* ctx, int* path, int* per_lane, int* threads, int* chunks_or_piece,
+                 double* row_spacing) {
+  if (!ctx || !path || !per_lane || !threads || !chunks_or_piece || !row_spacing)
+    return MMO_EINVAL;
+  *path = ctx->last_cull ? 1 : 0;
+  *per_lane = ctx->last_cull ? ctx->cplan.kp : ctx->plan.kp;
+  *threads = ctx->last_cull ? ctx->cplan.threads : ctx->plan.threads;
+  *chunks_or_piece = ctx->last_cull ? ctx->cplan.piece_atoms : ctx->plan.C;
+  *row_spacing = ctx->cull_h;
+  return MMO_OK;
+}
+
+int mmo_tune(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E, float* d_grad,
+             int* d_status, void* stream, double* ms_out) {
+  if (!ctx) return MMO_EINVAL;
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  MMO_CK(cudaStreamIsCapturing(st, &cap), "capture status");
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(ctx, MMO_ESTATE, "mmo_tune times launches and cannot run inside a stream capture");
+  const bool grad = flags & MMO_F_GRAD;
+  const bool inter = (flags & MMO_F_INTER) && ctx->prot.P > 0;
+  auto run = [&]() {
+    return score_device(ctx, B, d_dofs, flags, d_E, d_grad, d_status, ctx->d_err, 0, st);
+  };
+  const std::string key = tune_key(ctx, B, grad);
+  TunePlan best{};
+  int r = MMO_OK;
+  if (!ctx->tune_cache.empty() && tune_lookup(ctx->tune_cache, key, &best)) {
+    apply_plan(ctx, best, &r);
+    if (r || (r = run())) return r;
+    if (ms_out) *ms_out = -1.0;
+    return MMO_OK;
+  }
+  std::vector<TunePlan> cands;
+  if (inter && B >= 2) {
+    if (ctx->ph.inter_form == 0 && ctx->cull_ok)
+      for (double h : {1.5, 2.0, 3.0})
+        for (int kp : {1, 2, 4})
+          for (int piece : {256, 512}) {
+            cands.push_back({1, h, kp, piece, cull_max_threads(kp), 0});
+            if (cull_max_threads(kp) != 512) cands.push_back({1, h, kp, piece, 512, 0});
+          }
+    for (int kp : {1, 2, 4})
+      for (int ch : {4, 8, 12, 16, 24}) cands.push_back({0, ctx->cull_h, kp, 0, 512, ch});
+  }
+  if (cands.empty()) {  // nothing to choose: the plain call
+    if ((r = run())) return r;
+    if (ms_out) *ms_out = -1.0;
+    return MMO_OK;
+  }
+  cudaEvent_t a, b;
+  MMO_CK(cudaEventCreate(&a), "event");
+  MMO_CK(cudaEventCreate(&b), "event");
+  float best_ms = 3e38f;
+  for (const TunePlan& c : cands) {
+    apply_plan(ctx, c, &r);
+    if (r || (r = run()) || cudaStreamSynchronize(st) != cudaSuccess) continue;  // plan unusable
+    float t[3];
+    bool ok = true;
+    for (float& v : t) {
+      ok = ok && cudaEventRecord(a, st) == cudaSuccess && run() == MMO_OK &&
+           cudaEventRecord(b, st) == cudaSuccess && cudaEventSynchronize(b) == cudaSuccess &&
+           cudaEventElapsedTime(&v, a, b) == cudaSuccess;
+    }
+    if (!ok) continue;
+    std::sort(t, t + 3);
+    if (t[1] < best_ms) {
+      best_ms = t[1];
+      best = c;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  ctx->err.clear();
+  if (best_ms >= 3e38f) return fail(ctx, MMO_ECUDA, "mmo_tune: no launch plan ran");
+  apply_plan(ctx, best, &r);
+  if (r || (r = run())) return r;
+  if (ms_out) *ms_out = best_ms;
+  if (!ctx->tune_cache.empty()) {
+    if (FILE* f = fopen(ctx->tune_cache.c_str(), "a")) {
+      fprintf(f, "%s : %d %.3f %d %d %d %d %.4f\n", key.c_str(), best.cull, best.h, best.kp,
+              best.piece, best.threads, best.chunks, best_ms);
+      fclose(f);
+    }
+  }
+  return MMO_OK;
 }
 
 int mmo_sync(mmo_ctx* ctx, void* stream) {

@@ -11,7 +11,8 @@
 //                   bulk copy); a warp takes (group, protein piece) items from
 //                   a work counter, bounds its group by a box and sweeps the
 //                   rows of the piece that come within 12 A of the box
-//   k_cull_reduce   sums the pieces of each entry in piece order
+//                   and the last piece of a group to finish sums the group's
+//                   pieces in piece order
 //
 // Slot order only decides which entries share a warp.  Skipped pairs add
 // exact zeros and the FP32 partials are flushed at fixed rows, so the result
@@ -53,20 +54,30 @@ __global__ void k_cull_bin(const float4* __restrict__ X, int n, int L,
 }
 
 constexpr int kScanThreads = 1024;
-constexpr int kScanPer = kCullBins / kScanThreads;
+constexpr int kScanPer = kCullBins / kScanThreads;  // 32 consecutive bins per thread
+constexpr int kScanSmem = kScanThreads * (kScanPer + 1) * 4;  // padded rows: no bank conflicts
 
+// Exclusive scan of one segment's bin counts into first slots: coalesced
+// loads into shared memory, a serial scan of 32 consecutive bins per thread
+// and one block scan of the thread sums.  Also clears the work counter, the
+// pair counter and the groups' arrival counters of the sweep.
 __global__ void __launch_bounds__(kScanThreads) k_cull_scan(unsigned* hist, CullSegs seg,
-                                                             unsigned* queue) {
+                                                             unsigned* queue, int* arrive,
+                                                             int narrive) {
+  extern __shared__ unsigned sh[];  // [kScanThreads][kScanPer + 1]
   __shared__ unsigned wsum[kScanThreads / 32];
-  unsigned* h = hist + (size_t)blockIdx.x * kCullBins + threadIdx.x * kScanPer;
-  unsigned loc[kScanPer];
+  unsigned* h = hist + (size_t)blockIdx.x * kCullBins;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+#pragma unroll 8
+  for (int k = 0; k < kScanPer; ++k) {
+    const int i = k * kScanThreads + t;
+    sh[(i / kScanPer) * (kScanPer + 1) + i % kScanPer] = h[i];
+  }
+  __syncthreads();
+  unsigned* row = sh + t * (kScanPer + 1);
   unsigned s = 0;
 #pragma unroll
-  for (int k = 0; k < kScanPer; ++k) {
-    loc[k] = h[k];
-    s += loc[k];
-  }
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int k = 0; k < kScanPer; ++k) s += row[k];
   unsigned inc = s;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -88,10 +99,18 @@ __global__ void __launch_bounds__(kScanThreads) k_cull_scan(unsigned* hist, Cull
   unsigned run = (unsigned)seg.off[blockIdx.x] + (w ? wsum[w - 1] : 0u) + inc - s;
 #pragma unroll
   for (int k = 0; k < kScanPer; ++k) {
-    h[k] = run;
-    run += loc[k];
+    const unsigned c = row[k];
+    row[k] = run;
+    run += c;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  __syncthreads();
+#pragma unroll 8
+  for (int k = 0; k < kScanPer; ++k) {
+    const int i = k * kScanThreads + t;
+    h[i] = sh[(i / kScanPer) * (kScanPer + 1) + i % kScanPer];
+  }
+  for (int k = blockIdx.x * blockDim.x + t; k < narrive; k += gridDim.x * blockDim.x) arrive[k] = 0;
+  if (blockIdx.x == 0 && t == 0) {
     queue[0] = 0u;
     *reinterpret_cast<unsigned long long*>(queue + 2) = 0ull;
   }
@@ -121,7 +140,8 @@ __device__ __noinline__ float3 cull_exact_grad(const float4* sp, const float4* t
   float acc = 0.f, gx = 0.f, gy = 0.f, gz = 0.f, mn = 1e30f;
   for (int i = a0; i < a1; ++i) {
     const float4 p = sp[2 * i], pl = sp[2 * i + 1];
-    const float4 pv = trow[__float_as_int(pl.w)];
+    const float4 pv = *reinterpret_cast<const float4*>(reinterpret_cast<const char*>(trow) +
+                                                       __float_as_int(pl.w));
     pair_step<true, DIEL, 0, true>(xh, yh, zh, xl, yl, zl, p, pl, p.w * q, pv.x, pv.y, pv.z, c0,
                                    acc, gx, gy, gz, mn);
   }
@@ -140,7 +160,7 @@ __device__ __forceinline__ float warp_maxf(float v) {
 }
 
 template <int KP, bool GRAD, int DIEL>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(cull_max_threads(KP))
     k_pairs_cull(DevCull cull, const float4* __restrict__ tabv, CullSegs seg, CullScratch cs,
                  int* err) {
   extern __shared__ __align__(16) float4 sp[];  // [P][2], then the tables below
@@ -194,7 +214,7 @@ __global__ void __launch_bounds__(512)
     int t = 0;
     while (t + 1 < seg.nseg && slot0 >= seg.off[t + 1]) ++t;
     const int s_end = seg.off[t] + seg.n[t];
-    const float4* trow = s_tab + seg.type[t];  // + ptype * kNTypes (stored in the atom)
+    const float4* trow = s_tab + seg.type[t];  // + the byte offset of the protein type's row
 
     float xh[KP], yh[KP], zh[KP], xl[KP], yl[KP], zl[KP], q[KP];
     float acc[KP], gx[KP], gy[KP], gz[KP];
@@ -236,7 +256,10 @@ __global__ void __launch_bounds__(512)
       const float dz = fmaxf(fmaxf(rb.z - bhz, blz - rb.w), 0.f);
       const float d2 = fmaf(dy, dy, dz * dz);
       if (d2 < kCullR2) {
-        const float w = sqrtf(kCullR2 - d2);
+        // sqrt(kCullR2 - d2) from one reciprocal square root, rounded up: a
+        // wider window only visits more atoms
+        const float x = kCullR2 - d2;
+        const float w = fmaf(x, rsqrtf(x), 1e-3f);
         const float xlo = blx - w, xhi = bhx + w;
         const int a = s_rs[r], b = s_rs[r + 1];
         int nlo = 0, nhi = 0;
@@ -247,10 +270,12 @@ __global__ void __launch_bounds__(512)
           nhi += __popc(__ballot_sync(kFull, x <= xhi));
         }
         visited += nhi - nlo;
+        const float4* pe = sp + 2 * (a + nhi);
 #pragma unroll 2
-        for (int i = a + nlo; i < a + nhi; ++i) {
-          const float4 p = sp[2 * i], pl = sp[2 * i + 1];
-          const float4 pv = trow[__float_as_int(pl.w)];
+        for (const float4* pp = sp + 2 * (a + nlo); pp < pe; pp += 2) {
+          const float4 p = pp[0], pl = pp[1];
+          const float4 pv = *reinterpret_cast<const float4*>(
+              reinterpret_cast<const char*>(trow) + __float_as_int(pl.w));
 #pragma unroll
           for (int k = 0; k < KP; ++k)
             pair_step<GRAD, DIEL, 0>(xh[k], yh[k], zh[k], xl[k], yl[k], zl[k], p, pl, p.w * q[k],
@@ -282,43 +307,54 @@ __global__ void __launch_bounds__(512)
     }
     if (lane == 0 && visited) atomicAdd(cs.pairs, (unsigned long long)visited * G);
     constexpr float gs = DIEL == 0 ? -1.0f : -2.0f;
+    if (visited) {  // a piece out of range of the group adds nothing
 #pragma unroll
-    for (int k = 0; k < KP; ++k) {
-      const int s = slot0 + k * 32 + lane;
-      if (s < s_end) {
-        const size_t o = (size_t)pc * cs.slots + s;
-        cs.Ep[o] = ad[k];
-        if (GRAD) cs.Gp[o] = make_float4(gs * gx[k], gs * gy[k], gs * gz[k], 0.f);
+      for (int k = 0; k < KP; ++k) {
+        const int s = slot0 + k * 32 + lane;
+        if (s < s_end) {
+          const size_t o = (size_t)pc * cs.slots + s;
+          cs.Ep[o] = ad[k];
+          if (GRAD) cs.Gp[o] = make_float4(gs * gx[k], gs * gy[k], gs * gz[k], 0.f);
+        }
+      }
+    }
+    // the last piece of the group to finish sums the group's pieces in piece
+    // order (the arrival order does not matter)
+    if (lane == 0) cs.vis[(size_t)g * npieces + pc] = visited ? 1 : 0;
+    __threadfence();  // every lane's partials before the arrival
+    __syncwarp();
+    int last = 0;
+    if (lane == 0) last = atomicAdd(&cs.arrive[g], 1) == npieces - 1;
+    last = __shfl_sync(kFull, last, 0);
+    if (last) {
+      __threadfence();
+      const uint8_t* vg = cs.vis + (size_t)g * npieces;
+#pragma unroll
+      for (int k = 0; k < KP; ++k) {
+        const int s = slot0 + k * 32 + lane;
+        if (s >= s_end) continue;
+        double E = 0.0;
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+        for (int q2 = 0; q2 < npieces; ++q2) {
+          if (!__ldcg(vg + q2)) continue;
+          const size_t o = (size_t)q2 * cs.slots + s;
+          E += __ldcg(cs.Ep + o);
+          if (GRAD) {
+            const float4 g4 = __ldcg(cs.Gp + o);
+            sx += g4.x;
+            sy += g4.y;
+            sz += g4.z;
+          }
+        }
+        // an entry at a non-finite position can fall in a group far from the protein
+        if (!isfinite(xh[k]) || !isfinite(yh[k]) || !isfinite(zh[k]))
+          E = __longlong_as_double(0x7ff8000000000000ll);
+        const int e = cs.order[s];
+        cs.Eout[e] = E;
+        if (GRAD) cs.Gout[e] = make_float4(sx, sy, sz, 0.f);
       }
     }
   }
-}
-
-__global__ void k_cull_reduce(CullSegs seg, CullScratch cs, double* Epart, float4* Gpart,
-                              int grad) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= seg.off[seg.nseg]) return;
-  int t = 0;
-  while (t + 1 < seg.nseg && s >= seg.off[t + 1]) ++t;
-  if (s >= seg.off[t] + seg.n[t]) return;  // padding slot
-  const int e = cs.order[s];
-  double E = 0.0;
-  float gx = 0.f, gy = 0.f, gz = 0.f;
-  for (int pc = 0; pc < cs.npieces; ++pc) {
-    const size_t o = (size_t)pc * cs.slots + s;
-    E += cs.Ep[o];
-    if (grad) {
-      const float4 g = cs.Gp[o];
-      gx += g.x;
-      gy += g.y;
-      gz += g.z;
-    }
-  }
-  // an entry at a non-finite position can fall in a group far from the protein
-  const float4 h = cs.Xs[2 * (size_t)s];
-  if (!isfinite(h.x) || !isfinite(h.y) || !isfinite(h.z)) E = __longlong_as_double(0x7ff8000000000000ll);
-  Epart[e] = E;
-  if (grad) Gpart[e] = make_float4(gx, gy, gz, 0.f);
 }
 
 using CullFn = void (*)(DevCull, const float4*, CullSegs, CullScratch, int*);
@@ -363,7 +399,11 @@ cudaError_t launch_cull_sort(const DevCull& cull, const Scratch& s, const float*
   if (n <= 0) return cudaSuccess;
   const int tb = 256, nb = (n + tb - 1) / tb;
   k_cull_bin<<<nb, tb, 0, st>>>(s.X, n, L, cs.seg_of_atom, cull, cs.hist, cs.bin, cs.rank);
-  k_cull_scan<<<seg.nseg, kScanThreads, 0, st>>>(cs.hist, seg, cs.queue);
+  cudaError_t e = cudaFuncSetAttribute(k_cull_scan, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       kScanSmem);
+  if (e != cudaSuccess) return e;
+  k_cull_scan<<<seg.nseg, kScanThreads, kScanSmem, st>>>(cs.hist, seg, cs.queue, cs.arrive,
+                                                         seg.off[seg.nseg] / seg.G);
   k_cull_scatter<<<nb, tb, 0, st>>>(s.X, n, L, lig_q, cs.hist, cs.bin, cs.rank, cs.Xs, cs.order);
   return cudaGetLastError();
 }
@@ -375,14 +415,6 @@ cudaError_t launch_pairs_cull(const DevCull& cull, const float4* tab, const Cull
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, plan.smem);
   if (e != cudaSuccess) return e;
   fn<<<plan.blocks, plan.threads, plan.smem, st>>>(cull, tab, seg, cs, d_err);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_cull_reduce(const CullSegs& seg, const CullScratch& cs, const Scratch& s,
-                               int grad, cudaStream_t st) {
-  const int n = seg.off[seg.nseg];
-  if (n <= 0) return cudaSuccess;
-  k_cull_reduce<<<(n + 255) / 256, 256, 0, st>>>(seg, cs, s.Epart, s.Gpart, grad);
   return cudaGetLastError();
 }
 

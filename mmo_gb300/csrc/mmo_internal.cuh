@@ -132,7 +132,9 @@ constexpr int kCullFlush = 256;    // protein atoms per FP32 partial before the 
 // The protein ordered in rows of a (y, z) grid of spacing h: row order (iz, iy)
 // with empty rows dropped, atoms in a row sorted by x.
 struct DevCull {
-  const float4* atoms;       // [P][2]: (x_hi, y_hi, z_hi, K q), (x_lo, y_lo, z_lo, type * kNTypes as int bits)
+  const float4* atoms;       // [P][2]: (x_hi, y_hi, z_hi, K q), (x_lo, y_lo, z_lo, w): w holds the
+                             // int bits of type * kNTypes * 16, the byte offset of the type's
+                             // row in the shared pair table
   const int* row_start;      // [nrows + 1]
   const float4* row_box;     // [nrows] (y_min, y_max, z_min, z_max) of the row's atoms
   const int* row_flush;      // [nrows] 1: add the FP32 partial to the FP64 sum after this row
@@ -162,10 +164,17 @@ struct CullScratch {
   float4* Gp;            // [npieces][slots] -dE/dX (scaled) per protein piece
   unsigned* queue;       // work counter of the sweep
   unsigned long long* pairs;  // pair evaluations of the sweep (32 * KP per visited atom)
+  int* arrive;           // [groups] pieces of the group done
+  uint8_t* vis;          // [groups][npieces] 1: the piece came within 12 A of the group
+  double* Eout;          // [B * L] inter energy per entry (Scratch::Epart, one chunk)
+  float4* Gout;          // [B * L] dE/dX per entry (Scratch::Gpart, one chunk)
   const int* seg_of_atom;  // [L] ligand atom -> type segment
   const int* piece_row;  // [npieces + 1] first row of each protein piece
   int slots, npieces;
 };
+
+// threads per CTA of the cut-off sweep: the register budget of KP entries per lane
+constexpr int cull_max_threads(int kp) { return kp == 1 ? 1024 : (kp == 2 ? 768 : 512); }
 
 struct CullPlan {
   int kp, threads, blocks;
@@ -196,9 +205,6 @@ cudaError_t launch_cull_sort(const DevCull& cull, const Scratch& s, const float*
 cudaError_t launch_pairs_cull(const DevCull& cull, const float4* tab, const CullSegs& seg,
                               const CullScratch& cs, int flags, const Physics& ph,
                               const CullPlan& plan, int* d_err, cudaStream_t st);
-// sums the pieces of each slot into Epart / Gpart (one chunk) of its entry
-cudaError_t launch_cull_reduce(const CullSegs& seg, const CullScratch& cs, const Scratch& s,
-                               int grad, cudaStream_t st);
 int cull_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_bytes);
 int cull_smem_bytes(int P, int nrows, int npieces);
 cudaError_t launch_fma_peak(int sms, int iters, float* out, cudaStream_t st, double* flops);

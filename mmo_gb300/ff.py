@@ -108,6 +108,30 @@ class UFFScorer:
         self._check(self._lib.mmo_set_cull(self._h, mode, float(row_spacing), piece_atoms,
                                            entries_per_lane))
 
+    def tune_device(self, d_dofs: int, B: int, d_E: int, d_grad: int | None, d_status: int,
+                    flags: int, stream: int | None = None) -> float:
+        """Autotune the batched sweep on this device batch (mmo_tune); returns
+        the chosen plan's device ms (-1 when taken from the cache file)."""
+        ms = C.c_double()
+        self._check(self._lib.mmo_tune(self._h, B, d_dofs, flags, d_E, d_grad or None, d_status,
+                                       stream, C.byref(ms)))
+        return ms.value
+
+    def set_tune_cache(self, path: str | None) -> None:
+        self._check(self._lib.mmo_set_tune_cache(self._h, (path or "").encode()))
+
+    def plan(self) -> dict:
+        """Launch plan of the last batched call."""
+        v = [C.c_int() for _ in range(4)]
+        h = C.c_double()
+        self._check(self._lib.mmo_get_plan(self._h, *[C.byref(x) for x in v], C.byref(h)))
+        path, lane, threads, pc = (x.value for x in v)
+        if path == 1:
+            return {"sweep": "cut-off", "entries_per_lane": lane, "threads": threads,
+                    "piece_atoms": pc, "row_spacing_A": h.value}
+        return {"sweep": "full", "poses_per_lane": lane, "threads": threads,
+                "protein_chunks": pc}
+
     def sms(self) -> int:
         out = C.c_int()
         self._check(self._lib.mmo_device_sms(self._h, C.byref(out)))

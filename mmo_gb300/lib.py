@@ -38,6 +38,10 @@ SIGNATURES = {
     "mmo_sync": (_i, [_vp, _vp]),
     "mmo_set_tiles": (_i, [_vp, _i, _i, _i]),
     "mmo_set_cull": (_i, [_vp, _i, C.c_double, _i, _i]),
+    "mmo_tune": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp, _vp, _P(C.c_double)]),
+    "mmo_set_tune_cache": (_i, [_vp, C.c_char_p]),
+    "mmo_get_plan": (_i, [_vp, _P(C.c_int), _P(C.c_int), _P(C.c_int), _P(C.c_int),
+                          _P(C.c_double)]),
     "mmo_device_sms": (_i, [_vp, _P(_i)]),
     "mmo_set_profiling": (_i, [_vp, _i]),
     "mmo_stage_times": (_i, [_vp, _P(C.c_float)]),
