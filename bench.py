@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=0,
                     help="poses in the CPU-baseline sample (0: about 10 s of work)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep the default launch plan instead of the autotuner's")
     return ap.parse_args()
 
 
@@ -230,9 +232,10 @@ def main():
                               d_st.data_ptr(), flags, sp)
 
     # launch plan from the autotuner (times the candidate plans on this batch)
-    tune_ms = sc.tune_device(d_dofs.data_ptr(), B, d_E.data_ptr(), d_G.data_ptr(),
-                             d_st.data_ptr(), flags, sp)
-    plan = sc.plan()
+    tune_ms = None
+    if not args.no_tune:
+        tune_ms = sc.tune_device(d_dofs.data_ptr(), B, d_E.data_ptr(), d_G.data_ptr(),
+                                 d_st.data_ptr(), flags, sp)
     # warm-up (also builds the launch plan and scratch)
     for _ in range(max(args.warmup, 3)):
         flush.zero_()
@@ -262,6 +265,7 @@ def main():
     clk = clocks.stop()
     sc.set_profiling(False)
     sc.sync(sp)
+    plan = sc.plan()
     launches = sc.last_launches()
     pairs_ev, pairs_all = sc.pair_count()
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]

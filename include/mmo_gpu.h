@@ -153,7 +153,7 @@ int mmo_set_tiles(mmo_ctx* ctx, int poses_per_lane, int threads, int chunks);
  * automatic, used for batches of 2 or more poses under the shifted form when
  * the protein and its row index fit in shared memory; mode 1: off, every pair
  * is evaluated.  row_spacing: (y, z) spacing of the protein's row index in A
- * (<= 0: 2; a change rebuilds the index); piece_atoms: protein atoms per
+ * (<= 0: 3; a change rebuilds the index); piece_atoms: protein atoms per
  * work item (0: 256); entries_per_lane: 1, 2, 4 (0: 2). */
 int mmo_set_cull(mmo_ctx* ctx, int mode, double row_spacing, int piece_atoms,
                  int entries_per_lane);

@@ -101,7 +101,7 @@ struct mmo_ctx {
 
   // cut-off sweep of the shifted form (mmo_set_cull)
   int cull_mode = 0;        // 0: automatic, 1: off
-  double cull_h = 2.0;      // row spacing of the protein index, A
+  double cull_h = 3.0;      // row spacing of the protein index, A
   int cull_piece = 0;       // protein atoms per piece, 0: automatic
   int cull_kp = 0;          // entries per lane, 0: automatic
   bool cull_ok = false;     // row index built and resident in shared memory
@@ -410,7 +410,7 @@ int build_cull(mmo_ctx* ctx) {
       hi[d] = std::max(hi[d], v[d]);
     }
   }
-  double h = ctx->cull_h > 0 ? ctx->cull_h : 2.0;
+  double h = ctx->cull_h > 0 ? ctx->cull_h : 3.0;
   long ny = 0, nz = 0;
   for (;;) {
     ny = (long)std::floor((hi[1] - lo[1]) / h) + 1;
@@ -459,6 +459,11 @@ int build_cull(mmo_ctx* ctx) {
   rflush.push_back(1);
   rs.push_back(n);
   const int nrows = (int)rbox.size();
+  // flag -> end of the flush block that holds the row
+  for (int r = nrows - 1, end = nrows; r >= 0; --r) {
+    if (rflush[r]) end = r + 1;
+    rflush[r] = end;
+  }
   size_t off = 0;
   const size_t o_atoms = take(off, sizeof(float4) * atoms.size());
   const size_t o_rs = take(off, sizeof(int) * rs.size());
@@ -489,7 +494,7 @@ int build_cull(mmo_ctx* ctx) {
   ctx->cull_rows = rs;
   ++ctx->cull_version;
   // the sweep keeps the whole protein and its index in shared memory
-  ctx->cull_ok = cull_smem_bytes(n, nrows, nrows) <= ctx->smem_optin;
+  ctx->cull_ok = cull_smem_bytes(n, nrows, nrows, 1024) <= ctx->smem_optin;
   return MMO_OK;
 }
 
@@ -587,7 +592,7 @@ int cull_plan_for(mmo_ctx* ctx, int B, bool grad) {
     sg.type[t] = ctx->lseg_type[t];
     sg.off[t + 1] = sg.off[t] + (sg.n[t] + sg.G - 1) / sg.G * sg.G;
   }
-  p.smem = cull_smem_bytes(ctx->cull.P, ctx->cull.nrows, npieces);
+  p.smem = cull_smem_bytes(ctx->cull.P, ctx->cull.nrows, npieces, p.threads);
   const int bps = std::max(1, cull_max_blocks(p.kp, p.threads, grad, ctx->ph, p.smem));
   p.blocks = ctx->sms * bps;
   const long items = (long)sg.off[sg.nseg] / sg.G * npieces;
@@ -841,7 +846,7 @@ int mmo_set_cull(mmo_ctx* ctx, int mode, double row_spacing, int piece_atoms,
   ctx->cull_mode = mode;
   ctx->cull_piece = piece_atoms;
   ctx->cull_kp = entries_per_lane;
-  const double h = row_spacing > 0 ? row_spacing : 2.0;
+  const double h = row_spacing > 0 ? row_spacing : 3.0;
   if (h != ctx->cull_h) {
     ctx->cull_h = h;
     MMO_CK(cudaSetDevice(ctx->device), "set device");

@@ -24,6 +24,7 @@ namespace {
 
 constexpr uint32_t kWaitPolls = 1u << 22;
 constexpr unsigned kFull = 0xffffffffu;
+constexpr int kListCap = 64;  // a warp's list: under 32 left over plus one window of 32
 
 __device__ __forceinline__ uint32_t spread3(uint32_t v) {  // 5 bits -> every third bit
   v &= 0x1fu;
@@ -169,8 +170,9 @@ __global__ void __launch_bounds__(cull_max_threads(KP))
   float4* s_rbox = sp + 2 * P;
   float4* s_tab = s_rbox + nrows;                       // [ptype][ltype] (X, 1/D, c1, 0)
   int* s_rs = reinterpret_cast<int*>(s_tab + kNTypes * kNTypes);
-  int* s_flush = s_rs + nrows + 1;
+  int* s_flush = s_rs + nrows + 1;                      // end of the row's flush block
   int* s_piece = s_flush + nrows;
+  int* s_list = s_piece + npieces + 1;                  // [warps][kListCap] atoms to sweep
   if (threadIdx.x == 0) {
     mbar_init(&bar, 1);
     const uint32_t bytes = (uint32_t)P * 32u;
@@ -249,49 +251,65 @@ __global__ void __launch_bounds__(cull_max_threads(KP))
 
     float mn = 1e30f;
     int visited = 0;
+    // the atoms of the warp's candidate rows within 12 A of the box, compacted
+    // in ascending order into the warp's list and swept 32 or more at a time
+    int* wl = s_list + (threadIdx.x >> 5) * kListCap;
+    int cnt = 0;
+    auto sweep = [&](int n) {
+      __syncwarp();
+#pragma unroll 2
+      for (int v = 0; v < n; ++v) {
+        const float4* pp = sp + 2 * wl[v];
+        const float4 p = pp[0], pl = pp[1];
+        const float4 pv = *reinterpret_cast<const float4*>(reinterpret_cast<const char*>(trow) +
+                                                           __float_as_int(pl.w));
+#pragma unroll
+        for (int k = 0; k < KP; ++k)
+          pair_step<GRAD, DIEL, 0>(xh[k], yh[k], zh[k], xl[k], yl[k], zl[k], p, pl, p.w * q[k],
+                                   pv.x, pv.y, pv.z, c0v, acc[k], gx[k], gy[k], gz[k], mn);
+      }
+      __syncwarp();
+    };
     const int r0 = s_piece[pc], r1 = s_piece[pc + 1];
-    for (int r = r0; r < r1; ++r) {
-      const float4 rb = s_rbox[r];
-      const float dy = fmaxf(fmaxf(rb.x - bhy, bly - rb.y), 0.f);
-      const float dz = fmaxf(fmaxf(rb.z - bhz, blz - rb.w), 0.f);
-      const float d2 = fmaf(dy, dy, dz * dz);
-      if (d2 < kCullR2) {
-        // sqrt(kCullR2 - d2) from one reciprocal square root, rounded up: a
-        // wider window only visits more atoms
-        const float x = kCullR2 - d2;
-        const float w = fmaf(x, rsqrtf(x), 1e-3f);
-        const float xlo = blx - w, xhi = bhx + w;
+    // rows in flush blocks: the FP32 partials go into the FP64 sums once per
+    // block (fixed rows of the protein) and at the end of the piece
+    for (int r = r0; r < r1;) {
+      const int rend = min(r1, s_flush[r]);
+      for (; r < rend; ++r) {
+        const float4 rb = s_rbox[r];
+        const float dy = fmaxf(fmaxf(rb.x - bhy, bly - rb.y), 0.f);
+        const float dz = fmaxf(fmaxf(rb.z - bhz, blz - rb.w), 0.f);
+        if (fmaf(dy, dy, dz * dz) >= kCullR2) continue;
         const int a = s_rs[r], b = s_rs[r + 1];
-        int nlo = 0, nhi = 0;
         for (int i0 = a; i0 < b; i0 += 32) {
           const int i = i0 + lane;
-          const float x = i < b ? sp[2 * i].x : 3.0e38f;
-          nlo += __popc(__ballot_sync(kFull, x < xlo));
-          nhi += __popc(__ballot_sync(kFull, x <= xhi));
-        }
-        visited += nhi - nlo;
-        const float4* pe = sp + 2 * (a + nhi);
-#pragma unroll 2
-        for (const float4* pp = sp + 2 * (a + nlo); pp < pe; pp += 2) {
-          const float4 p = pp[0], pl = pp[1];
-          const float4 pv = *reinterpret_cast<const float4*>(
-              reinterpret_cast<const char*>(trow) + __float_as_int(pl.w));
-#pragma unroll
-          for (int k = 0; k < KP; ++k)
-            pair_step<GRAD, DIEL, 0>(xh[k], yh[k], zh[k], xl[k], yl[k], zl[k], p, pl, p.w * q[k],
-                                     pv.x, pv.y, pv.z, c0v, acc[k], gx[k], gy[k], gz[k], mn);
+          bool in = false;
+          if (i < b) {
+            const float4 ph = sp[2 * i];
+            const float ex = fmaxf(fmaxf(blx - ph.x, ph.x - bhx), 0.f);
+            const float ey = fmaxf(fmaxf(bly - ph.y, ph.y - bhy), 0.f);
+            const float ez = fmaxf(fmaxf(blz - ph.z, ph.z - bhz), 0.f);
+            in = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < kCullR2;
+          }
+          const unsigned m = __ballot_sync(kFull, in);
+          if (in) wl[cnt + __popc(m & ((1u << lane) - 1u))] = i;
+          cnt += __popc(m);
+          if (cnt >= 32) {
+            sweep(cnt);
+            visited += cnt;
+            cnt = 0;
+          }
         }
       }
-      if (s_flush[r]) {
+      sweep(cnt);
+      visited += cnt;
+      cnt = 0;
 #pragma unroll
-        for (int k = 0; k < KP; ++k) {
-          ad[k] += (double)acc[k];
-          acc[k] = 0.f;
-        }
+      for (int k = 0; k < KP; ++k) {
+        ad[k] += (double)acc[k];
+        acc[k] = 0.f;
       }
     }
-#pragma unroll
-    for (int k = 0; k < KP; ++k) ad[k] += (double)acc[k];
     if (GRAD && __any_sync(kFull, mn < kMinR2)) {
       // a pair closer than 0.01 A, where the clamped distance makes the
       // derivative 0: redo the gradient over the piece with the per-pair test
@@ -376,9 +394,9 @@ CullFn pick_cull(int kp, bool grad, const Physics& ph) {
 
 }  // namespace
 
-int cull_smem_bytes(int P, int nrows, int npieces) {
+int cull_smem_bytes(int P, int nrows, int npieces, int threads) {
   const long b = 32L * P + 16L * nrows + 16L * kNTypes * kNTypes + 4L * (nrows + 1) + 4L * nrows +
-                 4L * (npieces + 1);
+                 4L * (npieces + 1) + 4L * kListCap * (threads / 32);
   return (int)((b + 15) / 16 * 16);
 }
 

@@ -137,7 +137,8 @@ struct DevCull {
                              // row in the shared pair table
   const int* row_start;      // [nrows + 1]
   const float4* row_box;     // [nrows] (y_min, y_max, z_min, z_max) of the row's atoms
-  const int* row_flush;      // [nrows] 1: add the FP32 partial to the FP64 sum after this row
+  const int* row_flush;      // [nrows] end (exclusive) of the row's flush block: the FP32
+                             // partials go into the FP64 sums after row row_flush[r] - 1
   int P, nrows;
   float glo[3];              // entry binning grid origin and cells per A
   float ginv;
@@ -206,7 +207,7 @@ cudaError_t launch_pairs_cull(const DevCull& cull, const float4* tab, const Cull
                               const CullScratch& cs, int flags, const Physics& ph,
                               const CullPlan& plan, int* d_err, cudaStream_t st);
 int cull_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_bytes);
-int cull_smem_bytes(int P, int nrows, int npieces);
+int cull_smem_bytes(int P, int nrows, int npieces, int threads);
 cudaError_t launch_fma_peak(int sms, int iters, float* out, cudaStream_t st, double* flops);
 
 // ---- device helpers ------------------------------------------------------
