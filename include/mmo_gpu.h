@@ -161,7 +161,7 @@ int mmo_set_cull(mmo_ctx* ctx, int mode, double row_spacing, int piece_atoms,
 /* Autotuner of the batched pair sweep (no counterpart in the reference).
  * Times launch plans on this batch and keeps the fastest as the context's
  * settings (mmo_set_cull, mmo_set_tiles): under the shifted form the cut-off
- * sweep's row spacing (1.5, 2, 3 A), entries per lane (1, 2, 4) and piece
+ * sweep's row spacing (2, 3, 4 A), entries per lane (1, 2, 4) and piece
  * size (256, 512 atoms) against the full sweep's poses per lane (1, 2, 4) and
  * protein chunks (4 to 24); under the global form the full sweep's plans.
  * Arguments as mmo_score_poses_device, whose outputs it leaves as computed by

@@ -1225,7 +1225,7 @@ int mmo_tune(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E, f
   std::vector<TunePlan> cands;
   if (inter && B >= 2) {
     if (ctx->ph.inter_form == 0 && ctx->cull_ok)
-      for (double h : {1.5, 2.0, 3.0})
+      for (double h : {2.0, 3.0, 4.0})
         for (int kp : {1, 2, 4})
           for (int piece : {256, 512}) {
             cands.push_back({1, h, kp, piece, cull_max_threads(kp), 0});

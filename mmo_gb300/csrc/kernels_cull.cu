@@ -4,7 +4,7 @@
 // bisector-tree neighbour query returns within 12 A).  Here the query is made for a
 // group of 32 * KP (pose, ligand atom) entries at once:
 //
-//   k_cull_bin      entry -> (ligand type segment, Morton cell of its position)
+//   k_cull_bin      entry -> (ligand type segment, Hilbert cell of its position)
 //   k_cull_scan     bin counts -> first slot of each bin (one CTA per segment)
 //   k_cull_scatter  entries copied into slot order
 //   k_pairs_cull    persistent CTAs, protein resident in shared memory (TMA
@@ -26,12 +26,38 @@ constexpr uint32_t kWaitPolls = 1u << 22;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kListCap = 64;  // a warp's list: under 32 left over plus one window of 32
 
-__device__ __forceinline__ uint32_t spread3(uint32_t v) {  // 5 bits -> every third bit
-  v &= 0x1fu;
-  v = (v | (v << 8)) & 0x0300F00Fu;
-  v = (v | (v << 4)) & 0x030C30C3u;
-  v = (v | (v << 2)) & 0x09249249u;
-  return v;
+// Index of cell (x, y, z) of the 32^3 binning grid along a 3-D Hilbert curve
+// (J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc. 707, 2004:
+// axes to transposed index, then the bits interleaved).  Consecutive slots in
+// Hilbert order stay closer together than in Morton order, so the groups'
+// boxes are smaller.
+__device__ __forceinline__ uint32_t hilbert_cell(uint32_t x, uint32_t y, uint32_t z) {
+  constexpr int kBits = 5;
+  uint32_t X[3] = {x, y, z};
+  for (uint32_t Q = 1u << (kBits - 1); Q > 1; Q >>= 1) {
+    const uint32_t P = Q - 1;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      if (X[i] & Q) {
+        X[0] ^= P;
+      } else {
+        const uint32_t t = (X[0] ^ X[i]) & P;
+        X[0] ^= t;
+        X[i] ^= t;
+      }
+    }
+  }
+  X[1] ^= X[0];
+  X[2] ^= X[1];
+  uint32_t t = 0;
+  for (uint32_t Q = 1u << (kBits - 1); Q > 1; Q >>= 1)
+    if (X[2] & Q) t ^= Q - 1;
+  uint32_t k = 0;
+#pragma unroll
+  for (int b = kBits - 1; b >= 0; --b)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) k = (k << 1) | (((X[i] ^ t) >> b) & 1u);
+  return k;
 }
 
 __device__ __forceinline__ int grid_cell(float v, float lo, float inv) {
@@ -48,8 +74,7 @@ __global__ void k_cull_bin(const float4* __restrict__ X, int n, int L,
   const uint32_t cx = grid_cell(h.x, cull.glo[0], cull.ginv);
   const uint32_t cy = grid_cell(h.y, cull.glo[1], cull.ginv);
   const uint32_t cz = grid_cell(h.z, cull.glo[2], cull.ginv);
-  const int b = seg_of_atom[e % L] * kCullBins +
-                (int)(spread3(cx) | (spread3(cy) << 1) | (spread3(cz) << 2));
+  const int b = seg_of_atom[e % L] * kCullBins + (int)hilbert_cell(cx, cy, cz);
   bin[e] = b;
   rank[e] = (int)atomicAdd(&hist[b], 1u);
 }

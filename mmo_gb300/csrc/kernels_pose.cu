@@ -20,6 +20,7 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kRebuildThreads = 128;  // threads per rebuild block
 constexpr int kWarpsPerBlock = 4;     // poses per finish block
+constexpr int kFinishBlocksPerSM = 7;  // resident finish blocks: 4,096 poses in one wave on 152 SMs
 
 // ---------------------------------------------------------------------------
 // k_rebuild
@@ -167,17 +168,30 @@ __device__ __forceinline__ float intra_pair_g(const float4* sh, const float4* sl
   return g;
 }
 
+// shared memory of one finishing warp, in float4: coordinates hi and lo [L],
+// torsion axes and centres [2 nrb], torsion records [3 nrb], then the per-lane
+// torsion partials [nrb][33] as floats
+__host__ __device__ constexpr int finish_warp_f4(int L, int nrb) {
+  return 2 * L + 5 * nrb + (33 * nrb + 3) / 4;
+}
+
 template <bool GRAD, bool RECENTER, int DIEL, int IFORM>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, kFinishBlocksPerSM)
     k_finish(DevLigand lig, PoseIO io, Scratch scr, int flags) {
-  __shared__ float4 sxh[kWarpsPerBlock][kMaxLig];
-  __shared__ float4 sxl[kWarpsPerBlock][kMaxLig];
-  __shared__ float4 saxis[kWarpsPerBlock][2 * kMaxTors];
-  __shared__ float sdti[kWarpsPerBlock][kMaxTors][33];  // per-lane torsion partials
+  extern __shared__ __align__(16) float4 fsm[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int b = blockIdx.x * kWarpsPerBlock + wib;
   if (b >= io.B) return;
   const int L = lig.L, C = scr.C, nrb = lig.nrb, nd = 6 + nrb;
+  float4* sxh = fsm + wib * finish_warp_f4(L, nrb);
+  float4* sxl = sxh + L;
+  float4* saxis = sxl + L;        // [nrb] final axes, then [nrb] centres
+  float4* srec = saxis + 2 * nrb;  // [nrb][3] torsion records
+  float* sdti = reinterpret_cast<float*>(srec + 3 * nrb);  // [nrb][33]
+  if (GRAD) {  // the reverse pass reads them last: start the loads now
+    const float4* recb = scr.rec + (size_t)b * nrb * 3;
+    for (int k = lane; k < 3 * nrb; k += 32) srec[k] = recb[k];
+  }
   const bool intra = flags & kFlagIntra, inter = flags & kFlagInter;
   double e = 0.0;
   if (inter) {
@@ -186,8 +200,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
   }
   if (intra) {
     for (int a = lane; a < L; a += 32) {
-      sxh[wib][a] = scr.X[((size_t)b * L + a) * 2];
-      sxl[wib][a] = scr.X[((size_t)b * L + a) * 2 + 1];
+      sxh[a] = scr.X[((size_t)b * L + a) * 2];
+      sxl[a] = scr.X[((size_t)b * L + a) * 2 + 1];
     }
     __syncwarp();
   }
@@ -196,15 +210,15 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     // final axis w_t and centre C_t of every torsion, from the posed coordinates
     if (lane < nrb) {
       const int2 bd = lig.bonds[lane];
-      const float4 rh = sxh[wib][bd.y], rl = sxl[wib][bd.y];
-      const float4 lh = sxh[wib][bd.x], ll = sxl[wib][bd.x];
+      const float4 rh = sxh[bd.y], rl = sxl[bd.y];
+      const float4 lh = sxh[bd.x], ll = sxl[bd.x];
       const float ax = split_diff(rh.x, rl.x, lh.x, ll.x), ay = split_diff(rh.y, rl.y, lh.y, ll.y),
                   az = split_diff(rh.z, rl.z, lh.z, ll.z);
       const float inv = rsqrtf(ax * ax + ay * ay + az * az);
-      saxis[wib][lane] = make_float4(ax * inv, ay * inv, az * inv, 0.f);
-      saxis[wib][kMaxTors + lane] = rh;
+      saxis[lane] = make_float4(ax * inv, ay * inv, az * inv, 0.f);
+      saxis[nrb + lane] = rh;
     }
-    for (int t = 0; t < nrb; ++t) sdti[wib][t][lane] = 0.f;
+    for (int t = 0; t < nrb; ++t) sdti[t * 33 + lane] = 0.f;
     __syncwarp();
   }
   if (intra) {
@@ -216,7 +230,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       const int2 ij = lig.pair_ij[p];
       const float4 par = lig.pair_par[p];
       float ep, dx, dy, dz;
-      const float g = intra_pair_g<DIEL, IFORM>(sxh[wib], sxl[wib], ij.x, ij.y, par, ep, dx, dy, dz);
+      const float g = intra_pair_g<DIEL, IFORM>(sxh, sxl, ij.x, ij.y, par, ep, dx, dy, dz);
       acc += ep;
       if (crossing) {
         const uint32_t mi = lig.amask[ij.x], mj = lig.amask[ij.y];
@@ -225,12 +239,12 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
           const int t = __ffs(x) - 1;
           x &= x - 1;
           const bool in_i = (mi >> t) & 1u;
-          const float4 w = saxis[wib][t], cc = saxis[wib][kMaxTors + t];
-          const float4 m = sxh[wib][in_i ? ij.x : ij.y];
+          const float4 w = saxis[t], cc = saxis[nrb + t];
+          const float4 m = sxh[in_i ? ij.x : ij.y];
           const float lx = m.x - cc.x, ly = m.y - cc.y, lz = m.z - cc.z;
           const float v = dx * (w.y * lz - w.z * ly) + dy * (w.z * lx - w.x * lz) +
                           dz * (w.x * ly - w.y * lx);
-          sdti[wib][t][lane] = fmaf(in_i ? g : -g, v, sdti[wib][t][lane]);
+          sdti[t * 33 + lane] = fmaf(in_i ? g : -g, v, sdti[t * 33 + lane]);
         }
       }
     }
@@ -267,11 +281,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     for (int s = 0; s < kSlots; ++s) {
       const int a = lane + 32 * s;
       if (a < L) {
-        const float4 ah = sxh[wib][a], al = sxl[wib][a];
+        const float4 ah = sxh[a], al = sxl[a];
         float acc = 0.f;
         for (int k = lig.nb_off[a]; k < lig.nb_off[a + 1]; ++k) {
           const int j = lig.nb_idx[k];
-          const float4 bh = sxh[wib][j], bl = sxl[wib][j];
+          const float4 bh = sxh[j], bl = sxl[j];
           const float4 par = lig.nb_par[k];
           uff_pair<true, DIEL, IFORM>(split_diff(ah.x, al.x, bh.x, bl.x),
                                       split_diff(ah.y, al.y, bh.y, bl.y),
@@ -379,13 +393,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
   if (crossing) {
     __syncwarp();
     if (lane < nrb)
-      for (int k = 0; k < 32; ++k) dti_mine += sdti[wib][lane][k];
+      for (int k = 0; k < 32; ++k) dti_mine += sdti[lane * 33 + k];
   }
   // reverse through the torsions, undoing each rotation on the way back
-  const float4* recb = scr.rec + (size_t)b * nrb * 3;
+  __syncwarp();  // the prefetched torsion records
   for (int t = nrb - 1; t >= 0; --t) {
-    const float4 r0 = recb[3 * t], r1 = recb[3 * t + 1];
-    const float ilen = recb[3 * t + 2].x;
+    const float4 r0 = srec[3 * t], r1 = srec[3 * t + 1];
+    const float ilen = srec[3 * t + 2].x;
     float Rt[9];
     axis_angle(r1.x, r1.y, r1.z, r0.w, r1.w, Rt);
     float q[10];
@@ -517,7 +531,13 @@ template <bool G, bool RC, int DIEL, int IFORM>
 cudaError_t finish_t(const DevLigand& lig, const PoseIO& io, const Scratch& s, int flags,
                      cudaStream_t st) {
   const int blocks = (io.B + kWarpsPerBlock - 1) / kWarpsPerBlock;
-  k_finish<G, RC, DIEL, IFORM><<<blocks, kWarpsPerBlock * 32, 0, st>>>(lig, io, s, flags);
+  const int smem = kWarpsPerBlock * finish_warp_f4(lig.L, lig.nrb) * (int)sizeof(float4);
+  if (smem > 48 * 1024) {
+    const cudaError_t e = cudaFuncSetAttribute(k_finish<G, RC, DIEL, IFORM>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+  }
+  k_finish<G, RC, DIEL, IFORM><<<blocks, kWarpsPerBlock * 32, smem, st>>>(lig, io, s, flags);
   return cudaGetLastError();
 }
 

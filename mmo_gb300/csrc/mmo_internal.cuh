@@ -125,7 +125,7 @@ struct PairPlan {
 // fixed pieces of the protein, so an entry's result does not depend on which
 // entries share its group.
 constexpr int kCullGrid = 32;                                   // entry binning cells per axis
-constexpr int kCullBins = kCullGrid * kCullGrid * kCullGrid;    // Morton-ordered cells
+constexpr int kCullBins = kCullGrid * kCullGrid * kCullGrid;    // cells in Hilbert order
 constexpr float kCullR2 = 145.0f;  // visit radius^2: 1 - r^2/144 < 0 in FP32 beyond it
 constexpr int kCullFlush = 256;    // protein atoms per FP32 partial before the FP64 add
 
