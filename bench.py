@@ -325,6 +325,16 @@ def main():
     flops = FLOPS_PAIR_GRAD * pairs_ev
     achieved = flops / (pair_avg * 1e-3) * 1e-12
     culled = pairs_ev < pairs_all
+    # DRAM bytes per launch of the sweep from the committed ncu capture of this workload
+    traffic = None
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
+                               "traffic.json")) as f:
+            tr = json.load(f).get("k_pairs_cull" if culled else "k_pairs")
+        if tr and B == 4096 and P == 6000 and L_atoms == 48:
+            traffic = tr["dram_bytes_per_launch"]
+    except (OSError, ValueError, KeyError):
+        traffic = None
 
     line = {
         "metric": METRIC, "value": value, "unit": "poses/s", "n_gpus": world,
@@ -348,7 +358,8 @@ def main():
                      "kernel": ("k_pairs_cull (cut-off pair sweep, energy+gradient)" if culled
                                 else "k_pairs (pair sweep, energy+gradient)"),
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": traffic,
+                     "traffic_unit": "DRAM bytes per launch (ncu capture)",
                      "peak_source": "measured FP32 FMA probe on this GPU (mmo_fp32_fma_peak)",
                      "flops_per_pair": FLOPS_PAIR_GRAD, "pairs_evaluated": pairs_ev,
                      "pairs_all": pairs_all, "flops_per_launch": flops,
