@@ -14,6 +14,7 @@
 
 #include "../../include/mmo_diag.h"
 #include "../../include/mmo_gpu.h"
+#include "../../include/mmo_mc.h"
 #include "mmo_internal.cuh"
 
 using namespace mmo;
@@ -86,8 +87,9 @@ struct mmo_ctx {
   float4* d_tab4 = nullptr;  // device copy of tab4
   int tile_kp = 0, tile_threads = 0, tile_chunks = 0;
   // last launch plan and the inputs it was made for
-  PairPlan plan{};
-  long plan_key[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+  // launch plans, one per gradient flag, and the inputs they were made for
+  PairPlan plan[2] = {};
+  long plan_key[2][8] = {{-1, -1, -1, -1, -1, -1, -1, -1}, {-1, -1, -1, -1, -1, -1, -1, -1}};
 
   // protein
   DevProtein prot{};
@@ -111,15 +113,19 @@ struct mmo_ctx {
   std::vector<int> cull_rows;  // host copy of row_start
   int smem_optin = 0;
   CullScratch cs{};
-  CullSegs segs{};
-  CullPlan cplan{};
-  long cplan_key[10] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+  CullSegs segs[2] = {};
+  CullPlan cplan[2] = {};
+  long cplan_key[2][10] = {{-1, -1, -1, -1, -1, -1, -1, -1, -1, -1},
+                           {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1}};
+  long piece_key[2] = {-1, -1};  // (row index version, piece atoms) of the uploaded pieces
+  int npieces = 0;
   int* d_piece = nullptr;
   size_t capPiece = 0, capHist = 0, capBin = 0, capRank = 0, capXs = 0, capOrd = 0, capEp = 0,
          capGp = 0, capArr = 0, capVis = 0;
   std::string tune_cache;        // file of tuned plans (mmo_set_tune_cache)
   unsigned* d_queue = nullptr;  // [0] work counter, [2..3] pair evaluations (u64)
   bool last_cull = false;       // the last call's inter term used the cut-off sweep
+  int last_grad = 0;            // the last call computed the gradient
   double last_pairs = 0;        // poses x ligand atoms x protein atoms of the last call
   int last_launches = 0;        // kernels of the last scoring call
 
@@ -142,6 +148,15 @@ struct mmo_ctx {
   bool profiling = false;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   bool ev_valid = false;
+
+  // Monte Carlo chains (mmo_mc_run): one blob of per-chain buffers and the
+  // CUDA graph of a block of steps
+  void* d_mc = nullptr;
+  size_t cap_mc = 0;
+  cudaGraphExec_t mc_exec = nullptr;
+  std::vector<long> mc_key;
+  cudaEvent_t mc_ev[2] = {nullptr, nullptr};
+  long epoch = 0;  // bumped whenever baked launch arguments (buffers, uploads, plans) change
 
   // host-API staging
   char* h_in = nullptr;
@@ -197,6 +212,7 @@ int upload_table(mmo_ctx* ctx) {
 
 int grow(mmo_ctx* ctx, void** p, size_t* cap, size_t bytes, const char* what) {
   if (bytes <= *cap) return MMO_OK;
+  ++ctx->epoch;
   if (*p) cudaFree(*p);
   *p = nullptr;
   *cap = 0;
@@ -382,6 +398,7 @@ int upload_ligand(mmo_ctx* ctx) {
   ctx->lig = layout(base);
   ctx->has_lig = true;
   ++ctx->lig_version;
+  ++ctx->epoch;
   return MMO_OK;
 }
 
@@ -493,6 +510,7 @@ int build_cull(mmo_ctx* ctx) {
   ctx->cull = c;
   ctx->cull_rows = rs;
   ++ctx->cull_version;
+  ++ctx->epoch;
   // the sweep keeps the whole protein and its index in shared memory
   ctx->cull_ok = cull_smem_bytes(n, nrows, nrows, 1024) <= ctx->smem_optin;
   return MMO_OK;
@@ -504,11 +522,12 @@ PairPlan make_plan(mmo_ctx* ctx, int B, bool grad);
 PairPlan plan_for(mmo_ctx* ctx, int B, bool grad) {
   const long key[8] = {B, grad, ctx->prot.P, ctx->lig.L, ctx->tile_kp, ctx->tile_threads,
                        ctx->tile_chunks, ctx->ph.dielectric * 2 + ctx->ph.inter_form};
-  if (!std::equal(key, key + 8, ctx->plan_key)) {
-    ctx->plan = make_plan(ctx, B, grad);
-    std::copy(key, key + 8, ctx->plan_key);
+  const int g = grad ? 1 : 0;
+  if (!std::equal(key, key + 8, ctx->plan_key[g])) {
+    ctx->plan[g] = make_plan(ctx, B, grad);
+    std::copy(key, key + 8, ctx->plan_key[g]);
   }
-  return ctx->plan;
+  return ctx->plan[g];
 }
 
 PairPlan make_plan(mmo_ctx* ctx, int B, bool grad) {
@@ -559,30 +578,40 @@ int cull_plan_for(mmo_ctx* ctx, int B, bool grad) {
   const long key[10] = {B, grad, ctx->prot_version, ctx->lig_version, ctx->cull_kp,
                         ctx->cull_piece, ctx->tile_threads, ctx->ph.dielectric,
                         ctx->cull_version, ctx->prot.P};
-  if (std::equal(key, key + 10, ctx->cplan_key)) return MMO_OK;
+  const int g = grad ? 1 : 0;
+  if (std::equal(key, key + 10, ctx->cplan_key[g])) {
+    ctx->cs.npieces = ctx->npieces;
+    return MMO_OK;
+  }
   CullPlan p{};
   p.kp = ctx->cull_kp ? ctx->cull_kp : 2;
   p.threads = std::min(ctx->tile_threads ? ctx->tile_threads : 1024, cull_max_threads(p.kp));
   p.piece_atoms = ctx->cull_piece ? ctx->cull_piece : 256;
-  const std::vector<int>& rs = ctx->cull_rows;
-  const int nrows = (int)rs.size() - 1;
-  // pieces: consecutive rows of about piece_atoms atoms
-  std::vector<int> pr{0};
-  int acc = 0;
-  for (int r = 0; r < nrows; ++r) {
-    acc += rs[r + 1] - rs[r];
-    if (acc >= p.piece_atoms && r + 1 < nrows) {
-      pr.push_back(r + 1);
-      acc = 0;
+  if (ctx->piece_key[0] != ctx->cull_version || ctx->piece_key[1] != p.piece_atoms) {
+    // pieces: consecutive rows of about piece_atoms atoms
+    const std::vector<int>& rs = ctx->cull_rows;
+    const int nrows = (int)rs.size() - 1;
+    std::vector<int> pr{0};
+    int acc = 0;
+    for (int r = 0; r < nrows; ++r) {
+      acc += rs[r + 1] - rs[r];
+      if (acc >= p.piece_atoms && r + 1 < nrows) {
+        pr.push_back(r + 1);
+        acc = 0;
+      }
     }
+    pr.push_back(nrows);
+    int r = grow(ctx, (void**)&ctx->d_piece, &ctx->capPiece, sizeof(int) * pr.size(),
+                 "piece table");
+    if (r) return r;
+    MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before piece table upload");
+    MMO_CK(cudaMemcpy(ctx->d_piece, pr.data(), sizeof(int) * pr.size(), cudaMemcpyHostToDevice),
+           "piece table upload");
+    ctx->npieces = (int)pr.size() - 1;
+    ctx->piece_key[0] = ctx->cull_version;
+    ctx->piece_key[1] = p.piece_atoms;
   }
-  pr.push_back(nrows);
-  const int npieces = (int)pr.size() - 1;
-  int r = grow(ctx, (void**)&ctx->d_piece, &ctx->capPiece, sizeof(int) * pr.size(), "piece table");
-  if (r) return r;
-  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before piece table upload");
-  MMO_CK(cudaMemcpy(ctx->d_piece, pr.data(), sizeof(int) * pr.size(), cudaMemcpyHostToDevice),
-         "piece table upload");
+  const int npieces = ctx->npieces;
   CullSegs sg{};
   sg.nseg = (int)ctx->lseg_type.size();
   sg.G = 32 * p.kp;
@@ -598,16 +627,16 @@ int cull_plan_for(mmo_ctx* ctx, int B, bool grad) {
   const long items = (long)sg.off[sg.nseg] / sg.G * npieces;
   const long need = (items + p.threads / 32 - 1) / (p.threads / 32);
   if (need < p.blocks) p.blocks = (int)std::max(1L, need);
-  ctx->cplan = p;
-  ctx->segs = sg;
+  ctx->cplan[g] = p;
+  ctx->segs[g] = sg;
   ctx->cs.npieces = npieces;
-  std::copy(key, key + 10, ctx->cplan_key);
+  std::copy(key, key + 10, ctx->cplan_key[g]);
   return MMO_OK;
 }
 
 int ensure_cull_scratch(mmo_ctx* ctx, int B, int L, bool grad) {
   int r;
-  const CullSegs& sg = ctx->segs;
+  const CullSegs& sg = ctx->segs[grad ? 1 : 0];
   const size_t slots = sg.off[sg.nseg], np = ctx->cs.npieces;
   CullScratch& c = ctx->cs;
   if ((r = grow(ctx, (void**)&c.hist, &ctx->capHist, sizeof(unsigned) * sg.nseg * kCullBins,
@@ -659,6 +688,7 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
   const int L = ctx->lig.L;
   const bool cull = inter && use_cull(ctx, B);
   ctx->last_cull = cull;
+  ctx->last_grad = grad ? 1 : 0;
   ctx->last_pairs = inter ? (double)B * L * ctx->prot.P : 0.0;
   // rebuild + finish, and the sweep: entry bin, scan, scatter, sweep
   ctx->last_launches = 2 + (cull ? 4 : (inter ? 1 : 0));
@@ -696,13 +726,13 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
   MMO_CK(launch_rebuild(ctx->lig, io, ctx->scr, fl, st), "rebuild kernel");
   MMO_CK(mark(1), "event");
   if (cull) {
-    const CullSegs& sg = ctx->segs;
+    const CullSegs& sg = ctx->segs[grad ? 1 : 0];
     MMO_CK(cudaMemsetAsync(ctx->cs.hist, 0, sizeof(unsigned) * sg.nseg * kCullBins, st),
            "entry bin reset");
     MMO_CK(launch_cull_sort(ctx->cull, ctx->scr, ctx->lig.q, B, L, sg, ctx->cs, st),
            "entry sort kernels");
     MMO_CK(mark(2), "event");
-    MMO_CK(launch_pairs_cull(ctx->cull, ctx->d_tab4, sg, ctx->cs, fl, ctx->ph, ctx->cplan, d_err,
+    MMO_CK(launch_pairs_cull(ctx->cull, ctx->d_tab4, sg, ctx->cs, fl, ctx->ph, ctx->cplan[grad], d_err,
                              st),
            "cut-off pair kernel");
     MMO_CK(mark(3), "event");
@@ -800,6 +830,10 @@ int mmo_ctx_destroy(mmo_ctx* ctx) {
   cudaFree(ctx->cs.Gp);
   cudaFree(ctx->cs.arrive);
   cudaFree(ctx->cs.vis);
+  cudaFree(ctx->d_mc);
+  if (ctx->mc_exec) cudaGraphExecDestroy(ctx->mc_exec);
+  for (auto& e : ctx->mc_ev)
+    if (e) cudaEventDestroy(e);
   cudaFree(ctx->d_in);
   cudaFree(ctx->d_out);
   if (ctx->h_in) cudaFreeHost(ctx->h_in);
@@ -813,6 +847,7 @@ int mmo_set_physics(mmo_ctx* ctx, int dielectric, int mixing, int inter_form, in
   if (!ctx) return MMO_EINVAL;
   if ((dielectric | mixing | inter_form | intra_form) & ~1)
     return fail(ctx, MMO_EINVAL, "physics switches are 0 or 1");
+  ++ctx->epoch;
   ctx->ph = Physics{dielectric, mixing, inter_form, intra_form};
   rebuild_table(ctx);
   if (int r = upload_table(ctx)) return r;
@@ -830,6 +865,7 @@ int mmo_set_tiles(mmo_ctx* ctx, int kp, int threads, int chunks) {
   ctx->tile_kp = kp;
   ctx->tile_threads = threads;
   ctx->tile_chunks = chunks;
+  ++ctx->epoch;
   return MMO_OK;
 }
 
@@ -846,6 +882,7 @@ int mmo_set_cull(mmo_ctx* ctx, int mode, double row_spacing, int piece_atoms,
   ctx->cull_mode = mode;
   ctx->cull_piece = piece_atoms;
   ctx->cull_kp = entries_per_lane;
+  ++ctx->epoch;
   const double h = row_spacing > 0 ? row_spacing : 3.0;
   if (h != ctx->cull_h) {
     ctx->cull_h = h;
@@ -941,6 +978,7 @@ int mmo_set_protein(mmo_ctx* ctx, int n, const double* xs, const double* ys, con
     ctx->ptypes[i] = type[i];
   }
   ++ctx->prot_version;
+  ++ctx->epoch;
   return build_cull(ctx);
 }
 
@@ -1136,6 +1174,7 @@ struct TunePlan {
 };
 
 void apply_plan(mmo_ctx* ctx, const TunePlan& p, int* r) {
+  ++ctx->epoch;
   ctx->cull_mode = p.cull ? 0 : 1;
   ctx->cull_kp = p.cull ? p.kp : 0;
   ctx->cull_piece = p.cull ? p.piece : 0;
@@ -1192,9 +1231,10 @@ int mmo_get_plan(const mmo_ctx* ctx, int* path, int* per_lane, int* threads, int
   if (!ctx || !path || !per_lane || !threads || !chunks_or_piece || !row_spacing)
     return MMO_EINVAL;
   *path = ctx->last_cull ? 1 : 0;
-  *per_lane = ctx->last_cull ? ctx->cplan.kp : ctx->plan.kp;
-  *threads = ctx->last_cull ? ctx->cplan.threads : ctx->plan.threads;
-  *chunks_or_piece = ctx->last_cull ? ctx->cplan.piece_atoms : ctx->plan.C;
+  const int g = ctx->last_grad;
+  *per_lane = ctx->last_cull ? ctx->cplan[g].kp : ctx->plan[g].kp;
+  *threads = ctx->last_cull ? ctx->cplan[g].threads : ctx->plan[g].threads;
+  *chunks_or_piece = ctx->last_cull ? ctx->cplan[g].piece_atoms : ctx->plan[g].C;
   *row_spacing = ctx->cull_h;
   return MMO_OK;
 }
@@ -1274,6 +1314,194 @@ int mmo_tune(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E, f
       fclose(f);
     }
   }
+  return MMO_OK;
+}
+
+namespace {
+
+// per-chain buffers of mmo_mc_run in one allocation
+MCDev mc_layout(char* base, int B, int nd, int nrb, size_t* bytes) {
+  size_t off = 0;
+  MCDev s{};
+  s.cur = align_ptr<float>(base, off, (size_t)B * nd);
+  s.trial = align_ptr<float>(base, off, (size_t)B * nd);
+  s.best = align_ptr<float>(base, off, (size_t)B * nd);
+  s.G_cur = align_ptr<float>(base, off, (size_t)B * nd);
+  s.G_trial = align_ptr<float>(base, off, (size_t)B * nd);
+  s.E_cur = align_ptr<double>(base, off, B);
+  s.E_trial = align_ptr<double>(base, off, B);
+  s.E_best = align_ptr<double>(base, off, B);
+  s.st_trial = align_ptr<int>(base, off, B);
+  s.moved = align_ptr<int>(base, off, B);
+  s.accepted = align_ptr<int>(base, off, B);
+  s.status_or = align_ptr<int>(base, off, B);
+  s.steps = align_ptr<float>(base, off, (size_t)B * (2 + nrb));
+  s.cnt = align_ptr<int>(base, off, (size_t)B * (kMcCounts + 2 * nrb));
+  s.eta = align_ptr<float>(base, off, B);
+  *bytes = off;
+  return s;
+}
+
+// one block of MC steps, optionally ending with a minimisation: a fixed launch
+// sequence on st (captured into a graph, or launched directly)
+int mc_block(mmo_ctx* ctx, const MCDev& s, const MCParams& p, int nsteps, bool minimize,
+             int iters, int flags, cudaStream_t st) {
+  int r;
+  for (int k = 0; k < nsteps; ++k) {
+    MMO_CK(launch_k_mc_propose(s, p, st), "MC propose kernel");
+    if ((r = score_device(ctx, p.B, s.trial, flags, s.E_trial, nullptr, s.st_trial, ctx->d_err, 0,
+                          st)))
+      return r;
+    MMO_CK(launch_k_mc_accept(s, p, st), "MC accept kernel");
+  }
+  if (minimize) {
+    const int gf = flags | MMO_F_GRAD;
+    MMO_CK(launch_k_gd_begin(s, p, st), "GD kernel");
+    if ((r = score_device(ctx, p.B, s.cur, gf, s.E_trial, s.G_trial, s.st_trial, ctx->d_err, 0, st)))
+      return r;
+    MMO_CK(launch_k_gd_take(s, p, st), "GD kernel");
+    for (int it = 0; it < iters; ++it) {
+      MMO_CK(launch_k_gd_propose(s, p, st), "GD propose kernel");
+      if ((r = score_device(ctx, p.B, s.trial, gf, s.E_trial, s.G_trial, s.st_trial, ctx->d_err, 0,
+                            st)))
+        return r;
+      MMO_CK(launch_k_gd_accept(s, p, st), "GD accept kernel");
+    }
+  }
+  return MMO_OK;
+}
+
+}  // namespace
+
+int mmo_mc_run(mmo_ctx* ctx, int chains, int steps, const mmo_mc_params* prm,
+               const mmo_mc_state* state, void* stream, int use_graph) {
+  if (!ctx) return MMO_EINVAL;
+  if (!ctx->has_lig) return fail(ctx, MMO_ESTATE, "no ligand: call mmo_set_ligand first");
+  if (chains <= 0 || steps < 0 || !prm || !state || !state->dofs || !state->E)
+    return fail(ctx, MMO_EINVAL, "mmo_mc_run: bad arguments");
+  if (!(prm->kT > 0) || !std::isfinite(prm->kT) || !(prm->rot_step >= 0) ||
+      !(prm->trans_step >= 0) || !(prm->tors_step >= 0) || !std::isfinite(prm->rot_step) ||
+      !std::isfinite(prm->trans_step) || !std::isfinite(prm->tors_step) ||
+      (prm->move_law != MMO_MC_UNIFORM && prm->move_law != MMO_MC_GAUSSIAN) ||
+      prm->minimize_every < 0 || prm->minimize_iters < 0 || prm->flip_every < 0 ||
+      !(prm->gd_step >= 0) || !std::isfinite(prm->gd_step))
+    return fail(ctx, MMO_EINVAL, "mmo_mc_run: bad parameters");
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  cudaStream_t us = reinterpret_cast<cudaStream_t>(stream);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  MMO_CK(cudaStreamIsCapturing(us, &cap), "capture status");
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(ctx, MMO_ESTATE, "mmo_mc_run: the stream is being captured");
+  const int B = chains, nrb = ctx->lig.nrb, nd = 6 + nrb;
+  size_t bytes = 0;
+  mc_layout(nullptr, B, nd, nrb, &bytes);
+  int r;
+  if ((r = grow(ctx, &ctx->d_mc, &ctx->cap_mc, bytes, "MC chain buffers"))) return r;
+  const MCDev s = mc_layout(static_cast<char*>(ctx->d_mc), B, nd, nrb, &bytes);
+  MCParams p{};
+  p.kT = prm->kT;
+  p.rot = (float)prm->rot_step;
+  p.trans = (float)prm->trans_step;
+  p.tors = (float)prm->tors_step;
+  p.gd_step = (float)prm->gd_step;
+  p.law = prm->move_law;
+  p.adapt = prm->adapt ? 1 : 0;
+  p.flip_every = prm->flip_every;
+  p.key0 = (uint32_t)(prm->seed & 0xffffffffu);
+  p.key1 = (uint32_t)(prm->seed >> 32);
+  p.B = B;
+  p.nd = nd;
+  p.nrb = nrb;
+  const int flags = (ctx->prot.P > 0 ? MMO_F_INTER : 0) | MMO_F_INTRA | MMO_F_RECENTER;
+  const bool minimize = prm->minimize_every > 0 && prm->minimize_iters > 0;
+  const int block = std::max(1, std::min(steps, minimize ? prm->minimize_every : 50));
+  const bool prof = ctx->profiling;
+  ctx->profiling = false;  // no stage events inside a graph
+  for (auto& e : ctx->mc_ev)
+    if (!e) MMO_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+  // work on the context's stream, ordered after the caller's stream
+  cudaStream_t st = ctx->stream;
+  MMO_CK(cudaEventRecord(ctx->mc_ev[0], us), "event");
+  MMO_CK(cudaStreamWaitEvent(st, ctx->mc_ev[0], 0), "stream wait");
+  auto body = [&]() -> int {
+    MMO_CK(cudaMemcpyAsync(s.cur, state->dofs, sizeof(float) * B * nd, cudaMemcpyDeviceToDevice, st),
+           "start poses");
+    MMO_CK(launch_k_mc_init(s, p, st), "MC init kernel");
+    int q;
+    if ((q = score_device(ctx, B, s.cur, flags, s.E_cur, nullptr, s.st_trial, ctx->d_err, 0, st)))
+      return q;
+    MMO_CK(launch_k_mc_start(s, p, st), "MC start kernel");
+    // plans and work buffers of both scorings before any capture
+    if (minimize &&
+        (q = score_device(ctx, B, s.cur, flags | MMO_F_GRAD, s.E_trial, s.G_trial, s.st_trial,
+                          ctx->d_err, 0, st)))
+      return q;
+    const int nfull = steps / block, rem = steps % block;
+    if (use_graph && nfull > 0) {
+      std::vector<long> key = {B, block, minimize, prm->minimize_iters, flags, ctx->epoch, nd,
+                               (long)(size_t)ctx->d_mc};
+      const long* pw = reinterpret_cast<const long*>(&p);
+      key.insert(key.end(), pw, pw + sizeof(MCParams) / sizeof(long));
+      if (!ctx->mc_exec || key != ctx->mc_key) {
+        if (ctx->mc_exec) cudaGraphExecDestroy(ctx->mc_exec);
+        ctx->mc_exec = nullptr;
+        MMO_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+        q = mc_block(ctx, s, p, block, minimize, prm->minimize_iters, flags, st);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(st, &g);
+        if (q) {
+          if (g) cudaGraphDestroy(g);
+          return q;
+        }
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "end capture");
+        const cudaError_t ie = cudaGraphInstantiate(&ctx->mc_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) {
+          ctx->mc_exec = nullptr;
+          return cuda_fail(ctx, ie, "graph instantiate");
+        }
+        ctx->mc_key = key;
+      }
+      for (int i = 0; i < nfull; ++i) MMO_CK(cudaGraphLaunch(ctx->mc_exec, st), "graph launch");
+    } else {
+      for (int i = 0; i < nfull; ++i)
+        if ((q = mc_block(ctx, s, p, block, minimize, prm->minimize_iters, flags, st))) return q;
+    }
+    if (rem && (q = mc_block(ctx, s, p, rem, false, 0, flags, st))) return q;
+    MMO_CK(cudaMemcpyAsync(state->dofs, s.cur, sizeof(float) * B * nd, cudaMemcpyDeviceToDevice, st),
+           "final poses");
+    MMO_CK(cudaMemcpyAsync(state->E, s.E_cur, sizeof(double) * B, cudaMemcpyDeviceToDevice, st),
+           "final energies");
+    if (state->best_dofs)
+      MMO_CK(cudaMemcpyAsync(state->best_dofs, s.best, sizeof(float) * B * nd,
+                             cudaMemcpyDeviceToDevice, st), "best poses");
+    if (state->best_E)
+      MMO_CK(cudaMemcpyAsync(state->best_E, s.E_best, sizeof(double) * B, cudaMemcpyDeviceToDevice,
+                             st), "best energies");
+    if (state->accepted)
+      MMO_CK(cudaMemcpyAsync(state->accepted, s.accepted, sizeof(int) * B,
+                             cudaMemcpyDeviceToDevice, st), "accepted moves");
+    if (state->status)
+      MMO_CK(cudaMemcpyAsync(state->status, s.status_or, sizeof(int) * B,
+                             cudaMemcpyDeviceToDevice, st), "status");
+    return MMO_OK;
+  };
+  r = body();
+  ctx->profiling = prof;
+  // the caller's stream waits for the run (also after an error: nothing is left pending)
+  cudaEventRecord(ctx->mc_ev[1], st);
+  cudaStreamWaitEvent(us, ctx->mc_ev[1], 0);
+  return r;
+}
+
+int mmo_philox4x32(mmo_ctx* ctx, unsigned k0, unsigned k1, unsigned c1, unsigned c2, int n,
+                   unsigned* out, void* stream) {
+  if (!ctx) return MMO_EINVAL;
+  if (n < 0 || (n > 0 && !out)) return fail(ctx, MMO_EINVAL, "mmo_philox4x32: bad arguments");
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  MMO_CK(launch_philox(k0, k1, c1, c2, n, reinterpret_cast<uint4*>(out),
+                       reinterpret_cast<cudaStream_t>(stream)),
+         "Philox kernel");
   return MMO_OK;
 }
 

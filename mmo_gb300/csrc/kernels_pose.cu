@@ -75,9 +75,9 @@ __global__ void __launch_bounds__(kRebuildThreads) k_rebuild(DevLigand lig, Pose
     for (int k = lig.grp_off[t] + sub; k < lig.grp_off[t + 1]; k += TPP) {
       const int i = lig.grp_atoms[k];
       const double vx = AT(X, i) - cx, vy = AT(Yc, i) - cy, vz = AT(Zc, i) - cz;
-      AT(X, i) = R0 * vx + R1 * vy + R2 * vz + cx;
-      AT(Yc, i) = R3 * vx + R4 * vy + R5 * vz + cy;
-      AT(Zc, i) = R6 * vx + R7 * vy + R8 * vz + cz;
+      AT(X, i) = fma(R0, vx, fma(R1, vy, fma(R2, vz, cx)));
+      AT(Yc, i) = fma(R3, vx, fma(R4, vy, fma(R5, vz, cy)));
+      AT(Zc, i) = fma(R6, vx, fma(R7, vy, fma(R8, vz, cz)));
     }
     if (RECORD && live && sub == 0) {
       float4* r = scr.rec + ((size_t)b * nrb + t) * 3;
@@ -122,8 +122,9 @@ __global__ void __launch_bounds__(kRebuildThreads) k_rebuild(DevLigand lig, Pose
   if (live) {
     for (int a = sub; a < L; a += TPP) {
       const double vx = AT(X, a) - ox, vy = AT(Yc, a) - oy, vz = AT(Zc, a) - oz;
-      store_split(scr.X + ((size_t)b * L + a) * 2, R0 * vx + R1 * vy + R2 * vz + tx,
-                  R3 * vx + R4 * vy + R5 * vz + ty, R6 * vx + R7 * vy + R8 * vz + tz);
+      store_split(scr.X + ((size_t)b * L + a) * 2, fma(R0, vx, fma(R1, vy, fma(R2, vz, tx))),
+                  fma(R3, vx, fma(R4, vy, fma(R5, vz, ty))),
+                  fma(R6, vx, fma(R7, vy, fma(R8, vz, tz))));
       if (RECORD)
         scr.Y[(size_t)b * L + a] = make_float4((float)AT(X, a), (float)AT(Yc, a),
                                                 (float)AT(Zc, a), 0.f);

@@ -183,7 +183,50 @@ struct CullPlan {
   int smem;              // dynamic shared memory of the sweep
 };
 
+// ---- Monte Carlo chains (kernels_mc.cu) ----------------------------------
+enum : int { kMcUniform = 0, kMcGaussian = 1 };
+constexpr int kMcCounts = 4;   // per chain: step, rigid accepted in block, rigid moves, conformer moves
+constexpr int kMcBlock = 100;  // moves per adaptation block (params.ml:29)
+
+struct MCDev {
+  float* cur;       // [B][nd] current poses (optimiser layout)
+  float* trial;     // [B][nd] proposed poses
+  double* E_cur;    // [B]
+  double* E_trial;  // [B]
+  float* G_cur;     // [B][nd] gradient at the current pose (minimiser)
+  float* G_trial;   // [B][nd]
+  int* st_trial;    // [B] status bits of the trial pose
+  float* best;      // [B][nd] lowest-energy pose seen
+  double* E_best;   // [B]
+  float* steps;     // [B][2 + nrb] rotation (rad), translation (A), per-bond torsion step (rad)
+  int* cnt;         // [B][kMcCounts + 2 nrb] counters, then per bond (accepted, tried) in block
+  int* moved;       // [B] bond of the last conformer move, -1 after a rigid move
+  int* accepted;    // [B] accepted moves
+  int* status_or;   // [B] OR of the status bits of every scored pose
+  float* eta;       // [B] gradient-descent step
+};
+
+struct MCParams {
+  double kT;        // kcal/mol
+  float rot, trans, tors, gd_step;
+  int law;          // kMcUniform (Move.rand_*) or kMcGaussian
+  int adapt;        // step-size adaptation per 100 moves
+  int flip_every;   // uniform law: every flip_every-th conformer move in [-pi, pi]
+  uint32_t key0, key1;
+  int B, nd, nrb;
+};
+
 // ---- launchers (defined in the .cu files) --------------------------------
+cudaError_t launch_k_mc_init(const MCDev& s, const MCParams& p, cudaStream_t st);
+cudaError_t launch_k_mc_start(const MCDev& s, const MCParams& p, cudaStream_t st);
+cudaError_t launch_k_mc_propose(const MCDev& s, const MCParams& p, cudaStream_t st);
+cudaError_t launch_k_mc_accept(const MCDev& s, const MCParams& p, cudaStream_t st);
+cudaError_t launch_k_gd_begin(const MCDev& s, const MCParams& p, cudaStream_t st);
+cudaError_t launch_k_gd_propose(const MCDev& s, const MCParams& p, cudaStream_t st);
+cudaError_t launch_k_gd_accept(const MCDev& s, const MCParams& p, cudaStream_t st);
+cudaError_t launch_k_gd_take(const MCDev& s, const MCParams& p, cudaStream_t st);
+cudaError_t launch_philox(uint32_t k0, uint32_t k1, uint32_t c1, uint32_t c2, int n, uint4* out,
+                          cudaStream_t st);
 cudaError_t launch_rebuild(const DevLigand& lig, const PoseIO& io, const Scratch& s, int flags,
                            cudaStream_t st);
 cudaError_t launch_pairs_batched(const DevProtein& prot, const float4* tab,
@@ -249,9 +292,9 @@ __device__ __forceinline__ void uff_pair(float dx, float dy, float dz, float x2,
   const float p2 = x2 * ir2;
   const float p6 = p2 * p2 * p2;
   const float Dp6 = D * p6;
-  const float lj = Dp6 * (p6 - 2.0f);
+  // explicit fused forms: the energy rounds the same in every kernel variant
   const float el = DIEL == 0 ? qq * ir : qq * ir2;
-  const float e = lj + el;
+  const float e = fmaf(Dp6, p6 - 2.0f, el);
   float s = 1.0f, w = 1.0f;
   if (FORM == 0) {
     s = fmaxf(fmaf(r2c, -1.0f / 144.0f, 1.0f), 0.0f);
@@ -283,7 +326,7 @@ __device__ __forceinline__ void uff_pair_eg(float dx, float dy, float dz, float 
   const float p6 = p2 * p2 * p2;
   const float Dp6 = D * p6;
   const float el = DIEL == 0 ? qq * ir : qq * ir2;
-  const float e = Dp6 * (p6 - 2.0f) + el;
+  const float e = fmaf(Dp6, p6 - 2.0f, el);
   float s = 1.0f, w = 1.0f;
   if (FORM == 0) {
     s = fmaxf(fmaf(r2c, -1.0f / 144.0f, 1.0f), 0.0f);

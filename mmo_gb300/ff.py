@@ -132,6 +132,18 @@ class UFFScorer:
         return {"sweep": "full", "poses_per_lane": lane, "threads": threads,
                 "protein_chunks": pc}
 
+    def mc_run_device(self, chains: int, steps: int, params, d_dofs: int, d_E: int,
+                      d_best_dofs: int | None = None, d_best_E: int | None = None,
+                      d_accepted: int | None = None, d_status: int | None = None,
+                      stream: int | None = None, graph: bool = True) -> None:
+        """Monte Carlo chains (mmo_mc_run) on device buffers; params is a
+        lib.MCParams or a dict of its fields."""
+        if isinstance(params, dict):
+            params = _L.MCParams(**params)
+        st = _L.MCState(d_dofs, d_E, d_best_dofs, d_best_E, d_accepted, d_status)
+        self._check(self._lib.mmo_mc_run(self._h, chains, steps, C.byref(params), C.byref(st),
+                                         stream, int(graph)))
+
     def sms(self) -> int:
         out = C.c_int()
         self._check(self._lib.mmo_device_sms(self._h, C.byref(out)))

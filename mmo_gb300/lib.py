@@ -19,6 +19,23 @@ INTRA_PLAIN, INTRA_SHIFTED = 0, 1
 F_INTER, F_INTRA, F_GRAD, F_RECENTER = 1, 2, 4, 8
 S_TOO_LONG, S_NONFINITE = 1, 2
 
+MC_UNIFORM, MC_GAUSSIAN = 0, 1
+
+
+class MCParams(C.Structure):
+    """mmo_mc_params of include/mmo_mc.h."""
+    _fields_ = [("kT", C.c_double), ("rot_step", C.c_double), ("trans_step", C.c_double),
+                ("tors_step", C.c_double), ("move_law", C.c_int), ("adapt", C.c_int),
+                ("flip_every", C.c_int), ("minimize_every", C.c_int),
+                ("minimize_iters", C.c_int), ("gd_step", C.c_double), ("seed", C.c_ulonglong)]
+
+
+class MCState(C.Structure):
+    """mmo_mc_state of include/mmo_mc.h (device pointers)."""
+    _fields_ = [("dofs", C.c_void_p), ("E", C.c_void_p), ("best_dofs", C.c_void_p),
+                ("best_E", C.c_void_p), ("accepted", C.c_void_p), ("status", C.c_void_p)]
+
+
 # every symbol the header declares, with its ctypes signature
 _P = C.POINTER
 _d, _i, _vp, _cp = C.c_double, C.c_int, C.c_void_p, C.c_char_p
@@ -38,6 +55,8 @@ SIGNATURES = {
     "mmo_sync": (_i, [_vp, _vp]),
     "mmo_set_tiles": (_i, [_vp, _i, _i, _i]),
     "mmo_set_cull": (_i, [_vp, _i, C.c_double, _i, _i]),
+    "mmo_mc_run": (_i, [_vp, _i, _i, _P(MCParams), _P(MCState), _vp, _i]),
+    "mmo_philox4x32": (_i, [_vp, C.c_uint, C.c_uint, C.c_uint, C.c_uint, _i, _vp, _vp]),
     "mmo_tune": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp, _vp, _P(C.c_double)]),
     "mmo_set_tune_cache": (_i, [_vp, C.c_char_p]),
     "mmo_get_plan": (_i, [_vp, _P(C.c_int), _P(C.c_int), _P(C.c_int), _P(C.c_int),

@@ -683,3 +683,36 @@ void orc_score_batch(const orc_physics *ph, const orc_mol *prot, const orc_ligan
   free(th);
   orc_cells_free(cells);
 }
+
+/* ---- counter-based RNG of the Monte Carlo chains ---------------------------
+ * Philox4x32-10 (J. K. Salmon, M. A. Moraes, R. O. Dror, D. E. Shaw, "Parallel
+ * random numbers: as easy as 1, 2, 3", SC 2011): ten rounds of two 32x32->64
+ * multiplications by 0xD2511F53 and 0xCD9E8D57, the key bumped by the Weyl
+ * constants 0x9E3779B9 and 0xBB67AE85 between rounds.  The reference draws from
+ * OCaml's Random.State (src/lds.ml:931-934, src/move.ml:14-54); a counter-based
+ * generator keyed per chain replaces it so that chains are independent and
+ * reproducible in parallel. */
+void orc_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4]) {
+  uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+  uint32_t k0 = key_in[0], k1 = key_in[1];
+  for (int r = 0; r < 10; ++r) {
+    if (r) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+    const uint32_t n1 = (uint32_t)p1;
+    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+    const uint32_t n3 = (uint32_t)p0;
+    c0 = n0;
+    c1 = n1;
+    c2 = n2;
+    c3 = n3;
+  }
+  out[0] = c0;
+  out[1] = c1;
+  out[2] = c2;
+  out[3] = c3;
+}

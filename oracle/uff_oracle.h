@@ -124,6 +124,9 @@ void orc_score_batch(const orc_physics *ph, const orc_mol *prot, const orc_ligan
                      int B, const float *dofs, int flags, int mode, const double *eps,
                      int use_cells, int nthreads, double *E, double *grad, int *status);
 
+/* Philox4x32-10 block: out = philox(ctr, key) */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -45,6 +45,8 @@ def test_null_context_is_rejected(gpu_lib):
     assert gpu_lib.mmo_score_poses(None, 1, None, 0, None, None, None) == lib.EINVAL
     assert gpu_lib.mmo_sync(None, None) == lib.EINVAL
     assert gpu_lib.mmo_ctx_create(0, None) == lib.EINVAL
+    assert gpu_lib.mmo_mc_run(None, 1, 1, None, None, None, 1) == lib.EINVAL
+    assert gpu_lib.mmo_tune(None, 1, None, 0, None, None, None, None, None) == lib.EINVAL
 
 
 def test_create_without_gpu_fails_cleanly(gpu_lib):

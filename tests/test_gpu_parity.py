@@ -236,6 +236,20 @@ def test_cull_non_finite_pose(scorer_factory, batch):
     assert np.array_equal(E[keep], E1[keep])
 
 
+@pytest.mark.parametrize("sweep", ["cut-off", "full"])
+def test_energy_same_with_and_without_gradient(scorer_factory, batch, sweep):
+    """Asking for the gradient does not change the energies, bit for bit, in
+    the batched and the one-pose paths, with either pose map."""
+    s = scorer_factory(batch.pocket, batch.ligand)
+    if sweep == "full":
+        s.set_cull(mode=1)
+    for rc in (False, True):
+        for d in (batch.poses[:100], batch.poses[:1]):
+            E0, _, st0 = s.score_poses(d, recenter=rc)
+            E1, _, st1 = s.score_poses(d, grad=True, recenter=rc)
+            assert np.array_equal(E0, E1) and np.array_equal(st0, st1)
+
+
 def test_deterministic(scorer_factory, batch):
     s = scorer_factory(batch.pocket, batch.ligand)
     a = s.score_poses(batch.poses, grad=True)

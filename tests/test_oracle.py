@@ -225,3 +225,22 @@ def test_batch_matches_single(oracle):
         e, g, _ = oracle.grad_analytic(s.pocket, s.ligand, conf)
         assert E[b] == e and np.array_equal(G[b], g)
         assert Ec[b] == pytest.approx(e, rel=1e-12)
+
+
+def test_philox_known_answers(oracle):
+    """Philox4x32-10 against the known-answer vectors published with the
+    algorithm (Random123 kat_vectors: zero, all-ones and the pi digits)."""
+    import ctypes as C
+
+    f = oracle.lib().orc_philox4x32_10
+
+    def ph(ctr, key):
+        c, k, o = (C.c_uint32 * 4)(*ctr), (C.c_uint32 * 2)(*key), (C.c_uint32 * 4)()
+        f(c, k, o)
+        return list(o)
+
+    assert ph([0, 0, 0, 0], [0, 0]) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    assert ph([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2) == [0x408F276D, 0x41C83B0E, 0xA20BC7C6,
+                                                      0x6D5451FD]
+    assert ph([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0]) == \
+        [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
