@@ -15,6 +15,7 @@
 #include "../../include/mmo_diag.h"
 #include "../../include/mmo_gpu.h"
 #include "../../include/mmo_mc.h"
+#include "../../include/mmo_systems.h"
 #include "mmo_internal.cuh"
 
 using namespace mmo;
@@ -157,6 +158,7 @@ struct mmo_ctx {
   std::vector<long> mc_key;
   cudaEvent_t mc_ev[2] = {nullptr, nullptr};
   long epoch = 0;  // bumped whenever baked launch arguments (buffers, uploads, plans) change
+  struct SysBatch* sys = nullptr;  // ragged batch of systems (mmo_set_systems)
 
   // host-API staging
   char* h_in = nullptr;
@@ -258,18 +260,60 @@ int ensure_scratch(mmo_ctx* ctx, int B, int L, int C, bool grad) {
   return MMO_OK;
 }
 
-int upload_ligand(mmo_ctx* ctx) {
-  const int n = (int)ctx->lx.size(), nrb = (int)ctx->lbonds.size() / 2;
+// Host image of a ligand's device blob and what is needed to lay it out at
+// any base address.
+struct LigIn {
+  std::vector<double> x, y, z, q;
+  std::vector<int> type, bonds, goff, gat;
+  std::vector<uint8_t> inter;
+};
+
+struct LigBlob {
+  std::vector<char> host;
+  std::vector<int> seg_type, seg_count;
+  int n = 0, nrb = 0, np = 0, nbonds = 0, ngmask = 0, ngat = 0, nnb = 0;
+  bool nested = false;
+};
+
+DevLigand ligand_at(const LigBlob& B, char* b, size_t* bytes) {
+  size_t off = 0;
+  DevLigand L{};
+  const int n = B.n, nrb = B.nrb, np = B.np;
+  L.L = n;
+  L.nrb = nrb;
+  L.npairs = np;
+  L.nested = B.nested ? 1 : 0;
+  L.ref = align_ptr<float4>(b, off, n);
+  L.ref64 = align_ptr<double>(b, off, 3 * (size_t)n);
+  L.type = align_ptr<int>(b, off, n);
+  L.q = align_ptr<float>(b, off, n);
+  L.bonds = align_ptr<int2>(b, off, B.nbonds);
+  L.gmask = align_ptr<uint32_t>(b, off, B.ngmask);
+  L.pair_ij = align_ptr<int2>(b, off, std::max(np, 1));
+  L.pair_par = align_ptr<float4>(b, off, std::max(np, 1));
+  L.amask = align_ptr<uint32_t>(b, off, n);
+  L.grp_off = align_ptr<int>(b, off, nrb + 1);
+  L.grp_atoms = align_ptr<int>(b, off, std::max(B.ngat, 1));
+  L.nb_off = align_ptr<int>(b, off, n + 1);
+  L.nb_idx = align_ptr<int>(b, off, std::max(B.nnb, 1));
+  L.nb_par = align_ptr<float4>(b, off, std::max(B.nnb, 1));
+  L.seg_of_atom = align_ptr<int>(b, off, n);
+  if (bytes) *bytes = off;
+  return L;
+}
+
+void make_ligand_blob(int mixing, const LigIn& in, LigBlob* out) {
+  const int n = (int)in.x.size(), nrb = (int)in.bonds.size() / 2;
   // interacting pairs (mol.ml:203-208), i < j, in the reference's loop order
   std::vector<int2> pij;
   std::vector<float4> ppar;
   std::vector<std::vector<std::pair<int, float4>>> nb(n);
   for (int i = 0; i < n - 1; ++i)
     for (int j = i + 1; j < n; ++j) {
-      if (!ctx->linter[(size_t)i * n + j]) continue;
+      if (!in.inter[(size_t)i * n + j]) continue;
       double x2, d;
-      pair_xd(ctx->ph.mixing, ctx->ltype[i], ctx->ltype[j], &x2, &d);
-      const float4 par = make_float4((float)x2, (float)d, (float)(kElec * ctx->lq[i] * ctx->lq[j]), 0.f);
+      pair_xd(mixing, in.type[i], in.type[j], &x2, &d);
+      const float4 par = make_float4((float)x2, (float)d, (float)(kElec * in.q[i] * in.q[j]), 0.f);
       pij.push_back(make_int2(i, j));
       ppar.push_back(par);
       nb[i].push_back({j, par});
@@ -286,19 +330,19 @@ int upload_ligand(mmo_ctx* ctx) {
   }
   std::vector<float4> ref(n);
   for (int i = 0; i < n; ++i)
-    ref[i] = make_float4((float)ctx->lx[i], (float)ctx->ly[i], (float)ctx->lz[i], (float)ctx->lq[i]);
+    ref[i] = make_float4((float)in.x[i], (float)in.y[i], (float)in.z[i], (float)in.q[i]);
   std::vector<uint32_t> gmask((size_t)std::max(nrb, 1) * kSlots, 0u);
   for (int t = 0; t < nrb; ++t)
-    for (int k = ctx->lgoff[t]; k < ctx->lgoff[t + 1]; ++k) {
-      const int a = ctx->lgatoms[k];
+    for (int k = in.goff[t]; k < in.goff[t + 1]; ++k) {
+      const int a = in.gat[k];
       gmask[(size_t)t * kSlots + (a >> 5)] |= 1u << (a & 31);
     }
   std::vector<int2> bonds(std::max(nrb, 1));
-  for (int t = 0; t < nrb; ++t) bonds[t] = make_int2(ctx->lbonds[2 * t], ctx->lbonds[2 * t + 1]);
+  for (int t = 0; t < nrb; ++t) bonds[t] = make_int2(in.bonds[2 * t], in.bonds[2 * t + 1]);
   // nested groups: every two groups nested or disjoint; the axis of an inner
   // group inside its outer group or on the outer axis; no axis atom of one of
   // two disjoint groups inside the other
-  auto in = [&](int t, int a) { return (gmask[(size_t)t * kSlots + (a >> 5)] >> (a & 31)) & 1u; };
+  auto has = [&](int t, int a) { return (gmask[(size_t)t * kSlots + (a >> 5)] >> (a & 31)) & 1u; };
   auto subset = [&](int t, int u) {  // G_t subset of G_u
     for (int w = 0; w < kSlots; ++w)
       if (gmask[(size_t)t * kSlots + w] & ~gmask[(size_t)u * kSlots + w]) return false;
@@ -315,60 +359,43 @@ int upload_ligand(mmo_ctx* ctx) {
       if (t == u) continue;
       const int ul = bonds[u].x, ur = bonds[u].y, tl = bonds[t].x, tr = bonds[t].y;
       if (disjoint(t, u)) {
-        nested = !in(t, ul) && !in(t, ur);
+        nested = !has(t, ul) && !has(t, ur);
       } else if (subset(u, t)) {
-        nested = (in(t, ul) || ul == tl || ul == tr) && (in(t, ur) || ur == tl || ur == tr);
+        nested = (has(t, ul) || ul == tl || ul == tr) && (has(t, ur) || ur == tl || ur == tr);
       } else if (!subset(t, u)) {
         nested = false;
       }
     }
   const int np = (int)pij.size();
-  // one blob: sizes first, then copy
-  size_t off = 0;
-  char* base = nullptr;
-  auto layout = [&](char* b) {
-    off = 0;
-    DevLigand L{};
-    L.L = n;
-    L.nrb = nrb;
-    L.npairs = np;
-    L.nested = nested ? 1 : 0;
-    L.ref = align_ptr<float4>(b, off, n);
-    L.ref64 = align_ptr<double>(b, off, 3 * (size_t)n);
-    L.type = align_ptr<int>(b, off, n);
-    L.q = align_ptr<float>(b, off, n);
-    L.bonds = align_ptr<int2>(b, off, bonds.size());
-    L.gmask = align_ptr<uint32_t>(b, off, gmask.size());
-    L.pair_ij = align_ptr<int2>(b, off, std::max(np, 1));
-    L.pair_par = align_ptr<float4>(b, off, std::max(np, 1));
-    L.amask = align_ptr<uint32_t>(b, off, n);
-    L.grp_off = align_ptr<int>(b, off, nrb + 1);
-    L.grp_atoms = align_ptr<int>(b, off, std::max((int)ctx->lgatoms.size(), 1));
-    L.nb_off = align_ptr<int>(b, off, n + 1);
-    L.nb_idx = align_ptr<int>(b, off, std::max((int)nb_idx.size(), 1));
-    L.nb_par = align_ptr<float4>(b, off, std::max((int)nb_par.size(), 1));
-    L.seg_of_atom = align_ptr<int>(b, off, n);
-    return L;
-  };
-  layout(nullptr);
-  const size_t bytes = off;
-  std::vector<char> host(bytes, 0);
-  DevLigand H = layout(host.data());
+  LigBlob& B = *out;
+  B.n = n;
+  B.nrb = nrb;
+  B.np = np;
+  B.nbonds = (int)bonds.size();
+  B.ngmask = (int)gmask.size();
+  B.ngat = (int)in.gat.size();
+  B.nnb = (int)nb_idx.size();
+  B.nested = nested;
+  size_t bytes = 0;
+  ligand_at(B, nullptr, &bytes);
+  B.host.assign(bytes, 0);
+  std::vector<char>& host = B.host;
+  DevLigand H = ligand_at(B, host.data(), nullptr);
   for (int t = 0; t < nrb; ++t)
-    for (int k = ctx->lgoff[t]; k < ctx->lgoff[t + 1]; ++k)
-      const_cast<uint32_t*>(H.amask)[ctx->lgatoms[k]] |= 1u << t;
-  memcpy((void*)H.grp_off, ctx->lgoff.data(), sizeof(int) * (nrb + 1));
-  if (!ctx->lgatoms.empty())
-    memcpy((void*)H.grp_atoms, ctx->lgatoms.data(), sizeof(int) * ctx->lgatoms.size());
+    for (int k = in.goff[t]; k < in.goff[t + 1]; ++k)
+      const_cast<uint32_t*>(H.amask)[in.gat[k]] |= 1u << t;
+  memcpy((void*)H.grp_off, in.goff.data(), sizeof(int) * (nrb + 1));
+  if (!in.gat.empty())
+    memcpy((void*)H.grp_atoms, in.gat.data(), sizeof(int) * in.gat.size());
   memcpy((void*)H.ref, ref.data(), sizeof(float4) * n);
   for (int i = 0; i < n; ++i) {
     double* r64 = const_cast<double*>(H.ref64) + 3 * i;
-    r64[0] = ctx->lx[i];
-    r64[1] = ctx->ly[i];
-    r64[2] = ctx->lz[i];
+    r64[0] = in.x[i];
+    r64[1] = in.y[i];
+    r64[2] = in.z[i];
   }
-  memcpy((void*)H.type, ctx->ltype.data(), sizeof(int) * n);
-  for (int i = 0; i < n; ++i) const_cast<float*>(H.q)[i] = (float)ctx->lq[i];
+  memcpy((void*)H.type, in.type.data(), sizeof(int) * n);
+  for (int i = 0; i < n; ++i) const_cast<float*>(H.q)[i] = (float)in.q[i];
   memcpy((void*)H.bonds, bonds.data(), sizeof(int2) * bonds.size());
   memcpy((void*)H.gmask, gmask.data(), sizeof(uint32_t) * gmask.size());
   if (np) {
@@ -379,55 +406,78 @@ int upload_ligand(mmo_ctx* ctx) {
   }
   memcpy((void*)H.nb_off, nb_off.data(), sizeof(int) * (n + 1));
   // type segments of the cut-off sweep: the ligand's types in ascending order
-  ctx->lseg_type.clear();
-  ctx->lseg_count.clear();
+  B.seg_type.clear();
+  B.seg_count.clear();
   for (int t = 0; t < kNTypes; ++t) {
-    const int c = (int)std::count(ctx->ltype.begin(), ctx->ltype.end(), t);
+    const int c = (int)std::count(in.type.begin(), in.type.end(), t);
     if (!c) continue;
     for (int i = 0; i < n; ++i)
-      if (ctx->ltype[i] == t) const_cast<int*>(H.seg_of_atom)[i] = (int)ctx->lseg_type.size();
-    ctx->lseg_type.push_back(t);
-    ctx->lseg_count.push_back(c);
+      if (in.type[i] == t) const_cast<int*>(H.seg_of_atom)[i] = (int)B.seg_type.size();
+    B.seg_type.push_back(t);
+    B.seg_count.push_back(c);
   }
+}
+
+int upload_ligand(mmo_ctx* ctx) {
+  LigIn in;
+  in.x = ctx->lx;
+  in.y = ctx->ly;
+  in.z = ctx->lz;
+  in.q = ctx->lq;
+  in.type = ctx->ltype;
+  in.bonds = ctx->lbonds;
+  in.goff = ctx->lgoff;
+  in.gat = ctx->lgatoms;
+  in.inter = ctx->linter;
+  LigBlob B;
+  make_ligand_blob(ctx->ph.mixing, in, &B);
+  ctx->lseg_type = B.seg_type;
+  ctx->lseg_count = B.seg_count;
   MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before ligand upload");
   if (ctx->d_lig) cudaFree(ctx->d_lig);
   ctx->d_lig = nullptr;
-  MMO_CK(cudaMalloc(&ctx->d_lig, bytes), "ligand blob");
-  MMO_CK(cudaMemcpy(ctx->d_lig, host.data(), bytes, cudaMemcpyHostToDevice), "ligand upload");
-  base = reinterpret_cast<char*>(ctx->d_lig);
-  ctx->lig = layout(base);
+  MMO_CK(cudaMalloc(&ctx->d_lig, B.host.size()), "ligand blob");
+  MMO_CK(cudaMemcpy(ctx->d_lig, B.host.data(), B.host.size(), cudaMemcpyHostToDevice),
+         "ligand upload");
+  ctx->lig = ligand_at(B, reinterpret_cast<char*>(ctx->d_lig), nullptr);
   ctx->has_lig = true;
   ++ctx->lig_version;
   ++ctx->epoch;
   return MMO_OK;
 }
 
-// Row index of the protein for the cut-off sweep: rows of a (y, z) grid of
+// Row index of a protein for the cut-off sweep: rows of a (y, z) grid of
 // spacing h in (iz, iy) order, empty rows dropped, each row sorted by x; a
-// flush point after the row where 256 atoms have accumulated.
-int build_cull(mmo_ctx* ctx) {
-  ctx->cull_ok = false;
-  ctx->cull_rows.clear();
-  if (ctx->d_cull) {
-    MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before row index upload");
-    cudaFree(ctx->d_cull);
-  }
-  ctx->d_cull = nullptr;
-  const int n = (int)ctx->pxs.size();
-  if (n <= 0) return MMO_OK;
+// flush point after the row where 256 atoms have accumulated.  Coordinates are
+// in the device frame (origin subtracted).
+struct RowIndex {
+  std::vector<float4> atoms;    // [n][2]
+  std::vector<int> rs;          // [nrows + 1]
+  std::vector<float4> rbox;     // [nrows]
+  std::vector<int> flush_end;   // [nrows]
+  float lo[3], hi[3];           // bounding box (hi parts)
+};
+
+void build_rows(int n, const double* px, const double* py, const double* pz, const float* pkq,
+                const int* ptypes, double h, RowIndex* out) {
+  RowIndex& R = *out;
   std::vector<float> fx(n), fy(n), fz(n);
-  float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+  float* lo = R.lo;
+  float* hi = R.hi;
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = 1e30f;
+    hi[d] = -1e30f;
+  }
   for (int i = 0; i < n; ++i) {
-    fx[i] = (float)ctx->pxs[i];
-    fy[i] = (float)ctx->pys[i];
-    fz[i] = (float)ctx->pzs[i];
+    fx[i] = (float)px[i];
+    fy[i] = (float)py[i];
+    fz[i] = (float)pz[i];
     const float v[3] = {fx[i], fy[i], fz[i]};
     for (int d = 0; d < 3; ++d) {
       lo[d] = std::min(lo[d], v[d]);
       hi[d] = std::max(hi[d], v[d]);
     }
   }
-  double h = ctx->cull_h > 0 ? ctx->cull_h : 3.0;
   long ny = 0, nz = 0;
   for (;;) {
     ny = (long)std::floor((hi[1] - lo[1]) / h) + 1;
@@ -448,49 +498,83 @@ int build_cull(mmo_ctx* ctx) {
     if (fx[a] != fx[b]) return fx[a] < fx[b];
     return a < b;
   });
-  std::vector<float4> atoms(2 * (size_t)n);
-  std::vector<int> rs;
-  std::vector<float4> rbox;
+  R.atoms.assign(2 * (size_t)n, make_float4(0.f, 0.f, 0.f, 0.f));
+  R.rs.clear();
+  R.rbox.clear();
   std::vector<int> rflush;
   int since = 0;
   for (int k = 0; k < n; ++k) {
     const int i = idx[k];
-    split_store(&atoms[2 * (size_t)k], ctx->pxs[i], ctx->pys[i], ctx->pzs[i], ctx->pkq[i]);
-    const int tb = ctx->ptypes[i] * kNTypes * (int)sizeof(float4);
-    memcpy(&atoms[2 * (size_t)k + 1].w, &tb, sizeof tb);
+    split_store(&R.atoms[2 * (size_t)k], px[i], py[i], pz[i], pkq[i]);
+    const int tb = ptypes[i] * kNTypes * (int)sizeof(float4);
+    memcpy(&R.atoms[2 * (size_t)k + 1].w, &tb, sizeof tb);
     if (k == 0 || key[i] != key[idx[k - 1]]) {
       if (k) {
-        since += k - rs.back();
+        since += k - R.rs.back();
         rflush.push_back(since >= kCullFlush);
         if (since >= kCullFlush) since = 0;
       }
-      rs.push_back(k);
-      rbox.push_back(make_float4(1e30f, -1e30f, 1e30f, -1e30f));
+      R.rs.push_back(k);
+      R.rbox.push_back(make_float4(1e30f, -1e30f, 1e30f, -1e30f));
     }
-    float4& b = rbox.back();
-    b.x = std::min(b.x, fy[i]);
-    b.y = std::max(b.y, fy[i]);
-    b.z = std::min(b.z, fz[i]);
-    b.w = std::max(b.w, fz[i]);
+    float4& bx = R.rbox.back();
+    bx.x = std::min(bx.x, fy[i]);
+    bx.y = std::max(bx.y, fy[i]);
+    bx.z = std::min(bx.z, fz[i]);
+    bx.w = std::max(bx.w, fz[i]);
   }
   rflush.push_back(1);
-  rs.push_back(n);
-  const int nrows = (int)rbox.size();
+  R.rs.push_back(n);
+  const int nrows = (int)R.rbox.size();
   // flag -> end of the flush block that holds the row
+  R.flush_end.assign(nrows, nrows);
   for (int r = nrows - 1, end = nrows; r >= 0; --r) {
     if (rflush[r]) end = r + 1;
-    rflush[r] = end;
+    R.flush_end[r] = end;
   }
+}
+
+// pieces of a row index: consecutive rows of about piece_atoms atoms, as row
+// boundaries [0 .. nrows]
+std::vector<int> row_pieces(const std::vector<int>& rs, int piece_atoms) {
+  const int nrows = (int)rs.size() - 1;
+  std::vector<int> pr{0};
+  int acc = 0;
+  for (int r = 0; r < nrows; ++r) {
+    acc += rs[r + 1] - rs[r];
+    if (acc >= piece_atoms && r + 1 < nrows) {
+      pr.push_back(r + 1);
+      acc = 0;
+    }
+  }
+  pr.push_back(nrows);
+  return pr;
+}
+
+int build_cull(mmo_ctx* ctx) {
+  ctx->cull_ok = false;
+  ctx->cull_rows.clear();
+  if (ctx->d_cull) {
+    MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before row index upload");
+    cudaFree(ctx->d_cull);
+  }
+  ctx->d_cull = nullptr;
+  const int n = (int)ctx->pxs.size();
+  if (n <= 0) return MMO_OK;
+  RowIndex R;
+  build_rows(n, ctx->pxs.data(), ctx->pys.data(), ctx->pzs.data(), ctx->pkq.data(),
+             ctx->ptypes.data(), ctx->cull_h > 0 ? ctx->cull_h : 3.0, &R);
+  const int nrows = (int)R.rbox.size();
   size_t off = 0;
-  const size_t o_atoms = take(off, sizeof(float4) * atoms.size());
-  const size_t o_rs = take(off, sizeof(int) * rs.size());
-  const size_t o_box = take(off, sizeof(float4) * rbox.size());
-  const size_t o_fl = take(off, sizeof(int) * rflush.size());
+  const size_t o_atoms = take(off, sizeof(float4) * R.atoms.size());
+  const size_t o_rs = take(off, sizeof(int) * R.rs.size());
+  const size_t o_box = take(off, sizeof(float4) * R.rbox.size());
+  const size_t o_fl = take(off, sizeof(int) * R.flush_end.size());
   std::vector<char> blob(off, 0);
-  memcpy(blob.data() + o_atoms, atoms.data(), sizeof(float4) * atoms.size());
-  memcpy(blob.data() + o_rs, rs.data(), sizeof(int) * rs.size());
-  memcpy(blob.data() + o_box, rbox.data(), sizeof(float4) * rbox.size());
-  memcpy(blob.data() + o_fl, rflush.data(), sizeof(int) * rflush.size());
+  memcpy(blob.data() + o_atoms, R.atoms.data(), sizeof(float4) * R.atoms.size());
+  memcpy(blob.data() + o_rs, R.rs.data(), sizeof(int) * R.rs.size());
+  memcpy(blob.data() + o_box, R.rbox.data(), sizeof(float4) * R.rbox.size());
+  memcpy(blob.data() + o_fl, R.flush_end.data(), sizeof(int) * R.flush_end.size());
   MMO_CK(cudaMalloc(&ctx->d_cull, off), "protein row index");
   MMO_CK(cudaMemcpy(ctx->d_cull, blob.data(), off, cudaMemcpyHostToDevice), "row index upload");
   DevCull c{};
@@ -503,12 +587,12 @@ int build_cull(mmo_ctx* ctx) {
   c.nrows = nrows;
   // entry binning: a cube about the protein's box, 2 A beyond it
   float side = 0.f;
-  for (int d = 0; d < 3; ++d) side = std::max(side, hi[d] - lo[d]);
+  for (int d = 0; d < 3; ++d) side = std::max(side, R.hi[d] - R.lo[d]);
   side += 4.0f;
-  for (int d = 0; d < 3; ++d) c.glo[d] = 0.5f * (lo[d] + hi[d]) - 0.5f * side;
+  for (int d = 0; d < 3; ++d) c.glo[d] = 0.5f * (R.lo[d] + R.hi[d]) - 0.5f * side;
   c.ginv = (float)kCullGrid / side;
   ctx->cull = c;
-  ctx->cull_rows = rs;
+  ctx->cull_rows = R.rs;
   ++ctx->cull_version;
   ++ctx->epoch;
   // the sweep keeps the whole protein and its index in shared memory
@@ -588,19 +672,7 @@ int cull_plan_for(mmo_ctx* ctx, int B, bool grad) {
   p.threads = std::min(ctx->tile_threads ? ctx->tile_threads : 1024, cull_max_threads(p.kp));
   p.piece_atoms = ctx->cull_piece ? ctx->cull_piece : 256;
   if (ctx->piece_key[0] != ctx->cull_version || ctx->piece_key[1] != p.piece_atoms) {
-    // pieces: consecutive rows of about piece_atoms atoms
-    const std::vector<int>& rs = ctx->cull_rows;
-    const int nrows = (int)rs.size() - 1;
-    std::vector<int> pr{0};
-    int acc = 0;
-    for (int r = 0; r < nrows; ++r) {
-      acc += rs[r + 1] - rs[r];
-      if (acc >= p.piece_atoms && r + 1 < nrows) {
-        pr.push_back(r + 1);
-        acc = 0;
-      }
-    }
-    pr.push_back(nrows);
+    const std::vector<int> pr = row_pieces(ctx->cull_rows, p.piece_atoms);
     int r = grow(ctx, (void**)&ctx->d_piece, &ctx->capPiece, sizeof(int) * pr.size(),
                  "piece table");
     if (r) return r;
@@ -761,6 +833,421 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
 
 }  // namespace
 
+// ---- ragged batch of systems ----------------------------------------------
+struct SysBatch {
+  struct Sys {              // one user system
+    LigIn lig;
+    std::vector<double> px, py, pz;  // device frame
+    std::vector<float> pkq;
+    std::vector<int> ptype;
+    float origin[3];
+    int poses;
+  };
+  std::vector<Sys> in;
+  std::vector<int> pose_off, dof_off;  // per user system, nsys + 1
+  int B = 0, D = 0;                    // poses, DOF floats
+  // static layout (rebuilt when the physics or the row spacing changes)
+  long built_key[2] = {-1, -1};        // (mixing, row spacing in 1e-3 A)
+  std::vector<SysInfo> info;           // virtual systems: user systems cut to sort-sized pose ranges
+  std::vector<int> vuser;              // virtual -> user system
+  std::vector<std::vector<int>> rows;  // per user system: row starts of its row index
+  std::vector<int> atom0, row0;        // per user system: packed atom and row offsets
+  std::vector<std::vector<int>> segcount, segtype;  // per user system: ligand type segments
+  std::vector<int> Ls, nrbs;
+  void* d_static = nullptr;
+  size_t cap_static = 0;
+  DevSystems dev{};
+  int E = 0, R = 0, nrblk = 0, nfblk = 0, tpp = 4, Lmax = 1, nrbmax = 0;
+  // plan (pieces, groups, items) for (kp, piece atoms)
+  long plan_key[3] = {-1, -1, -1};
+  void* d_plan = nullptr;
+  size_t cap_plan = 0;
+  int kp = 2, threads = 256, blocks = 0, smem = 0, sort_smem = 0, slots = 0;
+  long launch_key[2][4] = {{-1, -1, -1, -1}, {-1, -1, -1, -1}};
+  int lthreads[2] = {0, 0}, lsmem[2] = {0, 0}, lblocks[2] = {0, 0};
+  long long npart = 0;
+  long nvis = 0;
+  // work buffers
+  Scratch scr{};
+  CullScratch cs{};
+  size_t capX = 0, capE = 0, capG = 0, capY = 0, capR = 0, capC = 0, capXs = 0, capO = 0,
+         capEp = 0, capGp = 0, capA = 0, capV = 0;
+};
+
+namespace {
+
+void sys_free(SysBatch* b) {
+  if (!b) return;
+  cudaFree(b->d_static);
+  cudaFree(b->d_plan);
+  cudaFree(b->scr.X);
+  cudaFree(b->scr.Epart);
+  cudaFree(b->scr.Gpart);
+  cudaFree(b->scr.Y);
+  cudaFree(b->scr.rec);
+  cudaFree(b->scr.cen);
+  cudaFree(b->cs.Xs);
+  cudaFree(b->cs.order);
+  cudaFree(b->cs.Ep);
+  cudaFree(b->cs.Gp);
+  cudaFree(b->cs.arrive);
+  cudaFree(b->cs.vis);
+  delete b;
+}
+
+// static layout: ligand blobs, packed proteins in row-index order, virtual
+// systems and the rebuild / finishing block tables
+int sys_build_static(mmo_ctx* ctx, SysBatch* S) {
+  const long key[2] = {ctx->ph.mixing, (long)std::llround((ctx->cull_h > 0 ? ctx->cull_h : 3.0) * 1e3)};
+  if (S->built_key[0] == key[0] && S->built_key[1] == key[1] && S->d_static) return MMO_OK;
+  const int ns = (int)S->in.size();
+  std::vector<LigBlob> blobs(ns);
+  std::vector<RowIndex> ri(ns);
+  S->rows.assign(ns, {});
+  S->atom0.assign(ns + 1, 0);
+  S->row0.assign(ns + 1, 0);
+  S->segcount.assign(ns, {});
+  S->segtype.assign(ns, {});
+  S->Ls.assign(ns, 0);
+  S->nrbs.assign(ns, 0);
+  S->Lmax = 1;
+  S->nrbmax = 0;
+  const double h = ctx->cull_h > 0 ? ctx->cull_h : 3.0;
+  for (int u = 0; u < ns; ++u) {
+    const SysBatch::Sys& sy = S->in[u];
+    make_ligand_blob(ctx->ph.mixing, sy.lig, &blobs[u]);
+    const int np = (int)sy.px.size();
+    if (np > 0) {
+      build_rows(np, sy.px.data(), sy.py.data(), sy.pz.data(), sy.pkq.data(), sy.ptype.data(), h,
+                 &ri[u]);
+    } else {
+      ri[u].rs = {0};
+      for (int d = 0; d < 3; ++d) ri[u].lo[d] = ri[u].hi[d] = 0.f;
+    }
+    S->rows[u] = ri[u].rs;
+    S->atom0[u + 1] = S->atom0[u] + np;
+    S->row0[u + 1] = S->row0[u] + (int)ri[u].rbox.size();
+    S->segcount[u] = blobs[u].seg_count;
+    S->segtype[u] = blobs[u].seg_type;
+    S->Ls[u] = blobs[u].n;
+    S->nrbs[u] = blobs[u].nrb;
+    S->Lmax = std::max(S->Lmax, blobs[u].n);
+    S->nrbmax = std::max(S->nrbmax, blobs[u].nrb);
+  }
+  // virtual systems: pose ranges of at most kSysSortMax entries
+  S->info.clear();
+  S->vuser.clear();
+  int pose = 0, ent = 0, rec = 0, dof = 0;
+  for (int u = 0; u < ns; ++u) {
+    const int L = S->Ls[u], nrb = S->nrbs[u];
+    const int chunk = std::max(1, kSysSortMax / L);
+    const RowIndex& R = ri[u];
+    float side = 0.f;
+    for (int d = 0; d < 3; ++d) side = std::max(side, R.hi[d] - R.lo[d]);
+    side += 4.0f;
+    for (int p0 = 0; p0 < S->in[u].poses; p0 += chunk) {
+      SysInfo v{};
+      v.poses = std::min(chunk, S->in[u].poses - p0);
+      v.pose0 = pose;
+      v.ent0 = ent;
+      v.rec0 = rec;
+      v.dof0 = dof;
+      v.L = L;
+      v.nrb = nrb;
+      v.nseg = (int)S->segtype[u].size();
+      v.ox = S->in[u].origin[0];
+      v.oy = S->in[u].origin[1];
+      v.oz = S->in[u].origin[2];
+      for (int d = 0; d < 3; ++d) v.glo[d] = 0.5f * (R.lo[d] + R.hi[d]) - 0.5f * side;
+      v.ginv = (float)kSysGrid / side;
+      pose += v.poses;
+      ent += v.poses * L;
+      rec += v.poses * nrb;
+      dof += v.poses * (6 + nrb);
+      S->info.push_back(v);
+      S->vuser.push_back(u);
+    }
+  }
+  S->E = ent;
+  S->R = rec;
+  const int nv = (int)S->info.size();
+  // threads per pose of the rebuild, as launch_rebuild chooses them
+  int tpp = 32;
+  while (tpp > 1 && (long)S->B * (tpp / 2) >= 20000) tpp /= 2;
+  while (tpp < 32 && sizeof(double) * (3.0 * S->Lmax + 2.0 * (3 + kMaxTors)) * (128 / tpp) >
+                         200.0 * 1024)
+    tpp *= 2;
+  S->tpp = tpp;
+  const int ppb = 128 / tpp;
+  std::vector<SysBlk> rblk, fblk;
+  for (int v = 0; v < nv; ++v) {
+    for (int p0 = 0; p0 < S->info[v].poses; p0 += ppb)
+      rblk.push_back({v, p0, std::min(ppb, S->info[v].poses - p0), 0});
+    for (int p0 = 0; p0 < S->info[v].poses; p0 += 4)
+      fblk.push_back({v, p0, std::min(4, S->info[v].poses - p0), 0});
+  }
+  S->nrblk = (int)rblk.size();
+  S->nfblk = (int)fblk.size();
+  // one device blob: ligands (256-aligned each), atoms, rows, boxes, flush ends, tables
+  std::vector<size_t> lig_off(ns);
+  size_t off = 0;
+  for (int u = 0; u < ns; ++u) {
+    off = (off + 255) & ~size_t(255);
+    lig_off[u] = off;
+    off += blobs[u].host.size();
+  }
+  const int P = S->atom0[ns], nrows = S->row0[ns];
+  const size_t o_atoms = take(off, sizeof(float4) * 2 * (size_t)std::max(P, 1));
+  const size_t o_rs = take(off, sizeof(int) * (nrows + 1));
+  const size_t o_box = take(off, sizeof(float4) * std::max(nrows, 1));
+  const size_t o_fe = take(off, sizeof(int) * std::max(nrows, 1));
+  const size_t o_info = take(off, sizeof(SysInfo) * std::max(nv, 1));
+  const size_t o_lig = take(off, sizeof(DevLigand) * std::max(nv, 1));
+  const size_t o_rb = take(off, sizeof(SysBlk) * std::max(S->nrblk, 1));
+  const size_t o_fb = take(off, sizeof(SysBlk) * std::max(S->nfblk, 1));
+  std::vector<char> host(off, 0);
+  for (int u = 0; u < ns; ++u)
+    memcpy(host.data() + lig_off[u], blobs[u].host.data(), blobs[u].host.size());
+  float4* atoms = reinterpret_cast<float4*>(host.data() + o_atoms);
+  int* rs = reinterpret_cast<int*>(host.data() + o_rs);
+  float4* box = reinterpret_cast<float4*>(host.data() + o_box);
+  int* fe = reinterpret_cast<int*>(host.data() + o_fe);
+  for (int u = 0; u < ns; ++u) {
+    const RowIndex& R = ri[u];
+    if (!R.atoms.empty())
+      memcpy(atoms + 2 * (size_t)S->atom0[u], R.atoms.data(), sizeof(float4) * R.atoms.size());
+    const int nr = (int)R.rbox.size();
+    for (int r = 0; r < nr; ++r) {
+      rs[S->row0[u] + r] = S->atom0[u] + R.rs[r];
+      box[S->row0[u] + r] = R.rbox[r];
+      fe[S->row0[u] + r] = S->row0[u] + R.flush_end[r];
+    }
+  }
+  rs[nrows] = P;
+  memcpy(host.data() + o_info, S->info.data(), sizeof(SysInfo) * nv);
+  memcpy(host.data() + o_rb, rblk.data(), sizeof(SysBlk) * rblk.size());
+  memcpy(host.data() + o_fb, fblk.data(), sizeof(SysBlk) * fblk.size());
+  int r;
+  if ((r = grow(ctx, &S->d_static, &S->cap_static, off, "system batch"))) return r;
+  char* d = static_cast<char*>(S->d_static);
+  DevLigand* ligs = reinterpret_cast<DevLigand*>(host.data() + o_lig);
+  for (int v = 0; v < nv; ++v) {
+    const int u = S->vuser[v];
+    ligs[v] = ligand_at(blobs[u], d + lig_off[u], nullptr);
+  }
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before system batch upload");
+  MMO_CK(cudaMemcpy(d, host.data(), off, cudaMemcpyHostToDevice), "system batch upload");
+  DevSystems& D = S->dev;
+  D = DevSystems{};
+  D.info = reinterpret_cast<const SysInfo*>(d + o_info);
+  D.lig = reinterpret_cast<const DevLigand*>(d + o_lig);
+  D.rblk = reinterpret_cast<const SysBlk*>(d + o_rb);
+  D.fblk = reinterpret_cast<const SysBlk*>(d + o_fb);
+  D.atoms = reinterpret_cast<const float4*>(d + o_atoms);
+  D.row_start = reinterpret_cast<const int*>(d + o_rs);
+  D.row_box = reinterpret_cast<const float4*>(d + o_box);
+  D.flush_end = reinterpret_cast<const int*>(d + o_fe);
+  D.nsys = nv;
+  D.B = S->B;
+  D.Lmax = S->Lmax;
+  D.nrbmax = S->nrbmax;
+  S->built_key[0] = key[0];
+  S->built_key[1] = key[1];
+  S->plan_key[0] = -1;  // the plan's tables refer to this layout
+  ++ctx->epoch;
+  return MMO_OK;
+}
+
+// plan: protein pieces, entry groups, segment slots, work items
+int sys_build_plan(mmo_ctx* ctx, SysBatch* S, bool grad) {
+  const int kp = ctx->cull_kp ? ctx->cull_kp : 2;
+  const int piece_atoms = ctx->cull_piece ? ctx->cull_piece : 256;
+  const long key[3] = {kp, piece_atoms, S->built_key[1]};
+  const int G = 32 * kp;
+  if (!(S->plan_key[0] == key[0] && S->plan_key[1] == key[1] && S->plan_key[2] == key[2])) {
+    const int ns = (int)S->in.size(), nv = (int)S->info.size();
+    std::vector<int4> pieces;
+    std::vector<int> piece0(ns), npieces(ns);
+    int amax = 1, rmax = 1;
+    for (int u = 0; u < ns; ++u) {
+      piece0[u] = (int)pieces.size();
+      const std::vector<int>& rs = S->rows[u];
+      const int nr = (int)rs.size() - 1;
+      if (nr <= 0) {  // no protein: one empty piece, so that the groups still close
+        pieces.push_back(make_int4(S->atom0[u], S->atom0[u], S->row0[u], S->row0[u]));
+      } else {
+        const std::vector<int> pr = row_pieces(rs, piece_atoms);
+        for (size_t k = 0; k + 1 < pr.size(); ++k) {
+          const int a0 = S->atom0[u] + rs[pr[k]], a1 = S->atom0[u] + rs[pr[k + 1]];
+          pieces.push_back(make_int4(a0, a1, S->row0[u] + pr[k], S->row0[u] + pr[k + 1]));
+          amax = std::max(amax, a1 - a0);
+          rmax = std::max(rmax, pr[k + 1] - pr[k]);
+        }
+      }
+      npieces[u] = (int)pieces.size() - piece0[u];
+    }
+    std::vector<SysGroup> groups;
+    std::vector<int> seg_slot;
+    std::vector<int2> items;
+    int slot = 0;
+    long long part = 0;
+    long vis = 0;
+    for (int v = 0; v < nv; ++v) {
+      SysInfo& inf = S->info[v];
+      const int u = S->vuser[v];
+      inf.piece0 = piece0[u];
+      inf.npieces = npieces[u];
+      inf.seg0 = (int)seg_slot.size();
+      inf.group0 = (int)groups.size();
+      for (int t = 0; t < inf.nseg; ++t) {
+        const int n = inf.poses * S->segcount[u][t];
+        seg_slot.push_back(slot);
+        for (int g0 = 0; g0 < n; g0 += G)
+          groups.push_back({slot + g0, slot + n, S->segtype[u][t], v});
+        slot += (n + G - 1) / G * G;
+      }
+      inf.ngroups = (int)groups.size() - inf.group0;
+      inf.vis0 = (int)vis;
+      inf.part0 = part;
+      vis += (long)inf.ngroups * inf.npieces;
+      part += (long long)inf.ngroups * inf.npieces * G;
+      if (inf.ngroups > 0)
+        for (int k = 0; k < inf.npieces; ++k) items.push_back(make_int2(v, inf.piece0 + k));
+    }
+    size_t off = 0;
+    const size_t o_info = take(off, sizeof(SysInfo) * std::max(nv, 1));
+    const size_t o_piece = take(off, sizeof(int4) * std::max<size_t>(pieces.size(), 1));
+    const size_t o_item = take(off, sizeof(int2) * std::max<size_t>(items.size(), 1));
+    const size_t o_group = take(off, sizeof(SysGroup) * std::max<size_t>(groups.size(), 1));
+    const size_t o_seg = take(off, sizeof(int) * std::max<size_t>(seg_slot.size(), 1));
+    std::vector<char> host(off, 0);
+    memcpy(host.data() + o_info, S->info.data(), sizeof(SysInfo) * nv);
+    memcpy(host.data() + o_piece, pieces.data(), sizeof(int4) * pieces.size());
+    memcpy(host.data() + o_item, items.data(), sizeof(int2) * items.size());
+    memcpy(host.data() + o_group, groups.data(), sizeof(SysGroup) * groups.size());
+    memcpy(host.data() + o_seg, seg_slot.data(), sizeof(int) * seg_slot.size());
+    int r;
+    if ((r = grow(ctx, &S->d_plan, &S->cap_plan, off, "system batch plan"))) return r;
+    char* d = static_cast<char*>(S->d_plan);
+    MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before plan upload");
+    MMO_CK(cudaMemcpy(d, host.data(), off, cudaMemcpyHostToDevice), "plan upload");
+    DevSystems& D = S->dev;
+    D.info = reinterpret_cast<const SysInfo*>(d + o_info);  // the plan's copy holds the piece fields
+    D.piece = reinterpret_cast<const int4*>(d + o_piece);
+    D.item = reinterpret_cast<const int2*>(d + o_item);
+    D.group = reinterpret_cast<const SysGroup*>(d + o_group);
+    D.seg_slot = reinterpret_cast<const int*>(d + o_seg);
+    D.nitems = (int)items.size();
+    D.ngroups = (int)groups.size();
+    D.G = G;
+    D.piece_atoms_max = amax;
+    D.piece_rows_max = rmax;
+    S->kp = kp;
+    S->slots = slot;
+    S->npart = part;
+    S->nvis = vis;
+    int sort_smem = 0;
+    for (const SysInfo& v : S->info)
+      sort_smem = std::max(sort_smem, (int)sizeof(unsigned) * (v.nseg * kSysCells + v.poses * v.L));
+    S->sort_smem = std::max(sort_smem, 16);
+    std::copy(key, key + 3, S->plan_key);
+    ++ctx->epoch;
+  }
+  // launch shape, per gradient flag (occupancy queried once per shape)
+  const int g = grad ? 1 : 0;
+  const int maxt = cull_max_threads(S->kp);
+  const int threads = std::min(ctx->tile_threads ? ctx->tile_threads : 256, maxt);
+  const long lkey[4] = {S->plan_key[0], S->plan_key[1], threads,
+                        ctx->ph.dielectric * 2 + ctx->ph.inter_form};
+  if (!std::equal(lkey, lkey + 4, S->launch_key[g])) {
+    const int smem = sys_pairs_smem(S->dev.piece_atoms_max, S->dev.piece_rows_max, threads);
+    const int bps = std::max(1, sys_pairs_max_blocks(S->kp, threads, grad, ctx->ph, smem));
+    S->lthreads[g] = threads;
+    S->lsmem[g] = smem;
+    S->lblocks[g] = ctx->sms * bps;
+    std::copy(lkey, lkey + 4, S->launch_key[g]);
+  }
+  S->threads = S->lthreads[g];
+  S->smem = S->lsmem[g];
+  S->blocks = S->lblocks[g];
+  return MMO_OK;
+}
+
+int sys_scratch(mmo_ctx* ctx, SysBatch* S, bool grad, bool inter) {
+  int r;
+  const size_t E = std::max(S->E, 1), B = std::max(S->B, 1), R = std::max(S->R, 1);
+  if ((r = grow(ctx, (void**)&S->scr.X, &S->capX, sizeof(float4) * 2 * E, "X"))) return r;
+  if ((r = grow(ctx, (void**)&S->scr.Epart, &S->capE, sizeof(double) * E, "Epart"))) return r;
+  if (grad) {
+    if ((r = grow(ctx, (void**)&S->scr.Gpart, &S->capG, sizeof(float4) * E, "Gpart"))) return r;
+    if ((r = grow(ctx, (void**)&S->scr.Y, &S->capY, sizeof(float4) * E, "Y"))) return r;
+    if ((r = grow(ctx, (void**)&S->scr.rec, &S->capR, sizeof(float4) * 3 * R, "records"))) return r;
+    if ((r = grow(ctx, (void**)&S->scr.cen, &S->capC, sizeof(float4) * B, "centroids"))) return r;
+  }
+  S->scr.C = 1;
+  if (inter) {
+    CullScratch& c = S->cs;
+    const size_t slots = std::max(S->slots, 1);
+    if ((r = grow(ctx, (void**)&c.Xs, &S->capXs, sizeof(float4) * 2 * slots, "sorted entries")))
+      return r;
+    if ((r = grow(ctx, (void**)&c.order, &S->capO, sizeof(int) * slots, "slot order"))) return r;
+    const size_t np = (size_t)std::max<long long>(S->npart, 1);
+    if ((r = grow(ctx, (void**)&c.Ep, &S->capEp, sizeof(double) * np, "piece energies"))) return r;
+    if (grad && (r = grow(ctx, (void**)&c.Gp, &S->capGp, sizeof(float4) * np, "piece gradients")))
+      return r;
+    if ((r = grow(ctx, (void**)&c.arrive, &S->capA, sizeof(int) * std::max(S->dev.ngroups, 1),
+                  "group arrivals")))
+      return r;
+    if ((r = grow(ctx, (void**)&c.vis, &S->capV, (size_t)std::max(S->nvis, 1L), "piece flags")))
+      return r;
+    c.queue = ctx->d_queue;
+    c.pairs = reinterpret_cast<unsigned long long*>(ctx->d_queue + 2);
+    c.Eout = S->scr.Epart;
+    c.Gout = S->scr.Gpart;
+  }
+  return MMO_OK;
+}
+
+int score_systems(mmo_ctx* ctx, const float* d_dofs, int flags, double* d_E, float* d_grad,
+                  int* d_status, int* d_err, cudaStream_t st) {
+  SysBatch* S = ctx->sys;
+  if (!S) return fail(ctx, MMO_ESTATE, "no systems: call mmo_set_systems first");
+  if (S->B > 0 && (!d_dofs || !d_E || !d_status))
+    return fail(ctx, MMO_EINVAL, "mmo_score_systems: bad arguments");
+  if ((flags & MMO_F_GRAD) && S->B > 0 && !d_grad)
+    return fail(ctx, MMO_EINVAL, "MMO_F_GRAD needs grad_out");
+  if (S->B == 0) return MMO_OK;
+  const bool grad = flags & MMO_F_GRAD;
+  const bool inter = flags & MMO_F_INTER;
+  int r;
+  if ((r = sys_build_static(ctx, S))) return r;
+  if (inter && (r = sys_build_plan(ctx, S, grad))) return r;
+  if ((r = sys_scratch(ctx, S, grad, inter))) return r;
+  PoseIO io{};
+  io.dofs = d_dofs;
+  io.E = d_E;
+  io.grad = grad ? d_grad : nullptr;
+  io.status = d_status;
+  io.err = d_err;
+  io.B = S->B;
+  const int fl = flags & (kFlagInter | kFlagIntra | kFlagGrad | kFlagRecenter);
+  ctx->last_cull = false;
+  ctx->last_pairs = 0;
+  ctx->last_launches = 2 + (inter ? 2 : 0);
+  MMO_CK(launch_sys_rebuild(S->dev, S->nrblk, S->tpp, io, S->scr, fl, st), "system rebuild kernel");
+  if (inter) {
+    MMO_CK(cudaMemsetAsync(ctx->d_queue, 0, 16, st), "work counter reset");
+    MMO_CK(launch_sys_sort(S->dev, S->scr, S->cs, S->sort_smem, st), "system sort kernel");
+    MMO_CK(launch_sys_pairs(S->dev, ctx->d_tab4, S->cs, S->kp, S->threads, S->blocks, S->smem,
+                            fl, ctx->ph, d_err, st),
+           "system pair kernel");
+  }
+  MMO_CK(launch_sys_finish(S->dev, S->nfblk, io, S->scr, fl, ctx->ph, st), "system finish kernel");
+  return MMO_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* mmo_last_error(const mmo_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_err; }
@@ -831,6 +1318,7 @@ int mmo_ctx_destroy(mmo_ctx* ctx) {
   cudaFree(ctx->cs.arrive);
   cudaFree(ctx->cs.vis);
   cudaFree(ctx->d_mc);
+  sys_free(ctx->sys);
   if (ctx->mc_exec) cudaGraphExecDestroy(ctx->mc_exec);
   for (auto& e : ctx->mc_ev)
     if (e) cudaEventDestroy(e);
@@ -982,17 +1470,19 @@ int mmo_set_protein(mmo_ctx* ctx, int n, const double* xs, const double* ys, con
   return build_cull(ctx);
 }
 
-int mmo_set_ligand(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
-                   const double* q, const int* anum, const uint8_t* interacting, int nrb,
-                   const int* bond_lr, const int* group_offsets, const int* group_atoms) {
-  if (!ctx) return MMO_EINVAL;
-  if (n < 1 || n > kMaxLig)
-    return fail(ctx, MMO_EINVAL, "mmo_set_ligand: n = %d outside 1..%d", n, kMaxLig);
+namespace {
+
+// the checks of mmo_set_ligand, into a LigIn
+int parse_ligand(mmo_ctx* ctx, const char* who, int n, const double* xs, const double* ys,
+                 const double* zs, const double* q, const int* anum, const uint8_t* interacting,
+                 int nrb, const int* bond_lr, const int* group_offsets, const int* group_atoms,
+                 LigIn* out) {
+  if (n < 1 || n > kMaxLig) return fail(ctx, MMO_EINVAL, "%s: n = %d outside 1..%d", who, n, kMaxLig);
   if (nrb < 0 || nrb > kMaxTors)
-    return fail(ctx, MMO_EINVAL, "mmo_set_ligand: nrb = %d outside 0..%d", nrb, kMaxTors);
+    return fail(ctx, MMO_EINVAL, "%s: nrb = %d outside 0..%d", who, nrb, kMaxTors);
   if (!xs || !ys || !zs || !q || !anum || !interacting ||
       (nrb > 0 && (!bond_lr || !group_offsets || !group_atoms)))
-    return fail(ctx, MMO_EINVAL, "mmo_set_ligand: null array");
+    return fail(ctx, MMO_EINVAL, "%s: null array", who);
   std::vector<int> type(n);
   for (int i = 0; i < n; ++i) {
     type[i] = type_of(anum[i]);
@@ -1021,15 +1511,61 @@ int mmo_set_ligand(mmo_ctx* ctx, int n, const double* xs, const double* ys, cons
     }
     gat.assign(group_atoms, group_atoms + goff[nrb]);
   }
-  ctx->lx.assign(xs, xs + n);
-  ctx->ly.assign(ys, ys + n);
-  ctx->lz.assign(zs, zs + n);
-  ctx->lq.assign(q, q + n);
-  ctx->ltype = type;
-  ctx->lbonds = bonds;
-  ctx->lgoff = nrb > 0 ? goff : std::vector<int>{0};
-  ctx->lgatoms = gat;
-  ctx->linter.assign(interacting, interacting + (size_t)n * n);
+  out->x.assign(xs, xs + n);
+  out->y.assign(ys, ys + n);
+  out->z.assign(zs, zs + n);
+  out->q.assign(q, q + n);
+  out->type = type;
+  out->bonds = bonds;
+  out->goff = nrb > 0 ? goff : std::vector<int>{0};
+  out->gat = gat;
+  out->inter.assign(interacting, interacting + (size_t)n * n);
+  return MMO_OK;
+}
+
+// the checks of mmo_set_protein; the device frame origin is the centroid
+int parse_protein(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
+                  const double* q, const int* anum, std::vector<int>* type, float of[3]) {
+  if (n < 0 || (n > 0 && (!xs || !ys || !zs || !q || !anum)))
+    return fail(ctx, MMO_EINVAL, "protein: bad arguments");
+  type->resize(n);
+  double o[3] = {0, 0, 0};
+  for (int i = 0; i < n; ++i) {
+    (*type)[i] = type_of(anum[i]);
+    if ((*type)[i] < 0)
+      return fail(ctx, MMO_EELEMENT, "protein atom %d: element %d not in the UFF table", i, anum[i]);
+    if (!std::isfinite(xs[i]) || !std::isfinite(ys[i]) || !std::isfinite(zs[i]) ||
+        !std::isfinite(q[i]))
+      return fail(ctx, MMO_EINVAL, "protein atom %d: non-finite coordinate or charge", i);
+    o[0] += xs[i];
+    o[1] += ys[i];
+    o[2] += zs[i];
+  }
+  if (n > 0)
+    for (int d = 0; d < 3; ++d) o[d] /= n;
+  for (int d = 0; d < 3; ++d) of[d] = (float)o[d];
+  return MMO_OK;
+}
+
+}  // namespace
+
+int mmo_set_ligand(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
+                   const double* q, const int* anum, const uint8_t* interacting, int nrb,
+                   const int* bond_lr, const int* group_offsets, const int* group_atoms) {
+  if (!ctx) return MMO_EINVAL;
+  LigIn in;
+  int r = parse_ligand(ctx, "mmo_set_ligand", n, xs, ys, zs, q, anum, interacting, nrb, bond_lr,
+                       group_offsets, group_atoms, &in);
+  if (r) return r;
+  ctx->lx = in.x;
+  ctx->ly = in.y;
+  ctx->lz = in.z;
+  ctx->lq = in.q;
+  ctx->ltype = in.type;
+  ctx->lbonds = in.bonds;
+  ctx->lgoff = in.goff;
+  ctx->lgatoms = in.gat;
+  ctx->linter = in.inter;
   MMO_CK(cudaSetDevice(ctx->device), "set device");
   return upload_ligand(ctx);
 }
@@ -1585,6 +2121,111 @@ int mmo_fp32_fma_peak(mmo_ctx* ctx, double* tflops, double* ms_out) {
   *tflops = best * 1e-12;
   if (ms_out) *ms_out = best_ms;
   return MMO_OK;
+}
+
+
+int mmo_set_systems(mmo_ctx* ctx, int nsys, const mmo_system* systems) {
+  if (!ctx) return MMO_EINVAL;
+  if (nsys < 0 || (nsys > 0 && !systems)) return fail(ctx, MMO_EINVAL, "mmo_set_systems: bad arguments");
+  SysBatch* S = new (std::nothrow) SysBatch();
+  if (!S) return MMO_ENOMEM;
+  S->in.resize(nsys);
+  S->pose_off.assign(nsys + 1, 0);
+  S->dof_off.assign(nsys + 1, 0);
+  for (int u = 0; u < nsys; ++u) {
+    const mmo_system& y = systems[u];
+    SysBatch::Sys& sy = S->in[u];
+    int r = parse_ligand(ctx, "mmo_set_systems", y.n_lig, y.lig_x, y.lig_y, y.lig_z, y.lig_q,
+                         y.lig_anum, y.interacting, y.nrb, y.bond_lr, y.group_offsets,
+                         y.group_atoms, &sy.lig);
+    if (!r) r = parse_protein(ctx, y.n_prot, y.prot_x, y.prot_y, y.prot_z, y.prot_q, y.prot_anum,
+                              &sy.ptype, sy.origin);
+    if (!r && y.poses < 0) r = fail(ctx, MMO_EINVAL, "mmo_set_systems: system %d: poses < 0", u);
+    if (r) {
+      delete S;
+      return r;
+    }
+    const int n = y.n_prot;
+    sy.px.resize(n);
+    sy.py.resize(n);
+    sy.pz.resize(n);
+    sy.pkq.resize(n);
+    for (int i = 0; i < n; ++i) {
+      sy.px[i] = y.prot_x[i] - (double)sy.origin[0];
+      sy.py[i] = y.prot_y[i] - (double)sy.origin[1];
+      sy.pz[i] = y.prot_z[i] - (double)sy.origin[2];
+      sy.pkq[i] = (float)(kElec * y.prot_q[i]);
+    }
+    sy.poses = y.poses;
+    S->pose_off[u + 1] = S->pose_off[u] + y.poses;
+    S->dof_off[u + 1] = S->dof_off[u] + y.poses * (6 + y.nrb);
+  }
+  S->B = S->pose_off[nsys];
+  S->D = S->dof_off[nsys];
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before replacing the systems");
+  sys_free(ctx->sys);
+  ctx->sys = S;
+  ++ctx->epoch;
+  return sys_build_static(ctx, S);
+}
+
+int mmo_systems_layout(const mmo_ctx* ctx, int* total_poses, int* total_dofs, int* pose_off,
+                       int* dof_off) {
+  if (!ctx || !total_poses || !total_dofs) return MMO_EINVAL;
+  const SysBatch* S = ctx->sys;
+  *total_poses = S ? S->B : 0;
+  *total_dofs = S ? S->D : 0;
+  if (S && pose_off) std::copy(S->pose_off.begin(), S->pose_off.end(), pose_off);
+  if (S && dof_off) std::copy(S->dof_off.begin(), S->dof_off.end(), dof_off);
+  return MMO_OK;
+}
+
+int mmo_score_systems_device(mmo_ctx* ctx, const float* d_dofs, int flags, double* d_E,
+                             float* d_grad, int* d_status, void* stream) {
+  if (!ctx) return MMO_EINVAL;
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  return score_systems(ctx, d_dofs, flags, d_E, d_grad, d_status, ctx->d_err,
+                       reinterpret_cast<cudaStream_t>(stream));
+}
+
+int mmo_score_systems(mmo_ctx* ctx, const float* dofs, int flags, double* E, float* grad,
+                      int* status) {
+  if (!ctx) return MMO_EINVAL;
+  SysBatch* S = ctx->sys;
+  if (!S) return fail(ctx, MMO_ESTATE, "no systems: call mmo_set_systems first");
+  const int B = S->B, D = S->D;
+  const bool g = flags & MMO_F_GRAD;
+  if (B > 0 && (!dofs || !E || (g && !grad))) return fail(ctx, MMO_EINVAL, "mmo_score_systems: bad arguments");
+  if (B == 0) return MMO_OK;
+  size_t off = 0;
+  take(off, sizeof(double) * B);
+  const size_t o_grad = take(off, g ? sizeof(float) * (size_t)D : 0);
+  const size_t o_st = take(off, sizeof(int) * B);
+  const size_t o_err = take(off, sizeof(int));
+  const size_t out_bytes = off, in_bytes = sizeof(float) * (size_t)D;
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  int r = grow_host(ctx, &ctx->h_in, &ctx->d_in, &ctx->cap_in, in_bytes);
+  if (r) return r;
+  r = grow_host(ctx, &ctx->h_out, &ctx->d_out, &ctx->cap_out, out_bytes);
+  if (r) return r;
+  memcpy(ctx->h_in, dofs, in_bytes);
+  MMO_CK(cudaMemcpyAsync(ctx->d_in, ctx->h_in, in_bytes, cudaMemcpyHostToDevice, ctx->stream),
+         "H2D");
+  MMO_CK(cudaMemsetAsync(ctx->d_out + o_err, 0, sizeof(int), ctx->stream), "error flag");
+  r = score_systems(ctx, reinterpret_cast<const float*>(ctx->d_in), flags,
+                    reinterpret_cast<double*>(ctx->d_out),
+                    g ? reinterpret_cast<float*>(ctx->d_out + o_grad) : nullptr,
+                    reinterpret_cast<int*>(ctx->d_out + o_st),
+                    reinterpret_cast<int*>(ctx->d_out + o_err), ctx->stream);
+  if (r) return r;
+  MMO_CK(cudaMemcpyAsync(ctx->h_out, ctx->d_out, out_bytes, cudaMemcpyDeviceToHost, ctx->stream),
+         "D2H");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync");
+  memcpy(E, ctx->h_out, sizeof(double) * B);
+  if (g) memcpy(grad, ctx->h_out + o_grad, sizeof(float) * (size_t)D);
+  if (status) memcpy(status, ctx->h_out + o_st, sizeof(int) * B);
+  return check_dev_err(ctx, *reinterpret_cast<int*>(ctx->h_out + o_err));
 }
 
 }  // extern "C"

@@ -31,8 +31,8 @@ constexpr int kListCap = 64;  // a warp's list: under 32 left over plus one wind
 // axes to transposed index, then the bits interleaved).  Consecutive slots in
 // Hilbert order stay closer together than in Morton order, so the groups'
 // boxes are smaller.
+template <int kBits = 5>
 __device__ __forceinline__ uint32_t hilbert_cell(uint32_t x, uint32_t y, uint32_t z) {
-  constexpr int kBits = 5;
   uint32_t X[3] = {x, y, z};
   for (uint32_t Q = 1u << (kBits - 1); Q > 1; Q >>= 1) {
     const uint32_t P = Q - 1;
@@ -158,7 +158,7 @@ __global__ void k_cull_scatter(const float4* __restrict__ X, int n, int L,
 // dE/dX of one entry over the protein atoms [a0, a1) with the per-pair test
 // of the 0.01 A clamp; the same arithmetic in the same order as the sweep, so
 // entries without a clamped pair get the sweep's value bit for bit.
-template <int DIEL>
+template <int DIEL, int FORM>
 __device__ __noinline__ float3 cull_exact_grad(const float4* sp, const float4* trow, int a0, int a1,
                                                float q, float xh, float yh, float zh, float xl,
                                                float yl, float zl) {
@@ -168,7 +168,7 @@ __device__ __noinline__ float3 cull_exact_grad(const float4* sp, const float4* t
     const float4 p = sp[2 * i], pl = sp[2 * i + 1];
     const float4 pv = *reinterpret_cast<const float4*>(reinterpret_cast<const char*>(trow) +
                                                        __float_as_int(pl.w));
-    pair_step<true, DIEL, 0, true>(xh, yh, zh, xl, yl, zl, p, pl, p.w * q, pv.x, pv.y, pv.z, c0,
+    pair_step<true, DIEL, FORM, true>(xh, yh, zh, xl, yl, zl, p, pl, p.w * q, pv.x, pv.y, pv.z, c0,
                                    acc, gx, gy, gz, mn);
   }
   return make_float3(gx, gy, gz);
@@ -183,6 +183,175 @@ __device__ __forceinline__ float warp_maxf(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(kFull, v, o));
   return v;
+}
+
+// One warp's work for one (group, protein piece) item: the group's entries
+// [slot0, s_end) (32 * KP slots, padding repeats the last entry) against the
+// piece's rows [r0, r1) resident in shared memory (sp, s_rbox, s_rs, s_flush),
+// then the piece's partials at P0 + kpc * PS (+ slot - slot0) and its flag at
+// V0 + kpc; the last of the group's npieces items to arrive sums them.  CULL
+// false visits every atom (the global form).
+template <int KP, bool GRAD, int DIEL, int FORM, bool CULL>
+__device__ __forceinline__ void sweep_item(const float4* sp, const float4* s_rbox, const int* s_rs,
+                                           const int* s_flush, int r0, int r1,
+                                           const float4* trow, int slot0, int s_end, int* wl,
+                                           const CullScratch& cs, long long P0, long long PS,
+                                           int kpc, long long V0, int npieces, int* arrive) {
+  constexpr float c0v = DIEL == 0 ? -10.0f : -4.0f;
+  constexpr int G = 32 * KP;
+  const int lane = threadIdx.x & 31;
+  float xh[KP], yh[KP], zh[KP], xl[KP], yl[KP], zl[KP], q[KP];
+  float acc[KP], gx[KP], gy[KP], gz[KP];
+  double ad[KP];
+  float blx = 1e30f, bly = 1e30f, blz = 1e30f, bhx = -1e30f, bhy = -1e30f, bhz = -1e30f;
+#pragma unroll
+  for (int k = 0; k < KP; ++k) {
+    const int s = min(slot0 + k * 32 + lane, s_end - 1);
+    const float4 h = cs.Xs[2 * (size_t)s], l = cs.Xs[2 * (size_t)s + 1];
+    xh[k] = h.x;
+    yh[k] = h.y;
+    zh[k] = h.z;
+    q[k] = h.w;
+    xl[k] = l.x;
+    yl[k] = l.y;
+    zl[k] = l.z;
+    acc[k] = gx[k] = gy[k] = gz[k] = 0.f;
+    ad[k] = 0.0;
+    blx = fminf(blx, h.x);
+    bly = fminf(bly, h.y);
+    blz = fminf(blz, h.z);
+    bhx = fmaxf(bhx, h.x);
+    bhy = fmaxf(bhy, h.y);
+    bhz = fmaxf(bhz, h.z);
+  }
+  blx = warp_min(blx);
+  bly = warp_min(bly);
+  blz = warp_min(blz);
+  bhx = warp_maxf(bhx);
+  bhy = warp_maxf(bhy);
+  bhz = warp_maxf(bhz);
+
+  float mn = 1e30f;
+  int visited = 0;
+  // the atoms of the warp's candidate rows within 12 A of the box, compacted
+  // in ascending order into the warp's list wl and swept 32 or more at a time
+  int cnt = 0;
+  auto sweep = [&](int n) {
+    __syncwarp();
+#pragma unroll 2
+    for (int v = 0; v < n; ++v) {
+      const float4* pp = sp + 2 * wl[v];
+      const float4 p = pp[0], pl = pp[1];
+      const float4 pv = *reinterpret_cast<const float4*>(reinterpret_cast<const char*>(trow) +
+                                                         __float_as_int(pl.w));
+#pragma unroll
+      for (int k = 0; k < KP; ++k)
+        pair_step<GRAD, DIEL, FORM>(xh[k], yh[k], zh[k], xl[k], yl[k], zl[k], p, pl, p.w * q[k],
+                                 pv.x, pv.y, pv.z, c0v, acc[k], gx[k], gy[k], gz[k], mn);
+    }
+    __syncwarp();
+  };
+  // rows in flush blocks: the FP32 partials go into the FP64 sums once per
+  // block (fixed rows of the protein) and at the end of the piece
+  for (int r = r0; r < r1;) {
+    const int rend = min(r1, s_flush[r]);
+    for (; r < rend; ++r) {
+      const float4 rb = s_rbox[r];
+      const float dy = fmaxf(fmaxf(rb.x - bhy, bly - rb.y), 0.f);
+      const float dz = fmaxf(fmaxf(rb.z - bhz, blz - rb.w), 0.f);
+      if (fmaf(dy, dy, dz * dz) >= kCullR2) continue;
+      const int a = s_rs[r], b = s_rs[r + 1];
+      for (int i0 = a; i0 < b; i0 += 32) {
+        const int i = i0 + lane;
+        bool in = false;
+        if (i < b) {
+          const float4 ph = sp[2 * i];
+          const float ex = fmaxf(fmaxf(blx - ph.x, ph.x - bhx), 0.f);
+          const float ey = fmaxf(fmaxf(bly - ph.y, ph.y - bhy), 0.f);
+          const float ez = fmaxf(fmaxf(blz - ph.z, ph.z - bhz), 0.f);
+          in = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < kCullR2;
+        }
+        const unsigned m = __ballot_sync(kFull, in);
+        if (in) wl[cnt + __popc(m & ((1u << lane) - 1u))] = i;
+        cnt += __popc(m);
+        if (cnt >= 32) {
+          sweep(cnt);
+          visited += cnt;
+          cnt = 0;
+        }
+      }
+    }
+    sweep(cnt);
+    visited += cnt;
+    cnt = 0;
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
+      ad[k] += (double)acc[k];
+      acc[k] = 0.f;
+    }
+  }
+  if (GRAD && __any_sync(kFull, mn < kMinR2)) {
+    // a pair closer than 0.01 A, where the clamped distance makes the
+    // derivative 0: redo the gradient over the piece with the per-pair test
+    const int a0 = s_rs[r0], a1 = s_rs[r1];
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
+      const float3 gg = cull_exact_grad<DIEL, FORM>(sp, trow, a0, a1, q[k], xh[k], yh[k], zh[k], xl[k],
+                                              yl[k], zl[k]);
+      gx[k] = gg.x;
+      gy[k] = gg.y;
+      gz[k] = gg.z;
+    }
+  }
+  if (lane == 0 && visited) atomicAdd(cs.pairs, (unsigned long long)visited * G);
+  constexpr float gs = DIEL == 0 ? -1.0f : -2.0f;
+  if (visited) {  // a piece out of range of the group adds nothing
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
+      const int s = slot0 + k * 32 + lane;
+      if (s < s_end) {
+        const size_t o = (size_t)(P0 + (long long)kpc * PS) + (size_t)(s - slot0);
+        cs.Ep[o] = ad[k];
+        if (GRAD) cs.Gp[o] = make_float4(gs * gx[k], gs * gy[k], gs * gz[k], 0.f);
+      }
+    }
+  }
+  // the last piece of the group to finish sums the group's pieces in piece
+  // order (the arrival order does not matter)
+  if (lane == 0) cs.vis[(size_t)V0 + kpc] = visited ? 1 : 0;
+  __threadfence();  // every lane's partials before the arrival
+  __syncwarp();
+  int last = 0;
+  if (lane == 0) last = atomicAdd(arrive, 1) == npieces - 1;
+  last = __shfl_sync(kFull, last, 0);
+  if (last) {
+    __threadfence();
+    const uint8_t* vg = cs.vis + (size_t)V0;
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
+      const int s = slot0 + k * 32 + lane;
+      if (s >= s_end) continue;
+      double E = 0.0;
+      float sx = 0.f, sy = 0.f, sz = 0.f;
+      for (int q2 = 0; q2 < npieces; ++q2) {
+        if (!__ldcg(vg + q2)) continue;
+        const size_t o = (size_t)(P0 + (long long)q2 * PS) + (size_t)(s - slot0);
+        E += __ldcg(cs.Ep + o);
+        if (GRAD) {
+          const float4 g4 = __ldcg(cs.Gp + o);
+          sx += g4.x;
+          sy += g4.y;
+          sz += g4.z;
+        }
+      }
+      // an entry at a non-finite position can fall in a group far from the protein
+      if (!isfinite(xh[k]) || !isfinite(yh[k]) || !isfinite(zh[k]))
+        E = __longlong_as_double(0x7ff8000000000000ll);
+      const int e = cs.order[s];
+      cs.Eout[e] = E;
+      if (GRAD) cs.Gout[e] = make_float4(sx, sy, sz, 0.f);
+    }
+  }
 }
 
 template <int KP, bool GRAD, int DIEL>
@@ -226,7 +395,6 @@ __global__ void __launch_bounds__(cull_max_threads(KP))
     return;
   }
 
-  constexpr float c0v = DIEL == 0 ? -10.0f : -4.0f;
   constexpr int G = 32 * KP;
   const int lane = threadIdx.x & 31;
   const int nitems = seg.off[seg.nseg] / G * npieces;
@@ -243,160 +411,169 @@ __global__ void __launch_bounds__(cull_max_threads(KP))
     const int s_end = seg.off[t] + seg.n[t];
     const float4* trow = s_tab + seg.type[t];  // + the byte offset of the protein type's row
 
-    float xh[KP], yh[KP], zh[KP], xl[KP], yl[KP], zl[KP], q[KP];
-    float acc[KP], gx[KP], gy[KP], gz[KP];
-    double ad[KP];
-    float blx = 1e30f, bly = 1e30f, blz = 1e30f, bhx = -1e30f, bhy = -1e30f, bhz = -1e30f;
-#pragma unroll
-    for (int k = 0; k < KP; ++k) {
-      const int s = min(slot0 + k * 32 + lane, s_end - 1);
-      const float4 h = cs.Xs[2 * (size_t)s], l = cs.Xs[2 * (size_t)s + 1];
-      xh[k] = h.x;
-      yh[k] = h.y;
-      zh[k] = h.z;
-      q[k] = h.w;
-      xl[k] = l.x;
-      yl[k] = l.y;
-      zl[k] = l.z;
-      acc[k] = gx[k] = gy[k] = gz[k] = 0.f;
-      ad[k] = 0.0;
-      blx = fminf(blx, h.x);
-      bly = fminf(bly, h.y);
-      blz = fminf(blz, h.z);
-      bhx = fmaxf(bhx, h.x);
-      bhy = fmaxf(bhy, h.y);
-      bhz = fmaxf(bhz, h.z);
-    }
-    blx = warp_min(blx);
-    bly = warp_min(bly);
-    blz = warp_min(blz);
-    bhx = warp_maxf(bhx);
-    bhy = warp_maxf(bhy);
-    bhz = warp_maxf(bhz);
+    sweep_item<KP, GRAD, DIEL, 0, true>(sp, s_rbox, s_rs, s_flush, s_piece[pc], s_piece[pc + 1],
+                                        trow, slot0, s_end, s_list + (threadIdx.x >> 5) * kListCap,
+                                        cs, slot0, cs.slots, pc, (long long)g * npieces, npieces,
+                                        &cs.arrive[g]);
+  }
+}
 
-    float mn = 1e30f;
-    int visited = 0;
-    // the atoms of the warp's candidate rows within 12 A of the box, compacted
-    // in ascending order into the warp's list and swept 32 or more at a time
-    int* wl = s_list + (threadIdx.x >> 5) * kListCap;
-    int cnt = 0;
-    auto sweep = [&](int n) {
-      __syncwarp();
-#pragma unroll 2
-      for (int v = 0; v < n; ++v) {
-        const float4* pp = sp + 2 * wl[v];
-        const float4 p = pp[0], pl = pp[1];
-        const float4 pv = *reinterpret_cast<const float4*>(reinterpret_cast<const char*>(trow) +
-                                                           __float_as_int(pl.w));
+// ---------------------------------------------------------------------------
+// ragged batch of systems
+// ---------------------------------------------------------------------------
+constexpr int kSysSortThreads = 512;
+
+// One CTA per system: its entries into slot order by (ligand type segment,
+// Hilbert cell of an 8^3 grid over the system's protein), counted in shared
+// memory; also clears the arrival counters of the system's groups.
+__global__ void __launch_bounds__(kSysSortThreads)
+    k_sys_sort(DevSystems S, const float4* __restrict__ X, CullScratch cs) {
+  extern __shared__ unsigned ssm[];  // [nseg * kSysCells] counts, then [n] bin | rank << 16
+  const int sys = blockIdx.x;
+  const SysInfo inf = S.info[sys];
+  const DevLigand& lig = S.lig[sys];
+  const int L = inf.L, n = inf.poses * L, nb = inf.nseg * kSysCells;
+  unsigned* hist = ssm;
+  unsigned* br = ssm + nb;
+  const int* seg_of_atom = lig.seg_of_atom;
+  for (int k = threadIdx.x; k < nb; k += blockDim.x) hist[k] = 0u;
+  for (int k = threadIdx.x; k < inf.ngroups; k += blockDim.x) cs.arrive[inf.group0 + k] = 0;
+  __syncthreads();
+  for (int e = threadIdx.x; e < n; e += blockDim.x) {
+    const float4 h = X[2 * ((size_t)inf.ent0 + e)];
+    const uint32_t cx = min(max(__float2int_rd((h.x - inf.glo[0]) * inf.ginv), 0), kSysGrid - 1);
+    const uint32_t cy = min(max(__float2int_rd((h.y - inf.glo[1]) * inf.ginv), 0), kSysGrid - 1);
+    const uint32_t cz = min(max(__float2int_rd((h.z - inf.glo[2]) * inf.ginv), 0), kSysGrid - 1);
+    const unsigned bin = (unsigned)seg_of_atom[e % L] * kSysCells + hilbert_cell<3>(cx, cy, cz);
+    const unsigned rank = atomicAdd(&hist[bin], 1u);
+    br[e] = bin | (rank << 16);
+  }
+  __syncthreads();
+  // per segment: exclusive scan of its cells into slots (a warp per segment)
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int t = w; t < inf.nseg; t += blockDim.x >> 5) {
+    unsigned* hs = hist + t * kSysCells;
+    constexpr int per = kSysCells / 32;
+    unsigned loc[per], sum = 0;
 #pragma unroll
-        for (int k = 0; k < KP; ++k)
-          pair_step<GRAD, DIEL, 0>(xh[k], yh[k], zh[k], xl[k], yl[k], zl[k], p, pl, p.w * q[k],
-                                   pv.x, pv.y, pv.z, c0v, acc[k], gx[k], gy[k], gz[k], mn);
-      }
-      __syncwarp();
-    };
-    const int r0 = s_piece[pc], r1 = s_piece[pc + 1];
-    // rows in flush blocks: the FP32 partials go into the FP64 sums once per
-    // block (fixed rows of the protein) and at the end of the piece
-    for (int r = r0; r < r1;) {
-      const int rend = min(r1, s_flush[r]);
-      for (; r < rend; ++r) {
-        const float4 rb = s_rbox[r];
-        const float dy = fmaxf(fmaxf(rb.x - bhy, bly - rb.y), 0.f);
-        const float dz = fmaxf(fmaxf(rb.z - bhz, blz - rb.w), 0.f);
-        if (fmaf(dy, dy, dz * dz) >= kCullR2) continue;
-        const int a = s_rs[r], b = s_rs[r + 1];
-        for (int i0 = a; i0 < b; i0 += 32) {
-          const int i = i0 + lane;
-          bool in = false;
-          if (i < b) {
-            const float4 ph = sp[2 * i];
-            const float ex = fmaxf(fmaxf(blx - ph.x, ph.x - bhx), 0.f);
-            const float ey = fmaxf(fmaxf(bly - ph.y, ph.y - bhy), 0.f);
-            const float ez = fmaxf(fmaxf(blz - ph.z, ph.z - bhz), 0.f);
-            in = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < kCullR2;
-          }
-          const unsigned m = __ballot_sync(kFull, in);
-          if (in) wl[cnt + __popc(m & ((1u << lane) - 1u))] = i;
-          cnt += __popc(m);
-          if (cnt >= 32) {
-            sweep(cnt);
-            visited += cnt;
-            cnt = 0;
-          }
-        }
-      }
-      sweep(cnt);
-      visited += cnt;
-      cnt = 0;
+    for (int k = 0; k < per; ++k) {
+      loc[k] = hs[lane * per + k];
+      sum += loc[k];
+    }
+    unsigned inc = sum;
 #pragma unroll
-      for (int k = 0; k < KP; ++k) {
-        ad[k] += (double)acc[k];
-        acc[k] = 0.f;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned v = __shfl_up_sync(kFull, inc, o);
+      if (lane >= o) inc += v;
+    }
+    unsigned run = (unsigned)S.seg_slot[inf.seg0 + t] + inc - sum;
+#pragma unroll
+    for (int k = 0; k < per; ++k) {
+      hs[lane * per + k] = run;
+      run += loc[k];
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < n; e += blockDim.x) {
+    const unsigned v = br[e];
+    const int slot = (int)(hist[v & 0xffffu] + (v >> 16));
+    const size_t ge = (size_t)inf.ent0 + e;
+    const float4 h = X[2 * ge], l = X[2 * ge + 1];
+    cs.Xs[2 * (size_t)slot] = make_float4(h.x, h.y, h.z, lig.q[e % L]);
+    cs.Xs[2 * (size_t)slot + 1] = make_float4(l.x, l.y, l.z, 0.f);
+    cs.order[slot] = (int)ge;
+  }
+}
+
+// Persistent CTAs over (system, protein piece) items: the piece's atoms are
+// staged into shared memory by the TMA bulk engine, then the CTA's warps sweep
+// every entry group of the system against it.
+template <int KP, bool GRAD, int DIEL, int FORM>
+__global__ void __launch_bounds__(cull_max_threads(KP), 1)
+    k_sys_pairs(DevSystems S, const float4* __restrict__ tabv, CullScratch cs, int* err) {
+  extern __shared__ __align__(16) float4 sp[];  // [piece atoms][2], then the row tables
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int s_item, s_fail;
+  const int amax = S.piece_atoms_max, rmax = S.piece_rows_max;
+  float4* s_rbox = sp + 2 * amax;
+  float4* s_tab = s_rbox + rmax;
+  int* s_rs = reinterpret_cast<int*>(s_tab + kNTypes * kNTypes);
+  int* s_flush = s_rs + rmax + 1;
+  int* s_list = s_flush + rmax;
+  for (int k = threadIdx.x; k < kNTypes * kNTypes; k += blockDim.x) {
+    const float4 v = tabv[k];
+    s_tab[k] = make_float4(v.x, v.y, (DIEL == 0 ? 11.0f : 5.0f) * v.y, 0.f);
+  }
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    s_fail = 0;
+  }
+  __syncthreads();
+  constexpr int G = 32 * KP;
+  const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (uint32_t phase = 0;; phase ^= 1u) {
+    if (threadIdx.x == 0) s_item = (int)atomicAdd(cs.queue, 1u);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= S.nitems) break;
+    const int2 ip = S.item[item];
+    const SysInfo& inf = S.info[ip.x];
+    const int4 pc = S.piece[ip.y];  // atom0, atom1, row0, row1
+    const int na = pc.y - pc.x, nr = pc.w - pc.z;
+    if (threadIdx.x == 0) {
+      const uint32_t bytes = (uint32_t)na * 32u;
+      mbar_expect_tx(&bar, bytes);
+      constexpr uint32_t kPiece = 32768u;
+      for (uint32_t off = 0; off < bytes; off += kPiece) {
+        const uint32_t m = bytes - off < kPiece ? bytes - off : kPiece;
+        bulk_g2s(reinterpret_cast<char*>(sp) + off,
+                 reinterpret_cast<const char*>(S.atoms + 2 * (size_t)pc.x) + off, m, &bar);
       }
     }
-    if (GRAD && __any_sync(kFull, mn < kMinR2)) {
-      // a pair closer than 0.01 A, where the clamped distance makes the
-      // derivative 0: redo the gradient over the piece with the per-pair test
-      const int a0 = s_rs[r0], a1 = s_rs[r1];
-#pragma unroll
-      for (int k = 0; k < KP; ++k) {
-        const float3 gg = cull_exact_grad<DIEL>(sp, trow, a0, a1, q[k], xh[k], yh[k], zh[k], xl[k],
-                                                yl[k], zl[k]);
-        gx[k] = gg.x;
-        gy[k] = gg.y;
-        gz[k] = gg.z;
-      }
+    for (int k = threadIdx.x; k < nr; k += blockDim.x) {
+      s_rbox[k] = S.row_box[pc.z + k];
+      s_rs[k] = S.row_start[pc.z + k] - pc.x;
+      s_flush[k] = S.flush_end[pc.z + k] - pc.z;
     }
-    if (lane == 0 && visited) atomicAdd(cs.pairs, (unsigned long long)visited * G);
-    constexpr float gs = DIEL == 0 ? -1.0f : -2.0f;
-    if (visited) {  // a piece out of range of the group adds nothing
-#pragma unroll
-      for (int k = 0; k < KP; ++k) {
-        const int s = slot0 + k * 32 + lane;
-        if (s < s_end) {
-          const size_t o = (size_t)pc * cs.slots + s;
-          cs.Ep[o] = ad[k];
-          if (GRAD) cs.Gp[o] = make_float4(gs * gx[k], gs * gy[k], gs * gz[k], 0.f);
-        }
-      }
+    if (threadIdx.x == 0) s_rs[nr] = na;
+    if (threadIdx.x == 0 && !mbar_wait(&bar, phase, kWaitPolls)) {
+      atomicOr(err, kErrTimeout);
+      mbar_wait(&bar, phase, kWaitPolls);
+      s_fail = 1;
     }
-    // the last piece of the group to finish sums the group's pieces in piece
-    // order (the arrival order does not matter)
-    if (lane == 0) cs.vis[(size_t)g * npieces + pc] = visited ? 1 : 0;
-    __threadfence();  // every lane's partials before the arrival
-    __syncwarp();
-    int last = 0;
-    if (lane == 0) last = atomicAdd(&cs.arrive[g], 1) == npieces - 1;
-    last = __shfl_sync(kFull, last, 0);
-    if (last) {
-      __threadfence();
-      const uint8_t* vg = cs.vis + (size_t)g * npieces;
-#pragma unroll
-      for (int k = 0; k < KP; ++k) {
-        const int s = slot0 + k * 32 + lane;
-        if (s >= s_end) continue;
-        double E = 0.0;
-        float sx = 0.f, sy = 0.f, sz = 0.f;
-        for (int q2 = 0; q2 < npieces; ++q2) {
-          if (!__ldcg(vg + q2)) continue;
-          const size_t o = (size_t)q2 * cs.slots + s;
-          E += __ldcg(cs.Ep + o);
-          if (GRAD) {
-            const float4 g4 = __ldcg(cs.Gp + o);
-            sx += g4.x;
-            sy += g4.y;
-            sz += g4.z;
-          }
-        }
-        // an entry at a non-finite position can fall in a group far from the protein
-        if (!isfinite(xh[k]) || !isfinite(yh[k]) || !isfinite(zh[k]))
-          E = __longlong_as_double(0x7ff8000000000000ll);
-        const int e = cs.order[s];
-        cs.Eout[e] = E;
-        if (GRAD) cs.Gout[e] = make_float4(sx, sy, sz, 0.f);
-      }
+    __syncthreads();
+    if (s_fail) return;
+    const int kpc = ip.y - inf.piece0;
+    for (int g = inf.group0 + warp; g < inf.group0 + inf.ngroups; g += nwarps) {
+      const SysGroup gr = S.group[g];
+      const long long gl = g - inf.group0;
+      sweep_item<KP, GRAD, DIEL, FORM, FORM == 0>(
+          sp, s_rbox, s_rs, s_flush, 0, nr, s_tab + gr.ltype, gr.slot0, gr.s_end,
+          s_list + warp * kListCap, cs, inf.part0 + gl * inf.npieces * G, G, kpc,
+          inf.vis0 + gl * inf.npieces, inf.npieces, &cs.arrive[g]);
     }
+    __syncthreads();  // the piece stays until every warp is done with it
+  }
+}
+
+using SysFn = void (*)(DevSystems, const float4*, CullScratch, int*);
+
+template <int KP>
+SysFn pick_sys_kp(bool grad, int diel, int form) {
+  if (grad) {
+    if (diel) return form ? k_sys_pairs<KP, true, 1, 1> : k_sys_pairs<KP, true, 1, 0>;
+    return form ? k_sys_pairs<KP, true, 0, 1> : k_sys_pairs<KP, true, 0, 0>;
+  }
+  if (diel) return form ? k_sys_pairs<KP, false, 1, 1> : k_sys_pairs<KP, false, 1, 0>;
+  return form ? k_sys_pairs<KP, false, 0, 1> : k_sys_pairs<KP, false, 0, 0>;
+}
+
+SysFn pick_sys(int kp, bool grad, const Physics& ph) {
+  const int d = ph.dielectric ? 1 : 0, f = ph.inter_form ? 1 : 0;
+  switch (kp) {
+    case 1: return pick_sys_kp<1>(grad, d, f);
+    case 2: return pick_sys_kp<2>(grad, d, f);
+    default: return pick_sys_kp<4>(grad, d, f);
   }
 }
 
@@ -458,6 +635,42 @@ cudaError_t launch_pairs_cull(const DevCull& cull, const float4* tab, const Cull
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, plan.smem);
   if (e != cudaSuccess) return e;
   fn<<<plan.blocks, plan.threads, plan.smem, st>>>(cull, tab, seg, cs, d_err);
+  return cudaGetLastError();
+}
+
+
+int sys_pairs_smem(int piece_atoms_max, int piece_rows_max, int threads) {
+  const long b = 32L * piece_atoms_max + 16L * piece_rows_max + 16L * kNTypes * kNTypes +
+                 4L * (piece_rows_max + 1) + 4L * piece_rows_max + 4L * kListCap * (threads / 32);
+  return (int)((b + 15) / 16 * 16);
+}
+
+int sys_pairs_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem) {
+  SysFn fn = pick_sys(kp, grad != 0, ph);
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, smem) != cudaSuccess) return 0;
+  return nb;
+}
+
+cudaError_t launch_sys_sort(const DevSystems& S, const Scratch& s, const CullScratch& cs,
+                            int smem, cudaStream_t st) {
+  if (S.nsys <= 0) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(k_sys_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  k_sys_sort<<<S.nsys, kSysSortThreads, smem, st>>>(S, s.X, cs);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sys_pairs(const DevSystems& S, const float4* tab, const CullScratch& cs,
+                             int kp, int threads, int blocks, int smem, int flags,
+                             const Physics& ph, int* d_err, cudaStream_t st) {
+  if (S.nitems <= 0) return cudaSuccess;
+  SysFn fn = pick_sys(kp, (flags & kFlagGrad) != 0, ph);
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  fn<<<blocks, threads, smem, st>>>(S, tab, cs, d_err);
   return cudaGetLastError();
 }
 

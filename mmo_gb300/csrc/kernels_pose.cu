@@ -37,21 +37,26 @@ __device__ __forceinline__ void store_split(float4* X, double x, double y, doubl
 // cosines of the pose's angles are computed once, split over the TPP threads.
 // Small batches use many threads per pose (the one-pose path uses a whole
 // warp), large batches one thread per pose.
+//
+// rebuild_pose: one pose of the block's ligand; dof, Xo, Yo, reco, ceno and
+// statuso point at the pose's own slots (dof readable even when !live).
+// (not inlined: the one-system and the system-batch kernels share this code,
+// so both round every operation the same way)
 template <bool RECENTER, bool RECORD, int TPP>
-__global__ void __launch_bounds__(kRebuildThreads) k_rebuild(DevLigand lig, PoseIO io, Scratch scr) {
+__device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof, bool live,
+                                             float orx, float ory, float orz, float4* Xo,
+                                             float4* Yo, float4* reco, float4* ceno,
+                                             int* statuso) {
   constexpr int PPB = kRebuildThreads / TPP;  // poses per block
   constexpr int NANG = 3 + kMaxTors;
   extern __shared__ double sz[];  // [3][L][PPB] coordinates, then [PPB][NANG][2] sin, cos
   const int tid = threadIdx.x, p = tid / TPP, sub = tid % TPP;
-  const int b = blockIdx.x * PPB + p;
-  const int L = lig.L, nrb = lig.nrb, nd = 6 + nrb;
+  const int L = lig.L, nrb = lig.nrb;
   double* X = sz;
   double* Yc = sz + L * PPB;
   double* Zc = sz + 2 * L * PPB;
   double* SC = sz + 3 * L * PPB + p * NANG * 2;
 #define AT(arr, a) arr[(a) * PPB + p]
-  const bool live = b < io.B;
-  const float* dof = io.dofs + (size_t)(live ? b : 0) * nd;
   for (int a = sub; a < L; a += TPP) {
     AT(X, a) = lig.ref64[3 * a];
     AT(Yc, a) = lig.ref64[3 * a + 1];
@@ -80,7 +85,7 @@ __global__ void __launch_bounds__(kRebuildThreads) k_rebuild(DevLigand lig, Pose
       AT(Zc, i) = fma(R6, vx, fma(R7, vy, fma(R8, vz, cz)));
     }
     if (RECORD && live && sub == 0) {
-      float4* r = scr.rec + ((size_t)b * nrb + t) * 3;
+      float4* r = reco + (size_t)t * 3;
       r[0] = make_float4((float)cx, (float)cy, (float)cz, (float)cs);
       r[1] = make_float4((float)ux, (float)uy, (float)uz, (float)sn);
       r[2] = make_float4((float)inv, 0.f, 0.f, 0.f);
@@ -116,26 +121,38 @@ __global__ void __launch_bounds__(kRebuildThreads) k_rebuild(DevLigand lig, Pose
   const double R0 = cb * cg, R1 = cg * sa * sb - ca * sg, R2 = sa * sg + ca * cg * sb;
   const double R3 = cb * sg, R4 = ca * cg + sa * sb * sg, R5 = ca * sb * sg - cg * sa;
   const double R6 = -sb, R7 = cb * sa, R8 = ca * cb;
-  const double tx = (double)dof[0] - (double)io.ox, ty = (double)dof[1] - (double)io.oy,
-               tz = (double)dof[2] - (double)io.oz;
+  const double tx = (double)dof[0] - (double)orx, ty = (double)dof[1] - (double)ory,
+               tz = (double)dof[2] - (double)orz;
   const double ox = RECENTER ? mx : 0.0, oy = RECENTER ? my : 0.0, oz = RECENTER ? mz : 0.0;
   if (live) {
     for (int a = sub; a < L; a += TPP) {
       const double vx = AT(X, a) - ox, vy = AT(Yc, a) - oy, vz = AT(Zc, a) - oz;
-      store_split(scr.X + ((size_t)b * L + a) * 2, fma(R0, vx, fma(R1, vy, fma(R2, vz, tx))),
+      store_split(Xo + (size_t)a * 2, fma(R0, vx, fma(R1, vy, fma(R2, vz, tx))),
                   fma(R3, vx, fma(R4, vy, fma(R5, vz, ty))),
                   fma(R6, vx, fma(R7, vy, fma(R8, vz, tz))));
       if (RECORD)
-        scr.Y[(size_t)b * L + a] = make_float4((float)AT(X, a), (float)AT(Yc, a),
-                                                (float)AT(Zc, a), 0.f);
+        Yo[a] = make_float4((float)AT(X, a), (float)AT(Yc, a), (float)AT(Zc, a), 0.f);
     }
     if (sub == 0) {
-      if (RECORD) scr.cen[b] = make_float4((float)mx, (float)my, (float)mz, 0.f);
-      io.status[b] = status;
-      if (b == 0 && io.zero_err) *io.err = 0;
+      if (RECORD) *ceno = make_float4((float)mx, (float)my, (float)mz, 0.f);
+      *statuso = status;
     }
   }
 #undef AT
+}
+
+template <bool RECENTER, bool RECORD, int TPP>
+__global__ void __launch_bounds__(kRebuildThreads) k_rebuild(DevLigand lig, PoseIO io, Scratch scr) {
+  constexpr int PPB = kRebuildThreads / TPP;
+  const int b = blockIdx.x * PPB + (int)threadIdx.x / TPP;
+  const bool live = b < io.B;
+  const size_t bb = live ? b : 0;
+  const int L = lig.L, nrb = lig.nrb, nd = 6 + nrb;
+  rebuild_pose<RECENTER, RECORD, TPP>(
+      lig, io.dofs + bb * nd, live, io.ox, io.oy, io.oz, scr.X + bb * L * 2,
+      RECORD ? scr.Y + bb * L : nullptr, RECORD ? scr.rec + bb * nrb * 3 : nullptr,
+      RECORD ? scr.cen + bb : nullptr, io.status + bb);
+  if (live && b == 0 && threadIdx.x % TPP == 0 && io.zero_err) *io.err = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -176,33 +193,33 @@ __host__ __device__ constexpr int finish_warp_f4(int L, int nrb) {
   return 2 * L + 5 * nrb + (33 * nrb + 3) / 4;
 }
 
+// finish_pose: one warp, one pose.  ep / gp: the pose's inter partials
+// [C][L]; Xb, Yb, recb, cenp, dof, grad, Eo, sto: the pose's own slots;
+// wsm: the warp's shared memory (finish_warp_f4 float4).
+// (not inlined, as rebuild_pose)
 template <bool GRAD, bool RECENTER, int DIEL, int IFORM>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, kFinishBlocksPerSM)
-    k_finish(DevLigand lig, PoseIO io, Scratch scr, int flags) {
-  extern __shared__ __align__(16) float4 fsm[];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int b = blockIdx.x * kWarpsPerBlock + wib;
-  if (b >= io.B) return;
-  const int L = lig.L, C = scr.C, nrb = lig.nrb, nd = 6 + nrb;
-  float4* sxh = fsm + wib * finish_warp_f4(L, nrb);
+__device__ __noinline__ void finish_pose(const DevLigand& lig, int C, const double* ep,
+                                            const float4* gp, const float4* Xb, const float4* Yb,
+                                            const float4* recb, const float4* cenp,
+                                            const float* dof, float* grad, double* Eo, int* sto,
+                                            int flags, float4* wsm) {
+  const int lane = threadIdx.x & 31;
+  const int L = lig.L, nrb = lig.nrb;
+  float4* sxh = wsm;
   float4* sxl = sxh + L;
   float4* saxis = sxl + L;        // [nrb] final axes, then [nrb] centres
   float4* srec = saxis + 2 * nrb;  // [nrb][3] torsion records
   float* sdti = reinterpret_cast<float*>(srec + 3 * nrb);  // [nrb][33]
-  if (GRAD) {  // the reverse pass reads them last: start the loads now
-    const float4* recb = scr.rec + (size_t)b * nrb * 3;
+  if (GRAD)  // the reverse pass reads them last: start the loads now
     for (int k = lane; k < 3 * nrb; k += 32) srec[k] = recb[k];
-  }
   const bool intra = flags & kFlagIntra, inter = flags & kFlagInter;
   double e = 0.0;
-  if (inter) {
-    const double* ep = scr.Epart + (size_t)b * C * L;
+  if (inter)
     for (int k = lane; k < C * L; k += 32) e += ep[k];
-  }
   if (intra) {
     for (int a = lane; a < L; a += 32) {
-      sxh[a] = scr.X[((size_t)b * L + a) * 2];
-      sxl[a] = scr.X[((size_t)b * L + a) * 2 + 1];
+      sxh[a] = Xb[(size_t)a * 2];
+      sxl[a] = Xb[(size_t)a * 2 + 1];
     }
     __syncwarp();
   }
@@ -253,8 +270,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kFinishBlocksPerSM)
   }
   e = warp_sum(e);
   if (lane == 0) {
-    io.E[b] = e;
-    if (!isfinite(e)) io.status[b] |= kStatusNonFinite;
+    *Eo = e;
+    if (!isfinite(e)) *sto |= kStatusNonFinite;
   }
   if (!GRAD) return;
 
@@ -263,7 +280,6 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kFinishBlocksPerSM)
 #pragma unroll
   for (int s = 0; s < kSlots; ++s) gx[s] = gy[s] = gz[s] = 0.f;
   if (inter) {
-    const float4* gp = scr.Gpart + (size_t)b * C * L;
     for (int c = 0; c < C; ++c) {
 #pragma unroll
       for (int s = 0; s < kSlots; ++s) {
@@ -301,13 +317,12 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kFinishBlocksPerSM)
 #pragma unroll
   for (int s = 0; s < kSlots; ++s) {
     const int a = lane + 32 * s;
-    const float4 y = a < L ? scr.Y[(size_t)b * L + a] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 y = a < L ? Yb[a] : make_float4(0.f, 0.f, 0.f, 0.f);
     zx[s] = y.x;
     zy[s] = y.y;
     zz[s] = y.z;
   }
-  const float4 cen = RECENTER ? scr.cen[b] : make_float4(0.f, 0.f, 0.f, 0.f);
-  const float* dof = io.dofs + (size_t)b * nd;
+  const float4 cen = RECENTER ? *cenp : make_float4(0.f, 0.f, 0.f, 0.f);
   float sa, ca, sb, cb, sg, cg;
   sincosf(dof[3], &sa, &ca);
   sincosf(dof[4], &sb, &cb);
@@ -333,7 +348,6 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kFinishBlocksPerSM)
   }
 #pragma unroll
   for (int k = 0; k < 12; ++k) red[k] = warp_sum(red[k]);
-  float* grad = io.grad + (size_t)b * nd;
   if (lane == 0) {
     const float* M = red + 3;
     // d R / d a, d b, d g of rot.ml:52-66, entry by entry
@@ -477,6 +491,23 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kFinishBlocksPerSM)
   }
 }
 
+template <bool GRAD, bool RECENTER, int DIEL, int IFORM>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, kFinishBlocksPerSM)
+    k_finish(DevLigand lig, PoseIO io, Scratch scr, int flags) {
+  extern __shared__ __align__(16) float4 fsm[];
+  const int wib = threadIdx.x >> 5;
+  const int b = blockIdx.x * kWarpsPerBlock + wib;
+  if (b >= io.B) return;
+  const int L = lig.L, C = scr.C, nrb = lig.nrb, nd = 6 + nrb;
+  const size_t ent = (size_t)b * L;
+  finish_pose<GRAD, RECENTER, DIEL, IFORM>(
+      lig, C, scr.Epart + ent * C, GRAD ? scr.Gpart + ent * C : nullptr, scr.X + ent * 2,
+      GRAD ? scr.Y + ent : nullptr, GRAD ? scr.rec + (size_t)b * nrb * 3 : nullptr,
+      GRAD ? scr.cen + b : nullptr, io.dofs + (size_t)b * nd,
+      GRAD ? io.grad + (size_t)b * nd : nullptr, io.E + b, io.status + b, flags,
+      fsm + wib * finish_warp_f4(L, nrb));
+}
+
 // one warp: sum of n FP64 partials
 __global__ void k_reduce_plain(const double* Epart, int n, double* out) {
   double e = 0.0;
@@ -542,6 +573,84 @@ cudaError_t finish_t(const DevLigand& lig, const PoseIO& io, const Scratch& s, i
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// ragged batch of systems: the same per-pose bodies, one system per block
+// ---------------------------------------------------------------------------
+template <bool RECENTER, bool RECORD, int TPP>
+__global__ void __launch_bounds__(kRebuildThreads)
+    k_sys_rebuild(DevSystems S, PoseIO io, Scratch scr) {
+  __shared__ DevLigand slig;
+  const SysBlk blk = S.rblk[blockIdx.x];
+  if (threadIdx.x == 0) slig = S.lig[blk.sys];
+  __syncthreads();
+  const SysInfo& inf = S.info[blk.sys];
+  const int p = (int)threadIdx.x / TPP;
+  const bool live = p < blk.n;
+  const int lp = blk.p0 + (live ? p : 0);
+  const int L = slig.L, nrb = slig.nrb;
+  const size_t b = (size_t)inf.pose0 + lp, ent = (size_t)inf.ent0 + (size_t)lp * L;
+  const size_t rec = (size_t)inf.rec0 + (size_t)lp * nrb;
+  rebuild_pose<RECENTER, RECORD, TPP>(
+      slig, io.dofs + (size_t)inf.dof0 + (size_t)lp * (6 + nrb), live, inf.ox, inf.oy, inf.oz,
+      scr.X + ent * 2, RECORD ? scr.Y + ent : nullptr, RECORD ? scr.rec + rec * 3 : nullptr,
+      RECORD ? scr.cen + b : nullptr, io.status + b);
+}
+
+template <bool GRAD, bool RECENTER, int DIEL, int IFORM>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, kFinishBlocksPerSM)
+    k_sys_finish(DevSystems S, PoseIO io, Scratch scr, int flags) {
+  extern __shared__ __align__(16) float4 fsm[];
+  __shared__ DevLigand slig;
+  const SysBlk blk = S.fblk[blockIdx.x];
+  if (threadIdx.x == 0) slig = S.lig[blk.sys];
+  __syncthreads();
+  const int wib = threadIdx.x >> 5;
+  if (wib >= blk.n) return;
+  const SysInfo& inf = S.info[blk.sys];
+  const int lp = blk.p0 + wib;
+  const int L = slig.L, nrb = slig.nrb;
+  const size_t b = (size_t)inf.pose0 + lp, ent = (size_t)inf.ent0 + (size_t)lp * L;
+  const size_t rec = (size_t)inf.rec0 + (size_t)lp * nrb, dof = (size_t)inf.dof0 + (size_t)lp * (6 + nrb);
+  finish_pose<GRAD, RECENTER, DIEL, IFORM>(
+      slig, 1, scr.Epart + ent, GRAD ? scr.Gpart + ent : nullptr, scr.X + ent * 2,
+      GRAD ? scr.Y + ent : nullptr, GRAD ? scr.rec + rec * 3 : nullptr,
+      GRAD ? scr.cen + b : nullptr, io.dofs + dof, GRAD ? io.grad + dof : nullptr, io.E + b,
+      io.status + b, flags, fsm + wib * finish_warp_f4(S.Lmax, S.nrbmax));
+}
+
+template <bool RC, bool REC>
+cudaError_t sys_rebuild_tpp(int tpp, const DevSystems& S, int nblk, const PoseIO& io,
+                            const Scratch& s, cudaStream_t st) {
+  const int ppb = kRebuildThreads / tpp;
+  const int smem = (int)(sizeof(double) * (3 * (size_t)S.Lmax * ppb + (size_t)ppb * (3 + kMaxTors) * 2));
+#define MMO_SR(T)                                                                          \
+  case T: {                                                                                \
+    cudaError_t e = cudaFuncSetAttribute(k_sys_rebuild<RC, REC, T>,                        \
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem); \
+    if (e != cudaSuccess) return e;                                                        \
+    k_sys_rebuild<RC, REC, T><<<nblk, kRebuildThreads, smem, st>>>(S, io, s);              \
+    return cudaGetLastError();                                                             \
+  }
+  switch (tpp) {
+    MMO_SR(1) MMO_SR(2) MMO_SR(4) MMO_SR(8) MMO_SR(16) MMO_SR(32)
+  }
+#undef MMO_SR
+  return cudaErrorInvalidValue;
+}
+
+template <bool G, bool RC, int DIEL, int IFORM>
+cudaError_t sys_finish_t(const DevSystems& S, int nblk, const PoseIO& io, const Scratch& s,
+                         int flags, cudaStream_t st) {
+  const int smem = kWarpsPerBlock * finish_warp_f4(S.Lmax, S.nrbmax) * (int)sizeof(float4);
+  if (smem > 48 * 1024) {
+    const cudaError_t e = cudaFuncSetAttribute(k_sys_finish<G, RC, DIEL, IFORM>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+  }
+  k_sys_finish<G, RC, DIEL, IFORM><<<nblk, kWarpsPerBlock * 32, smem, st>>>(S, io, s, flags);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t launch_rebuild(const DevLigand& lig, const PoseIO& io, const Scratch& s, int flags,
@@ -601,6 +710,40 @@ cudaError_t launch_intra_plain(const DevLigand& lig, const float4* X, int form, 
     else k_intra_plain<0, 0><<<1, 32, 0, st>>>(lig, X, out);
   }
   return cudaGetLastError();
+}
+
+
+cudaError_t launch_sys_rebuild(const DevSystems& S, int nblk, int tpp, const PoseIO& io,
+                               const Scratch& s, int flags, cudaStream_t st) {
+  if (nblk <= 0) return cudaSuccess;
+  const bool rc = flags & kFlagRecenter;
+  const bool rec = (flags & kFlagGrad) && io.grad;
+  if (rc) return rec ? sys_rebuild_tpp<true, true>(tpp, S, nblk, io, s, st)
+                     : sys_rebuild_tpp<true, false>(tpp, S, nblk, io, s, st);
+  return rec ? sys_rebuild_tpp<false, true>(tpp, S, nblk, io, s, st)
+             : sys_rebuild_tpp<false, false>(tpp, S, nblk, io, s, st);
+}
+
+cudaError_t launch_sys_finish(const DevSystems& S, int nblk, const PoseIO& io, const Scratch& s,
+                              int flags, const Physics& ph, cudaStream_t st) {
+  if (nblk <= 0) return cudaSuccess;
+  const bool g = (flags & kFlagGrad) && io.grad;
+  const bool rc = flags & kFlagRecenter;
+  const int d = ph.dielectric ? 1 : 0, f = ph.intra_form ? 0 : 1;
+#define MMO_SF(G, RC, D, F) return sys_finish_t<G, RC, D, F>(S, nblk, io, s, flags, st)
+#define MMO_SF_D(G, RC)                                                   \
+  if (d == 0) { if (f) MMO_SF(G, RC, 0, 1); else MMO_SF(G, RC, 0, 0); } \
+  else { if (f) MMO_SF(G, RC, 1, 1); else MMO_SF(G, RC, 1, 0); }
+  if (!g) {
+    MMO_SF_D(false, false)
+  }
+  if (rc) {
+    MMO_SF_D(true, true)
+  } else {
+    MMO_SF_D(true, false)
+  }
+#undef MMO_SF_D
+#undef MMO_SF
 }
 
 }  // namespace mmo

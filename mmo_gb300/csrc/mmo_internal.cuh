@@ -183,6 +183,54 @@ struct CullPlan {
   int smem;              // dynamic shared memory of the sweep
 };
 
+// ---- ragged batch of systems ----------------------------------------------
+// Many (pocket, ligand) systems, each with its own number of poses, scored in
+// one pass.  Per system s the poses are consecutive ([pose0, pose0 + poses)),
+// and so are its entries (pose-major, L_s per pose), torsion records (nrb_s
+// per pose) and DOF rows (6 + nrb_s floats per pose).  Proteins are packed one
+// after the other in row-index order; the cut-off sweep works on pieces of one
+// protein (a few hundred atoms, whole rows) staged per CTA.
+constexpr int kSysGrid = 8;                      // binning cells per axis per system
+constexpr int kSysCells = kSysGrid * kSysGrid * kSysGrid;
+constexpr int kSysSortMax = 16384;               // entries one sort CTA holds
+
+struct SysInfo {
+  int pose0, ent0, rec0, dof0;   // first global pose, entry, torsion record, DOF float
+  int poses, L, nrb, nseg;       // poses, ligand atoms, torsions, ligand type segments
+  int piece0, npieces;           // the system's protein pieces
+  int group0, ngroups;           // the system's entry groups (cut-off sweep)
+  int seg0;                      // first (system, type) segment in the segment table
+  int vis0;                      // first piece flag: group-major [ngroups][npieces]
+  long long part0;               // first piece partial: [ngroups][npieces][G]
+  float ox, oy, oz;              // frame origin (centroid of the protein)
+  float glo[3], ginv;            // binning grid: origin, cells per A
+};
+
+struct SysBlk {                  // a block's system and its system-local poses [p0, p0 + n)
+  int sys, p0, n, pad;
+};
+
+struct SysGroup {                // a group of G slots of one (system, type) segment
+  int slot0, s_end, ltype, sys;
+};
+
+struct DevSystems {
+  const SysInfo* info;           // [nsys]
+  const DevLigand* lig;          // [nsys] descriptors into the packed ligand blob
+  const SysBlk* rblk;            // rebuild blocks (32 / TPP poses each)
+  const SysBlk* fblk;            // finishing blocks (4 poses each)
+  const int4* piece;             // [npieces] (atom0, atom1, row0, row1), packed indices
+  const int2* item;              // [nitems] (system, piece) work items of the sweep
+  const SysGroup* group;         // [ngroups]
+  const int* seg_slot;           // [nsegs] first slot of each (system, type) segment
+  const float4* atoms;           // [Ptot][2] packed proteins, row order, as DevCull::atoms
+  const int* row_start;          // [rows + 1] packed atom index of each row's first atom
+  const float4* row_box;         // [rows]
+  const int* flush_end;          // [rows] packed row index ending the row's flush block
+  int nsys, B, nitems, ngroups, G;
+  int Lmax, nrbmax, piece_atoms_max, piece_rows_max;
+};
+
 // ---- Monte Carlo chains (kernels_mc.cu) ----------------------------------
 enum : int { kMcUniform = 0, kMcGaussian = 1 };
 constexpr int kMcCounts = 4;   // per chain: step, rigid accepted in block, rigid moves, conformer moves
@@ -227,6 +275,18 @@ cudaError_t launch_k_gd_accept(const MCDev& s, const MCParams& p, cudaStream_t s
 cudaError_t launch_k_gd_take(const MCDev& s, const MCParams& p, cudaStream_t st);
 cudaError_t launch_philox(uint32_t k0, uint32_t k1, uint32_t c1, uint32_t c2, int n, uint4* out,
                           cudaStream_t st);
+// ragged batch of systems (kernels_pose.cu, kernels_cull.cu)
+cudaError_t launch_sys_rebuild(const DevSystems& S, int nblk, int tpp, const PoseIO& io,
+                               const Scratch& s, int flags, cudaStream_t st);
+cudaError_t launch_sys_finish(const DevSystems& S, int nblk, const PoseIO& io, const Scratch& s,
+                              int flags, const Physics& ph, cudaStream_t st);
+cudaError_t launch_sys_sort(const DevSystems& S, const Scratch& s, const CullScratch& cs,
+                            int smem, cudaStream_t st);
+cudaError_t launch_sys_pairs(const DevSystems& S, const float4* tab, const CullScratch& cs,
+                             int kp, int threads, int blocks, int smem, int flags,
+                             const Physics& ph, int* d_err, cudaStream_t st);
+int sys_pairs_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem);
+int sys_pairs_smem(int piece_atoms_max, int piece_rows_max, int threads);
 cudaError_t launch_rebuild(const DevLigand& lig, const PoseIO& io, const Scratch& s, int flags,
                            cudaStream_t st);
 cudaError_t launch_pairs_batched(const DevProtein& prot, const float4* tab,

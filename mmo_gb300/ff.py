@@ -66,6 +66,7 @@ class UFFScorer:
         self.physics = physics
         self.protein: Mol | None = None
         self.ligand: Mol | None = None
+        self.systems: list = []
         if physics != Physics():
             self.set_physics(physics)
 
@@ -173,6 +174,61 @@ class UFFScorer:
             inter.ctypes.data_as(C.POINTER(C.c_uint8)), lig.nrb, _ip(bonds), _ip(off),
             _ip(atoms)))
         self.ligand = lig
+
+    # -- ragged batches of systems (include/mmo_systems.h) -----------------
+    def set_systems(self, systems) -> None:
+        """systems: a sequence of (pocket Mol, ligand Mol, poses) triples."""
+        keep, arr = [], (_L.System * max(1, len(systems)))()
+        for k, (prot, lig, poses) in enumerate(systems):
+            px, py, pz, pq = (_f64(v) for v in (prot.x, prot.y, prot.z, prot.q))
+            pa = np.ascontiguousarray(prot.anum, np.int32)
+            lx, ly, lz, lq = (_f64(v) for v in (lig.x, lig.y, lig.z, lig.q))
+            la = np.ascontiguousarray(lig.anum, np.int32)
+            inter = np.ascontiguousarray(lig.interacting, np.uint8)
+            bonds = np.ascontiguousarray(lig.rbonds.reshape(-1), np.int32)
+            off, atoms = lig.group_arrays()
+            off = np.ascontiguousarray(off, np.int32)
+            atoms = np.ascontiguousarray(atoms if atoms.size else np.zeros(1, np.int32), np.int32)
+            if not bonds.size:
+                bonds = np.zeros(2, np.int32)
+            bufs = (px, py, pz, pq, pa, lx, ly, lz, lq, la, inter, bonds, off, atoms)
+            keep.append(bufs)
+            arr[k] = _L.System(prot.n, *(b.ctypes.data for b in bufs[:5]), lig.n,
+                               *(b.ctypes.data for b in bufs[5:11]), lig.nrb,
+                               bonds.ctypes.data, off.ctypes.data, atoms.ctypes.data, int(poses))
+        self._check(self._lib.mmo_set_systems(self._h, len(systems), arr))
+        self.systems = [(p, l, int(n)) for p, l, n in systems]
+
+    def systems_layout(self):
+        """(pose_off [nsys + 1], dof_off [nsys + 1]) of the packed layout."""
+        n = len(self.systems)
+        B, D = C.c_int(), C.c_int()
+        po, do = (C.c_int * (n + 1))(), (C.c_int * (n + 1))()
+        self._check(self._lib.mmo_systems_layout(self._h, C.byref(B), C.byref(D), po, do))
+        return np.array(po[:], np.int64), np.array(do[:], np.int64)
+
+    def score_systems(self, dofs, inter=True, intra=True, grad=False, recenter=False):
+        """Packed float32 DOFs of every system's poses (systems_layout) ->
+        E [B] float64, grad (packed like dofs) or None, status [B]."""
+        po, do = self.systems_layout()
+        dofs = np.ascontiguousarray(dofs, np.float32).reshape(-1)
+        if dofs.size != do[-1]:
+            raise ValueError("dofs must hold %d floats" % do[-1])
+        B = int(po[-1])
+        flags = ((_L.F_INTER if inter else 0) | (_L.F_INTRA if intra else 0) |
+                 (_L.F_GRAD if grad else 0) | (_L.F_RECENTER if recenter else 0))
+        E = np.zeros(B, np.float64)
+        G = np.zeros(dofs.size, np.float32) if grad else None
+        st = np.zeros(B, np.int32)
+        self._check(self._lib.mmo_score_systems(
+            self._h, dofs.ctypes.data_as(C.POINTER(C.c_float)), flags, _dp(E),
+            G.ctypes.data_as(C.POINTER(C.c_float)) if G is not None else None, _ip(st)))
+        return E, G, st
+
+    def score_systems_device(self, d_dofs: int, d_E: int, d_grad: int | None, d_status: int,
+                             flags: int, stream: int | None = None) -> None:
+        self._check(self._lib.mmo_score_systems_device(self._h, d_dofs, flags, d_E,
+                                                       d_grad or None, d_status, stream))
 
     # -- plain drop-ins (one call per Mol.t, like the reference closures) --
     def ene_inter(self, lig: Mol) -> float:

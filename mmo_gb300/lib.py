@@ -36,6 +36,16 @@ class MCState(C.Structure):
                 ("best_E", C.c_void_p), ("accepted", C.c_void_p), ("status", C.c_void_p)]
 
 
+class System(C.Structure):
+    """mmo_system of include/mmo_systems.h."""
+    _fields_ = [("n_prot", C.c_int), ("prot_x", C.c_void_p), ("prot_y", C.c_void_p),
+                ("prot_z", C.c_void_p), ("prot_q", C.c_void_p), ("prot_anum", C.c_void_p),
+                ("n_lig", C.c_int), ("lig_x", C.c_void_p), ("lig_y", C.c_void_p),
+                ("lig_z", C.c_void_p), ("lig_q", C.c_void_p), ("lig_anum", C.c_void_p),
+                ("interacting", C.c_void_p), ("nrb", C.c_int), ("bond_lr", C.c_void_p),
+                ("group_offsets", C.c_void_p), ("group_atoms", C.c_void_p), ("poses", C.c_int)]
+
+
 # every symbol the header declares, with its ctypes signature
 _P = C.POINTER
 _d, _i, _vp, _cp = C.c_double, C.c_int, C.c_void_p, C.c_char_p
@@ -56,6 +66,10 @@ SIGNATURES = {
     "mmo_set_tiles": (_i, [_vp, _i, _i, _i]),
     "mmo_set_cull": (_i, [_vp, _i, C.c_double, _i, _i]),
     "mmo_mc_run": (_i, [_vp, _i, _i, _P(MCParams), _P(MCState), _vp, _i]),
+    "mmo_set_systems": (_i, [_vp, _i, _P(System)]),
+    "mmo_systems_layout": (_i, [_vp, _P(_i), _P(_i), _P(_i), _P(_i)]),
+    "mmo_score_systems_device": (_i, [_vp, _vp, _i, _vp, _vp, _vp, _vp]),
+    "mmo_score_systems": (_i, [_vp, _P(C.c_float), _i, _P(_d), _P(C.c_float), _P(_i)]),
     "mmo_philox4x32": (_i, [_vp, C.c_uint, C.c_uint, C.c_uint, C.c_uint, _i, _vp, _vp]),
     "mmo_tune": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp, _vp, _P(C.c_double)]),
     "mmo_set_tune_cache": (_i, [_vp, C.c_char_p]),
