@@ -57,6 +57,11 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the default launch plan instead of the autotuner's")
+    ap.add_argument("--workload", default="poses", choices=["poses", "ragged", "mc"],
+                    help="poses: the energy+gradient pose batch (default); ragged: 1,024 "
+                         "systems x 64 poses in one pass; mc: 512 Monte Carlo chains")
+    ap.add_argument("--systems", type=int, default=1024, help="ragged: systems in the batch")
+    ap.add_argument("--mc-steps", type=int, default=10000, help="mc: steps per chain")
     return ap.parse_args()
 
 
@@ -189,10 +194,223 @@ def run_reference(args):
     return 0
 
 
+def _timed_region(torch, stream, step, steps, clocks=None):
+    """CUDA-event times (ms) of `steps` calls of step() on `stream`."""
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    torch.cuda.synchronize()
+    if clocks:
+        clocks.start()
+    for a, b in ev:
+        a.record(stream)
+        step()
+        b.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop() if clocks else None
+    return [a.elapsed_time(b) for a, b in ev], clk
+
+
+def run_ragged(args):
+    """1,024 independent ligand/pocket systems (12-80 ligand atoms, 0-15
+    torsions, 2,000-8,000 pocket atoms), 64 poses each, energy and gradient of
+    every pose in one pass of the system-batch kernels."""
+    from mmo_gb300 import synth
+
+    # made before CUDA starts, in spawned processes
+    systems = synth.ragged_systems(args.systems, 64, seed=3, workers=os.cpu_count() or 1)
+    import torch
+
+    from mmo_gb300 import lib as L
+    from mmo_gb300.ff import UFFScorer
+
+    dev = torch.device("cuda", 0)
+    sc = UFFScorer(0)
+    sc.set_systems([(s.pocket, s.ligand, len(s.poses)) for s in systems])
+    po, do = sc.systems_layout()
+    B = int(po[-1])
+    h = np.concatenate([s.poses.reshape(-1) for s in systems]).astype(np.float32)
+    d = torch.from_numpy(h).to(dev)
+    E = torch.empty(B, dtype=torch.float64, device=dev)
+    G = torch.empty_like(d)
+    st = torch.empty(B, dtype=torch.int32, device=dev)
+    flags = L.F_INTER | L.F_INTRA | L.F_GRAD
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    sp = stream.cuda_stream
+    tune_ms = None
+    if not args.no_tune:
+        tune_ms = sc.tune_systems_device(d.data_ptr(), E.data_ptr(), G.data_ptr(), st.data_ptr(),
+                                         flags, sp)
+
+    def step():
+        sc.score_systems_device(d.data_ptr(), E.data_ptr(), G.data_ptr(), st.data_ptr(), flags, sp)
+
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    sc.set_profiling(True)
+    sms = []
+    torch.cuda.synchronize()
+    ev = []
+    clocks = Clocks(0)
+    clocks.start()
+    for _ in range(args.steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step()
+        b.record(stream)
+        ev.append((a, b))
+        sms.append(sc.stage_times())
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    sc.set_profiling(False)
+    ms = [a.elapsed_time(b) for a, b in ev]
+    value = B * len(ms) / (sum(ms) * 1e-3)
+    pairs_ev, pairs_all = sc.pair_count()
+    stages = np.mean(np.array(sms), axis=0)
+    # CUDA graph of the whole step
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        step()
+    for _ in range(3):
+        g.replay()
+    gms, _ = _timed_region(torch, stream, g.replay, args.steps)
+    gval = B * len(gms) / (sum(gms) * 1e-3)
+    # end to end with host buffers
+    e2e = []
+    for k in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        Eh, Gh, sth = sc.score_systems(h, grad=True)
+        if k >= args.warmup:
+            e2e.append(time.perf_counter() - t)
+    e2e_val = B * len(e2e) / sum(e2e)
+    peak = sc.fp32_peak_tflops()
+    achieved = FLOPS_PAIR_GRAD * pairs_ev / (stages[1] * 1e-3) * 1e-12
+    Ls = [s.ligand.n for s in systems]
+    Ps = [s.pocket.n for s in systems]
+    line = {
+        "metric": "poses/s (energy+grad), ragged batch of %d systems x 64 poses, one pass" %
+                  len(systems),
+        "value": value, "unit": "poses/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": float(np.mean(ms)), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "ragged: %d systems, ligands %d-%d atoms (mean %.1f), 0-15 "
+                               "torsions, pockets %d-%d atoms (mean %.0f), 64 poses each" %
+                               (len(systems), min(Ls), max(Ls), np.mean(Ls), min(Ps), max(Ps),
+                                np.mean(Ps)),
+                   "poses": B, "plan": dict(sc.systems_plan(), tuned_ms=tune_ms),
+                   "l2": "flushed before every timed step (256 MiB write), not timed"},
+        "graph": {"value": gval, "unit": "poses/s", "ms_per_step": float(np.mean(gms))},
+        "e2e": {"value": e2e_val, "unit": "poses/s", "h2d_bytes_per_step": int(h.nbytes),
+                "d2h_bytes_per_step": int(Eh.nbytes + Gh.nbytes + sth.nbytes)},
+        "stages_ms": {"rebuild": float(stages[0]), "sort": float(stages[3]),
+                      "sweep": float(stages[1]), "finish": float(stages[2])},
+        "roofline": {"bound": "fp32", "kernel": "k_sys_pairs (sweep of every system)",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "pairs_evaluated": pairs_ev,
+                     "pairs_all": pairs_all, "flops_per_pair": FLOPS_PAIR_GRAD,
+                     "ms_per_launch": float(stages[1])},
+        "gpu_launches": sc.last_launches() * args.steps,
+        "clocks": clk,
+        "status_bits_set": int(np.count_nonzero(st.cpu().numpy())),
+    }
+    print(json.dumps(line), flush=True)
+    sc.close()
+    return 0
+
+
+def run_mc(args):
+    """512 Monte Carlo chains per system of the uneven batch's kind (Gaussian
+    moves 5 deg / 0.3 A / 30 deg, kT 0.593, 20 gradient-descent iterations every
+    50 steps), the block of steps replayed as a CUDA graph."""
+    from mmo_gb300 import synth
+
+    systems = [synth.ragged_system(i, seed=3, poses_per=512) for i in (1, 2, 3, 4)]
+    import torch
+
+    from mmo_gb300 import lib as L
+    from mmo_gb300.ff import UFFScorer
+
+    dev = torch.device("cuda", 0)
+    prm = dict(kT=0.593, rot_step=np.radians(5.0), trans_step=0.3, tors_step=np.radians(30.0),
+               move_law=L.MC_GAUSSIAN, adapt=0, flip_every=0, minimize_every=50,
+               minimize_iters=20, gd_step=0.1, seed=2024)
+    runs, tot_steps, tot_s, finals = [], 0, 0.0, []
+    for s in systems:
+        sc = UFFScorer(0)
+        sc.set_protein(s.pocket)
+        sc.set_ligand(s.ligand)
+        chains = len(s.poses)
+        d = torch.from_numpy(s.poses).to(dev)
+        E = torch.empty(chains, dtype=torch.float64, device=dev)
+        acc = torch.empty(chains, dtype=torch.int32, device=dev)
+        stt = torch.empty(chains, dtype=torch.int32, device=dev)
+        # warm-up run: plans, buffers and the graph of a block
+        w = d.clone()
+        sc.mc_run_device(chains, 100, prm, w.data_ptr(), E.data_ptr(), None, None, None, None,
+                         None, True)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        sc.mc_run_device(chains, args.mc_steps, prm, d.data_ptr(), E.data_ptr(), None, None,
+                         acc.data_ptr(), stt.data_ptr(), None, True)
+        b.record()
+        torch.cuda.synchronize()
+        sec = a.elapsed_time(b) * 1e-3
+        tot_steps += chains * args.mc_steps
+        tot_s += sec
+        runs.append({"system": s.name, "ligand_atoms": s.ligand.n, "torsions": s.ligand.nrb,
+                     "pocket_atoms": s.pocket.n, "chains": chains,
+                     "chain_steps_per_s": chains * args.mc_steps / sec,
+                     "acceptance": float(acc.float().mean().item() / args.mc_steps)})
+        finals.append((s, d.cpu().numpy(), E.cpu().numpy()))
+        sc.close()
+    line = {
+        "metric": "MC chain-steps/s (energy per step, 20 GD iterations every 50 steps)",
+        "value": tot_steps / tot_s, "unit": "chain-steps/s", "n_gpus": 1,
+        "steps": args.mc_steps, "warmup": 100, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "512 chains x %d steps on each of 4 systems of the uneven batch "
+                               "(Gaussian moves 5 deg / 0.3 A / 30 deg, kT 0.593 kcal/mol)" %
+                               args.mc_steps, "graph": True},
+        "runs": runs,
+    }
+    if not args.no_cpu:
+        from oracle import np_twin as T
+        from oracle import oracle as O
+
+        errs = []
+        for s, dofs, Eg in finals:
+            n = 16
+            E64, _, _ = O.score_batch(s.pocket, s.ligand, dofs[:n],
+                                      flags=O.F_INTER | O.F_INTRA | O.F_RECENTER,
+                                      nthreads=os.cpu_count() or 1)
+            p, lg = s.pocket, s.ligand
+            for k in range(n):
+                xyz, _ = O.apply_config(lg, dofs[k].astype(np.float64), O.F_RECENTER)
+                scale = (T.ene_inter(p.xyz(), p.q, p.anum, xyz, lg.q, lg.anum, shifted=True,
+                                     dielectric=0, absolute=True) +
+                         T.ene_intra(xyz, lg.q, lg.anum, lg.interacting, dielectric=0,
+                                     absolute=True))
+                errs.append(abs(Eg[k] - E64[k]) / max(abs(E64[k]), scale, 1e-300))
+        line["cpu_baseline"] = {"kind": "port", "cores": os.cpu_count() or 1,
+                                "final_E_max_rel_err_vs_fp64": float(max(errs)),
+                                "error_scale": "max(|E64|, sum of |pair energies|)",
+                                "sample": "16 final chains per system re-scored in FP64"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "ragged":
+        return run_ragged(args)
+    if args.workload == "mc":
+        return run_mc(args)
 
     import torch
 

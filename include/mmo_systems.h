@@ -63,7 +63,20 @@ int mmo_systems_layout(const mmo_ctx* ctx, int* total_poses, int* total_dofs, in
 int mmo_score_systems_device(mmo_ctx* ctx, const float* d_dofs, int flags, double* d_E,
                              float* d_grad, int* d_status, void* stream);
 
-/* The same with host buffers (copies in and out through pinned staging). */
+/* Autotuner of the batch's sweep: times entries per lane (1, 2, 4), piece
+ * atoms (256, 512) and threads per CTA (128, 256, 512 where the registers
+ * allow) on this batch and keeps the fastest as the context's settings
+ * (mmo_set_cull / mmo_set_tiles).  Arguments as mmo_score_systems_device,
+ * whose outputs it leaves as the chosen plan computes them; *ms (may be NULL)
+ * the chosen plan's device milliseconds.  Refused inside a stream capture. */
+int mmo_tune_systems(mmo_ctx* ctx, const float* d_dofs, int flags, double* d_E, float* d_grad,
+                     int* d_status, void* stream, double* ms);
+
+/* The plan of the batch's last scoring call. */
+int mmo_systems_plan(const mmo_ctx* ctx, int* per_lane, int* threads, int* piece_atoms);
+
+/* mmo_score_systems_device with host buffers (copies in and out through
+ * pinned staging). */
 int mmo_score_systems(mmo_ctx* ctx, const float* dofs, int flags, double* E, float* grad,
                       int* status);
 

@@ -858,6 +858,7 @@ struct SysBatch {
   size_t cap_static = 0;
   DevSystems dev{};
   int E = 0, R = 0, nrblk = 0, nfblk = 0, tpp = 4, Lmax = 1, nrbmax = 0;
+  double pairs_all = 0.0;  // poses x ligand atoms x protein atoms over the batch
   // plan (pieces, groups, items) for (kp, piece atoms)
   long plan_key[3] = {-1, -1, -1};
   void* d_plan = nullptr;
@@ -970,6 +971,9 @@ int sys_build_static(mmo_ctx* ctx, SysBatch* S) {
   }
   S->E = ent;
   S->R = rec;
+  S->pairs_all = 0.0;
+  for (int u = 0; u < ns; ++u)
+    S->pairs_all += (double)S->in[u].poses * S->Ls[u] * (double)S->in[u].px.size();
   const int nv = (int)S->info.size();
   // threads per pose of the rebuild, as launch_rebuild chooses them
   int tpp = 32;
@@ -1231,18 +1235,31 @@ int score_systems(mmo_ctx* ctx, const float* d_dofs, int flags, double* d_E, flo
   io.err = d_err;
   io.B = S->B;
   const int fl = flags & (kFlagInter | kFlagIntra | kFlagGrad | kFlagRecenter);
-  ctx->last_cull = false;
-  ctx->last_pairs = 0;
+  ctx->last_cull = inter;  // the sweep counts its pair evaluations
+  ctx->last_grad = grad ? 1 : 0;
+  ctx->last_pairs = inter ? S->pairs_all : 0.0;
   ctx->last_launches = 2 + (inter ? 2 : 0);
+  const bool prof = ctx->profiling;
+  auto mark = [&](int k) { return prof ? cudaEventRecord(ctx->ev[k], st) : cudaSuccess; };
+  MMO_CK(mark(0), "event");
   MMO_CK(launch_sys_rebuild(S->dev, S->nrblk, S->tpp, io, S->scr, fl, st), "system rebuild kernel");
+  MMO_CK(mark(1), "event");
   if (inter) {
     MMO_CK(cudaMemsetAsync(ctx->d_queue, 0, 16, st), "work counter reset");
     MMO_CK(launch_sys_sort(S->dev, S->scr, S->cs, S->sort_smem, st), "system sort kernel");
+    MMO_CK(mark(2), "event");
     MMO_CK(launch_sys_pairs(S->dev, ctx->d_tab4, S->cs, S->kp, S->threads, S->blocks, S->smem,
                             fl, ctx->ph, d_err, st),
            "system pair kernel");
+  } else {
+    MMO_CK(mark(2), "event");
   }
+  MMO_CK(mark(3), "event");
   MMO_CK(launch_sys_finish(S->dev, S->nfblk, io, S->scr, fl, ctx->ph, st), "system finish kernel");
+  if (prof) {
+    MMO_CK(mark(4), "event");
+    ctx->ev_valid = true;
+  }
   return MMO_OK;
 }
 
@@ -2168,6 +2185,70 @@ int mmo_set_systems(mmo_ctx* ctx, int nsys, const mmo_system* systems) {
   ctx->sys = S;
   ++ctx->epoch;
   return sys_build_static(ctx, S);
+}
+
+int mmo_tune_systems(mmo_ctx* ctx, const float* d_dofs, int flags, double* d_E, float* d_grad,
+                     int* d_status, void* stream, double* ms_out) {
+  if (!ctx) return MMO_EINVAL;
+  if (!ctx->sys) return fail(ctx, MMO_ESTATE, "no systems: call mmo_set_systems first");
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  MMO_CK(cudaStreamIsCapturing(st, &cap), "capture status");
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(ctx, MMO_ESTATE, "mmo_tune_systems cannot run inside a stream capture");
+  auto run = [&]() { return score_systems(ctx, d_dofs, flags, d_E, d_grad, d_status, ctx->d_err, st); };
+  struct Cand { int kp, piece, threads; };
+  std::vector<Cand> cands;
+  for (int kp : {1, 2, 4})
+    for (int piece : {256, 512})
+      for (int th : {128, 256, 512})
+        if (th <= cull_max_threads(kp)) cands.push_back({kp, piece, th});
+  cudaEvent_t a, b;
+  MMO_CK(cudaEventCreate(&a), "event");
+  MMO_CK(cudaEventCreate(&b), "event");
+  float best_ms = 3e38f;
+  Cand best{0, 0, 0};
+  int r = MMO_OK;
+  for (const Cand& c : cands) {
+    ctx->cull_kp = c.kp;
+    ctx->cull_piece = c.piece;
+    ctx->tile_threads = c.threads;
+    ++ctx->epoch;
+    if (run() != MMO_OK || cudaStreamSynchronize(st) != cudaSuccess) continue;
+    float t[3];
+    bool ok = true;
+    for (float& v : t)
+      ok = ok && cudaEventRecord(a, st) == cudaSuccess && run() == MMO_OK &&
+           cudaEventRecord(b, st) == cudaSuccess && cudaEventSynchronize(b) == cudaSuccess &&
+           cudaEventElapsedTime(&v, a, b) == cudaSuccess;
+    if (!ok) continue;
+    std::sort(t, t + 3);
+    if (t[1] < best_ms) {
+      best_ms = t[1];
+      best = c;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  ctx->err.clear();
+  if (best_ms >= 3e38f) return fail(ctx, MMO_ECUDA, "mmo_tune_systems: no launch plan ran");
+  ctx->cull_kp = best.kp;
+  ctx->cull_piece = best.piece;
+  ctx->tile_threads = best.threads;
+  ++ctx->epoch;
+  if ((r = run())) return r;
+  if (ms_out) *ms_out = best_ms;
+  return MMO_OK;
+}
+
+int mmo_systems_plan(const mmo_ctx* ctx, int* per_lane, int* threads, int* piece_atoms) {
+  if (!ctx || !per_lane || !threads || !piece_atoms) return MMO_EINVAL;
+  if (!ctx->sys) return fail(const_cast<mmo_ctx*>(ctx), MMO_ESTATE, "no systems");
+  *per_lane = ctx->sys->kp;
+  *threads = ctx->sys->threads;
+  *piece_atoms = (int)ctx->sys->plan_key[1];
+  return MMO_OK;
 }
 
 int mmo_systems_layout(const mmo_ctx* ctx, int* total_poses, int* total_dofs, int* pose_off,

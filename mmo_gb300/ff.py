@@ -230,6 +230,18 @@ class UFFScorer:
         self._check(self._lib.mmo_score_systems_device(self._h, d_dofs, flags, d_E,
                                                        d_grad or None, d_status, stream))
 
+    def tune_systems_device(self, d_dofs: int, d_E: int, d_grad: int | None, d_status: int,
+                            flags: int, stream: int | None = None) -> float:
+        ms = C.c_double()
+        self._check(self._lib.mmo_tune_systems(self._h, d_dofs, flags, d_E, d_grad or None,
+                                               d_status, stream, C.byref(ms)))
+        return ms.value
+
+    def systems_plan(self) -> dict:
+        kp, th, pa = C.c_int(), C.c_int(), C.c_int()
+        self._check(self._lib.mmo_systems_plan(self._h, C.byref(kp), C.byref(th), C.byref(pa)))
+        return {"entries_per_lane": kp.value, "threads": th.value, "piece_atoms": pa.value}
+
     # -- plain drop-ins (one call per Mol.t, like the reference closures) --
     def ene_inter(self, lig: Mol) -> float:
         """Mol.ene_inter_UFF_shifted_bst prot_bst prot lig (src/mol.ml:958-960)."""

@@ -70,6 +70,8 @@ SIGNATURES = {
     "mmo_systems_layout": (_i, [_vp, _P(_i), _P(_i), _P(_i), _P(_i)]),
     "mmo_score_systems_device": (_i, [_vp, _vp, _i, _vp, _vp, _vp, _vp]),
     "mmo_score_systems": (_i, [_vp, _P(C.c_float), _i, _P(_d), _P(C.c_float), _P(_i)]),
+    "mmo_tune_systems": (_i, [_vp, _vp, _i, _vp, _vp, _vp, _vp, _P(C.c_double)]),
+    "mmo_systems_plan": (_i, [_vp, _P(_i), _P(_i), _P(_i)]),
     "mmo_philox4x32": (_i, [_vp, C.c_uint, C.c_uint, C.c_uint, C.c_uint, _i, _vp, _vp]),
     "mmo_tune": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp, _vp, _P(C.c_double)]),
     "mmo_set_tune_cache": (_i, [_vp, C.c_char_p]),

@@ -216,20 +216,36 @@ def pose_batch(n_poses=65536, seed=1, n_atoms=48, n_rot=8, n_pocket=6000, radius
     return System("poses%d_L%d_P%d" % (n_poses, n_atoms, n_pocket), pocket, lig, poses)
 
 
-def ragged_systems(n_systems=1024, poses_per=64, seed=3, density=None) -> list[System]:
-    """Uneven batch: ligand size log-uniform in 12-80 atoms, 0-15 rotatable
-    bonds, pocket size uniform in 2,000-8,000 atoms at the density of the
-    6,000-atom 18 A pocket."""
-    rng = np.random.default_rng(seed)
+def ragged_system(index: int, seed=3, poses_per=64, density=None) -> System:
+    """System ``index`` of the uneven batch: ligand size log-uniform in 12-80
+    atoms, 0-15 rotatable bonds, pocket size uniform in 2,000-8,000 atoms at the
+    density of the 6,000-atom 18 A pocket, ``poses_per`` random poses.  Each
+    system has its own generator (seeded by (seed, index)), so a batch can be
+    made in any order or in parallel."""
+    rng = np.random.default_rng([seed, index])
     density = density or 6000.0 / (4.0 / 3.0 * math.pi * 18.0 ** 3)
-    out = []
-    for s in range(n_systems):
-        n_l = int(round(math.exp(rng.uniform(math.log(12), math.log(80)))))
-        n_r = int(rng.integers(0, 16))
-        n_p = int(rng.integers(2000, 8001))
-        radius = (3.0 * n_p / (4.0 * math.pi * density)) ** (1.0 / 3.0)
-        lig = random_ligand(rng, n_l, n_r, "lig%d" % s)
-        pocket = random_pocket(rng, n_p, radius, "pocket%d" % s)
-        poses = random_poses(rng, poses_per, lig.nrb, 4.0)
-        out.append(System("sys%d" % s, pocket, lig, poses))
-    return out
+    n_l = int(round(math.exp(rng.uniform(math.log(12), math.log(80)))))
+    n_r = int(rng.integers(0, 16))
+    n_p = int(rng.integers(2000, 8001))
+    radius = (3.0 * n_p / (4.0 * math.pi * density)) ** (1.0 / 3.0)
+    lig = random_ligand(rng, n_l, n_r, "lig%d" % index)
+    pocket = random_pocket(rng, n_p, radius, "pocket%d" % index)
+    poses = random_poses(rng, poses_per, lig.nrb, 4.0)
+    return System("sys%d" % index, pocket, lig, poses)
+
+
+def _ragged_one(a):
+    return ragged_system(*a)
+
+
+def ragged_systems(n_systems=1024, poses_per=64, seed=3, density=None, workers=0) -> list[System]:
+    """The uneven batch of ragged_system 0 .. n_systems - 1; workers > 1 makes
+    them in that many spawned processes (start them before CUDA is used)."""
+    args = [(s, seed, poses_per, density) for s in range(n_systems)]
+    if workers and workers > 1 and n_systems > 1:
+        import concurrent.futures as cf
+        import multiprocessing as mp
+
+        with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+            return list(ex.map(_ragged_one, args, chunksize=max(1, n_systems // (4 * workers))))
+    return [_ragged_one(a) for a in args]

@@ -49,8 +49,9 @@ def test_systems_match_one_system_path(scorer_factory, systems, recenter):
         one = scorer_factory(s.pocket, s.ligand)
         E1, G1, st1 = one.score_poses(s.poses, grad=True, recenter=recenter)
         assert np.array_equal(sts[k], st1)
-        if s.pocket.n <= 6000 and not recenter:
+        if s.pocket.n <= 6000 and not recenter and len(s.poses) >= 2:
             # same row index, pieces and arithmetic as the one-system cut-off sweep
+            # (a single pose takes the one-pose kernel there)
             assert np.array_equal(Es[k], E1), k
             g = Gs[k].reshape(G1.shape)
             bad = ~((g == G1) | (np.isnan(g) & np.isnan(G1)))
