@@ -253,3 +253,42 @@ def score_batch(prot, lig, dofs, flags=F_INTER | F_INTRA, mode=0, eps=None, use_
                           int(use_cells), nthreads, _dp(E), _dp(G) if G is not None else None,
                           _ip(st))
     return E, G, st
+
+
+def grid_point(prot, p, type_anum, type_q, max_E=100000.0, ph=REF):
+    """Grid values of Lds.pre_calculate_FF_components_grid at point p (one per type)."""
+    P = OMol.of(prot)
+    ta = np.ascontiguousarray(type_anum, np.int32)
+    tq = np.ascontiguousarray(type_q, np.float64)
+    out = np.zeros(len(ta))
+    pp = np.ascontiguousarray(p, np.float64)
+    lib().orc_grid_point(C.byref(ph), C.byref(P.c), _dp(pp), len(ta), _ip(ta), _dp(tq),
+                         C.c_double(max_E), _dp(out))
+    return out
+
+
+def trilin(step, dims, values, p):
+    """G3D.trilin on float32 values [nz][ny][nx] (x fastest); (value, off-lattice)."""
+    v = np.ascontiguousarray(values, np.float32)
+    pp = np.ascontiguousarray(p, np.float64)
+    off = C.c_int(0)
+    f = lib().orc_trilin
+    f.restype = C.c_double
+    e = f(C.c_double(step), dims[0], dims[1], dims[2], v.ctypes.data_as(C.POINTER(C.c_float)),
+          _dp(pp), C.byref(off))
+    return e, bool(off.value)
+
+
+def ene_inter_interp(step, dims, grids, xyz, types):
+    """Mol.ene_inter_UFF_interp: grids float32 [ntypes][nz][ny][nx], xyz in the
+    lattice frame; (energy, off-lattice)."""
+    g = np.ascontiguousarray(grids, np.float32)
+    xyz = np.asarray(xyz, np.float64)
+    x, y, z = (np.ascontiguousarray(xyz[:, k]) for k in range(3))
+    t = np.ascontiguousarray(types, np.int32)
+    off = C.c_int(0)
+    f = lib().orc_ene_inter_interp
+    f.restype = C.c_double
+    e = f(C.c_double(step), dims[0], dims[1], dims[2], g.ctypes.data_as(C.POINTER(C.c_float)),
+          len(t), _dp(x), _dp(y), _dp(z), _ip(t), C.byref(off))
+    return e, bool(off.value)

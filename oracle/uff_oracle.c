@@ -716,3 +716,71 @@ void orc_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint3
   out[2] = c2;
   out[3] = c3;
 }
+
+/* ---- precomputed grids and their trilinear interpolation -------------------
+ * orc_grid_point: Mol.ene_inter_UFF_shifted_grid (src/mol.ml:964-989) at one
+ * point for single-atom "ligands" of (anum, charge) types, capped at max_E as
+ * Lds.pre_calculate_FF_components_grid does (src/lds.ml:452-469):
+ *   E_l(p) = min(max_E, K sum_i w q_i q_l / r + sum_i w D_il (p6^2 - 2 p6)),
+ * r = max(|p - r_i|, 0.01), w = shift_12A(r), over the protein atoms within
+ * 12 A.  The dielectric switch of ph selects q/r (eps 4, the reference) or
+ * q/r^2 (eps 4r). */
+void orc_grid_point(const orc_physics *ph, const orc_mol *prot, const double p[3], int ntypes,
+                    const int *type_anum, const double *type_q, double max_E, double *out) {
+  for (int l = 0; l < ntypes; ++l) {
+    double se = 0.0, sv = 0.0;
+    for (int i = 0; i < prot->n; ++i) {
+      const double dx = p[0] - prot->x[i], dy = p[1] - prot->y[i], dz = p[2] - prot->z[i];
+      const double d2 = dx * dx + dy * dy + dz * dz;
+      if (!(d2 < 144.0)) continue;
+      const double r = orc_non_zero_dist(sqrt(d2));
+      const double w = orc_shift_12A(r);
+      double x_ij, d_ij;
+      orc_pair_params(ph, type_anum[l], prot->anum[i], &x_ij, &d_ij);
+      const double p1 = x_ij / r, p6 = p1 * p1 * p1 * p1 * p1 * p1;
+      se += w * (prot->q[i] * type_q[l]) / (ph->dielectric ? r * r : r);
+      sv += w * (d_ij * ((-2.0 * p6) + (p6 * p6)));
+    }
+    const double e = orc_elec_weight() * se + sv;
+    out[l] = e < max_E ? e : max_E;
+  }
+}
+
+/* G3D.trilin (src/G3D.ml:97-157) on a lattice with its lowest point at the
+ * origin (x = i step), values x-fastest: v[i + j nx + k nx ny] (float32, as the
+ * reference's .ba1 files).  Returns 0 and sets *off when a corner falls off the
+ * lattice (the reference does not check). */
+double orc_trilin(double step, int nx, int ny, int nz, const float *v, const double p[3],
+                  int *off) {
+  const double inv = 1.0 / step;
+  const int i0 = (int)(p[0] * inv), j0 = (int)(p[1] * inv), k0 = (int)(p[2] * inv);
+  const int i1 = i0 + 1, j1 = j0 + 1, k1 = k0 + 1;
+  if (p[0] < 0 || p[1] < 0 || p[2] < 0 || i1 >= nx || j1 >= ny || k1 >= nz) {
+    if (off) *off = 1;
+    return 0.0;
+  }
+  const long j0x = (long)j0 * nx, j1x = (long)j1 * nx, k0xy = (long)k0 * nx * ny,
+             k1xy = (long)k1 * nx * ny;
+  const double wlx = (p[0] - i0 * step) * inv, wly = (p[1] - j0 * step) * inv,
+               wlz = (p[2] - k0 * step) * inv;
+  const double whx = 1.0 - wlx, why = 1.0 - wly, whz = 1.0 - wlz;
+  return v[i0 + j0x + k0xy] * (whx * why * whz) + v[i1 + j0x + k0xy] * (wlx * why * whz) +
+         v[i1 + j1x + k0xy] * (wlx * wly * whz) + v[i0 + j1x + k0xy] * (whx * wly * whz) +
+         v[i0 + j0x + k1xy] * (whx * why * wlz) + v[i1 + j0x + k1xy] * (wlx * why * wlz) +
+         v[i1 + j1x + k1xy] * (wlx * wly * wlz) + v[i0 + j1x + k1xy] * (whx * wly * wlz);
+}
+
+/* Mol.ene_inter_UFF_interp (src/mol.ml:1010-1020): sum over the ligand atoms of
+ * the trilinear value of the atom type's grid at the atom (coordinates in the
+ * lattice frame). */
+double orc_ene_inter_interp(double step, int nx, int ny, int nz, const float *grids, int n,
+                            const double *x, const double *y, const double *z, const int *type,
+                            int *off) {
+  double e = 0.0;
+  const size_t per = (size_t)nx * ny * nz;
+  for (int j = 0; j < n; ++j) {
+    const double p[3] = {x[j], y[j], z[j]};
+    e += orc_trilin(step, nx, ny, nz, grids + per * type[j], p, off);
+  }
+  return e;
+}

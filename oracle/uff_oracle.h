@@ -127,6 +127,16 @@ void orc_score_batch(const orc_physics *ph, const orc_mol *prot, const orc_ligan
 /* Philox4x32-10 block: out = philox(ctr, key) */
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
+/* precomputed interaction grids (src/lds.ml:452-469, src/mol.ml:964-989) and
+ * their trilinear interpolation (src/G3D.ml:97-157, src/mol.ml:1010-1020) */
+void orc_grid_point(const orc_physics *ph, const orc_mol *prot, const double p[3], int ntypes,
+                    const int *type_anum, const double *type_q, double max_E, double *out);
+double orc_trilin(double step, int nx, int ny, int nz, const float *v, const double p[3],
+                  int *off);
+double orc_ene_inter_interp(double step, int nx, int ny, int nz, const float *grids, int n,
+                            const double *x, const double *y, const double *z, const int *type,
+                            int *off);
+
 #ifdef __cplusplus
 }
 #endif

@@ -244,3 +244,39 @@ def test_philox_known_answers(oracle):
                                                       0x6D5451FD]
     assert ph([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0]) == \
         [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
+
+
+def test_grid_point_is_single_atom_inter_energy(oracle):
+    """A grid value is the shifted inter energy of a one-atom ligand of that
+    type at the point (Mol.ene_inter_UFF_shifted_grid == _shifted_brute on a
+    one-atom ligand), capped at max_E."""
+    from mmo_gb300 import synth
+
+    rng = np.random.default_rng(0)
+    prot = synth.random_pocket(rng, 300, 9.0)
+    types_a, types_q = [6, 7, 8, 16, 1], [0.1, -0.3, -0.5, 0.0, 0.2]
+    for _ in range(5):
+        p = rng.uniform(-6, 6, 3)
+        g = oracle.grid_point(prot, p, types_a, types_q, max_E=1e30)
+        for l, (a, q) in enumerate(zip(types_a, types_q)):
+            one = Mol("one", np.array([p[0]]), np.array([p[1]]), np.array([p[2]]),
+                      np.array([q]), np.array([a], np.int32), None, np.zeros((1, 1), np.int32))
+            e = oracle.ene_inter(prot, one)
+            assert abs(g[l] - e) <= 1e-12 * max(1.0, abs(e))
+    capped = oracle.grid_point(prot, prot.xyz()[0] + 0.05, [6], [0.0], max_E=100000.0)
+    assert capped[0] == 100000.0
+
+
+def test_trilin_reproduces_linear_functions(oracle):
+    step, dims = 0.5, (7, 6, 5)
+    k, j, i = np.meshgrid(np.arange(dims[2]), np.arange(dims[1]), np.arange(dims[0]),
+                          indexing="ij")
+    v = (1.5 + 0.25 * i * step - 0.5 * j * step + 2.0 * k * step).astype(np.float32)
+    rng = np.random.default_rng(1)
+    for _ in range(20):
+        p = rng.uniform(0, [(d - 1.01) * step for d in dims])
+        e, off = oracle.trilin(step, dims, v, p)
+        assert not off
+        assert abs(e - (1.5 + 0.25 * p[0] - 0.5 * p[1] + 2.0 * p[2])) < 1e-5
+    assert oracle.trilin(step, dims, v, [-0.1, 0.0, 0.0])[1]
+    assert oracle.trilin(step, dims, v, [0.0, 0.0, (dims[2] - 1) * step])[1]
