@@ -57,9 +57,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the default launch plan instead of the autotuner's")
-    ap.add_argument("--workload", default="poses", choices=["poses", "ragged", "mc"],
+    ap.add_argument("--workload", default="poses", choices=["poses", "ragged", "mc", "grid"],
                     help="poses: the energy+gradient pose batch (default); ragged: 1,024 "
-                         "systems x 64 poses in one pass; mc: 512 Monte Carlo chains")
+                         "systems x 64 poses in one pass; mc: 512 Monte Carlo chains; "
+                         "grid: per-type grids built, then the poses scored from them")
     ap.add_argument("--systems", type=int, default=1024, help="ragged: systems in the batch")
     ap.add_argument("--mc-steps", type=int, default=10000, help="mc: steps per chain")
     return ap.parse_args()
@@ -403,6 +404,214 @@ def run_mc(args):
     return 0
 
 
+def run_grid(args):
+    """The reference's default inter-energy path: per-type grids of the
+    4,096-pose workload's system built on the GPU (0.5 A lattice over the
+    protein's box plus the 36 A margin of src/lds.ml:1832, mask sphere of the
+    ROI's outer radius + 24 A about the pocket centre, 48 ligand atom types),
+    then the 4,096 poses scored (energy + gradient) by trilinear interpolation."""
+    import torch
+
+    from mmo_gb300 import grids as GR
+    from mmo_gb300 import lib as L
+    from mmo_gb300.ff import UFFScorer
+
+    s = system_for_rank(0, args.poses)
+    dev = torch.device("cuda", 0)
+    sc = UFFScorer(0)
+    sc.set_protein(s.pocket)
+    sc.set_ligand(s.ligand)
+    types, per = GR.type2id([s.ligand])
+    pxyz = s.pocket.xyz()
+    margin = 3.0 * GR.CHARGED_CUTOFF
+    origin, dims = GR.lattice_from_box(GR.GRID_STEP, pxyz.min(axis=0) - margin,
+                                       pxyz.max(axis=0) + margin)
+    roi_out_radius = 10.0
+    mask_c = np.zeros(3)
+    mask_r = GR.roi_mask_radius(roi_out_radius)
+    nelem = len({t[0] for t in types})
+
+    def build():
+        return sc.build_grids(GR.GRID_STEP, dims, origin, types, mask_center=mask_c,
+                              mask_radius=mask_r, max_E=GR.MAX_E)
+
+    sc.set_profiling(True)  # pair counts of the build (a counting variant of the kernel)
+    build()
+    st = sc.grid_build_stats()
+    sc.set_profiling(False)
+    # the faster launch shape (1 or 2 lattice points per lane; the values are the same)
+    shape_ms = {}
+    for kp in (1, 2):
+        sc.set_grid_build(kp)
+        build()
+        shape_ms[kp] = min(build() for _ in range(3))
+    kp_best = min(shape_ms, key=shape_ms.get)
+    sc.set_grid_build(kp_best)
+    for _ in range(max(args.warmup, 3)):
+        build()
+    steps = max(1, min(args.steps, 50))
+    clocks = Clocks(0)
+    clocks.start()
+    ms = [build() for _ in range(steps)]
+    clk = clocks.stop()
+    nvals = st["points"] * len(types)
+    value = nvals * len(ms) / (sum(ms) * 1e-3)
+    # end to end: protein upload, build and the download of every grid value
+    e2e = []
+    gbytes = 4 * len(types) * int(np.prod(dims))
+    for k in range(2 + steps // 5):
+        t = time.perf_counter()
+        sc.set_protein(s.pocket)
+        build()
+        g = sc.grid_values()
+        if k >= 2:
+            e2e.append(time.perf_counter() - t)
+    e2e_val = nvals * len(e2e) / sum(e2e)
+    # the interpolated scoring of the 4,096 poses (energy + gradient)
+    B, nd = s.poses.shape
+    d_dofs = torch.from_numpy(s.poses).to(dev)
+    d_E = torch.empty(B, dtype=torch.float64, device=dev)
+    d_G = torch.empty((B, nd), dtype=torch.float32, device=dev)
+    d_st = torch.empty(B, dtype=torch.int32, device=dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    sp = stream.cuda_stream
+    flags = L.F_INTER | L.F_INTRA | L.F_GRAD | L.F_GRID
+
+    def score():
+        sc.score_poses_device(d_dofs.data_ptr(), B, d_E.data_ptr(), d_G.data_ptr(),
+                              d_st.data_ptr(), flags, sp)
+
+    for _ in range(max(args.warmup, 3)):
+        score()
+    torch.cuda.synchronize()
+    sc.set_profiling(True)
+    ev, stages = [], []
+    for _ in range(args.steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        score()
+        b.record(stream)
+        ev.append((a, b))
+        stages.append(sc.stage_times())
+    torch.cuda.synchronize()
+    sc.set_profiling(False)
+    sms = [a.elapsed_time(b) for a, b in ev]
+    iv = B * len(sms) / (sum(sms) * 1e-3)
+    stg = np.mean(np.array(stages), axis=0)
+    st_bits = d_st.cpu().numpy()
+    h = torch.from_numpy(s.poses).pin_memory()
+    ie = []
+    for k in range(args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        Eh, Gh, sth = sc.score_poses(h.numpy(), grad=True, grid=True)
+        if k >= args.warmup:
+            ie.append(time.perf_counter() - t)
+    ie_val = B * len(ie) / sum(ie)
+    peak = sc.fp32_peak_tflops()
+    flops_pair = 24 + 8 * nelem
+    kernel_ms = float(np.mean(ms))
+    achieved = flops_pair * st["pairs_within_cutoff"] / (kernel_ms * 1e-3) * 1e-12
+    line = {
+        "metric": "grid values/s (per-type UFF interaction grids, 0.5 A lattice)",
+        "value": value, "unit": "values/s", "n_gpus": 1, "steps": steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": kernel_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "grids of the 4096-pose workload's system: 6000-atom pocket, "
+                               "%d ligand atom types (%d elements), lattice %dx%dx%d at 0.5 A "
+                               "(protein box + 36 A margin), mask sphere r = %.0f A "
+                               "(ROI outer radius %.0f A + 24 A)" %
+                               (len(types), nelem, dims[0], dims[1], dims[2], mask_r,
+                                roi_out_radius),
+                   "masked_points": st["points"], "values_per_build": nvals,
+                   "points_per_lane": kp_best, "shape_ms": shape_ms,
+                   "grid_bytes": gbytes,
+                   "l2": "each build writes %.1f GB (> L2)" % (gbytes / 1e9)},
+        "e2e": {"value": e2e_val, "unit": "values/s", "h2d_bytes_per_step": int(36 * s.pocket.n),
+                "d2h_bytes_per_step": gbytes,
+                "what": "mmo_set_protein + mmo_build_grids + mmo_grid_values (host copy)"},
+        "interp": {"metric": "poses/s (energy+grad) by grid interpolation", "value": iv,
+                   "unit": "poses/s", "ms_per_step": float(np.mean(sms)),
+                   "stages_ms": {"rebuild": float(stg[0]), "lookup": float(stg[1]),
+                                 "finish": float(stg[2])},
+                   "e2e": {"value": ie_val, "unit": "poses/s",
+                           "h2d_bytes_per_step": int(s.poses.nbytes),
+                           "d2h_bytes_per_step": int(Eh.nbytes + Gh.nbytes + sth.nbytes)},
+                   "status_off_grid": int(np.count_nonzero(st_bits & L.S_OFF_GRID)),
+                   "l2": "flushed before every timed step (256 MiB write), not timed"},
+        "roofline": {"bound": "fp32", "kernel": "k_grid_build", "achieved": achieved,
+                     "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "traffic": None,
+                     "flops_per_pair": flops_pair, "pairs_within_cutoff": st["pairs_within_cutoff"],
+                     "pairs_evaluated": st["pairs_evaluated"], "ms_per_launch": kernel_ms,
+                     "peak_source": "measured FP32 FMA probe on this GPU (mmo_fp32_fma_peak)"},
+        "gpu_launches": steps,
+        "clocks": clk,
+    }
+    if not args.no_cpu:
+        from oracle import oracle as O
+
+        nthreads = os.cpu_count() or 1
+        # every masked lattice point (the whole build), in random order
+        rng = np.random.default_rng(11)
+        ax = [np.arange(n) for n in dims]
+        ii, jj, kk = np.meshgrid(*ax, indexing="ij")
+        pts = origin + GR.GRID_STEP * np.stack([ii.ravel(), jj.ravel(), kk.ravel()], axis=1)
+        pts = pts[((pts - mask_c) ** 2).sum(axis=1) < mask_r * mask_r]
+        pts = pts[rng.permutation(len(pts))]
+        ta = np.array([t[0] for t in types], np.int32)
+        tq = np.array([t[1] for t in types])
+        n0 = 256
+        t0 = time.perf_counter()
+        O.grid_points(s.pocket, pts[:n0], ta, tq, nthreads=nthreads)
+        per = (time.perf_counter() - t0) / n0
+        n = int(min(len(pts), max(n0, 30.0 / max(per, 1e-9))))
+        t0 = time.perf_counter()
+        ref = O.grid_points(s.pocket, pts[:n], ta, tq, nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        # the error of the GPU values relative to max(|E|, sum of |pair terms|) on a
+        # sub-sample (capped values excluded: both sides hold max_E)
+        m = min(n, 20000)
+        ref_s, scale = O.grid_points(s.pocket, pts[:m], ta, tq, nthreads=nthreads,
+                                     with_scale=True)
+        gi = np.rint((pts[:m] - origin) / GR.GRID_STEP).astype(int)
+        got = g[:, gi[:, 2], gi[:, 1], gi[:, 0]].T.astype(np.float64)
+        free = ref_s < GR.MAX_E
+        # over values whose terms reach 1e-3 kcal/mol: near the 12 A cut-off a lone
+        # switched term of ~1e-6 carries the FP32 rounding of r^2 (relative
+        # 1e-7 of 144) as a relative error of ~1e-4 of itself
+        big = free & (scale >= 1e-3)
+        rel = np.where(big, np.abs(got - ref_s) /
+                       np.maximum(np.maximum(np.abs(ref_s), scale), 1e-300), 0.0)
+        err = float(rel.max())
+        abs_err = float(np.abs(got - ref_s)[free].max())
+        wk, wl = np.unravel_index(int(rel.argmax()), rel.shape)
+        wp = pts[wk]
+        worst = {"got": float(got[wk, wl]), "ref": float(ref_s[wk, wl]),
+                 "scale": float(scale[wk, wl]), "type": int(wl),
+                 "ijk": [int(v) for v in gi[wk]],
+                 "mask_margin_A": float(mask_r - np.sqrt(((wp - mask_c) ** 2).sum())),
+                 "nearest_atom_A": float(np.sqrt(((pxyz - wp) ** 2).sum(axis=1)).min())}
+        cap_ok = bool(np.all(got[~free] == GR.MAX_E))
+        line["cpu_baseline"] = {"value": n * len(types) / dt, "unit": "values/s",
+                                "cores": nthreads, "kind": "port",
+                                "sample": "%d of the %d masked lattice points x %d types, "
+                                          "%.1f s (12 A cell-list neighbour sum per point)" %
+                                          (n, len(pts), len(types), dt),
+                                "max_rel_err_gpu_vs_fp64": err,
+                                "error_scale": "max(|E|, sum of |pair terms|), 20000 points, "
+                                               "values with terms >= 1e-3 kcal/mol",
+                                "max_abs_err_kcal": abs_err,
+                                "capped_values_equal": cap_ok, "worst": worst}
+    print(json.dumps(line), flush=True)
+    sc.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -411,6 +620,8 @@ def main():
         return run_ragged(args)
     if args.workload == "mc":
         return run_mc(args)
+    if args.workload == "grid":
+        return run_grid(args)
 
     import torch
 

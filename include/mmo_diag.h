@@ -39,6 +39,13 @@ int mmo_last_launches(const mmo_ctx* ctx, int* kernels);
  * with CUDA events; *tflops = 2 * FMAs / time. */
 int mmo_fp32_fma_peak(mmo_ctx* ctx, double* tflops, double* ms);
 
+/* The last mmo_build_grids: lattice points inside the mask, (point, protein
+ * atom) pairs the build kernel evaluated for them, and those within 12 A (the
+ * pairs the grid values need); the pair counts are made only while
+ * mmo_set_profiling is on (else 0).  Any pointer may be NULL. */
+int mmo_grid_build_stats(const mmo_ctx* ctx, double* points, double* pairs_evaluated,
+                         double* pairs_within_cutoff);
+
 #ifdef __cplusplus
 }
 #endif

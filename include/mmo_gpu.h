@@ -51,10 +51,14 @@ extern "C" {
 #define MMO_F_INTRA 2         /* add the intra-ligand energy                      */
 #define MMO_F_GRAD 4          /* also dE/d[x, y, z, a, b, g, tau_0 ..]            */
 #define MMO_F_RECENTER 8      /* MC pose map (mol.ml:705-710) instead of Optim.apply_config (optim.ml:64-80) */
+#define MMO_F_GRID 16         /* with MMO_F_INTER: the inter energy interpolated from the
+                                 precomputed grids (mmo_grid.h, mol.ml:1010-1020) */
 
 /* ---- per-pose status bits ------------------------------------------------- */
 #define MMO_S_TOO_LONG 1      /* enclosing radius > 12 A: Mol.Too_long (mol.ml:587-591) */
 #define MMO_S_NONFINITE 2     /* energy is not finite                             */
+#define MMO_S_OFF_GRID 4      /* MMO_F_GRID: an atom's lattice cell falls off the grids; its
+                                 inter term is 0 (the reference reads out of bounds) */
 
 typedef struct mmo_ctx mmo_ctx;
 

@@ -46,6 +46,8 @@ typedef struct mmo_mc_params {
   int minimize_iters;    /* gradient-descent iterations per minimisation */
   double gd_step;        /* first gradient-descent step (A or rad, max norm) */
   unsigned long long seed;
+  int use_grid;          /* 1: inter energy from the precomputed grids (MMO_F_GRID, mmo_grid.h),
+                            the reference's default (src/lds.ml:1963-1975); 0: pair sums */
 } mmo_mc_params;
 
 /* Device buffers of a run.  dofs holds the start poses on entry and the final

@@ -14,6 +14,7 @@
 
 #include "../../include/mmo_diag.h"
 #include "../../include/mmo_gpu.h"
+#include "../../include/mmo_grid.h"
 #include "../../include/mmo_mc.h"
 #include "../../include/mmo_systems.h"
 #include "mmo_internal.cuh"
@@ -159,6 +160,23 @@ struct mmo_ctx {
   cudaEvent_t mc_ev[2] = {nullptr, nullptr};
   long epoch = 0;  // bumped whenever baked launch arguments (buffers, uploads, plans) change
   struct SysBatch* sys = nullptr;  // ragged batch of systems (mmo_set_systems)
+
+  // precomputed interaction grids (mmo_build_grids / mmo_load_grids)
+  bool grid_ok = false;
+  double grid_step = 0.0;
+  int grid_n[3] = {0, 0, 0};
+  double grid_origin[3] = {0, 0, 0};  // lattice point (0, 0, 0) in the user's frame
+  std::vector<int> grid_anum;
+  std::vector<double> grid_q;
+  float* d_grid = nullptr;            // [ntypes][nz][ny][nx]
+  size_t cap_grid = 0;
+  int* d_grid_lt = nullptr;           // [L] grid type of each ligand atom
+  size_t cap_grid_lt = 0;
+  std::vector<int> grid_lt;           // host copy
+  bool grid_map_ok = false;
+  std::string grid_map_err = "no grids: call mmo_build_grids or mmo_load_grids first";
+  double grid_stats[3] = {0, 0, 0};   // last build: masked points, pairs evaluated, within 12 A
+  int grid_kp_set = 0;                // lattice points per lane of the build kernel, 0: automatic
 
   // host-API staging
   char* h_in = nullptr;
@@ -450,6 +468,108 @@ int upload_ligand(mmo_ctx* ctx) {
 // spacing h in (iz, iy) order, empty rows dropped, each row sorted by x; a
 // flush point after the row where 256 atoms have accumulated.  Coordinates are
 // in the device frame (origin subtracted).
+// Grid type of each ligand atom: the grid type of the atom's element and
+// charge (the reference types a ligand's atoms by its unique (anum, charge)
+// pairs, Mol.get_typ / Mol.get_all_vdW_elec_types, src/mol.ml:295-304).  An
+// atom without a grid type leaves MMO_F_GRID scoring refused (not an error of
+// the upload that found it).
+int grid_map(mmo_ctx* ctx) {
+  ctx->grid_map_ok = false;
+  if (!ctx->grid_ok) {
+    ctx->grid_map_err = "no grids: call mmo_build_grids or mmo_load_grids first";
+    return MMO_OK;
+  }
+  if (!ctx->has_lig) {
+    ctx->grid_map_err = "no ligand: call mmo_set_ligand first";
+    return MMO_OK;
+  }
+  const int L = (int)ctx->ltype.size(), nt = (int)ctx->grid_anum.size();
+  std::vector<int> lt(L, -1);
+  for (int a = 0; a < L; ++a) {
+    for (int l = 0; l < nt && lt[a] < 0; ++l)
+      if (type_of(ctx->grid_anum[l]) == ctx->ltype[a] && ctx->grid_q[l] == ctx->lq[a]) lt[a] = l;
+    if (lt[a] < 0) {
+      char buf[160];
+      snprintf(buf, sizeof buf, "ligand atom %d (UFF row %d, charge %.9g) has no grid type", a,
+               ctx->ltype[a], ctx->lq[a]);
+      ctx->grid_map_err = buf;
+      return MMO_OK;
+    }
+  }
+  int r = grow(ctx, (void**)&ctx->d_grid_lt, &ctx->cap_grid_lt, sizeof(int) * L, "grid atom types");
+  if (r) return r;
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before grid type upload");
+  MMO_CK(cudaMemcpy(ctx->d_grid_lt, lt.data(), sizeof(int) * L, cudaMemcpyHostToDevice),
+         "grid atom type upload");
+  ctx->grid_lt = lt;
+  ctx->grid_map_ok = true;
+  ++ctx->epoch;
+  return MMO_OK;
+}
+
+// checks of a grid spec shared by the build and the load; on success the
+// context's lattice, types and value array are set (values not yet written)
+int grid_take_spec(mmo_ctx* ctx, const char* who, const mmo_grid_spec* sp, bool build) {
+  if (!sp) return fail(ctx, MMO_EINVAL, "%s: spec is NULL", who);
+  if (!(sp->step > 0) || !std::isfinite(sp->step))
+    return fail(ctx, MMO_EINVAL, "%s: step must be a positive finite number", who);
+  const int n[3] = {sp->nx, sp->ny, sp->nz};
+  for (int d = 0; d < 3; ++d)
+    if (n[d] < 2 || n[d] > (1 << 14))
+      return fail(ctx, MMO_EINVAL, "%s: lattice points per axis must be in 2..16384", who);
+  const size_t pts = (size_t)n[0] * n[1] * n[2];
+  if (pts > (size_t)INT32_MAX)
+    return fail(ctx, MMO_EINVAL, "%s: more than 2^31 - 1 lattice points", who);
+  if (sp->ntypes < 1 || sp->ntypes > kMaxLig || !sp->type_anum || !sp->type_q)
+    return fail(ctx, MMO_EINVAL, "%s: ntypes must be in 1..%d with both type arrays", who,
+                kMaxLig);
+  for (int d = 0; d < 3; ++d)
+    if (!std::isfinite(sp->origin[d]))
+      return fail(ctx, MMO_EINVAL, "%s: non-finite origin", who);
+  if (build) {
+    if (std::isnan(sp->max_E)) return fail(ctx, MMO_EINVAL, "%s: max_E is NaN", who);
+    if (std::isnan(sp->mask_radius) || (sp->mask_radius > 0 && !std::isfinite(sp->mask_radius)))
+      return fail(ctx, MMO_EINVAL, "%s: mask_radius must be finite (or <= 0: no mask)", who);
+    for (int d = 0; d < 3; ++d)
+      if (sp->mask_radius > 0 && !std::isfinite(sp->mask_center[d]))
+        return fail(ctx, MMO_EINVAL, "%s: non-finite mask centre", who);
+  }
+  for (int l = 0; l < sp->ntypes; ++l) {
+    if (type_of(sp->type_anum[l]) < 0)
+      return fail(ctx, MMO_EELEMENT, "%s: type %d: element %d not in the UFF table", who, l,
+                  sp->type_anum[l]);
+    if (!std::isfinite(sp->type_q[l]))
+      return fail(ctx, MMO_EINVAL, "%s: type %d: non-finite charge", who, l);
+  }
+  ctx->grid_ok = false;
+  ctx->grid_map_ok = false;
+  ctx->grid_map_err = "no grids: call mmo_build_grids or mmo_load_grids first";
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before grid upload");
+  int r = grow(ctx, (void**)&ctx->d_grid, &ctx->cap_grid, sizeof(float) * pts * sp->ntypes,
+               "grid values");
+  if (r) return r;
+  ctx->grid_step = sp->step;
+  for (int d = 0; d < 3; ++d) {
+    ctx->grid_n[d] = n[d];
+    ctx->grid_origin[d] = sp->origin[d];
+  }
+  ctx->grid_anum.assign(sp->type_anum, sp->type_anum + sp->ntypes);
+  ctx->grid_q.assign(sp->type_q, sp->type_q + sp->ntypes);
+  return MMO_OK;
+}
+
+// the lattice of the context's grids in the device frame
+GridLook grid_look(const mmo_ctx* ctx) {
+  GridLook g{};
+  for (int d = 0; d < 3; ++d) g.o[d] = ctx->grid_origin[d] - ctx->origin[d];
+  g.inv = 1.0 / ctx->grid_step;
+  g.nx = ctx->grid_n[0];
+  g.ny = ctx->grid_n[1];
+  g.nz = ctx->grid_n[2];
+  return g;
+}
+
 struct RowIndex {
   std::vector<float4> atoms;    // [n][2]
   std::vector<int> rs;          // [nrows + 1]
@@ -749,25 +869,29 @@ int check_dev_err(mmo_ctx* ctx, int flag) {
 int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E,
                  float* d_grad, int* d_status, int* d_err, int zero_err, cudaStream_t st) {
   if (!ctx->has_lig) return fail(ctx, MMO_ESTATE, "no ligand: call mmo_set_ligand first");
-  if ((flags & MMO_F_INTER) && ctx->prot.P <= 0)
+  const bool use_grid = (flags & MMO_F_INTER) && (flags & MMO_F_GRID);
+  if (use_grid && !ctx->grid_map_ok)
+    return fail(ctx, MMO_ESTATE, "MMO_F_GRID: %s", ctx->grid_map_err.c_str());
+  if ((flags & MMO_F_INTER) && !use_grid && ctx->prot.P <= 0)
     return fail(ctx, MMO_ESTATE, "no protein: call mmo_set_protein first");
   if (B < 0 || (B > 0 && (!d_dofs || !d_E || !d_status)))
     return fail(ctx, MMO_EINVAL, "bad batch arguments");
   if ((flags & MMO_F_GRAD) && !d_grad) return fail(ctx, MMO_EINVAL, "MMO_F_GRAD needs grad_out");
   if (B == 0) return MMO_OK;
   const bool grad = flags & MMO_F_GRAD;
-  const bool inter = (flags & MMO_F_INTER) && ctx->prot.P > 0;
+  const bool inter = use_grid || ((flags & MMO_F_INTER) && ctx->prot.P > 0);
   const int L = ctx->lig.L;
-  const bool cull = inter && use_cull(ctx, B);
+  const bool cull = inter && !use_grid && use_cull(ctx, B);
   ctx->last_cull = cull;
   ctx->last_grad = grad ? 1 : 0;
-  ctx->last_pairs = inter ? (double)B * L * ctx->prot.P : 0.0;
-  // rebuild + finish, and the sweep: entry bin, scan, scatter, sweep
+  ctx->last_pairs = inter && !use_grid ? (double)B * L * ctx->prot.P : 0.0;
+  // rebuild + finish, and the sweep: entry bin, scan, scatter, sweep (or the
+  // grid lookup)
   ctx->last_launches = 2 + (cull ? 4 : (inter ? 1 : 0));
   PairPlan plan{};
   int C = 1;
   int r;
-  if (inter) {
+  if (inter && !use_grid) {
     if (B == 1) {
       C = std::max(1, (ctx->prot.P + 255) / 256);
     } else if (cull) {
@@ -810,7 +934,11 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
     MMO_CK(mark(3), "event");
   } else {
     MMO_CK(mark(2), "event");
-    if (inter) {
+    if (use_grid) {
+      MMO_CK(launch_grid_inter(grid_look(ctx), ctx->scr.X, B * L, L, ctx->d_grid_lt, ctx->d_grid,
+                               ctx->scr.Epart, grad ? ctx->scr.Gpart : nullptr, d_status, grad, st),
+             "grid lookup kernel");
+    } else if (inter) {
       if (B == 1) {
         MMO_CK(launch_pairs_plain(ctx->prot, ctx->tab, ctx->scr.X, ctx->lig.q, ctx->lig.type, L,
                                   C, ctx->scr.Epart, ctx->scr.Gpart, grad, ctx->ph, st),
@@ -1335,6 +1463,8 @@ int mmo_ctx_destroy(mmo_ctx* ctx) {
   cudaFree(ctx->cs.arrive);
   cudaFree(ctx->cs.vis);
   cudaFree(ctx->d_mc);
+  cudaFree(ctx->d_grid);
+  cudaFree(ctx->d_grid_lt);
   sys_free(ctx->sys);
   if (ctx->mc_exec) cudaGraphExecDestroy(ctx->mc_exec);
   for (auto& e : ctx->mc_ev)
@@ -1584,7 +1714,8 @@ int mmo_set_ligand(mmo_ctx* ctx, int n, const double* xs, const double* ys, cons
   ctx->lgatoms = in.gat;
   ctx->linter = in.inter;
   MMO_CK(cudaSetDevice(ctx->device), "set device");
-  return upload_ligand(ctx);
+  if ((r = upload_ligand(ctx))) return r;
+  return grid_map(ctx);
 }
 
 int mmo_ene_inter(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
@@ -1965,7 +2096,11 @@ int mmo_mc_run(mmo_ctx* ctx, int chains, int steps, const mmo_mc_params* prm,
   p.B = B;
   p.nd = nd;
   p.nrb = nrb;
-  const int flags = (ctx->prot.P > 0 ? MMO_F_INTER : 0) | MMO_F_INTRA | MMO_F_RECENTER;
+  if (prm->use_grid && !ctx->grid_map_ok)
+    return fail(ctx, MMO_ESTATE, "mmo_mc_run: use_grid: %s", ctx->grid_map_err.c_str());
+  const int flags = (prm->use_grid ? MMO_F_INTER | MMO_F_GRID
+                                   : (ctx->prot.P > 0 ? MMO_F_INTER : 0)) |
+                    MMO_F_INTRA | MMO_F_RECENTER;
   const bool minimize = prm->minimize_every > 0 && prm->minimize_iters > 0;
   const int block = std::max(1, std::min(steps, minimize ? prm->minimize_every : 50));
   const bool prof = ctx->profiling;
@@ -2309,6 +2444,190 @@ int mmo_score_systems(mmo_ctx* ctx, const float* dofs, int flags, double* E, flo
   return check_dev_err(ctx, *reinterpret_cast<int*>(ctx->h_out + o_err));
 }
 
+// ---- precomputed interaction grids ------------------------------------------
+int mmo_build_grids(mmo_ctx* ctx, const mmo_grid_spec* spec, double* ms) {
+  if (!ctx) return MMO_EINVAL;
+  if (ctx->prot.P <= 0 || !ctx->d_cull)
+    return fail(ctx, MMO_ESTATE, "mmo_build_grids: no protein: call mmo_set_protein first");
+  int r = grid_take_spec(ctx, "mmo_build_grids", spec, true);
+  if (r) return r;
+  const int nt = spec->ntypes, nx = spec->nx, ny = spec->ny, nz = spec->nz;
+  // the distinct elements of the types, in order of first appearance
+  std::vector<int> elems, type_elem(nt);
+  for (int l = 0; l < nt; ++l) {
+    const int t = type_of(spec->type_anum[l]);
+    const auto it = std::find(elems.begin(), elems.end(), t);
+    type_elem[l] = (int)(it - elems.begin());
+    if (it == elems.end()) elems.push_back(t);
+  }
+  GridBuild gb{};
+  gb.ntypes = nt;
+  gb.nelem = (int)elems.size();
+  gb.nx = nx;
+  gb.ny = ny;
+  gb.nz = nz;
+  gb.step = spec->step;
+  gb.max_Ef = (float)spec->max_E;
+  for (int d = 0; d < 3; ++d) {
+    gb.o[d] = spec->origin[d] - ctx->origin[d];
+    gb.mc[d] = spec->mask_center[d] - ctx->origin[d];
+  }
+  const bool masked = spec->mask_radius > 0;
+  gb.mr2 = masked ? spec->mask_radius * spec->mask_radius : HUGE_VAL;
+  for (int pt = 0; pt < kNTypes; ++pt)
+    for (int e = 0; e < gb.nelem; ++e) {
+      double x2, d;
+      pair_xd(ctx->ph.mixing, pt, elems[e], &x2, &d);
+      // (X, 1/D), X = D^(1/3) x^2: (X / r^2)^3 = D (x / r)^6
+      gb.el[pt * kGridElems + e] =
+          make_float2((float)(std::cbrt(d) * x2), d > 0.0 ? (float)(1.0 / d) : 0.f);
+    }
+  // the point tiles that meet the mask sphere (and the points inside it)
+  std::vector<int3> tiles;
+  double npts = masked ? 0.0 : (double)nx * ny * nz;
+  // the counting variant of the kernel (profiling) has one point per lane
+  gb.kp = ctx->profiling ? 1 : (ctx->grid_kp_set ? ctx->grid_kp_set : 2);
+  const int TX = kGridTileX, TY = kGridTileY, TZ = 2 * gb.kp;
+  for (int tz = 0; tz < (nz + TZ - 1) / TZ; ++tz)
+    for (int ty = 0; ty < (ny + TY - 1) / TY; ++ty)
+      for (int tx = 0; tx < (nx + TX - 1) / TX; ++tx) {
+        if (masked) {
+          const int lo[3] = {TX * tx, TY * ty, TZ * tz};
+          const int hi[3] = {std::min(TX * tx + TX - 1, nx - 1), std::min(TY * ty + TY - 1, ny - 1),
+                             std::min(TZ * tz + TZ - 1, nz - 1)};
+          double d2 = 0.0;
+          for (int d = 0; d < 3; ++d) {
+            const double a = gb.o[d] + spec->step * lo[d], b = gb.o[d] + spec->step * hi[d];
+            const double c = gb.mc[d];
+            const double g = c < a ? a - c : (c > b ? c - b : 0.0);
+            d2 += g * g;
+          }
+          if (!(d2 < gb.mr2)) continue;
+          for (int k = lo[2]; k <= hi[2]; ++k)
+            for (int j = lo[1]; j <= hi[1]; ++j)
+              for (int i = lo[0]; i <= hi[0]; ++i) {
+                const double px = gb.o[0] + spec->step * i - gb.mc[0];
+                const double py = gb.o[1] + spec->step * j - gb.mc[1];
+                const double pz = gb.o[2] + spec->step * k - gb.mc[2];
+                npts += px * px + py * py + pz * pz < gb.mr2;
+              }
+        }
+        tiles.push_back(make_int3(tx, ty, tz));
+      }
+  gb.ntiles = (int)tiles.size();
+  size_t off = 0;
+  const size_t o_cnt = take(off, 2 * sizeof(unsigned long long));
+  const size_t o_tiles = take(off, sizeof(int3) * std::max<size_t>(tiles.size(), 1));
+  const size_t o_q = take(off, sizeof(float) * nt);
+  const size_t o_el = take(off, sizeof(int) * nt);
+  std::vector<char> blob(off, 0);
+  if (!tiles.empty()) memcpy(blob.data() + o_tiles, tiles.data(), sizeof(int3) * tiles.size());
+  for (int l = 0; l < nt; ++l) {
+    const float qf = (float)spec->type_q[l];
+    memcpy(blob.data() + o_q + sizeof(float) * l, &qf, sizeof qf);
+  }
+  memcpy(blob.data() + o_el, type_elem.data(), sizeof(int) * nt);
+  char* d_blob = nullptr;
+  MMO_CK(cudaMalloc((void**)&d_blob, off), "grid build tables");
+  cudaError_t e = cudaMemcpy(d_blob, blob.data(), off, cudaMemcpyHostToDevice);
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  if (e == cudaSuccess) e = cudaEventCreate(&ev[0]);
+  if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+  gb.tiles = reinterpret_cast<const int3*>(d_blob + o_tiles);
+  gb.type_qf = reinterpret_cast<const float*>(d_blob + o_q);
+  gb.type_elem = reinterpret_cast<const int*>(d_blob + o_el);
+  // pair counts only under mmo_set_profiling (a separate instantiation of the kernel)
+  gb.pairs = ctx->profiling ? reinterpret_cast<unsigned long long*>(d_blob + o_cnt) : nullptr;
+  const size_t bytes = sizeof(float) * (size_t)nx * ny * nz * nt;
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_grid, 0, bytes, ctx->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(ev[0], ctx->stream);
+  if (e == cudaSuccess) e = launch_grid_build(ctx->cull, gb, ctx->ph.dielectric, ctx->d_grid,
+                                              ctx->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(ev[1], ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  float t = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&t, ev[0], ev[1]);
+  unsigned long long cnt[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(cnt, d_blob + o_cnt, sizeof cnt, cudaMemcpyDeviceToHost);
+  for (auto& v : ev)
+    if (v) cudaEventDestroy(v);
+  cudaFree(d_blob);
+  ctx->grid_stats[0] = npts;
+  ctx->grid_stats[1] = (double)cnt[0];
+  ctx->grid_stats[2] = (double)cnt[1];
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "grid build");
+  if (ms) *ms = t;
+  ctx->grid_ok = true;
+  ++ctx->epoch;
+  return grid_map(ctx);
+}
+
+int mmo_set_grid_build(mmo_ctx* ctx, int points_per_lane) {
+  if (!ctx) return MMO_EINVAL;
+  if (points_per_lane < 0 || points_per_lane > 2)
+    return fail(ctx, MMO_EINVAL, "mmo_set_grid_build: points_per_lane must be 0, 1 or 2");
+  ctx->grid_kp_set = points_per_lane;
+  return MMO_OK;
+}
+
+int mmo_load_grids(mmo_ctx* ctx, const mmo_grid_spec* spec, const float* values) {
+  if (!ctx) return MMO_EINVAL;
+  if (!values) return fail(ctx, MMO_EINVAL, "mmo_load_grids: values is NULL");
+  int r = grid_take_spec(ctx, "mmo_load_grids", spec, false);
+  if (r) return r;
+  const size_t bytes = sizeof(float) * (size_t)spec->nx * spec->ny * spec->nz * spec->ntypes;
+  MMO_CK(cudaMemcpy(ctx->d_grid, values, bytes, cudaMemcpyHostToDevice), "grid upload");
+  ctx->grid_ok = true;
+  ++ctx->epoch;
+  return grid_map(ctx);
+}
+
+int mmo_grid_values(mmo_ctx* ctx, float* values) {
+  if (!ctx) return MMO_EINVAL;
+  if (!ctx->grid_ok) return fail(ctx, MMO_ESTATE, "mmo_grid_values: no grids");
+  if (!values) return fail(ctx, MMO_EINVAL, "mmo_grid_values: values is NULL");
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before grid download");
+  const size_t bytes = sizeof(float) * (size_t)ctx->grid_n[0] * ctx->grid_n[1] * ctx->grid_n[2] *
+                       ctx->grid_anum.size();
+  MMO_CK(cudaMemcpy(values, ctx->d_grid, bytes, cudaMemcpyDeviceToHost), "grid download");
+  return MMO_OK;
+}
+
+int mmo_grid_dims(const mmo_ctx* ctx, int* ntypes, int* nx, int* ny, int* nz) {
+  if (!ctx) return MMO_EINVAL;
+  if (!ctx->grid_ok) return MMO_ESTATE;
+  if (ntypes) *ntypes = (int)ctx->grid_anum.size();
+  if (nx) *nx = ctx->grid_n[0];
+  if (ny) *ny = ctx->grid_n[1];
+  if (nz) *nz = ctx->grid_n[2];
+  return MMO_OK;
+}
+
+int mmo_grid_build_stats(const mmo_ctx* ctx, double* points, double* pairs_evaluated,
+                         double* pairs_within_cutoff) {
+  if (!ctx) return MMO_EINVAL;
+  if (points) *points = ctx->grid_stats[0];
+  if (pairs_evaluated) *pairs_evaluated = ctx->grid_stats[1];
+  if (pairs_within_cutoff) *pairs_within_cutoff = ctx->grid_stats[2];
+  return MMO_OK;
+}
+
+int mmo_grid_device(const mmo_ctx* ctx, const float** d_values) {
+  if (!ctx || !d_values) return MMO_EINVAL;
+  if (!ctx->grid_ok) return MMO_ESTATE;
+  *d_values = ctx->d_grid;
+  return MMO_OK;
+}
+
+int mmo_grid_atom_types(mmo_ctx* ctx, int* out) {
+  if (!ctx) return MMO_EINVAL;
+  if (!out) return fail(ctx, MMO_EINVAL, "mmo_grid_atom_types: out is NULL");
+  if (!ctx->grid_map_ok) return fail(ctx, MMO_EINVAL, "%s", ctx->grid_map_err.c_str());
+  std::copy(ctx->grid_lt.begin(), ctx->grid_lt.end(), out);
+  return MMO_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
@@ -2355,7 +2674,10 @@ extern "C" int mmo_score_poses_noalloc(mmo_ctx* ctx, int B, const float* d_dofs,
                                        double* d_E, float* d_grad, int* d_status, void* stream) {
   if (!ctx) return MMO_EINVAL;
   if (!ctx->has_lig) return fail(ctx, MMO_ESTATE, "no ligand: call mmo_set_ligand first");
-  if ((flags & MMO_F_INTER) && ctx->prot.P <= 0)
+  const bool use_grid = (flags & MMO_F_INTER) && (flags & MMO_F_GRID);
+  if (use_grid && !ctx->grid_map_ok)
+    return fail(ctx, MMO_ESTATE, "MMO_F_GRID: %s", ctx->grid_map_err.c_str());
+  if ((flags & MMO_F_INTER) && !use_grid && ctx->prot.P <= 0)
     return fail(ctx, MMO_ESTATE, "no protein: call mmo_set_protein first");
   if (B < 0 || (B > 0 && (!d_dofs || !d_E || !d_status)))
     return fail(ctx, MMO_EINVAL, "mmo_score_poses_noalloc: bad batch arguments");
@@ -2363,7 +2685,7 @@ extern "C" int mmo_score_poses_noalloc(mmo_ctx* ctx, int B, const float* d_dofs,
     return fail(ctx, MMO_EINVAL, "mmo_score_poses_noalloc: MMO_F_GRAD needs grad_out");
   if (B == 0) return MMO_OK;
   const bool grad = flags & MMO_F_GRAD;
-  const bool inter = (flags & MMO_F_INTER) && ctx->prot.P > 0;
+  const bool inter = use_grid || ((flags & MMO_F_INTER) && ctx->prot.P > 0);
   const int L = ctx->lig.L;
   // scratch layout: X[B][L][2] | (gradient: Y[B][L] | rec[B][nrb][3] | cen[B]) |
   // Epart[B][C][L] | (gradient: Gpart[B][C][L])
@@ -2371,7 +2693,7 @@ extern "C" int mmo_score_poses_noalloc(mmo_ctx* ctx, int B, const float* d_dofs,
   const size_t fixed = 256 * 6 + sizeof(float4) * 2 * (size_t)B * L +
                        (grad ? sizeof(float4) * ((size_t)B * L + 3 * (size_t)B * nrb + B) : 0);
   const size_t per_chunk = (sizeof(double) + (grad ? sizeof(float4) : 0)) * (size_t)B * L;
-  const int nslices = inter ? (ctx->prot.P + kSliceAtoms - 1) / kSliceAtoms : 1;
+  const int nslices = inter && !use_grid ? (ctx->prot.P + kSliceAtoms - 1) / kSliceAtoms : 1;
   const long c_fit = fixed < kNoAllocBytes ? (long)((kNoAllocBytes - fixed) / per_chunk) : 0;
   if (c_fit < nslices) {
     const size_t need = fixed + per_chunk * nslices;
@@ -2387,7 +2709,7 @@ extern "C" int mmo_score_poses_noalloc(mmo_ctx* ctx, int B, const float* d_dofs,
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   PairPlan plan{};
   int C = 1;
-  if (inter) {
+  if (inter && !use_grid) {
     plan = plan_for(ctx, B, grad);
     const int c_slice = std::max(1, std::min(plan.C / nslices, (int)(c_fit / nslices)));
     C = c_slice * nslices;
@@ -2429,9 +2751,13 @@ extern "C" int mmo_score_poses_noalloc(mmo_ctx* ctx, int B, const float* d_dofs,
   if (!inter) fl &= ~kFlagInter;
   // every region a kernel reads is written first in this call: X, Y, the
   // torsion records and the centroids by the rebuild, each (pose, chunk,
-  // atom) partial by the pair sweep
+  // atom) partial by the pair sweep or the grid lookup
   MMO_CK(launch_rebuild(ctx->lig, io, s, fl, st), "rebuild kernel");
-  if (inter)
+  if (use_grid)
+    MMO_CK(launch_grid_inter(grid_look(ctx), s.X, B * L, L, ctx->d_grid_lt, ctx->d_grid, s.Epart,
+                             grad ? s.Gpart : nullptr, d_status, grad, st),
+           "grid lookup kernel");
+  else if (inter)
     MMO_CK(launch_pairs_batched(ctx->prot, ctx->d_tab4, ctx->lig, s, B, fl, ctx->ph, plan,
                                 ctx->d_err, st),
            "batched pair kernel");

@@ -1,0 +1,391 @@
+// kernels_grid.cu -- precomputed interaction grids and the energy they give.
+//
+// k_grid_build: the values of Lds.pre_calculate_FF_components_grid
+// (UnixJunkie/MMO src/lds.ml:452-469, the point sum Mol.ene_inter_UFF_shifted_grid
+// of src/mol.ml:964-989): for every lattice point within the mask sphere and
+// every ligand atom type l = (element a_l, charge q_l),
+//   E_l(p) = min(max_E, q_l phi(p) + V_{a_l}(p)),
+//   phi(p) = K sum_i w q_i / r,  V_a(p) = sum_i w D_ia (p6^2 - 2 p6),
+// over the protein atoms within 12 A (w the 12 A switch, r clamped at 0.01 A).
+// A warp owns a 4 x 4 x 4 tile of lattice points (two per lane); the protein
+// is read through its row index, culled against the tile's box and compacted
+// per warp as in the cut-off sweep; pair terms in FP32, sums per row and
+// per block of rows in FP32, over the blocks in compensated FP32.
+//
+// k_grid_inter: Mol.ene_inter_UFF_interp (src/mol.ml:1010-1020) with
+// G3D.trilin (src/G3D.ml:97-157) for every (pose, ligand atom) entry, and the
+// derivative of the trilinear form, into the same per-entry partials as the
+// pair sweep (so the finishing pass adds the intra term and the adjoint).
+#include "mmo_internal.cuh"
+
+namespace mmo {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kGridList = 64;         // compacted atoms per warp (< 32 + 32)
+constexpr int kGridFlushAtoms = 1024;  // protein atoms per FP32 block sum
+
+__device__ __forceinline__ float gwmin(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
+// acc + x as an unevaluated float pair (TwoSum: the rounding error of the
+// high part's sum is exact and goes to the low part)
+__device__ __forceinline__ float2 two_sum_add(float2 acc, float x) {
+  const float s = __fadd_rn(acc.x, x);
+  const float bp = __fsub_rn(s, acc.x);
+  const float ap = __fsub_rn(s, bp);
+  const float err = __fadd_rn(__fsub_rn(acc.x, ap), __fsub_rn(x, bp));
+  return make_float2(s, __fadd_rn(acc.y, err));
+}
+
+__device__ __forceinline__ float gwmax(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
+
+// A warp owns a 4 x 4 x 2 KP tile of lattice points, KP per lane (lane
+// (i, j, k0) holds k0, k0 + 2, ...).  The protein atoms that pass the box test
+// are staged in the warp's shared list (both float4 halves), so the
+// evaluation loop reads only shared memory (broadcast); the pair parameters of
+// the atom's type for the NE grid elements follow as NE / 2 float4.  The block
+// sums (compensated float pairs) live in shared memory: they change only at
+// block ends.
+constexpr int kGridWarps = 8;  // tiles per CTA
+
+template <int NE, int KP>
+constexpr int grid_smem_bytes() {
+  return kNTypes * ((NE + 1) / 2) * 16 + kGridWarps * kGridList * 32 +
+         kGridWarps * (NE + 1) * KP * 32 * (int)sizeof(float2);
+}
+
+// KP lattice points per lane (1 or 2): a warp tile of 4 x 4 x 2 KP points
+template <int DIEL, int NE, int KP, bool COUNT>
+__global__ void __launch_bounds__(kGridWarps * 32) k_grid_build(DevCull cull, GridBuild gb,
+                                                                 float* grids) {
+  constexpr int kGridPts = KP;
+  constexpr int NE2 = (NE + 1) / 2;
+  extern __shared__ __align__(16) float4 gsm[];
+  float4* s_el = gsm;                                  // [ptype][NE2] (X, 1/D) of 2 elements
+  float4* s_list = s_el + kNTypes * NE2;               // [warp][kGridList][2] staged atoms
+  float2* s_ad = reinterpret_cast<float2*>(s_list + kGridWarps * kGridList * 2);
+  for (int k = threadIdx.x; k < kNTypes * NE2; k += blockDim.x) {
+    const int pt = k / NE2, q = k % NE2;
+    const float2 a = gb.el[pt * kGridElems + 2 * q];
+    const float2 b = 2 * q + 1 < kGridElems ? gb.el[pt * kGridElems + 2 * q + 1]
+                                            : make_float2(0.f, 0.f);
+    s_el[k] = make_float4(a.x, a.y, b.x, b.y);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int tile = blockIdx.x * kGridWarps + w;
+  if (tile >= gb.ntiles) return;  // whole warps leave: no block-wide barrier follows
+  static_assert(kGridTileX == 4 && kGridTileY == 4, "lane layout of the tile");
+  const int3 t = gb.tiles[tile];
+  const int i = t.x * 4 + (lane & 3), j = t.y * 4 + ((lane >> 2) & 3);
+  int kk[kGridPts];
+  bool in_lattice[kGridPts], masked[kGridPts];
+  float xh[kGridPts], yh[kGridPts], zh[kGridPts], xl[kGridPts], yl[kGridPts], zl[kGridPts];
+  const float big = 1e30f;
+  float lox = big, loy = big, loz = big, hix = -big, hiy = -big, hiz = -big;
+#pragma unroll
+  for (int c = 0; c < kGridPts; ++c) {
+    kk[c] = t.z * (2 * KP) + (lane >> 4) + 2 * c;
+    in_lattice[c] = i < gb.nx && j < gb.ny && kk[c] < gb.nz;
+    // lattice point in the device frame, as a float pair
+    const double px = gb.o[0] + gb.step * i, py = gb.o[1] + gb.step * j,
+                 pz = gb.o[2] + gb.step * kk[c];
+    const double mx = px - gb.mc[0], my = py - gb.mc[1], mz = pz - gb.mc[2];
+    masked[c] = in_lattice[c] && mx * mx + my * my + mz * mz < gb.mr2;
+    xh[c] = (float)px;
+    yh[c] = (float)py;
+    zh[c] = (float)pz;
+    xl[c] = (float)(px - xh[c]);
+    yl[c] = (float)(py - yh[c]);
+    zl[c] = (float)(pz - zh[c]);
+    if (masked[c]) {
+      lox = fminf(lox, xh[c]);
+      loy = fminf(loy, yh[c]);
+      loz = fminf(loz, zh[c]);
+      hix = fmaxf(hix, xh[c]);
+      hiy = fmaxf(hiy, yh[c]);
+      hiz = fmaxf(hiz, zh[c]);
+    }
+  }
+  // the tile's box over its masked points
+  const float blx = gwmin(lox), bly = gwmin(loy), blz = gwmin(loz);
+  const float bhx = gwmax(hix), bhy = gwmax(hiy), bhz = gwmax(hiz);
+  // Sums in three levels: the atoms of one row in FP32 (af), the rows of one
+  // block of kGridFlushAtoms protein atoms in FP32 (bf), the blocks in
+  // compensated FP32 (s_ad: hi + lo pairs updated by TwoSum, about twice the
+  // FP32 precision, without the FP64 pipe).  Atoms the box test drops are beyond 12.04 A of every masked point
+  // of the tile, where the switched terms are exactly 0, and a row or block
+  // that is not visited adds exactly 0: each value is the same whatever the
+  // tile's box (and so the mask) is.
+  float2* ad = s_ad + (size_t)w * (NE + 1) * kGridPts * 32 + lane;  // [e][c] stride 32
+  float af[kGridPts][NE + 1], bf[kGridPts][NE + 1];
+#pragma unroll
+  for (int c = 0; c < kGridPts; ++c)
+#pragma unroll
+    for (int e = 0; e <= NE; ++e) {
+      af[c][e] = 0.f;
+      bf[c][e] = 0.f;
+      ad[(e * kGridPts + c) * 32] = make_float2(0.f, 0.f);
+    }
+  float4* wl = s_list + (size_t)w * kGridList * 2;
+  unsigned n_eval[kGridPts] = {}, n_near[kGridPts] = {};
+  auto evaluate = [&](int n) {
+    __syncwarp();
+    if (COUNT) {
+#pragma unroll
+      for (int c = 0; c < kGridPts; ++c) n_eval[c] += n;
+    }
+#pragma unroll 2
+    for (int v = 0; v < n; ++v) {
+      const float4 p = wl[2 * v], pl = wl[2 * v + 1];
+      // pl.w holds the bits of type * kNTypes * 16 (the pair table's row offset)
+      const float4* er = s_el + (__float_as_int(pl.w) / (16 * kNTypes)) * NE2;
+      float4 prm[NE2];
+#pragma unroll
+      for (int q = 0; q < NE2; ++q) prm[q] = er[q];
+#pragma unroll
+      for (int c = 0; c < kGridPts; ++c) {
+        const float dx = (xh[c] - p.x) + (xl[c] - pl.x);
+        const float dy = (yh[c] - p.y) + (yl[c] - pl.y);
+        const float dz = (zh[c] - p.z) + (zl[c] - pl.z);
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        if (COUNT) n_near[c] += r2 < kCut2;
+        const float r2c = fmaxf(r2, kMinR2);
+        const float ir = rsqrtf(r2c);
+        const float ir2 = ir * ir;
+        const float sw = fmaxf(fmaf(r2c, -1.0f / 144.0f, 1.0f), 0.0f);
+        const float ws = sw * sw;
+        af[c][NE] = fmaf(ws * p.w, DIEL == 0 ? ir : ir2, af[c][NE]);
+#pragma unroll
+        for (int e = 0; e < NE; ++e) {
+          // X = D^(1/3) x^2: q6 = (X / r^2)^3 = D (x/r)^6, and
+          // D ((x/r)^12 - 2 (x/r)^6) = q6 (q6 / D - 2)
+          const float X = (e & 1) ? prm[e / 2].z : prm[e / 2].x;
+          const float iD = (e & 1) ? prm[e / 2].w : prm[e / 2].y;
+          const float q2 = X * ir2;
+          const float q6 = (q2 * q2) * q2;
+          af[c][e] = fmaf(ws, q6 * fmaf(q6, iD, -2.0f), af[c][e]);
+        }
+      }
+    }
+    __syncwarp();
+  };
+  bool mine = false;
+#pragma unroll
+  for (int c = 0; c < kGridPts; ++c) mine = mine || masked[c];
+  const bool any = __any_sync(kFull, mine);
+  if (any) {
+    bool dirty = false;
+    for (int r = 0; r < cull.nrows; ++r) {
+      const int a = cull.row_start[r], b = cull.row_start[r + 1];
+      const float4 rb = cull.row_box[r];
+      const float ey = fmaxf(fmaxf(rb.x - bhy, bly - rb.y), 0.f);
+      const float ez = fmaxf(fmaxf(rb.z - bhz, blz - rb.w), 0.f);
+      if (fmaf(ey, ey, ez * ez) < kCullR2) {
+        int cnt = 0;
+        for (int i0 = a; i0 < b; i0 += 32) {
+          const int ia = i0 + lane;
+          bool in = false;
+          float4 ph = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (ia < b) {
+            ph = cull.atoms[2 * (size_t)ia];
+            const float ex = fmaxf(fmaxf(blx - ph.x, ph.x - bhx), 0.f);
+            const float fy = fmaxf(fmaxf(bly - ph.y, ph.y - bhy), 0.f);
+            const float fz = fmaxf(fmaxf(blz - ph.z, ph.z - bhz), 0.f);
+            in = fmaf(ex, ex, fmaf(fy, fy, fz * fz)) < kCullR2;
+          }
+          const unsigned m = __ballot_sync(kFull, in);
+          if (in) {
+            const int at = cnt + __popc(m & ((1u << lane) - 1u));
+            wl[2 * at] = ph;
+            wl[2 * at + 1] = cull.atoms[2 * (size_t)ia + 1];
+          }
+          cnt += __popc(m);
+          if (cnt >= 32) {
+            evaluate(cnt);
+            cnt = 0;
+          }
+        }
+        evaluate(cnt);
+#pragma unroll
+        for (int c = 0; c < kGridPts; ++c)
+#pragma unroll
+          for (int e = 0; e <= NE; ++e) {
+            bf[c][e] += af[c][e];
+            af[c][e] = 0.f;
+          }
+        dirty = true;
+      }
+      // the block ends where the atom index crosses a multiple of kGridFlushAtoms
+      if (dirty && (r + 1 == cull.nrows || (b - 1) / kGridFlushAtoms != b / kGridFlushAtoms)) {
+#pragma unroll
+        for (int c = 0; c < kGridPts; ++c)
+#pragma unroll
+          for (int e = 0; e <= NE; ++e) {
+            float2& acc = ad[(e * kGridPts + c) * 32];
+            acc = two_sum_add(acc, bf[c][e]);
+            bf[c][e] = 0.f;
+          }
+        dirty = false;
+      }
+    }
+  }
+  if (COUNT) {
+    unsigned long long ev = 0, cv = 0;
+#pragma unroll
+    for (int c = 0; c < kGridPts; ++c) {
+      ev += masked[c] ? n_eval[c] : 0u;
+      cv += masked[c] ? n_near[c] : 0u;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      ev += __shfl_xor_sync(kFull, ev, o);
+      cv += __shfl_xor_sync(kFull, cv, o);
+    }
+    if (lane == 0 && ev) {
+      atomicAdd(gb.pairs, ev);
+      atomicAdd(gb.pairs + 1, cv);
+    }
+  }
+  const size_t per = (size_t)gb.nx * gb.ny * gb.nz;
+#pragma unroll
+  for (int c = 0; c < kGridPts; ++c) {
+    if (!in_lattice[c]) continue;
+    const size_t idx = (size_t)i + (size_t)j * gb.nx + (size_t)kk[c] * gb.nx * gb.ny;
+    const float2 phi = ad[(NE * kGridPts + c) * 32];
+    for (int l = 0; l < gb.ntypes; ++l) {
+      float v = 0.f;
+      if (masked[c]) {
+        // q phi + V in float pairs: one rounding of the sum of the high parts,
+        // the low parts added to it
+        const float q = gb.type_qf[l];
+        const float2 vdw = ad[(gb.type_elem[l] * kGridPts + c) * 32];
+        const float e = fmaf(q, phi.x, vdw.x) + fmaf(q, phi.y, vdw.y);
+        v = e < gb.max_Ef ? e : gb.max_Ef;
+      }
+      grids[per * l + idx] = v;
+    }
+  }
+}
+
+// One thread per entry: E = trilin of the atom's type grid at the atom, and
+// dE/dx (the derivative of the trilinear form), into Epart / Gpart.
+template <bool GRAD>
+__global__ void k_grid_inter(GridLook g, const float4* __restrict__ X, int n, int L,
+                             const int* __restrict__ atom_type, const float* __restrict__ grids,
+                             double* Epart, float4* Gpart, int* status) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const float4 h = X[2 * (size_t)e], l = X[2 * (size_t)e + 1];
+  const double ux = ((double)h.x + (double)l.x - g.o[0]) * g.inv;
+  const double uy = ((double)h.y + (double)l.y - g.o[1]) * g.inv;
+  const double uz = ((double)h.z + (double)l.z - g.o[2]) * g.inv;
+  double E = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
+  // the low corner truncates toward zero (int_of_float); its high corner
+  // (int) u + 1 is on the lattice iff 0 <= u < n - 1, tested before the
+  // conversion (the reference does not check)
+  if (!(ux >= 0.0 && uy >= 0.0 && uz >= 0.0 && ux < g.nx - 1 && uy < g.ny - 1 &&
+        uz < g.nz - 1)) {
+    atomicOr(&status[e / L], kStatusOffGrid);
+  } else {
+    const int i0 = (int)ux, j0 = (int)uy, k0 = (int)uz;
+    const size_t nx = g.nx, nxy = (size_t)g.nx * g.ny;
+    const float* v = grids + (size_t)atom_type[e % L] * nxy * g.nz + i0 + j0 * nx + k0 * nxy;
+    const double a = v[0], b = v[1], c = v[1 + nx], d = v[nx];
+    const double ee = v[nxy], f = v[1 + nxy], gg = v[1 + nx + nxy], hh = v[nx + nxy];
+    const double wlx = ux - i0, wly = uy - j0, wlz = uz - k0;
+    const double whx = 1.0 - wlx, why = 1.0 - wly, whz = 1.0 - wlz;
+    E = a * (whx * why * whz) + b * (wlx * why * whz) + c * (wlx * wly * whz) +
+        d * (whx * wly * whz) + ee * (whx * why * wlz) + f * (wlx * why * wlz) +
+        gg * (wlx * wly * wlz) + hh * (whx * wly * wlz);
+    if (GRAD) {
+      gx = g.inv * ((b - a) * why * whz + (c - d) * wly * whz + (f - ee) * why * wlz +
+                    (gg - hh) * wly * wlz);
+      gy = g.inv * ((d - a) * whx * whz + (c - b) * wlx * whz + (hh - ee) * whx * wlz +
+                    (gg - f) * wlx * wlz);
+      gz = g.inv * ((ee - a) * whx * why + (f - b) * wlx * why + (gg - c) * wlx * wly +
+                    (hh - d) * whx * wly);
+    }
+  }
+  Epart[e] = E;
+  if (GRAD) Gpart[e] = make_float4((float)gx, (float)gy, (float)gz, 0.f);
+}
+
+}  // namespace
+
+namespace {
+template <int DIEL, int NE, int KP, bool COUNT>
+cudaError_t grid_build_as(const DevCull& cull, const GridBuild& gb, float* grids,
+                          cudaStream_t st) {
+  constexpr int smem = grid_smem_bytes<NE, KP>();
+  // the opt-in above 48 KB (per device: set on every launch)
+  const cudaError_t e = cudaFuncSetAttribute(k_grid_build<DIEL, NE, KP, COUNT>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  const int blocks = (gb.ntiles + kGridWarps - 1) / kGridWarps;
+  k_grid_build<DIEL, NE, KP, COUNT><<<blocks, kGridWarps * 32, smem, st>>>(cull, gb, grids);
+  return cudaGetLastError();
+}
+
+// NE = the number of grid elements exactly, so that no element slot is
+// evaluated in vain
+template <int DIEL, int KP, bool COUNT>
+cudaError_t grid_build_ne(const DevCull& cull, const GridBuild& gb, float* grids,
+                          cudaStream_t st) {
+  switch (gb.nelem) {
+    case 1: return grid_build_as<DIEL, 1, KP, COUNT>(cull, gb, grids, st);
+    case 2: return grid_build_as<DIEL, 2, KP, COUNT>(cull, gb, grids, st);
+    case 3: return grid_build_as<DIEL, 3, KP, COUNT>(cull, gb, grids, st);
+    case 4: return grid_build_as<DIEL, 4, KP, COUNT>(cull, gb, grids, st);
+    case 5: return grid_build_as<DIEL, 5, KP, COUNT>(cull, gb, grids, st);
+    case 6: return grid_build_as<DIEL, 6, KP, COUNT>(cull, gb, grids, st);
+    case 7: return grid_build_as<DIEL, 7, KP, COUNT>(cull, gb, grids, st);
+    case 8: return grid_build_as<DIEL, 8, KP, COUNT>(cull, gb, grids, st);
+    case 9: return grid_build_as<DIEL, 9, KP, COUNT>(cull, gb, grids, st);
+    case 10: return grid_build_as<DIEL, 10, KP, COUNT>(cull, gb, grids, st);
+    case 11: return grid_build_as<DIEL, 11, KP, COUNT>(cull, gb, grids, st);
+    default: return grid_build_as<DIEL, kGridElems, KP, COUNT>(cull, gb, grids, st);
+  }
+}
+
+// the counting variant (pair statistics) exists for one point per lane only
+template <int DIEL, bool COUNT>
+cudaError_t grid_build_kp(const DevCull& cull, const GridBuild& gb, float* grids,
+                          cudaStream_t st) {
+  if (COUNT && gb.kp != 1) return cudaErrorInvalidValue;
+  if (!COUNT && gb.kp == 2) return grid_build_ne<DIEL, 2, false>(cull, gb, grids, st);
+  return grid_build_ne<DIEL, 1, COUNT>(cull, gb, grids, st);
+}
+}  // namespace
+
+cudaError_t launch_grid_build(const DevCull& cull, const GridBuild& gb, int dielectric,
+                              float* grids, cudaStream_t st) {
+  if (gb.ntiles <= 0) return cudaSuccess;
+  if (gb.nelem < 1 || gb.nelem > kGridElems || (gb.kp != 1 && gb.kp != 2))
+    return cudaErrorInvalidValue;
+  const bool count = gb.pairs != nullptr;
+  if (dielectric)
+    return count ? grid_build_kp<1, true>(cull, gb, grids, st)
+                 : grid_build_kp<1, false>(cull, gb, grids, st);
+  return count ? grid_build_kp<0, true>(cull, gb, grids, st)
+               : grid_build_kp<0, false>(cull, gb, grids, st);
+}
+
+cudaError_t launch_grid_inter(const GridLook& g, const float4* X, int n, int L,
+                              const int* atom_type, const float* grids, double* Epart,
+                              float4* Gpart, int* status, int grad, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int blocks = (n + 255) / 256;
+  if (grad) k_grid_inter<true><<<blocks, 256, 0, st>>>(g, X, n, L, atom_type, grids, Epart, Gpart, status);
+  else k_grid_inter<false><<<blocks, 256, 0, st>>>(g, X, n, L, atom_type, grids, Epart, Gpart, status);
+  return cudaGetLastError();
+}
+
+}  // namespace mmo

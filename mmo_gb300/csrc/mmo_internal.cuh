@@ -96,7 +96,7 @@ struct PoseIO {
 };
 
 enum : int { kFlagInter = 1, kFlagIntra = 2, kFlagGrad = 4, kFlagRecenter = 8 };
-enum : int { kStatusTooLong = 1, kStatusNonFinite = 2 };
+enum : int { kStatusTooLong = 1, kStatusNonFinite = 2, kStatusOffGrid = 4 };
 enum : int { kErrTimeout = 1 };
 
 struct Physics {
@@ -264,6 +264,34 @@ struct MCParams {
   int B, nd, nrb;
 };
 
+// ---- precomputed interaction grids (kernels_grid.cu) --------------------
+// One float32 lattice per ligand atom type (element, charge), x fastest:
+// value[type][k][j][i] at the point o + step (i, j, k) of the device frame.
+constexpr int kGridElems = kNTypes;  // distinct ligand elements of one set of grids
+constexpr int kGridTileX = 4, kGridTileY = 4;  // lattice points per warp tile along x, y
+                                                // (2 kp along z)
+
+struct GridBuild {
+  const int3* tiles;       // [ntiles] 4 x 4 x 2 kp point tiles that meet the mask sphere
+  const float* type_qf;    // [ntypes] charge of each grid type
+  const int* type_elem;    // [ntypes] rank of the type's element among the grid elements
+  int ntiles, ntypes, nelem;
+  int kp;                  // lattice points per lane: 1 or 2
+  int nx, ny, nz;
+  double o[3], step;       // lattice point (0, 0, 0) in the device frame, spacing
+  double mc[3], mr2;       // mask sphere (device frame); points outside hold 0
+  float max_Ef;            // cap of every value (rounded to float, as the values are)
+  float2 el[kNTypes * kGridElems];  // [protein type][grid element] (D^(1/3) x^2, 1/D)
+                                    // (1/D := 0 when D = 0)
+  unsigned long long* pairs;  // [2] (point, atom) pairs evaluated for masked points, and
+                              // those within 12 A (may be null)
+};
+
+struct GridLook {
+  double o[3], inv;        // lattice origin (device frame), 1 / step
+  int nx, ny, nz;
+};
+
 // ---- launchers (defined in the .cu files) --------------------------------
 cudaError_t launch_k_mc_init(const MCDev& s, const MCParams& p, cudaStream_t st);
 cudaError_t launch_k_mc_start(const MCDev& s, const MCParams& p, cudaStream_t st);
@@ -311,6 +339,11 @@ cudaError_t launch_pairs_cull(const DevCull& cull, const float4* tab, const Cull
                               const CullPlan& plan, int* d_err, cudaStream_t st);
 int cull_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_bytes);
 int cull_smem_bytes(int P, int nrows, int npieces, int threads);
+cudaError_t launch_grid_build(const DevCull& cull, const GridBuild& gb, int dielectric,
+                              float* grids, cudaStream_t st);
+cudaError_t launch_grid_inter(const GridLook& g, const float4* X, int n, int L,
+                              const int* atom_type, const float* grids, double* Epart,
+                              float4* Gpart, int* status, int grad, cudaStream_t st);
 cudaError_t launch_fma_peak(int sms, int iters, float* out, cudaStream_t st, double* flops);
 
 // ---- device helpers ------------------------------------------------------

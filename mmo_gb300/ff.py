@@ -260,12 +260,79 @@ class UFFScorer:
         self._check(self._lib.mmo_ene_intra(self._h, _dp(x), _dp(y), _dp(z), C.byref(out)))
         return out.value
 
+    # -- precomputed interaction grids (include/mmo_grid.h) ----------------
+    def _grid_spec(self, step, dims, origin, types, mask_center=None, mask_radius=0.0,
+                   max_E=1e5):
+        ta = np.ascontiguousarray([t[0] for t in types], np.int32)
+        tq = np.ascontiguousarray([t[1] for t in types], np.float64)
+        sp = _L.GridSpec()
+        sp.step = float(step)
+        sp.nx, sp.ny, sp.nz = (int(v) for v in dims)
+        sp.origin[:] = [float(v) for v in origin]
+        sp.mask_center[:] = [float(v) for v in (mask_center if mask_center is not None
+                                                else (0.0, 0.0, 0.0))]
+        sp.mask_radius = float(mask_radius)
+        sp.max_E = float(max_E)
+        sp.ntypes = len(ta)
+        sp.type_anum = ta.ctypes.data
+        sp.type_q = tq.ctypes.data
+        return sp, (ta, tq)  # the arrays must outlive the call
+
+    def build_grids(self, step, dims, origin, types, mask_center=None, mask_radius=0.0,
+                    max_E=1e5) -> float:
+        """Lds.pre_calculate_FF_components_grid (src/lds.ml:452-469) on the GPU
+        for the protein of set_protein: types is a list of (anum, charge);
+        returns the build kernel's milliseconds."""
+        sp, keep = self._grid_spec(step, dims, origin, types, mask_center, mask_radius, max_E)
+        ms = C.c_double()
+        self._check(self._lib.mmo_build_grids(self._h, C.byref(sp), C.byref(ms)))
+        del keep
+        return ms.value
+
+    def set_grid_build(self, points_per_lane: int = 0) -> None:
+        """Launch shape of the grid build (1 or 2 lattice points per lane, 0 automatic)."""
+        self._check(self._lib.mmo_set_grid_build(self._h, points_per_lane))
+
+    def load_grids(self, step, dims, origin, types, values) -> None:
+        """Grids computed elsewhere: values float32 [ntypes, nz, ny, nx]."""
+        v = np.ascontiguousarray(values, np.float32)
+        nx, ny, nz = (int(d) for d in dims)
+        if v.size != len(types) * nx * ny * nz:
+            raise ValueError("values must hold ntypes * nz * ny * nx floats")
+        sp, keep = self._grid_spec(step, dims, origin, types)
+        self._check(self._lib.mmo_load_grids(self._h, C.byref(sp),
+                                             v.ctypes.data_as(C.POINTER(C.c_float))))
+        del keep
+
+    def grid_values(self) -> np.ndarray:
+        """The context's grids, float32 [ntypes, nz, ny, nx]."""
+        nt, nx, ny, nz = (C.c_int() for _ in range(4))
+        self._check(self._lib.mmo_grid_dims(self._h, C.byref(nt), C.byref(nx), C.byref(ny),
+                                            C.byref(nz)))
+        out = np.zeros((nt.value, nz.value, ny.value, nx.value), np.float32)
+        self._check(self._lib.mmo_grid_values(self._h, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def grid_build_stats(self) -> dict:
+        """Masked points and (point, protein atom) pair counts of the last build."""
+        v = [C.c_double() for _ in range(3)]
+        self._check(self._lib.mmo_grid_build_stats(self._h, *(C.byref(x) for x in v)))
+        return {"points": v[0].value, "pairs_evaluated": v[1].value,
+                "pairs_within_cutoff": v[2].value}
+
+    def grid_atom_types(self) -> np.ndarray:
+        """Grid type of each ligand atom (Mol.get_typ)."""
+        out = np.zeros(self.ligand.n, np.int32)
+        self._check(self._lib.mmo_grid_atom_types(self._h, _ip(out)))
+        return out
+
     # -- batched poses -----------------------------------------------------
-    def score_poses(self, dofs, inter=True, intra=True, grad=False, recenter=False):
+    def score_poses(self, dofs, inter=True, intra=True, grad=False, recenter=False, grid=False):
         """E (float64 [B]), grad (float32 [B, 6+nrb] or None), status (int32 [B]).
 
         dofs: float32 [B, 6 + nrb] in the Optim.config layout
-        [x, y, z, a, b, g, tau_0 ...] (src/optim.ml:19-22)."""
+        [x, y, z, a, b, g, tau_0 ...] (src/optim.ml:19-22); grid: the inter
+        term interpolated from the grids of build_grids / load_grids."""
         dofs = np.ascontiguousarray(dofs, np.float32)
         if dofs.ndim == 1:
             dofs = dofs[None, :]
@@ -273,7 +340,8 @@ class UFFScorer:
         if self.ligand is None or nd != 6 + self.ligand.nrb:
             raise ValueError("dofs must be [B, 6 + nrb] for the ligand of set_ligand")
         flags = ((_L.F_INTER if inter else 0) | (_L.F_INTRA if intra else 0) |
-                 (_L.F_GRAD if grad else 0) | (_L.F_RECENTER if recenter else 0))
+                 (_L.F_GRAD if grad else 0) | (_L.F_RECENTER if recenter else 0) |
+                 (_L.F_GRID if grid else 0))
         E = np.zeros(B, np.float64)
         G = np.zeros((B, nd), np.float32) if grad else None
         st = np.zeros(B, np.int32)

@@ -16,8 +16,8 @@ DIEL_CONST, DIEL_DIST = 0, 1
 MIX_GEOMEAN, MIX_LB = 0, 1
 INTER_SHIFTED, INTER_GLOBAL = 0, 1
 INTRA_PLAIN, INTRA_SHIFTED = 0, 1
-F_INTER, F_INTRA, F_GRAD, F_RECENTER = 1, 2, 4, 8
-S_TOO_LONG, S_NONFINITE = 1, 2
+F_INTER, F_INTRA, F_GRAD, F_RECENTER, F_GRID = 1, 2, 4, 8, 16
+S_TOO_LONG, S_NONFINITE, S_OFF_GRID = 1, 2, 4
 
 MC_UNIFORM, MC_GAUSSIAN = 0, 1
 
@@ -27,7 +27,16 @@ class MCParams(C.Structure):
     _fields_ = [("kT", C.c_double), ("rot_step", C.c_double), ("trans_step", C.c_double),
                 ("tors_step", C.c_double), ("move_law", C.c_int), ("adapt", C.c_int),
                 ("flip_every", C.c_int), ("minimize_every", C.c_int),
-                ("minimize_iters", C.c_int), ("gd_step", C.c_double), ("seed", C.c_ulonglong)]
+                ("minimize_iters", C.c_int), ("gd_step", C.c_double), ("seed", C.c_ulonglong),
+                ("use_grid", C.c_int)]
+
+
+class GridSpec(C.Structure):
+    """mmo_grid_spec of include/mmo_grid.h."""
+    _fields_ = [("step", C.c_double), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("origin", C.c_double * 3), ("mask_center", C.c_double * 3),
+                ("mask_radius", C.c_double), ("max_E", C.c_double), ("ntypes", C.c_int),
+                ("type_anum", C.c_void_p), ("type_q", C.c_void_p)]
 
 
 class MCState(C.Structure):
@@ -83,6 +92,14 @@ SIGNATURES = {
     "mmo_pair_count": (_i, [_vp, _P(C.c_double), _P(C.c_double)]),
     "mmo_last_launches": (_i, [_vp, _P(C.c_int)]),
     "mmo_fp32_fma_peak": (_i, [_vp, _P(_d), _P(_d)]),
+    "mmo_build_grids": (_i, [_vp, _P(GridSpec), _P(_d)]),
+    "mmo_load_grids": (_i, [_vp, _P(GridSpec), _P(C.c_float)]),
+    "mmo_set_grid_build": (_i, [_vp, _i]),
+    "mmo_grid_values": (_i, [_vp, _P(C.c_float)]),
+    "mmo_grid_dims": (_i, [_vp, _P(_i), _P(_i), _P(_i), _P(_i)]),
+    "mmo_grid_device": (_i, [_vp, _P(_vp)]),
+    "mmo_grid_atom_types": (_i, [_vp, _P(_i)]),
+    "mmo_grid_build_stats": (_i, [_vp, _P(_d), _P(_d), _P(_d)]),
 }
 
 

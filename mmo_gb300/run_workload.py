@@ -29,12 +29,33 @@ def main(argv=None) -> int:
     ap.add_argument("--row-spacing", type=float, default=0.0)
     ap.add_argument("--dielectric", type=int, default=0)
     ap.add_argument("--energy-only", action="store_true")
+    ap.add_argument("--grid-margin", type=float, default=None,
+                    help="build the per-type grids (0.5 A lattice over the protein's box plus "
+                         "this margin, mask sphere of 34 A) --repeat times, then score the poses "
+                         "from them")
+    ap.add_argument("--grid-kp", type=int, default=0, help="lattice points per lane (1, 2)")
     args = ap.parse_args(argv)
 
     s = synth.pose_batch(n_poses=args.poses, seed=1)
     sc = UFFScorer(0, Physics(args.dielectric, 0, 0, 0))
     sc.set_protein(s.pocket)
     sc.set_ligand(s.ligand)
+    if args.grid_margin is not None:
+        from . import grids as GR
+
+        types, _ = GR.type2id([s.ligand])
+        sc.set_grid_build(args.grid_kp)
+        p = s.pocket.xyz()
+        origin, dims = GR.lattice_from_box(GR.GRID_STEP, p.min(axis=0) - args.grid_margin,
+                                           p.max(axis=0) + args.grid_margin)
+        ms = [sc.build_grids(GR.GRID_STEP, dims, origin, types, mask_center=(0.0, 0.0, 0.0),
+                             mask_radius=GR.roi_mask_radius(10.0)) for _ in range(args.repeat)]
+        E, G, st = sc.score_poses(s.poses, grad=not args.energy_only, grid=True)
+        print("grids %s x %d types  build ms %s  E[0] %.6e  status bits %d" %
+              (dims, len(types), " ".join("%.3f" % m for m in ms), E[0],
+               int(np.count_nonzero(st))))
+        sc.close()
+        return 0
     if args.sweep == "cut-off":
         sc.set_cull(0, args.row_spacing, args.piece, args.per_lane)
         sc.set_tiles(0, args.threads, 0)

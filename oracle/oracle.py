@@ -76,6 +76,12 @@ def lib():
                                       P(i)]),
             "orc_score_batch": (v, [P(Physics), P(CMol), P(CLigand), i, P(C.c_float), i, i,
                                     P(d), i, i, P(d), P(d), P(i)]),
+            "orc_grid_point": (v, [P(Physics), P(CMol), P(d), i, P(i), P(d), d, P(d)]),
+            "orc_grid_points": (v, [P(Physics), P(CMol), i, P(d), i, P(i), P(d), d, i, P(d),
+                                    P(d)]),
+            "orc_trilin": (d, [d, i, i, i, P(C.c_float), P(d), P(i)]),
+            "orc_ene_inter_interp": (d, [d, i, i, i, P(C.c_float), i, P(d), P(d), P(d), P(i),
+                                         P(i)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -267,13 +273,28 @@ def grid_point(prot, p, type_anum, type_q, max_E=100000.0, ph=REF):
     return out
 
 
+def grid_points(prot, pts, type_anum, type_q, max_E=100000.0, nthreads=1, ph=REF,
+                with_scale=False):
+    """grid_point at many points (cell list, threads): float64 [n, ntypes]
+    (and the sum of |pair terms| of each value with with_scale)."""
+    P = OMol.of(prot)
+    ta = np.ascontiguousarray(type_anum, np.int32)
+    tq = np.ascontiguousarray(type_q, np.float64)
+    pp = np.ascontiguousarray(pts, np.float64).reshape(-1, 3)
+    out = np.zeros((len(pp), len(ta)))
+    sc = np.zeros_like(out) if with_scale else None
+    lib().orc_grid_points(C.byref(ph), C.byref(P.c), len(pp), _dp(pp), len(ta), _ip(ta),
+                          _dp(tq), C.c_double(max_E), int(nthreads), _dp(out),
+                          _dp(sc) if sc is not None else None)
+    return (out, sc) if with_scale else out
+
+
 def trilin(step, dims, values, p):
     """G3D.trilin on float32 values [nz][ny][nx] (x fastest); (value, off-lattice)."""
     v = np.ascontiguousarray(values, np.float32)
     pp = np.ascontiguousarray(p, np.float64)
     off = C.c_int(0)
     f = lib().orc_trilin
-    f.restype = C.c_double
     e = f(C.c_double(step), dims[0], dims[1], dims[2], v.ctypes.data_as(C.POINTER(C.c_float)),
           _dp(pp), C.byref(off))
     return e, bool(off.value)
@@ -288,7 +309,6 @@ def ene_inter_interp(step, dims, grids, xyz, types):
     t = np.ascontiguousarray(types, np.int32)
     off = C.c_int(0)
     f = lib().orc_ene_inter_interp
-    f.restype = C.c_double
     e = f(C.c_double(step), dims[0], dims[1], dims[2], g.ctypes.data_as(C.POINTER(C.c_float)),
           len(t), _dp(x), _dp(y), _dp(z), _ip(t), C.byref(off))
     return e, bool(off.value)

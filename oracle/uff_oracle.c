@@ -753,12 +753,15 @@ void orc_grid_point(const orc_physics *ph, const orc_mol *prot, const double p[3
 double orc_trilin(double step, int nx, int ny, int nz, const float *v, const double p[3],
                   int *off) {
   const double inv = 1.0 / step;
-  const int i0 = (int)(p[0] * inv), j0 = (int)(p[1] * inv), k0 = (int)(p[2] * inv);
-  const int i1 = i0 + 1, j1 = j0 + 1, k1 = k0 + 1;
-  if (p[0] < 0 || p[1] < 0 || p[2] < 0 || i1 >= nx || j1 >= ny || k1 >= nz) {
+  const double ux = p[0] * inv, uy = p[1] * inv, uz = p[2] * inv;
+  /* the high corner (int) u + 1 is on the lattice iff 0 <= u < n - 1 (tested
+   * before the conversion, which is undefined for huge u) */
+  if (!(ux >= 0 && uy >= 0 && uz >= 0 && ux < nx - 1 && uy < ny - 1 && uz < nz - 1)) {
     if (off) *off = 1;
     return 0.0;
   }
+  const int i0 = (int)ux, j0 = (int)uy, k0 = (int)uz;
+  const int i1 = i0 + 1, j1 = j0 + 1, k1 = k0 + 1;
   const long j0x = (long)j0 * nx, j1x = (long)j1 * nx, k0xy = (long)k0 * nx * ny,
              k1xy = (long)k1 * nx * ny;
   const double wlx = (p[0] - i0 * step) * inv, wly = (p[1] - j0 * step) * inv,
@@ -783,4 +786,103 @@ double orc_ene_inter_interp(double step, int nx, int ny, int nz, const float *gr
     e += orc_trilin(step, nx, ny, nz, grids + per * type[j], p, off);
   }
   return e;
+}
+
+/* orc_grid_point at n points (pts[n][3]) into out[n][ntypes] through the cell
+ * list (scale, if not NULL: the sum of |pair terms| of each value), with the factorisation of Mol.ene_inter_UFF_shifted_grid
+ * (src/mol.ml:964-989): the point's neighbours within 12 A once, then every
+ * type; pair parameters looked up per (type, protein element).  nthreads
+ * POSIX threads over the points. */
+typedef struct {
+  const orc_physics *ph;
+  const orc_cells *cells;
+  const double *pts;
+  int p0, p1, ntypes;
+  const double *type_q;
+  const double *xt, *dt; /* [ntypes][128] x_ij, D_ij by protein atomic number */
+  double max_E;
+  double *out, *scale;
+} grid_job;
+
+static void *grid_worker(void *arg) {
+  grid_job *J = (grid_job *)arg;
+  const orc_cells *c = J->cells;
+  const orc_mol *prot = &c->prot;
+  const int nt = J->ntypes;
+  double *se = (double *)malloc(sizeof(double) * 3 * (size_t)nt);
+  double *sv = se + nt, *sa = sv + nt;
+  for (int k = J->p0; k < J->p1; ++k) {
+    const double *p = J->pts + 3 * (size_t)k;
+    for (int l = 0; l < nt; ++l) se[l] = sv[l] = sa[l] = 0.0;
+    const int cx = (int)floor((p[0] - c->lo[0]) / CUTOFF);
+    const int cy = (int)floor((p[1] - c->lo[1]) / CUTOFF);
+    const int cz = (int)floor((p[2] - c->lo[2]) / CUTOFF);
+    for (int gz = cz - 1; gz <= cz + 1; ++gz) {
+      if (gz < 0 || gz >= c->dim[2]) continue;
+      for (int gy = cy - 1; gy <= cy + 1; ++gy) {
+        if (gy < 0 || gy >= c->dim[1]) continue;
+        for (int gx = cx - 1; gx <= cx + 1; ++gx) {
+          if (gx < 0 || gx >= c->dim[0]) continue;
+          const int cell = (gz * c->dim[1] + gy) * c->dim[0] + gx;
+          for (int m = c->start[cell]; m < c->start[cell + 1]; ++m) {
+            const int i = c->idx[m];
+            const double dx = p[0] - prot->x[i], dy = p[1] - prot->y[i], dz = p[2] - prot->z[i];
+            const double d2 = dx * dx + dy * dy + dz * dz;
+            if (!(d2 < 144.0)) continue;
+            const double r = orc_non_zero_dist(sqrt(d2));
+            const double w = orc_shift_12A(r);
+            const double qr = prot->q[i] / (J->ph->dielectric ? r * r : r);
+            const int an = prot->anum[i] & 127;
+            for (int l = 0; l < nt; ++l) {
+              const double p1 = J->xt[l * 128 + an] / r, p2 = p1 * p1, p6 = p2 * p2 * p2;
+              const double el = w * (qr * J->type_q[l]);
+              const double vd = w * (J->dt[l * 128 + an] * ((-2.0 * p6) + (p6 * p6)));
+              se[l] += el;
+              sv[l] += vd;
+              if (J->scale) sa[l] += orc_elec_weight() * fabs(el) + fabs(vd);
+            }
+          }
+        }
+      }
+    }
+    for (int l = 0; l < nt; ++l) {
+      const double e = orc_elec_weight() * se[l] + sv[l];
+      J->out[(size_t)k * nt + l] = e < J->max_E ? e : J->max_E;
+      if (J->scale) J->scale[(size_t)k * nt + l] = sa[l];
+    }
+  }
+  free(se);
+  return NULL;
+}
+
+void orc_grid_points(const orc_physics *ph, const orc_mol *prot, int n, const double *pts,
+                     int ntypes, const int *type_anum, const double *type_q, double max_E,
+                     int nthreads, double *out, double *scale) {
+  orc_cells *cells = orc_cells_build(prot);
+  double *xt = (double *)calloc((size_t)ntypes * 256, sizeof(double));
+  double *dt = xt + (size_t)ntypes * 128;
+  for (int l = 0; l < ntypes; ++l)
+    for (int i = 0; i < prot->n; ++i) {
+      const int an = prot->anum[i] & 127;
+      orc_pair_params(ph, type_anum[l], prot->anum[i], &xt[l * 128 + an], &dt[l * 128 + an]);
+    }
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > n) nthreads = n > 0 ? n : 1;
+  pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+  grid_job *jobs = (grid_job *)malloc(sizeof(grid_job) * nthreads);
+  for (int t = 0; t < nthreads; ++t) {
+    grid_job J = {ph, cells, pts, (int)((long)n * t / nthreads),
+                  (int)((long)n * (t + 1) / nthreads), ntypes, type_q, xt, dt, max_E, out, scale};
+    jobs[t] = J;
+    if (nthreads == 1)
+      grid_worker(&jobs[t]);
+    else
+      pthread_create(&th[t], NULL, grid_worker, &jobs[t]);
+  }
+  if (nthreads > 1)
+    for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+  free(jobs);
+  free(th);
+  free(xt);
+  orc_cells_free(cells);
 }

@@ -133,6 +133,9 @@ void orc_grid_point(const orc_physics *ph, const orc_mol *prot, const double p[3
                     const int *type_anum, const double *type_q, double max_E, double *out);
 double orc_trilin(double step, int nx, int ny, int nz, const float *v, const double p[3],
                   int *off);
+void orc_grid_points(const orc_physics *ph, const orc_mol *prot, int n, const double *pts,
+                     int ntypes, const int *type_anum, const double *type_q, double max_E,
+                     int nthreads, double *out, double *scale);
 double orc_ene_inter_interp(double step, int nx, int ny, int nz, const float *grids, int n,
                             const double *x, const double *y, const double *z, const int *type,
                             int *off);

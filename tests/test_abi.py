@@ -47,6 +47,13 @@ def test_null_context_is_rejected(gpu_lib):
     assert gpu_lib.mmo_ctx_create(0, None) == lib.EINVAL
     assert gpu_lib.mmo_mc_run(None, 1, 1, None, None, None, 1) == lib.EINVAL
     assert gpu_lib.mmo_tune(None, 1, None, 0, None, None, None, None, None) == lib.EINVAL
+    assert gpu_lib.mmo_build_grids(None, None, None) == lib.EINVAL
+    assert gpu_lib.mmo_load_grids(None, None, None) == lib.EINVAL
+    assert gpu_lib.mmo_set_grid_build(None, 1) == lib.EINVAL
+    assert gpu_lib.mmo_grid_values(None, None) == lib.EINVAL
+    assert gpu_lib.mmo_grid_dims(None, None, None, None, None) == lib.EINVAL
+    assert gpu_lib.mmo_grid_device(None, None) == lib.EINVAL
+    assert gpu_lib.mmo_grid_atom_types(None, None) == lib.EINVAL
 
 
 def test_create_without_gpu_fails_cleanly(gpu_lib):

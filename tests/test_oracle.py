@@ -280,3 +280,22 @@ def test_trilin_reproduces_linear_functions(oracle):
         assert abs(e - (1.5 + 0.25 * p[0] - 0.5 * p[1] + 2.0 * p[2])) < 1e-5
     assert oracle.trilin(step, dims, v, [-0.1, 0.0, 0.0])[1]
     assert oracle.trilin(step, dims, v, [0.0, 0.0, (dims[2] - 1) * step])[1]
+
+
+def test_grid_points_cells_equal_brute_grid_point(oracle):
+    """The threaded cell-list sum (the CPU baseline of the grid build) against
+    the brute per-point sum, at points inside, at the edge of and outside the
+    protein's box."""
+    from mmo_gb300 import synth
+
+    rng = np.random.default_rng(4)
+    prot = synth.random_pocket(rng, 800, 12.0)
+    ta = np.array([6, 8, 7, 1], np.int32)
+    tq = np.array([0.1, -0.4, 0.0, 0.25])
+    pts = rng.uniform(-25.0, 25.0, size=(40, 3))
+    pts[:5] = prot.xyz()[:5] + 0.05  # near atoms: capped values
+    got = oracle.grid_points(prot, pts, ta, tq, nthreads=3)
+    for k, p in enumerate(pts):
+        ref = oracle.grid_point(prot, p, ta, tq)
+        assert np.allclose(got[k], ref, rtol=1e-12, atol=1e-10)
+    assert np.any(got == 100000.0) and np.any(got == 0.0)
