@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmmo_gpu.so")
-SOURCES = ["capi.cu", "kernels_pairs.cu", "kernels_cull.cu", "kernels_pose.cu", "kernels_mc.cu", "kernels_grid.cu", "diag.cu"]
+SOURCES = ["capi.cu", "kernels_pairs.cu", "kernels_cull.cu", "kernels_pose.cu", "kernels_mc.cu", "kernels_grid.cu", "kernels_dock.cu", "diag.cu"]
 HEADERS = ["mmo_internal.cuh", os.path.join("..", "..", "include", "mmo_gpu.h"),
            os.path.join("..", "..", "include", "mmo_diag.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -14,6 +14,7 @@
 
 #include "../../include/mmo_diag.h"
 #include "../../include/mmo_gpu.h"
+#include "../../include/mmo_dock.h"
 #include "../../include/mmo_grid.h"
 #include "../../include/mmo_mc.h"
 #include "../../include/mmo_systems.h"
@@ -177,6 +178,24 @@ struct mmo_ctx {
   std::string grid_map_err = "no grids: call mmo_build_grids or mmo_load_grids first";
   double grid_stats[3] = {0, 0, 0};   // last build: masked points, pairs evaluated, within 12 A
   int grid_kp_set = 0;                // lattice points per lane of the build kernel, 0: automatic
+
+  // protein masks on the grids' lattice (mmo_build_masks / mmo_load_masks),
+  // ligand radii, desolvation contributions, docking and placement scratch
+  std::vector<int> cull_perm;         // row position -> mmo_set_protein index
+  bool masks_ok = false;
+  uint8_t* d_vdw = nullptr;           // [points]
+  uint8_t* d_shell = nullptr;         // [points]
+  size_t cap_vdw = 0, cap_shell = 0;
+  bool desolv_ok = false;
+  double* d_desolv = nullptr;         // [points] Lds.protein_desolv
+  size_t cap_desolv = 0;
+  std::vector<double> lradius;        // ligand atom radii (mmo_set_ligand_radii)
+  double* d_lradius = nullptr;
+  size_t cap_lradius = 0;
+  void* d_dock = nullptr;             // docking tables and candidates
+  size_t cap_dock = 0;
+  int* d_clash = nullptr;             // per-pose scratch status
+  size_t cap_clash = 0;
 
   // host-API staging
   char* h_in = nullptr;
@@ -541,6 +560,15 @@ int grid_take_spec(mmo_ctx* ctx, const char* who, const mmo_grid_spec* sp, bool 
     if (!std::isfinite(sp->type_q[l]))
       return fail(ctx, MMO_EINVAL, "%s: type %d: non-finite charge", who, l);
   }
+  const bool same_lattice = ctx->grid_ok && ctx->grid_step == sp->step &&
+                            ctx->grid_n[0] == n[0] && ctx->grid_n[1] == n[1] &&
+                            ctx->grid_n[2] == n[2] && ctx->grid_origin[0] == sp->origin[0] &&
+                            ctx->grid_origin[1] == sp->origin[1] &&
+                            ctx->grid_origin[2] == sp->origin[2];
+  if (!same_lattice) {  // masks live on the grids' lattice
+    ctx->masks_ok = false;
+    ctx->desolv_ok = false;
+  }
   ctx->grid_ok = false;
   ctx->grid_map_ok = false;
   ctx->grid_map_err = "no grids: call mmo_build_grids or mmo_load_grids first";
@@ -559,6 +587,24 @@ int grid_take_spec(mmo_ctx* ctx, const char* who, const mmo_grid_spec* sp, bool 
   return MMO_OK;
 }
 
+// Ptable.vdW_radii (src/ptable.ml:41-53); NaN for elements it lacks
+double vdw_radius(int anum) {
+  switch (anum) {
+    case 1: return 1.2;
+    case 6: return 1.7;
+    case 7: return 1.6;
+    case 8: return 1.55;
+    case 9: return 1.5;
+    case 12: return 2.2;
+    case 15: return 1.95;
+    case 16: return 1.8;
+    case 17: return 1.8;
+    case 35: return 1.9;
+    case 53: return 2.1;
+    default: return NAN;
+  }
+}
+
 // the lattice of the context's grids in the device frame
 GridLook grid_look(const mmo_ctx* ctx) {
   GridLook g{};
@@ -572,6 +618,7 @@ GridLook grid_look(const mmo_ctx* ctx) {
 
 struct RowIndex {
   std::vector<float4> atoms;    // [n][2]
+  std::vector<int> perm;        // [n] row position -> input index
   std::vector<int> rs;          // [nrows + 1]
   std::vector<float4> rbox;     // [nrows]
   std::vector<int> flush_end;   // [nrows]
@@ -619,6 +666,7 @@ void build_rows(int n, const double* px, const double* py, const double* pz, con
     return a < b;
   });
   R.atoms.assign(2 * (size_t)n, make_float4(0.f, 0.f, 0.f, 0.f));
+  R.perm = idx;
   R.rs.clear();
   R.rbox.clear();
   std::vector<int> rflush;
@@ -713,6 +761,9 @@ int build_cull(mmo_ctx* ctx) {
   c.ginv = (float)kCullGrid / side;
   ctx->cull = c;
   ctx->cull_rows = R.rs;
+  ctx->cull_perm = R.perm;
+  ctx->masks_ok = false;  // built on the old protein
+  ctx->desolv_ok = false;
   ++ctx->cull_version;
   ++ctx->epoch;
   // the sweep keeps the whole protein and its index in shared memory
@@ -1465,6 +1516,12 @@ int mmo_ctx_destroy(mmo_ctx* ctx) {
   cudaFree(ctx->d_mc);
   cudaFree(ctx->d_grid);
   cudaFree(ctx->d_grid_lt);
+  cudaFree(ctx->d_vdw);
+  cudaFree(ctx->d_shell);
+  cudaFree(ctx->d_desolv);
+  cudaFree(ctx->d_lradius);
+  cudaFree(ctx->d_dock);
+  cudaFree(ctx->d_clash);
   sys_free(ctx->sys);
   if (ctx->mc_exec) cudaGraphExecDestroy(ctx->mc_exec);
   for (auto& e : ctx->mc_ev)
@@ -2625,6 +2682,572 @@ int mmo_grid_atom_types(mmo_ctx* ctx, int* out) {
   if (!out) return fail(ctx, MMO_EINVAL, "mmo_grid_atom_types: out is NULL");
   if (!ctx->grid_map_ok) return fail(ctx, MMO_EINVAL, "%s", ctx->grid_map_err.c_str());
   std::copy(ctx->grid_lt.begin(), ctx->grid_lt.end(), out);
+  return MMO_OK;
+}
+
+// ---- protein masks, clash filters, docking, placement, desolvation ----------
+namespace {
+
+ClashArgs clash_args(const mmo_ctx* ctx, int tests) {
+  ClashArgs ca{};
+  ca.g = grid_look(ctx);
+  ca.vdw = ctx->masks_ok ? ctx->d_vdw : nullptr;
+  ca.tests = tests;
+  for (int a = 0; a < kNTypes; ++a) {
+    ca.heavy[a] = kUff[a].anum > 1;
+    for (int b = 0; b < kNTypes; ++b) {
+      // Ptable.vdW_clash_params2 (src/ptable.ml:62-80): (0.8 (r_i + r_j))^2
+      const double x = 0.8 * (vdw_radius(kUff[a].anum) + vdw_radius(kUff[b].anum));
+      ca.clash2[a * kNTypes + b] = (float)(x * x);
+    }
+  }
+  return ca;
+}
+
+size_t lattice_points(const mmo_ctx* ctx) {
+  return (size_t)ctx->grid_n[0] * ctx->grid_n[1] * ctx->grid_n[2];
+}
+
+// posed coordinates of B poses into the scratch (the rebuild kernel only)
+int pose_only(mmo_ctx* ctx, int B, const float* d_dofs, int flags, int* d_status,
+              cudaStream_t st) {
+  int r;
+  if ((r = ensure_scratch(ctx, B, ctx->lig.L, 1, false))) return r;
+  PoseIO io{};
+  io.dofs = d_dofs;
+  io.status = d_status;
+  io.err = ctx->d_err;
+  io.zero_err = 0;
+  io.B = B;
+  io.ox = ctx->origin_f[0];
+  io.oy = ctx->origin_f[1];
+  io.oz = ctx->origin_f[2];
+  MMO_CK(launch_rebuild(ctx->lig, io, ctx->scr, flags & kFlagRecenter, st), "rebuild kernel");
+  return MMO_OK;
+}
+
+}  // namespace
+
+int mmo_build_masks(mmo_ctx* ctx, const double* radius, double r_water) {
+  if (!ctx) return MMO_EINVAL;
+  if (ctx->prot.P <= 0 || !ctx->d_cull)
+    return fail(ctx, MMO_ESTATE, "mmo_build_masks: no protein: call mmo_set_protein first");
+  if (!ctx->grid_ok)
+    return fail(ctx, MMO_ESTATE, "mmo_build_masks: no lattice: build or load the grids first");
+  if (!radius || !(r_water >= 0) || !std::isfinite(r_water))
+    return fail(ctx, MMO_EINVAL, "mmo_build_masks: bad arguments");
+  const int P = ctx->prot.P;
+  std::vector<float> rf(P);
+  std::vector<double> rd(P);
+  double rmax = 0.0;
+  for (int k = 0; k < P; ++k) {
+    const double v = radius[ctx->cull_perm[k]];
+    if (!(v >= 0) || !std::isfinite(v))
+      return fail(ctx, MMO_EINVAL, "mmo_build_masks: atom %d: bad radius", ctx->cull_perm[k]);
+    rd[k] = v;
+    rf[k] = (float)v;
+    rmax = std::max(rmax, v);
+  }
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before mask build");
+  const size_t np = lattice_points(ctx);
+  int r;
+  if ((r = grow(ctx, (void**)&ctx->d_vdw, &ctx->cap_vdw, np, "vdW mask"))) return r;
+  if ((r = grow(ctx, (void**)&ctx->d_shell, &ctx->cap_shell, np, "solvent shell mask"))) return r;
+  char* d_tab = nullptr;
+  MMO_CK(cudaMalloc((void**)&d_tab, (sizeof(double) + sizeof(float)) * (size_t)P), "radii");
+  cudaError_t e = cudaMemcpy(d_tab, rd.data(), sizeof(double) * P, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(d_tab + sizeof(double) * P, rf.data(), sizeof(float) * P,
+                   cudaMemcpyHostToDevice);
+  MaskBuild mb{};
+  mb.radius = reinterpret_cast<const float*>(d_tab + sizeof(double) * P);
+  mb.nx = ctx->grid_n[0];
+  mb.ny = ctx->grid_n[1];
+  mb.nz = ctx->grid_n[2];
+  for (int d = 0; d < 3; ++d) mb.o[d] = ctx->grid_origin[d] - ctx->origin[d];
+  mb.step = ctx->grid_step;
+  mb.r_w = (float)r_water;
+  mb.r_max = (float)rmax;
+  if (e == cudaSuccess)
+    e = launch_masks(ctx->cull, mb, reinterpret_cast<const double*>(d_tab), ctx->d_vdw,
+                     ctx->d_shell, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d_tab);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "mask build");
+  ctx->masks_ok = true;
+  ctx->desolv_ok = false;
+  ++ctx->epoch;
+  return MMO_OK;
+}
+
+int mmo_load_masks(mmo_ctx* ctx, const uint8_t* vdw, const uint8_t* shell) {
+  if (!ctx) return MMO_EINVAL;
+  if (!ctx->grid_ok)
+    return fail(ctx, MMO_ESTATE, "mmo_load_masks: no lattice: build or load the grids first");
+  if (!vdw || !shell) return fail(ctx, MMO_EINVAL, "mmo_load_masks: NULL mask");
+  const size_t np = lattice_points(ctx);
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before mask upload");
+  int r;
+  if ((r = grow(ctx, (void**)&ctx->d_vdw, &ctx->cap_vdw, np, "vdW mask"))) return r;
+  if ((r = grow(ctx, (void**)&ctx->d_shell, &ctx->cap_shell, np, "solvent shell mask"))) return r;
+  MMO_CK(cudaMemcpy(ctx->d_vdw, vdw, np, cudaMemcpyHostToDevice), "vdW mask upload");
+  MMO_CK(cudaMemcpy(ctx->d_shell, shell, np, cudaMemcpyHostToDevice), "shell mask upload");
+  ctx->masks_ok = true;
+  ctx->desolv_ok = false;
+  ++ctx->epoch;
+  return MMO_OK;
+}
+
+int mmo_mask_values(mmo_ctx* ctx, uint8_t* vdw, uint8_t* shell) {
+  if (!ctx) return MMO_EINVAL;
+  if (!ctx->masks_ok) return fail(ctx, MMO_ESTATE, "mmo_mask_values: no masks");
+  const size_t np = lattice_points(ctx);
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before mask download");
+  if (vdw) MMO_CK(cudaMemcpy(vdw, ctx->d_vdw, np, cudaMemcpyDeviceToHost), "vdW mask download");
+  if (shell)
+    MMO_CK(cudaMemcpy(shell, ctx->d_shell, np, cudaMemcpyDeviceToHost), "shell mask download");
+  return MMO_OK;
+}
+
+int mmo_clash_poses_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, int tests,
+                           int* d_out, void* stream) {
+  if (!ctx) return MMO_EINVAL;
+  if (!ctx->has_lig) return fail(ctx, MMO_ESTATE, "no ligand: call mmo_set_ligand first");
+  if (B < 0 || (B > 0 && (!d_dofs || !d_out)) || (tests & ~7))
+    return fail(ctx, MMO_EINVAL, "mmo_clash_poses: bad arguments");
+  if ((tests & MMO_CLASH_HEAVY) && ctx->prot.P <= 0)
+    return fail(ctx, MMO_ESTATE, "MMO_CLASH_HEAVY: no protein");
+  if ((tests & MMO_CLASH_GRID) && !ctx->masks_ok)
+    return fail(ctx, MMO_ESTATE, "MMO_CLASH_GRID: no masks: call mmo_build_masks first");
+  if (B == 0) return MMO_OK;
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int r;
+  if ((r = pose_only(ctx, B, d_dofs, flags, d_out, st))) return r;
+  MMO_CK(launch_clash(ctx->lig, ctx->scr.X, B, ctx->cull, clash_args(ctx, tests), d_out, st),
+         "clash kernel");
+  return MMO_OK;
+}
+
+int mmo_clash_poses(mmo_ctx* ctx, int B, const float* dofs, int flags, int tests, int* out) {
+  if (!ctx) return MMO_EINVAL;
+  if (!ctx->has_lig) return fail(ctx, MMO_ESTATE, "no ligand: call mmo_set_ligand first");
+  if (B < 0 || (B > 0 && (!dofs || !out))) return fail(ctx, MMO_EINVAL, "mmo_clash_poses: bad arguments");
+  if (B == 0) return MMO_OK;
+  const size_t nd = 6 + ctx->lig.nrb;
+  const size_t in_b = sizeof(float) * B * nd, out_b = sizeof(int) * B;
+  int r;
+  if ((r = grow_host(ctx, &ctx->h_in, &ctx->d_in, &ctx->cap_in, in_b))) return r;
+  if ((r = grow_host(ctx, &ctx->h_out, &ctx->d_out, &ctx->cap_out, out_b))) return r;
+  memcpy(ctx->h_in, dofs, in_b);
+  MMO_CK(cudaMemcpyAsync(ctx->d_in, ctx->h_in, in_b, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+  if ((r = mmo_clash_poses_device(ctx, B, reinterpret_cast<const float*>(ctx->d_in), flags, tests,
+                                  reinterpret_cast<int*>(ctx->d_out), ctx->stream)))
+    return r;
+  MMO_CK(cudaMemcpyAsync(ctx->h_out, ctx->d_out, out_b, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync");
+  memcpy(out, ctx->h_out, out_b);
+  return MMO_OK;
+}
+
+int mmo_so3_rotations(int n, double* R) {
+  if (n < 0 || (n > 0 && !R)) return MMO_EINVAL;
+  // SO3.super_fibonacci (src/SO3.ml:18-32), then Quat.to_axis_angle and
+  // Rot.of_axis_angle (src/quat.ml:32-36, src/rot.ml:121-146)
+  const double kPiH = 4.0 * std::atan(1.0);
+  const double phi = std::sqrt(2.0), psi = 1.533751168755204288118041;
+  for (int i = 0; i < n; ++i) {
+    const double s = (double)i + 0.5, t = s / (double)n, d = 2.0 * kPiH * s;
+    const double cr = std::sqrt(t), cR = std::sqrt(1.0 - t), al = d / phi, be = d / psi;
+    const double w = cr * std::sin(al), x = cr * std::cos(al), y = cR * std::sin(be),
+                 z = cR * std::cos(be);
+    const double mag = std::sqrt(x * x + y * y + z * z);
+    const double ux = x / mag, uy = y / mag, uz = z / mag, th = 2.0 * std::atan2(mag, w);
+    const double c = std::cos(th), sn = std::sin(th), o = 1.0 - c;
+    double* M = R + 9 * (size_t)i;
+    M[0] = c + ux * ux * o;
+    M[1] = ux * uy * o - uz * sn;
+    M[2] = ux * uz * o + uy * sn;
+    M[3] = ux * uy * o + uz * sn;
+    M[4] = c + uy * uy * o;
+    M[5] = uy * uz * o - ux * sn;
+    M[6] = ux * uz * o - uy * sn;
+    M[7] = uy * uz * o + ux * sn;
+    M[8] = c + uz * uz * o;
+  }
+  return MMO_OK;
+}
+
+int mmo_dock_exhaustive(mmo_ctx* ctx, const mmo_dock_spec* sp, double* top_scores,
+                        long long* top_frames, mmo_dock_result* res) {
+  if (!ctx) return MMO_EINVAL;
+  if (!sp || !res) return fail(ctx, MMO_EINVAL, "mmo_dock_exhaustive: bad arguments");
+  if (!ctx->has_lig) return fail(ctx, MMO_ESTATE, "no ligand: call mmo_set_ligand first");
+  if (!ctx->grid_map_ok)
+    return fail(ctx, MMO_ESTATE, "mmo_dock_exhaustive: %s", ctx->grid_map_err.c_str());
+  if (!ctx->masks_ok)
+    return fail(ctx, MMO_ESTATE, "mmo_dock_exhaustive: no masks: call mmo_build_masks first");
+  if (!(sp->roi_radius > 0) || !std::isfinite(sp->roi_radius) || !(sp->trans_step > 0) ||
+      !std::isfinite(sp->trans_step) || sp->n_rotations < 1 || sp->topk < 1 ||
+      sp->topk > kDockMaxK || !std::isfinite(sp->const_intra))
+    return fail(ctx, MMO_EINVAL, "mmo_dock_exhaustive: bad spec");
+  if ((sp->topk > 0 && !top_scores))
+    return fail(ctx, MMO_EINVAL, "mmo_dock_exhaustive: top_scores is NULL");
+  const int L = ctx->lig.L, nrot = sp->n_rotations, k = sp->topk;
+  // Mol.is_ligand_center_vdW_occuppied on the centred reference conformer
+  double cen[3] = {0, 0, 0};
+  for (int a = 0; a < L; ++a) {
+    cen[0] += ctx->lx[a];
+    cen[1] += ctx->ly[a];
+    cen[2] += ctx->lz[a];
+  }
+  for (int d = 0; d < 3; ++d) cen[d] /= L;
+  int center_occ = 0;
+  for (int a = 0; a < L; ++a) {
+    const double ra = sp->lig_radius ? sp->lig_radius[a] : vdw_radius(kUff[ctx->ltype[a]].anum);
+    const double dx = cen[0] - ctx->lx[a], dy = cen[1] - ctx->ly[a], dz = cen[2] - ctx->lz[a];
+    if (std::sqrt(dx * dx + dy * dy + dz * dz) < ra) center_occ = 1;
+  }
+  // the position lattice (Grid.from_box trans_step of the ROI's cube), kept inside the ROI
+  const double r = sp->roi_radius, step = sp->trans_step;
+  const long long pdim = (long long)std::ceil(2.0 * r / step) + 1;
+  if (pdim * pdim * pdim > (long long)INT32_MAX)
+    return fail(ctx, MMO_EINVAL, "mmo_dock_exhaustive: too many positions");
+  std::vector<int> pos;
+  for (long long kk = 0; kk < pdim; ++kk)
+    for (long long jj = 0; jj < pdim; ++jj)
+      for (long long ii = 0; ii < pdim; ++ii) {
+        const double x = sp->roi_center[0] - r + step * ii, y = sp->roi_center[1] - r + step * jj,
+                     z = sp->roi_center[2] - r + step * kk;
+        const double dx = x - sp->roi_center[0], dy = y - sp->roi_center[1],
+                     dz = z - sp->roi_center[2];
+        if (dx * dx + dy * dy + dz * dz < r * r)
+          pos.push_back((int)(ii + jj * pdim + kk * pdim * pdim));
+      }
+  const long long total = (long long)pos.size() * nrot;
+  const long long blocks = (total + kDockPerBlock - 1) / kDockPerBlock;
+  if (blocks > (long long)INT32_MAX / kDockMaxK)
+    return fail(ctx, MMO_EINVAL, "mmo_dock_exhaustive: too many poses");
+  std::vector<double> rot(9 * (size_t)nrot);
+  mmo_so3_rotations(nrot, rot.data());
+  // device blob: rotations | positions | two candidate buffers | counters
+  const size_t ncand = (size_t)std::max<long long>(blocks, 1) * k;
+  size_t off = 0;
+  const size_t o_rot = take(off, sizeof(double) * rot.size());
+  const size_t o_pos = take(off, sizeof(int) * std::max<size_t>(pos.size(), 1));
+  const size_t o_c0 = take(off, 2 * sizeof(unsigned long long) * ncand);
+  const size_t o_c1 = take(off, 2 * sizeof(unsigned long long) * ncand);
+  const size_t o_cnt = take(off, 2 * sizeof(unsigned long long));
+  int rc;
+  if ((rc = grow(ctx, &ctx->d_dock, &ctx->cap_dock, off, "docking buffers"))) return rc;
+  char* base = static_cast<char*>(ctx->d_dock);
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before docking");
+  MMO_CK(cudaMemcpy(base + o_rot, rot.data(), sizeof(double) * rot.size(), cudaMemcpyHostToDevice),
+         "rotations upload");
+  if (!pos.empty())
+    MMO_CK(cudaMemcpy(base + o_pos, pos.data(), sizeof(int) * pos.size(), cudaMemcpyHostToDevice),
+           "positions upload");
+  MMO_CK(cudaMemsetAsync(base + o_cnt, 0, 2 * sizeof(unsigned long long), ctx->stream), "counters");
+  DockArgs a{};
+  a.ref = ctx->lig.ref64;
+  a.lig_type = ctx->d_grid_lt;
+  a.grids = ctx->d_grid;
+  a.g = grid_look(ctx);
+  a.vdw = ctx->d_vdw;
+  a.rot = reinterpret_cast<const double*>(base + o_rot);
+  a.pos_idx = reinterpret_cast<const int*>(base + o_pos);
+  a.L = L;
+  a.npos = (int)pos.size();
+  a.nrot = nrot;
+  a.pdim = (int)pdim;
+  for (int d = 0; d < 3; ++d) a.p0[d] = sp->roi_center[d] - r - ctx->origin[d];
+  a.pstep = step;
+  a.center_occ = center_occ;
+  a.const_intra = sp->const_intra;
+  a.k = k;
+  a.cand = reinterpret_cast<unsigned long long*>(base + o_c0);
+  a.counts = reinterpret_cast<unsigned long long*>(base + o_cnt);
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  MMO_CK(cudaEventCreate(&ev[0]), "event");
+  MMO_CK(cudaEventCreate(&ev[1]), "event");
+  cudaError_t e = cudaEventRecord(ev[0], ctx->stream);
+  if (e == cudaSuccess) e = launch_dock(a, (int)blocks, ctx->stream);
+  // merge the candidates k at a time until one group remains
+  unsigned long long* cur = a.cand;
+  unsigned long long* nxt = reinterpret_cast<unsigned long long*>(base + o_c1);
+  long long n = blocks * k;
+  while (e == cudaSuccess && n > k) {
+    e = launch_topk_merge(cur, (int)n, k, nxt, ctx->stream);
+    n = (n + kDockPerBlock - 1) / kDockPerBlock * k;
+    std::swap(cur, nxt);
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(ev[1], ctx->stream);
+  std::vector<unsigned long long> host(2 * (size_t)k + 2, ~0ull);
+  if (e == cudaSuccess && blocks > 0)
+    e = cudaMemcpyAsync(host.data(), cur, 2 * sizeof(unsigned long long) * k,
+                        cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(host.data() + 2 * k, base + o_cnt, 2 * sizeof(unsigned long long),
+                        cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "exhaustive docking");
+  *res = mmo_dock_result{};
+  res->best_score = HUGE_VAL;
+  res->positions = (long long)pos.size();
+  res->poses = total;
+  res->scored = (long long)host[2 * k];
+  res->clashed = (long long)host[2 * k + 1];
+  res->ms = ms;
+  int nt = 0;
+  for (int t = 0; t < k && blocks > 0; ++t) {
+    const unsigned long long key = host[2 * t], fr = host[2 * t + 1];
+    if (key == ~0ull) break;
+    const unsigned long long u = (key >> 63) ? (key & 0x7fffffffffffffffull) : ~key;
+    double sc;
+    memcpy(&sc, &u, sizeof sc);
+    top_scores[nt] = sc;
+    if (top_frames) top_frames[nt] = (long long)fr;
+    if (nt == 0) {
+      res->best_score = sc;
+      const long long pi = (long long)(fr / (unsigned long long)nrot);
+      res->best_rot = (int)(fr % (unsigned long long)nrot);
+      const long long ii = pi % pdim, jj = (pi / pdim) % pdim, kk = pi / (pdim * pdim);
+      res->best_pos[0] = sp->roi_center[0] - r + step * ii;
+      res->best_pos[1] = sp->roi_center[1] - r + step * jj;
+      res->best_pos[2] = sp->roi_center[2] - r + step * kk;
+    }
+    ++nt;
+  }
+  res->n_top = nt;
+  return MMO_OK;
+}
+
+int mmo_place_in_roi(mmo_ctx* ctx, const double center[3], double radius, int n,
+                     unsigned long long seed, float* dofs, long long* trials) {
+  if (!ctx) return MMO_EINVAL;
+  if (!center || !(radius > 0) || !std::isfinite(radius) || n < 0 || (n > 0 && !dofs))
+    return fail(ctx, MMO_EINVAL, "mmo_place_in_roi: bad arguments");
+  if (!ctx->has_lig) return fail(ctx, MMO_ESTATE, "no ligand: call mmo_set_ligand first");
+  if (ctx->prot.P <= 0) return fail(ctx, MMO_ESTATE, "no protein: call mmo_set_protein first");
+  if (n == 0) return MMO_OK;
+  const int per = 64, nd = 6 + ctx->lig.nrb;
+  size_t off = 0;
+  const size_t o_out = take(off, sizeof(float) * 7 * (size_t)n * per);
+  const size_t o_ids = take(off, sizeof(int) * (size_t)n);
+  int rc;
+  if ((rc = grow(ctx, &ctx->d_dock, &ctx->cap_dock, off, "placement buffers"))) return rc;
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before placement");
+  char* base = static_cast<char*>(ctx->d_dock);
+  PlaceArgs a{};
+  a.ref = ctx->lig.ref64;
+  a.type = ctx->lig.type;
+  a.L = ctx->lig.L;
+  a.per_slot = per;
+  for (int d = 0; d < 3; ++d) a.c[d] = center[d] - ctx->origin[d];
+  a.r = radius;
+  a.key0 = (uint32_t)(seed & 0xffffffffu);
+  a.key1 = (uint32_t)(seed >> 32);
+  a.out = reinterpret_cast<float*>(base + o_out);
+  a.slot_id = reinterpret_cast<const int*>(base + o_ids);
+  const ClashArgs ca = clash_args(ctx, MMO_CLASH_HEAVY);
+  // open placements; candidate c of placement s uses Philox counter (s, c, draw, 1)
+  std::vector<int> todo(n);
+  std::iota(todo.begin(), todo.end(), 0);
+  std::vector<float> host((size_t)7 * n * per);
+  long long drawn = 0;
+  for (int c0 = 0; !todo.empty(); c0 += per) {
+    if (c0 >= 100000)
+      return fail(ctx, MMO_ESTATE,
+                  "mmo_place_in_roi: placement %d found no clash-free pose in 100000 candidates",
+                  todo[0]);
+    const int m = (int)todo.size();
+    a.slots = m;
+    a.c0 = c0;
+    MMO_CK(cudaMemcpy(base + o_ids, todo.data(), sizeof(int) * m, cudaMemcpyHostToDevice),
+           "placement ids upload");
+    MMO_CK(launch_place(a, ctx->cull, ca, ctx->stream), "placement kernel");
+    MMO_CK(cudaMemcpyAsync(host.data(), a.out, sizeof(float) * 7 * (size_t)m * per,
+                           cudaMemcpyDeviceToHost, ctx->stream),
+           "placement download");
+    MMO_CK(cudaStreamSynchronize(ctx->stream), "sync");
+    std::vector<int> still;
+    for (int t = 0; t < m; ++t) {
+      int hit = -1;
+      for (int c = 0; c < per && hit < 0; ++c)
+        if (host[(size_t)7 * (per * t + c) + 6] != 0.f) hit = c;
+      if (hit < 0) {
+        drawn += per;
+        still.push_back(todo[t]);
+        continue;
+      }
+      drawn += hit + 1;
+      const float* o = &host[(size_t)7 * (per * t + hit)];
+      float* d = dofs + (size_t)nd * todo[t];
+      for (int q = 0; q < 3; ++q) d[q] = (float)((double)o[q] + ctx->origin[q]);
+      for (int q = 3; q < 6; ++q) d[q] = o[q];
+      for (int q = 6; q < nd; ++q) d[q] = 0.f;
+    }
+    todo.swap(still);
+  }
+  if (trials) *trials = drawn;
+  return MMO_OK;
+}
+
+int mmo_set_ligand_radii(mmo_ctx* ctx, const double* radius) {
+  if (!ctx) return MMO_EINVAL;
+  if (!ctx->has_lig) return fail(ctx, MMO_ESTATE, "no ligand: call mmo_set_ligand first");
+  if (!radius) return fail(ctx, MMO_EINVAL, "mmo_set_ligand_radii: radius is NULL");
+  const int L = ctx->lig.L;
+  for (int a = 0; a < L; ++a)
+    if (!(radius[a] >= 0) || !std::isfinite(radius[a]))
+      return fail(ctx, MMO_EINVAL, "mmo_set_ligand_radii: atom %d: bad radius", a);
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before radii upload");
+  int r;
+  if ((r = grow(ctx, (void**)&ctx->d_lradius, &ctx->cap_lradius, sizeof(double) * L, "ligand radii")))
+    return r;
+  MMO_CK(cudaMemcpy(ctx->d_lradius, radius, sizeof(double) * L, cudaMemcpyHostToDevice),
+         "ligand radii upload");
+  ctx->lradius.assign(radius, radius + L);
+  return MMO_OK;
+}
+
+int mmo_protein_desolv(mmo_ctx* ctx, const double center[3], double radius, double* out) {
+  if (!ctx) return MMO_EINVAL;
+  if (!center || !(radius > 0) || !std::isfinite(radius))
+    return fail(ctx, MMO_EINVAL, "mmo_protein_desolv: bad arguments");
+  if (!ctx->masks_ok)
+    return fail(ctx, MMO_ESTATE, "mmo_protein_desolv: no masks: call mmo_build_masks first");
+  if (ctx->prot.P <= 0 || !ctx->d_cull) return fail(ctx, MMO_ESTATE, "no protein");
+  const int nx = ctx->grid_n[0], ny = ctx->grid_n[1], nz = ctx->grid_n[2];
+  const size_t np = lattice_points(ctx);
+  DesolvBuild db{};
+  db.shell = ctx->d_shell;
+  db.nx = nx;
+  db.ny = ny;
+  db.nz = nz;
+  for (int d = 0; d < 3; ++d) {
+    db.o[d] = ctx->grid_origin[d] - ctx->origin[d];
+    db.c[d] = center[d] - ctx->origin[d];
+  }
+  db.step = ctx->grid_step;
+  db.r2 = radius * radius;
+  const double vol = db.step * db.step * db.step;
+  db.scale = (1.0 / 4.0 - 1.0 / 78.5) / (8.0 * (4.0 * std::atan(1.0))) * vol / (kElec * kElec);
+  std::vector<int3> tiles;
+  for (int tz = 0; tz < (nz + 1) / 2; ++tz)
+    for (int ty = 0; ty < (ny + 3) / 4; ++ty)
+      for (int tx = 0; tx < (nx + 3) / 4; ++tx) {
+        const int lo[3] = {4 * tx, 4 * ty, 2 * tz};
+        const int hi[3] = {std::min(4 * tx + 3, nx - 1), std::min(4 * ty + 3, ny - 1),
+                           std::min(2 * tz + 1, nz - 1)};
+        double d2 = 0.0;
+        for (int d = 0; d < 3; ++d) {
+          const double a0 = db.o[d] + db.step * lo[d], a1 = db.o[d] + db.step * hi[d];
+          const double g = db.c[d] < a0 ? a0 - db.c[d] : (db.c[d] > a1 ? db.c[d] - a1 : 0.0);
+          d2 += g * g;
+        }
+        if (d2 < db.r2) tiles.push_back(make_int3(tx, ty, tz));
+      }
+  db.ntiles = (int)tiles.size();
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before desolvation");
+  int r;
+  if ((r = grow(ctx, (void**)&ctx->d_desolv, &ctx->cap_desolv, sizeof(double) * np,
+                "desolvation contributions")))
+    return r;
+  int3* d_tiles = nullptr;
+  MMO_CK(cudaMalloc((void**)&d_tiles, sizeof(int3) * std::max<size_t>(tiles.size(), 1)), "tiles");
+  cudaError_t e = cudaSuccess;
+  if (!tiles.empty())
+    e = cudaMemcpy(d_tiles, tiles.data(), sizeof(int3) * tiles.size(), cudaMemcpyHostToDevice);
+  db.tiles = d_tiles;
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_desolv, 0, sizeof(double) * np, ctx->stream);
+  if (e == cudaSuccess) e = launch_prot_desolv(ctx->cull, db, ctx->d_desolv, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d_tiles);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "protein desolvation");
+  if (out)
+    MMO_CK(cudaMemcpy(out, ctx->d_desolv, sizeof(double) * np, cudaMemcpyDeviceToHost),
+           "desolvation download");
+  ctx->desolv_ok = true;
+  return MMO_OK;
+}
+
+int mmo_desolvation_poses_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags,
+                                 double r_water, double* d_prot, double* d_lig, int* d_status,
+                                 void* stream) {
+  if (!ctx) return MMO_EINVAL;
+  if (!ctx->has_lig) return fail(ctx, MMO_ESTATE, "no ligand: call mmo_set_ligand first");
+  if (!ctx->desolv_ok)
+    return fail(ctx, MMO_ESTATE, "mmo_desolvation_poses: call mmo_protein_desolv first");
+  if ((int)ctx->lradius.size() != ctx->lig.L)
+    return fail(ctx, MMO_ESTATE, "mmo_desolvation_poses: call mmo_set_ligand_radii first");
+  if (B < 0 || (B > 0 && (!d_dofs || !d_prot || !d_lig || !d_status)) || !(r_water >= 0) ||
+      !std::isfinite(r_water))
+    return fail(ctx, MMO_EINVAL, "mmo_desolvation_poses: bad arguments");
+  if (B == 0) return MMO_OK;
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int r;
+  if ((r = pose_only(ctx, B, d_dofs, flags, d_status, st))) return r;
+  MMO_CK(cudaMemsetAsync(d_status, 0, sizeof(int) * B, st), "status reset");
+  DesolvPose d{};
+  d.X = ctx->scr.X;
+  d.q = ctx->lig.q;
+  d.radius = ctx->d_lradius;
+  d.shell = ctx->d_shell;
+  d.contrib = ctx->d_desolv;
+  d.g = grid_look(ctx);
+  d.step = ctx->grid_step;
+  d.r_w = (float)r_water;
+  d.L = ctx->lig.L;
+  d.B = B;
+  d.cap = 262144;
+  d.scale = (1.0 / 4.0 - 1.0 / 78.5) / (8.0 * (4.0 * std::atan(1.0))) * ctx->grid_step *
+            ctx->grid_step * ctx->grid_step;
+  d.prot = d_prot;
+  d.lig = d_lig;
+  d.status = d_status;
+  MMO_CK(launch_desolv_pose(d, st), "desolvation kernel");
+  return MMO_OK;
+}
+
+int mmo_desolvation_poses(mmo_ctx* ctx, int B, const float* dofs, int flags, double r_water,
+                          double* prot, double* lig, int* status) {
+  if (!ctx) return MMO_EINVAL;
+  if (!ctx->has_lig) return fail(ctx, MMO_ESTATE, "no ligand: call mmo_set_ligand first");
+  if (B < 0 || (B > 0 && (!dofs || !prot || !lig || !status)))
+    return fail(ctx, MMO_EINVAL, "mmo_desolvation_poses: bad arguments");
+  if (B == 0) return MMO_OK;
+  const size_t nd = 6 + ctx->lig.nrb;
+  const size_t in_b = sizeof(float) * B * nd;
+  const size_t o_lig = sizeof(double) * B, o_st = 2 * sizeof(double) * B;
+  const size_t out_b = o_st + sizeof(int) * B;
+  int r;
+  if ((r = grow_host(ctx, &ctx->h_in, &ctx->d_in, &ctx->cap_in, in_b))) return r;
+  if ((r = grow_host(ctx, &ctx->h_out, &ctx->d_out, &ctx->cap_out, out_b))) return r;
+  memcpy(ctx->h_in, dofs, in_b);
+  MMO_CK(cudaMemcpyAsync(ctx->d_in, ctx->h_in, in_b, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+  if ((r = mmo_desolvation_poses_device(
+           ctx, B, reinterpret_cast<const float*>(ctx->d_in), flags, r_water,
+           reinterpret_cast<double*>(ctx->d_out), reinterpret_cast<double*>(ctx->d_out + o_lig),
+           reinterpret_cast<int*>(ctx->d_out + o_st), ctx->stream)))
+    return r;
+  MMO_CK(cudaMemcpyAsync(ctx->h_out, ctx->d_out, out_b, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync");
+  memcpy(prot, ctx->h_out, sizeof(double) * B);
+  memcpy(lig, ctx->h_out + o_lig, sizeof(double) * B);
+  memcpy(status, ctx->h_out + o_st, sizeof(int) * B);
   return MMO_OK;
 }
 

@@ -19,26 +19,6 @@ namespace {
 
 constexpr double kPi = 3.14159265358979323846;
 
-// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC 2011)
-__device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
-#pragma unroll
-  for (int r = 0; r < 10; ++r) {
-    if (r) {
-      k0 += 0x9E3779B9u;
-      k1 += 0xBB67AE85u;
-    }
-    const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
-    const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
-    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
-  }
-  return c;
-}
-
-// uniform in [0, 1) with 53 random bits
-__device__ __forceinline__ double u01(uint32_t a, uint32_t b) {
-  return (double)(((uint64_t)a << 21) ^ (uint64_t)(b >> 11)) * (1.0 / 9007199254740992.0);
-}
-
 // standard normal pair from two uniforms (Box-Muller)
 __device__ __forceinline__ void normal2(double u1, double u2, double& n0, double& n1) {
   const double r = sqrt(-2.0 * log(1.0 - u1));  // 1 - u1 in (0, 1]

@@ -292,6 +292,82 @@ struct GridLook {
   int nx, ny, nz;
 };
 
+// ---- lattice masks, clash tests, exhaustive docking, placement and
+// desolvation (kernels_dock.cu) --------------------------------------------
+enum : int { kClashIntra = 1, kClashHeavy = 2, kClashGrid = 4 };
+constexpr int kDockBlock = 256;           // threads of a docking block
+constexpr int kDockPerBlock = 4096;       // poses a docking block scores and sorts
+constexpr int kDockMaxK = 1024;           // largest top-k
+constexpr float kHeavyClashMax = 3.52f;   // 0.8 (2.2 + 2.2): the largest clash distance
+
+// protein masks on the grids' lattice (Lds.vdW_volume, Lds.first_solvent_shell)
+struct MaskBuild {
+  const float* radius;     // [P] radius of each protein atom, row order
+  int nx, ny, nz;
+  double o[3], step;       // lattice point (0, 0, 0) in the device frame
+  float r_w, r_max;        // water radius, largest atom radius
+};
+
+struct ClashArgs {
+  GridLook g;                       // the masks' lattice (device frame)
+  const uint8_t* vdw;               // [points] protein vdW volume, or null
+  uint8_t heavy[kNTypes];           // 1 for the types of heavy atoms (anum > 1)
+  float clash2[kNTypes * kNTypes];  // (0.8 (r_i + r_j))^2 by UFF type; NaN without radii
+  int tests;                        // kClash* bits
+};
+
+struct DockArgs {
+  const double* ref;        // [L][3] centred reference conformer
+  const int* lig_type;      // [L] grid type of each atom
+  const float* grids;       // [ntypes][nz][ny][nx]
+  GridLook g;               // grids' lattice (device frame)
+  const uint8_t* vdw;       // [points] protein vdW volume on the same lattice
+  const double* rot;        // [nrot][9] rotations, row-major
+  const int* pos_idx;       // [npos] index of each position in the position lattice
+  int L, npos, nrot, pdim;  // positions: pdim points per axis
+  double p0[3], pstep;      // position lattice origin (device frame), spacing
+  int center_occ;           // the ligand's centre is inside one of its atoms
+  double const_intra;
+  int k;
+  unsigned long long* cand;    // [blocks][k][2] (sortable score, frame)
+  unsigned long long* counts;  // [2] poses scored, poses rejected by the clash test
+};
+
+struct PlaceArgs {
+  const double* ref;        // [L][3]
+  const int* type;          // [L] UFF type
+  const int* slot_id;       // [slots] placement index of each launch slot
+  int L, slots, per_slot, c0;  // candidates c0 .. c0 + per_slot - 1 of every slot
+  double c[3], r;           // ROI (device frame)
+  uint32_t key0, key1;
+  float* out;               // [slots][per_slot][7]: (x, y, z, a, b, g) device frame, ok
+};
+
+struct DesolvBuild {
+  const int3* tiles;        // [ntiles] 4 x 4 x 2 tiles meeting the ROI
+  const uint8_t* shell;     // [points] protein solvent shell
+  int ntiles, nx, ny, nz;
+  double o[3], step;
+  double c[3], r2;          // ROI (device frame)
+  double scale;             // C vol / K^2 (the atoms carry K q)
+};
+
+struct DesolvPose {
+  const float4* X;          // [B][L][2] posed atoms (hi, lo)
+  const float* q;           // [L]
+  const double* radius;     // [L]
+  const uint8_t* shell;     // [points] protein solvent shell
+  const double* contrib;    // [points] protein desolvation per point
+  GridLook g;
+  double step;
+  float r_w;
+  int L, B, cap;            // cap: lattice points of a pose's box the shared masks hold
+  double scale;             // C vol
+  double* prot;             // [B]
+  double* lig;              // [B]
+  int* status;              // [B] bit 1: the box exceeded cap
+};
+
 // ---- launchers (defined in the .cu files) --------------------------------
 cudaError_t launch_k_mc_init(const MCDev& s, const MCParams& p, cudaStream_t st);
 cudaError_t launch_k_mc_start(const MCDev& s, const MCParams& p, cudaStream_t st);
@@ -344,6 +420,18 @@ cudaError_t launch_grid_build(const DevCull& cull, const GridBuild& gb, int diel
 cudaError_t launch_grid_inter(const GridLook& g, const float4* X, int n, int L,
                               const int* atom_type, const float* grids, double* Epart,
                               float4* Gpart, int* status, int grad, cudaStream_t st);
+cudaError_t launch_masks(const DevCull& cull, const MaskBuild& mb, const double* radius64,
+                         uint8_t* vdw, uint8_t* shell, cudaStream_t st);
+cudaError_t launch_clash(const DevLigand& lig, const float4* X, int B, const DevCull& cull,
+                         const ClashArgs& ca, int* out, cudaStream_t st);
+cudaError_t launch_dock(const DockArgs& a, int blocks, cudaStream_t st);
+cudaError_t launch_topk_merge(const unsigned long long* in, int n, int k, unsigned long long* out,
+                              cudaStream_t st);
+cudaError_t launch_place(const PlaceArgs& a, const DevCull& cull, const ClashArgs& ca,
+                         cudaStream_t st);
+cudaError_t launch_prot_desolv(const DevCull& cull, const DesolvBuild& db, double* out,
+                               cudaStream_t st);
+cudaError_t launch_desolv_pose(const DesolvPose& d, cudaStream_t st);
 cudaError_t launch_fma_peak(int sms, int iters, float* out, cudaStream_t st, double* flops);
 
 // ---- device helpers ------------------------------------------------------
@@ -362,6 +450,26 @@ __device__ __forceinline__ float warp_max(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC 2011): counter c, key (k0, k1)
+__device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+    const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+  }
+  return c;
+}
+
+// uniform in [0, 1) with 53 random bits
+__device__ __forceinline__ double u01(uint32_t a, uint32_t b) {
+  return (double)(((uint64_t)a << 21) ^ (uint64_t)(b >> 11)) * (1.0 / 9007199254740992.0);
 }
 
 // pair difference a - b of two hi/lo coordinate pairs

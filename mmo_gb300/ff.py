@@ -326,6 +326,104 @@ class UFFScorer:
         self._check(self._lib.mmo_grid_atom_types(self._h, _ip(out)))
         return out
 
+    # -- binding-site clients (include/mmo_dock.h) --------------------------
+    def build_masks(self, radius, r_water: float = 1.4) -> None:
+        """Lds.vdW_volume and Lds.first_solvent_shell on the grids' lattice;
+        radius: one per protein atom (set_protein order)."""
+        r = _f64(radius)
+        if r.shape != (self.protein.n,):
+            raise ValueError("one radius per protein atom")
+        self._check(self._lib.mmo_build_masks(self._h, _dp(r), float(r_water)))
+
+    def load_masks(self, vdw, shell) -> None:
+        v = np.ascontiguousarray(vdw, np.uint8)
+        sh = np.ascontiguousarray(shell, np.uint8)
+        self._check(self._lib.mmo_load_masks(self._h, v.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                             sh.ctypes.data_as(C.POINTER(C.c_uint8))))
+
+    def mask_values(self):
+        """(vdW volume, solvent shell) as uint8 [nz, ny, nx]."""
+        nt, nx, ny, nz = (C.c_int() for _ in range(4))
+        self._check(self._lib.mmo_grid_dims(self._h, C.byref(nt), C.byref(nx), C.byref(ny),
+                                            C.byref(nz)))
+        v = np.zeros((nz.value, ny.value, nx.value), np.uint8)
+        sh = np.zeros_like(v)
+        self._check(self._lib.mmo_mask_values(self._h, v.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                              sh.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return v, sh
+
+    def clash_poses(self, dofs, tests=7, recenter=False) -> np.ndarray:
+        """MMO_CLASH_* bits of each pose (int32 [B])."""
+        dofs = np.ascontiguousarray(np.atleast_2d(dofs), np.float32)
+        out = np.zeros(len(dofs), np.int32)
+        self._check(self._lib.mmo_clash_poses(
+            self._h, len(dofs), dofs.ctypes.data_as(C.POINTER(C.c_float)),
+            _L.F_RECENTER if recenter else 0, int(tests), _ip(out)))
+        return out
+
+    def dock_exhaustive(self, center, radius, trans_step, n_rotations, topk=1,
+                        const_intra=0.0, lig_radius=None) -> dict:
+        """Lds.exhaustive_rigid_ligand_docking on the grids and the masks."""
+        sp = _L.DockSpec()
+        sp.roi_center[:] = [float(v) for v in center]
+        sp.roi_radius = float(radius)
+        sp.trans_step = float(trans_step)
+        sp.n_rotations = int(n_rotations)
+        sp.topk = int(topk)
+        sp.const_intra = float(const_intra)
+        lr = _f64(lig_radius) if lig_radius is not None else None
+        sp.lig_radius = lr.ctypes.data if lr is not None else None
+        scores = np.zeros(topk, np.float64)
+        frames = np.zeros(topk, np.int64)
+        res = _L.DockResult()
+        self._check(self._lib.mmo_dock_exhaustive(
+            self._h, C.byref(sp), _dp(scores), frames.ctypes.data_as(C.POINTER(C.c_longlong)),
+            C.byref(res)))
+        n = res.n_top
+        return {"scores": scores[:n], "frames": frames[:n], "best_score": res.best_score,
+                "best_pos": np.array(res.best_pos[:]), "best_rot": res.best_rot,
+                "positions": res.positions, "poses": res.poses, "scored": res.scored,
+                "clashed": res.clashed, "ms": res.ms}
+
+    def place_in_roi(self, center, radius, n, seed=0):
+        """Lds.place_ligand_in_ROI: (dofs float32 [n, 6 + nrb], candidates drawn)."""
+        c = _f64(center)
+        out = np.zeros((n, 6 + self.ligand.nrb), np.float32)
+        tr = C.c_longlong()
+        self._check(self._lib.mmo_place_in_roi(self._h, _dp(c), float(radius), int(n),
+                                               C.c_ulonglong(seed),
+                                               out.ctypes.data_as(C.POINTER(C.c_float)),
+                                               C.byref(tr)))
+        return out, tr.value
+
+    def set_ligand_radii(self, radius) -> None:
+        r = _f64(radius)
+        self._check(self._lib.mmo_set_ligand_radii(self._h, _dp(r)))
+
+    def protein_desolv(self, center, radius, download=True):
+        """Lds.protein_desolv: float64 [nz, ny, nx] (or None without download)."""
+        c = _f64(center)
+        out = None
+        if download:
+            nt, nx, ny, nz = (C.c_int() for _ in range(4))
+            self._check(self._lib.mmo_grid_dims(self._h, C.byref(nt), C.byref(nx), C.byref(ny),
+                                                C.byref(nz)))
+            out = np.zeros((nz.value, ny.value, nx.value), np.float64)
+        self._check(self._lib.mmo_protein_desolv(self._h, _dp(c), float(radius),
+                                                 _dp(out) if out is not None else None))
+        return out
+
+    def desolvation_poses(self, dofs, r_water=1.4, recenter=False):
+        """Lds.desolvation_penalty of each pose: (prot, lig, status)."""
+        dofs = np.ascontiguousarray(np.atleast_2d(dofs), np.float32)
+        B = len(dofs)
+        prot, lig = np.zeros(B), np.zeros(B)
+        st = np.zeros(B, np.int32)
+        self._check(self._lib.mmo_desolvation_poses(
+            self._h, B, dofs.ctypes.data_as(C.POINTER(C.c_float)),
+            _L.F_RECENTER if recenter else 0, float(r_water), _dp(prot), _dp(lig), _ip(st)))
+        return prot, lig, st
+
     # -- batched poses -----------------------------------------------------
     def score_poses(self, dofs, inter=True, intra=True, grad=False, recenter=False, grid=False):
         """E (float64 [B]), grad (float32 [B, 6+nrb] or None), status (int32 [B]).
@@ -394,6 +492,13 @@ class UFFScorer:
         t, ms = C.c_double(), C.c_double()
         self._check(self._lib.mmo_fp32_fma_peak(self._h, C.byref(t), C.byref(ms)))
         return t.value
+
+
+def so3_rotations(n: int) -> np.ndarray:
+    """SO3.rotations (src/SO3.ml:18-46): float64 [n, 3, 3]."""
+    out = np.zeros((n, 3, 3), np.float64)
+    _L.check(_L.load().mmo_so3_rotations(int(n), _dp(out)))
+    return out
 
 
 def ene_inter_builder(prot: Mol, ff_style: str = "Bst", device: int = 0,

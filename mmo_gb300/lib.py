@@ -20,6 +20,7 @@ F_INTER, F_INTRA, F_GRAD, F_RECENTER, F_GRID = 1, 2, 4, 8, 16
 S_TOO_LONG, S_NONFINITE, S_OFF_GRID = 1, 2, 4
 
 MC_UNIFORM, MC_GAUSSIAN = 0, 1
+CLASH_INTRA, CLASH_HEAVY, CLASH_GRID = 1, 2, 4
 
 
 class MCParams(C.Structure):
@@ -37,6 +38,20 @@ class GridSpec(C.Structure):
                 ("origin", C.c_double * 3), ("mask_center", C.c_double * 3),
                 ("mask_radius", C.c_double), ("max_E", C.c_double), ("ntypes", C.c_int),
                 ("type_anum", C.c_void_p), ("type_q", C.c_void_p)]
+
+
+class DockSpec(C.Structure):
+    """mmo_dock_spec of include/mmo_dock.h."""
+    _fields_ = [("roi_center", C.c_double * 3), ("roi_radius", C.c_double),
+                ("trans_step", C.c_double), ("n_rotations", C.c_int), ("topk", C.c_int),
+                ("const_intra", C.c_double), ("lig_radius", C.c_void_p)]
+
+
+class DockResult(C.Structure):
+    """mmo_dock_result of include/mmo_dock.h."""
+    _fields_ = [("n_top", C.c_int), ("best_score", C.c_double), ("best_pos", C.c_double * 3),
+                ("best_rot", C.c_int), ("positions", C.c_longlong), ("poses", C.c_longlong),
+                ("scored", C.c_longlong), ("clashed", C.c_longlong), ("ms", C.c_double)]
 
 
 class MCState(C.Structure):
@@ -100,6 +115,19 @@ SIGNATURES = {
     "mmo_grid_device": (_i, [_vp, _P(_vp)]),
     "mmo_grid_atom_types": (_i, [_vp, _P(_i)]),
     "mmo_grid_build_stats": (_i, [_vp, _P(_d), _P(_d), _P(_d)]),
+    "mmo_build_masks": (_i, [_vp, _P(_d), _d]),
+    "mmo_load_masks": (_i, [_vp, _P(C.c_uint8), _P(C.c_uint8)]),
+    "mmo_mask_values": (_i, [_vp, _P(C.c_uint8), _P(C.c_uint8)]),
+    "mmo_clash_poses_device": (_i, [_vp, _i, _vp, _i, _i, _vp, _vp]),
+    "mmo_clash_poses": (_i, [_vp, _i, _P(C.c_float), _i, _i, _P(_i)]),
+    "mmo_so3_rotations": (_i, [_i, _P(_d)]),
+    "mmo_dock_exhaustive": (_i, [_vp, _P(DockSpec), _P(_d), _P(C.c_longlong), _P(DockResult)]),
+    "mmo_place_in_roi": (_i, [_vp, _P(_d), _d, _i, C.c_ulonglong, _P(C.c_float),
+                              _P(C.c_longlong)]),
+    "mmo_set_ligand_radii": (_i, [_vp, _P(_d)]),
+    "mmo_protein_desolv": (_i, [_vp, _P(_d), _d, _P(_d)]),
+    "mmo_desolvation_poses_device": (_i, [_vp, _i, _vp, _i, _d, _vp, _vp, _vp, _vp]),
+    "mmo_desolvation_poses": (_i, [_vp, _i, _P(C.c_float), _i, _d, _P(_d), _P(_d), _P(_i)]),
 }
 
 

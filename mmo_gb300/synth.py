@@ -193,6 +193,33 @@ class System:
     poses: np.ndarray  # float32 [B, 6 + nrb]
 
 
+# Ptable.vdW_radii (src/ptable.ml:41-53) of the synthetic elements
+VDW_RADIUS = {1: 1.2, 6: 1.7, 7: 1.6, 8: 1.55, 16: 1.8}
+
+
+def radii(mol: Mol) -> np.ndarray:
+    """Ptable.vdW_radii of each atom (the .pqrs radius column of real inputs)."""
+    return np.array([VDW_RADIUS[int(a)] for a in mol.anum], np.float64)
+
+
+def docking_site(seed=0, n_pocket=3000, r_in=7.5, r_out=16.0, n_atoms=16, n_rot=3) -> System:
+    """A cavity for docking: pocket atoms between r_in and r_out about the
+    origin, and a small ligand that fits in the empty core; no poses."""
+    rng = np.random.default_rng(seed)
+    pts = sphere_points(rng, int(n_pocket * 1.7), r_out)
+    pts = pts[np.einsum("ij,ij->i", pts, pts) >= r_in * r_in][:n_pocket]
+    types = rng.integers(0, len(TYPE_LABELS), size=len(pts))
+    q = rng.normal(0.0, 0.4, size=len(pts))
+    pocket = Mol("cavity%d" % len(pts), pts[:, 0].copy(), pts[:, 1].copy(), pts[:, 2].copy(), q,
+                 TYPE_ANUM[types].astype(np.int32), np.zeros(len(pts)))
+    pocket.type_labels = [TYPE_LABELS[t] for t in types]
+    pocket.radius = radii(pocket)
+    lig = random_ligand(rng, n_atoms, n_rot, "lig%d" % n_atoms)
+    lig.radius = radii(lig)
+    return System("dock_site_P%d_L%d" % (len(pts), n_atoms), pocket, lig,
+                  np.zeros((0, 6 + lig.nrb), np.float32))
+
+
 def single_pose(seed=0) -> System:
     """Plain single-pose score: 32-atom ligand with 5 rotatable bonds at the
     centre of a 1,500-atom pocket in a 14 A sphere, random torsions."""

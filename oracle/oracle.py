@@ -29,6 +29,19 @@ class CMol(C.Structure):
                 ("anum", C.POINTER(C.c_int))]
 
 
+class Lattice(C.Structure):
+    _fields_ = [("step", C.c_double), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("o", C.c_double * 3)]
+
+
+def lattice(step, dims, origin) -> Lattice:
+    g = Lattice()
+    g.step = float(step)
+    g.nx, g.ny, g.nz = (int(v) for v in dims)
+    g.o[:] = [float(v) for v in origin]
+    return g
+
+
 class CLigand(C.Structure):
     _fields_ = [("m", CMol), ("interacting", C.POINTER(C.c_uint8)), ("nrb", C.c_int),
                 ("bond_lr", C.POINTER(C.c_int)), ("grp_off", C.POINTER(C.c_int)),
@@ -80,6 +93,23 @@ def lib():
             "orc_grid_points": (v, [P(Physics), P(CMol), i, P(d), i, P(i), P(d), d, i, P(d),
                                     P(d)]),
             "orc_trilin": (d, [d, i, i, i, P(C.c_float), P(d), P(i)]),
+            "orc_vdw_radius": (d, [i]),
+            "orc_clash2": (d, [i, i]),
+            "orc_masks": (v, [P(Lattice), i, P(d), P(d), P(d), P(d), d, P(C.c_uint8),
+                              P(C.c_uint8)]),
+            "orc_clash_or": (i, [P(Lattice), P(C.c_uint8), P(d)]),
+            "orc_clash_and": (i, [P(Lattice), P(C.c_uint8), P(d)]),
+            "orc_protein_ligand_clash": (i, [P(Lattice), P(C.c_uint8), i, P(d), P(d), P(d)]),
+            "orc_center_occupied": (i, [i, P(d), P(d), P(d), P(d)]),
+            "orc_heavy_atom_clash": (i, [P(CMol), i, P(d), P(d), P(d), P(i)]),
+            "orc_intra_clash": (i, [i, P(d), P(d), P(d), P(i), P(C.c_uint8)]),
+            "orc_so3_rotation": (v, [i, i, P(d)]),
+            "orc_dock_scores": (v, [P(Lattice), P(C.c_float), P(C.c_uint8), P(CMol), P(i), P(d),
+                                    P(d), d, d, i, P(d), d, P(i), P(d)]),
+            "orc_desolv_constant": (d, []),
+            "orc_protein_desolv": (v, [P(Lattice), P(CMol), P(C.c_uint8), P(d), d, P(d)]),
+            "orc_desolvation_penalty": (v, [P(Lattice), P(d), P(C.c_uint8), i, P(d), P(d), P(d),
+                                            P(d), P(d), d, P(d)]),
             "orc_ene_inter_interp": (d, [d, i, i, i, P(C.c_float), i, P(d), P(d), P(d), P(i),
                                          P(i)]),
         }
@@ -312,3 +342,112 @@ def ene_inter_interp(step, dims, grids, xyz, types):
     e = f(C.c_double(step), dims[0], dims[1], dims[2], g.ctypes.data_as(C.POINTER(C.c_float)),
           len(t), _dp(x), _dp(y), _dp(z), _ip(t), C.byref(off))
     return e, bool(off.value)
+
+
+def _u8(a):
+    return a.ctypes.data_as(C.POINTER(C.c_uint8))
+
+
+def _xyz(xyz):
+    xyz = np.asarray(xyz, np.float64).reshape(-1, 3)
+    return [np.ascontiguousarray(xyz[:, k]) for k in range(3)]
+
+
+def vdw_radius(anum) -> float:
+    return lib().orc_vdw_radius(int(anum))
+
+
+def clash2(a1, a2) -> float:
+    return lib().orc_clash2(int(a1), int(a2))
+
+
+def masks(g: Lattice, xyz, radius, r_w=1.4):
+    """(vdW volume, solvent shell) uint8 [nz, ny, nx] of Lds.vdW_volume /
+    Lds.first_solvent_shell."""
+    x, y, z = _xyz(xyz)
+    r = np.ascontiguousarray(radius, np.float64)
+    v = np.zeros((g.nz, g.ny, g.nx), np.uint8)
+    sh = np.zeros_like(v)
+    lib().orc_masks(C.byref(g), len(r), _dp(x), _dp(y), _dp(z), _dp(r), C.c_double(r_w), _u8(v),
+                    _u8(sh))
+    return v, sh
+
+
+def protein_ligand_clash(g: Lattice, vdw, xyz) -> bool:
+    x, y, z = _xyz(xyz)
+    v = np.ascontiguousarray(vdw, np.uint8)
+    return bool(lib().orc_protein_ligand_clash(C.byref(g), _u8(v), len(x), _dp(x), _dp(y), _dp(z)))
+
+
+def clash_and(g: Lattice, vdw, p) -> bool:
+    v = np.ascontiguousarray(vdw, np.uint8)
+    pp = np.ascontiguousarray(p, np.float64)
+    return bool(lib().orc_clash_and(C.byref(g), _u8(v), _dp(pp)))
+
+
+def center_occupied(xyz, radius) -> bool:
+    x, y, z = _xyz(xyz)
+    r = np.ascontiguousarray(radius, np.float64)
+    return bool(lib().orc_center_occupied(len(r), _dp(x), _dp(y), _dp(z), _dp(r)))
+
+
+def heavy_atom_clash(prot, xyz, anum) -> bool:
+    P = OMol.of(prot)
+    x, y, z = _xyz(xyz)
+    a = np.ascontiguousarray(anum, np.int32)
+    return bool(lib().orc_heavy_atom_clash(C.byref(P.c), len(a), _dp(x), _dp(y), _dp(z), _ip(a)))
+
+
+def intra_clash(xyz, anum, interacting) -> bool:
+    x, y, z = _xyz(xyz)
+    a = np.ascontiguousarray(anum, np.int32)
+    it = np.ascontiguousarray(interacting, np.uint8)
+    return bool(lib().orc_intra_clash(len(a), _dp(x), _dp(y), _dp(z), _ip(a), _u8(it)))
+
+
+def so3_rotation(n, i):
+    R = np.zeros(9)
+    lib().orc_so3_rotation(int(n), int(i), _dp(R))
+    return R.reshape(3, 3)
+
+
+def dock_scores(g: Lattice, grids, vdw, lig_mol, lig_type, lig_radius, center, radius, step,
+                rotations, const_intra=0.0):
+    """Every exhaustive-docking score (+inf where skipped), in frame order."""
+    L = OMol.of(lig_mol)
+    gr = np.ascontiguousarray(grids, np.float32)
+    v = np.ascontiguousarray(vdw, np.uint8)
+    lt = np.ascontiguousarray(lig_type, np.int32)
+    lr = np.ascontiguousarray(lig_radius, np.float64)
+    c = np.ascontiguousarray(center, np.float64)
+    R = np.ascontiguousarray(rotations, np.float64).reshape(-1, 9)
+    dim = int(np.ceil(2.0 * radius / step)) + 1
+    out = np.zeros(dim ** 3 * len(R))
+    dims = np.zeros(3, np.int32)
+    lib().orc_dock_scores(C.byref(g), gr.ctypes.data_as(C.POINTER(C.c_float)), _u8(v),
+                          C.byref(L.c), _ip(lt), _dp(lr), _dp(c), C.c_double(radius),
+                          C.c_double(step), len(R), _dp(R), C.c_double(const_intra), _ip(dims),
+                          _dp(out))
+    return out, tuple(int(d) for d in dims)
+
+
+def protein_desolv(g: Lattice, prot, shell, center, radius):
+    P = OMol.of(prot)
+    sh = np.ascontiguousarray(shell, np.uint8)
+    c = np.ascontiguousarray(center, np.float64)
+    out = np.zeros((g.nz, g.ny, g.nx))
+    lib().orc_protein_desolv(C.byref(g), C.byref(P.c), _u8(sh), _dp(c), C.c_double(radius),
+                             _dp(out))
+    return out
+
+
+def desolvation_penalty(g: Lattice, contrib, shell, xyz, q, radius, r_w=1.4):
+    x, y, z = _xyz(xyz)
+    pc = np.ascontiguousarray(contrib, np.float64)
+    sh = np.ascontiguousarray(shell, np.uint8)
+    qq = np.ascontiguousarray(q, np.float64)
+    r = np.ascontiguousarray(radius, np.float64)
+    out = np.zeros(2)
+    lib().orc_desolvation_penalty(C.byref(g), _dp(pc), _u8(sh), len(qq), _dp(x), _dp(y), _dp(z),
+                                  _dp(qq), _dp(r), C.c_double(r_w), _dp(out))
+    return float(out[0]), float(out[1])

@@ -886,3 +886,307 @@ void orc_grid_points(const orc_physics *ph, const orc_mol *prot, int n, const do
   free(xt);
   orc_cells_free(cells);
 }
+
+/* ---- lattice masks, clash tests, SO(3) samples, exhaustive docking,
+ *      desolvation ------------------------------------------------------------
+ * The lattice of the grids: point (i, j, k) at o + step (i, j, k), index
+ * i + j nx + k nx ny (src/grid.ml).  Masks are one byte per point. */
+
+#define ORC_PI 3.14159265358979323846
+
+/* Ptable.vdW_radii (src/ptable.ml:41-53); NaN for other elements */
+double orc_vdw_radius(int anum) {
+  switch (anum) {
+    case 1: return 1.2;
+    case 6: return 1.7;
+    case 7: return 1.6;
+    case 8: return 1.55;
+    case 9: return 1.5;
+    case 12: return 2.2;
+    case 15: return 1.95;
+    case 16: return 1.8;
+    case 17: return 1.8;
+    case 35: return 1.9;
+    case 53: return 2.1;
+    default: return NAN;
+  }
+}
+
+/* Ptable.vdW_clash_params2 (src/ptable.ml:62-80): (0.8 (r_i + r_j))^2 */
+double orc_clash2(int a1, int a2) {
+  const double x = 0.8 * (orc_vdw_radius(a1) + orc_vdw_radius(a2));
+  return x * x;
+}
+
+/* Lds.atom_bitmask_set (src/lds.ml:149-169): the points of the cube of
+ * ceil(radius / step) cells about the atom's cell (Grid.coord_of_point:
+ * truncation toward zero) within radius are set to b; points off the lattice
+ * are skipped (the reference has the simulation box's margin for them). */
+void orc_atom_bitmask_set(const orc_lattice *g, const double p[3], double radius, uint8_t b,
+                          uint8_t *mask) {
+  const int ci = (int)((p[0] - g->o[0]) / g->step), cj = (int)((p[1] - g->o[1]) / g->step),
+            ck = (int)((p[2] - g->o[2]) / g->step);
+  const int rs = (int)ceil(radius / g->step);
+  const double r2 = radius * radius;
+  for (int i = ci - rs; i <= ci + rs; ++i) {
+    if (i < 0 || i >= g->nx) continue;
+    const double x = g->o[0] + g->step * i;
+    for (int j = cj - rs; j <= cj + rs; ++j) {
+      if (j < 0 || j >= g->ny) continue;
+      const double y = g->o[1] + g->step * j;
+      for (int k = ck - rs; k <= ck + rs; ++k) {
+        if (k < 0 || k >= g->nz) continue;
+        const double z = g->o[2] + g->step * k;
+        const double dx = p[0] - x, dy = p[1] - y, dz = p[2] - z;
+        if (dx * dx + dy * dy + dz * dz < r2)
+          mask[i + (size_t)j * g->nx + (size_t)k * g->nx * g->ny] = b;
+      }
+    }
+  }
+}
+
+/* Lds.vdW_volume (src/lds.ml:187-196) and Lds.first_solvent_shell
+ * (src/lds.ml:172-184): every point within r_i of an atom; every point within
+ * r_i + r_w of an atom and within r_j of none.  Either output may be NULL. */
+void orc_masks(const orc_lattice *g, int n, const double *x, const double *y, const double *z,
+               const double *radius, double r_w, uint8_t *vdw, uint8_t *shell) {
+  const size_t np = (size_t)g->nx * g->ny * g->nz;
+  if (vdw) {
+    memset(vdw, 0, np);
+    for (int a = 0; a < n; ++a) {
+      const double p[3] = {x[a], y[a], z[a]};
+      orc_atom_bitmask_set(g, p, radius[a], 1, vdw);
+    }
+  }
+  if (shell) {
+    memset(shell, 0, np);
+    for (int a = 0; a < n; ++a) {
+      const double p[3] = {x[a], y[a], z[a]};
+      orc_atom_bitmask_set(g, p, radius[a] + r_w, 1, shell);
+    }
+    for (int a = 0; a < n; ++a) {
+      const double p[3] = {x[a], y[a], z[a]};
+      orc_atom_bitmask_set(g, p, radius[a], 0, shell);
+    }
+  }
+}
+
+/* G3D.vdW_clash_OR / vdW_clash_AND (src/G3D.ml:159-213): the eight corners of
+ * p's cell; a corner off the lattice counts as not set (the reference reads out
+ * of bounds there). */
+static int corner_bits(const orc_lattice *g, const uint8_t *mask, const double p[3], int *all) {
+  const double u = (p[0] - g->o[0]) / g->step, v = (p[1] - g->o[1]) / g->step,
+               w = (p[2] - g->o[2]) / g->step;
+  int any = 0, every = 1;
+  const int i0 = (int)u, j0 = (int)v, k0 = (int)w;
+  for (int c = 0; c < 8; ++c) {
+    const int i = i0 + (c & 1), j = j0 + ((c >> 1) & 1), k = k0 + (c >> 2);
+    int bit = 0;
+    if (u > -1.0 && v > -1.0 && w > -1.0 && i >= 0 && j >= 0 && k >= 0 && i < g->nx &&
+        j < g->ny && k < g->nz && u < 2e9 && v < 2e9 && w < 2e9)
+      bit = mask[i + (size_t)j * g->nx + (size_t)k * g->nx * g->ny] != 0;
+    any |= bit;
+    every &= bit;
+  }
+  *all = every;
+  return any;
+}
+
+int orc_clash_or(const orc_lattice *g, const uint8_t *mask, const double p[3]) {
+  int all;
+  return corner_bits(g, mask, p, &all);
+}
+
+int orc_clash_and(const orc_lattice *g, const uint8_t *mask, const double p[3]) {
+  int all;
+  corner_bits(g, mask, p, &all);
+  return all;
+}
+
+/* Mol.protein_ligand_clash (src/mol.ml:1195-1207): any atom's cell touches the
+ * protein's vdW volume */
+int orc_protein_ligand_clash(const orc_lattice *g, const uint8_t *vdw, int n, const double *x,
+                             const double *y, const double *z) {
+  for (int a = 0; a < n; ++a) {
+    const double p[3] = {x[a], y[a], z[a]};
+    if (orc_clash_or(g, vdw, p)) return 1;
+  }
+  return 0;
+}
+
+/* Mol.is_ligand_center_vdW_occuppied (src/mol.ml:1209-1219) */
+int orc_center_occupied(int n, const double *x, const double *y, const double *z,
+                        const double *radius) {
+  double c[3] = {0, 0, 0};
+  for (int a = 0; a < n; ++a) {
+    c[0] += x[a];
+    c[1] += y[a];
+    c[2] += z[a];
+  }
+  for (int d = 0; d < 3; ++d) c[d] /= n;
+  for (int a = 0; a < n; ++a) {
+    const double dx = c[0] - x[a], dy = c[1] - y[a], dz = c[2] - z[a];
+    if (sqrt(dx * dx + dy * dy + dz * dz) < radius[a]) return 1;
+  }
+  return 0;
+}
+
+/* Mol.heavy_atom_clash (src/mol.ml:1170-1190): a ligand heavy atom (anum > 1)
+ * closer than 0.8 (r_i + r_j) to a protein heavy atom.  The reference
+ * gathers the candidates with a BST query of radius 2 Ptable.vdW_max, whose
+ * value is the intended 4.4 A here (every closer pair is a candidate). */
+int orc_heavy_atom_clash(const orc_mol *prot, int n, const double *x, const double *y,
+                         const double *z, const int *anum) {
+  for (int a = 0; a < n; ++a) {
+    if (anum[a] <= 1) continue;
+    for (int i = 0; i < prot->n; ++i) {
+      if (prot->anum[i] <= 1) continue;
+      const double dx = x[a] - prot->x[i], dy = y[a] - prot->y[i], dz = z[a] - prot->z[i];
+      if (dx * dx + dy * dy + dz * dz < orc_clash2(anum[a], prot->anum[i])) return 1;
+    }
+  }
+  return 0;
+}
+
+/* Mol.ligand_atoms_clash_fast (src/mol.ml:1077-1088): a pair at topological
+ * distance >= 3 closer than 0.8 (r_i + r_j) */
+int orc_intra_clash(int n, const double *x, const double *y, const double *z, const int *anum,
+                    const uint8_t *interacting) {
+  for (int i = 0; i < n; ++i)
+    for (int j = i + 1; j < n; ++j) {
+      if (!interacting[(size_t)i * n + j]) continue;
+      const double dx = x[i] - x[j], dy = y[i] - y[j], dz = z[i] - z[j];
+      if (dx * dx + dy * dy + dz * dz < orc_clash2(anum[i], anum[j])) return 1;
+    }
+  return 0;
+}
+
+/* SO3.super_fibonacci and SO3.rotations (src/SO3.ml:18-46, after Alexa, CVPR
+ * 2022, Algorithm 1): sample i of n as the quaternion
+ * (w, x, y, z) = (sqrt(t) sin(a), sqrt(t) cos(a), sqrt(1-t) sin(b), sqrt(1-t) cos(b)),
+ * s = i + 1/2, t = s / n, a = 2 pi s / sqrt(2), b = 2 pi s / psi, then the
+ * rotation of its axis and angle (Quat.to_axis_angle, Rot.of_axis_angle). */
+void orc_so3_rotation(int n, int i, double R[9]) {
+  const double phi = sqrt(2.0), psi = 1.533751168755204288118041;
+  const double s = (double)i + 0.5, t = s / (double)n, d = 2.0 * ORC_PI * s;
+  const double cr = sqrt(t), cR = sqrt(1.0 - t), al = d / phi, be = d / psi;
+  const double w = cr * sin(al), x = cr * cos(al), y = cR * sin(be), z = cR * cos(be);
+  const double mag = sqrt(x * x + y * y + z * z);
+  const double u[3] = {x / mag, y / mag, z / mag};
+  orc_rot_axis_angle(u, 2.0 * atan2(mag, w), R);
+}
+
+/* Lds.exhaustive_rigid_ligand_docking (src/lds.ml:1040-1114), every score:
+ * positions on the lattice Grid.from_box(trans_step) of the ROI's bounding
+ * cube (x_min + i step, ceil(2 r / step) + 1 points per axis), rotations
+ * R_r (nrot); score[(pos index) nrot + r] = const_intra + the interpolated
+ * inter energy of R_r x + pos, or +inf when pos is outside the ROI, when the
+ * ligand's centre is vdW-occupied and all eight corners of pos's cell are in
+ * the protein's vdW volume, or when the posed ligand clashes with it (any
+ * corner).  Returns the position lattice's points per axis in dims. */
+void orc_dock_scores(const orc_lattice *g, const float *grids, const uint8_t *vdw,
+                     const orc_mol *lig, const int *lig_type, const double *lig_radius,
+                     const double roi_c[3], double roi_r, double trans_step, int nrot,
+                     const double *R, double const_intra, int dims[3], double *scores) {
+  const int n = lig->n;
+  const int center_occ = orc_center_occupied(n, lig->x, lig->y, lig->z, lig_radius);
+  const int dim = (int)ceil(2.0 * roi_r / trans_step) + 1;
+  dims[0] = dims[1] = dims[2] = dim;
+  double *xs = (double *)malloc(sizeof(double) * 3 * (size_t)(n > 0 ? n : 1));
+  double *ys = xs + n, *zs = ys + n;
+  for (int k = 0; k < dim; ++k)
+    for (int j = 0; j < dim; ++j)
+      for (int i = 0; i < dim; ++i) {
+        const double pos[3] = {roi_c[0] - roi_r + trans_step * i, roi_c[1] - roi_r + trans_step * j,
+                               roi_c[2] - roi_r + trans_step * k};
+        const size_t pidx = (size_t)i + (size_t)j * dim + (size_t)k * dim * dim;
+        const double dx = pos[0] - roi_c[0], dy = pos[1] - roi_c[1], dz = pos[2] - roi_c[2];
+        const int skip = !(dx * dx + dy * dy + dz * dz < roi_r * roi_r) ||
+                         (center_occ && orc_clash_and(g, vdw, pos));
+        for (int r = 0; r < nrot; ++r) {
+          double *out = scores + pidx * nrot + r;
+          *out = INFINITY;
+          if (skip) continue;
+          const double *M = R + 9 * (size_t)r;
+          for (int a = 0; a < n; ++a) {
+            xs[a] = M[0] * lig->x[a] + M[1] * lig->y[a] + M[2] * lig->z[a] + pos[0];
+            ys[a] = M[3] * lig->x[a] + M[4] * lig->y[a] + M[5] * lig->z[a] + pos[1];
+            zs[a] = M[6] * lig->x[a] + M[7] * lig->y[a] + M[8] * lig->z[a] + pos[2];
+          }
+          if (orc_protein_ligand_clash(g, vdw, n, xs, ys, zs)) continue;
+          double e = 0.0;
+          const size_t per = (size_t)g->nx * g->ny * g->nz;
+          int off = 0;
+          for (int a = 0; a < n; ++a) {
+            const double p[3] = {xs[a] - g->o[0], ys[a] - g->o[1], zs[a] - g->o[2]};
+            e += orc_trilin(g->step, g->nx, g->ny, g->nz, grids + per * lig_type[a], p, &off);
+          }
+          *out = const_intra + e;
+        }
+      }
+  free(xs);
+}
+
+/* Lds.protein_desolv (src/lds.ml:204-233): for every point of the protein's
+ * solvent shell inside the ROI, C vol sum_j (q_j / d^2)^2 over the protein atoms
+ * within 12 A, C = (1/eps_prot - 1/eps_water) / (8 pi) (src/const.ml:31); 0
+ * elsewhere. */
+double orc_desolv_constant(void) { return (1.0 / 4.0 - 1.0 / 78.5) / (8.0 * ORC_PI); }
+
+void orc_protein_desolv(const orc_lattice *g, const orc_mol *prot, const uint8_t *shell,
+                        const double roi_c[3], double roi_r, double *out) {
+  const double vol = g->step * g->step * g->step;
+  for (int k = 0; k < g->nz; ++k)
+    for (int j = 0; j < g->ny; ++j)
+      for (int i = 0; i < g->nx; ++i) {
+        const size_t idx = i + (size_t)j * g->nx + (size_t)k * g->nx * g->ny;
+        out[idx] = 0.0;
+        if (!shell[idx]) continue;
+        const double p[3] = {g->o[0] + g->step * i, g->o[1] + g->step * j, g->o[2] + g->step * k};
+        const double rx = p[0] - roi_c[0], ry = p[1] - roi_c[1], rz = p[2] - roi_c[2];
+        if (!(rx * rx + ry * ry + rz * rz < roi_r * roi_r)) continue;
+        double s = 0.0;
+        for (int a = 0; a < prot->n; ++a) {
+          const double dx = p[0] - prot->x[a], dy = p[1] - prot->y[a], dz = p[2] - prot->z[a];
+          const double d2 = dx * dx + dy * dy + dz * dz;
+          if (!(d2 < 144.0)) continue;
+          const double v = prot->q[a] / d2;
+          s += v * v;
+        }
+        out[idx] = orc_desolv_constant() * (vol * s);
+      }
+}
+
+/* Lds.desolvation_penalty (src/lds.ml:236-267): the points of both solvent
+ * shells (the protein's and this ligand pose's); out[0] = the protein's
+ * contributions summed over them, out[1] = C vol sum over them of
+ * sum_j (q_j / d^2)^2 over the ligand atoms within 12 A. */
+void orc_desolvation_penalty(const orc_lattice *g, const double *prot_contrib,
+                             const uint8_t *prot_shell, int n, const double *x, const double *y,
+                             const double *z, const double *q, const double *radius, double r_w,
+                             double out[2]) {
+  const size_t np = (size_t)g->nx * g->ny * g->nz;
+  uint8_t *ls = (uint8_t *)malloc(np);
+  orc_masks(g, n, x, y, z, radius, r_w, NULL, ls);
+  const double vol = g->step * g->step * g->step;
+  double pd = 0.0, ld = 0.0;
+  for (int k = 0; k < g->nz; ++k)
+    for (int j = 0; j < g->ny; ++j)
+      for (int i = 0; i < g->nx; ++i) {
+        const size_t idx = i + (size_t)j * g->nx + (size_t)k * g->nx * g->ny;
+        if (!(ls[idx] && prot_shell[idx])) continue;
+        const double p[3] = {g->o[0] + g->step * i, g->o[1] + g->step * j, g->o[2] + g->step * k};
+        for (int a = 0; a < n; ++a) {
+          const double dx = p[0] - x[a], dy = p[1] - y[a], dz = p[2] - z[a];
+          const double d2 = dx * dx + dy * dy + dz * dz;
+          if (d2 < 144.0) {
+            const double v = q[a] / d2;
+            ld += v * v;
+          }
+        }
+        pd += prot_contrib[idx];
+      }
+  free(ls);
+  out[0] = pd;
+  out[1] = orc_desolv_constant() * (vol * ld);
+}

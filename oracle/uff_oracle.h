@@ -140,6 +140,45 @@ double orc_ene_inter_interp(double step, int nx, int ny, int nz, const float *gr
                             const double *x, const double *y, const double *z, const int *type,
                             int *off);
 
+/* lattice of the grids: point (i, j, k) at o + step (i, j, k) */
+typedef struct {
+  double step;
+  int nx, ny, nz;
+  double o[3];
+} orc_lattice;
+
+/* masks, clash tests, SO(3) samples, exhaustive docking, desolvation
+ * (src/lds.ml:149-267, 1040-1114; src/mol.ml:1077-1219; src/G3D.ml:159-213;
+ * src/SO3.ml:18-46; src/ptable.ml:41-80) */
+double orc_vdw_radius(int anum);
+double orc_clash2(int a1, int a2);
+void orc_atom_bitmask_set(const orc_lattice *g, const double p[3], double radius, uint8_t b,
+                          uint8_t *mask);
+void orc_masks(const orc_lattice *g, int n, const double *x, const double *y, const double *z,
+               const double *radius, double r_w, uint8_t *vdw, uint8_t *shell);
+int orc_clash_or(const orc_lattice *g, const uint8_t *mask, const double p[3]);
+int orc_clash_and(const orc_lattice *g, const uint8_t *mask, const double p[3]);
+int orc_protein_ligand_clash(const orc_lattice *g, const uint8_t *vdw, int n, const double *x,
+                             const double *y, const double *z);
+int orc_center_occupied(int n, const double *x, const double *y, const double *z,
+                        const double *radius);
+int orc_heavy_atom_clash(const orc_mol *prot, int n, const double *x, const double *y,
+                         const double *z, const int *anum);
+int orc_intra_clash(int n, const double *x, const double *y, const double *z, const int *anum,
+                    const uint8_t *interacting);
+void orc_so3_rotation(int n, int i, double R[9]);
+void orc_dock_scores(const orc_lattice *g, const float *grids, const uint8_t *vdw,
+                     const orc_mol *lig, const int *lig_type, const double *lig_radius,
+                     const double roi_c[3], double roi_r, double trans_step, int nrot,
+                     const double *R, double const_intra, int dims[3], double *scores);
+double orc_desolv_constant(void);
+void orc_protein_desolv(const orc_lattice *g, const orc_mol *prot, const uint8_t *shell,
+                        const double roi_c[3], double roi_r, double *out);
+void orc_desolvation_penalty(const orc_lattice *g, const double *prot_contrib,
+                             const uint8_t *prot_shell, int n, const double *x, const double *y,
+                             const double *z, const double *q, const double *radius, double r_w,
+                             double out[2]);
+
 #ifdef __cplusplus
 }
 #endif

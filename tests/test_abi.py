@@ -5,6 +5,8 @@ import glob
 import os
 import re
 
+import numpy as np
+
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -50,6 +52,12 @@ def test_null_context_is_rejected(gpu_lib):
     assert gpu_lib.mmo_build_grids(None, None, None) == lib.EINVAL
     assert gpu_lib.mmo_load_grids(None, None, None) == lib.EINVAL
     assert gpu_lib.mmo_set_grid_build(None, 1) == lib.EINVAL
+    assert gpu_lib.mmo_build_masks(None, None, 1.4) == lib.EINVAL
+    assert gpu_lib.mmo_clash_poses(None, 1, None, 0, 7, None) == lib.EINVAL
+    assert gpu_lib.mmo_dock_exhaustive(None, None, None, None, None) == lib.EINVAL
+    assert gpu_lib.mmo_place_in_roi(None, None, 1.0, 1, 0, None, None) == lib.EINVAL
+    assert gpu_lib.mmo_protein_desolv(None, None, 1.0, None) == lib.EINVAL
+    assert gpu_lib.mmo_so3_rotations(-1, None) == lib.EINVAL
     assert gpu_lib.mmo_grid_values(None, None) == lib.EINVAL
     assert gpu_lib.mmo_grid_dims(None, None, None, None, None) == lib.EINVAL
     assert gpu_lib.mmo_grid_device(None, None) == lib.EINVAL
@@ -80,3 +88,14 @@ def test_no_cpu_fallback_when_library_missing(tmp_path):
             lib.load(str(tmp_path / "absent.so"))
     finally:
         lib._lib = saved
+
+
+def test_so3_rotations_need_no_gpu(gpu_lib):
+    """mmo_so3_rotations is host arithmetic: proper rotations, the paper's
+    first sample."""
+    from mmo_gb300.ff import so3_rotations
+
+    R = so3_rotations(16)
+    for M in R:
+        assert np.allclose(M @ M.T, np.eye(3), atol=1e-12) and np.linalg.det(M) > 0
+    assert not np.allclose(R[0], R[1])

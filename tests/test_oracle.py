@@ -299,3 +299,137 @@ def test_grid_points_cells_equal_brute_grid_point(oracle):
         ref = oracle.grid_point(prot, p, ta, tq)
         assert np.allclose(got[k], ref, rtol=1e-12, atol=1e-10)
     assert np.any(got == 100000.0) and np.any(got == 0.0)
+
+
+# ---- masks, clash tests, SO(3) samples, docking, desolvation ----------------
+
+def _small_lattice(oracle, lo=-6.0, n=25, step=0.5):
+    return oracle.lattice(step, (n, n, n), (lo, lo, lo))
+
+
+def test_masks_are_the_sphere_predicates(oracle):
+    """Lds.vdW_volume / first_solvent_shell: the cube walk of atom_bitmask_set
+    equals the plain predicates over every lattice point."""
+    rng = np.random.default_rng(1)
+    g = _small_lattice(oracle)
+    xyz = rng.uniform(-4.0, 4.0, size=(12, 3))
+    r = rng.choice([1.2, 1.55, 1.7, 1.8], size=12)
+    vdw, shell = oracle.masks(g, xyz, r, 1.4)
+    ax = -6.0 + 0.5 * np.arange(25)
+    zz, yy, xx = np.meshgrid(ax, ax, ax, indexing="ij")
+    pts = np.stack([xx, yy, zz], axis=-1)
+    d2 = ((pts[..., None, :] - xyz) ** 2).sum(axis=-1)
+    inside = (d2 < r * r).any(axis=-1)
+    outer = (d2 < (r + 1.4) ** 2).any(axis=-1)
+    assert np.array_equal(vdw.astype(bool), inside)
+    assert np.array_equal(shell.astype(bool), outer & ~inside)
+
+
+def test_clash_params_and_corner_tests(oracle):
+    # Ptable.vdW_clash_params2: (0.8 (r_i + r_j))^2
+    assert oracle.clash2(6, 8) == pytest.approx((0.8 * (1.7 + 1.55)) ** 2, rel=1e-15)
+    assert oracle.clash2(1, 1) == pytest.approx((0.8 * 2.4) ** 2, rel=1e-15)
+    g = _small_lattice(oracle)
+    m = np.zeros((25, 25, 25), np.uint8)
+    m[10, 10, 10] = 1  # one set point at (-1, -1, -1)
+    assert oracle.protein_ligand_clash(g, m, [[-1.2, -1.2, -1.2]])   # cell (9, 9, 9) touches it
+    assert not oracle.protein_ligand_clash(g, m, [[-1.7, -1.7, -1.7]])
+    assert not oracle.clash_and(g, m, [-1.2, -1.2, -1.2])
+    m[10:12, 10:12, 10:12] = 1
+    assert oracle.clash_and(g, m, [-0.8, -0.8, -0.8])
+
+
+def test_super_fibonacci_rotations_match_the_paper_formula(oracle):
+    """SO3.super_fibonacci (Alexa 2022, Algorithm 1) restated in NumPy,
+    through the quaternion's rotation matrix; proper rotations."""
+    n = 50
+    psi = 1.533751168755204288118041
+    for i in (0, 1, 7, 49):
+        s = i + 0.5
+        t = s / n
+        d = 2.0 * np.pi * s
+        w, x = np.sqrt(t) * np.sin(d / np.sqrt(2.0)), np.sqrt(t) * np.cos(d / np.sqrt(2.0))
+        y, z = np.sqrt(1 - t) * np.sin(d / psi), np.sqrt(1 - t) * np.cos(d / psi)
+        Rq = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                       [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                       [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+        R = oracle.so3_rotation(n, i)
+        assert np.allclose(R, Rq, atol=1e-12)
+        assert np.allclose(R @ R.T, np.eye(3), atol=1e-12) and np.linalg.det(R) > 0
+
+
+def test_heavy_and_intra_clash(oracle):
+    from mmo_gb300 import synth
+    from mmo_gb300.topology import Mol
+
+    rad = {1: 1.2, 6: 1.7, 7: 1.6, 8: 1.55, 16: 1.8}
+    for seed in range(6):
+        lig = synth.random_ligand(np.random.default_rng(seed), 10, 2)
+        it = lig.interacting
+        for scale in (1.0, 1.3, 2.0):
+            xyz = lig.xyz() * scale
+            r = np.array([rad[int(a)] for a in lig.anum])
+            d2 = ((xyz[:, None] - xyz[None]) ** 2).sum(axis=-1)
+            want = bool(np.any(np.triu(it.astype(bool), 1) &
+                               (d2 < (0.8 * (r[:, None] + r[None])) ** 2)))
+            assert oracle.intra_clash(xyz, lig.anum, it) == want
+        assert not oracle.intra_clash(lig.xyz() * 2.0, lig.anum, it)
+    z = np.zeros(1)
+    prot = Mol("p", np.array([0.0]), z.copy(), z.copy(), z.copy(), np.array([6], np.int32), None)
+    near = np.array([[2.0, 0.0, 0.0]])
+    assert oracle.heavy_atom_clash(prot, near, [8])            # 2.0 < 0.8 (1.7 + 1.55) = 2.6
+    assert not oracle.heavy_atom_clash(prot, near, [1])        # hydrogens are not tested
+    assert not oracle.heavy_atom_clash(prot, [[2.7, 0.0, 0.0]], [8])
+
+
+def test_dock_scores_are_interpolated_energies(oracle):
+    """Every unskipped exhaustive-docking score is const + the interpolated
+    energy of its pose (the grid oracle), skipped ones are the clashing poses."""
+    from mmo_gb300 import grids as GR
+    from mmo_gb300 import synth
+
+    s = synth.docking_site(seed=3, n_pocket=600, n_atoms=8, n_rot=1)
+    types, (lt,) = GR.type2id([s.ligand])
+    g = oracle.lattice(0.5, (41, 41, 41), (-10.0, -10.0, -10.0))
+    rng = np.random.default_rng(0)
+    grids = rng.normal(size=(len(types), 41, 41, 41)).astype(np.float32)
+    vdw, _ = oracle.masks(g, s.pocket.xyz(), s.pocket.radius)
+    R = np.stack([oracle.so3_rotation(6, i) for i in range(6)])
+    sc, dims = oracle.dock_scores(g, grids, vdw, s.ligand, lt, s.ligand.radius, [0.0, 0.0, 0.0],
+                                  1.0, 0.5, R, const_intra=2.5)
+    assert dims == (5, 5, 5)
+    ok = np.isfinite(sc)
+    assert ok.any() and not ok.all()
+    for f in np.flatnonzero(ok)[:10]:
+        p, r = divmod(int(f), 6)
+        i, j, k = p % 5, (p // 5) % 5, p // 25
+        pos = np.array([-1.0 + 0.5 * i, -1.0 + 0.5 * j, -1.0 + 0.5 * k])
+        xyz = s.ligand.xyz() @ R[r].T + pos
+        e, off = oracle.ene_inter_interp(0.5, (41, 41, 41), grids, xyz + 10.0, lt)
+        assert sc[f] == pytest.approx(2.5 + e, rel=1e-12, abs=1e-12)
+        assert not oracle.protein_ligand_clash(g, vdw, xyz)
+
+
+def test_desolvation_is_the_sum_over_shell_points(oracle):
+    from mmo_gb300 import synth
+
+    s = synth.docking_site(seed=4, n_pocket=400, n_atoms=8, n_rot=1)
+    g = oracle.lattice(0.5, (41, 41, 41), (-10.0, -10.0, -10.0))
+    _, shell = oracle.masks(g, s.pocket.xyz(), s.pocket.radius)
+    C_ = (1.0 / 4.0 - 1.0 / 78.5) / (8.0 * np.pi)
+    contrib = oracle.protein_desolv(g, s.pocket, shell, [0.0, 0.0, 0.0], 8.0)
+    k, j, i = np.argwhere(contrib > 0)[0]
+    p = -10.0 + 0.5 * np.array([i, j, k])
+    d2 = ((s.pocket.xyz() - p) ** 2).sum(axis=1)
+    want = C_ * 0.125 * np.sum(np.where(d2 < 144.0, (s.pocket.q / d2) ** 2, 0.0))
+    assert contrib[k, j, i] == pytest.approx(want, rel=1e-12)
+    assert np.all(contrib[shell == 0] == 0.0)
+    xyz = s.ligand.xyz() + np.array([0.5, 0.0, 0.0])
+    prot, lig = oracle.desolvation_penalty(g, contrib, shell, xyz, s.ligand.q, s.ligand.radius)
+    _, lshell = oracle.masks(g, xyz, s.ligand.radius)
+    both = (lshell > 0) & (shell > 0)
+    assert prot == pytest.approx(contrib[both].sum(), rel=1e-12)
+    pts = np.argwhere(both)[:, ::-1] * 0.5 - 10.0
+    d2 = ((pts[:, None, :] - xyz) ** 2).sum(axis=-1)
+    want = C_ * 0.125 * np.sum(np.where(d2 < 144.0, (s.ligand.q / d2) ** 2, 0.0))
+    assert lig == pytest.approx(want, rel=1e-10)
