@@ -67,6 +67,15 @@ int mmo_grid_values(mmo_ctx* ctx, float* values);
 int mmo_grid_dims(const mmo_ctx* ctx, int* ntypes, int* nx, int* ny, int* nz);
 int mmo_grid_device(const mmo_ctx* ctx, const float** d_values);
 
+/* Plain drop-in for the closure Mol.ene_inter_UFF_interp grid ff_comps
+ * (src/lds.ml:1975, src/mol.ml:1010-1020): the interpolated inter energy of
+ * one ligand (any n <= 128 atoms) at the given coordinates, its atoms typed by
+ * (element, charge) among the grid types (MMO_EINVAL for an atom of no grid
+ * type).  *status (may be NULL) receives MMO_S_OFF_GRID when a corner of an
+ * atom's cell is off the lattice (that atom adds 0). */
+int mmo_ene_inter_grid(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
+                       const double* q, const int* anum, double* out, int* status);
+
 /* Type of each atom of the ligand of mmo_set_ligand among the grid types
  * (out[n]); MMO_EINVAL when an atom's (element, charge) is not a grid type,
  * which also makes MMO_F_GRID scoring fail. */

@@ -2677,6 +2677,64 @@ int mmo_grid_device(const mmo_ctx* ctx, const float** d_values) {
   return MMO_OK;
 }
 
+int mmo_ene_inter_grid(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
+                       const double* q, const int* anum, double* out, int* status) {
+  if (!ctx) return MMO_EINVAL;
+  if (n < 0 || n > kMaxLig || !out || (n > 0 && (!xs || !ys || !zs || !q || !anum)))
+    return fail(ctx, MMO_EINVAL, "mmo_ene_inter_grid: bad arguments (n <= %d)", kMaxLig);
+  if (!ctx->grid_ok) return fail(ctx, MMO_ESTATE, "mmo_ene_inter_grid: no grids");
+  if (status) *status = 0;
+  if (n == 0) {
+    *out = 0.0;
+    return MMO_OK;
+  }
+  // staging: X[n][2] float4 | type[n] int ; output: E parts [n] | E | status
+  size_t off = 0;
+  const size_t oX = take(off, sizeof(float4) * 2 * n);
+  const size_t ot = take(off, sizeof(int) * n);
+  const size_t in_bytes = off;
+  size_t ooff = 0;
+  const size_t oEp = take(ooff, sizeof(double) * n);
+  const size_t oE = take(ooff, sizeof(double));
+  const size_t oS = take(ooff, sizeof(int));
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  int r = grow_host(ctx, &ctx->h_in, &ctx->d_in, &ctx->cap_in, in_bytes);
+  if (r) return r;
+  if ((r = grow_host(ctx, &ctx->h_out, &ctx->d_out, &ctx->cap_out, ooff))) return r;
+  float4* hX = reinterpret_cast<float4*>(ctx->h_in + oX);
+  int* ht = reinterpret_cast<int*>(ctx->h_in + ot);
+  const int nt = (int)ctx->grid_anum.size();
+  for (int i = 0; i < n; ++i) {
+    int t = -1;
+    for (int l = 0; l < nt && t < 0; ++l)
+      if (ctx->grid_anum[l] == anum[i] && ctx->grid_q[l] == q[i]) t = l;
+    if (t < 0)
+      return fail(ctx, MMO_EINVAL, "mmo_ene_inter_grid: atom %d (element %d, charge %.9g) has no "
+                  "grid type", i, anum[i], q[i]);
+    split_store(&hX[2 * i], xs[i] - ctx->origin[0], ys[i] - ctx->origin[1],
+                zs[i] - ctx->origin[2], 0.f);
+    ht[i] = t;
+  }
+  double* dEp = reinterpret_cast<double*>(ctx->d_out + oEp);
+  int* dS = reinterpret_cast<int*>(ctx->d_out + oS);
+  MMO_CK(cudaMemcpyAsync(ctx->d_in, ctx->h_in, in_bytes, cudaMemcpyHostToDevice, ctx->stream),
+         "H2D");
+  MMO_CK(cudaMemsetAsync(dS, 0, sizeof(int), ctx->stream), "status reset");
+  MMO_CK(launch_grid_inter(grid_look(ctx), reinterpret_cast<const float4*>(ctx->d_in + oX), n, n,
+                           reinterpret_cast<const int*>(ctx->d_in + ot), ctx->d_grid, dEp, nullptr,
+                           dS, 0, ctx->stream),
+         "grid lookup kernel");
+  MMO_CK(launch_reduce_plain(dEp, n, reinterpret_cast<double*>(ctx->d_out + oE), ctx->stream),
+         "reduce kernel");
+  MMO_CK(cudaMemcpyAsync(ctx->h_out + oE, ctx->d_out + oE, ooff - oE, cudaMemcpyDeviceToHost,
+                         ctx->stream),
+         "D2H");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync");
+  memcpy(out, ctx->h_out + oE, sizeof(double));
+  if (status) memcpy(status, ctx->h_out + oS, sizeof(int));
+  return MMO_OK;
+}
+
 int mmo_grid_atom_types(mmo_ctx* ctx, int* out) {
   if (!ctx) return MMO_EINVAL;
   if (!out) return fail(ctx, MMO_EINVAL, "mmo_grid_atom_types: out is NULL");

@@ -320,6 +320,15 @@ class UFFScorer:
         return {"points": v[0].value, "pairs_evaluated": v[1].value,
                 "pairs_within_cutoff": v[2].value}
 
+    def ene_inter_grid(self, lig: Mol):
+        """Mol.ene_inter_UFF_interp on the context's grids: (energy, status)."""
+        x, y, z, q = (_f64(v) for v in (lig.x, lig.y, lig.z, lig.q))
+        an = np.ascontiguousarray(lig.anum, np.int32)
+        out, st = C.c_double(), C.c_int()
+        self._check(self._lib.mmo_ene_inter_grid(self._h, lig.n, _dp(x), _dp(y), _dp(z), _dp(q),
+                                                 _ip(an), C.byref(out), C.byref(st)))
+        return out.value, st.value
+
     def grid_atom_types(self) -> np.ndarray:
         """Grid type of each ligand atom (Mol.get_typ)."""
         out = np.zeros(self.ligand.n, np.int32)
@@ -512,6 +521,34 @@ def ene_inter_builder(prot: Mol, ff_style: str = "Bst", device: int = 0,
         return s.ene_inter(lig)
 
     ene_inter.scorer = s
+    return ene_inter
+
+
+def ene_inter_interp_builder(prot: Mol, ligands, step=0.5, margin=36.0, roi=None,
+                             device: int = 0, physics: Physics = Physics()):
+    """``ff1`` of src/lds.ml:1963-1975 on the GPU: the per-type grids of the
+    ligands' (element, charge) types built from prot (Grid.from_box over the
+    protein's box plus margin; mask sphere of the ROI (centre, outer radius)
+    plus 24 A when roi is given), then the closure
+    Mol.ene_inter_UFF_interp grid ff_comps : Mol -> float."""
+    from . import grids as GR
+
+    s = UFFScorer(device, physics)
+    s.set_protein(prot)
+    types, _ = GR.type2id(list(ligands))
+    p = prot.xyz()
+    origin, dims = GR.lattice_from_box(step, p.min(axis=0) - margin, p.max(axis=0) + margin)
+    if roi is not None:
+        s.build_grids(step, dims, origin, types, mask_center=roi[0],
+                      mask_radius=GR.roi_mask_radius(roi[1]))
+    else:
+        s.build_grids(step, dims, origin, types)
+
+    def ene_inter(lig: Mol) -> float:
+        return s.ene_inter_grid(lig)[0]
+
+    ene_inter.scorer = s
+    ene_inter.types = types
     return ene_inter
 
 

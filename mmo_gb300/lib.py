@@ -115,6 +115,7 @@ SIGNATURES = {
     "mmo_grid_device": (_i, [_vp, _P(_vp)]),
     "mmo_grid_atom_types": (_i, [_vp, _P(_i)]),
     "mmo_grid_build_stats": (_i, [_vp, _P(_d), _P(_d), _P(_d)]),
+    "mmo_ene_inter_grid": (_i, [_vp, _i, _P(_d), _P(_d), _P(_d), _P(_d), _P(_i), _P(_d), _P(_i)]),
     "mmo_build_masks": (_i, [_vp, _P(_d), _d]),
     "mmo_load_masks": (_i, [_vp, _P(C.c_uint8), _P(C.c_uint8)]),
     "mmo_mask_values": (_i, [_vp, _P(C.c_uint8), _P(C.c_uint8)]),

@@ -26,6 +26,12 @@ external score_poses_raw :
   ctx -> float array -> int -> int -> float array * float array * int array
   = "mmo_ocaml_score_poses"
 external score_config : ctx -> float array -> float = "mmo_ocaml_score_config"
+external build_grids_raw :
+  ctx -> float array -> int array -> int array -> float array -> float array -> float -> unit
+  = "mmo_ocaml_build_grids_byte" "mmo_ocaml_build_grids"
+external ene_inter_grid_raw :
+  ctx -> float array -> float array -> float array -> float array -> int array -> float
+  = "mmo_ocaml_ene_inter_grid_byte" "mmo_ocaml_ene_inter_grid"
 
 let () = Callback.register_exception "Mol.Too_long" Mol.Too_long
 
@@ -96,3 +102,24 @@ let score_configs ?(recenter = false) (confs: float array array) =
   let flags = f_inter lor f_intra lor f_grad lor (if recenter then f_recenter else 0) in
   let e, g, st = score_poses_raw c flat nd flags in
   (e, Array.init (Array.length e) (fun b -> Array.sub g (b * nd) nd), st)
+
+(* drop-in for [ff1] of lds.ml:1963-1975: the per-type grids of [types]
+ * (Mol.get_all_vdW_elec_types's (anum, charge) pairs, in type order) built on
+ * the GPU over [grid] (Grid.from_box; lowest point at the origin of the
+ * simulation box) with the ROI mask of Lds.bitmask_ROI_only, then
+ * Mol.ene_inter_UFF_interp grid ff_comps : Mol.t -> float *)
+let ene_inter_interp_builder (prot: Mol.t) (grid: Grid.t) (types: (int * float) array)
+    (roi_center: float * float * float) (roi_out_radius: float) =
+  let ready = ref false in
+  fun (lig: Mol.t) ->
+    let c = get_ctx () in
+    if not !ready then begin
+      set_protein c prot;
+      let cx, cy, cz = roi_center in
+      build_grids_raw c [| grid.Grid.step; 0.0; 0.0; 0.0 |]
+        [| grid.Grid.x_dim; grid.Grid.y_dim; grid.Grid.z_dim |]
+        (Array.map fst types) (Array.map snd types)
+        [| cx; cy; cz; roi_out_radius +. 2.0 *. 12.0 |] 100_000.0;
+      ready := true
+    end;
+    ene_inter_grid_raw c lig.Mol.xs lig.Mol.ys lig.Mol.zs lig.Mol.q_a lig.Mol.elt_a

@@ -23,7 +23,7 @@
 #include <stdint.h>
 #include <stdlib.h>
 
-#include "mmo_gpu.h"
+#include "mmo_grid.h"
 
 #define Ctx_val(v) (*((mmo_ctx **)Data_custom_val(v)))
 #define Doubles(v) ((double *)(v))
@@ -197,4 +197,60 @@ CAMLprim value mmo_ocaml_score_config(value ctx, value conf) {
     caml_failwith("Mol.Too_long");
   }
   CAMLreturn(caml_copy_double(E));
+}
+
+/* Lds.pre_calculate_FF_components_grid on the GPU (mmo_build_grids):
+ * lattice = [| step; origin x; y; z |], dims = [| nx; ny; nz |], the types'
+ * atomic numbers and charges (Mol.get_all_vdW_elec_types), mask =
+ * [| cx; cy; cz; radius |] (radius <= 0: no mask), max_E. */
+CAMLprim value mmo_ocaml_build_grids(value ctx, value lattice, value dims, value type_anum,
+                                     value type_q, value mask, value max_e) {
+  CAMLparam5(ctx, lattice, dims, type_anum, type_q);
+  CAMLxparam2(mask, max_e);
+  mmo_ctx *c = Ctx_val(ctx);
+  mmo_grid_spec sp;
+  int *ta = c_ints(type_anum), i, rc;
+  sp.step = Double_flat_field(lattice, 0);
+  for (i = 0; i < 3; ++i) {
+    sp.origin[i] = Double_flat_field(lattice, 1 + i);
+    sp.mask_center[i] = Double_flat_field(mask, i);
+  }
+  sp.nx = Int_val(Field(dims, 0));
+  sp.ny = Int_val(Field(dims, 1));
+  sp.nz = Int_val(Field(dims, 2));
+  sp.mask_radius = Double_flat_field(mask, 3);
+  sp.max_E = Double_val(max_e);
+  sp.ntypes = (int)Wosize_val(type_anum);
+  sp.type_anum = ta;
+  sp.type_q = Doubles(type_q);
+  rc = mmo_build_grids(c, &sp, NULL);
+  free(ta);
+  check(c, rc);
+  CAMLreturn(Val_unit);
+}
+
+CAMLprim value mmo_ocaml_build_grids_byte(value *argv, int argn) {
+  (void)argn;
+  return mmo_ocaml_build_grids(argv[0], argv[1], argv[2], argv[3], argv[4], argv[5], argv[6]);
+}
+
+/* Mol.ene_inter_UFF_interp grid ff_comps on the context's grids */
+CAMLprim value mmo_ocaml_ene_inter_grid(value ctx, value xs, value ys, value zs, value q,
+                                        value anum) {
+  CAMLparam5(ctx, xs, ys, zs, q);
+  CAMLxparam1(anum);
+  mmo_ctx *c = Ctx_val(ctx);
+  double e = 0.0;
+  int st = 0;
+  int *an = c_ints(anum);
+  int rc = mmo_ene_inter_grid(c, n_floats(xs), Doubles(xs), Doubles(ys), Doubles(zs), Doubles(q),
+                              an, &e, &st);
+  free(an);
+  check(c, rc);
+  CAMLreturn(caml_copy_double(e));
+}
+
+CAMLprim value mmo_ocaml_ene_inter_grid_byte(value *argv, int argn) {
+  (void)argn;
+  return mmo_ocaml_ene_inter_grid(argv[0], argv[1], argv[2], argv[3], argv[4], argv[5]);
 }

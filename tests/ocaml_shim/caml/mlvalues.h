@@ -13,6 +13,7 @@ typedef uintptr_t mlsize_t;
 #define Field(x, i) (((value *)(x))[i])
 #define Wosize_val(x) (((uintptr_t *)(x))[-1] >> 10)
 #define Double_flat_field(v, i) (((double *)(v))[i])
+#define Double_val(v) (*(double *)(v))
 #define Store_double_flat_field(v, i, d) (((double *)(v))[i] = (d))
 #define Bytes_val(x) ((unsigned char *)(x))
 #define Store_field(b, i, v) (Field(b, i) = (v))

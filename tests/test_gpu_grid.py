@@ -246,3 +246,24 @@ def test_mc_chains_on_grids(scorer_factory, system, lattice):
     # the grid energies differ from the pair sums (an interpolation), not wildly
     Ep, _, _ = s.score_poses(dn, recenter=True)
     assert np.all(np.isfinite(Ep))
+
+
+def test_plain_interp_closure_matches_oracle(oracle, gpu_lib, system, lattice):
+    """ene_inter_interp_builder: the closure of src/lds.ml:1975 on posed ligands."""
+    from mmo_gb300.ff import ene_inter_interp_builder
+
+    origin, dims = lattice
+    f = ene_inter_interp_builder(system.pocket, [system.ligand], step=STEP, margin=3.0)
+    s = f.scorer
+    g = s.grid_values()
+    nt, nx, ny, nz = g.shape
+    _, lt = _types(system.ligand)
+    p = system.pocket.xyz()
+    o2, d2 = GR.lattice_from_box(STEP, p.min(axis=0) - 3.0, p.max(axis=0) + 3.0)
+    for conf in system.poses[:6]:
+        xyz, _ = oracle.apply_config(system.ligand, conf.astype(np.float64), 0)
+        e = f(system.ligand.with_xyz(xyz))
+        e64, off = oracle.ene_inter_interp(STEP, d2, g, xyz - o2, lt)
+        assert not off
+        assert e == pytest.approx(e64, rel=1e-9, abs=1e-9)
+    f.scorer.close()

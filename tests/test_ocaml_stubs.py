@@ -22,10 +22,11 @@ def test_ocaml_stub_compiles_against_abi(tmp_path):
     syms = subprocess.run(["nm", str(out)], capture_output=True, text=True).stdout
     for name in ("mmo_ocaml_create", "mmo_ocaml_set_protein", "mmo_ocaml_set_ligand_byte",
                  "mmo_ocaml_ene_inter", "mmo_ocaml_ene_intra", "mmo_ocaml_score_poses",
-                 "mmo_ocaml_score_config"):
+                 "mmo_ocaml_score_config", "mmo_ocaml_build_grids", "mmo_ocaml_ene_inter_grid"):
         assert " T " + name in syms, name
     # every ABI call the stubs make is a symbol the library exports
-    for call in ("mmo_ctx_create", "mmo_set_ligand", "mmo_ene_inter", "mmo_score_poses"):
+    for call in ("mmo_ctx_create", "mmo_set_ligand", "mmo_ene_inter", "mmo_score_poses",
+                 "mmo_build_grids", "mmo_ene_inter_grid"):
         assert " U " + call in syms
 
 
