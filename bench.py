@@ -614,7 +614,7 @@ def run_grid(args):
     return 0
 
 
-def _dock_launches(poses, k, per_block=4096):
+def _dock_launches(poses, k, per_block=2048):
     """Kernels of one mmo_dock_exhaustive: the sweep, then the top-k merges."""
     n = -(-poses // per_block) * k
     launches = 1
@@ -687,8 +687,9 @@ def run_dock(args):
                    "grids": "%dx%dx%d x %d types, built in %.2f ms" %
                             (dims[0], dims[1], dims[2], len(types), grid_ms),
                    "masks_s": mask_s, "scored": res["scored"], "clashed": res["clashed"],
-                   "precision": "FP64 rotation and lattice coordinates, FP32 trilinear terms, "
-                                "FP64 sum per pose",
+                   "precision": "rotated atoms in lattice units as float pairs (FP64 once per "
+                                "rotation and atom), float-pair cell fractions, FP32 trilinear "
+                                "terms, compensated FP32 sum per pose",
                    "l2": "grids %.2f GB (> L2); the poses touch a small region of them, read "
                          "again by every call (not flushed)" %
                          (4.0 * len(types) * dims[0] * dims[1] * dims[2] / 1e9)},

@@ -184,6 +184,8 @@ struct mmo_ctx {
   std::vector<int> cull_perm;         // row position -> mmo_set_protein index
   bool masks_ok = false;
   uint8_t* d_vdw = nullptr;           // [points]
+  uint8_t* d_vcell = nullptr;         // [points] cell masks of the vdW volume (any / all corners)
+  size_t cap_vcell = 0;
   uint8_t* d_shell = nullptr;         // [points]
   size_t cap_vdw = 0, cap_shell = 0;
   bool desolv_ok = false;
@@ -1517,6 +1519,7 @@ int mmo_ctx_destroy(mmo_ctx* ctx) {
   cudaFree(ctx->d_grid);
   cudaFree(ctx->d_grid_lt);
   cudaFree(ctx->d_vdw);
+  cudaFree(ctx->d_vcell);
   cudaFree(ctx->d_shell);
   cudaFree(ctx->d_desolv);
   cudaFree(ctx->d_lradius);
@@ -2812,6 +2815,7 @@ int mmo_build_masks(mmo_ctx* ctx, const double* radius, double r_water) {
   int r;
   if ((r = grow(ctx, (void**)&ctx->d_vdw, &ctx->cap_vdw, np, "vdW mask"))) return r;
   if ((r = grow(ctx, (void**)&ctx->d_shell, &ctx->cap_shell, np, "solvent shell mask"))) return r;
+  if ((r = grow(ctx, (void**)&ctx->d_vcell, &ctx->cap_vcell, np, "vdW cell mask"))) return r;
   char* d_tab = nullptr;
   MMO_CK(cudaMalloc((void**)&d_tab, (sizeof(double) + sizeof(float)) * (size_t)P), "radii");
   cudaError_t e = cudaMemcpy(d_tab, rd.data(), sizeof(double) * P, cudaMemcpyHostToDevice);
@@ -2830,6 +2834,7 @@ int mmo_build_masks(mmo_ctx* ctx, const double* radius, double r_water) {
   if (e == cudaSuccess)
     e = launch_masks(ctx->cull, mb, reinterpret_cast<const double*>(d_tab), ctx->d_vdw,
                      ctx->d_shell, ctx->stream);
+  if (e == cudaSuccess) e = launch_cell_masks(grid_look(ctx), ctx->d_vdw, ctx->d_vcell, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   cudaFree(d_tab);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "mask build");
@@ -2852,6 +2857,9 @@ int mmo_load_masks(mmo_ctx* ctx, const uint8_t* vdw, const uint8_t* shell) {
   if ((r = grow(ctx, (void**)&ctx->d_shell, &ctx->cap_shell, np, "solvent shell mask"))) return r;
   MMO_CK(cudaMemcpy(ctx->d_vdw, vdw, np, cudaMemcpyHostToDevice), "vdW mask upload");
   MMO_CK(cudaMemcpy(ctx->d_shell, shell, np, cudaMemcpyHostToDevice), "shell mask upload");
+  if ((r = grow(ctx, (void**)&ctx->d_vcell, &ctx->cap_vcell, np, "vdW cell mask"))) return r;
+  MMO_CK(launch_cell_masks(grid_look(ctx), ctx->d_vdw, ctx->d_vcell, ctx->stream), "cell masks");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync after mask upload");
   ctx->masks_ok = true;
   ctx->desolv_ok = false;
   ++ctx->epoch;
@@ -2971,6 +2979,12 @@ int mmo_dock_exhaustive(mmo_ctx* ctx, const mmo_dock_spec* sp, double* top_score
   }
   // the position lattice (Grid.from_box trans_step of the ROI's cube), kept inside the ROI
   const double r = sp->roi_radius, step = sp->trans_step;
+  for (int d = 0; d < 3; ++d) {
+    const double lo = (sp->roi_center[d] - r - ctx->grid_origin[d]) / ctx->grid_step;
+    const double hi = (sp->roi_center[d] + r - ctx->grid_origin[d]) / ctx->grid_step;
+    if (!(std::fabs(lo) < 1e6) || !(std::fabs(hi) < 1e6))
+      return fail(ctx, MMO_EINVAL, "mmo_dock_exhaustive: the ROI is far off the grids' lattice");
+  }
   const long long pdim = (long long)std::ceil(2.0 * r / step) + 1;
   if (pdim * pdim * pdim > (long long)INT32_MAX)
     return fail(ctx, MMO_EINVAL, "mmo_dock_exhaustive: too many positions");
@@ -2999,6 +3013,9 @@ int mmo_dock_exhaustive(mmo_ctx* ctx, const mmo_dock_spec* sp, double* top_score
   const size_t o_c0 = take(off, 2 * sizeof(unsigned long long) * ncand);
   const size_t o_c1 = take(off, 2 * sizeof(unsigned long long) * ncand);
   const size_t o_cnt = take(off, 2 * sizeof(unsigned long long));
+  const size_t o_off = take(off, sizeof(float) * 6 * (size_t)nrot * L);
+  const size_t o_pc = take(off, sizeof(float4) * 2 * std::max<size_t>(pos.size(), 1));
+  const size_t o_pk = take(off, sizeof(int) * 2 * std::max<size_t>(pos.size(), 1));
   int rc;
   if ((rc = grow(ctx, &ctx->d_dock, &ctx->cap_dock, off, "docking buffers"))) return rc;
   char* base = static_cast<char*>(ctx->d_dock);
@@ -3015,8 +3032,11 @@ int mmo_dock_exhaustive(mmo_ctx* ctx, const mmo_dock_spec* sp, double* top_score
   a.lig_type = ctx->d_grid_lt;
   a.grids = ctx->d_grid;
   a.g = grid_look(ctx);
-  a.vdw = ctx->d_vdw;
+  a.vcell = ctx->d_vcell;
   a.rot = reinterpret_cast<const double*>(base + o_rot);
+  a.off = reinterpret_cast<float*>(base + o_off);
+  a.pcell = reinterpret_cast<float4*>(base + o_pc);
+  a.pcell_k = reinterpret_cast<int*>(base + o_pk);
   a.pos_idx = reinterpret_cast<const int*>(base + o_pos);
   a.L = L;
   a.npos = (int)pos.size();

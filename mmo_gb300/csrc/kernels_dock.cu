@@ -149,6 +149,26 @@ __global__ void __launch_bounds__(kWarps * 32) k_masks(DevCull cull, MaskBuild m
   if (shell) shell[idx] = (in_out && !in_vdw) ? 1 : 0;
 }
 
+// Per cell (i, j, k) of the lattice: bit 0 = any of its eight corners in the
+// mask (G3D.vdW_clash_OR), bit 1 = all of them (vdW_clash_AND); corners off the
+// lattice count as not set.
+__global__ void k_cell_masks(GridLook g, const uint8_t* __restrict__ mask, uint8_t* cell) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = (long long)g.nx * g.ny * g.nz;
+  if (t >= n) return;
+  const int i = (int)(t % g.nx), j = (int)((t / g.nx) % g.ny), k = (int)(t / ((long long)g.nx * g.ny));
+  bool any = false, every = true;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int ii = i + (c & 1), jj = j + ((c >> 1) & 1), kk = k + (c >> 2);
+    const bool bit = ii < g.nx && jj < g.ny && kk < g.nz &&
+                     mask[ii + (size_t)jj * g.nx + (size_t)kk * g.nx * g.ny] != 0;
+    any = any || bit;
+    every = every && bit;
+  }
+  cell[t] = (any ? 1 : 0) | (every ? 2 : 0);
+}
+
 // ---- clash tests of posed ligands ------------------------------------------------
 // Protein heavy atoms within kHeavyClashMax of (x, y, z) (device frame) that
 // clash with a ligand atom of type lt: rows whose (y, z) box is that close,
@@ -245,18 +265,96 @@ __device__ void block_sort(unsigned long long* sk, unsigned long long* sf, int n
   __syncthreads();
 }
 
-// One thread per pose: the ligand rotated (FP64) and put at the position, the
-// eight-corner vdW test of every atom (a clash ends the pose), then the
-// trilinear interpolation of each atom's grid (FP64 lattice coordinates, FP32
-// weights and values, FP64 sum over the atoms).
+// The rotated ligand in lattice units, once per (rotation, atom):
+// off[r][a] = R_r x_a / step as float pairs (hi x, y, z, lo x, y, z); rotation
+// and scaling in FP64.
+__global__ void k_dock_offsets(DockArgs a) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < a.npos) {
+    // the position's lattice coordinate: cell and float-pair fraction per axis
+    const int pi = a.pos_idx[t];
+    const int ii = pi % a.pdim, jj = (pi / a.pdim) % a.pdim, kk = pi / (a.pdim * a.pdim);
+    const double up[3] = {(a.p0[0] + a.pstep * ii - a.g.o[0]) * a.g.inv,
+                          (a.p0[1] + a.pstep * jj - a.g.o[1]) * a.g.inv,
+                          (a.p0[2] + a.pstep * kk - a.g.o[2]) * a.g.inv};
+    float4* P = a.pcell + 2 * (size_t)t;
+    float v[6];
+    int c[3];
+    for (int d = 0; d < 3; ++d) {
+      const double fu = floor(up[d]);
+      c[d] = (int)fu;
+      const double w = up[d] - fu;
+      v[d] = (float)w;
+      v[3 + d] = (float)(w - v[d]);
+    }
+    P[0] = make_float4(v[0], v[1], v[2], __int_as_float(c[0]));
+    P[1] = make_float4(v[3], v[4], v[5], 0.f);
+    a.pcell_k[2 * (size_t)t] = c[1];
+    a.pcell_k[2 * (size_t)t + 1] = c[2];
+  }
+  if (t >= a.nrot * a.L) return;
+  const int r = t / a.L, at = t % a.L;
+  const double* M = a.rot + 9 * (size_t)r;
+  const double rx = a.ref[3 * at], ry = a.ref[3 * at + 1], rz = a.ref[3 * at + 2];
+  const double u[3] = {(M[0] * rx + M[1] * ry + M[2] * rz) * a.g.inv,
+                       (M[3] * rx + M[4] * ry + M[5] * rz) * a.g.inv,
+                       (M[6] * rx + M[7] * ry + M[8] * rz) * a.g.inv};
+  float* o = a.off + 6 * (size_t)t;
+  for (int d = 0; d < 3; ++d) {
+    const float h = (float)u[d];
+    o[d] = h;
+    o[3 + d] = (float)(u[d] - h);
+  }
+}
+
+// Cell of the lattice coordinate iu + (fh + fl) + (oh + ol): i = floor, w the
+// fraction in [0, 1), from float pairs (TwoSum of the high parts, the low parts
+// added); exact to about 1e-13 cells for |offsets| below 2^20.
+__device__ __forceinline__ void cell_of(int iu, float fh, float fl, float oh, float ol, int& i,
+                                        float& w) {
+  const float s = __fadd_rn(fh, oh);
+  const float bp = __fsub_rn(s, fh), ap = __fsub_rn(s, bp);
+  const float e = __fadd_rn(__fsub_rn(fh, ap), __fsub_rn(oh, bp));
+  const float lo = __fadd_rn(e, __fadd_rn(fl, ol));
+  const float f = floorf(s);
+  float frac = __fadd_rn(__fsub_rn(s, f), lo);
+  int k = (int)f;
+  if (frac < 0.f) {
+    frac = __fadd_rn(frac, 1.f);
+    --k;
+  } else if (frac >= 1.f) {
+    frac = __fsub_rn(frac, 1.f);
+    ++k;
+  }
+  if (frac >= 1.f) frac = 0.99999994f;  // a rounding of (1 - tiny) + 1 back to 1
+  i = iu + k;
+  w = frac;
+}
+
+// G3D's eight corners of the cell (i, w) per axis (u = i + w), from the cell
+// masks of k_cell_masks: the corner index truncates u toward zero
+// (int_of_float), so u in (-1, 0) uses cell 0 and u <= -1 none; a cell off the
+// lattice has no corner set.  Returns the mask bits (1: any, 2: all).
+__device__ __forceinline__ int cell_bits(const GridLook& g, const uint8_t* __restrict__ cell,
+                                         int i, float wi, int j, float wj, int k, float wk) {
+  const bool ok = (i >= 0 || (i == -1 && wi > 0.f)) && (j >= 0 || (j == -1 && wj > 0.f)) &&
+                  (k >= 0 || (k == -1 && wk > 0.f));
+  const int i0 = max(i, 0), j0 = max(j, 0), k0 = max(k, 0);
+  if (!ok || i0 >= g.nx || j0 >= g.ny || k0 >= g.nz) return 0;
+  return cell[i0 + (size_t)j0 * g.nx + (size_t)k0 * g.nx * g.ny];
+}
+
+// One thread per pose: the position's lattice coordinate split (FP64, once per
+// position) into a cell and a float-pair fraction, each atom's cell from the rotation's
+// offsets (float pairs), the eight-corner vdW test of every atom (a clash ends
+// the pose), then the trilinear interpolation of the atom's grid (FP32 weights
+// and values, a compensated FP32 sum over the atoms).
 __global__ void __launch_bounds__(kDockBlock) k_dock(DockArgs a) {
   extern __shared__ unsigned long long dsm[];
   unsigned long long* sk = dsm;
   unsigned long long* sf = dsm + kDockPerBlock;
-  __shared__ double s_ref[kMaxLig * 3];
   __shared__ int s_t[kMaxLig];
   __shared__ unsigned s_cnt[2];
-  for (int t = threadIdx.x; t < a.L * 3; t += blockDim.x) s_ref[t] = a.ref[t];
   for (int t = threadIdx.x; t < a.L; t += blockDim.x) s_t[t] = a.lig_type[t];
   if (threadIdx.x < 2) s_cnt[threadIdx.x] = 0;
   __syncthreads();
@@ -272,53 +370,64 @@ __global__ void __launch_bounds__(kDockBlock) k_dock(DockArgs a) {
       const int ps = (int)(gi / a.nrot), r = (int)(gi % a.nrot);
       const int pi = a.pos_idx[ps];
       fr = (unsigned long long)pi * (unsigned long long)a.nrot + (unsigned long long)r;
-      const int ii = pi % a.pdim, jj = (pi / a.pdim) % a.pdim, kk = pi / (a.pdim * a.pdim);
-      const double px = a.p0[0] + a.pstep * ii, py = a.p0[1] + a.pstep * jj,
-                   pz = a.p0[2] + a.pstep * kk;
+      const float4 P0 = a.pcell[2 * (size_t)ps], P1 = a.pcell[2 * (size_t)ps + 1];
+      const int iu[3] = {__float_as_int(P0.w), a.pcell_k[2 * (size_t)ps],
+                         a.pcell_k[2 * (size_t)ps + 1]};
+      const float fh[3] = {P0.x, P0.y, P0.z}, fl[3] = {P1.x, P1.y, P1.z};
       bool skip = false;
-      if (a.center_occ) {
-        bool all;
-        corners(a.g, a.vdw, (px - a.g.o[0]) * a.g.inv, (py - a.g.o[1]) * a.g.inv,
-                (pz - a.g.o[2]) * a.g.inv, &all);
-        skip = all;
-      }
+      if (a.center_occ)
+        skip = (cell_bits(a.g, a.vcell, iu[0], fh[0], iu[1], fh[1], iu[2], fh[2]) & 2) != 0;
       if (!skip) {
-        double M[9];
-#pragma unroll
-        for (int m = 0; m < 9; ++m) M[m] = a.rot[9 * (size_t)r + m];
-        double e = 0.0;
+        const float* off = a.off + 6 * (size_t)r * a.L;
+        float eh = 0.f, el = 0.f;  // compensated sum over the atoms (Neumaier)
         bool clash = false;
-        for (int at = 0; at < a.L; ++at) {
-          const double rx = s_ref[3 * at], ry = s_ref[3 * at + 1], rz = s_ref[3 * at + 2];
-          const double x = fma(M[0], rx, fma(M[1], ry, fma(M[2], rz, px)));
-          const double y = fma(M[3], rx, fma(M[4], ry, fma(M[5], rz, py)));
-          const double z = fma(M[6], rx, fma(M[7], ry, fma(M[8], rz, pz)));
-          const double u = (x - a.g.o[0]) * a.g.inv, v = (y - a.g.o[1]) * a.g.inv,
-                       w = (z - a.g.o[2]) * a.g.inv;
-          bool all;
-          if (corners(a.g, a.vdw, u, v, w, &all)) {
+        // two atoms at a time: their loads are independent and overlap
+        for (int at = 0; at < a.L && !clash; at += 2) {
+          const int na = min(2, a.L - at);
+          int ci[2][3];
+          float cw[2][3];
+          int bits[2] = {0, 0};
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            if (u < na) {
+              const float* o = off + 6 * (at + u);
+#pragma unroll
+              for (int d = 0; d < 3; ++d)
+                cell_of(iu[d], fh[d], fl[d], o[d], o[3 + d], ci[u][d], cw[u][d]);
+              bits[u] = cell_bits(a.g, a.vcell, ci[u][0], cw[u][0], ci[u][1], cw[u][1], ci[u][2],
+                                  cw[u][2]);
+            }
+          }
+          if ((bits[0] | bits[1]) & 1) {
             clash = true;
             break;
           }
-          if (u >= 0.0 && v >= 0.0 && w >= 0.0 && u < a.g.nx - 1 && v < a.g.ny - 1 &&
-              w < a.g.nz - 1) {
-            const int i0 = (int)u, j0 = (int)v, k0 = (int)w;
-            const float* gv = a.grids + per * s_t[at] + i0 + (size_t)j0 * a.g.nx + k0 * nxy;
-            const float wx = (float)(u - i0), wy = (float)(v - j0), wz = (float)(w - k0);
-            const float hx = 1.f - wx, hy = 1.f - wy, hz = 1.f - wz;
-            const float c00 = fmaf(gv[1], wx, gv[0] * hx);
-            const float c10 = fmaf(gv[1 + a.g.nx], wx, gv[a.g.nx] * hx);
-            const float c01 = fmaf(gv[1 + nxy], wx, gv[nxy] * hx);
-            const float c11 = fmaf(gv[1 + a.g.nx + nxy], wx, gv[a.g.nx + nxy] * hx);
-            const float c0 = fmaf(c10, wy, c00 * hy), c1 = fmaf(c11, wy, c01 * hy);
-            e += (double)fmaf(c1, wz, c0 * hz);
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            if (u < na && ci[u][0] >= 0 && ci[u][1] >= 0 && ci[u][2] >= 0 &&
+                ci[u][0] <= a.g.nx - 2 && ci[u][1] <= a.g.ny - 2 && ci[u][2] <= a.g.nz - 2) {
+              const float* gv = a.grids + per * s_t[at + u] + ci[u][0] + (size_t)ci[u][1] * a.g.nx +
+                                ci[u][2] * nxy;
+              const float wx = cw[u][0], wy = cw[u][1], wz = cw[u][2];
+              const float hx = 1.f - wx, hy = 1.f - wy, hz = 1.f - wz;
+              const float c00 = fmaf(gv[1], wx, gv[0] * hx);
+              const float c10 = fmaf(gv[1 + a.g.nx], wx, gv[a.g.nx] * hx);
+              const float c01 = fmaf(gv[1 + nxy], wx, gv[nxy] * hx);
+              const float c11 = fmaf(gv[1 + a.g.nx + nxy], wx, gv[a.g.nx + nxy] * hx);
+              const float c0 = fmaf(c10, wy, c00 * hy), c1 = fmaf(c11, wy, c01 * hy);
+              const float t = fmaf(c1, wz, c0 * hz);
+              const float sum = __fadd_rn(eh, t);
+              el = __fadd_rn(el, fabsf(eh) >= fabsf(t) ? __fadd_rn(__fsub_rn(eh, sum), t)
+                                                       : __fadd_rn(__fsub_rn(t, sum), eh));
+              eh = sum;
+            }
           }
         }
         if (clash) {
           ++clashed;
         } else {
           ++scored;
-          key = sort_key(a.const_intra + e);
+          key = sort_key(a.const_intra + ((double)eh + (double)el));
         }
       }
     }
@@ -648,6 +757,14 @@ cudaError_t launch_masks(const DevCull& cull, const MaskBuild& mb, const double*
   return cudaGetLastError();
 }
 
+cudaError_t launch_cell_masks(const GridLook& g, const uint8_t* mask, uint8_t* cell,
+                              cudaStream_t st) {
+  const long long n = (long long)g.nx * g.ny * g.nz;
+  if (n <= 0) return cudaSuccess;
+  k_cell_masks<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, mask, cell);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_clash(const DevLigand& lig, const float4* X, int B, const DevCull& cull,
                          const ClashArgs& ca, int* out, cudaStream_t st) {
   if (B <= 0) return cudaSuccess;
@@ -657,6 +774,8 @@ cudaError_t launch_clash(const DevLigand& lig, const float4* X, int B, const Dev
 
 cudaError_t launch_dock(const DockArgs& a, int blocks, cudaStream_t st) {
   if (blocks <= 0) return cudaSuccess;
+  const int no = max(a.nrot * a.L, a.npos);
+  k_dock_offsets<<<(no + 255) / 256, 256, 0, st>>>(a);
   const int smem = 2 * kDockPerBlock * (int)sizeof(unsigned long long);
   cudaError_t e = cudaFuncSetAttribute(k_dock, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;

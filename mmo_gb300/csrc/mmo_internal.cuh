@@ -296,7 +296,7 @@ struct GridLook {
 // desolvation (kernels_dock.cu) --------------------------------------------
 enum : int { kClashIntra = 1, kClashHeavy = 2, kClashGrid = 4 };
 constexpr int kDockBlock = 256;           // threads of a docking block
-constexpr int kDockPerBlock = 4096;       // poses a docking block scores and sorts
+constexpr int kDockPerBlock = 2048;       // poses a docking block scores and sorts
 constexpr int kDockMaxK = 1024;           // largest top-k
 constexpr float kHeavyClashMax = 3.52f;   // 0.8 (2.2 + 2.2): the largest clash distance
 
@@ -321,8 +321,11 @@ struct DockArgs {
   const int* lig_type;      // [L] grid type of each atom
   const float* grids;       // [ntypes][nz][ny][nx]
   GridLook g;               // grids' lattice (device frame)
-  const uint8_t* vdw;       // [points] protein vdW volume on the same lattice
+  const uint8_t* vcell;     // [points] cell masks of the vdW volume (k_cell_masks)
   const double* rot;        // [nrot][9] rotations, row-major
+  float* off;               // [nrot][L][6] rotated atoms in lattice units, float pairs
+  float4* pcell;            // [npos][2] position: fraction hi (x, y, z, bits of cell x), lo
+  int* pcell_k;             // [npos][2] position: cells y, z
   const int* pos_idx;       // [npos] index of each position in the position lattice
   int L, npos, nrot, pdim;  // positions: pdim points per axis
   double p0[3], pstep;      // position lattice origin (device frame), spacing
@@ -424,6 +427,8 @@ cudaError_t launch_masks(const DevCull& cull, const MaskBuild& mb, const double*
                          uint8_t* vdw, uint8_t* shell, cudaStream_t st);
 cudaError_t launch_clash(const DevLigand& lig, const float4* X, int B, const DevCull& cull,
                          const ClashArgs& ca, int* out, cudaStream_t st);
+cudaError_t launch_cell_masks(const GridLook& g, const uint8_t* mask, uint8_t* cell,
+                              cudaStream_t st);
 cudaError_t launch_dock(const DockArgs& a, int blocks, cudaStream_t st);
 cudaError_t launch_topk_merge(const unsigned long long* in, int n, int k, unsigned long long* out,
                               cudaStream_t st);
