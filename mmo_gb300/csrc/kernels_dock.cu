@@ -24,6 +24,7 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kList = 64;   // compacted atoms per warp
 constexpr int kWarps = 8;   // warps per CTA of the lattice kernels
 constexpr double kPiD = 3.14159265358979323846;
+constexpr int kDockAtoms = 4;  // atoms of a pose in flight together
 
 __device__ __forceinline__ float wmin(float v) {
 #pragma unroll
@@ -381,14 +382,16 @@ __global__ void __launch_bounds__(kDockBlock) k_dock(DockArgs a) {
         const float* off = a.off + 6 * (size_t)r * a.L;
         float eh = 0.f, el = 0.f;  // compensated sum over the atoms (Neumaier)
         bool clash = false;
-        // two atoms at a time: their loads are independent and overlap
-        for (int at = 0; at < a.L && !clash; at += 2) {
-          const int na = min(2, a.L - at);
-          int ci[2][3];
-          float cw[2][3];
-          int bits[2] = {0, 0};
+        // kDockAtoms atoms at a time: their loads are independent and overlap
+        for (int at = 0; at < a.L && !clash; at += kDockAtoms) {
+          const int na = min(kDockAtoms, a.L - at);
+          int ci[kDockAtoms][3];
+          float cw[kDockAtoms][3];
+          int bits[kDockAtoms];
+          int anyb = 0;
 #pragma unroll
-          for (int u = 0; u < 2; ++u) {
+          for (int u = 0; u < kDockAtoms; ++u) {
+            bits[u] = 0;
             if (u < na) {
               const float* o = off + 6 * (at + u);
 #pragma unroll
@@ -397,13 +400,14 @@ __global__ void __launch_bounds__(kDockBlock) k_dock(DockArgs a) {
               bits[u] = cell_bits(a.g, a.vcell, ci[u][0], cw[u][0], ci[u][1], cw[u][1], ci[u][2],
                                   cw[u][2]);
             }
+            anyb |= bits[u];
           }
-          if ((bits[0] | bits[1]) & 1) {
+          if (anyb & 1) {
             clash = true;
             break;
           }
 #pragma unroll
-          for (int u = 0; u < 2; ++u) {
+          for (int u = 0; u < kDockAtoms; ++u) {
             if (u < na && ci[u][0] >= 0 && ci[u][1] >= 0 && ci[u][2] >= 0 &&
                 ci[u][0] <= a.g.nx - 2 && ci[u][1] <= a.g.ny - 2 && ci[u][2] <= a.g.nz - 2) {
               const float* gv = a.grids + per * s_t[at + u] + ci[u][0] + (size_t)ci[u][1] * a.g.nx +
