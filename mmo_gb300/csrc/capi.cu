@@ -3000,7 +3000,12 @@ int mmo_dock_exhaustive(mmo_ctx* ctx, const mmo_dock_spec* sp, double* top_score
           pos.push_back((int)(ii + jj * pdim + kk * pdim * pdim));
       }
   const long long total = (long long)pos.size() * nrot;
-  const long long blocks = (total + kDockPerBlock - 1) / kDockPerBlock;
+  // CTA tiles of rtile rotations x (kDockPerBlock / rtile) positions; the
+  // tile's rotated atoms (24 B per atom) take at most 24 KB of shared memory
+  int rtile = 1;
+  while (rtile * 2 <= kDockPerBlock && rtile * 2 * L * 24 <= 24576 && rtile < nrot) rtile *= 2;
+  const long long ptile = kDockPerBlock / rtile;
+  const long long blocks = ((long long)pos.size() + ptile - 1) / ptile * ((nrot + rtile - 1) / rtile);
   if (blocks > (long long)INT32_MAX / kDockMaxK)
     return fail(ctx, MMO_EINVAL, "mmo_dock_exhaustive: too many poses");
   std::vector<double> rot(9 * (size_t)nrot);
@@ -3042,6 +3047,7 @@ int mmo_dock_exhaustive(mmo_ctx* ctx, const mmo_dock_spec* sp, double* top_score
   a.npos = (int)pos.size();
   a.nrot = nrot;
   a.pdim = (int)pdim;
+  a.rtile = rtile;
   for (int d = 0; d < 3; ++d) a.p0[d] = sp->roi_center[d] - r - ctx->origin[d];
   a.pstep = step;
   a.center_occ = center_occ;

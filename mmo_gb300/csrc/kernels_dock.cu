@@ -345,8 +345,11 @@ __device__ __forceinline__ int cell_bits(const GridLook& g, const uint8_t* __res
   return cell[i0 + (size_t)j0 * g.nx + (size_t)k0 * g.nx * g.ny];
 }
 
-// One thread per pose: the position's lattice coordinate split (FP64, once per
-// position) into a cell and a float-pair fraction, each atom's cell from the rotation's
+// A CTA per tile of rtile rotations x (kDockPerBlock / rtile) positions (the
+// tile's rotated atoms staged in shared memory; a warp's poses share a
+// position, so their lookups fall near each other).  One thread per pose: the
+// position's lattice coordinate split (FP64, once per position) into a cell
+// and a float-pair fraction, each atom's cell from the rotation's
 // offsets (float pairs), the eight-corner vdW test of every atom (a clash ends
 // the pose), then the trilinear interpolation of the atom's grid (FP32 weights
 // and values, a compensated FP32 sum over the atoms).
@@ -354,21 +357,26 @@ __global__ void __launch_bounds__(kDockBlock) k_dock(DockArgs a) {
   extern __shared__ unsigned long long dsm[];
   unsigned long long* sk = dsm;
   unsigned long long* sf = dsm + kDockPerBlock;
+  float* s_off = reinterpret_cast<float*>(dsm + 2 * kDockPerBlock);  // [rtile][L][6]
   __shared__ int s_t[kMaxLig];
   __shared__ unsigned s_cnt[2];
+  // the block's tile: rotations [r0, r0 + rtile) x positions [p0, p0 + ptile)
+  const int R = a.rtile, Pt = kDockPerBlock / a.rtile;
+  const int npb = (a.npos + Pt - 1) / Pt;
+  const int r0 = (blockIdx.x / npb) * R, p0 = (blockIdx.x % npb) * Pt;
+  const int nr = min(R, a.nrot - r0);
   for (int t = threadIdx.x; t < a.L; t += blockDim.x) s_t[t] = a.lig_type[t];
+  for (int t = threadIdx.x; t < nr * a.L * 6; t += blockDim.x)
+    s_off[t] = a.off[6 * (size_t)r0 * a.L + t];
   if (threadIdx.x < 2) s_cnt[threadIdx.x] = 0;
   __syncthreads();
-  const long long total = (long long)a.npos * a.nrot;
-  const long long base = (long long)blockIdx.x * kDockPerBlock;
   const size_t nxy = (size_t)a.g.nx * a.g.ny, per = nxy * a.g.nz;
   unsigned scored = 0, clashed = 0;
   for (int q = 0; q < kDockPerBlock / kDockBlock; ++q) {
     const int slot = q * kDockBlock + threadIdx.x;
-    const long long gi = base + slot;
+    const int rl = slot % R, ps = p0 + slot / R, r = r0 + rl;
     unsigned long long key = ~0ull, fr = ~0ull;
-    if (gi < total) {
-      const int ps = (int)(gi / a.nrot), r = (int)(gi % a.nrot);
+    if (rl < nr && ps < a.npos) {
       const int pi = a.pos_idx[ps];
       fr = (unsigned long long)pi * (unsigned long long)a.nrot + (unsigned long long)r;
       const float4 P0 = a.pcell[2 * (size_t)ps], P1 = a.pcell[2 * (size_t)ps + 1];
@@ -379,7 +387,7 @@ __global__ void __launch_bounds__(kDockBlock) k_dock(DockArgs a) {
       if (a.center_occ)
         skip = (cell_bits(a.g, a.vcell, iu[0], fh[0], iu[1], fh[1], iu[2], fh[2]) & 2) != 0;
       if (!skip) {
-        const float* off = a.off + 6 * (size_t)r * a.L;
+        const float* off = s_off + 6 * (size_t)rl * a.L;
         float eh = 0.f, el = 0.f;  // compensated sum over the atoms (Neumaier)
         bool clash = false;
         // kDockAtoms atoms at a time: their loads are independent and overlap
@@ -780,7 +788,8 @@ cudaError_t launch_dock(const DockArgs& a, int blocks, cudaStream_t st) {
   if (blocks <= 0) return cudaSuccess;
   const int no = max(a.nrot * a.L, a.npos);
   k_dock_offsets<<<(no + 255) / 256, 256, 0, st>>>(a);
-  const int smem = 2 * kDockPerBlock * (int)sizeof(unsigned long long);
+  const int smem = 2 * kDockPerBlock * (int)sizeof(unsigned long long) +
+                   a.rtile * a.L * 6 * (int)sizeof(float);
   cudaError_t e = cudaFuncSetAttribute(k_dock, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   k_dock<<<blocks, kDockBlock, smem, st>>>(a);

@@ -328,6 +328,7 @@ struct DockArgs {
   int* pcell_k;             // [npos][2] position: cells y, z
   const int* pos_idx;       // [npos] index of each position in the position lattice
   int L, npos, nrot, pdim;  // positions: pdim points per axis
+  int rtile;                // rotations per CTA tile (a power of 2 dividing kDockPerBlock)
   double p0[3], pstep;      // position lattice origin (device frame), spacing
   int center_occ;           // the ligand's centre is inside one of its atoms
   double const_intra;
