@@ -2534,14 +2534,29 @@ int mmo_build_grids(mmo_ctx* ctx, const mmo_grid_spec* spec, double* ms) {
   }
   const bool masked = spec->mask_radius > 0;
   gb.mr2 = masked ? spec->mask_radius * spec->mask_radius : HUGE_VAL;
-  for (int pt = 0; pt < kNTypes; ++pt)
-    for (int e = 0; e < gb.nelem; ++e) {
-      double x2, d;
-      pair_xd(ctx->ph.mixing, pt, elems[e], &x2, &d);
-      // (X, 1/D), X = D^(1/3) x^2: (X / r^2)^3 = D (x / r)^6
-      gb.el[pt * kGridElems + e] =
-          make_float2((float)(std::cbrt(d) * x2), d > 0.0 ? (float)(1.0 / d) : 0.f);
+  gb.fact = ctx->ph.mixing == MMO_MIX_GEOMEAN;
+  if (gb.fact) {
+    // x_ij = sqrt(x_i x_j), D_ij = sqrt(D_i D_j) (UFF.ml:47-48): the vdW terms
+    // factor into protein-side sums shared by every element
+    for (int pt = 0; pt < kNTypes; ++pt) {
+      const double x = kUff[pt].xi, sd = std::sqrt(kUff[pt].di);
+      gb.el[pt * kGridElems] = make_float2((float)(sd * std::pow(x, 6)), (float)(sd * x * x * x));
     }
+    for (int e = 0; e < gb.nelem; ++e) {
+      const double x = kUff[elems[e]].xi;
+      gb.elf[e] = make_float4((float)std::sqrt(kUff[elems[e]].di), (float)(2.0 * x * x * x),
+                              (float)std::pow(x, 6), 0.f);
+    }
+  } else {
+    for (int pt = 0; pt < kNTypes; ++pt)
+      for (int e = 0; e < gb.nelem; ++e) {
+        double x2, d;
+        pair_xd(ctx->ph.mixing, pt, elems[e], &x2, &d);
+        // (X, 1/D), X = D^(1/3) x^2: (X / r^2)^3 = D (x / r)^6
+        gb.el[pt * kGridElems + e] =
+            make_float2((float)(std::cbrt(d) * x2), d > 0.0 ? (float)(1.0 / d) : 0.f);
+      }
+  }
   // the point tiles that meet the mask sphere (and the points inside it)
   std::vector<int3> tiles;
   double npts = masked ? 0.0 : (double)nx * ny * nz;

@@ -55,10 +55,20 @@ __device__ __forceinline__ float gwmax(float v) {
 // block ends.
 constexpr int kGridWarps = 8;  // tiles per CTA
 
+// NE = 0: the factorised form of geometric mixing, vdW sums A12, A6 shared by
+// all elements; NE > 0: NE per-element vdW sums
+template <int NE>
+constexpr int grid_accs() {
+  return NE == 0 ? 3 : NE + 1;
+}
+template <int NE>
+constexpr int grid_el4() {
+  return NE == 0 ? 1 : (NE + 1) / 2;
+}
 template <int NE, int KP>
 constexpr int grid_smem_bytes() {
-  return kNTypes * ((NE + 1) / 2) * 16 + kGridWarps * kGridList * 32 +
-         kGridWarps * (NE + 1) * KP * 32 * (int)sizeof(float2);
+  return kNTypes * grid_el4<NE>() * 16 + kGridWarps * kGridList * 32 +
+         kGridWarps * grid_accs<NE>() * KP * 32 * (int)sizeof(float2);
 }
 
 // KP lattice points per lane (1 or 2): a warp tile of 4 x 4 x 2 KP points
@@ -66,16 +76,18 @@ template <int DIEL, int NE, int KP, bool COUNT>
 __global__ void __launch_bounds__(kGridWarps * 32) k_grid_build(DevCull cull, GridBuild gb,
                                                                  float* grids) {
   constexpr int kGridPts = KP;
-  constexpr int NE2 = (NE + 1) / 2;
+  constexpr bool FACT = NE == 0;
+  constexpr int NACC = grid_accs<NE>(), ELEC = NACC - 1, NE2 = grid_el4<NE>();
   extern __shared__ __align__(16) float4 gsm[];
-  float4* s_el = gsm;                                  // [ptype][NE2] (X, 1/D) of 2 elements
+  // [ptype][NE2]: (X, 1/D) of 2 elements, or (c12, c6) of the protein type (NE = 0)
+  float4* s_el = gsm;
   float4* s_list = s_el + kNTypes * NE2;               // [warp][kGridList][2] staged atoms
   float2* s_ad = reinterpret_cast<float2*>(s_list + kGridWarps * kGridList * 2);
   for (int k = threadIdx.x; k < kNTypes * NE2; k += blockDim.x) {
     const int pt = k / NE2, q = k % NE2;
     const float2 a = gb.el[pt * kGridElems + 2 * q];
-    const float2 b = 2 * q + 1 < kGridElems ? gb.el[pt * kGridElems + 2 * q + 1]
-                                            : make_float2(0.f, 0.f);
+    const float2 b = (!FACT && 2 * q + 1 < kGridElems) ? gb.el[pt * kGridElems + 2 * q + 1]
+                                                       : make_float2(0.f, 0.f);
     s_el[k] = make_float4(a.x, a.y, b.x, b.y);
   }
   __syncthreads();
@@ -124,12 +136,12 @@ __global__ void __launch_bounds__(kGridWarps * 32) k_grid_build(DevCull cull, Gr
   // of the tile, where the switched terms are exactly 0, and a row or block
   // that is not visited adds exactly 0: each value is the same whatever the
   // tile's box (and so the mask) is.
-  float2* ad = s_ad + (size_t)w * (NE + 1) * kGridPts * 32 + lane;  // [e][c] stride 32
-  float af[kGridPts][NE + 1], bf[kGridPts][NE + 1];
+  float2* ad = s_ad + (size_t)w * NACC * kGridPts * 32 + lane;  // [e][c] stride 32
+  float af[kGridPts][NACC], bf[kGridPts][NACC];
 #pragma unroll
   for (int c = 0; c < kGridPts; ++c)
 #pragma unroll
-    for (int e = 0; e <= NE; ++e) {
+    for (int e = 0; e < NACC; ++e) {
       af[c][e] = 0.f;
       bf[c][e] = 0.f;
       ad[(e * kGridPts + c) * 32] = make_float2(0.f, 0.f);
@@ -162,7 +174,15 @@ __global__ void __launch_bounds__(kGridWarps * 32) k_grid_build(DevCull cull, Gr
         const float ir2 = ir * ir;
         const float sw = fmaxf(fmaf(r2c, -1.0f / 144.0f, 1.0f), 0.0f);
         const float ws = sw * sw;
-        af[c][NE] = fmaf(ws * p.w, DIEL == 0 ? ir : ir2, af[c][NE]);
+        af[c][ELEC] = fmaf(ws * p.w, DIEL == 0 ? ir : ir2, af[c][ELEC]);
+        if (FACT) {
+          // geometric mixing: D_ij (x_ij/r)^12 = c12_i c12_e / r^12 and
+          // 2 D_ij (x_ij/r)^6 = 2 c6_i c6_e / r^6 with c12 = sqrt(D) x^6,
+          // c6 = sqrt(D) x^3: two sums for every element
+          const float ir6 = (ir2 * ir2) * ir2;
+          af[c][0] = fmaf(ws * prm[0].x, ir6 * ir6, af[c][0]);
+          af[c][1] = fmaf(ws * prm[0].y, ir6, af[c][1]);
+        }
 #pragma unroll
         for (int e = 0; e < NE; ++e) {
           // X = D^(1/3) x^2: q6 = (X / r^2)^3 = D (x/r)^6, and
@@ -217,7 +237,7 @@ __global__ void __launch_bounds__(kGridWarps * 32) k_grid_build(DevCull cull, Gr
 #pragma unroll
         for (int c = 0; c < kGridPts; ++c)
 #pragma unroll
-          for (int e = 0; e <= NE; ++e) {
+          for (int e = 0; e < NACC; ++e) {
             bf[c][e] += af[c][e];
             af[c][e] = 0.f;
           }
@@ -228,7 +248,7 @@ __global__ void __launch_bounds__(kGridWarps * 32) k_grid_build(DevCull cull, Gr
 #pragma unroll
         for (int c = 0; c < kGridPts; ++c)
 #pragma unroll
-          for (int e = 0; e <= NE; ++e) {
+          for (int e = 0; e < NACC; ++e) {
             float2& acc = ad[(e * kGridPts + c) * 32];
             acc = two_sum_add(acc, bf[c][e]);
             bf[c][e] = 0.f;
@@ -259,14 +279,31 @@ __global__ void __launch_bounds__(kGridWarps * 32) k_grid_build(DevCull cull, Gr
   for (int c = 0; c < kGridPts; ++c) {
     if (!in_lattice[c]) continue;
     const size_t idx = (size_t)i + (size_t)j * gb.nx + (size_t)kk[c] * gb.nx * gb.ny;
-    const float2 phi = ad[(NE * kGridPts + c) * 32];
+    const float2 phi = ad[(ELEC * kGridPts + c) * 32];
+    float2 a12 = make_float2(0.f, 0.f), a6 = a12;
+    if (FACT) {
+      a12 = ad[(0 * kGridPts + c) * 32];
+      a6 = ad[(1 * kGridPts + c) * 32];
+    }
     for (int l = 0; l < gb.ntypes; ++l) {
       float v = 0.f;
       if (masked[c]) {
+        float2 vdw;
+        if (FACT) {
+          // sqrt(D_e) (x_e^6 A12 - 2 x_e^3 A6) in float pairs
+          const float4 f = gb.elf[gb.type_elem[l]];  // (sqrt(D_e), 2 x_e^3, x_e^6, 0)
+          const float t1 = f.z * a12.x, t1l = fmaf(f.z, a12.x, -t1) + f.z * a12.y;
+          const float t2 = f.y * a6.x, t2l = fmaf(f.y, a6.x, -t2) + f.y * a6.y;
+          const float dh = __fsub_rn(t1, t2);
+          const float bp = __fsub_rn(dh, t1), ap = __fsub_rn(dh, bp);
+          const float dl = __fadd_rn(__fsub_rn(t1, ap), __fsub_rn(-t2, bp)) + (t1l - t2l);
+          vdw = make_float2(f.x * dh, fmaf(f.x, dh, -(f.x * dh)) + f.x * dl);
+        } else {
+          vdw = ad[(gb.type_elem[l] * kGridPts + c) * 32];
+        }
         // q phi + V in float pairs: one rounding of the sum of the high parts,
         // the low parts added to it
         const float q = gb.type_qf[l];
-        const float2 vdw = ad[(gb.type_elem[l] * kGridPts + c) * 32];
         const float e = fmaf(q, phi.x, vdw.x) + fmaf(q, phi.y, vdw.y);
         v = e < gb.max_Ef ? e : gb.max_Ef;
       }
@@ -339,6 +376,7 @@ cudaError_t grid_build_as(const DevCull& cull, const GridBuild& gb, float* grids
 template <int DIEL, int KP, bool COUNT>
 cudaError_t grid_build_ne(const DevCull& cull, const GridBuild& gb, float* grids,
                           cudaStream_t st) {
+  if (gb.fact) return grid_build_as<DIEL, 0, KP, COUNT>(cull, gb, grids, st);
   switch (gb.nelem) {
     case 1: return grid_build_as<DIEL, 1, KP, COUNT>(cull, gb, grids, st);
     case 2: return grid_build_as<DIEL, 2, KP, COUNT>(cull, gb, grids, st);

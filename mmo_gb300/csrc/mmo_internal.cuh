@@ -282,7 +282,10 @@ struct GridBuild {
   double mc[3], mr2;       // mask sphere (device frame); points outside hold 0
   float max_Ef;            // cap of every value (rounded to float, as the values are)
   float2 el[kNTypes * kGridElems];  // [protein type][grid element] (D^(1/3) x^2, 1/D)
-                                    // (1/D := 0 when D = 0)
+                                    // (1/D := 0 when D = 0); with fact, [protein type][0] =
+                                    // (sqrt(D) x^6, sqrt(D) x^3)
+  int fact;                         // 1: geometric mixing, the factorised vdW sums
+  float4 elf[kGridElems];           // with fact, per grid element (sqrt(D), 2 x^3, x^6, 0)
   unsigned long long* pairs;  // [2] (point, atom) pairs evaluated for masked points, and
                               // those within 12 A (may be null)
 };

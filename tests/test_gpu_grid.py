@@ -43,8 +43,8 @@ def _types(lig):
     return types, per[0]
 
 
-def _built(scorer_factory, system, lattice, **kw):
-    s = scorer_factory(system.pocket, system.ligand)
+def _built(scorer_factory, system, lattice, physics=None, **kw):
+    s = scorer_factory(system.pocket, system.ligand, physics)
     types, lt = _types(system.ligand)
     origin, dims = lattice
     ms = s.build_grids(STEP, dims, origin, types, **kw)
@@ -52,15 +52,21 @@ def _built(scorer_factory, system, lattice, **kw):
     return s, types, lt
 
 
-def _point_scale(T, pocket, p, anum, q):
+def _point_scale(T, pocket, p, anum, q, diel=0, mixing=0):
     return T.ene_inter(pocket.xyz(), pocket.q, pocket.anum, np.asarray(p)[None, :],
-                       np.array([q]), np.array([anum]), absolute=True)
+                       np.array([q]), np.array([anum]), mixing=mixing, dielectric=diel,
+                       absolute=True)
 
 
-def test_grid_values_match_oracle(oracle, scorer_factory, system, lattice):
+# (dielectric, mixing): the reference's eps = 4 with geometric means (the
+# factorised build), eps = 4 r, Lorentz-Berthelot (the per-element build)
+@pytest.mark.parametrize("diel,mixing", [(0, 0), (1, 0), (0, 1)])
+def test_grid_values_match_oracle(oracle, scorer_factory, system, lattice, diel, mixing):
+    from mmo_gb300.ff import Physics
     from oracle import np_twin as T
 
-    s, types, _ = _built(scorer_factory, system, lattice)
+    ph = oracle.physics(diel, mixing, 0, 0)
+    s, types, _ = _built(scorer_factory, system, lattice, Physics(diel, mixing, 0, 0))
     g = s.grid_values()
     origin, (nx, ny, nz) = lattice
     assert g.shape == (len(types), nz, ny, nx)
@@ -74,14 +80,14 @@ def test_grid_values_match_oracle(oracle, scorer_factory, system, lattice):
     capped = 0
     for i, j, k in np.concatenate([ijk, near, corners]):
         p = origin + STEP * np.array([i, j, k], np.float64)
-        ref = oracle.grid_point(system.pocket, p, ta, tq)
+        ref = oracle.grid_point(system.pocket, p, ta, tq, ph=ph)
         got = g[:, k, j, i].astype(np.float64)
         for l in range(len(types)):
             if ref[l] >= GR.MAX_E:
                 assert got[l] == GR.MAX_E
                 capped += 1
                 continue
-            sc = _point_scale(T, system.pocket, p, ta[l], tq[l])
+            sc = _point_scale(T, system.pocket, p, ta[l], tq[l], diel, mixing)
             err = abs(got[l] - ref[l]) / max(abs(ref[l]), sc, 1e-300)
             assert err <= E_TOL, (i, j, k, l, got[l], ref[l], err)
     assert capped > 0  # the near-atom points reach the cap
