@@ -612,6 +612,12 @@ GridLook grid_look(const mmo_ctx* ctx) {
   GridLook g{};
   for (int d = 0; d < 3; ++d) g.o[d] = ctx->grid_origin[d] - ctx->origin[d];
   g.inv = 1.0 / ctx->grid_step;
+  for (int d = 0; d < 3; ++d) {
+    g.oh[d] = (float)g.o[d];
+    g.ol[d] = (float)(g.o[d] - (double)g.oh[d]);
+  }
+  g.invh = (float)g.inv;
+  g.invl = (float)(g.inv - (double)g.invh);
   g.nx = ctx->grid_n[0];
   g.ny = ctx->grid_n[1];
   g.nz = ctx->grid_n[2];

@@ -293,6 +293,8 @@ struct GridBuild {
 struct GridLook {
   double o[3], inv;        // lattice origin (device frame), 1 / step
   int nx, ny, nz;
+  float oh[3], ol[3];      // the origin as float pairs
+  float invh, invl;        // 1 / step as a float pair
 };
 
 // ---- lattice masks, clash tests, exhaustive docking, placement and
