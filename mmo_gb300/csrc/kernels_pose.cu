@@ -1,6 +1,6 @@
 // kernels_pose.cu -- the per-pose kernels around the pair sweep.
 //
-// k_rebuild (one thread per pose, FP64): the pose map of UnixJunkie/MMO --
+// k_rebuild (a few threads per pose, double-float): the pose map of UnixJunkie/MMO --
 // torsions applied in bond order, each rotating its group about the current
 // (left, right) axis (src/optim.ml:68-71, src/mol.ml:610-631), the
 // enclosing-radius check (src/mol.ml:576-591), then x = Rz(g) Ry(b) Rx(a) y + t
@@ -25,18 +25,56 @@ constexpr int kFinishBlocksPerSM = 7;  // resident finish blocks: 4,096 poses in
 // ---------------------------------------------------------------------------
 // k_rebuild
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void store_split(float4* X, double x, double y, double z) {
-  const float xh = __double2float_rn(x), yh = __double2float_rn(y), zh = __double2float_rn(z);
-  X[0] = make_float4(xh, yh, zh, 0.f);
-  X[1] = make_float4(__double2float_rn(x - (double)xh), __double2float_rn(y - (double)yh),
-                     __double2float_rn(z - (double)zh), 0.f);
+// Double-float arithmetic: a value is an unevaluated pair h + l of floats
+// (|l| <= ulp(h) / 2), about 48 significant bits, on the FP32 pipe (GB300's
+// FP64 rate is 1/64 of its FP32 rate).  ts / qts are the error-free sums
+// (TwoSum, and Fast2Sum for |a| >= |b|); the products take their error by FMA.
+__device__ __forceinline__ float2 df_of(double x) {
+  const float h = __double2float_rn(x);
+  return make_float2(h, __double2float_rn(x - (double)h));
+}
+__device__ __forceinline__ float2 qts(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ float2 ts(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bp = __fsub_rn(s, a);
+  return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp)));
+}
+__device__ __forceinline__ float2 dadd(float2 a, float2 b) {
+  const float2 s = ts(a.x, b.x);
+  return qts(s.x, __fadd_rn(s.y, __fadd_rn(a.y, b.y)));
+}
+__device__ __forceinline__ float2 dneg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 dsub(float2 a, float2 b) { return dadd(a, dneg(b)); }
+__device__ __forceinline__ float2 dmul(float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  return qts(p, fmaf(a.x, b.y, fmaf(a.y, b.x, fmaf(a.x, b.x, -p))));
+}
+// a0 b0 + a1 b1 + a2 b2 + c
+__device__ __forceinline__ float2 ddot3c(float2 a0, float2 b0, float2 a1, float2 b1, float2 a2,
+                                         float2 b2, float2 c) {
+  return dadd(dadd(dadd(dmul(a0, b0), dmul(a1, b1)), dmul(a2, b2)), c);
+}
+__device__ __forceinline__ float2 dshfl_xor(float2 a, int o) {
+  return make_float2(__shfl_xor_sync(kFull, a.x, o), __shfl_xor_sync(kFull, a.y, o));
+}
+__device__ __forceinline__ bool dgt(float2 a, float2 b) {
+  return a.x > b.x || (a.x == b.x && a.y > b.y);
+}
+
+__device__ __forceinline__ void store_pair(float4* X, float2 x, float2 y, float2 z) {
+  X[0] = make_float4(x.x, y.x, z.x, 0.f);
+  X[1] = make_float4(x.y, y.y, z.y, 0.f);
 }
 
 // TPP threads share one pose: each rotates its share of the atoms while the
 // per-torsion axis and matrix are recomputed by all of them, and the sines and
-// cosines of the pose's angles are computed once, split over the TPP threads.
+// cosines of the pose's angles are computed once (FP64), split over the TPP
+// threads.  Coordinates, axes, matrices and the rigid map are double-float.
 // Small batches use many threads per pose (the one-pose path uses a whole
-// warp), large batches one thread per pose.
+// warp), large batches few.
 //
 // rebuild_pose: one pose of the block's ligand; dof, Xo, Yo, reco, ceno and
 // statuso point at the pose's own slots (dof readable even when !live).
@@ -49,92 +87,110 @@ __device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof
                                              int* statuso) {
   constexpr int PPB = kRebuildThreads / TPP;  // poses per block
   constexpr int NANG = 3 + kMaxTors;
-  extern __shared__ double sz[];  // [3][L][PPB] coordinates, then [PPB][NANG][2] sin, cos
+  // [3][L][PPB] double-float coordinates, then [PPB][NANG][2] FP64 sin, cos
+  extern __shared__ double sz[];
   const int tid = threadIdx.x, p = tid / TPP, sub = tid % TPP;
   const int L = lig.L, nrb = lig.nrb;
-  double* X = sz;
-  double* Yc = sz + L * PPB;
-  double* Zc = sz + 2 * L * PPB;
+  float2* X = reinterpret_cast<float2*>(sz);
+  float2* Yc = X + L * PPB;
+  float2* Zc = X + 2 * L * PPB;
   double* SC = sz + 3 * L * PPB + p * NANG * 2;
 #define AT(arr, a) arr[(a) * PPB + p]
   for (int a = sub; a < L; a += TPP) {
-    AT(X, a) = lig.ref64[3 * a];
-    AT(Yc, a) = lig.ref64[3 * a + 1];
-    AT(Zc, a) = lig.ref64[3 * a + 2];
+    AT(X, a) = df_of(lig.ref64[3 * a]);
+    AT(Yc, a) = df_of(lig.ref64[3 * a + 1]);
+    AT(Zc, a) = df_of(lig.ref64[3 * a + 2]);
   }
   for (int k = sub; k < 3 + nrb; k += TPP) sincos((double)dof[3 + k], &SC[2 * k], &SC[2 * k + 1]);
   __syncwarp();
+  const float2 one = make_float2(1.f, 0.f);
   for (int t = 0; t < nrb; ++t) {
     const int2 bd = lig.bonds[t];
-    const double cx = AT(X, bd.y), cy = AT(Yc, bd.y), cz = AT(Zc, bd.y);
-    const double ax = cx - AT(X, bd.x), ay = cy - AT(Yc, bd.x), az = cz - AT(Zc, bd.x);
-    const double inv = rnorm3d(ax, ay, az);
-    const double ux = ax * inv, uy = ay * inv, uz = az * inv;
-    const double sn = SC[2 * (3 + t)], cs = SC[2 * (3 + t) + 1];
+    const float2 cx = AT(X, bd.y), cy = AT(Yc, bd.y), cz = AT(Zc, bd.y);
+    const float2 ax = dsub(cx, AT(X, bd.x)), ay = dsub(cy, AT(Yc, bd.x)),
+                 az = dsub(cz, AT(Zc, bd.x));
+    // 1 / |a|: the float estimate and one Newton step in double-float
+    const float2 n2 = dadd(dadd(dmul(ax, ax), dmul(ay, ay)), dmul(az, az));
+    const float r0 = rsqrtf(n2.x);
+    const float2 err = dsub(one, dmul(n2, dmul(make_float2(r0, 0.f), make_float2(r0, 0.f))));
+    const float2 inv = qts(r0, __fmul_rn(0.5f * r0, err.x));
+    const float2 ux = dmul(ax, inv), uy = dmul(ay, inv), uz = dmul(az, inv);
+    const float2 sn = df_of(SC[2 * (3 + t)]), cs = df_of(SC[2 * (3 + t) + 1]);
     // Rodrigues matrix of rot.ml:136-146
-    const double o = 1.0 - cs;
-    const double R0 = cs + ux * ux * o, R1 = ux * uy * o - uz * sn, R2 = ux * uz * o + uy * sn;
-    const double R3 = ux * uy * o + uz * sn, R4 = cs + uy * uy * o, R5 = uy * uz * o - ux * sn;
-    const double R6 = ux * uz * o - uy * sn, R7 = uy * uz * o + ux * sn, R8 = cs + uz * uz * o;
+    const float2 o = dsub(one, cs);
+    const float2 xo = dmul(ux, o), yo = dmul(uy, o), zo = dmul(uz, o);
+    const float2 xs = dmul(ux, sn), ys = dmul(uy, sn), zs = dmul(uz, sn);
+    const float2 R0 = dadd(cs, dmul(ux, xo)), R1 = dsub(dmul(ux, yo), zs),
+                 R2 = dadd(dmul(ux, zo), ys);
+    const float2 R3 = dadd(dmul(ux, yo), zs), R4 = dadd(cs, dmul(uy, yo)),
+                 R5 = dsub(dmul(uy, zo), xs);
+    const float2 R6 = dsub(dmul(ux, zo), ys), R7 = dadd(dmul(uy, zo), xs),
+                 R8 = dadd(cs, dmul(uz, zo));
     __syncwarp();  // every thread of the pose has read the axis
     for (int k = lig.grp_off[t] + sub; k < lig.grp_off[t + 1]; k += TPP) {
       const int i = lig.grp_atoms[k];
-      const double vx = AT(X, i) - cx, vy = AT(Yc, i) - cy, vz = AT(Zc, i) - cz;
-      AT(X, i) = fma(R0, vx, fma(R1, vy, fma(R2, vz, cx)));
-      AT(Yc, i) = fma(R3, vx, fma(R4, vy, fma(R5, vz, cy)));
-      AT(Zc, i) = fma(R6, vx, fma(R7, vy, fma(R8, vz, cz)));
+      const float2 vx = dsub(AT(X, i), cx), vy = dsub(AT(Yc, i), cy), vz = dsub(AT(Zc, i), cz);
+      AT(X, i) = ddot3c(R0, vx, R1, vy, R2, vz, cx);
+      AT(Yc, i) = ddot3c(R3, vx, R4, vy, R5, vz, cy);
+      AT(Zc, i) = ddot3c(R6, vx, R7, vy, R8, vz, cz);
     }
     if (RECORD && live && sub == 0) {
       float4* r = reco + (size_t)t * 3;
-      r[0] = make_float4((float)cx, (float)cy, (float)cz, (float)cs);
-      r[1] = make_float4((float)ux, (float)uy, (float)uz, (float)sn);
-      r[2] = make_float4((float)inv, 0.f, 0.f, 0.f);
+      r[0] = make_float4(cx.x, cy.x, cz.x, cs.x);
+      r[1] = make_float4(ux.x, uy.x, uz.x, sn.x);
+      r[2] = make_float4(inv.x, 0.f, 0.f, 0.f);
     }
     __syncwarp();  // the rotated group is visible before the next axis is read
   }
   // centroid and enclosing radius, max_i (0.01 + |c - y_i|) > 12 (mol.ml:576-591)
-  double mx = 0.0, my = 0.0, mz = 0.0;
+  float2 mx = make_float2(0.f, 0.f), my = mx, mz = mx;
   for (int a = sub; a < L; a += TPP) {
-    mx += AT(X, a);
-    my += AT(Yc, a);
-    mz += AT(Zc, a);
+    mx = dadd(mx, AT(X, a));
+    my = dadd(my, AT(Yc, a));
+    mz = dadd(mz, AT(Zc, a));
   }
 #pragma unroll
   for (int o = TPP / 2; o > 0; o >>= 1) {
-    mx += __shfl_xor_sync(kFull, mx, o);
-    my += __shfl_xor_sync(kFull, my, o);
-    mz += __shfl_xor_sync(kFull, mz, o);
+    mx = dadd(mx, dshfl_xor(mx, o));
+    my = dadd(my, dshfl_xor(my, o));
+    mz = dadd(mz, dshfl_xor(mz, o));
   }
-  mx /= L;
-  my /= L;
-  mz /= L;
-  double d2max = 0.0;
+  const float2 iL = df_of(1.0 / L);
+  mx = dmul(mx, iL);
+  my = dmul(my, iL);
+  mz = dmul(mz, iL);
+  float2 d2max = make_float2(0.f, 0.f);
   for (int a = sub; a < L; a += TPP) {
-    const double dx = mx - AT(X, a), dy = my - AT(Yc, a), dz = mz - AT(Zc, a);
-    d2max = fmax(d2max, dx * dx + dy * dy + dz * dz);
+    const float2 dx = dsub(mx, AT(X, a)), dy = dsub(my, AT(Yc, a)), dz = dsub(mz, AT(Zc, a));
+    const float2 d2 = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
+    if (dgt(d2, d2max)) d2max = d2;
   }
 #pragma unroll
-  for (int o = TPP / 2; o > 0; o >>= 1) d2max = fmax(d2max, __shfl_xor_sync(kFull, d2max, o));
-  const int status = 0.01 + sqrt(d2max) > 12.0 ? kStatusTooLong : 0;
+  for (int o = TPP / 2; o > 0; o >>= 1) {
+    const float2 other = dshfl_xor(d2max, o);
+    if (dgt(other, d2max)) d2max = other;
+  }
+  const int status = 0.01 + sqrt((double)d2max.x + (double)d2max.y) > 12.0 ? kStatusTooLong : 0;
   // rigid map
   const double sa = SC[0], ca = SC[1], sb = SC[2], cb = SC[3], sg = SC[4], cg = SC[5];
-  const double R0 = cb * cg, R1 = cg * sa * sb - ca * sg, R2 = sa * sg + ca * cg * sb;
-  const double R3 = cb * sg, R4 = ca * cg + sa * sb * sg, R5 = ca * sb * sg - cg * sa;
-  const double R6 = -sb, R7 = cb * sa, R8 = ca * cb;
-  const double tx = (double)dof[0] - (double)orx, ty = (double)dof[1] - (double)ory,
-               tz = (double)dof[2] - (double)orz;
-  const double ox = RECENTER ? mx : 0.0, oy = RECENTER ? my : 0.0, oz = RECENTER ? mz : 0.0;
+  const float2 R0 = df_of(cb * cg), R1 = df_of(cg * sa * sb - ca * sg),
+               R2 = df_of(sa * sg + ca * cg * sb);
+  const float2 R3 = df_of(cb * sg), R4 = df_of(ca * cg + sa * sb * sg),
+               R5 = df_of(ca * sb * sg - cg * sa);
+  const float2 R6 = df_of(-sb), R7 = df_of(cb * sa), R8 = df_of(ca * cb);
+  const float2 tx = df_of((double)dof[0] - (double)orx), ty = df_of((double)dof[1] - (double)ory),
+               tz = df_of((double)dof[2] - (double)orz);
+  const float2 zero = make_float2(0.f, 0.f);
+  const float2 ox = RECENTER ? mx : zero, oy = RECENTER ? my : zero, oz = RECENTER ? mz : zero;
   if (live) {
     for (int a = sub; a < L; a += TPP) {
-      const double vx = AT(X, a) - ox, vy = AT(Yc, a) - oy, vz = AT(Zc, a) - oz;
-      store_split(Xo + (size_t)a * 2, fma(R0, vx, fma(R1, vy, fma(R2, vz, tx))),
-                  fma(R3, vx, fma(R4, vy, fma(R5, vz, ty))),
-                  fma(R6, vx, fma(R7, vy, fma(R8, vz, tz))));
-      if (RECORD)
-        Yo[a] = make_float4((float)AT(X, a), (float)AT(Yc, a), (float)AT(Zc, a), 0.f);
+      const float2 vx = dsub(AT(X, a), ox), vy = dsub(AT(Yc, a), oy), vz = dsub(AT(Zc, a), oz);
+      store_pair(Xo + (size_t)a * 2, ddot3c(R0, vx, R1, vy, R2, vz, tx),
+                 ddot3c(R3, vx, R4, vy, R5, vz, ty), ddot3c(R6, vx, R7, vy, R8, vz, tz));
+      if (RECORD) Yo[a] = make_float4(AT(X, a).x, AT(Yc, a).x, AT(Zc, a).x, 0.f);
     }
     if (sub == 0) {
-      if (RECORD) *ceno = make_float4((float)mx, (float)my, (float)mz, 0.f);
+      if (RECORD) *ceno = make_float4(mx.x, my.x, mz.x, 0.f);
       *statuso = status;
     }
   }
