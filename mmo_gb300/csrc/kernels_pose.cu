@@ -80,6 +80,61 @@ __device__ __forceinline__ void store_pair(float4* X, float2 x, float2 y, float2
 // statuso point at the pose's own slots (dof readable even when !live).
 // (not inlined: the one-system and the system-batch kernels share this code,
 // so both round every operation the same way)
+// entry k of the Rodrigues matrix of rot.ml:136-146 (c the cosine, o = 1 - c,
+// u the axis, us = u sin)
+__device__ __forceinline__ float2 rodrigues_entry(int k, float2 c, float2 ux, float2 uy, float2 uz,
+                                                  float2 o, float2 xs, float2 ys, float2 zs) {
+  switch (k) {
+    case 0: return dadd(c, dmul(ux, dmul(ux, o)));
+    case 1: return dsub(dmul(ux, dmul(uy, o)), zs);
+    case 2: return dadd(dmul(ux, dmul(uz, o)), ys);
+    case 3: return dadd(dmul(ux, dmul(uy, o)), zs);
+    case 4: return dadd(c, dmul(uy, dmul(uy, o)));
+    case 5: return dsub(dmul(uy, dmul(uz, o)), xs);
+    case 6: return dsub(dmul(ux, dmul(uz, o)), ys);
+    case 7: return dadd(dmul(uy, dmul(uz, o)), xs);
+    default: return dadd(c, dmul(uz, dmul(uz, o)));
+  }
+}
+
+// entry k of R = Rz(g) Ry(b) Rx(a) (rot.ml:52-66), k = 9..11 the translation
+__device__ __forceinline__ double rigid_entry(int k, const double* SC, const float* dof, float orx,
+                                              float ory, float orz) {
+  const double sa = SC[0], ca = SC[1], sb = SC[2], cb = SC[3], sg = SC[4], cg = SC[5];
+  switch (k) {
+    case 0: return cb * cg;
+    case 1: return cg * sa * sb - ca * sg;
+    case 2: return sa * sg + ca * cg * sb;
+    case 3: return cb * sg;
+    case 4: return ca * cg + sa * sb * sg;
+    case 5: return ca * sb * sg - cg * sa;
+    case 6: return -sb;
+    case 7: return cb * sa;
+    case 8: return ca * cb;
+    case 9: return (double)dof[0] - (double)orx;
+    case 10: return (double)dof[1] - (double)ory;
+    default: return (double)dof[2] - (double)orz;
+  }
+}
+
+// the value v of lane `src` of this pose's group of TPP lanes
+template <int TPP>
+__device__ __forceinline__ float2 from_lane(float2 v, int src) {
+  return make_float2(__shfl_sync(kFull, v.x, src, TPP), __shfl_sync(kFull, v.y, src, TPP));
+}
+
+// TPP threads share one pose: each rotates its share of the atoms; the
+// torsion axis is recomputed by all of them, the entries of each matrix are
+// split over them and exchanged by shuffles, and the sines and cosines of the
+// pose's angles are computed once (FP64), split over the TPP threads.
+// Coordinates, axes, matrices and the rigid map are double-float.  Small
+// batches use many threads per pose (the one-pose path uses a whole warp),
+// large batches fewer.
+//
+// rebuild_pose: one pose of the block's ligand; dof, Xo, Yo, reco, ceno and
+// statuso point at the pose's own slots (dof readable even when !live).
+// (not inlined: the one-system and the system-batch kernels share this code,
+// so both round every operation the same way)
 template <bool RECENTER, bool RECORD, int TPP>
 __device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof, bool live,
                                              float orx, float ory, float orz, float4* Xo,
@@ -116,23 +171,25 @@ __device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof
     const float2 inv = qts(r0, __fmul_rn(0.5f * r0, err.x));
     const float2 ux = dmul(ax, inv), uy = dmul(ay, inv), uz = dmul(az, inv);
     const float2 sn = df_of(SC[2 * (3 + t)]), cs = df_of(SC[2 * (3 + t) + 1]);
-    // Rodrigues matrix of rot.ml:136-146
     const float2 o = dsub(one, cs);
-    const float2 xo = dmul(ux, o), yo = dmul(uy, o), zo = dmul(uz, o);
     const float2 xs = dmul(ux, sn), ys = dmul(uy, sn), zs = dmul(uz, sn);
-    const float2 R0 = dadd(cs, dmul(ux, xo)), R1 = dsub(dmul(ux, yo), zs),
-                 R2 = dadd(dmul(ux, zo), ys);
-    const float2 R3 = dadd(dmul(ux, yo), zs), R4 = dadd(cs, dmul(uy, yo)),
-                 R5 = dsub(dmul(uy, zo), xs);
-    const float2 R6 = dsub(dmul(ux, zo), ys), R7 = dadd(dmul(uy, zo), xs),
-                 R8 = dadd(cs, dmul(uz, zo));
+    // the nine entries, split over the pose's lanes
+    float2 mine[(9 + TPP - 1) / TPP];
+#pragma unroll
+    for (int q = 0; q < (9 + TPP - 1) / TPP; ++q) {
+      const int k = sub + q * TPP;
+      mine[q] = k < 9 ? rodrigues_entry(k, cs, ux, uy, uz, o, xs, ys, zs) : one;
+    }
+    float2 R[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) R[k] = from_lane<TPP>(mine[k / TPP], k % TPP);
     __syncwarp();  // every thread of the pose has read the axis
     for (int k = lig.grp_off[t] + sub; k < lig.grp_off[t + 1]; k += TPP) {
       const int i = lig.grp_atoms[k];
       const float2 vx = dsub(AT(X, i), cx), vy = dsub(AT(Yc, i), cy), vz = dsub(AT(Zc, i), cz);
-      AT(X, i) = ddot3c(R0, vx, R1, vy, R2, vz, cx);
-      AT(Yc, i) = ddot3c(R3, vx, R4, vy, R5, vz, cy);
-      AT(Zc, i) = ddot3c(R6, vx, R7, vy, R8, vz, cz);
+      AT(X, i) = ddot3c(R[0], vx, R[1], vy, R[2], vz, cx);
+      AT(Yc, i) = ddot3c(R[3], vx, R[4], vy, R[5], vz, cy);
+      AT(Zc, i) = ddot3c(R[6], vx, R[7], vy, R[8], vz, cz);
     }
     if (RECORD && live && sub == 0) {
       float4* r = reco + (size_t)t * 3;
@@ -171,22 +228,24 @@ __device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof
     if (dgt(other, d2max)) d2max = other;
   }
   const int status = 0.01 + sqrt((double)d2max.x + (double)d2max.y) > 12.0 ? kStatusTooLong : 0;
-  // rigid map
-  const double sa = SC[0], ca = SC[1], sb = SC[2], cb = SC[3], sg = SC[4], cg = SC[5];
-  const float2 R0 = df_of(cb * cg), R1 = df_of(cg * sa * sb - ca * sg),
-               R2 = df_of(sa * sg + ca * cg * sb);
-  const float2 R3 = df_of(cb * sg), R4 = df_of(ca * cg + sa * sb * sg),
-               R5 = df_of(ca * sb * sg - cg * sa);
-  const float2 R6 = df_of(-sb), R7 = df_of(cb * sa), R8 = df_of(ca * cb);
-  const float2 tx = df_of((double)dof[0] - (double)orx), ty = df_of((double)dof[1] - (double)ory),
-               tz = df_of((double)dof[2] - (double)orz);
+  // rigid map: twelve entries (rotation, translation) split over the pose's lanes
+  float2 rm[(12 + TPP - 1) / TPP];
+#pragma unroll
+  for (int q = 0; q < (12 + TPP - 1) / TPP; ++q) {
+    const int k = sub + q * TPP;
+    rm[q] = k < 12 ? df_of(rigid_entry(k, SC, dof, orx, ory, orz)) : one;
+  }
+  float2 G[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) G[k] = from_lane<TPP>(rm[k / TPP], k % TPP);
   const float2 zero = make_float2(0.f, 0.f);
   const float2 ox = RECENTER ? mx : zero, oy = RECENTER ? my : zero, oz = RECENTER ? mz : zero;
   if (live) {
     for (int a = sub; a < L; a += TPP) {
       const float2 vx = dsub(AT(X, a), ox), vy = dsub(AT(Yc, a), oy), vz = dsub(AT(Zc, a), oz);
-      store_pair(Xo + (size_t)a * 2, ddot3c(R0, vx, R1, vy, R2, vz, tx),
-                 ddot3c(R3, vx, R4, vy, R5, vz, ty), ddot3c(R6, vx, R7, vy, R8, vz, tz));
+      store_pair(Xo + (size_t)a * 2, ddot3c(G[0], vx, G[1], vy, G[2], vz, G[9]),
+                 ddot3c(G[3], vx, G[4], vy, G[5], vz, G[10]),
+                 ddot3c(G[6], vx, G[7], vy, G[8], vz, G[11]));
       if (RECORD) Yo[a] = make_float4(AT(X, a).x, AT(Yc, a).x, AT(Zc, a).x, 0.f);
     }
     if (sub == 0) {
@@ -714,8 +773,8 @@ cudaError_t launch_rebuild(const DevLigand& lig, const PoseIO& io, const Scratch
   if (io.B <= 0) return cudaSuccess;
   const bool rc = flags & kFlagRecenter;
   const bool rec = (flags & kFlagGrad) && io.grad;
-  // threads per pose: enough threads in flight to hide FP64 latency (about
-  // 20,000, two 128-thread blocks per SM), within 200 KB of shared memory
+  // threads per pose: enough threads in flight to hide the latency (about
+  // 20,000), within 200 KB of shared memory
   int tpp = 32;
   while (tpp > 1 && (long)io.B * (tpp / 2) >= 20000) tpp /= 2;
   while (tpp < 32 && sizeof(double) * (3.0 * lig.L + 2.0 * (3 + kMaxTors)) *
