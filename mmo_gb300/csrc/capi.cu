@@ -324,6 +324,7 @@ DevLigand ligand_at(const LigBlob& B, char* b, size_t* bytes) {
   L.nested = B.nested ? 1 : 0;
   L.ref = align_ptr<float4>(b, off, n);
   L.ref64 = align_ptr<double>(b, off, 3 * (size_t)n);
+  L.ref2 = align_ptr<float2>(b, off, 3 * (size_t)n);
   L.type = align_ptr<int>(b, off, n);
   L.q = align_ptr<float>(b, off, n);
   L.bonds = align_ptr<int2>(b, off, B.nbonds);
@@ -432,6 +433,11 @@ void make_ligand_blob(int mixing, const LigIn& in, LigBlob* out) {
     r64[0] = in.x[i];
     r64[1] = in.y[i];
     r64[2] = in.z[i];
+    float2* r2 = const_cast<float2*>(H.ref2) + 3 * i;
+    for (int d = 0; d < 3; ++d) {
+      const float h = (float)r64[d];
+      r2[d] = make_float2(h, (float)(r64[d] - (double)h));
+    }
   }
   memcpy((void*)H.type, in.type.data(), sizeof(int) * n);
   for (int i = 0; i < n; ++i) const_cast<float*>(H.q)[i] = (float)in.q[i];
@@ -1165,8 +1171,8 @@ int sys_build_static(mmo_ctx* ctx, SysBatch* S) {
   // threads per pose of the rebuild, as launch_rebuild chooses them
   int tpp = 32;
   while (tpp > 1 && (long)S->B * (tpp / 2) >= 20000) tpp /= 2;
-  while (tpp < 32 && sizeof(double) * (3.0 * S->Lmax + 2.0 * (3 + kMaxTors)) * (128 / tpp) >
-                         200.0 * 1024)
+  while (tpp < 32 && (sizeof(double) * (3.0 * S->Lmax + 2.0 * (3 + kMaxTors)) +
+                      sizeof(float4) * kMaxTors) * (128 / tpp) > 200.0 * 1024)
     tpp *= 2;
   S->tpp = tpp;
   const int ppb = 128 / tpp;

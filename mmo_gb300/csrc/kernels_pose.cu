@@ -142,7 +142,8 @@ __device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof
                                              int* statuso) {
   constexpr int PPB = kRebuildThreads / TPP;  // poses per block
   constexpr int NANG = 3 + kMaxTors;
-  // [3][L][PPB] double-float coordinates, then [PPB][NANG][2] FP64 sin, cos
+  // [3][L][PPB] double-float coordinates, then [PPB][NANG] FP64 (sin, cos),
+  // then [PPB][kMaxTors] double-float (sin, cos) of the torsions
   extern __shared__ double sz[];
   const int tid = threadIdx.x, p = tid / TPP, sub = tid % TPP;
   const int L = lig.L, nrb = lig.nrb;
@@ -150,13 +151,20 @@ __device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof
   float2* Yc = X + L * PPB;
   float2* Zc = X + 2 * L * PPB;
   double* SC = sz + 3 * L * PPB + p * NANG * 2;
+  float4* TSC = reinterpret_cast<float4*>(sz + 3 * L * PPB + PPB * NANG * 2) + p * kMaxTors;
 #define AT(arr, a) arr[(a) * PPB + p]
   for (int a = sub; a < L; a += TPP) {
-    AT(X, a) = df_of(lig.ref64[3 * a]);
-    AT(Yc, a) = df_of(lig.ref64[3 * a + 1]);
-    AT(Zc, a) = df_of(lig.ref64[3 * a + 2]);
+    AT(X, a) = lig.ref2[3 * a];
+    AT(Yc, a) = lig.ref2[3 * a + 1];
+    AT(Zc, a) = lig.ref2[3 * a + 2];
   }
-  for (int k = sub; k < 3 + nrb; k += TPP) sincos((double)dof[3 + k], &SC[2 * k], &SC[2 * k + 1]);
+  for (int k = sub; k < 3 + nrb; k += TPP) {
+    sincos((double)dof[3 + k], &SC[2 * k], &SC[2 * k + 1]);
+    if (k >= 3) {
+      const float2 sn = df_of(SC[2 * k]), cs = df_of(SC[2 * k + 1]);
+      TSC[k - 3] = make_float4(sn.x, sn.y, cs.x, cs.y);
+    }
+  }
   __syncwarp();
   const float2 one = make_float2(1.f, 0.f);
   for (int t = 0; t < nrb; ++t) {
@@ -170,7 +178,8 @@ __device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof
     const float2 err = dsub(one, dmul(n2, dmul(make_float2(r0, 0.f), make_float2(r0, 0.f))));
     const float2 inv = qts(r0, __fmul_rn(0.5f * r0, err.x));
     const float2 ux = dmul(ax, inv), uy = dmul(ay, inv), uz = dmul(az, inv);
-    const float2 sn = df_of(SC[2 * (3 + t)]), cs = df_of(SC[2 * (3 + t) + 1]);
+    const float4 tsc = TSC[t];
+    const float2 sn = make_float2(tsc.x, tsc.y), cs = make_float2(tsc.z, tsc.w);
     const float2 o = dsub(one, cs);
     const float2 xs = dmul(ux, sn), ys = dmul(uy, sn), zs = dmul(uz, sn);
     // the nine entries, split over the pose's lanes
@@ -653,7 +662,8 @@ template <bool RC, bool REC, int TPP>
 cudaError_t rebuild_t(const DevLigand& lig, const PoseIO& io, const Scratch& s, cudaStream_t st) {
   constexpr int PPB = kRebuildThreads / TPP;
   const int blocks = (io.B + PPB - 1) / PPB;
-  const size_t smem = sizeof(double) * ((size_t)3 * lig.L * PPB + (size_t)PPB * (3 + kMaxTors) * 2);
+  const size_t smem = sizeof(double) * ((size_t)3 * lig.L * PPB + (size_t)PPB * (3 + kMaxTors) * 2) +
+                      sizeof(float4) * (size_t)PPB * kMaxTors;
   cudaError_t e = cudaFuncSetAttribute(k_rebuild<RC, REC, TPP>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -737,7 +747,8 @@ template <bool RC, bool REC>
 cudaError_t sys_rebuild_tpp(int tpp, const DevSystems& S, int nblk, const PoseIO& io,
                             const Scratch& s, cudaStream_t st) {
   const int ppb = kRebuildThreads / tpp;
-  const int smem = (int)(sizeof(double) * (3 * (size_t)S.Lmax * ppb + (size_t)ppb * (3 + kMaxTors) * 2));
+  const int smem = (int)(sizeof(double) * (3 * (size_t)S.Lmax * ppb + (size_t)ppb * (3 + kMaxTors) * 2) +
+                         sizeof(float4) * (size_t)ppb * kMaxTors);
 #define MMO_SR(T)                                                                          \
   case T: {                                                                                \
     cudaError_t e = cudaFuncSetAttribute(k_sys_rebuild<RC, REC, T>,                        \
@@ -777,8 +788,8 @@ cudaError_t launch_rebuild(const DevLigand& lig, const PoseIO& io, const Scratch
   // 20,000), within 200 KB of shared memory
   int tpp = 32;
   while (tpp > 1 && (long)io.B * (tpp / 2) >= 20000) tpp /= 2;
-  while (tpp < 32 && sizeof(double) * (3.0 * lig.L + 2.0 * (3 + kMaxTors)) *
-                             (kRebuildThreads / tpp) > 200.0 * 1024)
+  while (tpp < 32 && (sizeof(double) * (3.0 * lig.L + 2.0 * (3 + kMaxTors)) +
+                      sizeof(float4) * kMaxTors) * (kRebuildThreads / tpp) > 200.0 * 1024)
     tpp *= 2;
   if (rc) return rec ? rebuild_tpp<true, true>(tpp, lig, io, s, st)
                      : rebuild_tpp<true, false>(tpp, lig, io, s, st);

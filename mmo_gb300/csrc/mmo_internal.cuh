@@ -57,6 +57,7 @@ struct DevLigand {
   int nested;
   const float4* ref;        // [L] (x, y, z, q) centred conformer, rounded to float
   const double* ref64;      // [L][3] the same conformer in double
+  const float2* ref2;       // [L][3] the same conformer as float pairs (hi, lo)
   const int* type;          // [L] type index
   const float* q;           // [L] partial charge
   const int2* bonds;        // [nrb] (left, right) rotation axis
