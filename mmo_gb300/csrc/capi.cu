@@ -636,8 +636,45 @@ struct RowIndex {
   std::vector<int> rs;          // [nrows + 1]
   std::vector<float4> rbox;     // [nrows]
   std::vector<int> flush_end;   // [nrows]
+  std::vector<float4> pairs;    // [npairs][4] the cut-off sweep's layout (build_pairs)
+  std::vector<int> prs;         // [nrows + 1] first pair of each row
   float lo[3], hi[3];           // bounding box (hi parts)
 };
+
+// The cut-off sweep's copy of a row index: the atoms of each row in pairs
+// (2j, 2j + 1), as four float4 per pair, negated coordinates so that the sweep
+// adds them: (-x_hi a, -x_hi b, -y_hi a, -y_hi b), (-z_hi a, -z_hi b, Kq a, Kq b),
+// the lo halves likewise, (-z_lo a, -z_lo b, type offset a, type offset b).  A
+// row of odd length ends with a null partner: its last atom again, with charge
+// -0 (a zero charge of a real atom is +0) and the null type row (all zeros),
+// whose terms are exact zeros.
+void build_pairs(RowIndex* io) {
+  RowIndex& R = *io;
+  const int nrows = (int)R.rbox.size();
+  R.prs.assign(nrows + 1, 0);
+  R.pairs.clear();
+  for (int r = 0; r < nrows; ++r) {
+    R.prs[r] = (int)(R.pairs.size() / 4);
+    for (int a = R.rs[r]; a < R.rs[r + 1]; a += 2) {
+      const bool real_b = a + 1 < R.rs[r + 1];
+      const float4 ah = R.atoms[2 * (size_t)a], al = R.atoms[2 * (size_t)a + 1];
+      const float4 bh = real_b ? R.atoms[2 * (size_t)a + 2] : ah;
+      const float4 bl = real_b ? R.atoms[2 * (size_t)a + 3] : al;
+      const float wa = ah.w == 0.f ? 0.f : ah.w;
+      const float wb = real_b ? (bh.w == 0.f ? 0.f : bh.w) : -0.f;
+      float offb = bl.w;
+      if (!real_b) {
+        const int nb = kNullTypeRow * kNTypes * (int)sizeof(float4);
+        memcpy(&offb, &nb, sizeof nb);
+      }
+      R.pairs.push_back(make_float4(-ah.x, -bh.x, -ah.y, -bh.y));
+      R.pairs.push_back(make_float4(-ah.z, -bh.z, wa, wb));
+      R.pairs.push_back(make_float4(-al.x, -bl.x, -al.y, -bl.y));
+      R.pairs.push_back(make_float4(-al.z, -bl.z, al.w, offb));
+    }
+  }
+  R.prs[nrows] = (int)(R.pairs.size() / 4);
+}
 
 void build_rows(int n, const double* px, const double* py, const double* pz, const float* pkq,
                 const int* ptypes, double h, RowIndex* out) {
@@ -714,6 +751,7 @@ void build_rows(int n, const double* px, const double* py, const double* pz, con
     if (rflush[r]) end = r + 1;
     R.flush_end[r] = end;
   }
+  build_pairs(&R);
 }
 
 // pieces of a row index: consecutive rows of about piece_atoms atoms, as row
@@ -752,11 +790,15 @@ int build_cull(mmo_ctx* ctx) {
   const size_t o_rs = take(off, sizeof(int) * R.rs.size());
   const size_t o_box = take(off, sizeof(float4) * R.rbox.size());
   const size_t o_fl = take(off, sizeof(int) * R.flush_end.size());
+  const size_t o_pairs = take(off, sizeof(float4) * R.pairs.size());
+  const size_t o_prs = take(off, sizeof(int) * R.prs.size());
   std::vector<char> blob(off, 0);
   memcpy(blob.data() + o_atoms, R.atoms.data(), sizeof(float4) * R.atoms.size());
   memcpy(blob.data() + o_rs, R.rs.data(), sizeof(int) * R.rs.size());
   memcpy(blob.data() + o_box, R.rbox.data(), sizeof(float4) * R.rbox.size());
   memcpy(blob.data() + o_fl, R.flush_end.data(), sizeof(int) * R.flush_end.size());
+  memcpy(blob.data() + o_pairs, R.pairs.data(), sizeof(float4) * R.pairs.size());
+  memcpy(blob.data() + o_prs, R.prs.data(), sizeof(int) * R.prs.size());
   MMO_CK(cudaMalloc(&ctx->d_cull, off), "protein row index");
   MMO_CK(cudaMemcpy(ctx->d_cull, blob.data(), off, cudaMemcpyHostToDevice), "row index upload");
   DevCull c{};
@@ -765,8 +807,11 @@ int build_cull(mmo_ctx* ctx) {
   c.row_start = reinterpret_cast<const int*>(base + o_rs);
   c.row_box = reinterpret_cast<const float4*>(base + o_box);
   c.row_flush = reinterpret_cast<const int*>(base + o_fl);
+  c.pairs = reinterpret_cast<const float4*>(base + o_pairs);
+  c.pair_start = reinterpret_cast<const int*>(base + o_prs);
   c.P = n;
   c.nrows = nrows;
+  c.npairs = R.prs[nrows];
   // entry binning: a cube about the protein's box, 2 A beyond it
   float side = 0.f;
   for (int d = 0; d < 3; ++d) side = std::max(side, R.hi[d] - R.lo[d]);
@@ -781,7 +826,7 @@ int build_cull(mmo_ctx* ctx) {
   ++ctx->cull_version;
   ++ctx->epoch;
   // the sweep keeps the whole protein and its index in shared memory
-  ctx->cull_ok = cull_smem_bytes(n, nrows, nrows, 1024) <= ctx->smem_optin;
+  ctx->cull_ok = cull_smem_bytes(c.npairs, nrows, nrows, 1024) <= ctx->smem_optin;
   return MMO_OK;
 }
 
@@ -878,7 +923,7 @@ int cull_plan_for(mmo_ctx* ctx, int B, bool grad) {
     sg.type[t] = ctx->lseg_type[t];
     sg.off[t + 1] = sg.off[t] + (sg.n[t] + sg.G - 1) / sg.G * sg.G;
   }
-  p.smem = cull_smem_bytes(ctx->cull.P, ctx->cull.nrows, npieces, p.threads);
+  p.smem = cull_smem_bytes(ctx->cull.npairs, ctx->cull.nrows, npieces, p.threads);
   const int bps = std::max(1, cull_max_blocks(p.kp, p.threads, grad, ctx->ph, p.smem));
   p.blocks = ctx->sms * bps;
   const long items = (long)sg.off[sg.nseg] / sg.G * npieces;
@@ -1044,7 +1089,8 @@ struct SysBatch {
   std::vector<SysInfo> info;           // virtual systems: user systems cut to sort-sized pose ranges
   std::vector<int> vuser;              // virtual -> user system
   std::vector<std::vector<int>> rows;  // per user system: row starts of its row index
-  std::vector<int> atom0, row0;        // per user system: packed atom and row offsets
+  std::vector<std::vector<int>> prows;  // per user system: first pair of each row
+  std::vector<int> row0, pair0;        // per user system: packed row and pair offsets
   std::vector<std::vector<int>> segcount, segtype;  // per user system: ligand type segments
   std::vector<int> Ls, nrbs;
   void* d_static = nullptr;
@@ -1098,7 +1144,8 @@ int sys_build_static(mmo_ctx* ctx, SysBatch* S) {
   std::vector<LigBlob> blobs(ns);
   std::vector<RowIndex> ri(ns);
   S->rows.assign(ns, {});
-  S->atom0.assign(ns + 1, 0);
+  S->pair0.assign(ns + 1, 0);
+  S->prows.assign(ns, {});
   S->row0.assign(ns + 1, 0);
   S->segcount.assign(ns, {});
   S->segtype.assign(ns, {});
@@ -1116,10 +1163,12 @@ int sys_build_static(mmo_ctx* ctx, SysBatch* S) {
                  &ri[u]);
     } else {
       ri[u].rs = {0};
+      ri[u].prs = {0};
       for (int d = 0; d < 3; ++d) ri[u].lo[d] = ri[u].hi[d] = 0.f;
     }
     S->rows[u] = ri[u].rs;
-    S->atom0[u + 1] = S->atom0[u] + np;
+    S->prows[u] = ri[u].prs;
+    S->pair0[u + 1] = S->pair0[u] + (int)(ri[u].pairs.size() / 4);
     S->row0[u + 1] = S->row0[u] + (int)ri[u].rbox.size();
     S->segcount[u] = blobs[u].seg_count;
     S->segtype[u] = blobs[u].seg_type;
@@ -1193,8 +1242,8 @@ int sys_build_static(mmo_ctx* ctx, SysBatch* S) {
     lig_off[u] = off;
     off += blobs[u].host.size();
   }
-  const int P = S->atom0[ns], nrows = S->row0[ns];
-  const size_t o_atoms = take(off, sizeof(float4) * 2 * (size_t)std::max(P, 1));
+  const int NP = S->pair0[ns], nrows = S->row0[ns];
+  const size_t o_atoms = take(off, sizeof(float4) * 4 * (size_t)std::max(NP, 1));
   const size_t o_rs = take(off, sizeof(int) * (nrows + 1));
   const size_t o_box = take(off, sizeof(float4) * std::max(nrows, 1));
   const size_t o_fe = take(off, sizeof(int) * std::max(nrows, 1));
@@ -1211,16 +1260,16 @@ int sys_build_static(mmo_ctx* ctx, SysBatch* S) {
   int* fe = reinterpret_cast<int*>(host.data() + o_fe);
   for (int u = 0; u < ns; ++u) {
     const RowIndex& R = ri[u];
-    if (!R.atoms.empty())
-      memcpy(atoms + 2 * (size_t)S->atom0[u], R.atoms.data(), sizeof(float4) * R.atoms.size());
+    if (!R.pairs.empty())
+      memcpy(atoms + 4 * (size_t)S->pair0[u], R.pairs.data(), sizeof(float4) * R.pairs.size());
     const int nr = (int)R.rbox.size();
     for (int r = 0; r < nr; ++r) {
-      rs[S->row0[u] + r] = S->atom0[u] + R.rs[r];
+      rs[S->row0[u] + r] = S->pair0[u] + R.prs[r];
       box[S->row0[u] + r] = R.rbox[r];
       fe[S->row0[u] + r] = S->row0[u] + R.flush_end[r];
     }
   }
-  rs[nrows] = P;
+  rs[nrows] = NP;
   memcpy(host.data() + o_info, S->info.data(), sizeof(SysInfo) * nv);
   memcpy(host.data() + o_rb, rblk.data(), sizeof(SysBlk) * rblk.size());
   memcpy(host.data() + o_fb, fblk.data(), sizeof(SysBlk) * fblk.size());
@@ -1240,7 +1289,7 @@ int sys_build_static(mmo_ctx* ctx, SysBatch* S) {
   D.lig = reinterpret_cast<const DevLigand*>(d + o_lig);
   D.rblk = reinterpret_cast<const SysBlk*>(d + o_rb);
   D.fblk = reinterpret_cast<const SysBlk*>(d + o_fb);
-  D.atoms = reinterpret_cast<const float4*>(d + o_atoms);
+  D.pairs = reinterpret_cast<const float4*>(d + o_atoms);
   D.row_start = reinterpret_cast<const int*>(d + o_rs);
   D.row_box = reinterpret_cast<const float4*>(d + o_box);
   D.flush_end = reinterpret_cast<const int*>(d + o_fe);
@@ -1271,11 +1320,12 @@ int sys_build_plan(mmo_ctx* ctx, SysBatch* S, bool grad) {
       const std::vector<int>& rs = S->rows[u];
       const int nr = (int)rs.size() - 1;
       if (nr <= 0) {  // no protein: one empty piece, so that the groups still close
-        pieces.push_back(make_int4(S->atom0[u], S->atom0[u], S->row0[u], S->row0[u]));
+        pieces.push_back(make_int4(S->pair0[u], S->pair0[u], S->row0[u], S->row0[u]));
       } else {
         const std::vector<int> pr = row_pieces(rs, piece_atoms);
+        const std::vector<int>& prs = S->prows[u];
         for (size_t k = 0; k + 1 < pr.size(); ++k) {
-          const int a0 = S->atom0[u] + rs[pr[k]], a1 = S->atom0[u] + rs[pr[k + 1]];
+          const int a0 = S->pair0[u] + prs[pr[k]], a1 = S->pair0[u] + prs[pr[k + 1]];
           pieces.push_back(make_int4(a0, a1, S->row0[u] + pr[k], S->row0[u] + pr[k + 1]));
           amax = std::max(amax, a1 - a0);
           rmax = std::max(rmax, pr[k + 1] - pr[k]);
@@ -1337,7 +1387,7 @@ int sys_build_plan(mmo_ctx* ctx, SysBatch* S, bool grad) {
     D.nitems = (int)items.size();
     D.ngroups = (int)groups.size();
     D.G = G;
-    D.piece_atoms_max = amax;
+    D.piece_pairs_max = amax;
     D.piece_rows_max = rmax;
     S->kp = kp;
     S->slots = slot;
@@ -1357,7 +1407,7 @@ int sys_build_plan(mmo_ctx* ctx, SysBatch* S, bool grad) {
   const long lkey[4] = {S->plan_key[0], S->plan_key[1], threads,
                         ctx->ph.dielectric * 2 + ctx->ph.inter_form};
   if (!std::equal(lkey, lkey + 4, S->launch_key[g])) {
-    const int smem = sys_pairs_smem(S->dev.piece_atoms_max, S->dev.piece_rows_max, threads);
+    const int smem = sys_pairs_smem(S->dev.piece_pairs_max, S->dev.piece_rows_max, threads);
     const int bps = std::max(1, sys_pairs_max_blocks(S->kp, threads, grad, ctx->ph, smem));
     S->lthreads[g] = threads;
     S->lsmem[g] = smem;
@@ -2024,8 +2074,11 @@ int mmo_tune(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E, f
       for (double h : {2.0, 3.0, 4.0})
         for (int kp : {1, 2, 4})
           for (int piece : {256, 512}) {
-            cands.push_back({1, h, kp, piece, cull_max_threads(kp), 0});
-            if (cull_max_threads(kp) != 512) cands.push_back({1, h, kp, piece, 512, 0});
+            // the register budget's thread count, and fewer warps with more shared
+            // memory left to the L1
+            const int th = cull_max_threads(kp);
+            cands.push_back({1, h, kp, piece, th, 0});
+            if (th >= 512) cands.push_back({1, h, kp, piece, th - 256, 0});
           }
     for (int kp : {1, 2, 4})
       for (int ch : {4, 8, 12, 16, 24}) cands.push_back({0, ctx->cull_h, kp, 0, 512, ch});

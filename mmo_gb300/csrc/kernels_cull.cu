@@ -25,6 +25,21 @@ namespace {
 constexpr uint32_t kWaitPolls = 1u << 22;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kListCap = 64;  // a warp's list: under 32 left over plus one window of 32
+constexpr int kTabRows = kNullTypeRow + 1;  // protein types of the shared pair table
+
+// the pair table in shared memory: [ptype][ltype] (X, 1/D, c1, 0) with
+// c1 = 11/D (eps = 4) or 5/D (eps = 4r), and the null type row of zeros
+template <int DIEL>
+__device__ __forceinline__ void stage_pair_table(const float4* __restrict__ tabv, float4* s_tab) {
+  for (int k = threadIdx.x; k < kTabRows * kNTypes; k += blockDim.x) {
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (k < kNTypes * kNTypes) {
+      v = tabv[k];
+      v = make_float4(v.x, v.y, (DIEL == 0 ? 11.0f : 5.0f) * v.y, 0.f);
+    }
+    s_tab[k] = v;
+  }
+}
 
 // Index of cell (x, y, z) of the 32^3 binning grid along a 3-D Hilbert curve
 // (J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc. 707, 2004:
@@ -155,7 +170,20 @@ __global__ void k_cull_scatter(const float4* __restrict__ X, int n, int L,
   order[slot] = e;
 }
 
-// dE/dX of one entry over the protein atoms [a0, a1) with the per-pair test
+// (X, 1/D, c1) of the protein atoms a and b of a pair against the warp's
+// ligand type (trow): their rows of the pair table, at the byte offsets a3.zw
+__device__ __forceinline__ void pair_params(const float4* trow, float4 a3, float2& X, float2& iD,
+                                            float2& c1) {
+  const float* ta =
+      reinterpret_cast<const float*>(reinterpret_cast<const char*>(trow) + __float_as_int(a3.z));
+  const float* tb =
+      reinterpret_cast<const float*>(reinterpret_cast<const char*>(trow) + __float_as_int(a3.w));
+  X = make_float2(ta[0], tb[0]);
+  iD = make_float2(ta[1], tb[1]);
+  c1 = make_float2(ta[2], tb[2]);
+}
+
+// dE/dX of one entry over the protein pairs [a0, a1) with the per-pair test
 // of the 0.01 A clamp; the same arithmetic in the same order as the sweep, so
 // entries without a clamped pair get the sweep's value bit for bit.
 template <int DIEL, int FORM>
@@ -163,15 +191,18 @@ __device__ __noinline__ float3 cull_exact_grad(const float4* sp, const float4* t
                                                float q, float xh, float yh, float zh, float xl,
                                                float yl, float zl) {
   constexpr float c0 = DIEL == 0 ? -10.0f : -4.0f;
-  float acc = 0.f, gx = 0.f, gy = 0.f, gz = 0.f, mn = 1e30f;
+  float2 acc = bc2(0.f), gx = bc2(0.f), gy = bc2(0.f), gz = bc2(0.f);
+  float mn = 1e30f;
   for (int i = a0; i < a1; ++i) {
-    const float4 p = sp[2 * i], pl = sp[2 * i + 1];
-    const float4 pv = *reinterpret_cast<const float4*>(reinterpret_cast<const char*>(trow) +
-                                                       __float_as_int(pl.w));
-    pair_step<true, DIEL, FORM, true>(xh, yh, zh, xl, yl, zl, p, pl, p.w * q, pv.x, pv.y, pv.z, c0,
-                                   acc, gx, gy, gz, mn);
+    const float4* pp = sp + 4 * i;
+    const float4 p0 = pp[0], p1 = pp[1], p2 = pp[2], p3 = pp[3];
+    float2 X, iD, c1;
+    pair_params(trow, p3, X, iD, c1);
+    pair_step_ab<true, DIEL, FORM, true>(bc2(xh), bc2(yh), bc2(zh), bc2(xl), bc2(yl), bc2(zl),
+                                         bc2(q), p0, p1, p2, p3, X, iD, c1, c0, acc, gx, gy, gz,
+                                         mn);
   }
-  return make_float3(gx, gy, gz);
+  return make_float3(gx.x + gx.y, gy.x + gy.y, gz.x + gz.y);
 }
 
 __device__ __forceinline__ float warp_min(float v) {
@@ -185,12 +216,22 @@ __device__ __forceinline__ float warp_maxf(float v) {
   return v;
 }
 
+// squared distance from (x, y, z) to the box [bl, bh]
+__device__ __forceinline__ float box_d2(float x, float y, float z, float blx, float bly, float blz,
+                                        float bhx, float bhy, float bhz) {
+  const float ex = fmaxf(fmaxf(blx - x, x - bhx), 0.f);
+  const float ey = fmaxf(fmaxf(bly - y, y - bhy), 0.f);
+  const float ez = fmaxf(fmaxf(blz - z, z - bhz), 0.f);
+  return fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+}
+
 // One warp's work for one (group, protein piece) item: the group's entries
 // [slot0, s_end) (32 * KP slots, padding repeats the last entry) against the
-// piece's rows [r0, r1) resident in shared memory (sp, s_rbox, s_rs, s_flush),
-// then the piece's partials at P0 + kpc * PS (+ slot - slot0) and its flag at
-// V0 + kpc; the last of the group's npieces items to arrive sums them.  CULL
-// false visits every atom (the global form).
+// piece's rows [r0, r1) resident in shared memory (sp: pairs of atoms, s_rbox,
+// s_rs: first pair of each row, s_flush), then the piece's partials at
+// P0 + kpc * PS (+ slot - slot0) and its flag at V0 + kpc; the last of the
+// group's npieces items to arrive sums them.  CULL false visits every atom
+// (the global form).
 template <int KP, bool GRAD, int DIEL, int FORM, bool CULL>
 __device__ __forceinline__ void sweep_item(const float4* sp, const float4* s_rbox, const int* s_rs,
                                            const int* s_flush, int r0, int r1,
@@ -200,22 +241,24 @@ __device__ __forceinline__ void sweep_item(const float4* sp, const float4* s_rbo
   constexpr float c0v = DIEL == 0 ? -10.0f : -4.0f;
   constexpr int G = 32 * KP;
   const int lane = threadIdx.x & 31;
-  float xh[KP], yh[KP], zh[KP], xl[KP], yl[KP], zl[KP], q[KP];
-  float acc[KP], gx[KP], gy[KP], gz[KP];
+  // the lane's entries, each value in both halves (one per atom of a pair);
+  // half x sums the even atoms of each row, half y the odd ones
+  float2 xh[KP], yh[KP], zh[KP], xl[KP], yl[KP], zl[KP], q[KP];
+  float2 acc[KP], gx[KP], gy[KP], gz[KP];
   double ad[KP];
   float blx = 1e30f, bly = 1e30f, blz = 1e30f, bhx = -1e30f, bhy = -1e30f, bhz = -1e30f;
 #pragma unroll
   for (int k = 0; k < KP; ++k) {
     const int s = min(slot0 + k * 32 + lane, s_end - 1);
     const float4 h = cs.Xs[2 * (size_t)s], l = cs.Xs[2 * (size_t)s + 1];
-    xh[k] = h.x;
-    yh[k] = h.y;
-    zh[k] = h.z;
-    q[k] = h.w;
-    xl[k] = l.x;
-    yl[k] = l.y;
-    zl[k] = l.z;
-    acc[k] = gx[k] = gy[k] = gz[k] = 0.f;
+    xh[k] = bc2(h.x);
+    yh[k] = bc2(h.y);
+    zh[k] = bc2(h.z);
+    q[k] = bc2(h.w);
+    xl[k] = bc2(l.x);
+    yl[k] = bc2(l.y);
+    zl[k] = bc2(l.z);
+    acc[k] = gx[k] = gy[k] = gz[k] = bc2(0.f);
     ad[k] = 0.0;
     blx = fminf(blx, h.x);
     bly = fminf(bly, h.y);
@@ -232,22 +275,24 @@ __device__ __forceinline__ void sweep_item(const float4* sp, const float4* s_rbo
   bhz = warp_maxf(bhz);
 
   float mn = 1e30f;
-  int visited = 0;
-  // the atoms of the warp's candidate rows within 12 A of the box, compacted
-  // in ascending order into the warp's list wl and swept 32 or more at a time
+  int visited = 0;       // pairs swept
+  unsigned natoms = 0;   // atoms of them within reach of the box (the pair counter)
+  // the pairs of the warp's candidate rows with an atom within 12 A of the
+  // box, compacted in ascending order into the warp's list wl and swept 32 or
+  // more at a time
   int cnt = 0;
   auto sweep = [&](int n) {
     __syncwarp();
 #pragma unroll 2
     for (int v = 0; v < n; ++v) {
-      const float4* pp = sp + 2 * wl[v];
-      const float4 p = pp[0], pl = pp[1];
-      const float4 pv = *reinterpret_cast<const float4*>(reinterpret_cast<const char*>(trow) +
-                                                         __float_as_int(pl.w));
+      const float4* pp = sp + 4 * wl[v];
+      const float4 p0 = pp[0], p1 = pp[1], p2 = pp[2], p3 = pp[3];
+      float2 X, iD, c1;
+      pair_params(trow, p3, X, iD, c1);
 #pragma unroll
       for (int k = 0; k < KP; ++k)
-        pair_step<GRAD, DIEL, FORM>(xh[k], yh[k], zh[k], xl[k], yl[k], zl[k], p, pl, p.w * q[k],
-                                 pv.x, pv.y, pv.z, c0v, acc[k], gx[k], gy[k], gz[k], mn);
+        pair_step_ab<GRAD, DIEL, FORM>(xh[k], yh[k], zh[k], xl[k], yl[k], zl[k], q[k], p0, p1, p2,
+                                       p3, X, iD, c1, c0v, acc[k], gx[k], gy[k], gz[k], mn);
     }
     __syncwarp();
   };
@@ -259,21 +304,24 @@ __device__ __forceinline__ void sweep_item(const float4* sp, const float4* s_rbo
       const float4 rb = s_rbox[r];
       const float dy = fmaxf(fmaxf(rb.x - bhy, bly - rb.y), 0.f);
       const float dz = fmaxf(fmaxf(rb.z - bhz, blz - rb.w), 0.f);
-      if (fmaf(dy, dy, dz * dz) >= kCullR2) continue;
+      if (CULL && fmaf(dy, dy, dz * dz) >= kCullR2) continue;
       const int a = s_rs[r], b = s_rs[r + 1];
       for (int i0 = a; i0 < b; i0 += 32) {
         const int i = i0 + lane;
-        bool in = false;
+        bool in_a = false, in_b = false;
         if (i < b) {
-          const float4 ph = sp[2 * i];
-          const float ex = fmaxf(fmaxf(blx - ph.x, ph.x - bhx), 0.f);
-          const float ey = fmaxf(fmaxf(bly - ph.y, ph.y - bhy), 0.f);
-          const float ez = fmaxf(fmaxf(blz - ph.z, ph.z - bhz), 0.f);
-          in = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < kCullR2;
+          const float4 p0 = sp[4 * i], p1 = sp[4 * i + 1];
+          const bool null_b = __float_as_uint(p1.w) == 0x80000000u;
+          in_a = !CULL || box_d2(-p0.x, -p0.z, -p1.x, blx, bly, blz, bhx, bhy, bhz) < kCullR2;
+          in_b = !null_b &&
+                 (!CULL || box_d2(-p0.y, -p0.w, -p1.y, blx, bly, blz, bhx, bhy, bhz) < kCullR2);
         }
+        const bool in = in_a || in_b;
         const unsigned m = __ballot_sync(kFull, in);
         if (in) wl[cnt + __popc(m & ((1u << lane) - 1u))] = i;
         cnt += __popc(m);
+        // the atoms that pass the test (a partner that does not is swept anyway)
+        natoms += __popc(__ballot_sync(kFull, in_a)) + __popc(__ballot_sync(kFull, in_b));
         if (cnt >= 32) {
           sweep(cnt);
           visited += cnt;
@@ -286,24 +334,25 @@ __device__ __forceinline__ void sweep_item(const float4* sp, const float4* s_rbo
     cnt = 0;
 #pragma unroll
     for (int k = 0; k < KP; ++k) {
-      ad[k] += (double)acc[k];
-      acc[k] = 0.f;
+      ad[k] += (double)acc[k].x;
+      ad[k] += (double)acc[k].y;
+      acc[k] = bc2(0.f);
     }
   }
+  float3 gsum[KP];
+#pragma unroll
+  for (int k = 0; k < KP; ++k)
+    gsum[k] = make_float3(gx[k].x + gx[k].y, gy[k].x + gy[k].y, gz[k].x + gz[k].y);
   if (GRAD && __any_sync(kFull, mn < kMinR2)) {
     // a pair closer than 0.01 A, where the clamped distance makes the
     // derivative 0: redo the gradient over the piece with the per-pair test
     const int a0 = s_rs[r0], a1 = s_rs[r1];
 #pragma unroll
-    for (int k = 0; k < KP; ++k) {
-      const float3 gg = cull_exact_grad<DIEL, FORM>(sp, trow, a0, a1, q[k], xh[k], yh[k], zh[k], xl[k],
-                                              yl[k], zl[k]);
-      gx[k] = gg.x;
-      gy[k] = gg.y;
-      gz[k] = gg.z;
-    }
+    for (int k = 0; k < KP; ++k)
+      gsum[k] = cull_exact_grad<DIEL, FORM>(sp, trow, a0, a1, q[k].x, xh[k].x, yh[k].x, zh[k].x,
+                                            xl[k].x, yl[k].x, zl[k].x);
   }
-  if (lane == 0 && visited) atomicAdd(cs.pairs, (unsigned long long)visited * G);
+  if (lane == 0 && natoms) atomicAdd(cs.pairs, (unsigned long long)natoms * G);
   constexpr float gs = DIEL == 0 ? -1.0f : -2.0f;
   if (visited) {  // a piece out of range of the group adds nothing
 #pragma unroll
@@ -312,7 +361,7 @@ __device__ __forceinline__ void sweep_item(const float4* sp, const float4* s_rbo
       if (s < s_end) {
         const size_t o = (size_t)(P0 + (long long)kpc * PS) + (size_t)(s - slot0);
         cs.Ep[o] = ad[k];
-        if (GRAD) cs.Gp[o] = make_float4(gs * gx[k], gs * gy[k], gs * gz[k], 0.f);
+        if (GRAD) cs.Gp[o] = make_float4(gs * gsum[k].x, gs * gsum[k].y, gs * gsum[k].z, 0.f);
       }
     }
   }
@@ -345,7 +394,7 @@ __device__ __forceinline__ void sweep_item(const float4* sp, const float4* s_rbo
         }
       }
       // an entry at a non-finite position can fall in a group far from the protein
-      if (!isfinite(xh[k]) || !isfinite(yh[k]) || !isfinite(zh[k]))
+      if (!isfinite(xh[k].x) || !isfinite(yh[k].x) || !isfinite(zh[k].x))
         E = __longlong_as_double(0x7ff8000000000000ll);
       const int e = cs.order[s];
       cs.Eout[e] = E;
@@ -358,23 +407,23 @@ template <int KP, bool GRAD, int DIEL>
 __global__ void __launch_bounds__(cull_max_threads(KP))
     k_pairs_cull(DevCull cull, const float4* __restrict__ tabv, CullSegs seg, CullScratch cs,
                  int* err) {
-  extern __shared__ __align__(16) float4 sp[];  // [P][2], then the tables below
+  extern __shared__ __align__(16) float4 sp[];  // [npairs][4], then the tables below
   __shared__ __align__(8) uint64_t bar;
-  const int P = cull.P, nrows = cull.nrows, npieces = cs.npieces;
-  float4* s_rbox = sp + 2 * P;
+  const int NP = cull.npairs, nrows = cull.nrows, npieces = cs.npieces;
+  float4* s_rbox = sp + 4 * NP;
   float4* s_tab = s_rbox + nrows;                       // [ptype][ltype] (X, 1/D, c1, 0)
-  int* s_rs = reinterpret_cast<int*>(s_tab + kNTypes * kNTypes);
+  int* s_rs = reinterpret_cast<int*>(s_tab + kTabRows * kNTypes);  // first pair of each row
   int* s_flush = s_rs + nrows + 1;                      // end of the row's flush block
   int* s_piece = s_flush + nrows;
   int* s_list = s_piece + npieces + 1;                  // [warps][kListCap] atoms to sweep
   if (threadIdx.x == 0) {
     mbar_init(&bar, 1);
-    const uint32_t bytes = (uint32_t)P * 32u;
+    const uint32_t bytes = (uint32_t)NP * 64u;
     mbar_expect_tx(&bar, bytes);
     constexpr uint32_t kPiece = 32768u;
     for (uint32_t off = 0; off < bytes; off += kPiece) {
       const uint32_t n = bytes - off < kPiece ? bytes - off : kPiece;
-      bulk_g2s(reinterpret_cast<char*>(sp) + off, reinterpret_cast<const char*>(cull.atoms) + off,
+      bulk_g2s(reinterpret_cast<char*>(sp) + off, reinterpret_cast<const char*>(cull.pairs) + off,
                n, &bar);
     }
   }
@@ -382,12 +431,9 @@ __global__ void __launch_bounds__(cull_max_threads(KP))
     s_rbox[k] = cull.row_box[k];
     s_flush[k] = cull.row_flush[k];
   }
-  for (int k = threadIdx.x; k <= nrows; k += blockDim.x) s_rs[k] = cull.row_start[k];
+  for (int k = threadIdx.x; k <= nrows; k += blockDim.x) s_rs[k] = cull.pair_start[k];
   for (int k = threadIdx.x; k <= npieces; k += blockDim.x) s_piece[k] = cs.piece_row[k];
-  for (int k = threadIdx.x; k < kNTypes * kNTypes; k += blockDim.x) {
-    const float4 v = tabv[k];
-    s_tab[k] = make_float4(v.x, v.y, (DIEL == 0 ? 11.0f : 5.0f) * v.y, 0.f);
-  }
+  stage_pair_table<DIEL>(tabv, s_tab);
   __syncthreads();
   if (!mbar_wait(&bar, 0, kWaitPolls)) {
     if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
@@ -491,19 +537,16 @@ __global__ void __launch_bounds__(kSysSortThreads)
 template <int KP, bool GRAD, int DIEL, int FORM>
 __global__ void __launch_bounds__(cull_max_threads(KP), 1)
     k_sys_pairs(DevSystems S, const float4* __restrict__ tabv, CullScratch cs, int* err) {
-  extern __shared__ __align__(16) float4 sp[];  // [piece atoms][2], then the row tables
+  extern __shared__ __align__(16) float4 sp[];  // [piece pairs][4], then the row tables
   __shared__ __align__(8) uint64_t bar;
   __shared__ int s_item, s_fail;
-  const int amax = S.piece_atoms_max, rmax = S.piece_rows_max;
-  float4* s_rbox = sp + 2 * amax;
+  const int amax = S.piece_pairs_max, rmax = S.piece_rows_max;
+  float4* s_rbox = sp + 4 * amax;
   float4* s_tab = s_rbox + rmax;
-  int* s_rs = reinterpret_cast<int*>(s_tab + kNTypes * kNTypes);
+  int* s_rs = reinterpret_cast<int*>(s_tab + kTabRows * kNTypes);
   int* s_flush = s_rs + rmax + 1;
   int* s_list = s_flush + rmax;
-  for (int k = threadIdx.x; k < kNTypes * kNTypes; k += blockDim.x) {
-    const float4 v = tabv[k];
-    s_tab[k] = make_float4(v.x, v.y, (DIEL == 0 ? 11.0f : 5.0f) * v.y, 0.f);
-  }
+  stage_pair_table<DIEL>(tabv, s_tab);
   if (threadIdx.x == 0) {
     mbar_init(&bar, 1);
     s_fail = 0;
@@ -518,16 +561,16 @@ __global__ void __launch_bounds__(cull_max_threads(KP), 1)
     if (item >= S.nitems) break;
     const int2 ip = S.item[item];
     const SysInfo& inf = S.info[ip.x];
-    const int4 pc = S.piece[ip.y];  // atom0, atom1, row0, row1
+    const int4 pc = S.piece[ip.y];  // pair0, pair1, row0, row1
     const int na = pc.y - pc.x, nr = pc.w - pc.z;
     if (threadIdx.x == 0) {
-      const uint32_t bytes = (uint32_t)na * 32u;
+      const uint32_t bytes = (uint32_t)na * 64u;
       mbar_expect_tx(&bar, bytes);
       constexpr uint32_t kPiece = 32768u;
       for (uint32_t off = 0; off < bytes; off += kPiece) {
         const uint32_t m = bytes - off < kPiece ? bytes - off : kPiece;
         bulk_g2s(reinterpret_cast<char*>(sp) + off,
-                 reinterpret_cast<const char*>(S.atoms + 2 * (size_t)pc.x) + off, m, &bar);
+                 reinterpret_cast<const char*>(S.pairs + 4 * (size_t)pc.x) + off, m, &bar);
       }
     }
     for (int k = threadIdx.x; k < nr; k += blockDim.x) {
@@ -596,8 +639,8 @@ CullFn pick_cull(int kp, bool grad, const Physics& ph) {
 
 }  // namespace
 
-int cull_smem_bytes(int P, int nrows, int npieces, int threads) {
-  const long b = 32L * P + 16L * nrows + 16L * kNTypes * kNTypes + 4L * (nrows + 1) + 4L * nrows +
+int cull_smem_bytes(int npairs, int nrows, int npieces, int threads) {
+  const long b = 64L * npairs + 16L * nrows + 16L * kTabRows * kNTypes + 4L * (nrows + 1) + 4L * nrows +
                  4L * (npieces + 1) + 4L * kListCap * (threads / 32);
   return (int)((b + 15) / 16 * 16);
 }
@@ -639,8 +682,8 @@ cudaError_t launch_pairs_cull(const DevCull& cull, const float4* tab, const Cull
 }
 
 
-int sys_pairs_smem(int piece_atoms_max, int piece_rows_max, int threads) {
-  const long b = 32L * piece_atoms_max + 16L * piece_rows_max + 16L * kNTypes * kNTypes +
+int sys_pairs_smem(int piece_pairs_max, int piece_rows_max, int threads) {
+  const long b = 64L * piece_pairs_max + 16L * piece_rows_max + 16L * kTabRows * kNTypes +
                  4L * (piece_rows_max + 1) + 4L * piece_rows_max + 4L * kListCap * (threads / 32);
   return (int)((b + 15) / 16 * 16);
 }

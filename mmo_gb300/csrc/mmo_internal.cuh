@@ -128,6 +128,8 @@ struct PairPlan {
 constexpr int kCullGrid = 32;                                   // entry binning cells per axis
 constexpr int kCullBins = kCullGrid * kCullGrid * kCullGrid;    // cells in Hilbert order
 constexpr float kCullR2 = 145.0f;  // visit radius^2: 1 - r^2/144 < 0 in FP32 beyond it
+// protein type row of the cut-off sweep's null pair partner: (X, 1/D, c1) all 0
+constexpr int kNullTypeRow = kNTypes;
 constexpr int kCullFlush = 256;    // protein atoms per FP32 partial before the FP64 add
 
 // The protein ordered in rows of a (y, z) grid of spacing h: row order (iz, iy)
@@ -140,7 +142,10 @@ struct DevCull {
   const float4* row_box;     // [nrows] (y_min, y_max, z_min, z_max) of the row's atoms
   const int* row_flush;      // [nrows] end (exclusive) of the row's flush block: the FP32
                              // partials go into the FP64 sums after row row_flush[r] - 1
-  int P, nrows;
+  const float4* pairs;       // [npairs][4] the cut-off sweep's layout of the same rows: atoms
+                             // in pairs, negated coordinates (see pair_step_ab)
+  const int* pair_start;     // [nrows + 1] first pair of each row
+  int P, nrows, npairs;
   float glo[3];              // entry binning grid origin and cells per A
   float ginv;
 };
@@ -175,8 +180,9 @@ struct CullScratch {
   int slots, npieces;
 };
 
-// threads per CTA of the cut-off sweep: the register budget of KP entries per lane
-constexpr int cull_max_threads(int kp) { return kp == 1 ? 1024 : (kp == 2 ? 768 : 512); }
+// threads per CTA of the cut-off sweep: the register budget of KP entries per
+// lane (each entry value held in both halves of a register pair)
+constexpr int cull_max_threads(int kp) { return kp == 1 ? 768 : (kp == 2 ? 512 : 256); }
 
 struct CullPlan {
   int kp, threads, blocks;
@@ -224,12 +230,12 @@ struct DevSystems {
   const int2* item;              // [nitems] (system, piece) work items of the sweep
   const SysGroup* group;         // [ngroups]
   const int* seg_slot;           // [nsegs] first slot of each (system, type) segment
-  const float4* atoms;           // [Ptot][2] packed proteins, row order, as DevCull::atoms
-  const int* row_start;          // [rows + 1] packed atom index of each row's first atom
+  const float4* pairs;           // [pairs][4] packed proteins, row order, as DevCull::pairs
+  const int* row_start;          // [rows + 1] packed pair index of each row's first pair
   const float4* row_box;         // [rows]
   const int* flush_end;          // [rows] packed row index ending the row's flush block
   int nsys, B, nitems, ngroups, G;
-  int Lmax, nrbmax, piece_atoms_max, piece_rows_max;
+  int Lmax, nrbmax, piece_pairs_max, piece_rows_max;
 };
 
 // ---- Monte Carlo chains (kernels_mc.cu) ----------------------------------
@@ -400,7 +406,7 @@ cudaError_t launch_sys_pairs(const DevSystems& S, const float4* tab, const CullS
                              int kp, int threads, int blocks, int smem, int flags,
                              const Physics& ph, int* d_err, cudaStream_t st);
 int sys_pairs_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem);
-int sys_pairs_smem(int piece_atoms_max, int piece_rows_max, int threads);
+int sys_pairs_smem(int piece_pairs_max, int piece_rows_max, int threads);
 cudaError_t launch_rebuild(const DevLigand& lig, const PoseIO& io, const Scratch& s, int flags,
                            cudaStream_t st);
 cudaError_t launch_pairs_batched(const DevProtein& prot, const float4* tab,
@@ -424,7 +430,7 @@ cudaError_t launch_pairs_cull(const DevCull& cull, const float4* tab, const Cull
                               const CullScratch& cs, int flags, const Physics& ph,
                               const CullPlan& plan, int* d_err, cudaStream_t st);
 int cull_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_bytes);
-int cull_smem_bytes(int P, int nrows, int npieces, int threads);
+int cull_smem_bytes(int npairs, int nrows, int npieces, int threads);
 cudaError_t launch_grid_build(const DevCull& cull, const GridBuild& gb, int dielectric,
                               float* grids, cudaStream_t st);
 cudaError_t launch_grid_inter(const GridLook& g, const float4* X, int n, int L,
@@ -593,6 +599,63 @@ __device__ __forceinline__ void pair_step(float xh, float yh, float zh, float xl
     gx = fmaf(g, dx, gx);
     gy = fmaf(g, dy, gy);
     gz = fmaf(g, dz, gz);
+  }
+}
+
+// both halves of a packed FP32 operand
+__device__ __forceinline__ float2 bc2(float v) { return make_float2(v, v); }
+
+// One entry (the same values in both halves) against a pair of protein atoms
+// (a, b) of the cut-off sweep's layout, on the packed FP32 instructions:
+// a0 = (-x_hi a, -x_hi b, -y_hi a, -y_hi b), a1 = (-z_hi a, -z_hi b, Kq a, Kq b),
+// a2, a3 the lo halves (a3.zw: type offsets), (X, 1/D, c1) of a and b.  Each
+// half is pair_step's arithmetic in its order; the half of atom a accumulates
+// the even atoms of a row, that of b the odd ones.  A packed instruction does
+// two FP32 operations on the FMA pipes in one issue slot, and the atoms' values
+// come in pairs from shared memory, so nothing is broadcast in the loop.
+__device__ __forceinline__ float2 lo_pair(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi_pair(float4 v) { return make_float2(v.z, v.w); }
+template <bool GRAD, int DIEL, int FORM, bool MASK = false>
+__device__ __forceinline__ void pair_step_ab(float2 xh, float2 yh, float2 zh, float2 xl,
+                                             float2 yl, float2 zl, float2 q, float4 a0, float4 a1,
+                                             float4 a2, float4 a3, float2 X, float2 invD,
+                                             float2 c1, float c0, float2& acc, float2& gx,
+                                             float2& gy, float2& gz, float& mn) {
+  const float2 dx = __fadd2_rn(__fadd2_rn(xh, lo_pair(a0)), __fadd2_rn(xl, lo_pair(a2)));
+  const float2 dy = __fadd2_rn(__fadd2_rn(yh, hi_pair(a0)), __fadd2_rn(yl, hi_pair(a2)));
+  const float2 dz = __fadd2_rn(__fadd2_rn(zh, lo_pair(a1)), __fadd2_rn(zl, lo_pair(a3)));
+  const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+  const float2 r2c = make_float2(fmaxf(r2.x, kMinR2), fmaxf(r2.y, kMinR2));
+  const float2 ir = make_float2(rsqrtf(r2c.x), rsqrtf(r2c.y));
+  const float2 ir2 = __fmul2_rn(ir, ir);
+  const float2 P = __fmul2_rn(X, ir2);
+  const float2 Dp6 = __fmul2_rn(__fmul2_rn(P, P), P);
+  const float2 lj = __fmul2_rn(Dp6, __ffma2_rn(Dp6, invD, bc2(-2.0f)));
+  const float2 qq = __fmul2_rn(hi_pair(a1), q);
+  const float2 e = __ffma2_rn(qq, DIEL == 0 ? ir : ir2, lj);
+  float2 s = bc2(1.0f);
+  if (FORM == 0) {
+    const float2 t = __ffma2_rn(r2c, bc2(-1.0f / 144.0f), bc2(1.0f));
+    s = make_float2(fmaxf(t.x, 0.0f), fmaxf(t.y, 0.0f));
+    acc = __ffma2_rn(__fmul2_rn(s, s), e, acc);
+  } else {
+    acc = __fadd2_rn(acc, e);
+  }
+  if (GRAD) {
+    const float2 nt = __ffma2_rn(Dp6, __ffma2_rn(Dp6, c1, bc2(c0)), e);
+    const float2 na = __fmul2_rn(nt, ir2);
+    float2 g = na;
+    if (FORM == 0)
+      g = __fmul2_rn(s, __ffma2_rn(s, na,
+                                   __fmul2_rn(e, bc2(DIEL == 0 ? 1.0f / 36.0f : 1.0f / 72.0f))));
+    if (MASK) {  // clamped distance: derivative 0
+      g.x = r2.x < kMinR2 ? 0.0f : g.x;
+      g.y = r2.y < kMinR2 ? 0.0f : g.y;
+    }
+    mn = fminf(mn, fminf(r2.x, r2.y));
+    gx = __ffma2_rn(g, dx, gx);
+    gy = __ffma2_rn(g, dy, gy);
+    gz = __ffma2_rn(g, dz, gz);
   }
 }
 
