@@ -641,13 +641,44 @@ struct RowIndex {
   float lo[3], hi[3];           // bounding box (hi parts)
 };
 
+// The partners of a row's atoms: in x order, each atom not yet taken with the
+// nearest of the next few untaken atoms of its row, so that the two atoms of a
+// pair are close (a pair is swept when either atom is within reach of the
+// entry group's box, and the farther one's work is then mostly wasted).  Only
+// the row's last untaken atom can be left without one (b = -1).
+std::vector<int2> pair_row(const RowIndex& R, int a0, int a1) {
+  constexpr int kLook = 6;
+  std::vector<int2> out;
+  std::vector<char> taken(a1 - a0, 0);
+  for (int a = a0; a < a1; ++a) {
+    if (taken[a - a0]) continue;
+    taken[a - a0] = 1;
+    const float4 p = R.atoms[2 * (size_t)a];
+    int best = -1, seen = 0;
+    float bd = 0.f;
+    for (int b = a + 1; b < a1 && seen < kLook; ++b) {
+      if (taken[b - a0]) continue;
+      ++seen;
+      const float4 q = R.atoms[2 * (size_t)b];
+      const float d = (p.x - q.x) * (p.x - q.x) + (p.y - q.y) * (p.y - q.y) + (p.z - q.z) * (p.z - q.z);
+      if (best < 0 || d < bd) {
+        best = b;
+        bd = d;
+      }
+    }
+    if (best >= 0) taken[best - a0] = 1;
+    out.push_back(make_int2(a, best));
+  }
+  return out;
+}
+
 // The cut-off sweep's copy of a row index: the atoms of each row in pairs
-// (2j, 2j + 1), as four float4 per pair, negated coordinates so that the sweep
+// (pair_row), as four float4 per pair, negated coordinates so that the sweep
 // adds them: (-x_hi a, -x_hi b, -y_hi a, -y_hi b), (-z_hi a, -z_hi b, Kq a, Kq b),
-// the lo halves likewise, (-z_lo a, -z_lo b, type offset a, type offset b).  A
-// row of odd length ends with a null partner: its last atom again, with charge
-// -0 (a zero charge of a real atom is +0) and the null type row (all zeros),
-// whose terms are exact zeros.
+// the lo halves likewise, (-z_lo a, -z_lo b, type offset a, type offset b).  An
+// atom without a partner gets a null one: itself again, with charge -0 (a zero
+// charge of a real atom is +0) and the null type row (all zeros), whose terms
+// are exact zeros.
 void build_pairs(RowIndex* io) {
   RowIndex& R = *io;
   const int nrows = (int)R.rbox.size();
@@ -655,11 +686,12 @@ void build_pairs(RowIndex* io) {
   R.pairs.clear();
   for (int r = 0; r < nrows; ++r) {
     R.prs[r] = (int)(R.pairs.size() / 4);
-    for (int a = R.rs[r]; a < R.rs[r + 1]; a += 2) {
-      const bool real_b = a + 1 < R.rs[r + 1];
+    for (const int2 ab : pair_row(R, R.rs[r], R.rs[r + 1])) {
+      const int a = ab.x, b = ab.y;
+      const bool real_b = b >= 0;
       const float4 ah = R.atoms[2 * (size_t)a], al = R.atoms[2 * (size_t)a + 1];
-      const float4 bh = real_b ? R.atoms[2 * (size_t)a + 2] : ah;
-      const float4 bl = real_b ? R.atoms[2 * (size_t)a + 3] : al;
+      const float4 bh = real_b ? R.atoms[2 * (size_t)b] : ah;
+      const float4 bl = real_b ? R.atoms[2 * (size_t)b + 1] : al;
       const float wa = ah.w == 0.f ? 0.f : ah.w;
       const float wb = real_b ? (bh.w == 0.f ? 0.f : bh.w) : -0.f;
       float offb = bl.w;
