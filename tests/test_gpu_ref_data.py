@@ -1,0 +1,147 @@
+"""The reference's own molecules on the GPU against the FP64 oracle: the
+48-atom ligand of data/docked.mol2, data/minimized.mol2 and data/ligdecs.mol2
+(one molecule in three poses) in the 3A2J receptor of data/xtal.pdb, as
+committed by tests/golden/make_ref_data.py.
+
+* the batched energy and gradient of each pose and of poses perturbed about
+  it (rigid moves, torsions), with the reference's physics and its variants,
+  both pose maps, and the one-pose path;
+* the closures ``ff0 prot`` (ene_inter_builder) and ``ene_intra``
+  (ene_intra_builder; ff_score's per-ligand intra energy);
+* interpolated scoring on grids built about the binding site;
+* exhaustive rigid docking about the docked pose's centre.
+
+Tolerances are the scoring contract's: energies within 1e-5 of
+max(|E64|, sum |pair energies|), gradients within 1e-4 of the largest
+component; the poses here are mostly clash-free, so the first term counts."""
+import numpy as np
+import pytest
+
+from mmo_gb300 import grids as GR
+from mmo_gb300 import synth
+from test_gpu_parity import assert_energy, assert_grad, ref_batch
+from test_ref_data import ref_molecules
+
+pytestmark = pytest.mark.gpu
+
+STEP = 0.5
+
+
+@pytest.fixture(scope="module")
+def ref():
+    return ref_molecules()
+
+
+def _poses(lig, n, seed, recenter):
+    """n poses about the conformer as it is (pose 0 leaves it in place)."""
+    rng = np.random.default_rng(seed)
+    d = np.zeros((n, 6 + lig.nrb), np.float32)
+    if recenter:
+        d[:, :3] = lig.xyz().mean(axis=0)
+    d[1:, :3] += rng.uniform(-0.4, 0.4, size=(n - 1, 3)).astype(np.float32)
+    if recenter:  # rotations about the centroid
+        d[1:, 3:6] = rng.uniform(-0.2, 0.2, size=(n - 1, 3))
+    d[1:, 6:] = rng.uniform(-0.5, 0.5, size=(n - 1, lig.nrb))
+    return d
+
+
+@pytest.mark.parametrize("phys", [(0, 0, 0, 0), (1, 0, 0, 0), (0, 0, 1, 0), (0, 1, 0, 0)],
+                         ids=["reference", "eps4r", "global", "lorentz-berthelot"])
+@pytest.mark.parametrize("recenter", [False, True])
+def test_ref_poses_match_oracle(oracle, scorer_factory, ref, phys, recenter):
+    from mmo_gb300.ff import Physics
+
+    rec, ligs = ref
+    for k, lig in enumerate(ligs):
+        s = scorer_factory(rec, lig, Physics(*phys))
+        d = _poses(lig, 24, 10 + k, recenter)
+        E, G, st = s.score_poses(d, grad=True, recenter=recenter)
+        assert np.all(st == 0)
+        system = synth.System(lig.name, rec, lig, d)
+        E64, G64, st64, scale = ref_batch(oracle, system, d, grad=True, recenter=recenter,
+                                          ph=oracle.physics(*phys))
+        assert np.array_equal(st, st64)
+        assert_energy(E, E64, scale)
+        assert_grad(G, G64)
+        # one pose per call: the plain path
+        E1, G1, _ = s.score_poses(d[:1], grad=True, recenter=recenter)
+        assert_energy(E1, E64[:1], scale[:1])
+        assert_grad(G1, G64[:1])
+    if phys == (0, 0, 0, 0) and not recenter:
+        # the docked pose binds: its inter energy is favourable
+        s = scorer_factory(rec, ligs[0])
+        e, _, _ = s.score_poses(_poses(ligs[0], 1, 0, False), intra=False)
+        assert e[0] < -5.0
+
+
+def test_ref_closures_match_oracle(oracle, gpu_lib, ref):
+    from oracle import np_twin as T
+
+    from mmo_gb300.ff import ene_inter_builder, ene_intra_builder
+
+    rec, ligs = ref
+    ff0 = ene_inter_builder(rec)
+    for lig in ligs:
+        e64 = oracle.ene_inter(rec, lig)
+        scale = T.ene_inter(rec.xyz(), rec.q, rec.anum, lig.xyz(), lig.q, lig.anum, absolute=True)
+        assert abs(ff0(lig) - e64) <= 1e-5 * max(abs(e64), scale)
+        intra = ene_intra_builder(lig.centered())
+        ei64 = oracle.ene_intra(lig)
+        si = T.ene_intra(lig.xyz(), lig.q, lig.anum, lig.interacting, absolute=True)
+        assert abs(intra(lig) - ei64) <= 1e-5 * max(abs(ei64), si)
+        intra.scorer.close()
+    ff0.scorer.close()
+
+
+def _site_lattice(lig, margin=6.0):
+    lo, hi = lig.xyz().min(axis=0) - margin, lig.xyz().max(axis=0) + margin
+    return GR.lattice_from_box(STEP, lo, hi)
+
+
+def test_ref_interpolated_scoring_matches_oracle(oracle, scorer_factory, ref):
+    from test_gpu_grid import _corner_scale
+
+    rec, ligs = ref
+    origin, dims = _site_lattice(ligs[0])
+    types, per = GR.type2id(ligs)
+    for lig, lt in zip(ligs, per):
+        s = scorer_factory(rec, lig)
+        s.build_grids(STEP, dims, origin, types)
+        g = s.grid_values()
+        d = _poses(lig, 8, 3, False)
+        E, _, st = s.score_poses(d, intra=False, grid=True)
+        assert np.all(st == 0)
+        for b in range(len(d)):
+            xyz, _ = oracle.apply_config(lig, d[b].astype(np.float64), 0)
+            e, off = oracle.ene_inter_interp(STEP, dims, g, xyz - origin, lt)
+            assert not off
+            sc = _corner_scale(g, lt, (xyz - origin) / STEP)
+            assert abs(E[b] - e) <= 1e-6 * max(sc, 1e-300), (b, E[b], e)
+
+
+def test_ref_exhaustive_docking_matches_oracle(oracle, scorer_factory, ref):
+    rec, ligs = ref
+    lig = ligs[0]
+    origin, dims = _site_lattice(lig, margin=9.0)
+    types, (lt,) = GR.type2id([lig])
+    s = scorer_factory(rec, lig)
+    s.build_grids(STEP, dims, origin, types)
+    s.build_masks(rec.radius)
+    g = s.grid_values()
+    vdw, _ = s.mask_values()
+    center, radius, step, nrot, k = lig.xyz().mean(axis=0), 1.0, 0.5, 48, 16
+    res = s.dock_exhaustive(center, radius, step, nrot, topk=k, const_intra=0.0,
+                            lig_radius=lig.radius)
+    R = np.stack([oracle.so3_rotation(nrot, i) for i in range(nrot)])
+    sc, _ = oracle.dock_scores(oracle.lattice(STEP, dims, origin), g, vdw, lig, lt, lig.radius,
+                               center, radius, step, R, const_intra=0.0)
+    ok = np.isfinite(sc)
+    assert res["scored"] == ok.sum() > 0
+    order = np.lexsort((np.arange(len(sc)), sc))[:min(k, ok.sum())]
+    tol = 1e-6 * max(1.0, np.abs(sc[order]).max())
+    assert np.allclose(res["scores"], sc[order], rtol=0, atol=tol)
+    for t in range(len(order)):
+        gap = min(abs(sc[order[t]] - sc[order[t - 1]]) if t else np.inf,
+                  abs(sc[order[t + 1]] - sc[order[t]]) if t + 1 < len(order) else np.inf)
+        if gap > 4 * tol:
+            assert res["frames"][t] == order[t], t
