@@ -102,9 +102,11 @@ def test_ref_interpolated_scoring_matches_oracle(oracle, scorer_factory, ref):
     from test_gpu_grid import _corner_scale
 
     rec, ligs = ref
-    origin, dims = _site_lattice(ligs[0])
     types, per = GR.type2id(ligs)
     for lig, lt in zip(ligs, per):
+        # about each pose: only data/docked.mol2 sits in the pocket, the other
+        # two poses of the molecule lie near the origin
+        origin, dims = _site_lattice(lig)
         s = scorer_factory(rec, lig)
         s.build_grids(STEP, dims, origin, types)
         g = s.grid_values()
