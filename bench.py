@@ -280,12 +280,17 @@ def run_ragged(args):
         g.replay()
     gms, _ = _timed_region(torch, stream, g.replay, args.steps)
     gval = B * len(gms) / (sum(gms) * 1e-3)
-    # end to end with host buffers
+    # end to end with host buffers (page-locked, as a caller keeps them)
+    h_in = torch.from_numpy(h).pin_memory().numpy()
+    h_out = (torch.empty(B, dtype=torch.float64).pin_memory().numpy(),
+             torch.empty(int(h.size), dtype=torch.float32).pin_memory().numpy(),
+             torch.empty(B, dtype=torch.int32).pin_memory().numpy())
     e2e = []
     for k in range(args.warmup + args.steps):
+        flush.zero_()
         torch.cuda.synchronize()
         t = time.perf_counter()
-        Eh, Gh, sth = sc.score_systems(h, grad=True)
+        Eh, Gh, sth = sc.score_systems(h_in, grad=True, out=h_out)
         if k >= args.warmup:
             e2e.append(time.perf_counter() - t)
     e2e_val = B * len(e2e) / sum(e2e)
@@ -304,7 +309,9 @@ def run_ragged(args):
                                (len(systems), min(Ls), max(Ls), np.mean(Ls), min(Ps), max(Ps),
                                 np.mean(Ps)),
                    "poses": B, "plan": dict(sc.systems_plan(), tuned_ms=tune_ms),
-                   "l2": "flushed before every timed step (256 MiB write), not timed"},
+                   "l2": "flushed before every timed step of value and e2e (256 MiB write), not "
+                         "timed; the graph line replays back to back on inputs larger than L2 "
+                         "(%.0f MB of packed proteins)" % (32e-6 * sum(Ps))},
         "graph": {"value": gval, "unit": "poses/s", "ms_per_step": float(np.mean(gms))},
         "e2e": {"value": e2e_val, "unit": "poses/s", "h2d_bytes_per_step": int(h.nbytes),
                 "d2h_bytes_per_step": int(Eh.nbytes + Gh.nbytes + sth.nbytes)},
@@ -835,12 +842,16 @@ def main():
 
     # ---- end to end through the C ABI with host buffers -------------------
     h_dofs = torch.from_numpy(s.poses).pin_memory()
+    # page-locked result buffers, as a caller keeps them between calls
+    h_out = (torch.empty(B, dtype=torch.float64).pin_memory().numpy(),
+             torch.empty(tuple(s.poses.shape), dtype=torch.float32).pin_memory().numpy(),
+             torch.empty(B, dtype=torch.int32).pin_memory().numpy())
     e2e_ms = []
     for k in range(args.warmup + args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         t = time.perf_counter()
-        E_h, G_h, st_h = sc.score_poses(h_dofs.numpy(), grad=True)
+        E_h, G_h, st_h = sc.score_poses(h_dofs.numpy(), grad=True, out=h_out)
         if k >= args.warmup:
             e2e_ms.append((time.perf_counter() - t) * 1e3)
     e2e_tot = sum(e2e_ms)

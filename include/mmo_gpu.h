@@ -108,7 +108,9 @@ int mmo_ene_intra(mmo_ctx* ctx, const double* xs, const double* ys, const double
  * E_out[B] (FP64): E_inter and/or E_intra as flags select.  grad_out (null
  * unless MMO_F_GRAD): B x (6 + nrb) floats, the analytic gradient replacing
  * approx_local_gradient (lds.ml:1118-1136).  status_out[B] (nullable):
- * MMO_S_* bits.  B = 1 runs the one-pose-per-launch plain path. */
+ * MMO_S_* bits.  B = 1 runs the one-pose-per-launch plain path.  Page-locked
+ * buffers (cudaHostAlloc / cudaHostRegister) are read and written by DMA
+ * directly; other host memory goes through the context's staging buffers. */
 int mmo_score_poses(mmo_ctx* ctx, int B, const float* dofs, int flags, double* E_out,
                     float* grad_out, int* status_out);
 

@@ -63,6 +63,17 @@ void split_store(float4* dst, double x, double y, double z, float w) {
                        0.f);
 }
 
+// true for page-locked (or registered) host memory, which a copy can reach by DMA
+bool host_pinned(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // not a pointer the runtime knows: ordinary host memory
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
 // next 16-byte aligned offset of a block of `bytes`
 size_t take(size_t& off, size_t bytes) {
   const size_t o = (off + 15) & ~size_t(15);
@@ -1951,6 +1962,67 @@ int mmo_ene_intra(mmo_ctx* ctx, const double* xs, const double* ys, const double
   return MMO_OK;
 }
 
+// The host side of a scoring call: in_bytes of inputs to the device, run(d_in,
+// d_E, d_grad, d_status, d_err) queued on the context's stream, then nE
+// doubles, ngrad floats and nst ints of results back into E, grad, status
+// (grad and status nullable), and the device error flag.  Page-locked caller
+// buffers are copied by DMA directly, other host memory through the
+// context's page-locked staging buffers.
+extern "C++" {
+template <class Run>
+int host_call(mmo_ctx* ctx, const void* in, size_t in_bytes, double* E, size_t nE, float* grad,
+              size_t ngrad, int* status, size_t nst, Run run) {
+  size_t off = 0;
+  take(off, sizeof(double) * nE);
+  const size_t o_grad = take(off, grad ? sizeof(float) * ngrad : 0);
+  const size_t o_st = take(off, sizeof(int) * nst);
+  const size_t o_err = take(off, sizeof(int));
+  const size_t out_bytes = off;
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  int r = grow_host(ctx, &ctx->h_in, &ctx->d_in, &ctx->cap_in, in_bytes);
+  if (r) return r;
+  r = grow_host(ctx, &ctx->h_out, &ctx->d_out, &ctx->cap_out, out_bytes);
+  if (r) return r;
+  const bool pin_in = host_pinned(in);
+  const bool pin_out =
+      host_pinned(E) && (!grad || host_pinned(grad)) && (!status || host_pinned(status));
+  if (!pin_in) memcpy(ctx->h_in, in, in_bytes);
+  MMO_CK(cudaMemcpyAsync(ctx->d_in, pin_in ? in : ctx->h_in, in_bytes, cudaMemcpyHostToDevice,
+                         ctx->stream),
+         "H2D");
+  r = run(reinterpret_cast<const float*>(ctx->d_in), reinterpret_cast<double*>(ctx->d_out),
+          grad ? reinterpret_cast<float*>(ctx->d_out + o_grad) : nullptr,
+          reinterpret_cast<int*>(ctx->d_out + o_st), reinterpret_cast<int*>(ctx->d_out + o_err));
+  if (r) return r;
+  if (pin_out) {
+    MMO_CK(cudaMemcpyAsync(E, ctx->d_out, sizeof(double) * nE, cudaMemcpyDeviceToHost,
+                           ctx->stream),
+           "D2H");
+    if (grad)
+      MMO_CK(cudaMemcpyAsync(grad, ctx->d_out + o_grad, sizeof(float) * ngrad,
+                             cudaMemcpyDeviceToHost, ctx->stream),
+             "D2H");
+    if (status)
+      MMO_CK(cudaMemcpyAsync(status, ctx->d_out + o_st, sizeof(int) * nst,
+                             cudaMemcpyDeviceToHost, ctx->stream),
+             "D2H");
+    MMO_CK(cudaMemcpyAsync(ctx->h_out + o_err, ctx->d_out + o_err, sizeof(int),
+                           cudaMemcpyDeviceToHost, ctx->stream),
+           "D2H");
+  } else {
+    MMO_CK(cudaMemcpyAsync(ctx->h_out, ctx->d_out, out_bytes, cudaMemcpyDeviceToHost, ctx->stream),
+           "D2H");
+  }
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync");
+  if (!pin_out) {
+    memcpy(E, ctx->h_out, sizeof(double) * nE);
+    if (grad) memcpy(grad, ctx->h_out + o_grad, sizeof(float) * ngrad);
+    if (status) memcpy(status, ctx->h_out + o_st, sizeof(int) * nst);
+  }
+  return check_dev_err(ctx, *reinterpret_cast<int*>(ctx->h_out + o_err));
+}
+}  // extern "C++"
+
 int mmo_score_poses(mmo_ctx* ctx, int B, const float* dofs, int flags, double* E_out,
                     float* grad_out, int* status_out) {
   if (!ctx) return MMO_EINVAL;
@@ -1960,35 +2032,12 @@ int mmo_score_poses(mmo_ctx* ctx, int B, const float* dofs, int flags, double* E
   if (B == 0) return MMO_OK;
   const int nd = 6 + ctx->lig.nrb;
   const bool grad = flags & MMO_F_GRAD;
-  // output block: E[B] | grad[B][nd] | status[B] | err
-  size_t off = 0;
-  take(off, sizeof(double) * B);
-  const size_t o_grad = take(off, grad ? sizeof(float) * (size_t)B * nd : 0);
-  const size_t o_st = take(off, sizeof(int) * B);
-  const size_t o_err = take(off, sizeof(int));
-  const size_t out_bytes = off;
-  const size_t in_bytes = sizeof(float) * (size_t)B * nd;
-  MMO_CK(cudaSetDevice(ctx->device), "set device");
-  int r = grow_host(ctx, &ctx->h_in, &ctx->d_in, &ctx->cap_in, in_bytes);
-  if (r) return r;
-  r = grow_host(ctx, &ctx->h_out, &ctx->d_out, &ctx->cap_out, out_bytes);
-  if (r) return r;
-  memcpy(ctx->h_in, dofs, in_bytes);
-  MMO_CK(cudaMemcpyAsync(ctx->d_in, ctx->h_in, in_bytes, cudaMemcpyHostToDevice, ctx->stream),
-         "H2D");
-  r = score_device(ctx, B, reinterpret_cast<const float*>(ctx->d_in), flags,
-                   reinterpret_cast<double*>(ctx->d_out),
-                   grad ? reinterpret_cast<float*>(ctx->d_out + o_grad) : nullptr,
-                   reinterpret_cast<int*>(ctx->d_out + o_st),
-                   reinterpret_cast<int*>(ctx->d_out + o_err), 1, ctx->stream);
-  if (r) return r;
-  MMO_CK(cudaMemcpyAsync(ctx->h_out, ctx->d_out, out_bytes, cudaMemcpyDeviceToHost, ctx->stream),
-         "D2H");
-  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync");
-  memcpy(E_out, ctx->h_out, sizeof(double) * B);
-  if (grad) memcpy(grad_out, ctx->h_out + o_grad, sizeof(float) * (size_t)B * nd);
-  if (status_out) memcpy(status_out, ctx->h_out + o_st, sizeof(int) * B);
-  return check_dev_err(ctx, *reinterpret_cast<int*>(ctx->h_out + o_err));
+  return host_call(ctx, dofs, sizeof(float) * (size_t)B * nd, E_out, B,
+                   grad ? grad_out : nullptr, (size_t)B * nd, status_out, B,
+                   [&](const float* d_in, double* d_E, float* d_grad, int* d_st, int* d_err) {
+                     return score_device(ctx, B, d_in, flags, d_E, d_grad, d_st, d_err, 1,
+                                         ctx->stream);
+                   });
 }
 
 int mmo_score_poses_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E,
@@ -2571,34 +2620,11 @@ int mmo_score_systems(mmo_ctx* ctx, const float* dofs, int flags, double* E, flo
   const bool g = flags & MMO_F_GRAD;
   if (B > 0 && (!dofs || !E || (g && !grad))) return fail(ctx, MMO_EINVAL, "mmo_score_systems: bad arguments");
   if (B == 0) return MMO_OK;
-  size_t off = 0;
-  take(off, sizeof(double) * B);
-  const size_t o_grad = take(off, g ? sizeof(float) * (size_t)D : 0);
-  const size_t o_st = take(off, sizeof(int) * B);
-  const size_t o_err = take(off, sizeof(int));
-  const size_t out_bytes = off, in_bytes = sizeof(float) * (size_t)D;
-  MMO_CK(cudaSetDevice(ctx->device), "set device");
-  int r = grow_host(ctx, &ctx->h_in, &ctx->d_in, &ctx->cap_in, in_bytes);
-  if (r) return r;
-  r = grow_host(ctx, &ctx->h_out, &ctx->d_out, &ctx->cap_out, out_bytes);
-  if (r) return r;
-  memcpy(ctx->h_in, dofs, in_bytes);
-  MMO_CK(cudaMemcpyAsync(ctx->d_in, ctx->h_in, in_bytes, cudaMemcpyHostToDevice, ctx->stream),
-         "H2D");
-  MMO_CK(cudaMemsetAsync(ctx->d_out + o_err, 0, sizeof(int), ctx->stream), "error flag");
-  r = score_systems(ctx, reinterpret_cast<const float*>(ctx->d_in), flags,
-                    reinterpret_cast<double*>(ctx->d_out),
-                    g ? reinterpret_cast<float*>(ctx->d_out + o_grad) : nullptr,
-                    reinterpret_cast<int*>(ctx->d_out + o_st),
-                    reinterpret_cast<int*>(ctx->d_out + o_err), ctx->stream);
-  if (r) return r;
-  MMO_CK(cudaMemcpyAsync(ctx->h_out, ctx->d_out, out_bytes, cudaMemcpyDeviceToHost, ctx->stream),
-         "D2H");
-  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync");
-  memcpy(E, ctx->h_out, sizeof(double) * B);
-  if (g) memcpy(grad, ctx->h_out + o_grad, sizeof(float) * (size_t)D);
-  if (status) memcpy(status, ctx->h_out + o_st, sizeof(int) * B);
-  return check_dev_err(ctx, *reinterpret_cast<int*>(ctx->h_out + o_err));
+  return host_call(ctx, dofs, sizeof(float) * (size_t)D, E, B, g ? grad : nullptr, D, status, B,
+                   [&](const float* d_in, double* d_E, float* d_grad, int* d_st, int* d_err) {
+                     MMO_CK(cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream), "error flag");
+                     return score_systems(ctx, d_in, flags, d_E, d_grad, d_st, d_err, ctx->stream);
+                   });
 }
 
 // ---- precomputed interaction grids ------------------------------------------

@@ -207,9 +207,10 @@ class UFFScorer:
         self._check(self._lib.mmo_systems_layout(self._h, C.byref(B), C.byref(D), po, do))
         return np.array(po[:], np.int64), np.array(do[:], np.int64)
 
-    def score_systems(self, dofs, inter=True, intra=True, grad=False, recenter=False):
+    def score_systems(self, dofs, inter=True, intra=True, grad=False, recenter=False, out=None):
         """Packed float32 DOFs of every system's poses (systems_layout) ->
-        E [B] float64, grad (packed like dofs) or None, status [B]."""
+        E [B] float64, grad (packed like dofs) or None, status [B]; out: those
+        arrays to fill instead of new ones (as score_poses)."""
         po, do = self.systems_layout()
         dofs = np.ascontiguousarray(dofs, np.float32).reshape(-1)
         if dofs.size != do[-1]:
@@ -217,9 +218,20 @@ class UFFScorer:
         B = int(po[-1])
         flags = ((_L.F_INTER if inter else 0) | (_L.F_INTRA if intra else 0) |
                  (_L.F_GRAD if grad else 0) | (_L.F_RECENTER if recenter else 0))
-        E = np.zeros(B, np.float64)
-        G = np.zeros(dofs.size, np.float32) if grad else None
-        st = np.zeros(B, np.int32)
+        if out is not None:
+            E, G, st = out
+            ok = (E.dtype == np.float64 and E.shape == (B,) and st.dtype == np.int32 and
+                  st.shape == (B,) and E.flags.c_contiguous and st.flags.c_contiguous and
+                  (not grad or (G is not None and G.dtype == np.float32 and
+                                G.shape == (dofs.size,) and G.flags.c_contiguous)))
+            if not ok:
+                raise ValueError("out must be (float64 [B], float32 [DOFs] or None, int32 [B])")
+            if not grad:
+                G = None
+        else:
+            E = np.zeros(B, np.float64)
+            G = np.zeros(dofs.size, np.float32) if grad else None
+            st = np.zeros(B, np.int32)
         self._check(self._lib.mmo_score_systems(
             self._h, dofs.ctypes.data_as(C.POINTER(C.c_float)), flags, _dp(E),
             G.ctypes.data_as(C.POINTER(C.c_float)) if G is not None else None, _ip(st)))
@@ -434,12 +446,15 @@ class UFFScorer:
         return prot, lig, st
 
     # -- batched poses -----------------------------------------------------
-    def score_poses(self, dofs, inter=True, intra=True, grad=False, recenter=False, grid=False):
+    def score_poses(self, dofs, inter=True, intra=True, grad=False, recenter=False, grid=False,
+                    out=None):
         """E (float64 [B]), grad (float32 [B, 6+nrb] or None), status (int32 [B]).
 
         dofs: float32 [B, 6 + nrb] in the Optim.config layout
         [x, y, z, a, b, g, tau_0 ...] (src/optim.ml:19-22); grid: the inter
-        term interpolated from the grids of build_grids / load_grids."""
+        term interpolated from the grids of build_grids / load_grids.  out:
+        (E, grad or None, status) arrays to fill instead of new ones (for
+        instance views of page-locked memory, which the copies reach by DMA)."""
         dofs = np.ascontiguousarray(dofs, np.float32)
         if dofs.ndim == 1:
             dofs = dofs[None, :]
@@ -449,9 +464,20 @@ class UFFScorer:
         flags = ((_L.F_INTER if inter else 0) | (_L.F_INTRA if intra else 0) |
                  (_L.F_GRAD if grad else 0) | (_L.F_RECENTER if recenter else 0) |
                  (_L.F_GRID if grid else 0))
-        E = np.zeros(B, np.float64)
-        G = np.zeros((B, nd), np.float32) if grad else None
-        st = np.zeros(B, np.int32)
+        if out is not None:
+            E, G, st = out
+            ok = (E.dtype == np.float64 and E.shape == (B,) and st.dtype == np.int32 and
+                  st.shape == (B,) and E.flags.c_contiguous and st.flags.c_contiguous and
+                  (not grad or (G is not None and G.dtype == np.float32 and G.shape == (B, nd)
+                                and G.flags.c_contiguous)))
+            if not ok:
+                raise ValueError("out must be (float64 [B], float32 [B, 6+nrb] or None, int32 [B])")
+            if not grad:
+                G = None
+        else:
+            E = np.zeros(B, np.float64)
+            G = np.zeros((B, nd), np.float32) if grad else None
+            st = np.zeros(B, np.int32)
         self._check(self._lib.mmo_score_poses(
             self._h, B, dofs.ctypes.data_as(C.POINTER(C.c_float)), flags, _dp(E),
             G.ctypes.data_as(C.POINTER(C.c_float)) if G is not None else None, _ip(st)))

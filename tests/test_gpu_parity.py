@@ -257,6 +257,27 @@ def test_deterministic(scorer_factory, batch):
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
 
 
+def test_page_locked_buffers_give_the_same_results(scorer_factory, batch):
+    """mmo_score_poses copies page-locked caller buffers by DMA directly, and
+    other host memory through its staging buffers: the same bits either way,
+    for inputs and outputs page-locked or not, with and without the gradient."""
+    torch = pytest.importorskip("torch")
+    s = scorer_factory(batch.pocket, batch.ligand)
+    d = batch.poses[:300]
+    B, nd = d.shape
+    E0, G0, st0 = s.score_poses(d, grad=True)
+    pin_d = torch.from_numpy(np.ascontiguousarray(d)).pin_memory().numpy()
+    out = (torch.zeros(B, dtype=torch.float64).pin_memory().numpy(),
+           torch.zeros((B, nd), dtype=torch.float32).pin_memory().numpy(),
+           torch.zeros(B, dtype=torch.int32).pin_memory().numpy())
+    for dofs in (d, pin_d):
+        E, G, st = s.score_poses(dofs, grad=True, out=out)
+        assert E is out[0] and G is out[1] and st is out[2]
+        assert np.array_equal(E, E0) and np.array_equal(G, G0) and np.array_equal(st, st0)
+        E1, _, st1 = s.score_poses(dofs, out=(np.zeros(B), None, np.zeros(B, np.int32)))
+        assert np.array_equal(E1, E0) and np.array_equal(st1, st0)
+
+
 def test_plain_and_batched_agree(scorer_factory, batch):
     s = scorer_factory(batch.pocket, batch.ligand)
     d = batch.poses[:40]

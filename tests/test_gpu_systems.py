@@ -137,3 +137,20 @@ def test_systems_graph_replay_and_device_entry(scorer_factory, systems):
         torch.cuda.synchronize()
         assert np.array_equal(E.cpu().numpy(), E0) and np.array_equal(G.cpu().numpy(), G0)
         assert np.array_equal(st.cpu().numpy(), st0)
+
+
+def test_systems_page_locked_buffers_give_the_same_results(scorer_factory, systems):
+    torch = pytest.importorskip("torch")
+    sc = scorer_factory()
+    sc.set_systems([(s.pocket, s.ligand, len(s.poses)) for s in systems])
+    po, do = sc.systems_layout()
+    h = _packed(systems)
+    E0, G0, st0 = sc.score_systems(h, grad=True)
+    B = int(po[-1])
+    out = (torch.zeros(B, dtype=torch.float64).pin_memory().numpy(),
+           torch.zeros(h.size, dtype=torch.float32).pin_memory().numpy(),
+           torch.zeros(B, dtype=torch.int32).pin_memory().numpy())
+    E, G, st = sc.score_systems(torch.from_numpy(h).pin_memory().numpy(), grad=True, out=out)
+    assert E is out[0] and G is out[1] and st is out[2]
+    assert np.array_equal(E, E0) and np.array_equal(st, st0)
+    assert not (~((G == G0) | (np.isnan(G) & np.isnan(G0)))).any()
