@@ -114,6 +114,15 @@ int mmo_ene_intra(mmo_ctx* ctx, const double* xs, const double* ys, const double
 int mmo_score_poses(mmo_ctx* ctx, int B, const float* dofs, int flags, double* E_out,
                     float* grad_out, int* status_out);
 
+/* The posed coordinates of B poses (the pose map of mmo_score_poses alone:
+ * Optim.apply_config, optim.ml:64-80, or with MMO_F_RECENTER the MC map,
+ * mol.ml:705-710; other flags are ignored): xyz_out B x L x 3 doubles in the
+ * input frame, from the kernel's float-pair coordinates; status_out[B]
+ * (nullable): MMO_S_TOO_LONG as Optim.apply_config raises Mol.Too_long.  The
+ * coordinates a caller writes out as a pose (.xyz, .pqrs). */
+int mmo_posed_coords(mmo_ctx* ctx, int B, const float* dofs, int flags, double* xyz_out,
+                     int* status_out);
+
 /* As mmo_score_poses with device pointers, queued on `stream` (a
  * cudaStream_t; NULL is the legacy default stream) without synchronising;
  * mmo_sync() waits and reports device-side errors.  Calls on one context

@@ -2040,6 +2040,56 @@ int mmo_score_poses(mmo_ctx* ctx, int B, const float* dofs, int flags, double* E
                    });
 }
 
+int mmo_posed_coords(mmo_ctx* ctx, int B, const float* dofs, int flags, double* xyz_out,
+                     int* status_out) {
+  if (!ctx) return MMO_EINVAL;
+  if (!ctx->has_lig) return fail(ctx, MMO_ESTATE, "no ligand: call mmo_set_ligand first");
+  if (B < 0 || (B > 0 && (!dofs || !xyz_out)))
+    return fail(ctx, MMO_EINVAL, "mmo_posed_coords: bad arguments");
+  if (B == 0) return MMO_OK;
+  const int L = ctx->lig.L, nd = 6 + ctx->lig.nrb;
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  int r = ensure_scratch(ctx, B, L, 1, false);
+  if (r) return r;
+  size_t off = 0;
+  const size_t o_st = take(off, sizeof(int) * B);
+  const size_t o_err = take(off, sizeof(int));
+  const size_t in_bytes = sizeof(float) * (size_t)B * nd, st_bytes = off;
+  const size_t x_bytes = sizeof(float4) * 2 * (size_t)B * L;
+  if ((r = grow_host(ctx, &ctx->h_in, &ctx->d_in, &ctx->cap_in, in_bytes))) return r;
+  if ((r = grow_host(ctx, &ctx->h_out, &ctx->d_out, &ctx->cap_out, st_bytes + x_bytes))) return r;
+  memcpy(ctx->h_in, dofs, in_bytes);
+  MMO_CK(cudaMemcpyAsync(ctx->d_in, ctx->h_in, in_bytes, cudaMemcpyHostToDevice, ctx->stream),
+         "H2D");
+  PoseIO io{};
+  io.dofs = reinterpret_cast<const float*>(ctx->d_in);
+  io.status = reinterpret_cast<int*>(ctx->d_out + o_st);
+  io.err = reinterpret_cast<int*>(ctx->d_out + o_err);
+  io.zero_err = 1;
+  io.B = B;
+  io.ox = ctx->origin_f[0];
+  io.oy = ctx->origin_f[1];
+  io.oz = ctx->origin_f[2];
+  MMO_CK(launch_rebuild(ctx->lig, io, ctx->scr, flags & kFlagRecenter, ctx->stream),
+         "rebuild kernel");
+  MMO_CK(cudaMemcpyAsync(ctx->h_out, ctx->d_out, st_bytes, cudaMemcpyDeviceToHost, ctx->stream),
+         "D2H");
+  MMO_CK(cudaMemcpyAsync(ctx->h_out + st_bytes, ctx->scr.X, x_bytes, cudaMemcpyDeviceToHost,
+                         ctx->stream),
+         "D2H");
+  MMO_CK(cudaStreamSynchronize(ctx->stream), "sync");
+  // the posed atoms as hi + lo float pairs in the device frame -> FP64, input frame
+  const float4* X = reinterpret_cast<const float4*>(ctx->h_out + st_bytes);
+  for (size_t e = 0; e < (size_t)B * L; ++e) {
+    const float4 h = X[2 * e], l = X[2 * e + 1];
+    xyz_out[3 * e] = ((double)h.x + (double)l.x) + ctx->origin[0];
+    xyz_out[3 * e + 1] = ((double)h.y + (double)l.y) + ctx->origin[1];
+    xyz_out[3 * e + 2] = ((double)h.z + (double)l.z) + ctx->origin[2];
+  }
+  if (status_out) memcpy(status_out, ctx->h_out + o_st, sizeof(int) * B);
+  return MMO_OK;
+}
+
 int mmo_score_poses_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E,
                            float* d_grad, int* d_status, void* stream) {
   if (!ctx) return MMO_EINVAL;

@@ -483,6 +483,22 @@ class UFFScorer:
             G.ctypes.data_as(C.POINTER(C.c_float)) if G is not None else None, _ip(st)))
         return E, G, st
 
+    def posed_coords(self, dofs, recenter=False):
+        """(xyz float64 [B, L, 3], status int32 [B]): the ligand's atoms after the
+        pose map (Optim.apply_config, or the MC map with recenter), as scored."""
+        dofs = np.ascontiguousarray(dofs, np.float32)
+        if dofs.ndim == 1:
+            dofs = dofs[None, :]
+        B, nd = dofs.shape
+        if self.ligand is None or nd != 6 + self.ligand.nrb:
+            raise ValueError("dofs must be [B, 6 + nrb] for the ligand of set_ligand")
+        xyz = np.zeros((B, self.ligand.n, 3), np.float64)
+        st = np.zeros(B, np.int32)
+        self._check(self._lib.mmo_posed_coords(
+            self._h, B, dofs.ctypes.data_as(C.POINTER(C.c_float)),
+            _L.F_RECENTER if recenter else 0, _dp(xyz), _ip(st)))
+        return xyz, st
+
     def score_config(self, conf, recenter=False) -> float:
         """E_inter + E_intra of one Optim.config, raising TooLong as
         Optim.apply_config does (src/optim.ml:75)."""

@@ -9,11 +9,15 @@ committed by tests/golden/make_ref_data.py.
 * the closures ``ff0 prot`` (ene_inter_builder) and ``ene_intra``
   (ene_intra_builder; ff_score's per-ligand intra energy);
 * interpolated scoring on grids built about the binding site;
-* exhaustive rigid docking about the docked pose's centre.
+* exhaustive rigid docking about the docked pose's centre;
+* the pose map's coordinates (mmo_posed_coords), and the ff_score / ff_opt
+  scripts on these molecules.
 
 Tolerances are the scoring contract's: energies within 1e-5 of
 max(|E64|, sum |pair energies|), gradients within 1e-4 of the largest
 component; the poses here are mostly clash-free, so the first term counts."""
+import os
+
 import numpy as np
 import pytest
 
@@ -147,3 +151,73 @@ def test_ref_exhaustive_docking_matches_oracle(oracle, scorer_factory, ref):
                   abs(sc[order[t + 1]] - sc[order[t]]) if t + 1 < len(order) else np.inf)
         if gap > 4 * tol:
             assert res["frames"][t] == order[t], t
+
+
+@pytest.mark.parametrize("recenter", [False, True])
+def test_posed_coordinates_match_oracle(oracle, scorer_factory, ref, recenter):
+    """mmo_posed_coords: the pose map's atoms (double-float on the GPU)
+    against Optim.apply_config / the MC map in FP64, to 1e-9 A."""
+    rec, ligs = ref
+    lig = ligs[0]
+    s = scorer_factory(rec, lig)
+    d = _poses(lig, 32, 7, recenter)
+    d[16:, 3:6] = np.random.default_rng(1).uniform(-np.pi, np.pi, size=(16, 3))
+    xyz, st = s.posed_coords(d, recenter=recenter)
+    for b in range(len(d)):
+        want, st64 = oracle.apply_config(lig, d[b].astype(np.float64),
+                                         oracle.F_RECENTER if recenter else 0)
+        assert st[b] == st64
+        assert np.abs(xyz[b] - want).max() <= 1e-9, (b, np.abs(xyz[b] - want).max())
+    if not recenter:
+        assert np.abs(xyz[0] - lig.xyz()).max() <= 1e-12  # zero DOFs: the conformer as read
+
+
+def test_ff_score_matches_oracle(oracle, gpu_lib, ref, tmp_path, capsys):
+    """mmo_gb300.ff_score (src/ff_score.ml): E_intra of each ligand as read."""
+    from oracle import np_twin as T
+
+    from mmo_gb300 import ff_score as F
+    from test_ref_data import GOLD
+
+    _, ligs = ref
+    res = F.ff_score(ligs)
+    assert [n for n, _ in res] == [m.name for m in ligs]
+    for (_, e), m in zip(res, ligs):
+        e64 = oracle.ene_intra(m)
+        sc = T.ene_intra(m.xyz(), m.q, m.anum, m.interacting, absolute=True)
+        assert abs(e - e64) <= 1e-5 * max(abs(e64), sc)
+    assert F.main([os.path.join(GOLD, "ref_ligands.pqrs")]) == 0
+    out = capsys.readouterr().out.splitlines()
+    assert len(out) == 3 and all(len(ln.split("\t")) == 2 for ln in out)
+
+
+def test_ff_opt_lowers_the_energy(oracle, gpu_lib, ref, capsys):
+    """mmo_gb300.ff_opt: L-BFGS on the adjoint's gradient lowers E_intra (and,
+    against the receptor, E_inter + E_intra); the written conformer scores, in
+    the oracle, the energy reported for it."""
+    from mmo_gb300 import ff_opt as O
+    from mmo_gb300.ff import UFFScorer
+    from test_ref_data import GOLD
+
+    rec, ligs = ref
+    s = UFFScorer(0)
+    try:
+        for lig in ligs:
+            s.set_ligand(lig)
+            e, xyz = O.minimize(s, lig, iters=40)
+            e0 = oracle.ene_intra(lig)
+            assert e < e0 - 1e-3
+            assert abs(oracle.ene_intra(lig.with_xyz(xyz)) - e) <= 1e-4 * max(1.0, abs(e))
+        s.set_protein(rec)
+        s.set_ligand(ligs[0])
+        e, xyz = O.minimize(s, ligs[0], receptor=True, iters=40)
+        e0 = oracle.ene_inter(rec, ligs[0]) + oracle.ene_intra(ligs[0])
+        moved = ligs[0].with_xyz(xyz)
+        assert e < e0 - 1e-3
+        assert abs(oracle.ene_inter(rec, moved) + oracle.ene_intra(moved) - e) <= \
+            1e-4 * max(1.0, abs(e))
+    finally:
+        s.close()
+    assert O.main([os.path.join(GOLD, "ref_ligands.pqrs"), "--iters", "5"]) == 0
+    out = capsys.readouterr().out.splitlines()
+    assert len(out) == 3 * (2 + 48) and out[1].split(":")[-1]
