@@ -160,7 +160,7 @@ int mmo_sync(mmo_ctx* ctx, void* stream);
 /* Tile shape of the batched pair kernels: poses per lane (1, 2, 4) and
  * protein chunks per pose (0: automatic) of the full sweep, and threads per
  * CTA (256, 512, 768, 1024; the full sweep runs at most 512, the cut-off
- * sweep at most 1024, 768 or 512 for 1, 2 or 4 entries per lane).  Setting 0
+ * sweep at most 768, 512 or 256 for 1, 2 or 4 entries per lane).  Setting 0
  * for all restores the automatic choice. */
 int mmo_set_tiles(mmo_ctx* ctx, int poses_per_lane, int threads, int chunks);
 
