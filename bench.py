@@ -448,9 +448,9 @@ def run_grid(args):
     build()
     st = sc.grid_build_stats()
     sc.set_profiling(False)
-    # the faster launch shape (1 or 2 lattice points per lane; the values are the same)
+    # the fastest launch shape (1, 2 or 4 lattice points per lane; the values are the same)
     shape_ms = {}
-    for kp in (1, 2):
+    for kp in (1, 2, 4):
         sc.set_grid_build(kp)
         build()
         shape_ms[kp] = min(build() for _ in range(3))

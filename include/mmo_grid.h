@@ -51,8 +51,9 @@ typedef struct mmo_grid_spec {
  * done; *ms (may be NULL) the build kernel's device milliseconds. */
 int mmo_build_grids(mmo_ctx* ctx, const mmo_grid_spec* spec, double* ms);
 
-/* Launch shape of the build kernel: lattice points per lane (1 or 2; 0 the
- * automatic choice).  The values do not depend on it. */
+/* Launch shape of the build kernel: lattice points per lane (1, 2, or 4 under
+ * geometric mixing, where 2 is used instead otherwise; 0 the automatic
+ * choice).  The values do not depend on it. */
 int mmo_set_grid_build(mmo_ctx* ctx, int points_per_lane);
 
 /* Load grids computed elsewhere (the reference's .ba1 files, one per type, in

@@ -2735,6 +2735,7 @@ int mmo_build_grids(mmo_ctx* ctx, const mmo_grid_spec* spec, double* ms) {
   double npts = masked ? 0.0 : (double)nx * ny * nz;
   // the counting variant of the kernel (profiling) has one point per lane
   gb.kp = ctx->profiling ? 1 : (ctx->grid_kp_set ? ctx->grid_kp_set : 2);
+  if (gb.kp == 4 && !gb.fact) gb.kp = 2;  // 4 points per lane: the factorised kernel only
   const int TX = kGridTileX, TY = kGridTileY, TZ = 2 * gb.kp;
   for (int tz = 0; tz < (nz + TZ - 1) / TZ; ++tz)
     for (int ty = 0; ty < (ny + TY - 1) / TY; ++ty)
@@ -2812,8 +2813,8 @@ int mmo_build_grids(mmo_ctx* ctx, const mmo_grid_spec* spec, double* ms) {
 
 int mmo_set_grid_build(mmo_ctx* ctx, int points_per_lane) {
   if (!ctx) return MMO_EINVAL;
-  if (points_per_lane < 0 || points_per_lane > 2)
-    return fail(ctx, MMO_EINVAL, "mmo_set_grid_build: points_per_lane must be 0, 1 or 2");
+  if (points_per_lane < 0 || points_per_lane > 4 || points_per_lane == 3)
+    return fail(ctx, MMO_EINVAL, "mmo_set_grid_build: points_per_lane must be 0, 1, 2 or 4");
   ctx->grid_kp_set = points_per_lane;
   return MMO_OK;
 }

@@ -71,6 +71,103 @@ constexpr int grid_smem_bytes() {
          kGridWarps * grid_accs<NE>() * KP * 32 * (int)sizeof(float2);
 }
 
+// The lattice points of one lane in a warp's tile: point c at (i, j, kk[c]),
+// as float pairs in the device frame, whether it is on the lattice and in the
+// mask sphere; and the box of the tile's masked points (warp-wide).
+template <int KP>
+struct TilePoints {
+  int i, j, kk[KP];
+  bool in_lattice[KP], masked[KP];
+  float xh[KP], yh[KP], zh[KP], xl[KP], yl[KP], zl[KP];
+  float blx, bly, blz, bhx, bhy, bhz;
+};
+
+template <int KP>
+__device__ __forceinline__ TilePoints<KP> tile_points(const GridBuild& gb, int3 t, int lane) {
+  static_assert(kGridTileX == 4 && kGridTileY == 4, "lane layout of the tile");
+  TilePoints<KP> P;
+  P.i = t.x * 4 + (lane & 3);
+  P.j = t.y * 4 + ((lane >> 2) & 3);
+  const float big = 1e30f;
+  float lox = big, loy = big, loz = big, hix = -big, hiy = -big, hiz = -big;
+#pragma unroll
+  for (int c = 0; c < KP; ++c) {
+    P.kk[c] = t.z * (2 * KP) + (lane >> 4) + 2 * c;
+    P.in_lattice[c] = P.i < gb.nx && P.j < gb.ny && P.kk[c] < gb.nz;
+    // lattice point in the device frame, as a float pair
+    const double px = gb.o[0] + gb.step * P.i, py = gb.o[1] + gb.step * P.j,
+                 pz = gb.o[2] + gb.step * P.kk[c];
+    const double mx = px - gb.mc[0], my = py - gb.mc[1], mz = pz - gb.mc[2];
+    P.masked[c] = P.in_lattice[c] && mx * mx + my * my + mz * mz < gb.mr2;
+    P.xh[c] = (float)px;
+    P.yh[c] = (float)py;
+    P.zh[c] = (float)pz;
+    P.xl[c] = (float)(px - P.xh[c]);
+    P.yl[c] = (float)(py - P.yh[c]);
+    P.zl[c] = (float)(pz - P.zh[c]);
+    if (P.masked[c]) {
+      lox = fminf(lox, P.xh[c]);
+      loy = fminf(loy, P.yh[c]);
+      loz = fminf(loz, P.zh[c]);
+      hix = fmaxf(hix, P.xh[c]);
+      hiy = fmaxf(hiy, P.yh[c]);
+      hiz = fmaxf(hiz, P.zh[c]);
+    }
+  }
+  P.blx = gwmin(lox);
+  P.bly = gwmin(loy);
+  P.blz = gwmin(loz);
+  P.bhx = gwmax(hix);
+  P.bhy = gwmax(hiy);
+  P.bhz = gwmax(hiz);
+  return P;
+}
+
+// The values of the lane's points for every grid type from the point's
+// compensated sums ad[(e * KP + c) * 32] (e = ELEC: the electrostatic sum;
+// FACT: e = 0, 1 the sums A12, A6; else e = the element's vdW sum), capped
+// at max_E; 0 outside the mask sphere.
+template <bool FACT, int KP, int ELEC>
+__device__ __forceinline__ void grid_store(const GridBuild& gb, const TilePoints<KP>& P,
+                                           const float2* ad, float* grids) {
+  const size_t per = (size_t)gb.nx * gb.ny * gb.nz;
+#pragma unroll
+  for (int c = 0; c < KP; ++c) {
+    if (!P.in_lattice[c]) continue;
+    const size_t idx = (size_t)P.i + (size_t)P.j * gb.nx + (size_t)P.kk[c] * gb.nx * gb.ny;
+    const float2 phi = ad[(ELEC * KP + c) * 32];
+    float2 a12 = make_float2(0.f, 0.f), a6 = a12;
+    if (FACT) {
+      a12 = ad[(0 * KP + c) * 32];
+      a6 = ad[(1 * KP + c) * 32];
+    }
+    for (int l = 0; l < gb.ntypes; ++l) {
+      float v = 0.f;
+      if (P.masked[c]) {
+        float2 vdw;
+        if (FACT) {
+          // sqrt(D_e) (x_e^6 A12 - 2 x_e^3 A6) in float pairs
+          const float4 f = gb.elf[gb.type_elem[l]];  // (sqrt(D_e), 2 x_e^3, x_e^6, 0)
+          const float t1 = f.z * a12.x, t1l = fmaf(f.z, a12.x, -t1) + f.z * a12.y;
+          const float t2 = f.y * a6.x, t2l = fmaf(f.y, a6.x, -t2) + f.y * a6.y;
+          const float dh = __fsub_rn(t1, t2);
+          const float bp = __fsub_rn(dh, t1), ap = __fsub_rn(dh, bp);
+          const float dl = __fadd_rn(__fsub_rn(t1, ap), __fsub_rn(-t2, bp)) + (t1l - t2l);
+          vdw = make_float2(f.x * dh, fmaf(f.x, dh, -(f.x * dh)) + f.x * dl);
+        } else {
+          vdw = ad[(gb.type_elem[l] * KP + c) * 32];
+        }
+        // q phi + V in float pairs: one rounding of the sum of the high parts,
+        // the low parts added to it
+        const float q = gb.type_qf[l];
+        const float e = fmaf(q, phi.x, vdw.x) + fmaf(q, phi.y, vdw.y);
+        v = e < gb.max_Ef ? e : gb.max_Ef;
+      }
+      grids[per * l + idx] = v;
+    }
+  }
+}
+
 // KP lattice points per lane (1 or 2): a warp tile of 4 x 4 x 2 KP points
 template <int DIEL, int NE, int KP, bool COUNT>
 __global__ void __launch_bounds__(kGridWarps * 32) k_grid_build(DevCull cull, GridBuild gb,
@@ -94,41 +191,8 @@ __global__ void __launch_bounds__(kGridWarps * 32) k_grid_build(DevCull cull, Gr
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int tile = blockIdx.x * kGridWarps + w;
   if (tile >= gb.ntiles) return;  // whole warps leave: no block-wide barrier follows
-  static_assert(kGridTileX == 4 && kGridTileY == 4, "lane layout of the tile");
-  const int3 t = gb.tiles[tile];
-  const int i = t.x * 4 + (lane & 3), j = t.y * 4 + ((lane >> 2) & 3);
-  int kk[kGridPts];
-  bool in_lattice[kGridPts], masked[kGridPts];
-  float xh[kGridPts], yh[kGridPts], zh[kGridPts], xl[kGridPts], yl[kGridPts], zl[kGridPts];
-  const float big = 1e30f;
-  float lox = big, loy = big, loz = big, hix = -big, hiy = -big, hiz = -big;
-#pragma unroll
-  for (int c = 0; c < kGridPts; ++c) {
-    kk[c] = t.z * (2 * KP) + (lane >> 4) + 2 * c;
-    in_lattice[c] = i < gb.nx && j < gb.ny && kk[c] < gb.nz;
-    // lattice point in the device frame, as a float pair
-    const double px = gb.o[0] + gb.step * i, py = gb.o[1] + gb.step * j,
-                 pz = gb.o[2] + gb.step * kk[c];
-    const double mx = px - gb.mc[0], my = py - gb.mc[1], mz = pz - gb.mc[2];
-    masked[c] = in_lattice[c] && mx * mx + my * my + mz * mz < gb.mr2;
-    xh[c] = (float)px;
-    yh[c] = (float)py;
-    zh[c] = (float)pz;
-    xl[c] = (float)(px - xh[c]);
-    yl[c] = (float)(py - yh[c]);
-    zl[c] = (float)(pz - zh[c]);
-    if (masked[c]) {
-      lox = fminf(lox, xh[c]);
-      loy = fminf(loy, yh[c]);
-      loz = fminf(loz, zh[c]);
-      hix = fmaxf(hix, xh[c]);
-      hiy = fmaxf(hiy, yh[c]);
-      hiz = fmaxf(hiz, zh[c]);
-    }
-  }
-  // the tile's box over its masked points
-  const float blx = gwmin(lox), bly = gwmin(loy), blz = gwmin(loz);
-  const float bhx = gwmax(hix), bhy = gwmax(hiy), bhz = gwmax(hiz);
+  const TilePoints<KP> P = tile_points<KP>(gb, gb.tiles[tile], lane);
+  const float blx = P.blx, bly = P.bly, blz = P.blz, bhx = P.bhx, bhy = P.bhy, bhz = P.bhz;
   // Sums in three levels: the atoms of one row in FP32 (af), the rows of one
   // block of kGridFlushAtoms protein atoms in FP32 (bf), the blocks in
   // compensated FP32 (s_ad: hi + lo pairs updated by TwoSum, about twice the
@@ -164,9 +228,9 @@ __global__ void __launch_bounds__(kGridWarps * 32) k_grid_build(DevCull cull, Gr
       for (int q = 0; q < NE2; ++q) prm[q] = er[q];
 #pragma unroll
       for (int c = 0; c < kGridPts; ++c) {
-        const float dx = (xh[c] - p.x) + (xl[c] - pl.x);
-        const float dy = (yh[c] - p.y) + (yl[c] - pl.y);
-        const float dz = (zh[c] - p.z) + (zl[c] - pl.z);
+        const float dx = (P.xh[c] - p.x) + (P.xl[c] - pl.x);
+        const float dy = (P.yh[c] - p.y) + (P.yl[c] - pl.y);
+        const float dz = (P.zh[c] - p.z) + (P.zl[c] - pl.z);
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         if (COUNT) n_near[c] += r2 < kCut2;
         const float r2c = fmaxf(r2, kMinR2);
@@ -199,7 +263,7 @@ __global__ void __launch_bounds__(kGridWarps * 32) k_grid_build(DevCull cull, Gr
   };
   bool mine = false;
 #pragma unroll
-  for (int c = 0; c < kGridPts; ++c) mine = mine || masked[c];
+  for (int c = 0; c < kGridPts; ++c) mine = mine || P.masked[c];
   const bool any = __any_sync(kFull, mine);
   if (any) {
     bool dirty = false;
@@ -261,8 +325,8 @@ __global__ void __launch_bounds__(kGridWarps * 32) k_grid_build(DevCull cull, Gr
     unsigned long long ev = 0, cv = 0;
 #pragma unroll
     for (int c = 0; c < kGridPts; ++c) {
-      ev += masked[c] ? n_eval[c] : 0u;
-      cv += masked[c] ? n_near[c] : 0u;
+      ev += P.masked[c] ? n_eval[c] : 0u;
+      cv += P.masked[c] ? n_near[c] : 0u;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -274,42 +338,196 @@ __global__ void __launch_bounds__(kGridWarps * 32) k_grid_build(DevCull cull, Gr
       atomicAdd(gb.pairs + 1, cv);
     }
   }
-  const size_t per = (size_t)gb.nx * gb.ny * gb.nz;
+  grid_store<FACT, KP, ELEC>(gb, P, ad, grids);
+}
+
+// squared distance from (x, y, z) to the box [bl, bh]
+__device__ __forceinline__ float gbox_d2(float x, float y, float z, const float* bl,
+                                         const float* bh) {
+  const float ex = fmaxf(fmaxf(bl[0] - x, x - bh[0]), 0.f);
+  const float ey = fmaxf(fmaxf(bl[1] - y, y - bh[1]), 0.f);
+  const float ez = fmaxf(fmaxf(bl[2] - z, z - bh[2]), 0.f);
+  return fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+}
+
+constexpr int kGridPairList = 64;  // compacted atom pairs per warp (< 32 + 32)
+constexpr int kGridRec = 5;        // float4 per staged pair
+
+template <int KP>
+constexpr int grid_pk_smem_bytes() {
+  return (kNTypes + 1) * 16 + kGridWarps * kGridPairList * kGridRec * 16 +
+         kGridWarps * 3 * KP * 32 * (int)sizeof(float2);
+}
+
+// The factorised build (geometric mixing) on the packed FP32 instructions
+// (add/mul/fma .f32x2) over pairs of protein atoms: the protein as the cut-off
+// sweep's pairs (DevCull::pairs: the atoms of each row in pairs, negated
+// coordinates, a null partner closing a row of odd length), the lane's
+// lattice points in both halves of their registers.  A warp stages the pairs
+// of a row that have an atom within 12.04 A of its tile's box, with the two
+// atoms' (sqrt(D) x^6, sqrt(D) x^3), as five float4; every lane then sums
+// them for its points, half a over the pairs' first atoms and half b over
+// their partners (a split fixed by the layout), in the scalar kernel's
+// arithmetic.  Atoms out of reach add exact zeros, so each value is the same
+// bits whatever the tile's shape or the mask.
+template <int DIEL, int KP, bool COUNT>
+__global__ void __launch_bounds__(kGridWarps * 32) k_grid_build_pk(DevCull cull, GridBuild gb,
+                                                                    float* grids) {
+  constexpr int NACC = 3, ELEC = 2;
+  extern __shared__ __align__(16) float4 gsm[];
+  float4* s_cc = gsm;                           // [ptype] (c12, c6, 0, 0), the null type 0
+  float4* s_list = s_cc + kNTypes + 1;          // [warp][kGridPairList][kGridRec]
+  float2* s_ad = reinterpret_cast<float2*>(s_list + kGridWarps * kGridPairList * kGridRec);
+  for (int k = threadIdx.x; k <= kNTypes; k += blockDim.x) {
+    const float2 v = k < kNTypes ? gb.el[k * kGridElems] : make_float2(0.f, 0.f);
+    s_cc[k] = make_float4(v.x, v.y, 0.f, 0.f);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int tile = blockIdx.x * kGridWarps + w;
+  if (tile >= gb.ntiles) return;  // whole warps leave: no block-wide barrier follows
+  const TilePoints<KP> P = tile_points<KP>(gb, gb.tiles[tile], lane);
+  const float bl[3] = {P.blx, P.bly, P.blz}, bh[3] = {P.bhx, P.bhy, P.bhz};
+  float2 xh[KP], yh[KP], zh[KP], xl[KP], yl[KP], zl[KP];
 #pragma unroll
-  for (int c = 0; c < kGridPts; ++c) {
-    if (!in_lattice[c]) continue;
-    const size_t idx = (size_t)i + (size_t)j * gb.nx + (size_t)kk[c] * gb.nx * gb.ny;
-    const float2 phi = ad[(ELEC * kGridPts + c) * 32];
-    float2 a12 = make_float2(0.f, 0.f), a6 = a12;
-    if (FACT) {
-      a12 = ad[(0 * kGridPts + c) * 32];
-      a6 = ad[(1 * kGridPts + c) * 32];
+  for (int c = 0; c < KP; ++c) {
+    xh[c] = bc2(P.xh[c]);
+    yh[c] = bc2(P.yh[c]);
+    zh[c] = bc2(P.zh[c]);
+    xl[c] = bc2(P.xl[c]);
+    yl[c] = bc2(P.yl[c]);
+    zl[c] = bc2(P.zl[c]);
+  }
+  // sums in three levels, as the scalar kernel: a row in FP32 (af), the rows of
+  // a 1,024-atom block in FP32 (bf), the blocks as compensated float pairs
+  float2* ad = s_ad + (size_t)w * NACC * KP * 32 + lane;  // [e][c] stride 32
+  float2 af[KP][NACC], bf[KP][NACC];
+#pragma unroll
+  for (int c = 0; c < KP; ++c)
+#pragma unroll
+    for (int e = 0; e < NACC; ++e) {
+      af[c][e] = bf[c][e] = bc2(0.f);
+      ad[(e * KP + c) * 32] = make_float2(0.f, 0.f);
     }
-    for (int l = 0; l < gb.ntypes; ++l) {
-      float v = 0.f;
-      if (masked[c]) {
-        float2 vdw;
-        if (FACT) {
-          // sqrt(D_e) (x_e^6 A12 - 2 x_e^3 A6) in float pairs
-          const float4 f = gb.elf[gb.type_elem[l]];  // (sqrt(D_e), 2 x_e^3, x_e^6, 0)
-          const float t1 = f.z * a12.x, t1l = fmaf(f.z, a12.x, -t1) + f.z * a12.y;
-          const float t2 = f.y * a6.x, t2l = fmaf(f.y, a6.x, -t2) + f.y * a6.y;
-          const float dh = __fsub_rn(t1, t2);
-          const float bp = __fsub_rn(dh, t1), ap = __fsub_rn(dh, bp);
-          const float dl = __fadd_rn(__fsub_rn(t1, ap), __fsub_rn(-t2, bp)) + (t1l - t2l);
-          vdw = make_float2(f.x * dh, fmaf(f.x, dh, -(f.x * dh)) + f.x * dl);
-        } else {
-          vdw = ad[(gb.type_elem[l] * kGridPts + c) * 32];
-        }
-        // q phi + V in float pairs: one rounding of the sum of the high parts,
-        // the low parts added to it
-        const float q = gb.type_qf[l];
-        const float e = fmaf(q, phi.x, vdw.x) + fmaf(q, phi.y, vdw.y);
-        v = e < gb.max_Ef ? e : gb.max_Ef;
+  float4* wl = s_list + (size_t)w * kGridPairList * kGridRec;
+  unsigned n_eval = 0, n_near[KP] = {};
+  auto evaluate = [&](int n, int nnull) {
+    __syncwarp();
+    if (COUNT) n_eval += 2u * n - nnull;
+#pragma unroll 2
+    for (int v = 0; v < n; ++v) {
+      const float4* rr = wl + kGridRec * v;
+      const float4 r0 = rr[0], r1 = rr[1], r2 = rr[2], r3 = rr[3], r4 = rr[4];
+#pragma unroll
+      for (int c = 0; c < KP; ++c) {
+        const float2 dx = __fadd2_rn(__fadd2_rn(xh[c], lo_pair(r0)), __fadd2_rn(xl[c], lo_pair(r2)));
+        const float2 dy = __fadd2_rn(__fadd2_rn(yh[c], hi_pair(r0)), __fadd2_rn(yl[c], hi_pair(r2)));
+        const float2 dz = __fadd2_rn(__fadd2_rn(zh[c], lo_pair(r1)), __fadd2_rn(zl[c], lo_pair(r3)));
+        const float2 d2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+        if (COUNT)
+          n_near[c] += (d2.x < kCut2) + (d2.y < kCut2 && __float_as_uint(r1.w) != 0x80000000u);
+        const float2 r2c = make_float2(fmaxf(d2.x, kMinR2), fmaxf(d2.y, kMinR2));
+        const float2 ir = make_float2(rsqrtf(r2c.x), rsqrtf(r2c.y));
+        const float2 ir2 = __fmul2_rn(ir, ir);
+        const float2 t = __ffma2_rn(r2c, bc2(-1.0f / 144.0f), bc2(1.0f));
+        const float2 sw = make_float2(fmaxf(t.x, 0.0f), fmaxf(t.y, 0.0f));
+        const float2 ws = __fmul2_rn(sw, sw);
+        af[c][ELEC] = __ffma2_rn(__fmul2_rn(ws, hi_pair(r1)), DIEL == 0 ? ir : ir2, af[c][ELEC]);
+        // D_ij (x_ij/r)^12 = c12_i c12_e / r^12, 2 D_ij (x_ij/r)^6 = 2 c6_i c6_e / r^6
+        const float2 ir6 = __fmul2_rn(__fmul2_rn(ir2, ir2), ir2);
+        af[c][0] = __ffma2_rn(__fmul2_rn(ws, lo_pair(r4)), __fmul2_rn(ir6, ir6), af[c][0]);
+        af[c][1] = __ffma2_rn(__fmul2_rn(ws, hi_pair(r4)), ir6, af[c][1]);
       }
-      grids[per * l + idx] = v;
+    }
+    __syncwarp();
+  };
+  bool mine = false;
+#pragma unroll
+  for (int c = 0; c < KP; ++c) mine = mine || P.masked[c];
+  if (__any_sync(kFull, mine)) {
+    bool dirty = false;
+    for (int r = 0; r < cull.nrows; ++r) {
+      const int b = cull.row_start[r + 1];
+      const float4 rb = cull.row_box[r];
+      const float ey = fmaxf(fmaxf(rb.x - bh[1], bl[1] - rb.y), 0.f);
+      const float ez = fmaxf(fmaxf(rb.z - bh[2], bl[2] - rb.w), 0.f);
+      if (fmaf(ey, ey, ez * ez) < kCullR2) {
+        const int pa = cull.pair_start[r], pb = cull.pair_start[r + 1];
+        int cnt = 0, nnull = 0;
+        for (int i0 = pa; i0 < pb; i0 += 32) {
+          const int ip = i0 + lane;
+          bool in = false, null_b = false;
+          float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
+          if (ip < pb) {
+            q0 = cull.pairs[4 * (size_t)ip];
+            q1 = cull.pairs[4 * (size_t)ip + 1];
+            null_b = __float_as_uint(q1.w) == 0x80000000u;
+            in = gbox_d2(-q0.x, -q0.z, -q1.x, bl, bh) < kCullR2 ||
+                 (!null_b && gbox_d2(-q0.y, -q0.w, -q1.y, bl, bh) < kCullR2);
+          }
+          const unsigned m = __ballot_sync(kFull, in);
+          if (in) {
+            float4* dst = wl + kGridRec * (cnt + __popc(m & ((1u << lane) - 1u)));
+            const float4 q2 = cull.pairs[4 * (size_t)ip + 2], q3 = cull.pairs[4 * (size_t)ip + 3];
+            // q3.zw: the atoms' type row offsets of the pair table (type * kNTypes * 16)
+            const float4 ca = s_cc[__float_as_int(q3.z) / (16 * kNTypes)];
+            const float4 cb = s_cc[__float_as_int(q3.w) / (16 * kNTypes)];
+            dst[0] = q0;
+            dst[1] = q1;
+            dst[2] = q2;
+            dst[3] = q3;
+            dst[4] = make_float4(ca.x, cb.x, ca.y, cb.y);
+          }
+          if (COUNT) nnull += __popc(__ballot_sync(kFull, in && null_b));
+          cnt += __popc(m);
+          if (cnt >= 32) {
+            evaluate(cnt, nnull);
+            cnt = 0;
+            nnull = 0;
+          }
+        }
+        evaluate(cnt, nnull);
+#pragma unroll
+        for (int c = 0; c < KP; ++c)
+#pragma unroll
+          for (int e = 0; e < NACC; ++e) {
+            bf[c][e] = __fadd2_rn(bf[c][e], af[c][e]);
+            af[c][e] = bc2(0.f);
+          }
+        dirty = true;
+      }
+      // the block ends where the atom index crosses a multiple of kGridFlushAtoms
+      if (dirty && (r + 1 == cull.nrows || (b - 1) / kGridFlushAtoms != b / kGridFlushAtoms)) {
+#pragma unroll
+        for (int c = 0; c < KP; ++c)
+#pragma unroll
+          for (int e = 0; e < NACC; ++e) {
+            float2& acc = ad[(e * KP + c) * 32];
+            acc = two_sum_add(two_sum_add(acc, bf[c][e].x), bf[c][e].y);
+            bf[c][e] = bc2(0.f);
+          }
+        dirty = false;
+      }
     }
   }
+  if (COUNT) {
+    unsigned long long ev = 0, cv = 0;
+#pragma unroll
+    for (int c = 0; c < KP; ++c) {
+      ev += P.masked[c] ? n_eval : 0u;
+      cv += P.masked[c] ? n_near[c] : 0u;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      ev += __shfl_xor_sync(kFull, ev, o);
+      cv += __shfl_xor_sync(kFull, cv, o);
+    }
+    if (lane == 0 && ev) {
+      atomicAdd(gb.pairs, ev);
+      atomicAdd(gb.pairs + 1, cv);
+    }
+  }
+  grid_store<true, KP, ELEC>(gb, P, ad, grids);
 }
 
 // Lattice coordinate u = (x - o) / step of a float-pair coordinate on one axis,
@@ -402,9 +620,21 @@ cudaError_t grid_build_as(const DevCull& cull, const GridBuild& gb, float* grids
 // NE = the number of grid elements exactly, so that no element slot is
 // evaluated in vain
 template <int DIEL, int KP, bool COUNT>
+cudaError_t grid_build_pk(const DevCull& cull, const GridBuild& gb, float* grids,
+                          cudaStream_t st) {
+  constexpr int smem = grid_pk_smem_bytes<KP>();
+  const cudaError_t e = cudaFuncSetAttribute(k_grid_build_pk<DIEL, KP, COUNT>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  const int blocks = (gb.ntiles + kGridWarps - 1) / kGridWarps;
+  k_grid_build_pk<DIEL, KP, COUNT><<<blocks, kGridWarps * 32, smem, st>>>(cull, gb, grids);
+  return cudaGetLastError();
+}
+
+template <int DIEL, int KP, bool COUNT>
 cudaError_t grid_build_ne(const DevCull& cull, const GridBuild& gb, float* grids,
                           cudaStream_t st) {
-  if (gb.fact) return grid_build_as<DIEL, 0, KP, COUNT>(cull, gb, grids, st);
+  if (gb.fact) return grid_build_pk<DIEL, KP, COUNT>(cull, gb, grids, st);
   switch (gb.nelem) {
     case 1: return grid_build_as<DIEL, 1, KP, COUNT>(cull, gb, grids, st);
     case 2: return grid_build_as<DIEL, 2, KP, COUNT>(cull, gb, grids, st);
@@ -426,6 +656,10 @@ template <int DIEL, bool COUNT>
 cudaError_t grid_build_kp(const DevCull& cull, const GridBuild& gb, float* grids,
                           cudaStream_t st) {
   if (COUNT && gb.kp != 1) return cudaErrorInvalidValue;
+  if (!COUNT && gb.kp == 4) {  // the packed (factorised) kernel only
+    if (!gb.fact) return cudaErrorInvalidValue;
+    return grid_build_pk<DIEL, 4, false>(cull, gb, grids, st);
+  }
   if (!COUNT && gb.kp == 2) return grid_build_ne<DIEL, 2, false>(cull, gb, grids, st);
   return grid_build_ne<DIEL, 1, COUNT>(cull, gb, grids, st);
 }
@@ -434,7 +668,7 @@ cudaError_t grid_build_kp(const DevCull& cull, const GridBuild& gb, float* grids
 cudaError_t launch_grid_build(const DevCull& cull, const GridBuild& gb, int dielectric,
                               float* grids, cudaStream_t st) {
   if (gb.ntiles <= 0) return cudaSuccess;
-  if (gb.nelem < 1 || gb.nelem > kGridElems || (gb.kp != 1 && gb.kp != 2))
+  if (gb.nelem < 1 || gb.nelem > kGridElems || (gb.kp != 1 && gb.kp != 2 && gb.kp != 4))
     return cudaErrorInvalidValue;
   const bool count = gb.pairs != nullptr;
   if (dielectric)

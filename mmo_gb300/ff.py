@@ -302,7 +302,8 @@ class UFFScorer:
         return ms.value
 
     def set_grid_build(self, points_per_lane: int = 0) -> None:
-        """Launch shape of the grid build (1 or 2 lattice points per lane, 0 automatic)."""
+        """Launch shape of the grid build (1, 2 or, under geometric mixing, 4
+        lattice points per lane; 0 automatic)."""
         self._check(self._lib.mmo_set_grid_build(self._h, points_per_lane))
 
     def load_grids(self, step, dims, origin, types, values) -> None:
