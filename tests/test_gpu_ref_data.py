@@ -10,6 +10,7 @@ committed by tests/golden/make_ref_data.py.
   (ene_intra_builder; ff_score's per-ligand intra energy);
 * interpolated scoring on grids built about the binding site;
 * exhaustive rigid docking about the docked pose's centre;
+* Monte Carlo chains from the docked pose;
 * the pose map's coordinates (mmo_posed_coords), and the ff_score / ff_opt
   scripts on these molecules.
 
@@ -221,3 +222,28 @@ def test_ff_opt_lowers_the_energy(oracle, gpu_lib, ref, capsys):
     assert O.main([os.path.join(GOLD, "ref_ligands.pqrs"), "--iters", "5"]) == 0
     out = capsys.readouterr().out.splitlines()
     assert len(out) == 3 * (2 + 48) and out[1].split(":")[-1]
+
+
+def test_mc_chains_on_the_real_complex(oracle, scorer_factory, ref):
+    """Monte Carlo chains (mmo_mc_run, CUDA graph, gradient-descent
+    minimisation every 40 steps) from the docked pose of data/docked.mol2 in
+    the 3A2J receptor: the best energies never exceed the start, the returned
+    energies are the scorer's of the returned poses, and the final poses
+    re-scored in FP64 agree within the scoring contract."""
+    torch = pytest.importorskip("torch")
+    from mmo_gb300 import lib as L
+    from test_gpu_mc import _run
+
+    rec, ligs = ref
+    lig = ligs[0]
+    sc = scorer_factory(rec, lig)
+    d0 = _poses(lig, 32, 5, True)
+    E_start, _, _ = sc.score_poses(d0, recenter=True)
+    d, E, bd, bE, acc, st = _run(torch, sc, L, d0, 160, minimize_every=40, minimize_iters=8)
+    assert np.all(np.isfinite(E)) and np.all(acc > 0)
+    assert np.all(bE <= E_start)
+    Er, _, _ = sc.score_poses(d, recenter=True)
+    assert np.array_equal(Er, E)
+    system = synth.System(lig.name, rec, lig, d)
+    E64, _, _, scale = ref_batch(oracle, system, d[:12], recenter=True)
+    assert_energy(E[:12], E64, scale)
