@@ -81,3 +81,29 @@ def test_oracle_gradient_on_the_real_complex(oracle):
         fd = oracle.grad_fd(rec, lig, confs[b], 1e-6)
         scale = np.abs(fd).max()
         assert np.abs(G[b] - fd).max() <= 1e-5 * scale, b
+
+
+def test_reference_reader_reads_our_pqrs(tmp_path):
+    """The reference's own .pqrs reader (bin/pqrs_center.py: the header and the
+    atom lines, their geometric centre) on molecules written by this
+    repository's .pqrs writer: the same header and centre as ours."""
+    import subprocess
+
+    from mmo_gb300.topology import write_pqrs
+
+    sys.path.insert(0, GOLD)
+    import make_ref_data as G
+
+    tool = os.path.join(G.DEFAULT_REF, "bin", "pqrs_center.py")
+    if not os.path.isfile(tool):
+        pytest.skip("the reference's bin/pqrs_center.py is not on this machine")
+    rec, ligs = ref_molecules()
+    for k, (m, receptor) in enumerate([(rec, True)] + [(l, False) for l in ligs]):
+        fn = os.path.join(tmp_path, "m%d.pqrs" % k)
+        write_pqrs(fn, [m], receptor=receptor)
+        out = subprocess.run([sys.executable, tool, fn], capture_output=True, text=True,
+                             check=True).stdout.splitlines()
+        head = "%d:%s" % (m.n, m.name) if receptor else "%d:%d:%s" % (m.n, m.nrb, m.name)
+        assert out[0] == head
+        got = np.array([float(v) for v in out[1].split()])
+        assert np.allclose(got, m.xyz().mean(axis=0), rtol=1e-5, atol=1e-5)
