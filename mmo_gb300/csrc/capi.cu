@@ -435,6 +435,12 @@ void make_ligand_blob(int mixing, const LigIn& in, LigBlob* out) {
   for (int t = 0; t < nrb; ++t)
     for (int k = in.goff[t]; k < in.goff[t + 1]; ++k)
       const_cast<uint32_t*>(H.amask)[in.gat[k]] |= 1u << t;
+  // the torsions whose group holds exactly one atom of the pair, as bits in the
+  // pair parameters' w (unused by the pair term)
+  for (int p = 0; p < np; ++p) {
+    const uint32_t cross = H.amask[pij[p].x] ^ H.amask[pij[p].y];
+    memcpy(&ppar[p].w, &cross, sizeof cross);
+  }
   memcpy((void*)H.grp_off, in.goff.data(), sizeof(int) * (nrb + 1));
   if (!in.gat.empty())
     memcpy((void*)H.grp_atoms, in.gat.data(), sizeof(int) * in.gat.size());

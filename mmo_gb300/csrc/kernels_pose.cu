@@ -300,8 +300,10 @@ __device__ __forceinline__ void axis_angle(float ux, float uy, float uz, float c
 template <int DIEL, int IFORM>
 __device__ __forceinline__ float intra_pair_g(const float4* sh, const float4* sl, int i, int j,
                                               float4 par, float& e, float& dx, float& dy,
-                                              float& dz) {
-  const float4 ih = sh[i], il = sl[i], jh = sh[j], jl = sl[j];
+                                              float& dz, float4& ih, float4& jh) {
+  ih = sh[i];
+  jh = sh[j];
+  const float4 il = sl[i], jl = sl[j];
   dx = split_diff(ih.x, il.x, jh.x, jl.x);
   dy = split_diff(ih.y, il.y, jh.y, jl.y);
   dz = split_diff(ih.z, il.z, jh.z, jl.z);
@@ -372,17 +374,18 @@ __device__ __noinline__ void finish_pose(const DevLigand& lig, int C, const doub
       const int2 ij = lig.pair_ij[p];
       const float4 par = lig.pair_par[p];
       float ep, dx, dy, dz;
-      const float g = intra_pair_g<DIEL, IFORM>(sxh, sxl, ij.x, ij.y, par, ep, dx, dy, dz);
+      float4 ih, jh;
+      const float g = intra_pair_g<DIEL, IFORM>(sxh, sxl, ij.x, ij.y, par, ep, dx, dy, dz, ih, jh);
       acc += ep;
-      if (crossing) {
-        const uint32_t mi = lig.amask[ij.x], mj = lig.amask[ij.y];
-        uint32_t x = mi ^ mj;
+      uint32_t x = __float_as_uint(par.w);  // the torsions the pair straddles
+      if (crossing && x) {
+        const uint32_t mi = lig.amask[ij.x];
         while (x) {
           const int t = __ffs(x) - 1;
           x &= x - 1;
           const bool in_i = (mi >> t) & 1u;
           const float4 w = saxis[t], cc = saxis[nrb + t];
-          const float4 m = sxh[in_i ? ij.x : ij.y];
+          const float4 m = in_i ? ih : jh;
           const float lx = m.x - cc.x, ly = m.y - cc.y, lz = m.z - cc.z;
           const float v = dx * (w.y * lz - w.z * ly) + dy * (w.z * lx - w.x * lz) +
                           dz * (w.x * ly - w.y * lx);

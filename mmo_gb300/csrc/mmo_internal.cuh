@@ -63,7 +63,8 @@ struct DevLigand {
   const int2* bonds;        // [nrb] (left, right) rotation axis
   const uint32_t* gmask;    // [nrb][kSlots] group bitmask, bit (a & 31) of word (a >> 5)
   const int2* pair_ij;      // [npairs] interacting pairs i < j (mol.ml:203-208)
-  const float4* pair_par;   // [npairs] (x^2, D, K q_i q_j, 0)
+  const float4* pair_par;   // [npairs] (x^2, D, K q_i q_j, the bits of the torsions whose
+                            // group holds exactly one of the two atoms)
   const uint32_t* amask;    // [L] bit t set when the atom is in rotation group t
   const int* grp_off;       // [nrb + 1] rotation groups as CSR
   const int* grp_atoms;
