@@ -809,7 +809,7 @@ def main():
     sc.set_profiling(True)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    pair_ms = []
+    pair_ms, stage_ms = [], []
     clocks = Clocks(local)
     if dist:
         dist.barrier()
@@ -821,7 +821,8 @@ def main():
         starts[k].record(stream)
         step()
         ends[k].record(stream)
-        pair_ms.append(sc.stage_times()[1])  # waits for this step's events
+        stage_ms.append(sc.stage_times())  # waits for this step's events
+        pair_ms.append(stage_ms[-1][1])
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     clk = clocks.stop()
@@ -930,6 +931,8 @@ def main():
                      "flops_per_pair": FLOPS_PAIR_GRAD, "pairs_evaluated": pairs_ev,
                      "pairs_all": pairs_all, "flops_per_launch": flops,
                      "ms_per_launch": pair_avg},
+        "stages_ms": dict(zip(("rebuild", "sweep", "finish", "sort"),
+                              (float(v) for v in np.mean(np.array(stage_ms), axis=0)))),
         "clocks": clk,
         "wall_s_timed": wall,
         "status_bits_set": int(np.count_nonzero(st)),
