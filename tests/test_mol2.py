@@ -116,3 +116,25 @@ def test_receptor_and_errors(tmp_path):
     # a disconnected atom: the ligand is skipped
     src.write_text(LIG.replace("    11     8    11    1\n", "").replace(" 11 11 0", " 11 10 0"))
     assert M.mol2_to_pqrs(str(src), str(dst)) == ["test_lig"]
+
+
+def test_ff_score_reads_mol2_like_pqrs(tmp_path):
+    """mmo_gb300.ff_score's input: a .mol2 file gives the same ligands as its
+    .pqrs conversion (topology, charges, coordinates), and a ligand with a
+    disconnected atom is skipped as mol2pqrs skips it."""
+    from mmo_gb300.ff_score import load_ligands
+
+    src = tmp_path / "lig.mol2"
+    src.write_text(LIG)
+    dst = tmp_path / "lig.pqrs"
+    M.mol2_to_pqrs(str(src), str(dst))
+    (a,) = load_ligands(str(src))
+    (b,) = load_ligands(str(dst))
+    assert a.n == b.n and a.nrb == b.nrb
+    assert np.array_equal(a.dists, b.dists) and np.array_equal(a.anum, b.anum)
+    assert np.allclose(a.q, b.q) and np.allclose(a.xyz(), b.xyz())
+    assert [sorted(g) for g in a.rgroups] == [sorted(g) for g in b.rgroups]
+    lone = LIG.replace("     11     8    11    1\n", "").replace(" 11 11 0 0 0", " 11 10 0 0 0")
+    src2 = tmp_path / "lone.mol2"
+    src2.write_text(lone)
+    assert load_ligands(str(src2)) == []
