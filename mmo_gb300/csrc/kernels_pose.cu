@@ -319,16 +319,67 @@ __host__ __device__ constexpr int finish_warp_f4(int L, int nrb) {
   return 2 * L + 5 * nrb + (33 * nrb + 3) / 4;
 }
 
+// Final axis w_t and centre C_t of torsion t from the posed coordinates:
+// saxis[t] = w_t, saxis[nrb + t] = C_t.
+__device__ __forceinline__ void torsion_frame(const DevLigand& lig, const float4* sxh,
+                                              const float4* sxl, float4* saxis, int t) {
+  const int nrb = lig.nrb;
+  const int2 bd = lig.bonds[t];
+  const float4 rh = sxh[bd.y], rl = sxl[bd.y];
+  const float4 lh = sxh[bd.x], ll = sxl[bd.x];
+  const float ax = split_diff(rh.x, rl.x, lh.x, ll.x), ay = split_diff(rh.y, rl.y, lh.y, ll.y),
+              az = split_diff(rh.z, rl.z, lh.z, ll.z);
+  const float inv = rsqrtf(ax * ax + ay * ay + az * az);
+  saxis[t] = make_float4(ax * inv, ay * inv, az * inv, 0.f);
+  saxis[nrb + t] = rh;
+}
+
+// Interacting pair p (i < j): its energy into acc and, when crossing, the
+// torsion terms (dE/dX_moving) . (w_t x (X_moving - C_t)) of every torsion
+// whose group holds exactly one of the two atoms, into col[t * stride].
+template <int DIEL, int IFORM>
+__device__ __forceinline__ void intra_pair_terms(const DevLigand& lig, const float4* sxh,
+                                                 const float4* sxl, const float4* saxis, int p,
+                                                 bool crossing, float& acc, float* col,
+                                                 int stride) {
+  const int nrb = lig.nrb;
+  const int2 ij = lig.pair_ij[p];
+  const float4 par = lig.pair_par[p];
+  float ep, dx, dy, dz;
+  float4 ih, jh;
+  const float g = intra_pair_g<DIEL, IFORM>(sxh, sxl, ij.x, ij.y, par, ep, dx, dy, dz, ih, jh);
+  acc += ep;
+  uint32_t x = __float_as_uint(par.w);  // the torsions the pair straddles
+  if (crossing && x) {
+    const uint32_t mi = lig.amask[ij.x];
+    while (x) {
+      const int t = __ffs(x) - 1;
+      x &= x - 1;
+      const bool in_i = (mi >> t) & 1u;
+      const float4 w = saxis[t], cc = saxis[nrb + t];
+      const float4 m = in_i ? ih : jh;
+      const float lx = m.x - cc.x, ly = m.y - cc.y, lz = m.z - cc.z;
+      const float v = dx * (w.y * lz - w.z * ly) + dy * (w.z * lx - w.x * lz) +
+                      dz * (w.x * ly - w.y * lx);
+      col[t * stride] = fmaf(in_i ? g : -g, v, col[t * stride]);
+    }
+  }
+}
+
 // finish_pose: one warp, one pose.  ep / gp: the pose's inter partials
 // [C][L]; Xb, Yb, recb, cenp, dof, grad, Eo, sto: the pose's own slots;
-// wsm: the warp's shared memory (finish_warp_f4 float4).
+// wsm: the warp's shared memory (finish_warp_f4 float4).  pre_dti non-null:
+// the intra energy (pre_e) and the nested groups' torsion terms (pre_dti[t])
+// were summed beforehand (k_finish_one), so the pair loop is skipped.
 // (not inlined, as rebuild_pose)
 template <bool GRAD, bool RECENTER, int DIEL, int IFORM>
 __device__ __noinline__ void finish_pose(const DevLigand& lig, int C, const double* ep,
                                             const float4* gp, const float4* Xb, const float4* Yb,
                                             const float4* recb, const float4* cenp,
                                             const float* dof, float* grad, double* Eo, int* sto,
-                                            int flags, float4* wsm) {
+                                            int flags, float4* wsm, double pre_e = 0.0,
+                                            const float* pre_dti = nullptr) {
+  const bool pre = pre_dti != nullptr;
   const int lane = threadIdx.x & 31;
   const int L = lig.L, nrb = lig.nrb;
   float4* sxh = wsm;
@@ -350,51 +401,18 @@ __device__ __noinline__ void finish_pose(const DevLigand& lig, int C, const doub
     __syncwarp();
   }
   const bool crossing = GRAD && intra && lig.nested && nrb > 0;
-  if (crossing) {
-    // final axis w_t and centre C_t of every torsion, from the posed coordinates
-    if (lane < nrb) {
-      const int2 bd = lig.bonds[lane];
-      const float4 rh = sxh[bd.y], rl = sxl[bd.y];
-      const float4 lh = sxh[bd.x], ll = sxl[bd.x];
-      const float ax = split_diff(rh.x, rl.x, lh.x, ll.x), ay = split_diff(rh.y, rl.y, lh.y, ll.y),
-                  az = split_diff(rh.z, rl.z, lh.z, ll.z);
-      const float inv = rsqrtf(ax * ax + ay * ay + az * az);
-      saxis[lane] = make_float4(ax * inv, ay * inv, az * inv, 0.f);
-      saxis[nrb + lane] = rh;
-    }
+  if (crossing && !pre) {
+    if (lane < nrb) torsion_frame(lig, sxh, sxl, saxis, lane);
     for (int t = 0; t < nrb; ++t) sdti[t * 33 + lane] = 0.f;
     __syncwarp();
   }
-  if (intra) {
-    // interacting pairs i < j: the energy, and for nested groups the torsion
-    // terms (dE/dX_moving) . (w_t x (X_moving - C_t)) of every torsion whose
-    // group holds exactly one of the two atoms
+  if (intra && !pre) {
     float acc = 0.f;
-    for (int p = lane; p < lig.npairs; p += 32) {
-      const int2 ij = lig.pair_ij[p];
-      const float4 par = lig.pair_par[p];
-      float ep, dx, dy, dz;
-      float4 ih, jh;
-      const float g = intra_pair_g<DIEL, IFORM>(sxh, sxl, ij.x, ij.y, par, ep, dx, dy, dz, ih, jh);
-      acc += ep;
-      uint32_t x = __float_as_uint(par.w);  // the torsions the pair straddles
-      if (crossing && x) {
-        const uint32_t mi = lig.amask[ij.x];
-        while (x) {
-          const int t = __ffs(x) - 1;
-          x &= x - 1;
-          const bool in_i = (mi >> t) & 1u;
-          const float4 w = saxis[t], cc = saxis[nrb + t];
-          const float4 m = in_i ? ih : jh;
-          const float lx = m.x - cc.x, ly = m.y - cc.y, lz = m.z - cc.z;
-          const float v = dx * (w.y * lz - w.z * ly) + dy * (w.z * lx - w.x * lz) +
-                          dz * (w.x * ly - w.y * lx);
-          sdti[t * 33 + lane] = fmaf(in_i ? g : -g, v, sdti[t * 33 + lane]);
-        }
-      }
-    }
+    for (int p = lane; p < lig.npairs; p += 32)
+      intra_pair_terms<DIEL, IFORM>(lig, sxh, sxl, saxis, p, crossing, acc, sdti + lane, 33);
     e += (double)acc;
   }
+  if (intra && pre && lane == 0) e += pre_e;
   e = warp_sum(e);
   if (lane == 0) {
     *Eo = e;
@@ -532,7 +550,9 @@ __device__ __noinline__ void finish_pose(const DevLigand& lig, int C, const doub
   }
   // intra torsion terms of nested groups, each summed in lane order
   float dti_mine = 0.f;
-  if (crossing) {
+  if (crossing && pre) {
+    if (lane < nrb) dti_mine = pre_dti[lane];
+  } else if (crossing) {
     __syncwarp();
     if (lane < nrb)
       for (int k = 0; k < 32; ++k) dti_mine += sdti[lane * 33 + k];
@@ -635,6 +655,67 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kFinishBlocksPerSM)
       fsm + wib * finish_warp_f4(L, nrb));
 }
 
+// One pose (the one-pose path): the CTA's threads share the interacting pairs
+// (the intra energy and the nested groups' torsion terms, each summed in a
+// fixed order), then warp 0 runs the rest of finish_pose with those sums.
+constexpr int kFinishOne = 256;
+
+__host__ __device__ constexpr int finish_one_f4(int L, int nrb) {
+  return 2 * L + 2 * nrb + kFinishOne / 64 + 1 + (nrb * (kFinishOne + 2) + 3) / 4 +
+         finish_warp_f4(L, nrb);
+}
+
+template <bool GRAD, bool RECENTER, int DIEL, int IFORM>
+__global__ void __launch_bounds__(kFinishOne)
+    k_finish_one(DevLigand lig, PoseIO io, Scratch scr, int flags) {
+  extern __shared__ __align__(16) float4 fsm[];
+  const int L = lig.L, nrb = lig.nrb, tid = threadIdx.x;
+  float4* sxh = fsm;
+  float4* sxl = sxh + L;
+  float4* saxis = sxl + L;                                          // [2 nrb]
+  double* sred = reinterpret_cast<double*>(saxis + 2 * nrb);        // [warps], then the total
+  float* sdt = reinterpret_cast<float*>(saxis + 2 * nrb + kFinishOne / 64 + 1);
+  float* stot = sdt + (size_t)nrb * (kFinishOne + 1);               // [nrb] torsion totals
+  float4* wsm = saxis + 2 * nrb + kFinishOne / 64 + 1 + (nrb * (kFinishOne + 2) + 3) / 4;
+  const bool intra = flags & kFlagIntra;
+  const bool crossing = GRAD && intra && lig.nested && nrb > 0;
+  if (intra)
+    for (int a = tid; a < L; a += kFinishOne) {
+      sxh[a] = scr.X[(size_t)a * 2];
+      sxl[a] = scr.X[(size_t)a * 2 + 1];
+    }
+  if (crossing)
+    for (int k = tid; k < nrb * (kFinishOne + 1); k += kFinishOne) sdt[k] = 0.f;
+  __syncthreads();
+  if (crossing && tid < nrb) torsion_frame(lig, sxh, sxl, saxis, tid);
+  __syncthreads();
+  if (intra) {
+    float acc = 0.f;
+    for (int p = tid; p < lig.npairs; p += kFinishOne)
+      intra_pair_terms<DIEL, IFORM>(lig, sxh, sxl, saxis, p, crossing, acc, sdt + tid,
+                                    kFinishOne + 1);
+    const double w = warp_sum((double)acc);
+    if ((tid & 31) == 0) sred[tid >> 5] = w;
+  }
+  __syncthreads();
+  if (intra && tid == 0) {
+    double e = 0.0;
+    for (int k = 0; k < kFinishOne / 32; ++k) e += sred[k];
+    sred[kFinishOne / 32] = e;
+  }
+  if (crossing && tid < nrb) {
+    float t = 0.f;
+    for (int k = 0; k < kFinishOne; ++k) t += sdt[tid * (kFinishOne + 1) + k];
+    stot[tid] = t;
+  }
+  __syncthreads();
+  if (tid >= 32) return;  // warp 0 alone from here: no block-wide barrier follows
+  finish_pose<GRAD, RECENTER, DIEL, IFORM>(
+      lig, scr.C, scr.Epart, GRAD ? scr.Gpart : nullptr, scr.X, GRAD ? scr.Y : nullptr,
+      GRAD ? scr.rec : nullptr, GRAD ? scr.cen : nullptr, io.dofs, GRAD ? io.grad : nullptr,
+      io.E, io.status, flags, wsm, intra ? sred[kFinishOne / 32] : 0.0, stot);
+}
+
 // one warp: sum of n FP64 partials
 __global__ void k_reduce_plain(const double* Epart, int n, double* out) {
   double e = 0.0;
@@ -690,6 +771,16 @@ cudaError_t rebuild_tpp(int tpp, const DevLigand& lig, const PoseIO& io, const S
 template <bool G, bool RC, int DIEL, int IFORM>
 cudaError_t finish_t(const DevLigand& lig, const PoseIO& io, const Scratch& s, int flags,
                      cudaStream_t st) {
+  if (io.B == 1) {  // one pose: a CTA shares its intra pairs
+    const int smem = finish_one_f4(lig.L, lig.nrb) * (int)sizeof(float4);
+    if (smem > 48 * 1024) {
+      const cudaError_t e = cudaFuncSetAttribute(k_finish_one<G, RC, DIEL, IFORM>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      if (e != cudaSuccess) return e;
+    }
+    k_finish_one<G, RC, DIEL, IFORM><<<1, kFinishOne, smem, st>>>(lig, io, s, flags);
+    return cudaGetLastError();
+  }
   const int blocks = (io.B + kWarpsPerBlock - 1) / kWarpsPerBlock;
   const int smem = kWarpsPerBlock * finish_warp_f4(lig.L, lig.nrb) * (int)sizeof(float4);
   if (smem > 48 * 1024) {
