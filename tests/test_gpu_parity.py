@@ -315,6 +315,12 @@ def test_edge_max_ligand_and_two_slices(oracle, scorer_factory):
     assert_energy(E, E64, scale)
     assert_grad(G, G64)
     assert np.array_equal(st, st64)
+    # one pose per call: the one-pose finishing CTA at its largest shared memory
+    for b in (0, 7):
+        E1, G1, st1 = s.score_poses(d[b:b + 1], grad=True)
+        assert_energy(E1, E64[b:b + 1], scale[b:b + 1])
+        assert_grad(G1, G64[b:b + 1])
+        assert st1[0] == st64[b]
 
 
 def test_edge_rigid_ligand_and_tiny_pocket(oracle, scorer_factory):
