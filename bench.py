@@ -16,7 +16,12 @@ analytic gradient with respect to the 6 rigid-body and 8 torsion DOFs
   device's measured FP32 FMA rate.
 * ``cpu_baseline``: the FP64 CPU restatement of the reference path timed on
   the host cores, energy plus central-difference gradient as the reference
-  computes it (src/lds.ml:1118-1136).
+  computes it (src/lds.ml:1118-1136); ``legs`` adds the same on one thread,
+  the brute L x P sum and the analytic gradient.
+* ``errors``: every pose of the step against the FP64 oracle (energy relative
+  error, gradient per-component error).
+* ``energy_only_65536``: the 65,536-pose energy-only batch on the same
+  system, with its own roofline and errors on 4,096 sampled poses.
 
 ``--impl reference`` times only that CPU path (the reference itself is OCaml
 and cannot be built here) and prints its own line.
@@ -55,6 +60,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=0,
                     help="poses in the CPU-baseline sample (0: about 10 s of work)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-energy-only", action="store_true",
+                    help="skip the 65,536-pose energy-only measurement of the main workload")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the default launch plan instead of the autotuner's")
     ap.add_argument("--workload", default="poses",
@@ -132,18 +139,26 @@ def system_for_rank(rank: int, poses: int):
     return s
 
 
-def cpu_baseline(system, sample: int, nthreads: int, gpu_E=None):
-    """The oracle (FP64 restatement of the reference path), energy + central
-    differences with the reference's steps (0.1 A, 1 degree), 12 A cell
-    neighbour sum; returns (poses/s, seconds, sample, max rel E error vs GPU)."""
+FD_EPS_NOTE = "central differences with the reference's steps, 0.1 A / 1 deg (lds.ml:1118-1136)"
+
+
+def _fd_eps(nd):
+    return np.array([0.1] * 3 + [np.pi / 180.0] * (nd - 3))
+
+
+def cpu_baseline(system, sample: int, nthreads: int, gpu_E=None, use_cells=True, mode=2):
+    """The oracle (FP64 restatement of the reference path) on `sample` poses:
+    energy + central differences with the reference's steps (mode 2, 29
+    scorings per pose) or + the analytic gradient (mode 1); the 12 A cell
+    neighbour sum (the BST query of mol.ml:939) or the brute L x P sum.
+    Returns (poses/s, seconds, sample, max rel E error vs GPU)."""
     from oracle import oracle as O
 
     nd = 6 + system.ligand.nrb
-    eps = np.array([0.1] * 3 + [np.pi / 180.0] * (nd - 3))
     d = system.poses[:sample]
     t0 = time.perf_counter()
-    E, _, _ = O.score_batch(system.pocket, system.ligand, d, mode=2, eps=eps, use_cells=True,
-                            nthreads=nthreads)
+    E, _, _ = O.score_batch(system.pocket, system.ligand, d, mode=mode, eps=_fd_eps(nd),
+                            use_cells=use_cells, nthreads=nthreads)
     dt = time.perf_counter() - t0
     err = None
     if gpu_E is not None:
@@ -152,17 +167,70 @@ def cpu_baseline(system, sample: int, nthreads: int, gpu_E=None):
     return sample / dt, dt, err
 
 
-def calibrate_sample(system, nthreads: int, target_s=10.0) -> int:
+def calibrate_sample(system, nthreads: int, target_s=10.0, use_cells=True, mode=2) -> int:
     from oracle import oracle as O
 
     nd = 6 + system.ligand.nrb
-    eps = np.array([0.1] * 3 + [np.pi / 180.0] * (nd - 3))
-    n0 = max(nthreads, 8)
+    n0 = max(nthreads, 4)
     t0 = time.perf_counter()
-    O.score_batch(system.pocket, system.ligand, system.poses[:n0], mode=2, eps=eps,
-                  use_cells=True, nthreads=nthreads)
+    O.score_batch(system.pocket, system.ligand, system.poses[:n0], mode=mode, eps=_fd_eps(nd),
+                  use_cells=use_cells, nthreads=nthreads)
     per = (time.perf_counter() - t0) / n0
     return int(max(n0, min(len(system.poses), target_s / max(per, 1e-9))))
+
+
+def cpu_legs(system, nthreads: int, gpu_E, target_s=10.0):
+    """The CPU baselines: the reference's method (energy + central
+    differences, cell-list sum) on all host threads (the headline CPU
+    figure), the same on one thread (the shape of the reference's own
+    per-process loop), the brute L x P sum on all threads, and the analytic
+    FP64 gradient on all threads.  Each is a bounded sample of the poses."""
+    legs = {}
+    for name, threads, cells, mode in (("all_threads", nthreads, True, 2),
+                                       ("single_thread", 1, True, 2),
+                                       ("brute_all_threads", nthreads, False, 2),
+                                       ("analytic_all_threads", nthreads, False, 1)):
+        n = calibrate_sample(system, threads, target_s, cells, mode)
+        v, dt, err = cpu_baseline(system, n, threads, gpu_E, cells, mode)
+        legs[name] = {"value": v, "unit": "poses/s", "cores": threads, "sample_poses": n,
+                      "seconds": dt,
+                      "inter_sum": "12 A cell list" if cells else "brute L x P",
+                      "gradient": FD_EPS_NOTE if mode == 2 else "analytic FP64 (reverse mode)",
+                      "max_rel_err_E_gpu_vs_fp64": err}
+    return legs
+
+
+def errors_vs_oracle(system, E, G, nthreads: int, poses=None):
+    """The GPU results against the FP64 oracle on the given poses, under the
+    scoring contract: energies |E - E64| / |E64| (cancellation cases, where
+    S = sum over pairs of w (|elec| + D p12 + 2 D p6) exceeds 100 |E64|, are
+    reported apart), gradient components |G - G64| / max(|G64|, 0.01 GA)
+    with GA the per-component sum of |terms| (orc_grad_scale), and the plain
+    per-component relative error."""
+    from oracle import oracle as O
+
+    d = system.poses if poses is None else system.poses[poses]
+    E = np.asarray(E, np.float64)
+    mode = 1 if G is not None else 0
+    E64, G64, _ = O.score_batch(system.pocket, system.ligand, d, mode=mode, nthreads=nthreads)
+    S, GA, _ = O.score_batch(system.pocket, system.ligand, d, mode=3, nthreads=nthreads)
+    rel = np.abs(E - E64) / np.abs(E64)
+    cancel = S > 100.0 * np.abs(E64)
+    out = {"poses": int(len(d)),
+           "max_rel_err_E": float(rel[~cancel].max()) if (~cancel).any() else None,
+           "max_err_E_cond": float((np.abs(E - E64) / np.maximum(np.abs(E64), S)).max()),
+           "cancellation_poses": int(np.count_nonzero(cancel)),
+           "tolerance_E": 1e-5}
+    if G is not None:
+        dG = np.abs(np.asarray(G, np.float64) - G64)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            plain = np.where(dG == 0, 0.0, dG / np.abs(G64))
+        out.update({"max_rel_err_G": float((dG / np.maximum(np.abs(G64), 0.01 * GA)).max()),
+                    "max_rel_err_G_plain": float(plain.max()),
+                    "frac_G_components_plain_within_1e-4": float(np.mean(plain <= 1e-4)),
+                    "tolerance_G": 1e-4,
+                    "G_rule": "per component, relative to max(|G64_k|, 0.01 GA_k)"})
+    return out
 
 
 def run_reference(args):
@@ -173,21 +241,33 @@ def run_reference(args):
     s = system_for_rank(0, args.poses)
     # about two minutes of CPU work over all the timed steps
     budget = 120.0 / max(args.steps, 1)
-    sample = args.cpu_sample or min(args.poses, calibrate_sample(s, nthreads, target_s=budget))
+    # the brute L x P sum (the reference's -ff BrL, mol.ml:822-849): on this
+    # pocket it is faster than the 12 A cell list standing in for -ff Bst
+    sample = args.cpu_sample or min(args.poses, calibrate_sample(s, nthreads, target_s=budget,
+                                                                 use_cells=False))
     times = []
     for _ in range(max(args.warmup, 0) and 1):
-        cpu_baseline(s, min(sample, nthreads), nthreads)
+        cpu_baseline(s, min(sample, nthreads), nthreads, use_cells=False)
     for _ in range(args.steps):
-        _, dt, _ = cpu_baseline(s, sample, nthreads)
+        _, dt, _ = cpu_baseline(s, sample, nthreads, use_cells=False)
         times.append(dt)
     v = sample * len(times) / sum(times)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "poses/s", "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "poses_per_step": sample,
-                       "gradient": "central differences, 0.1 A / 1 deg (lds.ml:1118-1136)",
-                       "inter_sum": "12 A cell-list neighbour sum (the BST query of mol.ml:939)"},
+            "config": {"workload": WORKLOAD, "poses_per_step_per_gpu": args.poses,
+                       "ligand_atoms": s.ligand.n, "torsions": s.ligand.nrb,
+                       "pocket_atoms": s.pocket.n,
+                       "precision": "fp64 (the reference computes in OCaml floats)",
+                       "parallelism": "host threads over poses (the reference forks workers)"},
+            "sampling": {"poses_scored_per_step": sample,
+                         "note": "each step scores a bounded sample of the step's %d poses; "
+                                 "value = poses scored / seconds" % args.poses,
+                         "gradient": FD_EPS_NOTE,
+                         "inter_sum": "brute L x P with the 12 A switch (-ff BrL, "
+                                      "mol.ml:822-849; faster here than the 12 A cell list "
+                                      "that stands in for the BST query of -ff Bst)"},
             "cpu_baseline": {"value": v, "unit": "poses/s", "cores": nthreads, "kind": "port",
                              "sample": "%d poses per step of the 4096-pose workload" % sample},
             "e2e": {"value": v, "unit": "poses/s", "h2d_bytes_per_step": 0,
@@ -743,6 +823,84 @@ def run_dock(args):
     return 0
 
 
+def energy_only_batch(args, torch, sc, L, dev, stream, flush):
+    """65,536 poses of inter + intra energy (no gradient) per step, on the
+    4,096-pose workload's ligand and pocket: device-resident poses/s (L2
+    flushed before every step), end to end through mmo_score_poses with
+    page-locked host buffers, and the sweep's roofline at 26 flops per
+    counted pair.  The autotuner picks this batch's plan first."""
+    from mmo_gb300 import synth
+
+    big = synth.pose_batch(n_poses=65536, seed=1)
+    B = len(big.poses)
+    sp = stream.cuda_stream
+    d_dofs = torch.from_numpy(big.poses).to(dev)
+    d_E = torch.empty(B, dtype=torch.float64, device=dev)
+    d_st = torch.empty(B, dtype=torch.int32, device=dev)
+    flags = L.F_INTER | L.F_INTRA
+
+    def step():
+        sc.score_poses_device(d_dofs.data_ptr(), B, d_E.data_ptr(), None, d_st.data_ptr(),
+                              flags, sp)
+
+    tune_ms = None
+    if not args.no_tune:
+        tune_ms = sc.tune_device(d_dofs.data_ptr(), B, d_E.data_ptr(), None, d_st.data_ptr(),
+                                 flags, sp)
+    for _ in range(3):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    steps = max(5, min(args.steps, 40))
+    sc.set_profiling(True)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    sweep_ms = []
+    for a, b in ev:
+        flush.zero_()
+        a.record(stream)
+        step()
+        b.record(stream)
+        sweep_ms.append(sc.stage_times()[1])
+    torch.cuda.synchronize()
+    sc.set_profiling(False)
+    pairs_ev, pairs_all = sc.pair_count()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    E = d_E.cpu().numpy()
+    h_dofs = torch.from_numpy(big.poses).pin_memory()
+    h_out = (torch.empty(B, dtype=torch.float64).pin_memory().numpy(), None,
+             torch.empty(B, dtype=torch.int32).pin_memory().numpy())
+    e2e = []
+    for k in range(3 + min(steps, 10)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        sc.score_poses(h_dofs.numpy(), grad=False, out=h_out)
+        if k >= 3:
+            e2e.append(time.perf_counter() - t)
+    peak = sc.fp32_peak_tflops()
+    sweep = float(np.mean(sweep_ms))
+    achieved = FLOPS_PAIR_E * pairs_ev / (sweep * 1e-3) * 1e-12
+    return {"metric": "poses/s (energy: inter + intra, no gradient)",
+            "value": B * steps / (sum(ms) * 1e-3), "unit": "poses/s",
+            "ms_per_step": sum(ms) / steps, "steps": steps,
+            "config": {"workload": "energy only, 65536 poses/step, 48-atom ligand (8 torsions) "
+                                   "vs 6000-atom pocket, the same system as the main line",
+                       "poses_per_step_per_gpu": B, "l2": "flushed before every timed step",
+                       "plan": dict(sc.plan(), tuned_ms=tune_ms)},
+            "e2e": {"value": B * len(e2e) / sum(e2e), "unit": "poses/s",
+                    "h2d_bytes_per_step": int(big.poses.nbytes),
+                    "d2h_bytes_per_step": int(B * 8 + B * 4)},
+            "roofline": {"bound": "fp32", "kernel": "k_pairs_cull (cut-off pair sweep, energy)",
+                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "flops_per_pair": FLOPS_PAIR_E,
+                         "pairs_evaluated": pairs_ev, "pairs_all": pairs_all,
+                         "ms_per_launch": sweep,
+                         "peak_source": "measured FP32 FMA probe on this GPU"},
+            "status_bits_set": int(np.count_nonzero(d_st.cpu().numpy())),
+            "E": E, "system": big}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -839,6 +997,7 @@ def main():
         tot_ms = float(t.item())
     value = world * B * args.steps / (tot_ms * 1e-3)
     E_gpu = d_E.cpu().numpy()
+    G_gpu = d_G.cpu().numpy()
     st = d_st.cpu().numpy()
 
     # ---- end to end through the C ABI with host buffers -------------------
@@ -885,6 +1044,11 @@ def main():
     plain_e2e_ms = (time.perf_counter() - t) * 1e3
     plain_v = n_plain / (plain_dev_ms * 1e-3)
     plain_e2e = n_plain / (plain_e2e_ms * 1e-3)
+
+    # ---- the 65,536-pose energy-only batch (same ligand and pocket) ----------
+    cfg1 = None
+    if not args.no_energy_only:
+        cfg1 = energy_only_batch(args, torch, sc, L, dev, stream, flush)
 
     # ---- roofline of the pair sweep -----------------------------------------
     peak = sc.fp32_peak_tflops()
@@ -939,12 +1103,30 @@ def main():
     }
     if rank == 0 and not args.no_cpu:
         nthreads = os.cpu_count() or 1
-        sample = args.cpu_sample or calibrate_sample(s, nthreads)
-        v, dt, err = cpu_baseline(s, sample, nthreads, gpu_E=E_gpu)
-        line["cpu_baseline"] = {"value": v, "unit": "poses/s", "cores": nthreads, "kind": "port",
+        legs = cpu_legs(s, nthreads, E_gpu)
+        # the faster of the two sums on all host threads (both are the
+        # reference's: -ff BrL brute, -ff Bst through its 12 A neighbour query)
+        key = max(("all_threads", "brute_all_threads"), key=lambda k: legs[k]["value"])
+        main = legs[key]
+        line["cpu_baseline"] = {"value": main["value"], "unit": "poses/s", "cores": nthreads,
+                                "kind": "port",
                                 "sample": "%d of the 4096 poses, %.1f s, energy + central "
-                                          "differences (29 scorings/pose)" % (sample, dt),
-                                "max_rel_err_E_gpu_vs_fp64": err}
+                                          "differences (29 scorings/pose), %s"
+                                          % (main["sample_poses"], main["seconds"],
+                                             main["inter_sum"]),
+                                "max_rel_err_E_gpu_vs_fp64": main["max_rel_err_E_gpu_vs_fp64"],
+                                "legs": legs}
+        # every pose of the step against the FP64 oracle (energy and gradient)
+        line["errors"] = errors_vs_oracle(s, E_gpu, G_gpu, nthreads)
+        if cfg1 is not None:
+            idx = np.random.default_rng(7).choice(len(cfg1["E"]), 4096, replace=False)
+            cfg1_sys = cfg1.pop("system")
+            cfg1["errors"] = errors_vs_oracle(cfg1_sys, cfg1.pop("E")[idx], None, nthreads,
+                                              poses=idx)
+    if cfg1 is not None:
+        cfg1.pop("E", None)
+        cfg1.pop("system", None)
+        line["energy_only_65536"] = cfg1
     if rank == 0:
         print(json.dumps(line), flush=True)
     sc.close()

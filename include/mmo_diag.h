@@ -46,6 +46,17 @@ int mmo_fp32_fma_peak(mmo_ctx* ctx, double* tflops, double* ms);
 int mmo_grid_build_stats(const mmo_ctx* ctx, double* points, double* pairs_evaluated,
                          double* pairs_within_cutoff);
 
+/* Failure-path check of the device-side waits (no counterpart in the
+ * reference).  The sweep kernels wait for their TMA copies into shared memory
+ * on an mbarrier with a bounded number of polls; a wait that gives up sets a
+ * device-side error flag that mmo_sync reports as MMO_ETIMEOUT, and the CTA
+ * then waits once more, with the default bound, for the copy in flight before
+ * it returns, so that nothing is left waiting.  This sets the poll limit of
+ * the first wait of every later launch: 0 makes it give up at once (the
+ * copies still land during the second wait); polls < 0 restores the default
+ * (2^22).  Results of a call whose wait gave up are not valid. */
+int mmo_diag_set_wait_polls(mmo_ctx* ctx, long long polls);
+
 #ifdef __cplusplus
 }
 #endif

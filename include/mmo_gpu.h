@@ -132,15 +132,15 @@ int mmo_score_poses_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, 
 
 /* Allocation-free variant of mmo_score_poses_device (no counterpart in the
  * reference).  For callers that cannot allocate device memory while they
- * score: code that runs inside a CUDA stream capture, real-time loops that may
- * not stall on the allocator, and hosts whose device memory is owned by
- * another allocator (a framework's caching allocator or a fixed arena).  The
+ * score: real-time loops that may not stall on the allocator, and hosts whose
+ * device memory is owned by another allocator (a framework's caching
+ * allocator, or a fixed arena reserved up front).  The
  * caller passes every input and output as device pointers; the call's work
  * buffers come from a static 32 MiB device array that every GPU loading this
  * library holds until the process exits, so this function calls no cudaMalloc
  * or cudaFree.  It always runs the full pair sweep (not the cut-off sweep of
  * mmo_set_cull, whose work buffers are larger).  A call needs 32*B*L bytes,
- * with MMO_F_GRAD another 16*B*L + 48*B*nrb + 16*B, and 8*B*L (24*B*L with
+ * with MMO_F_GRAD another 32*B*L + 48*B*nrb + 32*B, and 8*B*L (24*B*L with
  * MMO_F_GRAD) per protein chunk; a batch that does not fit with one chunk
  * per shared-memory slice of the protein is rejected with MMO_EINVAL and a
  * message naming the sizes (4,096 poses of a 48-atom ligand fit, with the

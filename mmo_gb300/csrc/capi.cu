@@ -157,6 +157,7 @@ struct mmo_ctx {
   Scratch scr{};
   size_t capX = 0, capE = 0, capG = 0, capI = 0, capY = 0, capR = 0;
   int* d_err = nullptr;
+  uint32_t first_wait_polls = kWaitPollsDefault;  // mmo_diag_set_wait_polls
 
   // stage timing (mmo_set_profiling): start, rebuilt, sorted, swept, finished
   bool profiling = false;
@@ -298,12 +299,12 @@ int ensure_scratch(mmo_ctx* ctx, int B, int L, int C, bool grad) {
     return r;
   if (grad) {
     const size_t nrb = std::max(1, ctx->lig.nrb);
-    if ((r = grow(ctx, (void**)&ctx->scr.Y, &ctx->capY, sizeof(float4) * (size_t)B * L, "Y")))
+    if ((r = grow(ctx, (void**)&ctx->scr.Y, &ctx->capY, sizeof(float4) * 2 * (size_t)B * L, "Y")))
       return r;
     if ((r = grow(ctx, (void**)&ctx->scr.rec, &ctx->capR, sizeof(float4) * 3 * (size_t)B * nrb,
                   "torsion records")))
       return r;
-    if ((r = grow(ctx, (void**)&ctx->scr.cen, &ctx->capI, sizeof(float4) * (size_t)B, "centroids")))
+    if ((r = grow(ctx, (void**)&ctx->scr.cen, &ctx->capI, sizeof(float4) * 2 * (size_t)B, "centroids")))
       return r;
   }
   ctx->scr.C = C;
@@ -1075,6 +1076,8 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
   io.oz = ctx->origin_f[2];
   int fl = flags & (kFlagInter | kFlagIntra | kFlagGrad | kFlagRecenter);
   if (!inter) fl &= ~kFlagInter;
+  ctx->scr.first_wait_polls = ctx->first_wait_polls;
+  ctx->cs.first_wait_polls = ctx->first_wait_polls;
   const bool prof = ctx->profiling;
   auto mark = [&](int k) { return prof ? cudaEventRecord(ctx->ev[k], st) : cudaSuccess; };
   MMO_CK(mark(0), "event");
@@ -1476,9 +1479,9 @@ int sys_scratch(mmo_ctx* ctx, SysBatch* S, bool grad, bool inter) {
   if ((r = grow(ctx, (void**)&S->scr.Epart, &S->capE, sizeof(double) * E, "Epart"))) return r;
   if (grad) {
     if ((r = grow(ctx, (void**)&S->scr.Gpart, &S->capG, sizeof(float4) * E, "Gpart"))) return r;
-    if ((r = grow(ctx, (void**)&S->scr.Y, &S->capY, sizeof(float4) * E, "Y"))) return r;
+    if ((r = grow(ctx, (void**)&S->scr.Y, &S->capY, sizeof(float4) * 2 * E, "Y"))) return r;
     if ((r = grow(ctx, (void**)&S->scr.rec, &S->capR, sizeof(float4) * 3 * R, "records"))) return r;
-    if ((r = grow(ctx, (void**)&S->scr.cen, &S->capC, sizeof(float4) * B, "centroids"))) return r;
+    if ((r = grow(ctx, (void**)&S->scr.cen, &S->capC, sizeof(float4) * 2 * B, "centroids"))) return r;
   }
   S->scr.C = 1;
   if (inter) {
@@ -1540,6 +1543,7 @@ int score_systems(mmo_ctx* ctx, const float* d_dofs, int flags, double* d_E, flo
     MMO_CK(cudaMemsetAsync(ctx->d_queue, 0, 16, st), "work counter reset");
     MMO_CK(launch_sys_sort(S->dev, S->scr, S->cs, S->sort_smem, st), "system sort kernel");
     MMO_CK(mark(2), "event");
+    S->cs.first_wait_polls = ctx->first_wait_polls;
     MMO_CK(launch_sys_pairs(S->dev, ctx->d_tab4, S->cs, S->kp, S->threads, S->blocks, S->smem,
                             fl, ctx->ph, d_err, st),
            "system pair kernel");
@@ -2503,6 +2507,15 @@ int mmo_pair_count(mmo_ctx* ctx, double* evaluated, double* all) {
     MMO_CK(cudaMemcpy(&n, ctx->d_queue + 2, sizeof n, cudaMemcpyDeviceToHost), "pair count");
     *evaluated = (double)n;
   }
+  return MMO_OK;
+}
+
+int mmo_diag_set_wait_polls(mmo_ctx* ctx, long long polls) {
+  if (!ctx) return MMO_EINVAL;
+  if (polls > 0xffffffffLL)
+    return fail(ctx, MMO_EINVAL, "mmo_diag_set_wait_polls: %lld polls above 2^32 - 1", polls);
+  ctx->first_wait_polls = polls < 0 ? kWaitPollsDefault : (uint32_t)polls;
+  ++ctx->epoch;  // graphs captured with the old limit are rebuilt
   return MMO_OK;
 }
 
@@ -3589,11 +3602,12 @@ extern "C" int mmo_score_poses_noalloc(mmo_ctx* ctx, int B, const float* d_dofs,
   const bool grad = flags & MMO_F_GRAD;
   const bool inter = use_grid || ((flags & MMO_F_INTER) && ctx->prot.P > 0);
   const int L = ctx->lig.L;
-  // scratch layout: X[B][L][2] | (gradient: Y[B][L] | rec[B][nrb][3] | cen[B]) |
+  // scratch layout: X[B][L][2] | (gradient: Y[B][L][2] | rec[B][nrb][3] | cen[B][2]) |
   // Epart[B][C][L] | (gradient: Gpart[B][C][L])
   const size_t nrb = std::max(1, ctx->lig.nrb);
   const size_t fixed = 256 * 6 + sizeof(float4) * 2 * (size_t)B * L +
-                       (grad ? sizeof(float4) * ((size_t)B * L + 3 * (size_t)B * nrb + B) : 0);
+                       (grad ? sizeof(float4) * (2 * (size_t)B * L + 3 * (size_t)B * nrb + 2 * B)
+                             : 0);
   const size_t per_chunk = (sizeof(double) + (grad ? sizeof(float4) : 0)) * (size_t)B * L;
   const int nslices = inter && !use_grid ? (ctx->prot.P + kSliceAtoms - 1) / kSliceAtoms : 1;
   const long c_fit = fixed < kNoAllocBytes ? (long)((kNoAllocBytes - fixed) / per_chunk) : 0;
@@ -3625,11 +3639,11 @@ extern "C" int mmo_score_poses_noalloc(mmo_ctx* ctx, int B, const float* d_dofs,
   s.X = reinterpret_cast<float4*>(base + take(off, sizeof(float4) * 2 * (size_t)B * L));
   off = (off + 255) & ~size_t(255);
   if (grad) {
-    s.Y = reinterpret_cast<float4*>(base + take(off, sizeof(float4) * (size_t)B * L));
+    s.Y = reinterpret_cast<float4*>(base + take(off, sizeof(float4) * 2 * (size_t)B * L));
     off = (off + 255) & ~size_t(255);
     s.rec = reinterpret_cast<float4*>(base + take(off, sizeof(float4) * 3 * (size_t)B * nrb));
     off = (off + 255) & ~size_t(255);
-    s.cen = reinterpret_cast<float4*>(base + take(off, sizeof(float4) * (size_t)B));
+    s.cen = reinterpret_cast<float4*>(base + take(off, sizeof(float4) * 2 * (size_t)B));
     off = (off + 255) & ~size_t(255);
   }
   s.Epart = reinterpret_cast<double*>(base + take(off, sizeof(double) * (size_t)B * C * L));

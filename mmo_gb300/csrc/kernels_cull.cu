@@ -22,7 +22,7 @@
 namespace mmo {
 namespace {
 
-constexpr uint32_t kWaitPolls = 1u << 22;
+constexpr uint32_t kWaitPolls = kWaitPollsDefault;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kListCap = 64;  // a warp's list: under 32 left over plus one window of 32
 constexpr int kTabRows = kNullTypeRow + 1;  // protein types of the shared pair table
@@ -435,7 +435,9 @@ __global__ void __launch_bounds__(cull_max_threads(KP))
   for (int k = threadIdx.x; k <= npieces; k += blockDim.x) s_piece[k] = cs.piece_row[k];
   stage_pair_table<DIEL>(tabv, s_tab);
   __syncthreads();
-  if (!mbar_wait(&bar, 0, kWaitPolls)) {
+  if (!mbar_wait(&bar, 0, cs.first_wait_polls)) {
+    // the copy did not land in time: flag it, wait once more (bounded) for the
+    // copy in flight so that it does not write into a finished CTA, and stop
     if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
     mbar_wait(&bar, 0, kWaitPolls);
     return;
@@ -579,7 +581,7 @@ __global__ void __launch_bounds__(cull_max_threads(KP), 1)
       s_flush[k] = S.flush_end[pc.z + k] - pc.z;
     }
     if (threadIdx.x == 0) s_rs[nr] = na;
-    if (threadIdx.x == 0 && !mbar_wait(&bar, phase, kWaitPolls)) {
+    if (threadIdx.x == 0 && !mbar_wait(&bar, phase, cs.first_wait_polls)) {
       atomicOr(err, kErrTimeout);
       mbar_wait(&bar, phase, kWaitPolls);
       s_fail = 1;

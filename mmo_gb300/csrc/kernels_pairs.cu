@@ -20,7 +20,7 @@ namespace mmo {
 namespace {
 
 constexpr int kFlush = 256;  // protein atoms per FP32 partial before the FP64 add
-constexpr uint32_t kWaitPolls = 1u << 22;
+constexpr uint32_t kWaitPolls = kWaitPollsDefault;
 
 // dE/dX of one pose for the protein atoms [c0, c1) with the per-pair test
 // of the 0.01 A clamp (rarely needed, so kept out of the main loop's registers)
@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(512)
     }
   }
   __syncthreads();
-  if (!mbar_wait(&bar, 0, kWaitPolls)) {
+  if (!mbar_wait(&bar, 0, scr.first_wait_polls)) {
     // the copy did not land: flag it, give the copy one more bounded wait so
     // that it is not left writing into a finished CTA, and stop
     if (threadIdx.x == 0) atomicOr(err, kErrTimeout);

@@ -204,7 +204,7 @@ __device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof
       float4* r = reco + (size_t)t * 3;
       r[0] = make_float4(cx.x, cy.x, cz.x, cs.x);
       r[1] = make_float4(ux.x, uy.x, uz.x, sn.x);
-      r[2] = make_float4(inv.x, 0.f, 0.f, 0.f);
+      r[2] = make_float4(inv.x, cx.y, cy.y, cz.y);  // 1 / |a| and the centre's lo part
     }
     __syncwarp();  // the rotated group is visible before the next axis is read
   }
@@ -255,10 +255,16 @@ __device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof
       store_pair(Xo + (size_t)a * 2, ddot3c(G[0], vx, G[1], vy, G[2], vz, G[9]),
                  ddot3c(G[3], vx, G[4], vy, G[5], vz, G[10]),
                  ddot3c(G[6], vx, G[7], vy, G[8], vz, G[11]));
-      if (RECORD) Yo[a] = make_float4(AT(X, a).x, AT(Yc, a).x, AT(Zc, a).x, 0.f);
+      if (RECORD) {  // hi and lo parts: the reverse pass takes its lever arms from them
+        Yo[2 * a] = make_float4(AT(X, a).x, AT(Yc, a).x, AT(Zc, a).x, 0.f);
+        Yo[2 * a + 1] = make_float4(AT(X, a).y, AT(Yc, a).y, AT(Zc, a).y, 0.f);
+      }
     }
     if (sub == 0) {
-      if (RECORD) *ceno = make_float4(mx.x, my.x, mz.x, 0.f);
+      if (RECORD) {
+        ceno[0] = make_float4(mx.x, my.x, mz.x, 0.f);
+        ceno[1] = make_float4(mx.y, my.y, mz.y, 0.f);
+      }
       *statuso = status;
     }
   }
@@ -274,8 +280,8 @@ __global__ void __launch_bounds__(kRebuildThreads) k_rebuild(DevLigand lig, Pose
   const int L = lig.L, nrb = lig.nrb, nd = 6 + nrb;
   rebuild_pose<RECENTER, RECORD, TPP>(
       lig, io.dofs + bb * nd, live, io.ox, io.oy, io.oz, scr.X + bb * L * 2,
-      RECORD ? scr.Y + bb * L : nullptr, RECORD ? scr.rec + bb * nrb * 3 : nullptr,
-      RECORD ? scr.cen + bb : nullptr, io.status + bb);
+      RECORD ? scr.Y + bb * L * 2 : nullptr, RECORD ? scr.rec + bb * nrb * 3 : nullptr,
+      RECORD ? scr.cen + bb * 2 : nullptr, io.status + bb);
   if (live && b == 0 && threadIdx.x % TPP == 0 && io.zero_err) *io.err = 0;
 }
 
@@ -300,10 +306,12 @@ __device__ __forceinline__ void axis_angle(float ux, float uy, float uz, float c
 template <int DIEL, int IFORM>
 __device__ __forceinline__ float intra_pair_g(const float4* sh, const float4* sl, int i, int j,
                                               float4 par, float& e, float& dx, float& dy,
-                                              float& dz, float4& ih, float4& jh) {
+                                              float& dz, float4& ih, float4& jh, float4& il,
+                                              float4& jl) {
   ih = sh[i];
   jh = sh[j];
-  const float4 il = sl[i], jl = sl[j];
+  il = sl[i];
+  jl = sl[j];
   dx = split_diff(ih.x, il.x, jh.x, jl.x);
   dy = split_diff(ih.y, il.y, jh.y, jl.y);
   dz = split_diff(ih.z, il.z, jh.z, jl.z);
@@ -320,7 +328,8 @@ __host__ __device__ constexpr int finish_warp_f4(int L, int nrb) {
 }
 
 // Final axis w_t and centre C_t of torsion t from the posed coordinates:
-// saxis[t] = w_t, saxis[nrb + t] = C_t.
+// saxis[t] = (w_t, index of the centre atom as int bits), saxis[nrb + t] = C_t
+// (hi part).
 __device__ __forceinline__ void torsion_frame(const DevLigand& lig, const float4* sxh,
                                               const float4* sxl, float4* saxis, int t) {
   const int nrb = lig.nrb;
@@ -330,7 +339,7 @@ __device__ __forceinline__ void torsion_frame(const DevLigand& lig, const float4
   const float ax = split_diff(rh.x, rl.x, lh.x, ll.x), ay = split_diff(rh.y, rl.y, lh.y, ll.y),
               az = split_diff(rh.z, rl.z, lh.z, ll.z);
   const float inv = rsqrtf(ax * ax + ay * ay + az * az);
-  saxis[t] = make_float4(ax * inv, ay * inv, az * inv, 0.f);
+  saxis[t] = make_float4(ax * inv, ay * inv, az * inv, __int_as_float(bd.y));
   saxis[nrb + t] = rh;
 }
 
@@ -346,8 +355,9 @@ __device__ __forceinline__ void intra_pair_terms(const DevLigand& lig, const flo
   const int2 ij = lig.pair_ij[p];
   const float4 par = lig.pair_par[p];
   float ep, dx, dy, dz;
-  float4 ih, jh;
-  const float g = intra_pair_g<DIEL, IFORM>(sxh, sxl, ij.x, ij.y, par, ep, dx, dy, dz, ih, jh);
+  float4 ih, jh, il, jl;
+  const float g =
+      intra_pair_g<DIEL, IFORM>(sxh, sxl, ij.x, ij.y, par, ep, dx, dy, dz, ih, jh, il, jl);
   acc += ep;
   uint32_t x = __float_as_uint(par.w);  // the torsions the pair straddles
   if (crossing && x) {
@@ -356,9 +366,15 @@ __device__ __forceinline__ void intra_pair_terms(const DevLigand& lig, const flo
       const int t = __ffs(x) - 1;
       x &= x - 1;
       const bool in_i = (mi >> t) & 1u;
-      const float4 w = saxis[t], cc = saxis[nrb + t];
-      const float4 m = in_i ? ih : jh;
-      const float lx = m.x - cc.x, ly = m.y - cc.y, lz = m.z - cc.z;
+      // the lever X_moving - C_t from the hi/lo pairs: the hi parts alone
+      // carry about 1e-6 A of rounding, which the cancelling terms amplify
+      const float4 w = saxis[t];
+      const int ci = __float_as_int(w.w);
+      const float4 ch = sxh[ci], cl = sxl[ci];
+      const float4 mh = in_i ? ih : jh, ml = in_i ? il : jl;
+      const float lx = split_diff(mh.x, ml.x, ch.x, cl.x);
+      const float ly = split_diff(mh.y, ml.y, ch.y, cl.y);
+      const float lz = split_diff(mh.z, ml.z, ch.z, cl.z);
       const float v = dx * (w.y * lz - w.z * ly) + dy * (w.z * lx - w.x * lz) +
                       dz * (w.x * ly - w.y * lx);
       col[t * stride] = fmaf(in_i ? g : -g, v, col[t * stride]);
@@ -457,17 +473,23 @@ __device__ __noinline__ void finish_pose(const DevLigand& lig, int C, const doub
       }
     }
   }
-  // coordinates after the torsions (recorded by k_rebuild)
+  // coordinates after the torsions (recorded by k_rebuild): hi parts in
+  // registers, lo parts in the warp's shared memory (the slot of the posed
+  // coordinates' lo parts, which nothing reads from here on)
+  float4* swl = sxl;
+  __syncwarp();  // every lane is done with the posed coordinates
   float zx[kSlots], zy[kSlots], zz[kSlots];
 #pragma unroll
   for (int s = 0; s < kSlots; ++s) {
     const int a = lane + 32 * s;
-    const float4 y = a < L ? Yb[a] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 y = a < L ? Yb[2 * a] : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a < L) swl[a] = Yb[2 * a + 1];
     zx[s] = y.x;
     zy[s] = y.y;
     zz[s] = y.z;
   }
-  const float4 cen = RECENTER ? *cenp : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 cen = RECENTER ? cenp[0] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 cenl = RECENTER ? cenp[1] : make_float4(0.f, 0.f, 0.f, 0.f);
   float sa, ca, sb, cb, sg, cg;
   sincosf(dof[3], &sa, &ca);
   sincosf(dof[4], &sb, &cb);
@@ -482,7 +504,10 @@ __device__ __noinline__ void finish_pose(const DevLigand& lig, int C, const doub
 #pragma unroll
   for (int s = 0; s < kSlots; ++s) {
     if (lane + 32 * s < L) {
-      const float yx = zx[s] - cen.x, yy = zy[s] - cen.y, yz = zz[s] - cen.z;
+      const float4 w = swl[lane + 32 * s];
+      const float yx = split_diff(zx[s], w.x, cen.x, cenl.x);
+      const float yy = split_diff(zy[s], w.y, cen.y, cenl.y);
+      const float yz = split_diff(zz[s], w.z, cen.z, cenl.z);
       red[0] += gx[s];
       red[1] += gy[s];
       red[2] += gz[s];
@@ -560,8 +585,8 @@ __device__ __noinline__ void finish_pose(const DevLigand& lig, int C, const doub
   // reverse through the torsions, undoing each rotation on the way back
   __syncwarp();  // the prefetched torsion records
   for (int t = nrb - 1; t >= 0; --t) {
-    const float4 r0 = srec[3 * t], r1 = srec[3 * t + 1];
-    const float ilen = srec[3 * t + 2].x;
+    const float4 r0 = srec[3 * t], r1 = srec[3 * t + 1], r2 = srec[3 * t + 2];
+    const float ilen = r2.x;  // r2.yzw: the lo part of the centre r0.xyz
     float Rt[9];
     axis_angle(r1.x, r1.y, r1.z, r0.w, r1.w, Rt);
     float q[10];
@@ -571,7 +596,12 @@ __device__ __noinline__ void finish_pose(const DevLigand& lig, int C, const doub
     for (int s = 0; s < kSlots; ++s) {
       if (32 * s >= L) break;  // uniform: no atoms in this slot
       if ((lig.gmask[t * kSlots + s] >> lane) & 1u) {
-        const float px = zx[s] - r0.x, py = zy[s] - r0.y, pz = zz[s] - r0.z;  // v'
+        // v' = z - c from the hi/lo pairs (the hi parts alone carry the
+        // rounding of coordinates far from the origin into the lever arms)
+        const float4 w = swl[lane + 32 * s];
+        const float px = split_diff(zx[s], w.x, r0.x, r2.y);
+        const float py = split_diff(zy[s], w.y, r0.y, r2.z);
+        const float pz = split_diff(zz[s], w.z, r0.z, r2.w);
         const float vx = Rt[0] * px + Rt[3] * py + Rt[6] * pz;                // v = R^T v'
         const float vy = Rt[1] * px + Rt[4] * py + Rt[7] * pz;
         const float vz = Rt[2] * px + Rt[5] * py + Rt[8] * pz;
@@ -594,9 +624,12 @@ __device__ __noinline__ void finish_pose(const DevLigand& lig, int C, const doub
         ax[s] = Rt[0] * Ax + Rt[3] * Ay + Rt[6] * Az;
         ay[s] = Rt[1] * Ax + Rt[4] * Ay + Rt[7] * Az;
         az[s] = Rt[2] * Ax + Rt[5] * Ay + Rt[8] * Az;
-        zx[s] = vx + r0.x;
-        zy[s] = vy + r0.y;
-        zz[s] = vz + r0.z;
+        // z = c + v as a hi/lo pair
+        float4 nw = make_float4(0.f, 0.f, 0.f, 0.f);
+        dadd_into(r0.x, r2.y, vx, zx[s], nw.x);
+        dadd_into(r0.y, r2.z, vy, zy[s], nw.y);
+        dadd_into(r0.z, r2.w, vz, zz[s], nw.z);
+        swl[lane + 32 * s] = nw;
       }
     }
 #pragma unroll
@@ -649,8 +682,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kFinishBlocksPerSM)
   const size_t ent = (size_t)b * L;
   finish_pose<GRAD, RECENTER, DIEL, IFORM>(
       lig, C, scr.Epart + ent * C, GRAD ? scr.Gpart + ent * C : nullptr, scr.X + ent * 2,
-      GRAD ? scr.Y + ent : nullptr, GRAD ? scr.rec + (size_t)b * nrb * 3 : nullptr,
-      GRAD ? scr.cen + b : nullptr, io.dofs + (size_t)b * nd,
+      GRAD ? scr.Y + ent * 2 : nullptr, GRAD ? scr.rec + (size_t)b * nrb * 3 : nullptr,
+      GRAD ? scr.cen + b * 2 : nullptr, io.dofs + (size_t)b * nd,
       GRAD ? io.grad + (size_t)b * nd : nullptr, io.E + b, io.status + b, flags,
       fsm + wib * finish_warp_f4(L, nrb));
 }
@@ -811,8 +844,8 @@ __global__ void __launch_bounds__(kRebuildThreads)
   const size_t rec = (size_t)inf.rec0 + (size_t)lp * nrb;
   rebuild_pose<RECENTER, RECORD, TPP>(
       slig, io.dofs + (size_t)inf.dof0 + (size_t)lp * (6 + nrb), live, inf.ox, inf.oy, inf.oz,
-      scr.X + ent * 2, RECORD ? scr.Y + ent : nullptr, RECORD ? scr.rec + rec * 3 : nullptr,
-      RECORD ? scr.cen + b : nullptr, io.status + b);
+      scr.X + ent * 2, RECORD ? scr.Y + ent * 2 : nullptr, RECORD ? scr.rec + rec * 3 : nullptr,
+      RECORD ? scr.cen + b * 2 : nullptr, io.status + b);
 }
 
 template <bool GRAD, bool RECENTER, int DIEL, int IFORM>
@@ -832,8 +865,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kFinishBlocksPerSM)
   const size_t rec = (size_t)inf.rec0 + (size_t)lp * nrb, dof = (size_t)inf.dof0 + (size_t)lp * (6 + nrb);
   finish_pose<GRAD, RECENTER, DIEL, IFORM>(
       slig, 1, scr.Epart + ent, GRAD ? scr.Gpart + ent : nullptr, scr.X + ent * 2,
-      GRAD ? scr.Y + ent : nullptr, GRAD ? scr.rec + rec * 3 : nullptr,
-      GRAD ? scr.cen + b : nullptr, io.dofs + dof, GRAD ? io.grad + dof : nullptr, io.E + b,
+      GRAD ? scr.Y + ent * 2 : nullptr, GRAD ? scr.rec + rec * 3 : nullptr,
+      GRAD ? scr.cen + b * 2 : nullptr, io.dofs + dof, GRAD ? io.grad + dof : nullptr, io.E + b,
       io.status + b, flags, fsm + wib * finish_warp_f4(S.Lmax, S.nrbmax));
 }
 

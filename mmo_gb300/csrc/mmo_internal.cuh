@@ -76,14 +76,24 @@ struct DevLigand {
 
 // Per-pose work buffers, pose-major so the warp-per-pose kernels read them
 // contiguously.  C = protein chunks per pose.
+// Polls of a bounded mbarrier wait on a TMA copy.  The first wait of a sweep
+// kernel takes its limit from the launch (first_wait_polls, this value unless
+// mmo_diag_set_wait_polls changed it); a wait that gives up sets kErrTimeout,
+// and the kernel then waits once more with this limit for the copy in flight
+// before its CTA returns.
+constexpr uint32_t kWaitPollsDefault = 1u << 22;
+
 struct Scratch {
   float4* X;       // [B][L][2] posed coordinates in the device frame, hi then lo
   double* Epart;   // [B][C][L] inter energy partial per chunk and ligand atom
   float4* Gpart;   // [B][C][L] dE/dX partial per chunk and ligand atom
-  float4* Y;       // [B][L] coordinates after the torsions, before the rigid map (gradient only)
-  float4* rec;     // [B][nrb][3] torsion records (c, cos), (u, sin), (1/|a|) (gradient only)
-  float4* cen;     // [B] centroid of Y (gradient only)
+  float4* Y;       // [B][L][2] coordinates after the torsions, before the rigid map, hi then
+                   // lo (gradient only)
+  float4* rec;     // [B][nrb][3] torsion records (c hi, cos), (u, sin), (1/|a|, c lo)
+                   // (gradient only)
+  float4* cen;     // [B][2] centroid of Y, hi then lo (gradient only)
   int C;
+  uint32_t first_wait_polls = kWaitPollsDefault;  // polls of the full sweep's first TMA wait
 };
 
 struct PoseIO {
@@ -179,6 +189,7 @@ struct CullScratch {
   const int* seg_of_atom;  // [L] ligand atom -> type segment
   const int* piece_row;  // [npieces + 1] first row of each protein piece
   int slots, npieces;
+  uint32_t first_wait_polls = kWaitPollsDefault;  // polls of the sweep's first TMA wait
 };
 
 // threads per CTA of the cut-off sweep: the register budget of KP entries per
@@ -494,6 +505,17 @@ __device__ __forceinline__ double u01(uint32_t a, uint32_t b) {
 // pair difference a - b of two hi/lo coordinate pairs
 __device__ __forceinline__ float split_diff(float ah, float al, float bh, float bl) {
   return (ah - bh) + (al - bl);
+}
+
+// (hi, lo) = (ch + cl) + v as a normalised float pair: TwoSum of ch and v
+// (Knuth), the low parts added, then Fast2Sum
+__device__ __forceinline__ void dadd_into(float ch, float cl, float v, float& hi, float& lo) {
+  const float s = ch + v;
+  const float bb = s - ch;
+  const float e = (ch - (s - bb)) + (v - bb);
+  const float t = e + cl;
+  hi = s + t;
+  lo = t - (hi - s);
 }
 
 // One UFF nonbonded pair, FP32.  d = ligand - partner.  FORM 0: shifted by

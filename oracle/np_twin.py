@@ -28,8 +28,9 @@ def pair_energy(r, qq, xij, dij, w, dielectric=0):
 
 def ene_inter(pxyz, pq, panum, lxyz, lq, lanum, shifted=True, mixing=0, dielectric=0,
               absolute=False):
-    """Sum of pair energies, or of their absolute values (absolute=True, the
-    conditioning scale used by the parity tests)."""
+    """Sum of pair energies, or of the absolute values of their parts
+    (absolute=True: w (|elec| + D (x/r)^12 + 2 D (x/r)^6), the conditioning
+    scale used by the parity tests)."""
     xp, dp = params(panum)
     xl, dl = params(lanum)
     d = np.linalg.norm(pxyz[:, None, :] - lxyz[None, :, :], axis=2)
@@ -43,7 +44,7 @@ def ene_inter(pxyz, pq, panum, lxyz, lq, lanum, shifted=True, mixing=0, dielectr
     e = pair_energy(r, pq[:, None] * lq[None, :], xij, dij, w, dielectric)
     if absolute:
         e = np.abs(w * ELEC * (pq[:, None] * lq[None, :]) / (r if dielectric == 0 else r * r)) + \
-            np.abs(w * dij * ((xij / r) ** 12 - 2.0 * (xij / r) ** 6))
+            np.abs(w * dij) * ((xij / r) ** 12 + 2.0 * (xij / r) ** 6)
     return float(e.sum())
 
 
@@ -58,7 +59,7 @@ def ene_intra(lxyz, lq, lanum, interacting, dielectric=0, absolute=False):
     if absolute:
         p6 = (xij / r) ** 6
         return float((np.abs(ELEC * qq / (r if dielectric == 0 else r * r)) +
-                      np.abs(dij * (p6 * p6 - 2.0 * p6))).sum())
+                      np.abs(dij) * (p6 * p6 + 2.0 * p6)).sum())
     return float(pair_energy(r, qq, xij, dij, np.ones_like(r), dielectric).sum())
 
 

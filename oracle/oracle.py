@@ -87,6 +87,7 @@ def lib():
                                 P(d)]),
             "orc_grad_analytic": (d, [P(Physics), P(CMol), P(CLigand), P(d), i, P(d), P(d),
                                       P(i)]),
+            "orc_grad_scale": (d, [P(Physics), P(CMol), P(CLigand), P(d), i, P(d)]),
             "orc_score_batch": (v, [P(Physics), P(CMol), P(CLigand), i, P(C.c_float), i, i,
                                     P(d), i, i, P(d), P(d), P(i)]),
             "orc_grid_point": (v, [P(Physics), P(CMol), P(d), i, P(i), P(d), d, P(d)]),
@@ -273,9 +274,21 @@ def grad_analytic(prot, lig, conf, flags=F_INTER | F_INTRA, ph=REF, want_xyz=Fal
     return e, g, st.value
 
 
+def grad_scale(prot, lig, conf, flags=F_INTER | F_INTRA, ph=REF):
+    """(S, grad_abs): the condition scales of the energy and of each analytic
+    gradient component of one configuration (orc_grad_scale)."""
+    p, L = OMol.of(prot), OLigand(lig)
+    conf = np.ascontiguousarray(conf, np.float64)
+    g = np.zeros_like(conf)
+    S = lib().orc_grad_scale(C.byref(ph), C.byref(p.c), C.byref(L.c), _dp(conf), flags, _dp(g))
+    return S, g
+
+
 def score_batch(prot, lig, dofs, flags=F_INTER | F_INTRA, mode=0, eps=None, use_cells=False,
                 nthreads=1, ph=REF):
-    """mode 0: energy; 1: + analytic gradient; 2: + central differences."""
+    """mode 0: energy; 1: + analytic gradient; 2: + central differences;
+    3: condition scales (E = sum of |pair energies|, G = per-component sums of
+    |terms| of the analytic gradient)."""
     p, L = OMol.of(prot), OLigand(lig)
     dofs = np.ascontiguousarray(dofs, np.float32)
     B, nd = dofs.shape

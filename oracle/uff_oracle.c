@@ -487,6 +487,36 @@ static double pair_energy_grad(int dielectric, int shifted, double r2, double qq
   return dEdr / r; /* dE/dd = (dE/dr) d / r */
 }
 
+/* the same pair term with every part taken by its absolute value:
+ * *e_out = w (|el| + D p6^2 + 2 D p6) and the return value bounds |dE/dd| / r
+ * by the same split of the derivative's parts */
+static double pair_energy_grad_abs(int dielectric, int shifted, double r2, double qqK,
+                                   double x_ij, double d_ij, double *e_out) {
+  double r = sqrt(r2);
+  int clamped = r < 0.01;
+  if (clamped) r = 0.01;
+  double w = 1.0, dw = 0.0;
+  if (shifted) {
+    double t = r / 12.0, s = 1.0 - t * t;
+    w = s * s;
+    dw = fabs(2.0 * s * (-2.0 * r / 144.0));
+  }
+  double p6 = pow6(x_ij / r);
+  double lj = fabs(d_ij) * (p6 * p6 + 2.0 * p6);
+  double dlj = fabs(d_ij) * (12.0 * p6 * p6 / r + 12.0 * p6 / r);
+  double el, del;
+  if (dielectric == 1) {
+    el = fabs(qqK) / (r * r);
+    del = 2.0 * fabs(qqK) / (r * r * r);
+  } else {
+    el = fabs(qqK) / r;
+    del = fabs(qqK) / (r * r);
+  }
+  *e_out = w * (lj + el);
+  if (clamped) return 0.0;
+  return (dw * (lj + el) + w * (dlj + del)) / r;
+}
+
 /* analytic reverse-mode gradient; see uff_oracle.h */
 double orc_grad_analytic(const orc_physics *ph, const orc_mol *prot, const orc_ligand *lig,
                          const double *conf, int flags, double *grad, double *gxyz,
@@ -628,6 +658,161 @@ double orc_grad_analytic(const orc_physics *ph, const orc_mol *prot, const orc_l
   return E;
 }
 
+/* ---- condition scales of the energy and of each gradient component --------
+ * The same forward pass and reverse pass as orc_grad_analytic, with every sum
+ * of terms replaced by the sum of their absolute values and every product by
+ * the product of absolute values (|a x b| by the componentwise bound
+ * |a_y||b_z| + |a_z||b_y|, a matrix by its entrywise absolute value), and each
+ * pair term split into its parts (elec, the two LJ powers, the switch).  The
+ * energy scale is S = sum over pairs of w (|elec| + D (x/r)^12 + 2 D (x/r)^6);
+ * grad_abs[k] bounds the sum of |terms| that the analytic gradient adds into
+ * component k.  A floating-point evaluation of the same sums with unit
+ * round-off u is accurate to about u * scale, whatever the cancellation. */
+static void abs3(const double a[3], double o[3]) {
+  o[0] = fabs(a[0]);
+  o[1] = fabs(a[1]);
+  o[2] = fabs(a[2]);
+}
+static void cross_abs(const double a[3], const double b[3], double c[3]) {
+  c[0] = fabs(a[1] * b[2]) + fabs(a[2] * b[1]);
+  c[1] = fabs(a[2] * b[0]) + fabs(a[0] * b[2]);
+  c[2] = fabs(a[0] * b[1]) + fabs(a[1] * b[0]);
+}
+static double dot_abs(const double a[3], const double b[3]) {
+  return fabs(a[0] * b[0]) + fabs(a[1] * b[1]) + fabs(a[2] * b[2]);
+}
+
+double orc_grad_scale(const orc_physics *ph, const orc_mol *prot, const orc_ligand *lig,
+                      const double *conf, int flags, double *grad_abs) {
+  int n = lig->m.n, nrb = lig->nrb;
+  double K = orc_elec_weight();
+  double *snap = (double *)malloc(sizeof(double) * 3 * n * (nrb + 1) + 1);
+  memcpy(snap, lig->m.x, sizeof(double) * n);
+  memcpy(snap + n, lig->m.y, sizeof(double) * n);
+  memcpy(snap + 2 * n, lig->m.z, sizeof(double) * n);
+  for (int t = 0; t < nrb; ++t) {
+    double *px = snap + 3 * n * t, *nx = snap + 3 * n * (t + 1);
+    memcpy(nx, px, sizeof(double) * 3 * n);
+    orc_rotate_bond(n, nx, nx + n, nx + 2 * n, lig->bond_lr[2 * t], lig->bond_lr[2 * t + 1],
+                    lig->grp_atoms + lig->grp_off[t], lig->grp_off[t + 1] - lig->grp_off[t],
+                    conf[6 + t]);
+  }
+  double *Y = snap + 3 * n * nrb;
+  double R[9], Ra[9], ctr[3] = {0, 0, 0};
+  orc_rot_xyz(conf[3], conf[4], conf[5], R);
+  for (int e = 0; e < 9; ++e) Ra[e] = fabs(R[e]);
+  if (flags & ORC_F_RECENTER) centroid(n, Y, Y + n, Y + 2 * n, ctr);
+  double *X = (double *)malloc(sizeof(double) * 3 * n + 1);
+  double *Yc = (double *)malloc(sizeof(double) * 3 * n + 1);
+  double *G = (double *)calloc(3 * n + 1, sizeof(double));
+  for (int i = 0; i < n; ++i) {
+    double v[3] = {Y[i] - ctr[0], Y[n + i] - ctr[1], Y[2 * n + i] - ctr[2]}, w[3];
+    for (int d = 0; d < 3; ++d) Yc[3 * i + d] = fabs(v[d]);
+    matvec(R, v, w);
+    for (int d = 0; d < 3; ++d) X[3 * i + d] = w[d] + conf[d];
+  }
+  double S = 0.0;
+  if (flags & ORC_F_INTER) {
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < prot->n; ++i) {
+        double d[3] = {X[3 * j] - prot->x[i], X[3 * j + 1] - prot->y[i],
+                       X[3 * j + 2] - prot->z[i]};
+        double r2 = dot(d, d);
+        if (ph->inter_form == 0 && !(r2 < 144.0)) continue;
+        double x_ij, d_ij, e;
+        orc_pair_params(ph, prot->anum[i], lig->m.anum[j], &x_ij, &d_ij);
+        double g = pair_energy_grad_abs(ph->dielectric, ph->inter_form == 0, r2,
+                                        K * prot->q[i] * lig->m.q[j], x_ij, d_ij, &e);
+        S += e;
+        for (int k = 0; k < 3; ++k) G[3 * j + k] += g * fabs(d[k]);
+      }
+  }
+  if (flags & ORC_F_INTRA) {
+    for (int i = 0; i < n - 1; ++i)
+      for (int j = i + 1; j < n; ++j) {
+        if (!lig->interacting[i * n + j]) continue;
+        double d[3] = {X[3 * i] - X[3 * j], X[3 * i + 1] - X[3 * j + 1],
+                       X[3 * i + 2] - X[3 * j + 2]};
+        double r2 = dot(d, d);
+        int shifted = ph->intra_form == 1;
+        if (shifted && !(orc_non_zero_dist(sqrt(r2)) < 12.0)) continue;
+        double x_ij, d_ij, e;
+        orc_pair_params(ph, lig->m.anum[i], lig->m.anum[j], &x_ij, &d_ij);
+        double g = pair_energy_grad_abs(ph->dielectric, shifted, r2,
+                                        K * lig->m.q[i] * lig->m.q[j], x_ij, d_ij, &e);
+        S += e;
+        for (int k = 0; k < 3; ++k) {
+          G[3 * i + k] += g * fabs(d[k]);
+          G[3 * j + k] += g * fabs(d[k]);
+        }
+      }
+  }
+  double dA[9], dB[9], dG[9], M[9] = {0};
+  rot_xyz_derivs(conf[3], conf[4], conf[5], dA, dB, dG);
+  grad_abs[0] = grad_abs[1] = grad_abs[2] = 0.0;
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) {
+      grad_abs[k] += G[3 * i + k];
+      for (int l = 0; l < 3; ++l) M[3 * k + l] += G[3 * i + k] * Yc[3 * i + l];
+    }
+  grad_abs[3] = grad_abs[4] = grad_abs[5] = 0.0;
+  for (int e = 0; e < 9; ++e) {
+    grad_abs[3] += M[e] * fabs(dA[e]);
+    grad_abs[4] += M[e] * fabs(dB[e]);
+    grad_abs[5] += M[e] * fabs(dG[e]);
+  }
+  double *A = (double *)malloc(sizeof(double) * 3 * n + 1);
+  double mean[3] = {0, 0, 0};
+  for (int i = 0; i < n; ++i) {
+    matTvec(Ra, G + 3 * i, A + 3 * i);
+    for (int k = 0; k < 3; ++k) mean[k] += A[3 * i + k];
+  }
+  if (flags & ORC_F_RECENTER)
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < 3; ++k) A[3 * i + k] += mean[k] / n;
+  for (int t = nrb - 1; t >= 0; --t) {
+    const double *pre = snap + 3 * n * t, *post = snap + 3 * n * (t + 1);
+    int left = lig->bond_lr[2 * t], right = lig->bond_lr[2 * t + 1];
+    double c[3], a[3], u[3], alen, Rt[9], ua[3];
+    bond_axis(pre, pre + n, pre + 2 * n, left, right, c, a, u, &alen);
+    double th = conf[6 + t], ct = fabs(1.0 - cos(th)), stt = fabs(sin(th));
+    orc_rot_axis_angle(u, th, Rt);
+    for (int e = 0; e < 9; ++e) Rt[e] = fabs(Rt[e]);
+    abs3(u, ua);
+    double dth = 0.0, dU[3] = {0, 0, 0}, dC[3] = {0, 0, 0};
+    for (int k = lig->grp_off[t]; k < lig->grp_off[t + 1]; ++k) {
+      int i = lig->grp_atoms[k];
+      double vp[3] = {post[i] - c[0], post[n + i] - c[1], post[2 * n + i] - c[2]};
+      double v[3] = {pre[i] - c[0], pre[n + i] - c[1], pre[2 * n + i] - c[2]}, va[3];
+      double *Ai = A + 3 * i, uxv[3], vxA[3], RtA[3];
+      abs3(v, va);
+      cross_abs(u, vp, uxv);
+      dth += dot_abs(Ai, uxv);
+      cross_abs(v, Ai, vxA);
+      double uv = dot_abs(u, v), Au = dot_abs(Ai, u);
+      for (int d = 0; d < 3; ++d) dU[d] += stt * vxA[d] + ct * (uv * Ai[d] + Au * va[d]);
+      matTvec(Rt, Ai, RtA);
+      for (int d = 0; d < 3; ++d) {
+        dC[d] += Ai[d] + RtA[d];
+        Ai[d] = RtA[d];
+      }
+    }
+    grad_abs[6 + t] = dth;
+    double uu = dot_abs(ua, dU);
+    for (int d = 0; d < 3; ++d) {
+      double da = (dU[d] + ua[d] * uu) / alen;
+      A[3 * right + d] += da + dC[d];
+      A[3 * left + d] += da;
+    }
+  }
+  free(A);
+  free(G);
+  free(Yc);
+  free(X);
+  free(snap);
+  return S;
+}
+
 /* ---- batch over poses on host threads ------------------------------------ */
 typedef struct {
   const orc_physics *ph;
@@ -650,6 +835,8 @@ static void *batch_worker(void *arg) {
     double *g = j->grad ? j->grad + (size_t)b * j->nd : NULL;
     if (j->mode == 1 && g) {
       j->E[b] = orc_grad_analytic(j->ph, j->prot, j->lig, conf, j->flags, g, NULL, &st);
+    } else if (j->mode == 3 && g) {
+      j->E[b] = orc_grad_scale(j->ph, j->prot, j->lig, conf, j->flags, g);
     } else {
       j->E[b] = orc_score_conf(j->ph, j->prot, j->cells, j->lig, conf, j->flags, &st);
       if (j->mode == 2 && g) orc_grad_fd(j->ph, j->prot, j->cells, j->lig, conf, j->flags, j->eps, g);

@@ -116,10 +116,19 @@ double orc_grad_analytic(const orc_physics *ph, const orc_mol *prot, const orc_l
                          const double *conf, int flags, double *grad, double *gxyz,
                          int *status);
 
+/* condition scales of one configuration: returns S = sum over pairs of
+ * w (|elec| + D (x/r)^12 + 2 D (x/r)^6) and fills grad_abs[6+nrb] with the sum of |terms| that
+ * orc_grad_analytic adds into each gradient component (pair terms split into
+ * their parts, products and cross products bounded by their absolute values).  An evaluation in a precision with unit round-off u is
+ * accurate to about u times these scales, whatever the cancellation. */
+double orc_grad_scale(const orc_physics *ph, const orc_mol *prot, const orc_ligand *lig,
+                      const double *conf, int flags, double *grad_abs);
+
 /* batch over poses on nthreads host threads.  dofs: B x (6+nrb) float32 (the
  * GPU input format, widened exactly).  mode 0: energy; 1: energy + analytic
  * gradient; 2: energy + central-difference gradient with eps (the reference's
- * method).  use_cells selects the 12 A neighbour form for E_inter. */
+ * method); 3: the condition scales of orc_grad_scale (E gets S, grad gets the
+ * per-component scales).  use_cells selects the 12 A neighbour form for E_inter. */
 void orc_score_batch(const orc_physics *ph, const orc_mol *prot, const orc_ligand *lig,
                      int B, const float *dofs, int flags, int mode, const double *eps,
                      int use_cells, int nthreads, double *E, double *grad, int *status);

@@ -12,9 +12,12 @@ BSD 3-Clause License, Copyright (c) 2024, Francois Berenger):
   charges, so the charges here follow a fixed rule (RULE below: a neutral
   backbone, charged side-chain ends) to give the Coulomb term something to sum.
 
-    python tests/golden/make_ref_data.py [reference root]
+    python tests/golden/make_ref_data.py <MMO checkout>
+    (or MMO_REFERENCE_ROOT=<MMO checkout> python tests/golden/make_ref_data.py)
 
-The outputs are committed; the tests read them and never the reference.
+The outputs are committed; the tests read them and never the reference.  The
+two CPU tests that regenerate them and run the reference's own .pqrs reader
+need MMO_REFERENCE_ROOT and are skipped without it.
 """
 import os
 import sys
@@ -55,10 +58,16 @@ def receptor_from_pdb(path) -> Mol:
                rad)
 
 
-DEFAULT_REF = "/root/reference"
+ENV = "MMO_REFERENCE_ROOT"
 
 
-def main(ref=DEFAULT_REF, out=HERE):
+def reference_root():
+    """The MMO checkout to read the molecules from: the MMO_REFERENCE_ROOT
+    environment variable, or None when it is not set."""
+    return os.environ.get(ENV) or None
+
+
+def main(ref, out=HERE):
     data = os.path.join(ref, "data")
     texts = []
     for fn in LIGANDS:
@@ -71,4 +80,7 @@ def main(ref=DEFAULT_REF, out=HERE):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REF)
+    root = sys.argv[1] if len(sys.argv) > 1 else reference_root()
+    if not root:
+        sys.exit("usage: make_ref_data.py <MMO checkout> (or set %s)" % ENV)
+    main(root)

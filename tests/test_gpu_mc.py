@@ -64,7 +64,7 @@ def test_final_energies_match_fp64_rescore(oracle, scorer_factory, system):
     torch = pytest.importorskip("torch")
     from mmo_gb300 import lib as L
 
-    from test_gpu_parity import assert_energy, ref_batch
+    from contract import assert_ref, ref_batch
 
     sc = scorer_factory(system.pocket, system.ligand)
     d0 = system.poses[:64]
@@ -77,8 +77,7 @@ def test_final_energies_match_fp64_rescore(oracle, scorer_factory, system):
     assert np.array_equal(Er, E)
     Eb, _, _ = sc.score_poses(bd, recenter=True)
     assert np.array_equal(Eb, bE)
-    E64, _, _, scale = ref_batch(oracle, system, d[:16], recenter=True)
-    assert_energy(E[:16], E64, scale)
+    assert_ref(E, None, ref_batch(oracle, system, d, recenter=True))
 
 
 def test_graph_equals_direct_launches(scorer_factory, system):

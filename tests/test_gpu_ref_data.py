@@ -24,7 +24,7 @@ import pytest
 
 from mmo_gb300 import grids as GR
 from mmo_gb300 import synth
-from test_gpu_parity import assert_energy, assert_grad, ref_batch
+from contract import assert_energy, assert_grad, assert_ref, ref_batch
 from test_ref_data import ref_molecules
 
 pytestmark = pytest.mark.gpu
@@ -63,15 +63,12 @@ def test_ref_poses_match_oracle(oracle, scorer_factory, ref, phys, recenter):
         E, G, st = s.score_poses(d, grad=True, recenter=recenter)
         assert np.all(st == 0)
         system = synth.System(lig.name, rec, lig, d)
-        E64, G64, st64, scale = ref_batch(oracle, system, d, grad=True, recenter=recenter,
-                                          ph=oracle.physics(*phys))
-        assert np.array_equal(st, st64)
-        assert_energy(E, E64, scale)
-        assert_grad(G, G64)
+        r = ref_batch(oracle, system, d, grad=True, recenter=recenter, ph=oracle.physics(*phys))
+        assert_ref(E, G, r, st)
         # one pose per call: the plain path
         E1, G1, _ = s.score_poses(d[:1], grad=True, recenter=recenter)
-        assert_energy(E1, E64[:1], scale[:1])
-        assert_grad(G1, G64[:1])
+        assert_energy(E1, r.E[:1], r.S[:1])
+        assert_grad(G1, r.G[:1], r.GA[:1])
     if phys == (0, 0, 0, 0) and not recenter:
         # the docked pose binds: its inter energy is favourable
         s = scorer_factory(rec, ligs[0])
@@ -89,11 +86,11 @@ def test_ref_closures_match_oracle(oracle, gpu_lib, ref):
     for lig in ligs:
         e64 = oracle.ene_inter(rec, lig)
         scale = T.ene_inter(rec.xyz(), rec.q, rec.anum, lig.xyz(), lig.q, lig.anum, absolute=True)
-        assert abs(ff0(lig) - e64) <= 1e-5 * max(abs(e64), scale)
+        assert_energy([ff0(lig)], [e64], [scale])
         intra = ene_intra_builder(lig.centered())
         ei64 = oracle.ene_intra(lig)
         si = T.ene_intra(lig.xyz(), lig.q, lig.anum, lig.interacting, absolute=True)
-        assert abs(intra(lig) - ei64) <= 1e-5 * max(abs(ei64), si)
+        assert_energy([intra(lig)], [ei64], [si])
         intra.scorer.close()
     ff0.scorer.close()
 
@@ -155,6 +152,31 @@ def test_ref_exhaustive_docking_matches_oracle(oracle, scorer_factory, ref):
 
 
 @pytest.mark.parametrize("recenter", [False, True])
+def test_ref_gradient_against_central_differences(oracle, scorer_factory, ref, recenter):
+    """On the reference's complex, the GPU gradient against FP64 central
+    differences with h = 1e-4 A / rad (the step of the benchmark's gradient
+    check), Richardson-extrapolated with h / 2, on every component where the
+    differences are accurate (tests/contract.py fd_check): most of them on
+    these poses, which clash far less than random ones."""
+    from contract import G_TOL, fd_check
+
+    rec, ligs = ref
+    for k, lig in enumerate(ligs):
+        s = scorer_factory(rec, lig)
+        d = _poses(lig, 24, 30 + k, recenter)
+        _, G, st = s.score_poses(d, grad=True, recenter=recenter)
+        assert np.all(st == 0)
+        system = synth.System(lig.name, rec, lig, d)
+        r = ref_batch(oracle, system, d, grad=True, recenter=recenter)
+        flags = oracle.F_INTER | oracle.F_INTRA | (oracle.F_RECENTER if recenter else 0)
+        _, F1, _ = oracle.score_batch(rec, lig, d, flags=flags, mode=2, eps=1e-4, nthreads=16)
+        _, F2, _ = oracle.score_batch(rec, lig, d, flags=flags, mode=2, eps=5e-5, nthreads=16)
+        err, trusted = fd_check(G, F1, F2, r.S, r.GA, 1e-4)
+        assert trusted.mean() >= 0.8, (k, trusted.mean())
+        assert err.max() <= G_TOL, (k, err.max())
+
+
+@pytest.mark.parametrize("recenter", [False, True])
 def test_posed_coordinates_match_oracle(oracle, scorer_factory, ref, recenter):
     """mmo_posed_coords: the pose map's atoms (double-float on the GPU)
     against Optim.apply_config / the MC map in FP64, to 1e-9 A."""
@@ -186,7 +208,7 @@ def test_ff_score_matches_oracle(oracle, gpu_lib, ref, tmp_path, capsys):
     for (_, e), m in zip(res, ligs):
         e64 = oracle.ene_intra(m)
         sc = T.ene_intra(m.xyz(), m.q, m.anum, m.interacting, absolute=True)
-        assert abs(e - e64) <= 1e-5 * max(abs(e64), sc)
+        assert_energy([e], [e64], [sc])
     assert F.main([os.path.join(GOLD, "ref_ligands.pqrs")]) == 0
     out = capsys.readouterr().out.splitlines()
     assert len(out) == 3 and all(len(ln.split("\t")) == 2 for ln in out)
@@ -245,5 +267,4 @@ def test_mc_chains_on_the_real_complex(oracle, scorer_factory, ref):
     Er, _, _ = sc.score_poses(d, recenter=True)
     assert np.array_equal(Er, E)
     system = synth.System(lig.name, rec, lig, d)
-    E64, _, _, scale = ref_batch(oracle, system, d[:12], recenter=True)
-    assert_energy(E[:12], E64, scale)
+    assert_ref(E, None, ref_batch(oracle, system, d, recenter=True))

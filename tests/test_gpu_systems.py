@@ -63,7 +63,7 @@ def test_systems_match_one_system_path(scorer_factory, systems, recenter):
 
 
 def test_systems_against_oracle(oracle, scorer_factory, systems):
-    from test_gpu_parity import assert_energy, assert_grad, ref_batch
+    from contract import assert_ref, ref_batch
 
     sc = scorer_factory()
     sc.set_systems([(s.pocket, s.ligand, len(s.poses)) for s in systems])
@@ -72,18 +72,16 @@ def test_systems_against_oracle(oracle, scorer_factory, systems):
     Es, Gs = _split(E, po), _split(G, do)
     for k in (0, 3, 5, 9):
         s = systems[k]
-        n = min(6, len(s.poses))
-        E64, G64, _, scale = ref_batch(oracle, s, s.poses[:n], grad=True)
-        assert_energy(Es[k][:n], E64, scale)
-        assert_grad(Gs[k].reshape(len(s.poses), -1)[:n], G64)
+        assert_ref(Es[k], Gs[k].reshape(len(s.poses), -1), ref_batch(oracle, s, s.poses,
+                                                                     grad=True))
 
 
 def test_systems_global_form(oracle, scorer_factory, systems):
     """The global form has no cut-off: every protein atom counts, also the
-    ones beyond 12 A of a pose (per pose against the FP64 oracle, whose
-    tolerance is relative to that pose's own sum of |pair energies|)."""
+    ones beyond 12 A of a pose (every pose against the FP64 oracle under the
+    scoring contract)."""
     from mmo_gb300.ff import Physics
-    from test_gpu_parity import assert_energy, assert_grad, ref_batch
+    from contract import assert_ref, ref_batch
 
     sub = [systems[0], systems[3], systems[6]]
     sc = scorer_factory(physics=Physics(1, 0, 1, 0))
@@ -97,11 +95,7 @@ def test_systems_global_form(oracle, scorer_factory, systems):
         g = G[do[k]:do[k + 1]].reshape(G1.shape)
         assert np.abs(e - E1).max() <= 1e-6 * np.abs(E1).max()
         assert (np.abs(g - G1).max(axis=1) / np.abs(G1).max(axis=1)).max() <= 1e-5
-        n = min(6, len(s.poses))
-        E64, G64, _, scale = ref_batch(oracle, s, s.poses[:n], grad=True,
-                                       ph=oracle.physics(1, 0, 1, 0))
-        assert_energy(e[:n], E64, scale)
-        assert_grad(g[:n], G64)
+        assert_ref(e, g, ref_batch(oracle, s, s.poses, grad=True, ph=oracle.physics(1, 0, 1, 0)))
 
 
 def test_systems_graph_replay_and_device_entry(scorer_factory, systems):

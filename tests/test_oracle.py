@@ -183,6 +183,36 @@ def test_gradient_vs_fd_h1e4(oracle):
         assert np.abs(g - gf).max() <= 1e-4 * np.abs(g).max()
 
 
+@pytest.mark.parametrize("flags", [3, 1, 2, 11])
+def test_condition_scales(oracle, flags):
+    """orc_grad_scale: S is the sum over pairs of w (|elec| + D p12 + 2 D p6)
+    (the NumPy twin's absolute sum), S >= |E|, each GA_k bounds |G_k|, and the batch mode
+    returns the same numbers."""
+    from oracle import np_twin as T
+
+    s = synth.pose_batch(n_poses=6, seed=12, n_atoms=20, n_rot=4, n_pocket=400, radius=10.0)
+    S, GA, _ = oracle.score_batch(s.pocket, s.ligand, s.poses, flags=flags, mode=3, nthreads=2)
+    _, G, _ = oracle.score_batch(s.pocket, s.ligand, s.poses, flags=flags, mode=1, nthreads=2)
+    for b, conf in enumerate(s.poses.astype(np.float64)):
+        Sb, gb = oracle.grad_scale(s.pocket, s.ligand, conf, flags=flags)
+        assert Sb == S[b] and np.array_equal(gb, GA[b])
+        xyz, _ = oracle.apply_config(s.ligand, conf, flags & oracle.F_RECENTER)
+        want = 0.0
+        if flags & oracle.F_INTER:
+            p = s.pocket
+            want += T.ene_inter(p.xyz(), p.q, p.anum, xyz, s.ligand.q, s.ligand.anum,
+                                absolute=True)
+        if flags & oracle.F_INTRA:
+            want += T.ene_intra(xyz, s.ligand.q, s.ligand.anum, s.ligand.interacting,
+                                absolute=True)
+        assert Sb == pytest.approx(want, rel=1e-10)
+    E, _, _ = oracle.score_batch(s.pocket, s.ligand, s.poses, flags=flags, mode=0)
+    assert np.all(S >= np.abs(E) * (1 - 1e-12))
+    assert np.all(GA >= np.abs(G) * (1 - 1e-12))
+    if flags == oracle.F_INTRA:  # intra energy is rigid-invariant: G_0..2 = 0, their scale not
+        assert np.all(np.abs(G[:, :3]) <= 1e-9 * GA[:, :3])
+
+
 def test_gradient_physics_variants(oracle):
     s = synth.pose_batch(n_poses=2, seed=9, n_atoms=16, n_rot=3, n_pocket=300, radius=9.0)
     for ph in (oracle.physics(1, 1, 1, 1), oracle.physics(0, 0, 1, 0), oracle.physics(1, 0, 0, 1)):

@@ -44,9 +44,10 @@ def test_fixture_regenerates(tmp_path):
     sys.path.insert(0, GOLD)
     import make_ref_data as G
 
-    if not os.path.isdir(os.path.join(G.DEFAULT_REF, "data")):
+    root = G.reference_root()
+    if not root or not os.path.isdir(os.path.join(root, "data")):
         pytest.skip("the reference's data directory is not on this machine")
-    G.main(G.DEFAULT_REF, str(tmp_path))
+    G.main(root, str(tmp_path))
     for fn in ("ref_ligands.pqrs", "ref_receptor.pqrs"):
         with open(os.path.join(GOLD, fn)) as a, open(os.path.join(tmp_path, fn)) as b:
             assert a.read() == b.read(), fn
@@ -94,7 +95,8 @@ def test_reference_reader_reads_our_pqrs(tmp_path):
     sys.path.insert(0, GOLD)
     import make_ref_data as G
 
-    tool = os.path.join(G.DEFAULT_REF, "bin", "pqrs_center.py")
+    root = G.reference_root()
+    tool = os.path.join(root, "bin", "pqrs_center.py") if root else ""
     if not os.path.isfile(tool):
         pytest.skip("the reference's bin/pqrs_center.py is not on this machine")
     rec, ligs = ref_molecules()
