@@ -1027,7 +1027,8 @@ int check_dev_err(mmo_ctx* ctx, int flag) {
 }
 
 int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E,
-                 float* d_grad, int* d_status, int* d_err, int zero_err, cudaStream_t st) {
+                 float* d_grad, int* d_status, int* d_err, int zero_err, cudaStream_t st,
+                 double* d_E_inter = nullptr) {
   if (!ctx->has_lig) return fail(ctx, MMO_ESTATE, "no ligand: call mmo_set_ligand first");
   const bool use_grid = (flags & MMO_F_INTER) && (flags & MMO_F_GRID);
   if (use_grid && !ctx->grid_map_ok)
@@ -1070,6 +1071,7 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
   io.status = d_status;
   io.err = d_err;
   io.zero_err = zero_err;
+  io.E_inter = d_E_inter;
   io.B = B;
   io.ox = ctx->origin_f[0];
   io.oy = ctx->origin_f[1];
@@ -2275,18 +2277,23 @@ MCDev mc_layout(char* base, int B, int nd, int nrb, size_t* bytes) {
   MCDev s{};
   s.cur = align_ptr<float>(base, off, (size_t)B * nd);
   s.trial = align_ptr<float>(base, off, (size_t)B * nd);
+  s.start = align_ptr<float>(base, off, (size_t)B * 6);
   s.best = align_ptr<float>(base, off, (size_t)B * nd);
   s.G_cur = align_ptr<float>(base, off, (size_t)B * nd);
   s.G_trial = align_ptr<float>(base, off, (size_t)B * nd);
   s.E_cur = align_ptr<double>(base, off, B);
   s.E_trial = align_ptr<double>(base, off, B);
+  s.Ei_trial = align_ptr<double>(base, off, B);
   s.E_best = align_ptr<double>(base, off, B);
   s.st_trial = align_ptr<int>(base, off, B);
   s.moved = align_ptr<int>(base, off, B);
   s.accepted = align_ptr<int>(base, off, B);
+  s.resets = align_ptr<int>(base, off, B);
+  s.stopped = align_ptr<int>(base, off, B);
   s.status_or = align_ptr<int>(base, off, B);
-  s.steps = align_ptr<float>(base, off, (size_t)B * (2 + nrb));
-  s.cnt = align_ptr<int>(base, off, (size_t)B * (kMcCounts + 2 * nrb));
+  s.steps = align_ptr<double>(base, off, (size_t)B * (2 + nrb));
+  s.cnt = align_ptr<int>(base, off, (size_t)B * kMcCounts);
+  s.win = align_ptr<int>(base, off, (size_t)B * (1 + nrb) * kMcWin);
   s.eta = align_ptr<float>(base, off, B);
   *bytes = off;
   return s;
@@ -2300,7 +2307,7 @@ int mc_block(mmo_ctx* ctx, const MCDev& s, const MCParams& p, int nsteps, bool m
   for (int k = 0; k < nsteps; ++k) {
     MMO_CK(launch_k_mc_propose(s, p, st), "MC propose kernel");
     if ((r = score_device(ctx, p.B, s.trial, flags, s.E_trial, nullptr, s.st_trial, ctx->d_err, 0,
-                          st)))
+                          st, s.Ei_trial)))
       return r;
     MMO_CK(launch_k_mc_accept(s, p, st), "MC accept kernel");
   }
@@ -2334,8 +2341,14 @@ int mmo_mc_run(mmo_ctx* ctx, int chains, int steps, const mmo_mc_params* prm,
       !std::isfinite(prm->trans_step) || !std::isfinite(prm->tors_step) ||
       (prm->move_law != MMO_MC_UNIFORM && prm->move_law != MMO_MC_GAUSSIAN) ||
       prm->minimize_every < 0 || prm->minimize_iters < 0 || prm->flip_every < 0 ||
-      !(prm->gd_step >= 0) || !std::isfinite(prm->gd_step))
+      !(prm->gd_step >= 0) || !std::isfinite(prm->gd_step) ||
+      !std::isfinite(prm->roi_radius) || !std::isfinite(prm->roi_center[0]) ||
+      !std::isfinite(prm->roi_center[1]) || !std::isfinite(prm->roi_center[2]))
     return fail(ctx, MMO_EINVAL, "mmo_mc_run: bad parameters");
+  if (steps > 0 && (state->trace_dofs || state->trace_E || state->trace_event) &&
+      (long long)steps * chains > (1LL << 31) / std::max(1, 6 + ctx->lig.nrb))
+    return fail(ctx, MMO_EINVAL, "mmo_mc_run: trace of %d steps x %d chains too large", steps,
+                chains);
   MMO_CK(cudaSetDevice(ctx->device), "set device");
   cudaStream_t us = reinterpret_cast<cudaStream_t>(stream);
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -2350,9 +2363,17 @@ int mmo_mc_run(mmo_ctx* ctx, int chains, int steps, const mmo_mc_params* prm,
   const MCDev s = mc_layout(static_cast<char*>(ctx->d_mc), B, nd, nrb, &bytes);
   MCParams p{};
   p.kT = prm->kT;
-  p.rot = (float)prm->rot_step;
-  p.trans = (float)prm->trans_step;
-  p.tors = (float)prm->tors_step;
+  p.rot = prm->rot_step;
+  p.trans = prm->trans_step;
+  p.tors = prm->tors_step;
+  for (int k = 0; k < 3; ++k) p.roi_c[k] = prm->roi_center[k];
+  p.roi_r = prm->roi_radius;
+  p.reset_zero = prm->reset_on_zero_inter ? 1 : 0;
+  p.too_long_ends = prm->too_long_ends_chain ? 1 : 0;
+  p.trace_steps = (state->trace_dofs || state->trace_E || state->trace_event) ? steps : 0;
+  p.trace_dofs = state->trace_dofs;
+  p.trace_E = state->trace_E;
+  p.trace_event = state->trace_event;
   p.gd_step = (float)prm->gd_step;
   p.law = prm->move_law;
   p.adapt = prm->adapt ? 1 : 0;
@@ -2438,6 +2459,9 @@ int mmo_mc_run(mmo_ctx* ctx, int chains, int steps, const mmo_mc_params* prm,
     if (state->status)
       MMO_CK(cudaMemcpyAsync(state->status, s.status_or, sizeof(int) * B,
                              cudaMemcpyDeviceToDevice, st), "status");
+    if (state->resets)
+      MMO_CK(cudaMemcpyAsync(state->resets, s.resets, sizeof(int) * B, cudaMemcpyDeviceToDevice,
+                             st), "resets");
     return MMO_OK;
   };
   r = body();

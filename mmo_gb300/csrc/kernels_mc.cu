@@ -34,20 +34,52 @@ __device__ __forceinline__ double wrap_pi(double a) {
   return a - kPi;
 }
 
-__device__ __forceinline__ int* chain_counts(const MCDev& s, int nrb, int b) {
-  return s.cnt + (size_t)b * (kMcCounts + 2 * nrb);
+__device__ __forceinline__ int* chain_counts(const MCDev& s, int b) {
+  return s.cnt + (size_t)b * kMcCounts;
 }
+
+// Sliding window of the last kMcBlock accept / reject events (SW.ml:7-37):
+// w[0..3] event bits (a ring), w[4] next slot, w[5] events held, w[6] accepts
+__device__ __forceinline__ int* chain_window(const MCDev& s, int nrb, int b, int k) {
+  return s.win + ((size_t)b * (1 + nrb) + k) * kMcWin;
+}
+
+__device__ __forceinline__ void sw_reset(int* w) {
+  for (int i = 0; i < kMcWin; ++i) w[i] = 0;
+}
+
+// SW.process: the event enters; beyond the window's length the oldest leaves
+__device__ __forceinline__ void sw_process(int* w, bool evt) {
+  const int head = w[4];
+  uint32_t* bits = reinterpret_cast<uint32_t*>(w);
+  const uint32_t m = 1u << (head & 31);
+  if (w[5] == kMcBlock) {  // full: the slot being written holds the oldest event
+    if (bits[head >> 5] & m) w[6] -= 1;
+  } else {
+    w[5] += 1;
+  }
+  bits[head >> 5] = evt ? (bits[head >> 5] | m) : (bits[head >> 5] & ~m);
+  w[6] += evt ? 1 : 0;
+  w[4] = head + 1 == kMcBlock ? 0 : head + 1;
+}
+
+// SW.get_ratio: accepts / events (NaN before the first event)
+__device__ __forceinline__ double sw_ratio(const int* w) { return (double)w[6] / (double)w[5]; }
 
 __global__ void k_mc_init(MCDev s, MCParams p) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= p.B) return;
-  float* st = s.steps + (size_t)b * (2 + p.nrb);
+  double* st = s.steps + (size_t)b * (2 + p.nrb);
   st[0] = p.rot;
   st[1] = p.trans;
   for (int i = 0; i < p.nrb; ++i) st[2 + i] = p.tors;
-  int* c = chain_counts(s, p.nrb, b);
-  for (int i = 0; i < kMcCounts + 2 * p.nrb; ++i) c[i] = 0;
+  int* c = chain_counts(s, b);
+  for (int i = 0; i < kMcCounts; ++i) c[i] = 0;
+  for (int k = 0; k <= p.nrb; ++k) sw_reset(chain_window(s, p.nrb, b, k));
+  for (int k = 0; k < 6; ++k) s.start[(size_t)b * 6 + k] = s.cur[(size_t)b * p.nd + k];
   s.accepted[b] = 0;
+  s.resets[b] = 0;
+  s.stopped[b] = 0;
   s.status_or[b] = 0;
 }
 
@@ -67,12 +99,18 @@ __global__ void k_mc_propose(MCDev s, MCParams p) {
   const float* cur = s.cur + (size_t)b * nd;
   float* tr = s.trial + (size_t)b * nd;
   for (int k = 0; k < nd; ++k) tr[k] = cur[k];
-  int* c = chain_counts(s, nrb, b);
+  const int* c = chain_counts(s, b);
   const int step = c[0];
-  const float* st = s.steps + (size_t)b * (2 + nrb);
+  const double* st = s.steps + (size_t)b * (2 + nrb);
+  const bool rigid = (step & 1) == 0;  // lds.ml:659-660, 883
+  if (s.stopped[b] || (!rigid && nrb == 0)) {
+    // an ended chain stays; a ligand without rotatable bonds makes no
+    // conformer move (its odd frames re-score the same pose, lds.ml:797-798)
+    s.moved[b] = -2;
+    return;
+  }
   const uint4 r0 = philox(make_uint4((uint32_t)b, (uint32_t)step, 0u, 0u), p.key0, p.key1);
   const uint4 r1 = philox(make_uint4((uint32_t)b, (uint32_t)step, 1u, 0u), p.key0, p.key1);
-  const bool rigid = nrb == 0 || (step & 1) == 0;  // lds.ml:659-660, 883
   if (rigid) {
     double ax = 0.0, ay = 0.0, az = 0.0, th, dt[3];
     if (p.law == kMcGaussian) {
@@ -81,29 +119,29 @@ __global__ void k_mc_propose(MCDev s, MCParams p) {
       normal2(u01(r1.x, r1.y), u01(r1.z, r1.w), n[2], n[3]);
       const uint4 r2 = philox(make_uint4((uint32_t)b, (uint32_t)step, 2u, 0u), p.key0, p.key1);
       normal2(u01(r2.x, r2.y), u01(r2.z, r2.w), n[4], n[5]);
-      const double il = rsqrt(fmax(n[0] * n[0] + n[1] * n[1] + n[2] * n[2], 1e-300));
+      const double il = 1.0 / sqrt(fmax(n[0] * n[0] + n[1] * n[1] + n[2] * n[2], 1e-300));
       ax = n[0] * il;  // uniform direction
       ay = n[1] * il;
       az = n[2] * il;
-      th = (double)st[0] * n[3];
-      dt[0] = (double)st[1] * n[4];
-      dt[1] = (double)st[1] * n[5];
+      th = st[0] * n[3];
+      dt[0] = st[1] * n[4];
+      dt[1] = st[1] * n[5];
       const uint4 r3 = philox(make_uint4((uint32_t)b, (uint32_t)step, 3u, 0u), p.key0, p.key1);
       double n6, n7;
       normal2(u01(r3.x, r3.y), u01(r3.z, r3.w), n6, n7);
-      dt[2] = (double)st[1] * n6;
+      dt[2] = st[1] * n6;
     } else {
       // Move.rand_rot: theta in [-dr, dr] about one of Ox, Oy, Oz; Move.rand_trans:
       // a direction in [-1, 1]^3 times dt
-      th = (2.0 * u01(r0.x, r0.y) - 1.0) * (double)st[0];
+      th = (2.0 * u01(r0.x, r0.y) - 1.0) * st[0];
       const int axis = min(2, (int)(u01(r0.z, r0.w) * 3.0));
       ax = axis == 0;
       ay = axis == 1;
       az = axis == 2;
-      dt[0] = (2.0 * u01(r1.x, r1.y) - 1.0) * (double)st[1];
-      dt[1] = (2.0 * u01(r1.z, r1.w) - 1.0) * (double)st[1];
+      dt[0] = (2.0 * u01(r1.x, r1.y) - 1.0) * st[1];
+      dt[1] = (2.0 * u01(r1.z, r1.w) - 1.0) * st[1];
       const uint4 r2 = philox(make_uint4((uint32_t)b, (uint32_t)step, 2u, 0u), p.key0, p.key1);
-      dt[2] = (2.0 * u01(r2.x, r2.y) - 1.0) * (double)st[1];
+      dt[2] = (2.0 * u01(r2.x, r2.y) - 1.0) * st[1];
     }
     // R' = Rm R, Rm = rotation by th about (ax, ay, az) (rot.ml:121-146),
     // R = r_xyz(a, b, g) (rot.ml:52-66)
@@ -135,87 +173,141 @@ __global__ void k_mc_propose(MCDev s, MCParams p) {
     s.moved[b] = -1;
   } else {
     // Mol.tweak_rbond: one bond, an angle in [-dr_i, dr_i] (or a Gaussian
-    // step), every flip_every-th conformer move Mol.flip_rbond in [-pi, pi]
+    // step); Mol.flip_rbond in [-pi, pi] on conformer frames whose count of
+    // earlier conformer frames is a positive multiple of flip_every
+    // (lds.ml:783-793)
     const int i = min(nrb - 1, (int)(u01(r0.x, r0.y) * nrb));
     double d;
     if (p.law == kMcGaussian) {
       double n0, n1;
       normal2(u01(r0.z, r0.w), u01(r1.x, r1.y), n0, n1);
-      d = (double)st[2 + i] * n0;
+      d = st[2 + i] * n0;
     } else {
-      const int confs = c[3];
+      const int confs = c[2];
       const bool flip = p.flip_every > 0 && confs > 0 && confs % p.flip_every == 0;
-      d = (2.0 * u01(r0.z, r0.w) - 1.0) * (flip ? kPi : (double)st[2 + i]);
+      d = (2.0 * u01(r0.z, r0.w) - 1.0) * (flip ? kPi : st[2 + i]);
     }
     tr[6 + i] = (float)wrap_pi((double)cur[6 + i] + d);
     s.moved[b] = i;
   }
 }
 
-// Metropolis: accept when E' <= E or U < exp(-(E' - E) / kT), compared in
-// FP64 (lds.ml:931-934); a trial pose whose status is not clean is rejected.
+// One frame of Lds.simulate_lig after the trial's scoring (lds.ml:906-988):
+//  * hard ROI (roi_r > 0): a trial whose ligand centre (the translation of the
+//    MC pose map) lies farther than roi_r from roi_c resets the chain;
+//  * otherwise, with reset_zero, a trial whose inter energy is exactly 0 (the
+//    ligand left the pocket) resets the chain;
+//  * otherwise Metropolis: accept when E' <= E or U < exp(-(E' - E) / kT),
+//    compared in FP64 (lds.ml:931-934); the event enters the rigid window or
+//    the moved bond's window (SW.ml); a new lowest energy becomes the best
+//    pose; on rigid frames after each 100 rigid frames the rigid steps adapt
+//    to the rigid window's ratio (x0.95 at <= 0.45, x1.05 at >= 0.55, the
+//    angle capped at pi, lds.ml:586-603), on conformer frames after each
+//    100 nrb conformer frames every bond's step adapts to its own window
+//    (lds.ml:606-621) -- kept only when the frame's move was accepted, since
+//    the reference adapts the trial conformer (lds.ml:971-976).
+// A reset (reset_run_params, lds.ml:652-671) puts the rigid part back to the
+// start pose and the rigid steps to their initial values, clears the rigid
+// window and sets the current and best energies to +inf (the next clean
+// trial is accepted); the conformer, the bond steps and the bond windows stay.
+// A trial that is not clean is rejected; an over-long trial conformer
+// (Mol.Too_long, mol.ml:576-591) is rejected, or ends the chain with
+// too_long_ends (the reference's exception leaves the frame loop,
+// lds.ml:989-991).  Rigid trials ignore the over-long bit (the reference
+// checks it on conformer moves only).
 __global__ void k_mc_accept(MCDev s, MCParams p) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= p.B) return;
   const int nd = p.nd, nrb = p.nrb;
-  int* c = chain_counts(s, nrb, b);
+  int* c = chain_counts(s, b);
   const int step = c[0];
+  const int mv = s.moved[b];
+  const bool rigid = (step & 1) == 0;
   const double Et = s.E_trial[b], E0 = s.E_cur[b];
   const int stt = s.st_trial[b];
-  s.status_or[b] |= stt;
-  const bool ok = stt == 0 && isfinite(Et);
-  bool acc = false;
-  if (ok) {
-    if (Et <= E0) {
-      acc = true;
-    } else {
-      const uint4 r = philox(make_uint4((uint32_t)b, (uint32_t)step, 7u, 0u), p.key0, p.key1);
-      acc = u01(r.x, r.y) < exp(-(Et - E0) / p.kT);
-    }
-  }
-  if (acc) {
-    for (int k = 0; k < nd; ++k) s.cur[(size_t)b * nd + k] = s.trial[(size_t)b * nd + k];
-    s.E_cur[b] = Et;
-    s.accepted[b] += 1;
-  }
-  if (ok && Et < s.E_best[b]) {
-    s.E_best[b] = Et;
-    for (int k = 0; k < nd; ++k) s.best[(size_t)b * nd + k] = s.trial[(size_t)b * nd + k];
-  }
-  // step-size adaptation per block of 100 moves (lds.ml:586-621, params.ml:29):
-  // acceptance <= 0.45 scales the step by 0.95, >= 0.55 by 1.05 (angles capped at pi)
-  float* st = s.steps + (size_t)b * (2 + nrb);
-  const int mv = s.moved[b];
-  if (mv < 0) {
-    c[1] += acc;
-    c[2] += 1;
-    if (p.adapt && c[2] % kMcBlock == 0) {
-      const float ratio = (float)c[1] / (float)kMcBlock;
-      if (ratio <= 0.45f) {
-        st[0] *= 0.95f;
-        st[1] *= 0.95f;
-      } else if (ratio >= 0.55f) {
-        st[0] = fminf((float)kPi, st[0] * 1.05f);
-        st[1] *= 1.05f;
-      }
-      c[1] = 0;
-    }
+  float* cur = s.cur + (size_t)b * nd;
+  const float* tr = s.trial + (size_t)b * nd;
+  double* st = s.steps + (size_t)b * (2 + nrb);
+  int event = 0;
+  if (s.stopped[b]) {
+    event = kMcStopped;
   } else {
-    int* bc = c + kMcCounts;
-    bc[2 * mv] += acc;
-    bc[2 * mv + 1] += 1;
-    c[3] += 1;
-    if (p.adapt && c[3] % (kMcBlock * nrb) == 0) {
-      for (int i = 0; i < nrb; ++i) {
-        if (bc[2 * i + 1] > 0) {
-          const float ratio = (float)bc[2 * i] / (float)bc[2 * i + 1];
-          if (ratio <= 0.45f) st[2 + i] *= 0.95f;
-          else if (ratio >= 0.55f) st[2 + i] = fminf((float)kPi, st[2 + i] * 1.05f);
+    s.status_or[b] |= stt;
+    bool reset = false;
+    if (p.roi_r > 0.0) {
+      const double dx = (double)tr[0] - p.roi_c[0], dy = (double)tr[1] - p.roi_c[1],
+                   dz = (double)tr[2] - p.roi_c[2];
+      reset = sqrt(dx * dx + dy * dy + dz * dz) > p.roi_r;
+    }
+    if (!reset && p.reset_zero && s.Ei_trial[b] == 0.0) reset = true;
+    if (reset) {
+      for (int k = 0; k < 6; ++k) cur[k] = s.start[(size_t)b * 6 + k];
+      s.E_cur[b] = __longlong_as_double(0x7ff0000000000000ll);  // +inf
+      s.E_best[b] = __longlong_as_double(0x7ff0000000000000ll);
+      for (int k = 0; k < nd; ++k) s.best[(size_t)b * nd + k] = cur[k];
+      st[0] = p.rot;
+      st[1] = p.trans;
+      sw_reset(chain_window(s, nrb, b, 0));
+      s.resets[b] += 1;
+      event = kMcReset;
+    } else {
+      const bool too_long = mv >= 0 && (stt & kStatusTooLong);
+      const bool blocked = !isfinite(Et) || too_long || (stt & ~kStatusTooLong);
+      if (too_long && p.too_long_ends) {
+        s.stopped[b] = 1;
+        event = kMcStopped;
+      } else {
+        bool acc = false;
+        if (!blocked) {
+          if (Et <= E0) {
+            acc = true;
+          } else {
+            const uint4 r =
+                philox(make_uint4((uint32_t)b, (uint32_t)step, 7u, 0u), p.key0, p.key1);
+            acc = u01(r.x, r.y) < exp(-(Et - E0) / p.kT);
+          }
         }
-        bc[2 * i] = bc[2 * i + 1] = 0;
+        if (mv == -1) sw_process(chain_window(s, nrb, b, 0), acc);
+        else if (mv >= 0) sw_process(chain_window(s, nrb, b, 1 + mv), acc);
+        if (acc) {
+          for (int k = 0; k < nd; ++k) cur[k] = tr[k];
+          s.E_cur[b] = Et;
+          s.accepted[b] += 1;
+        }
+        if (!blocked && Et < s.E_best[b]) {
+          s.E_best[b] = Et;
+          for (int k = 0; k < nd; ++k) s.best[(size_t)b * nd + k] = tr[k];
+        }
+        if (p.adapt && rigid && c[1] > 0 && c[1] % kMcBlock == 0) {
+          const double ratio = sw_ratio(chain_window(s, nrb, b, 0));
+          if (ratio <= 0.45) {
+            st[1] = 0.95 * st[1];
+            st[0] = 0.95 * st[0];
+          } else if (ratio >= 0.55) {
+            st[1] = 1.05 * st[1];
+            st[0] = fmin(kPi, 1.05 * st[0]);
+          }
+        }
+        if (p.adapt && acc && mv >= 0 && c[2] > 0 && c[2] % (kMcBlock * nrb) == 0) {
+          for (int i = 0; i < nrb; ++i) {
+            const double ratio = sw_ratio(chain_window(s, nrb, b, 1 + i));
+            if (ratio <= 0.45) st[2 + i] = 0.95 * st[2 + i];
+            else if (ratio >= 0.55) st[2 + i] = fmin(kPi, 1.05 * st[2 + i]);
+          }
+        }
+        event = (acc ? kMcAccepted : 0) | (blocked ? kMcBlocked : 0);
       }
     }
   }
+  if (step < p.trace_steps) {
+    const size_t o = (size_t)step * p.B + b;
+    if (p.trace_dofs)
+      for (int k = 0; k < nd; ++k) p.trace_dofs[o * nd + k] = tr[k];
+    if (p.trace_E) p.trace_E[o] = Et;
+    if (p.trace_event) p.trace_event[o] = event;
+  }
+  if (rigid) c[1] += 1;
+  else c[2] += 1;
   c[0] = step + 1;
 }
 

@@ -384,6 +384,7 @@ __device__ __forceinline__ void intra_pair_terms(const DevLigand& lig, const flo
 
 // finish_pose: one warp, one pose.  ep / gp: the pose's inter partials
 // [C][L]; Xb, Yb, recb, cenp, dof, grad, Eo, sto: the pose's own slots;
+// Eio, when not null, gets the inter part of the energy;
 // wsm: the warp's shared memory (finish_warp_f4 float4).  pre_dti non-null:
 // the intra energy (pre_e) and the nested groups' torsion terms (pre_dti[t])
 // were summed beforehand (k_finish_one), so the pair loop is skipped.
@@ -393,7 +394,8 @@ __device__ __noinline__ void finish_pose(const DevLigand& lig, int C, const doub
                                             const float4* gp, const float4* Xb, const float4* Yb,
                                             const float4* recb, const float4* cenp,
                                             const float* dof, float* grad, double* Eo, int* sto,
-                                            int flags, float4* wsm, double pre_e = 0.0,
+                                            double* Eio, int flags, float4* wsm,
+                                            double pre_e = 0.0,
                                             const float* pre_dti = nullptr) {
   const bool pre = pre_dti != nullptr;
   const int lane = threadIdx.x & 31;
@@ -433,6 +435,13 @@ __device__ __noinline__ void finish_pose(const DevLigand& lig, int C, const doub
   if (lane == 0) {
     *Eo = e;
     if (!isfinite(e)) *sto |= kStatusNonFinite;
+  }
+  if (Eio) {  // the inter partials alone, in the same order
+    double ei = 0.0;
+    if (inter)
+      for (int k = lane; k < C * L; k += 32) ei += ep[k];
+    ei = warp_sum(ei);
+    if (lane == 0) *Eio = ei;
   }
   if (!GRAD) return;
 
@@ -684,8 +693,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kFinishBlocksPerSM)
       lig, C, scr.Epart + ent * C, GRAD ? scr.Gpart + ent * C : nullptr, scr.X + ent * 2,
       GRAD ? scr.Y + ent * 2 : nullptr, GRAD ? scr.rec + (size_t)b * nrb * 3 : nullptr,
       GRAD ? scr.cen + b * 2 : nullptr, io.dofs + (size_t)b * nd,
-      GRAD ? io.grad + (size_t)b * nd : nullptr, io.E + b, io.status + b, flags,
-      fsm + wib * finish_warp_f4(L, nrb));
+      GRAD ? io.grad + (size_t)b * nd : nullptr, io.E + b, io.status + b,
+      io.E_inter ? io.E_inter + b : nullptr, flags, fsm + wib * finish_warp_f4(L, nrb));
 }
 
 // One pose (the one-pose path): the CTA's threads share the interacting pairs
@@ -746,7 +755,7 @@ __global__ void __launch_bounds__(kFinishOne)
   finish_pose<GRAD, RECENTER, DIEL, IFORM>(
       lig, scr.C, scr.Epart, GRAD ? scr.Gpart : nullptr, scr.X, GRAD ? scr.Y : nullptr,
       GRAD ? scr.rec : nullptr, GRAD ? scr.cen : nullptr, io.dofs, GRAD ? io.grad : nullptr,
-      io.E, io.status, flags, wsm, intra ? sred[kFinishOne / 32] : 0.0, stot);
+      io.E, io.status, io.E_inter, flags, wsm, intra ? sred[kFinishOne / 32] : 0.0, stot);
 }
 
 // one warp: sum of n FP64 partials
@@ -867,7 +876,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kFinishBlocksPerSM)
       slig, 1, scr.Epart + ent, GRAD ? scr.Gpart + ent : nullptr, scr.X + ent * 2,
       GRAD ? scr.Y + ent * 2 : nullptr, GRAD ? scr.rec + rec * 3 : nullptr,
       GRAD ? scr.cen + b * 2 : nullptr, io.dofs + dof, GRAD ? io.grad + dof : nullptr, io.E + b,
-      io.status + b, flags, fsm + wib * finish_warp_f4(S.Lmax, S.nrbmax));
+      io.status + b, nullptr, flags, fsm + wib * finish_warp_f4(S.Lmax, S.nrbmax));
 }
 
 template <bool RC, bool REC>

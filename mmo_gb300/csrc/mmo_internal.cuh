@@ -105,6 +105,7 @@ struct PoseIO {
   int zero_err;       // the rebuild kernel clears *err first
   int B;
   float ox, oy, oz;   // frame origin subtracted from the translation
+  double* E_inter;    // [B] the inter part of E, or null
 };
 
 enum : int { kFlagInter = 1, kFlagIntra = 2, kFlagGrad = 4, kFlagRecenter = 8 };
@@ -252,35 +253,52 @@ struct DevSystems {
 
 // ---- Monte Carlo chains (kernels_mc.cu) ----------------------------------
 enum : int { kMcUniform = 0, kMcGaussian = 1 };
-constexpr int kMcCounts = 4;   // per chain: step, rigid accepted in block, rigid moves, conformer moves
-constexpr int kMcBlock = 100;  // moves per adaptation block (params.ml:29)
+constexpr int kMcCounts = 3;   // per chain: step, rigid frames, conformer frames
+constexpr int kMcBlock = 100;  // adaptation period and sliding-window length (params.ml:29)
+constexpr int kMcWin = 8;      // ints per sliding window: 4 words of event bits, head, length,
+                               // accepts, padding
+// trace events of a step (mmo_mc_state.trace_event)
+enum : int { kMcAccepted = 1, kMcReset = 2, kMcStopped = 4, kMcBlocked = 8 };
 
 struct MCDev {
   float* cur;       // [B][nd] current poses (optimiser layout)
   float* trial;     // [B][nd] proposed poses
+  float* start;     // [B][6] rigid part of the start pose (the reset target)
   double* E_cur;    // [B]
   double* E_trial;  // [B]
+  double* Ei_trial; // [B] inter energy of the trial pose
   float* G_cur;     // [B][nd] gradient at the current pose (minimiser)
   float* G_trial;   // [B][nd]
   int* st_trial;    // [B] status bits of the trial pose
   float* best;      // [B][nd] lowest-energy pose seen
   double* E_best;   // [B]
-  float* steps;     // [B][2 + nrb] rotation (rad), translation (A), per-bond torsion step (rad)
-  int* cnt;         // [B][kMcCounts + 2 nrb] counters, then per bond (accepted, tried) in block
-  int* moved;       // [B] bond of the last conformer move, -1 after a rigid move
+  double* steps;    // [B][2 + nrb] rotation (rad), translation (A), per-bond torsion step (rad)
+  int* cnt;         // [B][kMcCounts] counters
+  int* win;         // [B][1 + nrb][kMcWin] sliding windows: rigid moves, then one per bond
+  int* moved;       // [B] bond of the last conformer move; -1 rigid move, -2 no move
   int* accepted;    // [B] accepted moves
+  int* resets;      // [B] resets (out of the ROI, or E_inter = 0)
+  int* stopped;     // [B] 1: the chain ended (an over-long trial conformer)
   int* status_or;   // [B] OR of the status bits of every scored pose
   float* eta;       // [B] gradient-descent step
 };
 
 struct MCParams {
   double kT;        // kcal/mol
-  float rot, trans, tors, gd_step;
+  double rot, trans, tors;  // initial step sizes
+  double roi_c[3], roi_r;   // hard region of interest (roi_r <= 0: off)
+  float gd_step;
   int law;          // kMcUniform (Move.rand_*) or kMcGaussian
-  int adapt;        // step-size adaptation per 100 moves
+  int adapt;        // step-size adaptation from the sliding windows
   int flip_every;   // uniform law: every flip_every-th conformer move in [-pi, pi]
+  int reset_zero;   // 1: a trial with E_inter exactly 0 resets the chain
+  int too_long_ends;  // 1: an over-long trial conformer ends the chain
   uint32_t key0, key1;
   int B, nd, nrb;
+  int trace_steps;  // steps of the trace buffers (0: no trace)
+  float* trace_dofs;     // [trace_steps][B][nd] trial poses
+  double* trace_E;       // [trace_steps][B] trial energies
+  int* trace_event;      // [trace_steps][B] kMc* bits
 };
 
 // ---- precomputed interaction grids (kernels_grid.cu) --------------------

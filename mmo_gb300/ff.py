@@ -136,12 +136,19 @@ class UFFScorer:
     def mc_run_device(self, chains: int, steps: int, params, d_dofs: int, d_E: int,
                       d_best_dofs: int | None = None, d_best_E: int | None = None,
                       d_accepted: int | None = None, d_status: int | None = None,
-                      stream: int | None = None, graph: bool = True) -> None:
+                      stream: int | None = None, graph: bool = True, d_resets: int | None = None,
+                      d_trace_dofs: int | None = None, d_trace_E: int | None = None,
+                      d_trace_event: int | None = None) -> None:
         """Monte Carlo chains (mmo_mc_run) on device buffers; params is a
         lib.MCParams or a dict of its fields."""
         if isinstance(params, dict):
+            params = dict(params)
+            roi = params.pop("roi_center", None)
             params = _L.MCParams(**params)
-        st = _L.MCState(d_dofs, d_E, d_best_dofs, d_best_E, d_accepted, d_status)
+            if roi is not None:
+                params.roi_center[:] = [float(v) for v in roi]
+        st = _L.MCState(d_dofs, d_E, d_best_dofs, d_best_E, d_accepted, d_status, d_resets,
+                        d_trace_dofs, d_trace_E, d_trace_event)
         self._check(self._lib.mmo_mc_run(self._h, chains, steps, C.byref(params), C.byref(st),
                                          stream, int(graph)))
 

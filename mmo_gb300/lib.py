@@ -20,6 +20,7 @@ F_INTER, F_INTRA, F_GRAD, F_RECENTER, F_GRID = 1, 2, 4, 8, 16
 S_TOO_LONG, S_NONFINITE, S_OFF_GRID = 1, 2, 4
 
 MC_UNIFORM, MC_GAUSSIAN = 0, 1
+MC_ACCEPTED, MC_RESET, MC_STOPPED, MC_BLOCKED = 1, 2, 4, 8
 CLASH_INTRA, CLASH_HEAVY, CLASH_GRID = 1, 2, 4
 
 
@@ -29,7 +30,8 @@ class MCParams(C.Structure):
                 ("tors_step", C.c_double), ("move_law", C.c_int), ("adapt", C.c_int),
                 ("flip_every", C.c_int), ("minimize_every", C.c_int),
                 ("minimize_iters", C.c_int), ("gd_step", C.c_double), ("seed", C.c_ulonglong),
-                ("use_grid", C.c_int)]
+                ("use_grid", C.c_int), ("roi_center", C.c_double * 3), ("roi_radius", C.c_double),
+                ("reset_on_zero_inter", C.c_int), ("too_long_ends_chain", C.c_int)]
 
 
 class GridSpec(C.Structure):
@@ -57,7 +59,9 @@ class DockResult(C.Structure):
 class MCState(C.Structure):
     """mmo_mc_state of include/mmo_mc.h (device pointers)."""
     _fields_ = [("dofs", C.c_void_p), ("E", C.c_void_p), ("best_dofs", C.c_void_p),
-                ("best_E", C.c_void_p), ("accepted", C.c_void_p), ("status", C.c_void_p)]
+                ("best_E", C.c_void_p), ("accepted", C.c_void_p), ("status", C.c_void_p),
+                ("resets", C.c_void_p), ("trace_dofs", C.c_void_p), ("trace_E", C.c_void_p),
+                ("trace_event", C.c_void_p)]
 
 
 class System(C.Structure):

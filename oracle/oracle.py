@@ -42,6 +42,20 @@ def lattice(step, dims, origin) -> Lattice:
     return g
 
 
+class MCParams(C.Structure):
+    _fields_ = [("kT", C.c_double), ("rot", C.c_double), ("trans", C.c_double),
+                ("tors", C.c_double), ("law", C.c_int), ("adapt", C.c_int),
+                ("flip_every", C.c_int), ("seed", C.c_uint64), ("roi_c", C.c_double * 3),
+                ("roi_r", C.c_double), ("reset_zero", C.c_int), ("too_long_ends", C.c_int)]
+
+
+class MCStats(C.Structure):
+    _fields_ = [("proposals", C.c_long), ("proposal_mismatch", C.c_long),
+                ("decisions", C.c_long), ("decision_mismatch", C.c_long),
+                ("ambiguous", C.c_long), ("resets", C.c_long), ("adapt_events", C.c_long),
+                ("max_rel_err_E", C.c_double)]
+
+
 class CLigand(C.Structure):
     _fields_ = [("m", CMol), ("interacting", C.POINTER(C.c_uint8)), ("nrb", C.c_int),
                 ("bond_lr", C.POINTER(C.c_int)), ("grp_off", C.POINTER(C.c_int)),
@@ -88,6 +102,11 @@ def lib():
             "orc_grad_analytic": (d, [P(Physics), P(CMol), P(CLigand), P(d), i, P(d), P(d),
                                       P(i)]),
             "orc_grad_scale": (d, [P(Physics), P(CMol), P(CLigand), P(d), i, P(d)]),
+            "orc_mc_replay": (v, [P(Physics), P(CMol), P(CLigand), P(MCParams), i,
+                                  P(C.c_float), i, P(C.c_float), P(d), P(C.c_int), d, i,
+                                  P(MCStats)]),
+            "orc_mc_run": (v, [P(Physics), P(CMol), P(CLigand), P(MCParams), i, P(C.c_float),
+                               i, P(C.c_float), P(d), P(C.c_int), i, P(MCStats)]),
             "orc_score_batch": (v, [P(Physics), P(CMol), P(CLigand), i, P(C.c_float), i, i,
                                     P(d), i, i, P(d), P(d), P(i)]),
             "orc_grid_point": (v, [P(Physics), P(CMol), P(d), i, P(i), P(d), d, P(d)]),
@@ -272,6 +291,53 @@ def grad_analytic(prot, lig, conf, flags=F_INTER | F_INTRA, ph=REF, want_xyz=Fal
     if want_xyz:
         return e, g, gx.reshape(-1, 3), st.value
     return e, g, st.value
+
+
+def _mc_params(params: dict) -> MCParams:
+    mp = MCParams()
+    for k, v in params.items():
+        if k == "roi_c":
+            mp.roi_c[:] = [float(x) for x in v]
+        else:
+            setattr(mp, k, v)
+    return mp
+
+
+def mc_run(prot, lig, params: dict, start, steps, nthreads=16, ph=REF):
+    """The oracle's own run of the chains (orc_mc_run): (trial [steps, B, nd],
+    E [steps, B], event [steps, B], stats)."""
+    p, L = OMol.of(prot), OLigand(lig)
+    start = np.ascontiguousarray(start, np.float32)
+    B, nd = start.shape
+    trial = np.zeros((steps, B, nd), np.float32)
+    E = np.zeros((steps, B))
+    event = np.zeros((steps, B), np.int32)
+    st = MCStats()
+    f = C.POINTER(C.c_float)
+    lib().orc_mc_run(C.byref(ph), C.byref(p.c), C.byref(L.c), C.byref(_mc_params(params)), B,
+                     start.ctypes.data_as(f), steps, trial.ctypes.data_as(f), _dp(E),
+                     event.ctypes.data_as(C.POINTER(C.c_int)), nthreads, C.byref(st))
+    return trial, E, event, {k: getattr(st, k) for k, _ in MCStats._fields_}
+
+
+def mc_replay(prot, lig, params: dict, start, trial, E, event, e_tol=1e-5, nthreads=16,
+              ph=REF) -> dict:
+    """Replay of a GPU Monte Carlo trace (orc_mc_replay): start [B, nd] float32,
+    trial [steps, B, nd] float32, E [steps, B], event [steps, B]."""
+    p, L = OMol.of(prot), OLigand(lig)
+    start = np.ascontiguousarray(start, np.float32)
+    trial = np.ascontiguousarray(trial, np.float32)
+    E = np.ascontiguousarray(E, np.float64)
+    event = np.ascontiguousarray(event, np.int32)
+    steps, B = E.shape
+    mp = _mc_params(params)
+    st = MCStats()
+    f = C.POINTER(C.c_float)
+    lib().orc_mc_replay(C.byref(ph), C.byref(p.c), C.byref(L.c), C.byref(mp), B,
+                        start.ctypes.data_as(f), steps, trial.ctypes.data_as(f), _dp(E),
+                        event.ctypes.data_as(C.POINTER(C.c_int)), e_tol, nthreads,
+                        C.byref(st))
+    return {k: getattr(st, k) for k, _ in MCStats._fields_}
 
 
 def grad_scale(prot, lig, conf, flags=F_INTER | F_INTRA, ph=REF):

@@ -1377,3 +1377,431 @@ void orc_desolvation_penalty(const orc_lattice *g, const double *prot_contrib,
   out[0] = pd;
   out[1] = orc_desolv_constant() * (vol * ld);
 }
+
+/* ---- Monte Carlo chains: replay of a GPU trace ------------------------------
+ * One chain of Lds.simulate_lig (src/lds.ml:882-995) frame by frame, in the
+ * reference's semantics as the GPU chains implement them: rigid moves on even
+ * frames (Move.rand_rot / rand_trans, src/move.ml:14-54, or the Gaussian law),
+ * one torsion on odd frames (Mol.tweak_rbond / flip_rbond, src/mol.ml:635-647,
+ * the flip cadence of src/lds.ml:783-793); the hard region of interest and the
+ * E_inter = 0 resets (reset_run_params, src/lds.ml:652-671, 906-928); the
+ * Metropolis test in FP64 (src/lds.ml:931-934); acceptance counted in sliding
+ * windows of 100 events (src/SW.ml:7-37) and the step-size adaptation of
+ * src/lds.ml:586-621, 962-988.  The random numbers are the GPU's: Philox4x32-10
+ * keyed by the seed, counter (chain, frame, draw, 0), two words per uniform
+ * with 53 random bits.  The trial poses are rounded to float32 as the GPU
+ * stores them.
+ *
+ * The replay walks the GPU's trace: each frame's proposal is recomputed from
+ * the chain's current state and compared bit for bit with the GPU's trial;
+ * the trial is scored in FP64 and the outcome (accepted, rejected, reset,
+ * chain ended) decided from the FP64 energies.  An outcome whose test lies
+ * within e_tol max(|E|, S) of its threshold (Metropolis), or whose trial sits
+ * on the cut-off or enclosing-radius boundary, is ambiguous: the replay takes
+ * the GPU's outcome there and counts it.  Any other difference is counted as
+ * a mismatch, and the replay then follows the GPU so that one difference
+ * does not hide the rest. */
+static double mc_u01(uint32_t a, uint32_t b) {
+  return (double)((((uint64_t)a) << 21) ^ (uint64_t)(b >> 11)) * (1.0 / 9007199254740992.0);
+}
+
+static void mc_philox(int b, int step, uint32_t draw, const uint32_t key[2], uint32_t out[4]) {
+  const uint32_t c[4] = {(uint32_t)b, (uint32_t)step, draw, 0u};
+  orc_philox4x32_10(c, key, out);
+}
+
+/* Box-Muller pair from two uniforms */
+static void mc_normal2(double u1, double u2, double *n0, double *n1) {
+  const double r = sqrt(-2.0 * log(1.0 - u1));
+  *n0 = r * cos(2.0 * ORC_PI * u2);
+  *n1 = r * sin(2.0 * ORC_PI * u2);
+}
+
+static double mc_wrap_pi(double a) {
+  a = fmod(a + ORC_PI, 2.0 * ORC_PI);
+  if (a < 0.0) a += 2.0 * ORC_PI;
+  return a - ORC_PI;
+}
+
+/* sliding window: ring of 100 event bits, length, accepts */
+typedef struct {
+  unsigned char ev[100];
+  int head, len, acc;
+} mc_window;
+
+static void mc_sw_reset(mc_window *w) { memset(w, 0, sizeof *w); }
+
+static void mc_sw_process(mc_window *w, int evt) {
+  if (w->len == 100) w->acc -= w->ev[w->head];
+  else w->len += 1;
+  w->ev[w->head] = (unsigned char)(evt != 0);
+  w->acc += evt != 0;
+  w->head = w->head + 1 == 100 ? 0 : w->head + 1;
+}
+
+static double mc_sw_ratio(const mc_window *w) { return (double)w->acc / (double)w->len; }
+
+/* the proposal of frame `step` of chain b from its current pose */
+static int mc_propose(const orc_mc_params *p, int nrb, int b, int step, int conf_steps,
+                      const double *st, const float *cur, float *tr) {
+  const int nd = 6 + nrb;
+  const uint32_t key[2] = {(uint32_t)(p->seed & 0xffffffffu), (uint32_t)(p->seed >> 32)};
+  memcpy(tr, cur, sizeof(float) * nd);
+  const int rigid = (step & 1) == 0;
+  if (!rigid && nrb == 0) return -2;
+  uint32_t r0[4], r1[4];
+  mc_philox(b, step, 0u, key, r0);
+  mc_philox(b, step, 1u, key, r1);
+  if (rigid) {
+    double ax, ay, az, th, dt[3];
+    if (p->law == 1) {
+      double n[6], n6, n7;
+      uint32_t r2[4], r3[4];
+      mc_normal2(mc_u01(r0[0], r0[1]), mc_u01(r0[2], r0[3]), &n[0], &n[1]);
+      mc_normal2(mc_u01(r1[0], r1[1]), mc_u01(r1[2], r1[3]), &n[2], &n[3]);
+      mc_philox(b, step, 2u, key, r2);
+      mc_normal2(mc_u01(r2[0], r2[1]), mc_u01(r2[2], r2[3]), &n[4], &n[5]);
+      double s2 = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
+      const double il = 1.0 / sqrt(s2 > 1e-300 ? s2 : 1e-300);
+      ax = n[0] * il;
+      ay = n[1] * il;
+      az = n[2] * il;
+      th = st[0] * n[3];
+      dt[0] = st[1] * n[4];
+      dt[1] = st[1] * n[5];
+      mc_philox(b, step, 3u, key, r3);
+      mc_normal2(mc_u01(r3[0], r3[1]), mc_u01(r3[2], r3[3]), &n6, &n7);
+      dt[2] = st[1] * n6;
+    } else {
+      uint32_t r2[4];
+      th = (2.0 * mc_u01(r0[0], r0[1]) - 1.0) * st[0];
+      int axis = (int)(mc_u01(r0[2], r0[3]) * 3.0);
+      if (axis > 2) axis = 2;
+      ax = axis == 0;
+      ay = axis == 1;
+      az = axis == 2;
+      dt[0] = (2.0 * mc_u01(r1[0], r1[1]) - 1.0) * st[1];
+      dt[1] = (2.0 * mc_u01(r1[2], r1[3]) - 1.0) * st[1];
+      mc_philox(b, step, 2u, key, r2);
+      dt[2] = (2.0 * mc_u01(r2[0], r2[1]) - 1.0) * st[1];
+    }
+    /* R' = Rm R (rot.ml:121-146 for Rm, rot.ml:52-66 for R), then
+     * Rot.decompose (rot.ml:71-75) */
+    double R[9], M[9], Q[9];
+    const double u[3] = {ax, ay, az};
+    orc_rot_xyz((double)cur[3], (double)cur[4], (double)cur[5], R);
+    orc_rot_axis_angle(u, th, M);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        Q[3 * i + j] = M[3 * i] * R[j] + M[3 * i + 1] * R[3 + j] + M[3 * i + 2] * R[6 + j];
+    const double beta = atan2(-Q[6], sqrt(Q[0] * Q[0] + Q[3] * Q[3]));
+    const double icb = 1.0 / cos(beta);
+    tr[3] = (float)atan2(Q[7] * icb, Q[8] * icb);
+    tr[4] = (float)beta;
+    tr[5] = (float)atan2(Q[3] * icb, Q[0] * icb);
+    for (int k = 0; k < 3; ++k) tr[k] = (float)((double)cur[k] + dt[k]);
+    return -1;
+  }
+  int i = (int)(mc_u01(r0[0], r0[1]) * nrb);
+  if (i > nrb - 1) i = nrb - 1;
+  double d;
+  if (p->law == 1) {
+    double n0, n1;
+    mc_normal2(mc_u01(r0[2], r0[3]), mc_u01(r1[0], r1[1]), &n0, &n1);
+    d = st[2 + i] * n0;
+  } else {
+    const int flip = p->flip_every > 0 && conf_steps > 0 && conf_steps % p->flip_every == 0;
+    d = (2.0 * mc_u01(r0[2], r0[3]) - 1.0) * (flip ? ORC_PI : st[2 + i]);
+  }
+  tr[6 + i] = (float)mc_wrap_pi((double)cur[6 + i] + d);
+  return i;
+}
+
+/* E, E_inter, the condition scale S, the smallest inter pair r^2 and the
+ * enclosing radius of one configuration under the MC pose map */
+static void mc_energies(const orc_physics *ph, const orc_mol *prot, const orc_ligand *lig,
+                        const double *conf, double *E, double *Ei, double *S, double *r2min,
+                        double *radius) {
+  const int n = lig->m.n;
+  const double K = orc_elec_weight();
+  double *x = (double *)malloc(sizeof(double) * 3 * n + 1), *y = x + n, *z = x + 2 * n;
+  double *t = (double *)malloc(sizeof(double) * 3 * n + 1);
+  apply_torsions(lig, conf + 6, t, t + n, t + 2 * n);
+  double c[3];
+  centroid(n, t, t + n, t + 2 * n, c);
+  double rad = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const double dx = c[0] - t[i], dy = c[1] - t[n + i], dz = c[2] - t[2 * n + i];
+    const double d = 0.01 + sqrt(dx * dx + dy * dy + dz * dz);
+    if (d > rad) rad = d;
+  }
+  orc_apply_config(lig, conf, ORC_F_RECENTER, x, y, z);
+  double e = 0.0, ei = 0.0, s = 0.0, mn = 1e300, ea;
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < prot->n; ++i) {
+      const double d[3] = {x[j] - prot->x[i], y[j] - prot->y[i], z[j] - prot->z[i]};
+      const double r2 = dot(d, d);
+      if (r2 < mn) mn = r2;
+      if (ph->inter_form == 0 && !(r2 < 144.0)) continue;
+      double x_ij, d_ij, ep;
+      orc_pair_params(ph, prot->anum[i], lig->m.anum[j], &x_ij, &d_ij);
+      const double qq = K * prot->q[i] * lig->m.q[j];
+      pair_energy_grad(ph->dielectric, ph->inter_form == 0, r2, qq, x_ij, d_ij, &ep);
+      pair_energy_grad_abs(ph->dielectric, ph->inter_form == 0, r2, qq, x_ij, d_ij, &ea);
+      ei += ep;
+      s += ea;
+    }
+  e = ei;
+  for (int i = 0; i < n - 1; ++i)
+    for (int j = i + 1; j < n; ++j) {
+      if (!lig->interacting[i * n + j]) continue;
+      const double d[3] = {x[i] - x[j], y[i] - y[j], z[i] - z[j]};
+      const double r2 = dot(d, d);
+      const int shifted = ph->intra_form == 1;
+      if (shifted && !(orc_non_zero_dist(sqrt(r2)) < 12.0)) continue;
+      double x_ij, d_ij, ep;
+      orc_pair_params(ph, lig->m.anum[i], lig->m.anum[j], &x_ij, &d_ij);
+      const double qq = K * lig->m.q[i] * lig->m.q[j];
+      pair_energy_grad(ph->dielectric, shifted, r2, qq, x_ij, d_ij, &ep);
+      pair_energy_grad_abs(ph->dielectric, shifted, r2, qq, x_ij, d_ij, &ea);
+      e += ep;
+      s += ea;
+    }
+  *E = e;
+  *Ei = ei;
+  *S = s;
+  *r2min = mn;
+  *radius = rad;
+  free(t);
+  free(x);
+}
+
+static int mc_metropolis(double Et, double E0, double u, double kT) {
+  return Et <= E0 || u < exp(-(Et - E0) / kT);
+}
+
+typedef struct {
+  const orc_physics *ph;
+  const orc_mol *prot;
+  const orc_ligand *lig;
+  const orc_mc_params *p;
+  int B, steps, b0, b1;
+  const float *start, *gpu_trial;
+  const double *gpu_E;
+  const int *gpu_event;
+  float *gen_trial; /* generate mode: the oracle's own trace goes here */
+  double *gen_E;
+  int *gen_event;
+  double e_tol;
+  orc_mc_stats st;
+} mc_job;
+
+static void *mc_worker(void *arg) {
+  mc_job *J = (mc_job *)arg;
+  const orc_mc_params *p = J->p;
+  const int nrb = J->lig->nrb, nd = 6 + nrb, B = J->B;
+  const uint32_t key[2] = {(uint32_t)(p->seed & 0xffffffffu), (uint32_t)(p->seed >> 32)};
+  float *cur = (float *)malloc(sizeof(float) * nd), *tr = (float *)malloc(sizeof(float) * nd);
+  double *st = (double *)malloc(sizeof(double) * (2 + nrb)), *conf = (double *)malloc(
+                                                                   sizeof(double) * nd);
+  mc_window *win = (mc_window *)malloc(sizeof(mc_window) * (1 + nrb));
+  double *ccur = (double *)malloc(sizeof(double) * nd);
+  for (int b = J->b0; b < J->b1; ++b) {
+    memcpy(cur, J->start + (size_t)b * nd, sizeof(float) * nd);
+    st[0] = p->rot;
+    st[1] = p->trans;
+    for (int i = 0; i < nrb; ++i) st[2 + i] = p->tors;
+    for (int k = 0; k <= nrb; ++k) mc_sw_reset(&win[k]);
+    for (int k = 0; k < nd; ++k) ccur[k] = (double)cur[k];
+    double E0, Ei0, S0, m0, rad0;
+    mc_energies(J->ph, J->prot, J->lig, ccur, &E0, &Ei0, &S0, &m0, &rad0);
+    int rigid_steps = 0, conf_steps = 0, stopped = 0;
+    for (int step = 0; step < J->steps; ++step) {
+      const size_t o = (size_t)step * B + b;
+      const int gen = J->gen_trial != NULL;
+      const int rigid = (step & 1) == 0;
+      int mv = -2;
+      if (!stopped) mv = mc_propose(p, nrb, b, step, conf_steps, st, cur, tr);
+      else memcpy(tr, cur, sizeof(float) * nd);
+      if (gen) memcpy(J->gen_trial + o * nd, tr, sizeof(float) * nd);
+      const float *gt = gen ? J->gen_trial + o * nd : J->gpu_trial + o * nd;
+      J->st.proposals += 1;
+      if (memcmp(tr, gt, sizeof(float) * nd) != 0) {
+        J->st.proposal_mismatch += 1;
+        memcpy(tr, gt, sizeof(float) * nd);
+      }
+      int ev = 0, amb = 0;
+      double Et = 0, Ei = 0, S = 0, r2m = 0, rad = 0;
+      if (stopped) {
+        ev = 4;
+      } else {
+        for (int k = 0; k < nd; ++k) conf[k] = (double)tr[k];
+        mc_energies(J->ph, J->prot, J->lig, conf, &Et, &Ei, &S, &r2m, &rad);
+        const int too_long = mv >= 0 && rad > 12.0;
+        if (mv >= 0 && fabs(rad - 12.0) < 1e-6) amb = 1;
+        if (gen) J->gen_E[o] = Et;
+        const double gE = gen ? Et : J->gpu_E[o];
+        if (isfinite(gE) && isfinite(Et)) {
+          const double den = fmax(fabs(Et), S);
+          const double err = den > 0 ? fabs(gE - Et) / den : 0.0;
+          if (err > J->st.max_rel_err_E) J->st.max_rel_err_E = err;
+        }
+        int reset = 0;
+        if (p->roi_r > 0.0) {
+          const double dx = (double)tr[0] - p->roi_c[0], dy = (double)tr[1] - p->roi_c[1],
+                       dz = (double)tr[2] - p->roi_c[2];
+          const double d = sqrt(dx * dx + dy * dy + dz * dz);
+          reset = d > p->roi_r;
+          if (fabs(d - p->roi_r) < 1e-9) amb = 1;
+        }
+        if (!reset && p->reset_zero) {
+          if (Ei == 0.0) reset = 1;
+          if (fabs(r2m - 144.0) < 1e-3) amb = 1;
+        }
+        if (reset) {
+          ev = 2;
+        } else if (too_long && p->too_long_ends) {
+          ev = 4;
+        } else {
+          const int blocked = !isfinite(Et) || too_long;
+          int acc = 0;
+          if (!blocked) {
+            uint32_t r[4];
+            mc_philox(b, step, 7u, key, r);
+            const double u = mc_u01(r[0], r[1]);
+            acc = mc_metropolis(Et, E0, u, p->kT);
+            const double dt = J->e_tol * fmax(fabs(Et), S), d0 = J->e_tol * fmax(fabs(E0), S0);
+            if (isfinite(E0) &&
+                mc_metropolis(Et + dt, E0 - d0, u, p->kT) != mc_metropolis(Et - dt, E0 + d0, u,
+                                                                           p->kT))
+              amb = 1;
+          }
+          ev = (acc ? 1 : 0) | (blocked ? 8 : 0);
+        }
+      }
+      if (gen) J->gen_event[o] = ev;
+      const int gev = gen ? ev : J->gpu_event[o];
+      J->st.decisions += 1;
+      if (ev != gev) {
+        if (amb) J->st.ambiguous += 1;
+        else J->st.decision_mismatch += 1;
+        ev = gev; /* follow the GPU */
+      } else if (amb) {
+        J->st.ambiguous += 1;
+      }
+      /* apply the outcome */
+      if (ev & 4) {
+        stopped = 1;
+      } else if (ev & 2) {
+        J->st.resets += 1;
+        memcpy(cur, J->start + (size_t)b * nd, sizeof(float) * 6);
+        E0 = INFINITY;
+        S0 = 0.0;
+        st[0] = p->rot;
+        st[1] = p->trans;
+        mc_sw_reset(&win[0]);
+      } else {
+        const int acc = ev & 1;
+        if (mv == -1) mc_sw_process(&win[0], acc);
+        else if (mv >= 0) mc_sw_process(&win[1 + mv], acc);
+        if (acc) {
+          memcpy(cur, tr, sizeof(float) * nd);
+          E0 = Et;
+          S0 = S;
+        }
+        if (p->adapt && rigid && rigid_steps > 0 && rigid_steps % 100 == 0) {
+          const double ratio = mc_sw_ratio(&win[0]);
+          if (ratio <= 0.45) {
+            st[1] = 0.95 * st[1];
+            st[0] = 0.95 * st[0];
+            J->st.adapt_events += 1;
+          } else if (ratio >= 0.55) {
+            st[1] = 1.05 * st[1];
+            st[0] = fmin(ORC_PI, 1.05 * st[0]);
+            J->st.adapt_events += 1;
+          }
+        }
+        if (p->adapt && acc && mv >= 0 && conf_steps > 0 && conf_steps % (100 * nrb) == 0) {
+          for (int i = 0; i < nrb; ++i) {
+            const double ratio = mc_sw_ratio(&win[1 + i]);
+            if (ratio <= 0.45) st[2 + i] = 0.95 * st[2 + i];
+            else if (ratio >= 0.55) st[2 + i] = fmin(ORC_PI, 1.05 * st[2 + i]);
+          }
+          J->st.adapt_events += 1;
+        }
+      }
+      if (rigid) rigid_steps += 1;
+      else conf_steps += 1;
+    }
+  }
+  free(ccur);
+  free(win);
+  free(conf);
+  free(st);
+  free(tr);
+  free(cur);
+  return NULL;
+}
+
+static void mc_run_jobs(const orc_physics *ph, const orc_mol *prot, const orc_ligand *lig,
+                        const orc_mc_params *p, int B, const float *start, int steps,
+                        const float *gpu_trial, const double *gpu_E, const int *gpu_event,
+                        float *gen_trial, double *gen_E, int *gen_event, double e_tol,
+                        int nthreads, orc_mc_stats *out) {
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > B) nthreads = B > 0 ? B : 1;
+  pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+  mc_job *jobs = (mc_job *)calloc(nthreads, sizeof(mc_job));
+  for (int t = 0; t < nthreads; ++t) {
+    mc_job *j = &jobs[t];
+    j->ph = ph;
+    j->prot = prot;
+    j->lig = lig;
+    j->p = p;
+    j->B = B;
+    j->steps = steps;
+    j->b0 = (int)((long)B * t / nthreads);
+    j->b1 = (int)((long)B * (t + 1) / nthreads);
+    j->start = start;
+    j->gpu_trial = gpu_trial;
+    j->gpu_E = gpu_E;
+    j->gpu_event = gpu_event;
+    j->gen_trial = gen_trial;
+    j->gen_E = gen_E;
+    j->gen_event = gen_event;
+    j->e_tol = e_tol;
+    if (nthreads == 1) mc_worker(j);
+    else pthread_create(&th[t], NULL, mc_worker, j);
+  }
+  if (nthreads > 1)
+    for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+  memset(out, 0, sizeof *out);
+  for (int t = 0; t < nthreads; ++t) {
+    const orc_mc_stats *s = &jobs[t].st;
+    out->proposals += s->proposals;
+    out->proposal_mismatch += s->proposal_mismatch;
+    out->decisions += s->decisions;
+    out->decision_mismatch += s->decision_mismatch;
+    out->ambiguous += s->ambiguous;
+    out->resets += s->resets;
+    out->adapt_events += s->adapt_events;
+    if (s->max_rel_err_E > out->max_rel_err_E) out->max_rel_err_E = s->max_rel_err_E;
+  }
+  free(jobs);
+  free(th);
+}
+
+void orc_mc_replay(const orc_physics *ph, const orc_mol *prot, const orc_ligand *lig,
+                   const orc_mc_params *p, int B, const float *start, int steps,
+                   const float *gpu_trial, const double *gpu_E, const int *gpu_event,
+                   double e_tol, int nthreads, orc_mc_stats *out) {
+  mc_run_jobs(ph, prot, lig, p, B, start, steps, gpu_trial, gpu_E, gpu_event, NULL, NULL, NULL,
+              e_tol, nthreads, out);
+}
+
+void orc_mc_run(const orc_physics *ph, const orc_mol *prot, const orc_ligand *lig,
+                const orc_mc_params *p, int B, const float *start, int steps, float *trial,
+                double *E, int *event, int nthreads, orc_mc_stats *out) {
+  mc_run_jobs(ph, prot, lig, p, B, start, steps, NULL, NULL, NULL, trial, E, event, 0.0,
+              nthreads, out);
+}

@@ -24,6 +24,8 @@
  *   src/mol.ml:928-960      ene_inter_UFF_shifted_bst (12 A neighbour sum)
  *   src/optim.ml:64-80      apply_config (torsions in order, Too_long, r_xyz, +t)
  *   src/lds.ml:1118-1136    approx_local_gradient (central finite differences)
+ *   src/lds.ml:882-995      simulate_lig frames (moves, resets, Metropolis,
+ *                           sliding-window step adaptation; src/SW.ml:7-37)
  *
  * Parity status: the reference ships no golden energies or gradients and its
  * OCaml toolchain is absent, so energy parity is UNPINNED against the reference
@@ -135,6 +137,43 @@ void orc_score_batch(const orc_physics *ph, const orc_mol *prot, const orc_ligan
 
 /* Philox4x32-10 block: out = philox(ctr, key) */
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+/* Monte Carlo chains (src/lds.ml:882-995): replay of a GPU trace of `steps`
+ * frames of B chains from the start poses (float32 [B][6+nrb], the MC pose
+ * map), frame by frame: each proposal is recomputed and compared bit for bit
+ * with the GPU's trial (gpu_trial [steps][B][6+nrb]); each outcome (the
+ * event bits of mmo_mc_state.trace_event) is decided from FP64 energies and
+ * compared with the GPU's (gpu_event [steps][B]); outcomes within
+ * e_tol max(|E|, S) of their threshold are ambiguous and follow the GPU.
+ * gpu_E [steps][B] is compared with the FP64 trial energy. */
+typedef struct {
+  double kT, rot, trans, tors; /* kT (kcal/mol), initial steps (rad, A, rad) */
+  int law;                     /* 0: uniform (src/move.ml), 1: Gaussian */
+  int adapt, flip_every;
+  uint64_t seed;               /* Philox key: low word, high word */
+  double roi_c[3], roi_r;      /* hard ROI; roi_r <= 0: off */
+  int reset_zero;              /* reset on E_inter = 0 */
+  int too_long_ends;           /* an over-long trial conformer ends the chain */
+} orc_mc_params;
+
+typedef struct {
+  long proposals, proposal_mismatch; /* trial poses compared, not bit-equal */
+  long decisions, decision_mismatch; /* outcomes compared, different and unambiguous */
+  long ambiguous;                    /* outcomes within the tolerance of their threshold */
+  long resets, adapt_events;         /* resets and step-size adaptations of the replay */
+  double max_rel_err_E;              /* max |E_gpu - E64| / max(|E64|, S) of scored trials */
+} orc_mc_stats;
+
+void orc_mc_replay(const orc_physics *ph, const orc_mol *prot, const orc_ligand *lig,
+                   const orc_mc_params *p, int B, const float *start, int steps,
+                   const float *gpu_trial, const double *gpu_E, const int *gpu_event,
+                   double e_tol, int nthreads, orc_mc_stats *out);
+
+/* The same chains run by the oracle alone (FP64 outcomes), writing the trace
+ * in the GPU's layout: trial [steps][B][6+nrb], E and event [steps][B]. */
+void orc_mc_run(const orc_physics *ph, const orc_mol *prot, const orc_ligand *lig,
+                const orc_mc_params *p, int B, const float *start, int steps, float *trial,
+                double *E, int *event, int nthreads, orc_mc_stats *out);
 
 /* precomputed interaction grids (src/lds.ml:452-469, src/mol.ml:964-989) and
  * their trilinear interpolation (src/G3D.ml:97-157, src/mol.ml:1010-1020) */

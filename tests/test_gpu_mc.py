@@ -147,3 +147,105 @@ def test_move_step_statistics(scorer_factory, system, law):
     both = acc2 == 2
     changed = (d2[both, 6:] != d1[both, 6:]).sum(axis=1)
     assert np.all(changed == 1)
+
+
+# -- step by step against the oracle ------------------------------------------------
+
+def _run_trace(torch, sc, L, dofs0, steps, **kw):
+    """A run with its trace: (final dofs, E, resets, trial [steps, B, nd],
+    E_trial [steps, B], event [steps, B])."""
+    dev = torch.device("cuda", 0)
+    B, nd = dofs0.shape
+    d = torch.from_numpy(np.ascontiguousarray(dofs0)).to(dev)
+    E = torch.empty(B, dtype=torch.float64, device=dev)
+    res = torch.zeros(B, dtype=torch.int32, device=dev)
+    tr = torch.zeros((steps, B, nd), dtype=torch.float32, device=dev)
+    tE = torch.zeros((steps, B), dtype=torch.float64, device=dev)
+    tev = torch.zeros((steps, B), dtype=torch.int32, device=dev)
+    sc.mc_run_device(B, steps, _params(L, **kw), d.data_ptr(), E.data_ptr(), graph=True,
+                     d_resets=res.data_ptr(), d_trace_dofs=tr.data_ptr(),
+                     d_trace_E=tE.data_ptr(), d_trace_event=tev.data_ptr())
+    torch.cuda.synchronize()
+    return tuple(x.cpu().numpy() for x in (d, E, res, tr, tE, tev))
+
+
+def _oracle_params(kw):
+    return dict(kT=kw["kT"], rot=kw["rot_step"], trans=kw["trans_step"], tors=kw["tors_step"],
+                law=kw["move_law"], adapt=kw["adapt"], flip_every=kw["flip_every"],
+                seed=kw["seed"], roi_c=kw.get("roi_center", (0.0, 0.0, 0.0)),
+                roi_r=kw.get("roi_radius", 0.0), reset_zero=kw.get("reset_on_zero_inter", 0),
+                too_long_ends=kw.get("too_long_ends_chain", 0))
+
+
+@pytest.mark.parametrize("law", ["uniform", "gaussian"])
+def test_every_step_replays_in_the_oracle(oracle, scorer_factory, system, law):
+    """900 frames of 24 chains, traced: every trial pose equals the oracle's
+    proposal from the chain's state bit for bit (Philox draws, move laws, the
+    flip cadence, step sizes adapted from the sliding windows); every outcome
+    (accepted, rejected, reset to the start) equals the oracle's FP64 outcome
+    except where the energies' tolerance straddles the Metropolis threshold;
+    hard-ROI and E_inter = 0 resets and the step-size adaptation all occur.
+    Four of the chains start 60 A from the pocket (E_inter = 0, a reset every
+    frame)."""
+    torch = pytest.importorskip("torch")
+    from mmo_gb300 import lib as L
+
+    sc = scorer_factory(system.pocket, system.ligand)
+    d0 = system.poses[:24].copy()
+    d0[20:, :3] += 60.0
+    kw = _params(L, move_law=L.MC_UNIFORM if law == "uniform" else L.MC_GAUSSIAN, adapt=1,
+                 flip_every=100, rot_step=np.radians(15.0), trans_step=0.15,
+                 tors_step=np.radians(5.0), roi_center=(0.0, 0.0, 0.0), roi_radius=4.2,
+                 reset_on_zero_inter=1, seed=4321)
+    steps = 900
+    d, E, res, tr, tE, tev = _run_trace(torch, sc, L, d0, steps, **kw)
+    r = oracle.mc_replay(system.pocket, system.ligand, _oracle_params(kw), d0, tr, tE, tev,
+                         e_tol=1e-5, nthreads=16)
+    n = steps * len(d0)
+    assert r["proposals"] == r["decisions"] == n
+    assert r["proposal_mismatch"] == 0, r
+    assert r["decision_mismatch"] == 0, r
+    assert r["ambiguous"] <= 0.02 * n, r
+    assert r["max_rel_err_E"] <= 1e-5, r
+    assert np.all(tev[:, 20:] == L.MC_RESET)  # far chains: E_inter = 0 every frame
+    assert res[:20].sum() > 0  # hard-ROI resets among the pocket chains
+    assert r["resets"] == res.sum()
+    assert r["adapt_events"] > 0
+    assert ((tev[:, :20] & L.MC_ACCEPTED) > 0).mean() > 0.05
+
+
+def test_over_long_conformer_ends_the_chain(oracle, scorer_factory):
+    """too_long_ends_chain: the first over-long trial conformer ends a chain
+    (the reference's Mol.Too_long leaves its frame loop), later frames keep
+    its pose; without it the trial is rejected and the chain goes on."""
+    torch = pytest.importorskip("torch")
+    from mmo_gb300 import lib as L
+    from mmo_gb300.topology import build_ligand
+
+    n = 22
+    xyz = np.array([[i * 1.22, 0.8 * (i % 2), 0.0] for i in range(n)])
+    lig = build_ligand("chain", xyz - xyz.mean(0), np.zeros(n), np.full(n, 6, np.int32),
+                       [(i, i + 1) for i in range(n - 1)])
+    pocket = synth.random_pocket(np.random.default_rng(2), 600, 12.0)
+    sc = scorer_factory(pocket, lig)
+    d0 = np.zeros((16, 6 + lig.nrb), np.float32)
+    d0[:, 6 + 9] = 1.85  # one fold: 11.9 A from the centroid, a random flip often unfolds it
+    d0[:, :3] = 30.0     # away from the pocket atoms
+    kw = _params(L, move_law=L.MC_UNIFORM, flip_every=1, kT=1e30, too_long_ends_chain=1,
+                 seed=77)
+    steps = 60
+    d, E, res, tr, tE, tev = _run_trace(torch, sc, L, d0, steps, **kw)
+    ended = (tev & L.MC_STOPPED) > 0
+    assert ended.any(axis=0).sum() >= 8
+    for b in range(16):
+        if ended[:, b].any():
+            k = int(np.argmax(ended[:, b]))
+            assert np.all(ended[k:, b])
+            assert np.array_equal(d[b], tr[-1, b])  # the pose stays from then on
+    r = oracle.mc_replay(pocket, lig, _oracle_params(kw), d0, tr, tE, tev, nthreads=16)
+    assert r["proposal_mismatch"] == 0 and r["decision_mismatch"] == 0, r
+    kw2 = dict(kw, too_long_ends_chain=0)
+    _, _, _, tr2, tE2, tev2 = _run_trace(torch, sc, L, d0, steps, **kw2)
+    assert not np.any(tev2 & L.MC_STOPPED) and np.any(tev2 & L.MC_BLOCKED)
+    r = oracle.mc_replay(pocket, lig, _oracle_params(kw2), d0, tr2, tE2, tev2, nthreads=16)
+    assert r["proposal_mismatch"] == 0 and r["decision_mismatch"] == 0, r

@@ -463,3 +463,51 @@ def test_desolvation_is_the_sum_over_shell_points(oracle):
     d2 = ((pts[:, None, :] - xyz) ** 2).sum(axis=-1)
     want = C_ * 0.125 * np.sum(np.where(d2 < 144.0, (s.ligand.q / d2) ** 2, 0.0))
     assert lig == pytest.approx(want, rel=1e-10)
+
+
+# -- Monte Carlo chains: the replay that checks GPU traces step by step ---------
+
+def _mc_setup():
+    s = synth.pose_batch(n_poses=8, seed=9, n_atoms=24, n_rot=4, n_pocket=1500, radius=14.0,
+                         half_box=1.0)
+    prm = dict(kT=0.593, rot=math.radians(15.0), trans=0.15, tors=math.radians(5.0), law=0,
+               adapt=1, flip_every=100, seed=7, roi_c=(0.0, 0.0, 0.0), roi_r=0.0,
+               reset_zero=1, too_long_ends=0)
+    return s, prm
+
+
+def test_mc_replay_of_its_own_trace_and_planted_mistakes(oracle):
+    """orc_mc_run writes a trace; orc_mc_replay of it finds no mismatch; a
+    flipped outcome and a trial pose moved by one float ulp, planted in the
+    trace, are each found."""
+    s, prm = _mc_setup()
+    tr, E, ev, st = oracle.mc_run(s.pocket, s.ligand, prm, s.poses, 500, nthreads=4)
+    assert st["adapt_events"] > 0 and (ev & 1).sum() > 0
+    r = oracle.mc_replay(s.pocket, s.ligand, prm, s.poses, tr, E, ev, nthreads=4)
+    assert r["proposal_mismatch"] == 0 and r["decision_mismatch"] == 0
+    assert r["proposals"] == r["decisions"] == 500 * len(s.poses)
+    ev2 = ev.copy()
+    k = tuple(np.argwhere((ev2 & 1) == 1)[3])
+    ev2[k] ^= 1
+    r = oracle.mc_replay(s.pocket, s.ligand, prm, s.poses, tr, E, ev2, e_tol=0.0, nthreads=4)
+    assert r["decision_mismatch"] == 1
+    tr2 = tr.copy()
+    tr2[201, 3, 7] = np.nextafter(tr2[201, 3, 7], np.float32(10.0))
+    r = oracle.mc_replay(s.pocket, s.ligand, prm, s.poses, tr2, E, ev, nthreads=4)
+    assert r["proposal_mismatch"] >= 1
+
+
+def test_mc_resets_of_the_reference(oracle):
+    """Far from the pocket E_inter is 0: with reset_zero every frame resets
+    (lds.ml:918-927); a hard ROI of 0.05 A about the start resets every rigid
+    frame whose translation leaves it (lds.ml:908-916) and never a conformer
+    frame, which keeps the translation."""
+    s, prm = _mc_setup()
+    far = s.poses[:2].copy()
+    far[:, :3] += 80.0
+    _, _, ev, st = oracle.mc_run(s.pocket, s.ligand, prm, far, 40, nthreads=2)
+    assert np.all(ev == 2) and st["resets"] == 80
+    near = s.poses[:2].copy()
+    roi = dict(prm, roi_c=tuple(float(v) for v in near[0, :3]), roi_r=0.05, reset_zero=0)
+    _, _, ev, _ = oracle.mc_run(s.pocket, s.ligand, roi, near[:1], 40, nthreads=1)
+    assert np.all(ev[0::2] == 2) and not np.any(ev[1::2] == 2)
