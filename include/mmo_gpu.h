@@ -167,11 +167,13 @@ int mmo_set_tiles(mmo_ctx* ctx, int poses_per_lane, int threads, int chunks);
 /* Cut-off sweep of the shifted form for batches (the counterpart of
  * Mol.ene_inter_UFF_shifted_bst, UnixJunkie/MMO src/mol.ml:928-962, which
  * visits only the protein atoms within 12 A of each ligand atom).  mode 0:
- * automatic, used for batches of 2 or more poses under the shifted form when
- * the protein and its row index fit in shared memory; mode 1: off, every pair
- * is evaluated.  row_spacing: (y, z) spacing of the protein's row index in A
- * (<= 0: 3; a change rebuilds the index); piece_atoms: protein atoms per
- * work item (0: 256); entries_per_lane: 1, 2, 4 (0: 2). */
+ * automatic, used for batches of 2 or more poses under the shifted form, the
+ * protein staged in shared memory when it fits (about 6,500 atoms) and read
+ * from global memory otherwise; mode 1: off, every pair is evaluated; mode 2:
+ * the cut-off sweep with the protein always read from global memory.
+ * row_spacing: (y, z) spacing of the protein's row index in A (<= 0: 3; a
+ * change rebuilds the index); piece_atoms: protein atoms per work item (0:
+ * 256); entries_per_lane: 1, 2, 4 (0: 2). */
 int mmo_set_cull(mmo_ctx* ctx, int mode, double row_spacing, int piece_atoms,
                  int entries_per_lane);
 
@@ -194,8 +196,9 @@ int mmo_tune(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E, f
 /* File of tuned plans for mmo_tune, one line per shape; NULL or "" for none. */
 int mmo_set_tune_cache(mmo_ctx* ctx, const char* path);
 
-/* Plan of the last batched call: *path 1 for the cut-off sweep, 0 for the
- * full sweep; entries (or poses) per lane; threads per CTA; piece atoms (or
+/* Plan of the last batched call: *path 1 for the cut-off sweep with the
+ * protein in shared memory, 2 for the cut-off sweep reading it from global
+ * memory, 0 for the full sweep; entries (or poses) per lane; threads per CTA; piece atoms (or
  * protein chunks per pose); the row spacing of the protein index. */
 int mmo_get_plan(const mmo_ctx* ctx, int* path, int* per_lane, int* threads,
                  int* piece_or_chunks, double* row_spacing);

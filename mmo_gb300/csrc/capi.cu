@@ -116,11 +116,15 @@ struct mmo_ctx {
   std::vector<int> ptypes;
 
   // cut-off sweep of the shifted form (mmo_set_cull)
-  int cull_mode = 0;        // 0: automatic, 1: off
+  int cull_mode = 0;        // 0: automatic, 1: off, 2: protein read from global memory
   double cull_h = 3.0;      // row spacing of the protein index, A
   int cull_piece = 0;       // protein atoms per piece, 0: automatic
   int cull_kp = 0;          // entries per lane, 0: automatic
-  bool cull_ok = false;     // row index built and resident in shared memory
+  bool cull_ok = false;     // row index built
+  bool cull_fits = false;   // the whole protein and its row index fit in shared memory
+  float4* d_pbox = nullptr;  // [npieces][2] piece boxes of the cut-off sweep
+  size_t capPbox = 0;
+  size_t capGcnt = 0, capGlist = 0, capItems = 0;
   long cull_version = 0;    // bumped by every rebuild of the row index
   DevCull cull{};
   void* d_cull = nullptr;
@@ -129,8 +133,8 @@ struct mmo_ctx {
   CullScratch cs{};
   CullSegs segs[2] = {};
   CullPlan cplan[2] = {};
-  long cplan_key[2][10] = {{-1, -1, -1, -1, -1, -1, -1, -1, -1, -1},
-                           {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1}};
+  long cplan_key[2][11] = {{-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1},
+                           {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1}};
   long piece_key[2] = {-1, -1};  // (row index version, piece atoms) of the uploaded pieces
   int npieces = 0;
   int* d_piece = nullptr;
@@ -875,8 +879,11 @@ int build_cull(mmo_ctx* ctx) {
   ctx->desolv_ok = false;
   ++ctx->cull_version;
   ++ctx->epoch;
-  // the sweep keeps the whole protein and its index in shared memory
-  ctx->cull_ok = cull_smem_bytes(c.npairs, nrows, nrows, 1024) <= ctx->smem_optin;
+  // the sweep can stage the whole protein and its index in shared memory, or
+  // read them from global memory (any size)
+  ctx->cull_ok = true;
+  // (the default plan's 512 threads with 2 entries per lane)
+  ctx->cull_fits = cull_smem_bytes(c.npairs, nrows, 512, false, 2) <= ctx->smem_optin;
   return MMO_OK;
 }
 
@@ -930,20 +937,20 @@ PairPlan make_plan(mmo_ctx* ctx, int B, bool grad) {
   return p;
 }
 
-// the cut-off sweep serves the shifted form when the protein's row index fits
-// in shared memory
+// the cut-off sweep serves the shifted form of batches of 2 or more poses
 bool use_cull(const mmo_ctx* ctx, int B) {
-  return ctx->cull_mode == 0 && ctx->cull_ok && ctx->ph.inter_form == 0 && B >= 2 &&
+  return ctx->cull_mode != 1 && ctx->cull_ok && ctx->ph.inter_form == 0 && B >= 2 &&
          !ctx->lseg_type.empty();
 }
 
-// plan of the cut-off sweep (pieces, type segments, grid), cached per input
+// plan of the cut-off sweep (pieces and their boxes, type segments, grid),
+// cached per input
 int cull_plan_for(mmo_ctx* ctx, int B, bool grad) {
-  const long key[10] = {B, grad, ctx->prot_version, ctx->lig_version, ctx->cull_kp,
+  const long key[11] = {B, grad, ctx->prot_version, ctx->lig_version, ctx->cull_kp,
                         ctx->cull_piece, ctx->tile_threads, ctx->ph.dielectric,
-                        ctx->cull_version, ctx->prot.P};
+                        ctx->cull_version, ctx->prot.P, ctx->cull_mode};
   const int g = grad ? 1 : 0;
-  if (std::equal(key, key + 10, ctx->cplan_key[g])) {
+  if (std::equal(key, key + 11, ctx->cplan_key[g])) {
     ctx->cs.npieces = ctx->npieces;
     return MMO_OK;
   }
@@ -951,15 +958,43 @@ int cull_plan_for(mmo_ctx* ctx, int B, bool grad) {
   p.kp = ctx->cull_kp ? ctx->cull_kp : 2;
   p.threads = std::min(ctx->tile_threads ? ctx->tile_threads : 1024, cull_max_threads(p.kp));
   p.piece_atoms = ctx->cull_piece ? ctx->cull_piece : 256;
+  p.global = (ctx->cull_mode == 2 ||
+              cull_smem_bytes(ctx->cull.npairs, ctx->cull.nrows, p.threads, false, p.kp) >
+                  ctx->smem_optin)
+                 ? 1
+                 : 0;
   if (ctx->piece_key[0] != ctx->cull_version || ctx->piece_key[1] != p.piece_atoms) {
     const std::vector<int> pr = row_pieces(ctx->cull_rows, p.piece_atoms);
+    const int np = (int)pr.size() - 1;
+    // each piece's bounding box over its atoms' FP32 coordinates (the
+    // broad phase's test, conservative for the sweep's per-atom test)
+    std::vector<float4> pb(2 * (size_t)np);
+    for (int q = 0; q < np; ++q) {
+      float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+      for (int k = ctx->cull_rows[pr[q]]; k < ctx->cull_rows[pr[q + 1]]; ++k) {
+        const int i = ctx->cull_perm[k];
+        const float v[3] = {(float)ctx->pxs[i], (float)ctx->pys[i], (float)ctx->pzs[i]};
+        for (int d = 0; d < 3; ++d) {
+          lo[d] = std::min(lo[d], v[d]);
+          hi[d] = std::max(hi[d], v[d]);
+        }
+      }
+      pb[2 * q] = make_float4(lo[0], lo[1], lo[2], 0.f);
+      pb[2 * q + 1] = make_float4(hi[0], hi[1], hi[2], 0.f);
+    }
     int r = grow(ctx, (void**)&ctx->d_piece, &ctx->capPiece, sizeof(int) * pr.size(),
                  "piece table");
     if (r) return r;
+    if ((r = grow(ctx, (void**)&ctx->d_pbox, &ctx->capPbox, sizeof(float4) * pb.size(),
+                  "piece boxes")))
+      return r;
     MMO_CK(cudaStreamSynchronize(ctx->stream), "sync before piece table upload");
     MMO_CK(cudaMemcpy(ctx->d_piece, pr.data(), sizeof(int) * pr.size(), cudaMemcpyHostToDevice),
            "piece table upload");
-    ctx->npieces = (int)pr.size() - 1;
+    MMO_CK(cudaMemcpy(ctx->d_pbox, pb.data(), sizeof(float4) * pb.size(),
+                      cudaMemcpyHostToDevice),
+           "piece box upload");
+    ctx->npieces = np;
     ctx->piece_key[0] = ctx->cull_version;
     ctx->piece_key[1] = p.piece_atoms;
   }
@@ -973,8 +1008,9 @@ int cull_plan_for(mmo_ctx* ctx, int B, bool grad) {
     sg.type[t] = ctx->lseg_type[t];
     sg.off[t + 1] = sg.off[t] + (sg.n[t] + sg.G - 1) / sg.G * sg.G;
   }
-  p.smem = cull_smem_bytes(ctx->cull.npairs, ctx->cull.nrows, npieces, p.threads);
-  const int bps = std::max(1, cull_max_blocks(p.kp, p.threads, grad, ctx->ph, p.smem));
+  p.smem = cull_smem_bytes(ctx->cull.npairs, ctx->cull.nrows, p.threads, p.global != 0, p.kp);
+  const int bps =
+      std::max(1, cull_max_blocks(p.kp, p.threads, grad, ctx->ph, p.smem, p.global != 0));
   p.blocks = ctx->sms * bps;
   const long items = (long)sg.off[sg.nseg] / sg.G * npieces;
   const long need = (items + p.threads / 32 - 1) / (p.threads / 32);
@@ -982,7 +1018,7 @@ int cull_plan_for(mmo_ctx* ctx, int B, bool grad) {
   ctx->cplan[g] = p;
   ctx->segs[g] = sg;
   ctx->cs.npieces = npieces;
-  std::copy(key, key + 10, ctx->cplan_key[g]);
+  std::copy(key, key + 11, ctx->cplan_key[g]);
   return MMO_OK;
 }
 
@@ -1010,8 +1046,17 @@ int ensure_cull_scratch(mmo_ctx* ctx, int B, int L, bool grad) {
   if ((r = grow(ctx, (void**)&c.arrive, &ctx->capArr, sizeof(int) * groups, "group arrivals")))
     return r;
   if ((r = grow(ctx, (void**)&c.vis, &ctx->capVis, groups * np, "piece flags"))) return r;
+  if ((r = grow(ctx, (void**)&c.gcount, &ctx->capGcnt, sizeof(int) * groups, "group counts")))
+    return r;
+  if ((r = grow(ctx, (void**)&c.glist, &ctx->capGlist, sizeof(int) * groups * np,
+                "group piece lists")))
+    return r;
+  if ((r = grow(ctx, (void**)&c.items, &ctx->capItems, sizeof(int2) * groups * np,
+                "sweep items")))
+    return r;
+  c.pbox = ctx->d_pbox;
   c.Eout = ctx->scr.Epart;
-  c.Gout = ctx->scr.Gpart;
+  c.Gout = grad ? ctx->scr.Gpart : nullptr;
   c.queue = ctx->d_queue;
   c.pairs = reinterpret_cast<unsigned long long*>(ctx->d_queue + 2);
   c.seg_of_atom = ctx->lig.seg_of_atom;
@@ -1046,9 +1091,9 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
   ctx->last_cull = cull;
   ctx->last_grad = grad ? 1 : 0;
   ctx->last_pairs = inter && !use_grid ? (double)B * L * ctx->prot.P : 0.0;
-  // rebuild + finish, and the sweep: entry bin, scan, scatter, sweep (or the
-  // grid lookup)
-  ctx->last_launches = 2 + (cull ? 4 : (inter ? 1 : 0));
+  // rebuild + finish, and the sweep: entry bin, scan, scatter, broad phase,
+  // sweep (or the grid lookup)
+  ctx->last_launches = 2 + (cull ? 5 : (inter ? 1 : 0));
   PairPlan plan{};
   int C = 1;
   int r;
@@ -1623,6 +1668,10 @@ int mmo_ctx_destroy(mmo_ctx* ctx) {
   cudaFree(ctx->d_queue);
   cudaFree(ctx->d_cull);
   cudaFree(ctx->d_piece);
+  cudaFree(ctx->d_pbox);
+  cudaFree(ctx->cs.gcount);
+  cudaFree(ctx->cs.glist);
+  cudaFree(ctx->cs.items);
   cudaFree(ctx->cs.hist);
   cudaFree(ctx->cs.bin);
   cudaFree(ctx->cs.rank);
@@ -1684,12 +1733,12 @@ int mmo_set_tiles(mmo_ctx* ctx, int kp, int threads, int chunks) {
 int mmo_set_cull(mmo_ctx* ctx, int mode, double row_spacing, int piece_atoms,
                  int entries_per_lane) {
   if (!ctx) return MMO_EINVAL;
-  if ((mode != 0 && mode != 1) || piece_atoms < 0 || piece_atoms > (1 << 20) ||
+  if (mode < 0 || mode > 2 || piece_atoms < 0 || piece_atoms > (1 << 20) ||
       !(entries_per_lane == 0 || entries_per_lane == 1 || entries_per_lane == 2 ||
         entries_per_lane == 4) ||
       !std::isfinite(row_spacing) || (row_spacing > 0 && (row_spacing < 0.25 || row_spacing > 64)))
     return fail(ctx, MMO_EINVAL,
-                "cull: mode 0 or 1, row spacing in [0.25, 64] A (<= 0: default), piece atoms "
+                "cull: mode 0, 1 or 2, row spacing in [0.25, 64] A (<= 0: default), piece atoms "
                 ">= 0, entries per lane in {0,1,2,4}");
   ctx->cull_mode = mode;
   ctx->cull_piece = piece_atoms;
@@ -2114,7 +2163,8 @@ namespace {
 
 // One launch plan of the batched pair sweep as the tuner sets it.
 struct TunePlan {
-  int cull;       // 1: cut-off sweep, 0: full sweep
+  int cull;       // 0: full sweep, 1: cut-off sweep, protein staged in shared memory, 2: cut-off
+                  // sweep, protein read from global memory
   double h;       // row spacing (cut-off)
   int kp;         // entries per lane (cut-off) or poses per lane (full)
   int piece;      // protein atoms per piece (cut-off)
@@ -2124,7 +2174,7 @@ struct TunePlan {
 
 void apply_plan(mmo_ctx* ctx, const TunePlan& p, int* r) {
   ++ctx->epoch;
-  ctx->cull_mode = p.cull ? 0 : 1;
+  ctx->cull_mode = p.cull == 0 ? 1 : (p.cull == 2 ? 2 : 0);
   ctx->cull_kp = p.cull ? p.kp : 0;
   ctx->cull_piece = p.cull ? p.piece : 0;
   ctx->tile_kp = p.cull ? 0 : p.kp;
@@ -2179,8 +2229,8 @@ int mmo_get_plan(const mmo_ctx* ctx, int* path, int* per_lane, int* threads, int
                  double* row_spacing) {
   if (!ctx || !path || !per_lane || !threads || !chunks_or_piece || !row_spacing)
     return MMO_EINVAL;
-  *path = ctx->last_cull ? 1 : 0;
   const int g = ctx->last_grad;
+  *path = ctx->last_cull ? 1 + ctx->cplan[g].global : 0;
   *per_lane = ctx->last_cull ? ctx->cplan[g].kp : ctx->plan[g].kp;
   *threads = ctx->last_cull ? ctx->cplan[g].threads : ctx->plan[g].threads;
   *chunks_or_piece = ctx->last_cull ? ctx->cplan[g].piece_atoms : ctx->plan[g].C;
@@ -2214,15 +2264,18 @@ int mmo_tune(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E, f
   std::vector<TunePlan> cands;
   if (inter && B >= 2) {
     if (ctx->ph.inter_form == 0 && ctx->cull_ok)
-      for (double h : {2.0, 3.0, 4.0})
-        for (int kp : {1, 2, 4})
-          for (int piece : {256, 512}) {
-            // the register budget's thread count, and fewer warps with more shared
-            // memory left to the L1
-            const int th = cull_max_threads(kp);
-            cands.push_back({1, h, kp, piece, th, 0});
-            if (th >= 512) cands.push_back({1, h, kp, piece, th - 256, 0});
-          }
+      for (int mem : {1, 2}) {
+        if (mem == 1 && !ctx->cull_fits) continue;  // the staged copy needs shared memory
+        for (double h : {2.0, 3.0, 4.0})
+          for (int kp : {1, 2, 4})
+            for (int piece : {256, 512}) {
+              // the register budget's thread count, and fewer warps with more shared
+              // memory left to the L1
+              const int th = cull_max_threads(kp);
+              cands.push_back({mem, h, kp, piece, th, 0});
+              if (th >= 512) cands.push_back({mem, h, kp, piece, th - 256, 0});
+            }
+      }
     for (int kp : {1, 2, 4})
       for (int ch : {4, 8, 12, 16, 24}) cands.push_back({0, ctx->cull_h, kp, 0, 512, ch});
   }

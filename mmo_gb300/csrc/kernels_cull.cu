@@ -152,7 +152,8 @@ __global__ void __launch_bounds__(kScanThreads) k_cull_scan(unsigned* hist, Cull
   }
   for (int k = blockIdx.x * blockDim.x + t; k < narrive; k += gridDim.x * blockDim.x) arrive[k] = 0;
   if (blockIdx.x == 0 && t == 0) {
-    queue[0] = 0u;
+    queue[0] = 0u;  // the sweep's work counter
+    queue[1] = 0u;  // its items, counted by the broad phase
     *reinterpret_cast<unsigned long long*>(queue + 2) = 0ull;
   }
 }
@@ -183,10 +184,23 @@ __device__ __forceinline__ void pair_params(const float4* trow, float4 a3, float
   c1 = make_float2(ta[2], tb[2]);
 }
 
+// Protein records: read from shared memory (the staged copy) or, with GLOB,
+// from global memory through the read-only path (L1 / L2)
+template <bool GLOB>
+__device__ __forceinline__ float4 ldp(const float4* p) {
+  if constexpr (GLOB) return __ldg(p);
+  else return *p;
+}
+template <bool GLOB>
+__device__ __forceinline__ int ldi(const int* p) {
+  if constexpr (GLOB) return __ldg(p);
+  else return *p;
+}
+
 // dE/dX of one entry over the protein pairs [a0, a1) with the per-pair test
 // of the 0.01 A clamp; the same arithmetic in the same order as the sweep, so
 // entries without a clamped pair get the sweep's value bit for bit.
-template <int DIEL, int FORM>
+template <int DIEL, int FORM, bool GLOB>
 __device__ __noinline__ float3 cull_exact_grad(const float4* sp, const float4* trow, int a0, int a1,
                                                float q, float xh, float yh, float zh, float xl,
                                                float yl, float zl) {
@@ -195,7 +209,8 @@ __device__ __noinline__ float3 cull_exact_grad(const float4* sp, const float4* t
   float mn = 1e30f;
   for (int i = a0; i < a1; ++i) {
     const float4* pp = sp + 4 * i;
-    const float4 p0 = pp[0], p1 = pp[1], p2 = pp[2], p3 = pp[3];
+    const float4 p0 = ldp<GLOB>(pp), p1 = ldp<GLOB>(pp + 1), p2 = ldp<GLOB>(pp + 2),
+                 p3 = ldp<GLOB>(pp + 3);
     float2 X, iD, c1;
     pair_params(trow, p3, X, iD, c1);
     pair_step_ab<true, DIEL, FORM, true>(bc2(xh), bc2(yh), bc2(zh), bc2(xl), bc2(yl), bc2(zl),
@@ -227,17 +242,20 @@ __device__ __forceinline__ float box_d2(float x, float y, float z, float blx, fl
 
 // One warp's work for one (group, protein piece) item: the group's entries
 // [slot0, s_end) (32 * KP slots, padding repeats the last entry) against the
-// piece's rows [r0, r1) resident in shared memory (sp: pairs of atoms, s_rbox,
-// s_rs: first pair of each row, s_flush), then the piece's partials at
-// P0 + kpc * PS (+ slot - slot0) and its flag at V0 + kpc; the last of the
-// group's npieces items to arrive sums them.  CULL false visits every atom
-// (the global form).
-template <int KP, bool GRAD, int DIEL, int FORM, bool CULL>
+// piece's rows [r0, r1) (sp: pairs of atoms, s_rbox, s_rs: first pair of each
+// row, s_flush; in shared memory, or in global memory with GLOB), then the
+// piece's partials at P0 + kpc * PS (+ slot - slot0).  The last of the
+// group's npieces items to arrive sums them in piece order: with LISTED the
+// pieces of plist[0 .. npieces) (the broad phase's list, every one written),
+// otherwise pieces 0 .. npieces - 1 whose flag at V0 + q says visited.  CULL
+// false visits every atom (the global form).
+template <int KP, bool GRAD, int DIEL, int FORM, bool CULL, bool LISTED = false, bool GLOB = false>
 __device__ __forceinline__ void sweep_item(const float4* sp, const float4* s_rbox, const int* s_rs,
                                            const int* s_flush, int r0, int r1,
                                            const float4* trow, int slot0, int s_end, int* wl,
                                            const CullScratch& cs, long long P0, long long PS,
-                                           int kpc, long long V0, int npieces, int* arrive) {
+                                           int kpc, long long V0, int npieces, int* arrive,
+                                           const int* plist = nullptr) {
   constexpr float c0v = DIEL == 0 ? -10.0f : -4.0f;
   constexpr int G = 32 * KP;
   const int lane = threadIdx.x & 31;
@@ -286,7 +304,8 @@ __device__ __forceinline__ void sweep_item(const float4* sp, const float4* s_rbo
 #pragma unroll 2
     for (int v = 0; v < n; ++v) {
       const float4* pp = sp + 4 * wl[v];
-      const float4 p0 = pp[0], p1 = pp[1], p2 = pp[2], p3 = pp[3];
+      const float4 p0 = ldp<GLOB>(pp), p1 = ldp<GLOB>(pp + 1), p2 = ldp<GLOB>(pp + 2),
+                   p3 = ldp<GLOB>(pp + 3);
       float2 X, iD, c1;
       pair_params(trow, p3, X, iD, c1);
 #pragma unroll
@@ -299,18 +318,18 @@ __device__ __forceinline__ void sweep_item(const float4* sp, const float4* s_rbo
   // rows in flush blocks: the FP32 partials go into the FP64 sums once per
   // block (fixed rows of the protein) and at the end of the piece
   for (int r = r0; r < r1;) {
-    const int rend = min(r1, s_flush[r]);
+    const int rend = min(r1, ldi<GLOB>(s_flush + r));
     for (; r < rend; ++r) {
-      const float4 rb = s_rbox[r];
+      const float4 rb = ldp<GLOB>(s_rbox + r);
       const float dy = fmaxf(fmaxf(rb.x - bhy, bly - rb.y), 0.f);
       const float dz = fmaxf(fmaxf(rb.z - bhz, blz - rb.w), 0.f);
       if (CULL && fmaf(dy, dy, dz * dz) >= kCullR2) continue;
-      const int a = s_rs[r], b = s_rs[r + 1];
+      const int a = ldi<GLOB>(s_rs + r), b = ldi<GLOB>(s_rs + r + 1);
       for (int i0 = a; i0 < b; i0 += 32) {
         const int i = i0 + lane;
         bool in_a = false, in_b = false;
         if (i < b) {
-          const float4 p0 = sp[4 * i], p1 = sp[4 * i + 1];
+          const float4 p0 = ldp<GLOB>(sp + 4 * i), p1 = ldp<GLOB>(sp + 4 * i + 1);
           const bool null_b = __float_as_uint(p1.w) == 0x80000000u;
           in_a = !CULL || box_d2(-p0.x, -p0.z, -p1.x, blx, bly, blz, bhx, bhy, bhz) < kCullR2;
           in_b = !null_b &&
@@ -346,15 +365,15 @@ __device__ __forceinline__ void sweep_item(const float4* sp, const float4* s_rbo
   if (GRAD && __any_sync(kFull, mn < kMinR2)) {
     // a pair closer than 0.01 A, where the clamped distance makes the
     // derivative 0: redo the gradient over the piece with the per-pair test
-    const int a0 = s_rs[r0], a1 = s_rs[r1];
+    const int a0 = ldi<GLOB>(s_rs + r0), a1 = ldi<GLOB>(s_rs + r1);
 #pragma unroll
     for (int k = 0; k < KP; ++k)
-      gsum[k] = cull_exact_grad<DIEL, FORM>(sp, trow, a0, a1, q[k].x, xh[k].x, yh[k].x, zh[k].x,
-                                            xl[k].x, yl[k].x, zl[k].x);
+      gsum[k] = cull_exact_grad<DIEL, FORM, GLOB>(sp, trow, a0, a1, q[k].x, xh[k].x, yh[k].x,
+                                                  zh[k].x, xl[k].x, yl[k].x, zl[k].x);
   }
   if (lane == 0 && natoms) atomicAdd(cs.pairs, (unsigned long long)natoms * G);
   constexpr float gs = DIEL == 0 ? -1.0f : -2.0f;
-  if (visited) {  // a piece out of range of the group adds nothing
+  if (LISTED || visited) {  // an unlisted or unvisited piece adds nothing
 #pragma unroll
     for (int k = 0; k < KP; ++k) {
       const int s = slot0 + k * 32 + lane;
@@ -367,7 +386,7 @@ __device__ __forceinline__ void sweep_item(const float4* sp, const float4* s_rbo
   }
   // the last piece of the group to finish sums the group's pieces in piece
   // order (the arrival order does not matter)
-  if (lane == 0) cs.vis[(size_t)V0 + kpc] = visited ? 1 : 0;
+  if (!LISTED && lane == 0) cs.vis[(size_t)V0 + kpc] = visited ? 1 : 0;
   __threadfence();  // every lane's partials before the arrival
   __syncwarp();
   int last = 0;
@@ -381,9 +400,11 @@ __device__ __forceinline__ void sweep_item(const float4* sp, const float4* s_rbo
       const int s = slot0 + k * 32 + lane;
       if (s >= s_end) continue;
       double E = 0.0;
-      float sx = 0.f, sy = 0.f, sz = 0.f;
-      for (int q2 = 0; q2 < npieces; ++q2) {
-        if (!__ldcg(vg + q2)) continue;
+      double sx = 0.0, sy = 0.0, sz = 0.0;
+      for (int j = 0; j < npieces; ++j) {
+        int q2 = j;
+        if (LISTED) q2 = __ldcg(plist + j);
+        else if (!__ldcg(vg + j)) continue;
         const size_t o = (size_t)(P0 + (long long)q2 * PS) + (size_t)(s - slot0);
         E += __ldcg(cs.Ep + o);
         if (GRAD) {
@@ -398,71 +419,167 @@ __device__ __forceinline__ void sweep_item(const float4* sp, const float4* s_rbo
         E = __longlong_as_double(0x7ff8000000000000ll);
       const int e = cs.order[s];
       cs.Eout[e] = E;
-      if (GRAD) cs.Gout[e] = make_float4(sx, sy, sz, 0.f);
+      if (GRAD) cs.Gout[e] = make_float4((float)sx, (float)sy, (float)sz, 0.f);
+    }
+    if (LISTED) {
+      // the group's piece partials are dead from here on: drop their L2 lines
+      // without a write-back to DRAM (128-byte lines: G doubles of energy and
+      // G float4 of gradient per piece, both aligned to G * 8 bytes)
+      constexpr int kEl = 32 * KP * 8 / 128, kGl = GRAD ? 32 * KP * 16 / 128 : 0;
+      for (int w = lane; w < npieces * (kEl + kGl); w += 32) {
+        const int j = w / (kEl + kGl), l = w - j * (kEl + kGl);
+        const int q2 = __ldcg(plist + j);
+        const size_t o = (size_t)(P0 + (long long)q2 * PS);
+        const char* a = l < kEl ? reinterpret_cast<const char*>(cs.Ep + o) + 128 * l
+                                : reinterpret_cast<const char*>(cs.Gp + o) + 128 * (l - kEl);
+        asm volatile("discard.global.L2 [%0], 128;" ::"l"(a) : "memory");
+      }
     }
   }
 }
 
-template <int KP, bool GRAD, int DIEL>
+// The broad phase: one warp per entry group bounds the group's entries by a
+// box and lists, in ascending order, the protein pieces whose box comes
+// within sqrt(145) A of it (any other piece's pairs are all beyond the
+// cut-off, so they would add exact zeros); it reserves one work item per
+// listed piece in the flat item list (queue[1] counts them) and clears the
+// group's arrival counter.
+__global__ void k_cull_items(CullSegs seg, CullScratch cs, int ngroups) {
+  const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (g >= ngroups) return;
+  const int lane = threadIdx.x & 31, G = seg.G;
+  const int slot0 = g * G;
+  int t = 0;
+  while (t + 1 < seg.nseg && slot0 >= seg.off[t + 1]) ++t;
+  const int s_end = seg.off[t] + seg.n[t];
+  float blx = 1e30f, bly = 1e30f, blz = 1e30f, bhx = -1e30f, bhy = -1e30f, bhz = -1e30f;
+  for (int k = lane; k < G; k += 32) {
+    const int s = min(slot0 + k, s_end - 1);
+    const float4 h = cs.Xs[2 * (size_t)s];
+    blx = fminf(blx, h.x);
+    bly = fminf(bly, h.y);
+    blz = fminf(blz, h.z);
+    bhx = fmaxf(bhx, h.x);
+    bhy = fmaxf(bhy, h.y);
+    bhz = fmaxf(bhz, h.z);
+  }
+  blx = warp_min(blx);
+  bly = warp_min(bly);
+  blz = warp_min(blz);
+  bhx = warp_maxf(bhx);
+  bhy = warp_maxf(bhy);
+  bhz = warp_maxf(bhz);
+  // fminf / fmaxf skip NaN, so a group with a non-finite position can have a
+  // box that excludes it: such a group keeps every piece (its energy is set
+  // to NaN by the sweep's last arrival anyway)
+  bool bad = false;
+  for (int k = lane; k < G; k += 32) {
+    const float4 h = cs.Xs[2 * (size_t)min(slot0 + k, s_end - 1)];
+    bad = bad || !isfinite(h.x) || !isfinite(h.y) || !isfinite(h.z);
+  }
+  bad = __any_sync(kFull, bad);
+  int* gl = cs.glist + (size_t)g * cs.npieces;
+  int cnt = 0;
+  for (int q0 = 0; q0 < cs.npieces; q0 += 32) {
+    const int q = q0 + lane;
+    bool in = false;
+    if (q < cs.npieces) {
+      const float4 lo = cs.pbox[2 * q], hi = cs.pbox[2 * q + 1];
+      const float ex = fmaxf(fmaxf(lo.x - bhx, blx - hi.x), 0.f);
+      const float ey = fmaxf(fmaxf(lo.y - bhy, bly - hi.y), 0.f);
+      const float ez = fmaxf(fmaxf(lo.z - bhz, blz - hi.z), 0.f);
+      in = bad || fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < kCullR2;
+    }
+    const unsigned m = __ballot_sync(kFull, in);
+    if (in) gl[cnt + __popc(m & ((1u << lane) - 1u))] = q;
+    cnt += __popc(m);
+  }
+  int base = 0;
+  if (lane == 0) {
+    cs.gcount[g] = cnt;
+    cs.arrive[g] = 0;
+    base = cnt ? (int)atomicAdd(cs.queue + 1, (unsigned)cnt) : 0;
+  }
+  base = __shfl_sync(kFull, base, 0);
+  __syncwarp();
+  for (int k = lane; k < cnt; k += 32) cs.items[base + k] = make_int2(g, gl[k]);
+  if (cnt == 0)  // no piece within reach: the group's inter terms are exact zeros
+    for (int s = slot0 + lane; s < min(slot0 + G, s_end); s += 32) {
+      const int e = cs.order[s];
+      cs.Eout[e] = 0.0;
+      if (cs.Gout) cs.Gout[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+// The cut-off sweep: persistent CTAs; a warp takes (group, piece) items of
+// the broad phase's list from a work counter.  The protein's pairs of atoms
+// and row tables are either staged once per CTA in shared memory with the TMA
+// bulk engine (GLOB false, proteins up to about 6,500 atoms) or read from
+// global memory through the read-only path (GLOB true, any size).
+template <int KP, bool GRAD, int DIEL, bool GLOB>
 __global__ void __launch_bounds__(cull_max_threads(KP))
     k_pairs_cull(DevCull cull, const float4* __restrict__ tabv, CullSegs seg, CullScratch cs,
                  int* err) {
-  extern __shared__ __align__(16) float4 sp[];  // [npairs][4], then the tables below
+  extern __shared__ __align__(16) float4 sp[];  // staged: [npairs][4], then the tables below
   __shared__ __align__(8) uint64_t bar;
-  const int NP = cull.npairs, nrows = cull.nrows, npieces = cs.npieces;
+  const int NP = GLOB ? 0 : cull.npairs, nrows = GLOB ? 0 : cull.nrows;
   float4* s_rbox = sp + 4 * NP;
   float4* s_tab = s_rbox + nrows;                       // [ptype][ltype] (X, 1/D, c1, 0)
   int* s_rs = reinterpret_cast<int*>(s_tab + kTabRows * kNTypes);  // first pair of each row
   int* s_flush = s_rs + nrows + 1;                      // end of the row's flush block
-  int* s_piece = s_flush + nrows;
-  int* s_list = s_piece + npieces + 1;                  // [warps][kListCap] atoms to sweep
-  if (threadIdx.x == 0) {
-    mbar_init(&bar, 1);
-    const uint32_t bytes = (uint32_t)NP * 64u;
-    mbar_expect_tx(&bar, bytes);
-    constexpr uint32_t kPiece = 32768u;
-    for (uint32_t off = 0; off < bytes; off += kPiece) {
-      const uint32_t n = bytes - off < kPiece ? bytes - off : kPiece;
-      bulk_g2s(reinterpret_cast<char*>(sp) + off, reinterpret_cast<const char*>(cull.pairs) + off,
-               n, &bar);
+  int* s_list = s_flush + nrows;                        // [warps][kListCap] atoms to sweep
+  if (!GLOB) {
+    if (threadIdx.x == 0) {
+      mbar_init(&bar, 1);
+      const uint32_t bytes = (uint32_t)NP * 64u;
+      mbar_expect_tx(&bar, bytes);
+      constexpr uint32_t kPiece = 32768u;
+      for (uint32_t off = 0; off < bytes; off += kPiece) {
+        const uint32_t n = bytes - off < kPiece ? bytes - off : kPiece;
+        bulk_g2s(reinterpret_cast<char*>(sp) + off,
+                 reinterpret_cast<const char*>(cull.pairs) + off, n, &bar);
+      }
     }
+    for (int k = threadIdx.x; k < nrows; k += blockDim.x) {
+      s_rbox[k] = cull.row_box[k];
+      s_flush[k] = cull.row_flush[k];
+    }
+    for (int k = threadIdx.x; k <= nrows; k += blockDim.x) s_rs[k] = cull.pair_start[k];
   }
-  for (int k = threadIdx.x; k < nrows; k += blockDim.x) {
-    s_rbox[k] = cull.row_box[k];
-    s_flush[k] = cull.row_flush[k];
-  }
-  for (int k = threadIdx.x; k <= nrows; k += blockDim.x) s_rs[k] = cull.pair_start[k];
-  for (int k = threadIdx.x; k <= npieces; k += blockDim.x) s_piece[k] = cs.piece_row[k];
   stage_pair_table<DIEL>(tabv, s_tab);
   __syncthreads();
-  if (!mbar_wait(&bar, 0, cs.first_wait_polls)) {
+  if (!GLOB && !mbar_wait(&bar, 0, cs.first_wait_polls)) {
     // the copy did not land in time: flag it, wait once more (bounded) for the
     // copy in flight so that it does not write into a finished CTA, and stop
     if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
     mbar_wait(&bar, 0, kWaitPolls);
     return;
   }
+  const float4* pr = GLOB ? cull.pairs : sp;
+  const float4* rbox = GLOB ? cull.row_box : s_rbox;
+  const int* rs = GLOB ? cull.pair_start : s_rs;
+  const int* fl = GLOB ? cull.row_flush : s_flush;
 
   constexpr int G = 32 * KP;
   const int lane = threadIdx.x & 31;
-  const int nitems = seg.off[seg.nseg] / G * npieces;
+  const int nitems = (int)__ldcg(cs.queue + 1);
   for (;;) {
     int item = 0;
     if (lane == 0) item = (int)atomicAdd(cs.queue, 1u);
     item = __shfl_sync(kFull, item, 0);
     if (item >= nitems) break;
-    const int g = item / npieces;
-    const int pc = item - g * npieces;
+    const int2 it = __ldcg(cs.items + item);
+    const int g = it.x, pc = it.y;
     const int slot0 = g * G;
     int t = 0;
     while (t + 1 < seg.nseg && slot0 >= seg.off[t + 1]) ++t;
     const int s_end = seg.off[t] + seg.n[t];
     const float4* trow = s_tab + seg.type[t];  // + the byte offset of the protein type's row
-
-    sweep_item<KP, GRAD, DIEL, 0, true>(sp, s_rbox, s_rs, s_flush, s_piece[pc], s_piece[pc + 1],
-                                        trow, slot0, s_end, s_list + (threadIdx.x >> 5) * kListCap,
-                                        cs, slot0, cs.slots, pc, (long long)g * npieces, npieces,
-                                        &cs.arrive[g]);
+    const int r0 = __ldg(cs.piece_row + pc), r1 = __ldg(cs.piece_row + pc + 1);
+    sweep_item<KP, GRAD, DIEL, 0, true, true, GLOB>(
+        pr, rbox, rs, fl, r0, r1, trow, slot0, s_end, s_list + (threadIdx.x >> 5) * kListCap, cs,
+        slot0, cs.slots, pc, 0, __ldcg(cs.gcount + g), &cs.arrive[g],
+        cs.glist + (size_t)g * cs.npieces);
   }
 }
 
@@ -624,31 +741,36 @@ SysFn pick_sys(int kp, bool grad, const Physics& ph) {
 
 using CullFn = void (*)(DevCull, const float4*, CullSegs, CullScratch, int*);
 
-template <int KP>
+template <int KP, bool GLOB>
 CullFn pick_kp(bool grad, int diel) {
-  if (grad) return diel ? k_pairs_cull<KP, true, 1> : k_pairs_cull<KP, true, 0>;
-  return diel ? k_pairs_cull<KP, false, 1> : k_pairs_cull<KP, false, 0>;
+  if (grad) return diel ? k_pairs_cull<KP, true, 1, GLOB> : k_pairs_cull<KP, true, 0, GLOB>;
+  return diel ? k_pairs_cull<KP, false, 1, GLOB> : k_pairs_cull<KP, false, 0, GLOB>;
 }
 
-CullFn pick_cull(int kp, bool grad, const Physics& ph) {
+CullFn pick_cull(int kp, bool grad, const Physics& ph, bool glob) {
   const int d = ph.dielectric ? 1 : 0;
   switch (kp) {
-    case 1: return pick_kp<1>(grad, d);
-    case 2: return pick_kp<2>(grad, d);
-    default: return pick_kp<4>(grad, d);
+    case 1: return glob ? pick_kp<1, true>(grad, d) : pick_kp<1, false>(grad, d);
+    case 2: return glob ? pick_kp<2, true>(grad, d) : pick_kp<2, false>(grad, d);
+    default: return glob ? pick_kp<4, true>(grad, d) : pick_kp<4, false>(grad, d);
   }
 }
 
 }  // namespace
 
-int cull_smem_bytes(int npairs, int nrows, int npieces, int threads) {
-  const long b = 64L * npairs + 16L * nrows + 16L * kTabRows * kNTypes + 4L * (nrows + 1) + 4L * nrows +
-                 4L * (npieces + 1) + 4L * kListCap * (threads / 32);
+// dynamic shared memory of the cut-off sweep: staged, the protein's pairs and
+// row tables, then the pair table and the warps' lists; global, the last two
+int cull_smem_bytes(int npairs, int nrows, int threads, bool glob, int kp) {
+  (void)kp;
+  if (glob) npairs = nrows = 0;
+  const long b = 64L * npairs + 16L * nrows + 16L * kTabRows * kNTypes + 4L * (nrows + 1) +
+                 4L * nrows + 4L * kListCap * (threads / 32);
   return (int)((b + 15) / 16 * 16);
 }
 
-int cull_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_bytes) {
-  CullFn fn = pick_cull(kp, grad != 0, ph);
+int cull_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_bytes,
+                    bool glob) {
+  CullFn fn = pick_cull(kp, grad != 0, ph, glob);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes) !=
       cudaSuccess)
     return 0;
@@ -670,13 +792,15 @@ cudaError_t launch_cull_sort(const DevCull& cull, const Scratch& s, const float*
   k_cull_scan<<<seg.nseg, kScanThreads, kScanSmem, st>>>(cs.hist, seg, cs.queue, cs.arrive,
                                                          seg.off[seg.nseg] / seg.G);
   k_cull_scatter<<<nb, tb, 0, st>>>(s.X, n, L, lig_q, cs.hist, cs.bin, cs.rank, cs.Xs, cs.order);
+  const int ngroups = seg.off[seg.nseg] / seg.G;
+  k_cull_items<<<(ngroups + 7) / 8, 256, 0, st>>>(seg, cs, ngroups);
   return cudaGetLastError();
 }
 
 cudaError_t launch_pairs_cull(const DevCull& cull, const float4* tab, const CullSegs& seg,
                               const CullScratch& cs, int flags, const Physics& ph,
                               const CullPlan& plan, int* d_err, cudaStream_t st) {
-  CullFn fn = pick_cull(plan.kp, (flags & kFlagGrad) != 0, ph);
+  CullFn fn = pick_cull(plan.kp, (flags & kFlagGrad) != 0, ph, plan.global != 0);
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, plan.smem);
   if (e != cudaSuccess) return e;
   fn<<<plan.blocks, plan.threads, plan.smem, st>>>(cull, tab, seg, cs, d_err);

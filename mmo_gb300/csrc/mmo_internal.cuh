@@ -189,6 +189,10 @@ struct CullScratch {
   float4* Gout;          // [B * L] dE/dX per entry (Scratch::Gpart, one chunk)
   const int* seg_of_atom;  // [L] ligand atom -> type segment
   const int* piece_row;  // [npieces + 1] first row of each protein piece
+  const float4* pbox;    // [npieces][2] bounding box of each piece's atoms (lo, hi)
+  int* gcount;           // [groups] pieces within reach of each group (the broad phase)
+  int* glist;            // [groups][npieces] those pieces, ascending
+  int2* items;           // [groups * npieces] (group, piece) work items; queue[1] counts them
   int slots, npieces;
   uint32_t first_wait_polls = kWaitPollsDefault;  // polls of the sweep's first TMA wait
 };
@@ -201,6 +205,8 @@ struct CullPlan {
   int kp, threads, blocks;
   int piece_atoms;
   int smem;              // dynamic shared memory of the sweep
+  int global;            // 1: protein records read from global memory (L1 / L2), 0: the whole
+                         // protein staged in shared memory
 };
 
 // ---- ragged batch of systems ----------------------------------------------
@@ -459,8 +465,9 @@ cudaError_t launch_cull_sort(const DevCull& cull, const Scratch& s, const float*
 cudaError_t launch_pairs_cull(const DevCull& cull, const float4* tab, const CullSegs& seg,
                               const CullScratch& cs, int flags, const Physics& ph,
                               const CullPlan& plan, int* d_err, cudaStream_t st);
-int cull_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_bytes);
-int cull_smem_bytes(int npairs, int nrows, int npieces, int threads);
+int cull_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_bytes,
+                    bool glob);
+int cull_smem_bytes(int npairs, int nrows, int threads, bool glob, int kp);
 cudaError_t launch_grid_build(const DevCull& cull, const GridBuild& gb, int dielectric,
                               float* grids, cudaStream_t st);
 cudaError_t launch_grid_inter(const GridLook& g, const float4* X, int n, int L,
@@ -525,6 +532,17 @@ __device__ __forceinline__ float split_diff(float ah, float al, float bh, float 
   return (ah - bh) + (al - bl);
 }
 
+// 1 / x from the reciprocal instruction (about one ulp; x >= 1e-4 here, so
+// flushing subnormals changes nothing).  The pair terms take 1 / r^2 from it
+// instead of squaring the reciprocal square root, whose error the squaring
+// doubles and the r^-12 and r^-14 terms of a close contact multiply six- and
+// sevenfold again.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // (hi, lo) = (ch + cl) + v as a normalised float pair: TwoSum of ch and v
 // (Knuth), the low parts added, then Fast2Sum
 __device__ __forceinline__ void dadd_into(float ch, float cl, float v, float& hi, float& lo) {
@@ -548,7 +566,7 @@ __device__ __forceinline__ void uff_pair(float dx, float dy, float dz, float x2,
   const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
   const float r2c = fmaxf(r2, kMinR2);
   const float ir = rsqrtf(r2c);
-  const float ir2 = ir * ir;
+  const float ir2 = rcp_approx(r2c);
   const float p2 = x2 * ir2;
   const float p6 = p2 * p2 * p2;
   const float Dp6 = D * p6;
@@ -581,7 +599,7 @@ __device__ __forceinline__ void uff_pair_eg(float dx, float dy, float dz, float 
   const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
   const float r2c = fmaxf(r2, kMinR2);
   const float ir = rsqrtf(r2c);
-  const float ir2 = ir * ir;
+  const float ir2 = rcp_approx(r2c);
   const float p2 = x2 * ir2;
   const float p6 = p2 * p2 * p2;
   const float Dp6 = D * p6;
@@ -618,7 +636,7 @@ __device__ __forceinline__ void pair_step(float xh, float yh, float zh, float xl
   const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
   const float r2c = fmaxf(r2, kMinR2);
   const float ir = rsqrtf(r2c);
-  const float ir2 = ir * ir;
+  const float ir2 = rcp_approx(r2c);
   const float P = X * ir2;
   const float Dp6 = (P * P) * P;
   const float lj = Dp6 * fmaf(Dp6, invD, -2.0f);
@@ -668,7 +686,7 @@ __device__ __forceinline__ void pair_step_ab(float2 xh, float2 yh, float2 zh, fl
   const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
   const float2 r2c = make_float2(fmaxf(r2.x, kMinR2), fmaxf(r2.y, kMinR2));
   const float2 ir = make_float2(rsqrtf(r2c.x), rsqrtf(r2c.y));
-  const float2 ir2 = __fmul2_rn(ir, ir);
+  const float2 ir2 = make_float2(rcp_approx(r2c.x), rcp_approx(r2c.y));
   const float2 P = __fmul2_rn(X, ir2);
   const float2 Dp6 = __fmul2_rn(__fmul2_rn(P, P), P);
   const float2 lj = __fmul2_rn(Dp6, __ffma2_rn(Dp6, invD, bc2(-2.0f)));

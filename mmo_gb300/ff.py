@@ -105,7 +105,8 @@ class UFFScorer:
         self._check(self._lib.mmo_set_tiles(self._h, poses_per_lane, threads, chunks))
 
     def set_cull(self, mode=0, row_spacing=0.0, piece_atoms=0, entries_per_lane=0) -> None:
-        """Cut-off sweep of the shifted form: mode 0 automatic, 1 off."""
+        """Cut-off sweep of the shifted form: mode 0 automatic, 1 off, 2 the
+        cut-off sweep reading the protein from global memory."""
         self._check(self._lib.mmo_set_cull(self._h, mode, float(row_spacing), piece_atoms,
                                            entries_per_lane))
 
@@ -127,9 +128,10 @@ class UFFScorer:
         h = C.c_double()
         self._check(self._lib.mmo_get_plan(self._h, *[C.byref(x) for x in v], C.byref(h)))
         path, lane, threads, pc = (x.value for x in v)
-        if path == 1:
+        if path in (1, 2):
             return {"sweep": "cut-off", "entries_per_lane": lane, "threads": threads,
-                    "piece_atoms": pc, "row_spacing_A": h.value}
+                    "piece_atoms": pc, "row_spacing_A": h.value,
+                    "protein": "shared memory" if path == 1 else "global memory"}
         return {"sweep": "full", "poses_per_lane": lane, "threads": threads,
                 "protein_chunks": pc}
 

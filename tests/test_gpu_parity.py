@@ -171,6 +171,56 @@ def test_cull_result_independent_of_grouping(scorer_factory, batch):
     assert np.array_equal(Es, E[17:50]) and np.array_equal(Gs, G[17:50])
 
 
+@pytest.mark.parametrize("P", [9000, 13000])
+def test_cull_large_pocket_against_oracle(oracle, scorer_factory, P):
+    """Pockets beyond the shared-memory copy (about 6,500 atoms) run the
+    cut-off sweep with the protein read from global memory: every pose under
+    the scoring contract, and the full sweep agrees."""
+    rng = np.random.default_rng(P)
+    lig = synth.random_ligand(rng, 48, 8)
+    pocket = synth.random_pocket(rng, P, 18.0 * (P / 6000.0) ** (1.0 / 3.0))
+    d = synth.random_poses(rng, 384, lig.nrb, 4.0)
+    sysm = synth.System("big", pocket, lig, d)
+    s = scorer_factory(pocket, lig)
+    E, G, st = s.score_poses(d, grad=True)
+    plan = s.plan()
+    assert plan["sweep"] == "cut-off" and plan["protein"] == "global memory", plan
+    assert_ref(E, G, ref_batch(oracle, sysm, d, grad=True), st)
+    s.set_cull(mode=1)
+    E1, G1, st1 = s.score_poses(d, grad=True)
+    assert np.array_equal(st, st1)
+    assert np.abs(E1 - E).max() <= 1e-6 * np.abs(E).max()
+
+
+def test_cull_protein_in_global_memory_same_bits(scorer_factory, batch):
+    """The cut-off sweep reading the protein from global memory (mode 2) gives
+    the bits of the sweep staging it in shared memory."""
+    s = scorer_factory(batch.pocket, batch.ligand)
+    E0, G0, st0 = s.score_poses(batch.poses, grad=True)
+    assert s.plan()["protein"] == "shared memory"
+    s.set_cull(mode=2)
+    E1, G1, st1 = s.score_poses(batch.poses, grad=True)
+    assert s.plan()["protein"] == "global memory"
+    assert np.array_equal(E0, E1) and np.array_equal(G0, G1) and np.array_equal(st0, st1)
+
+
+def test_cull_groups_out_of_reach(scorer_factory, batch):
+    """Poses far from the pocket: the broad phase lists no protein piece for
+    their entry groups, whose inter energies and forces are exact zeros; in a
+    batch mixed with near poses the near ones keep their bits."""
+    s = scorer_factory(batch.pocket, batch.ligand)
+    far = batch.poses[:200].copy()
+    far[:, :3] += 200.0
+    E, G, st = s.score_poses(far, grad=True)
+    Ei, Gi, _ = s.score_poses(far, inter=False, grad=True)
+    assert np.array_equal(E, Ei) and np.array_equal(G, Gi)
+    mixed = np.concatenate([far[:100], batch.poses[:100]])
+    Em, Gm, _ = s.score_poses(mixed, grad=True)
+    En, Gn, _ = s.score_poses(batch.poses[:100], grad=True)
+    assert np.array_equal(Em[100:], En) and np.array_equal(Gm[100:], Gn)
+    assert np.array_equal(Em[:100], E[:100])
+
+
 def test_cull_non_finite_pose(scorer_factory, batch):
     s = scorer_factory(batch.pocket, batch.ligand)
     d = batch.poses[:64].copy()
