@@ -1041,6 +1041,7 @@ def main():
     ev1.record(stream)
     torch.cuda.synchronize()
     plain_dev_ms = ev0.elapsed_time(ev1)
+    plain_launches = sc.last_launches()
     t = time.perf_counter()
     for k in range(n_plain):
         sc.score_poses(s.poses[k:k + 1], grad=True)
@@ -1085,7 +1086,7 @@ def main():
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": launches * args.steps,
         "plain": {"value": plain_v, "e2e": plain_e2e, "unit": "poses/s", "sample": n_plain,
-                  "launches_per_pose": 3},
+                  "launches_per_pose": plain_launches},
         "batched_vs_plain": value / world / plain_v,
         "batched_vs_plain_e2e": e2e_val / world / plain_e2e,
         "roofline": {"bound": "fp32",

@@ -46,6 +46,13 @@ int mmo_fp32_fma_peak(mmo_ctx* ctx, double* tflops, double* ms);
 int mmo_grid_build_stats(const mmo_ctx* ctx, double* points, double* pairs_evaluated,
                          double* pairs_within_cutoff);
 
+/* Accuracy check of the device's double-float sine and cosine (no
+ * counterpart in the reference; the one-pose kernel takes the angles' sines
+ * and cosines from it instead of the FP64 library): for n host floats x,
+ * out[4 i .. 4 i + 3] = sin(x_i) hi, lo, cos(x_i) hi, lo, the values being
+ * hi + lo.  Synchronous. */
+int mmo_diag_sincos(mmo_ctx* ctx, int n, const float* x, float* out);
+
 /* Failure-path check of the device-side waits (no counterpart in the
  * reference).  The sweep kernels wait for their TMA copies into shared memory
  * on an mbarrier with a bounded number of polls; a wait that gives up sets a

@@ -162,6 +162,10 @@ struct mmo_ctx {
   size_t capX = 0, capE = 0, capG = 0, capI = 0, capY = 0, capR = 0;
   int* d_err = nullptr;
   uint32_t first_wait_polls = kWaitPollsDefault;  // mmo_diag_set_wait_polls
+  // the one-pose path (k_one_pose): per-CTA partials and the arrival count
+  OneScratch one{};
+  bool one_ok = false;       // its shared memory fits (set with the ligand)
+  size_t capOneE = 0, capOneG = 0;
 
   // stage timing (mmo_set_profiling): start, rebuilt, sorted, swept, finished
   bool profiling = false;
@@ -338,6 +342,8 @@ DevLigand ligand_at(const LigBlob& B, char* b, size_t* bytes) {
   L.nrb = nrb;
   L.npairs = np;
   L.nested = B.nested ? 1 : 0;
+  L.ilh = n > 0 ? (float)(1.0 / n) : 0.f;
+  L.ill = n > 0 ? (float)(1.0 / n - (double)L.ilh) : 0.f;
   L.ref = align_ptr<float4>(b, off, n);
   L.ref64 = align_ptr<double>(b, off, 3 * (size_t)n);
   L.ref2 = align_ptr<float2>(b, off, 3 * (size_t)n);
@@ -508,6 +514,7 @@ int upload_ligand(mmo_ctx* ctx) {
          "ligand upload");
   ctx->lig = ligand_at(B, reinterpret_cast<char*>(ctx->d_lig), nullptr);
   ctx->has_lig = true;
+  ctx->one_ok = one_pose_smem(ctx->lig.L, ctx->lig.nrb) <= ctx->smem_optin;
   ++ctx->lig_version;
   ++ctx->epoch;
   return MMO_OK;
@@ -1071,6 +1078,25 @@ int check_dev_err(mmo_ctx* ctx, int flag) {
   return MMO_OK;
 }
 
+// the one-pose path's per-CTA partials: ncta CTAs of 64 protein atoms
+int ensure_one_scratch(mmo_ctx* ctx, int L) {
+  OneScratch& o = ctx->one;
+  o.chunk = kOneChunk;
+  o.ncta = std::max(1, (ctx->prot.P + o.chunk - 1) / o.chunk);
+  int r;
+  if ((r = grow(ctx, (void**)&o.E, &ctx->capOneE, sizeof(float2) * (size_t)o.ncta * L,
+                "one-pose partials")))
+    return r;
+  if ((r = grow(ctx, (void**)&o.G, &ctx->capOneG, sizeof(float4) * (size_t)o.ncta * L,
+                "one-pose partials")))
+    return r;
+  if (!o.arrive) {
+    MMO_CK(cudaMalloc((void**)&o.arrive, sizeof(unsigned)), "one-pose counter");
+    MMO_CK(cudaMemset(o.arrive, 0, sizeof(unsigned)), "one-pose counter");
+  }
+  return MMO_OK;
+}
+
 int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E,
                  float* d_grad, int* d_status, int* d_err, int zero_err, cudaStream_t st,
                  double* d_E_inter = nullptr) {
@@ -1091,15 +1117,17 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
   ctx->last_cull = cull;
   ctx->last_grad = grad ? 1 : 0;
   ctx->last_pairs = inter && !use_grid ? (double)B * L * ctx->prot.P : 0.0;
+  // one pose with pair sums: the fused one-launch path (k_one_pose)
+  const bool one = B == 1 && inter && !use_grid && ctx->one_ok;
   // rebuild + finish, and the sweep: entry bin, scan, scatter, broad phase,
   // sweep (or the grid lookup)
-  ctx->last_launches = 2 + (cull ? 5 : (inter ? 1 : 0));
+  ctx->last_launches = one ? 1 : 2 + (cull ? 5 : (inter ? 1 : 0));
   PairPlan plan{};
   int C = 1;
   int r;
   if (inter && !use_grid) {
     if (B == 1) {
-      C = std::max(1, (ctx->prot.P + 255) / 256);
+      C = one ? 1 : std::max(1, (ctx->prot.P + 255) / 256);
     } else if (cull) {
       if ((r = cull_plan_for(ctx, B, grad))) return r;
     } else {
@@ -1109,6 +1137,7 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
   }
   if ((r = ensure_scratch(ctx, B, L, C, grad))) return r;
   if (cull && (r = ensure_cull_scratch(ctx, B, L, grad))) return r;
+  if (one && (r = ensure_one_scratch(ctx, L))) return r;
   PoseIO io{};
   io.dofs = d_dofs;
   io.E = d_E;
@@ -1127,6 +1156,31 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
   ctx->cs.first_wait_polls = ctx->first_wait_polls;
   const bool prof = ctx->profiling;
   auto mark = [&](int k) { return prof ? cudaEventRecord(ctx->ev[k], st) : cudaSuccess; };
+  if (one) {  // the whole call is the "sweep" stage of the stage timings
+    MMO_CK(mark(0), "event");
+    MMO_CK(mark(1), "event");
+    MMO_CK(mark(2), "event");
+    int stage = 0;
+    const cudaError_t pending = cudaGetLastError();
+    if (pending != cudaSuccess)
+      return cuda_fail(ctx, pending, "error left by an earlier runtime call");
+    const cudaError_t e1 =
+        launch_one_pose(ctx->lig, ctx->prot, ctx->d_tab4, io, ctx->scr, ctx->one, fl, ctx->ph, st,
+                        &stage);
+    if (e1 != cudaSuccess) {
+      char what[96];
+      snprintf(what, sizeof what, "one-pose kernel (%s, %d bytes of shared memory)",
+               stage == 1 ? "shared-memory attribute" : "launch",
+               one_pose_smem(ctx->lig.L, ctx->lig.nrb));
+      return cuda_fail(ctx, e1, what);
+    }
+    MMO_CK(mark(3), "event");
+    if (prof) {
+      MMO_CK(mark(4), "event");
+      ctx->ev_valid = true;
+    }
+    return MMO_OK;
+  }
   MMO_CK(mark(0), "event");
   MMO_CK(launch_rebuild(ctx->lig, io, ctx->scr, fl, st), "rebuild kernel");
   MMO_CK(mark(1), "event");
@@ -1669,6 +1723,9 @@ int mmo_ctx_destroy(mmo_ctx* ctx) {
   cudaFree(ctx->d_cull);
   cudaFree(ctx->d_piece);
   cudaFree(ctx->d_pbox);
+  cudaFree(ctx->one.E);
+  cudaFree(ctx->one.G);
+  cudaFree(ctx->one.arrive);
   cudaFree(ctx->cs.gcount);
   cudaFree(ctx->cs.glist);
   cudaFree(ctx->cs.items);
@@ -2593,6 +2650,29 @@ int mmo_diag_set_wait_polls(mmo_ctx* ctx, long long polls) {
     return fail(ctx, MMO_EINVAL, "mmo_diag_set_wait_polls: %lld polls above 2^32 - 1", polls);
   ctx->first_wait_polls = polls < 0 ? kWaitPollsDefault : (uint32_t)polls;
   ++ctx->epoch;  // graphs captured with the old limit are rebuilt
+  return MMO_OK;
+}
+
+int mmo_diag_sincos(mmo_ctx* ctx, int n, const float* x, float* out) {
+  if (!ctx) return MMO_EINVAL;
+  if (n < 0 || (n > 0 && (!x || !out)))
+    return fail(ctx, MMO_EINVAL, "mmo_diag_sincos: bad arguments");
+  if (n == 0) return MMO_OK;
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  float* dx = nullptr;
+  float4* dout = nullptr;
+  cudaError_t e = cudaMalloc(&dx, sizeof(float) * (size_t)n);
+  if (e == cudaSuccess) e = cudaMalloc(&dout, sizeof(float4) * (size_t)n);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dx, x, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = launch_df_sincos(dx, n, dout, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out, dout, sizeof(float4) * (size_t)n, cudaMemcpyDeviceToHost,
+                        ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(dx);
+  cudaFree(dout);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "mmo_diag_sincos");
   return MMO_OK;
 }
 

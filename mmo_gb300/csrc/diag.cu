@@ -1,5 +1,7 @@
 // diag.cu -- FP32 FMA throughput probe (the denominator of the pair kernel's
-// roofline fraction): independent FMA chains, no memory traffic.
+// roofline fraction): independent FMA chains, no memory traffic; and the
+// double-float sine and cosine (df_sincos) over an array, for its accuracy
+// check.
 #include "mmo_internal.cuh"
 
 namespace mmo {
@@ -26,7 +28,22 @@ __global__ void __launch_bounds__(256) k_fma_peak(float* out, int iters, float s
   if (s == -1.0f) out[0] = s;  // never true; keeps the chains live
 }
 
+// out[4 i .. 4 i + 3] = sin(x_i) hi, lo, cos(x_i) hi, lo from df_sincos
+__global__ void k_df_sincos(const float* x, int n, float4* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float2 s, c;
+  df_sincos(x[i], s, c);
+  out[i] = make_float4(s.x, s.y, c.x, c.y);
+}
+
 }  // namespace
+
+cudaError_t launch_df_sincos(const float* x, int n, float4* out, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_df_sincos<<<(n + 255) / 256, 256, 0, st>>>(x, n, out);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_fma_peak(int sms, int iters, float* out, cudaStream_t st, double* flops) {
   const int blocks = sms * 8, threads = 256;

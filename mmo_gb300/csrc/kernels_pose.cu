@@ -25,44 +25,16 @@ constexpr int kFinishBlocksPerSM = 7;  // resident finish blocks: 4,096 poses in
 // ---------------------------------------------------------------------------
 // k_rebuild
 // ---------------------------------------------------------------------------
-// Double-float arithmetic: a value is an unevaluated pair h + l of floats
-// (|l| <= ulp(h) / 2), about 48 significant bits, on the FP32 pipe (GB300's
-// FP64 rate is 1/64 of its FP32 rate).  ts / qts are the error-free sums
-// (TwoSum, and Fast2Sum for |a| >= |b|); the products take their error by FMA.
-__device__ __forceinline__ float2 df_of(double x) {
-  const float h = __double2float_rn(x);
-  return make_float2(h, __double2float_rn(x - (double)h));
+// kStatusTooLong when 0.01 + sqrt(d2) > 12 A (mol.ml:576-591) for the largest
+// squared distance d2 (double-float) from the centroid; the FP64 test runs only
+// near the limit: with |lo| <= ulp(hi) / 2, hi < 143 gives a radius below
+// 11.97 A and hi > 144.5 one above 12.02 A
+__device__ __forceinline__ int too_long_of(float2 d2) {
+  if (d2.x < 143.f) return 0;
+  if (d2.x > 144.5f) return kStatusTooLong;
+  return 0.01 + sqrt((double)d2.x + (double)d2.y) > 12.0 ? kStatusTooLong : 0;
 }
-__device__ __forceinline__ float2 qts(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
-}
-__device__ __forceinline__ float2 ts(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  const float bp = __fsub_rn(s, a);
-  return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp)));
-}
-__device__ __forceinline__ float2 dadd(float2 a, float2 b) {
-  const float2 s = ts(a.x, b.x);
-  return qts(s.x, __fadd_rn(s.y, __fadd_rn(a.y, b.y)));
-}
-__device__ __forceinline__ float2 dneg(float2 a) { return make_float2(-a.x, -a.y); }
-__device__ __forceinline__ float2 dsub(float2 a, float2 b) { return dadd(a, dneg(b)); }
-__device__ __forceinline__ float2 dmul(float2 a, float2 b) {
-  const float p = __fmul_rn(a.x, b.x);
-  return qts(p, fmaf(a.x, b.y, fmaf(a.y, b.x, fmaf(a.x, b.x, -p))));
-}
-// a0 b0 + a1 b1 + a2 b2 + c
-__device__ __forceinline__ float2 ddot3c(float2 a0, float2 b0, float2 a1, float2 b1, float2 a2,
-                                         float2 b2, float2 c) {
-  return dadd(dadd(dadd(dmul(a0, b0), dmul(a1, b1)), dmul(a2, b2)), c);
-}
-__device__ __forceinline__ float2 dshfl_xor(float2 a, int o) {
-  return make_float2(__shfl_xor_sync(kFull, a.x, o), __shfl_xor_sync(kFull, a.y, o));
-}
-__device__ __forceinline__ bool dgt(float2 a, float2 b) {
-  return a.x > b.x || (a.x == b.x && a.y > b.y);
-}
+
 
 __device__ __forceinline__ void store_pair(float4* X, float2 x, float2 y, float2 z) {
   X[0] = make_float4(x.x, y.x, z.x, 0.f);
@@ -114,6 +86,29 @@ __device__ __forceinline__ double rigid_entry(int k, const double* SC, const flo
     case 9: return (double)dof[0] - (double)orx;
     case 10: return (double)dof[1] - (double)ory;
     default: return (double)dof[2] - (double)orz;
+  }
+}
+
+// rigid_entry from the double-float sines and cosines t[0..2] = (sin hi, sin
+// lo, cos hi, cos lo) of a, b, g: the same products in double-float
+__device__ __forceinline__ float2 rigid_entry_df(int k, const float4* t, const float* dof,
+                                                 float orx, float ory, float orz) {
+  const float2 sa = make_float2(t[0].x, t[0].y), ca = make_float2(t[0].z, t[0].w);
+  const float2 sb = make_float2(t[1].x, t[1].y), cb = make_float2(t[1].z, t[1].w);
+  const float2 sg = make_float2(t[2].x, t[2].y), cg = make_float2(t[2].z, t[2].w);
+  switch (k) {
+    case 0: return dmul(cb, cg);
+    case 1: return dsub(dmul(dmul(cg, sa), sb), dmul(ca, sg));
+    case 2: return dadd(dmul(sa, sg), dmul(dmul(ca, cg), sb));
+    case 3: return dmul(cb, sg);
+    case 4: return dadd(dmul(ca, cg), dmul(dmul(sa, sb), sg));
+    case 5: return dsub(dmul(dmul(ca, sb), sg), dmul(cg, sa));
+    case 6: return dneg(sb);
+    case 7: return dmul(cb, sa);
+    case 8: return dmul(ca, cb);
+    case 9: return ts(dof[0], -orx);
+    case 10: return ts(dof[1], -ory);
+    default: return ts(dof[2], -orz);
   }
 }
 
@@ -221,7 +216,7 @@ __device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof
     my = dadd(my, dshfl_xor(my, o));
     mz = dadd(mz, dshfl_xor(mz, o));
   }
-  const float2 iL = df_of(1.0 / L);
+  const float2 iL = make_float2(lig.ilh, lig.ill);  // df_of(1.0 / L)
   mx = dmul(mx, iL);
   my = dmul(my, iL);
   mz = dmul(mz, iL);
@@ -236,7 +231,7 @@ __device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof
     const float2 other = dshfl_xor(d2max, o);
     if (dgt(other, d2max)) d2max = other;
   }
-  const int status = 0.01 + sqrt((double)d2max.x + (double)d2max.y) > 12.0 ? kStatusTooLong : 0;
+  const int status = too_long_of(d2max);
   // rigid map: twelve entries (rotation, translation) split over the pose's lanes
   float2 rm[(12 + TPP - 1) / TPP];
 #pragma unroll
@@ -346,14 +341,12 @@ __device__ __forceinline__ void torsion_frame(const DevLigand& lig, const float4
 // Interacting pair p (i < j): its energy into acc and, when crossing, the
 // torsion terms (dE/dX_moving) . (w_t x (X_moving - C_t)) of every torsion
 // whose group holds exactly one of the two atoms, into col[t * stride].
+// (ij, par: the pair's atoms and parameters; amask: the atoms' group bits)
 template <int DIEL, int IFORM>
-__device__ __forceinline__ void intra_pair_terms(const DevLigand& lig, const float4* sxh,
-                                                 const float4* sxl, const float4* saxis, int p,
-                                                 bool crossing, float& acc, float* col,
-                                                 int stride) {
-  const int nrb = lig.nrb;
-  const int2 ij = lig.pair_ij[p];
-  const float4 par = lig.pair_par[p];
+__device__ __forceinline__ void intra_pair_terms_at(const float4* sxh, const float4* sxl,
+                                                    const float4* saxis, int2 ij, float4 par,
+                                                    const uint32_t* amask, bool crossing,
+                                                    float& acc, float* col, int stride) {
   float ep, dx, dy, dz;
   float4 ih, jh, il, jl;
   const float g =
@@ -361,7 +354,7 @@ __device__ __forceinline__ void intra_pair_terms(const DevLigand& lig, const flo
   acc += ep;
   uint32_t x = __float_as_uint(par.w);  // the torsions the pair straddles
   if (crossing && x) {
-    const uint32_t mi = lig.amask[ij.x];
+    const uint32_t mi = amask[ij.x];
     while (x) {
       const int t = __ffs(x) - 1;
       x &= x - 1;
@@ -380,6 +373,16 @@ __device__ __forceinline__ void intra_pair_terms(const DevLigand& lig, const flo
       col[t * stride] = fmaf(in_i ? g : -g, v, col[t * stride]);
     }
   }
+}
+
+// the same for pair p of the ligand's list
+template <int DIEL, int IFORM>
+__device__ __forceinline__ void intra_pair_terms(const DevLigand& lig, const float4* sxh,
+                                                 const float4* sxl, const float4* saxis, int p,
+                                                 bool crossing, float& acc, float* col,
+                                                 int stride) {
+  intra_pair_terms_at<DIEL, IFORM>(sxh, sxl, saxis, lig.pair_ij[p], lig.pair_par[p], lig.amask,
+                                   crossing, acc, col, stride);
 }
 
 // finish_pose: one warp, one pose.  ep / gp: the pose's inter partials
@@ -707,10 +710,11 @@ __host__ __device__ constexpr int finish_one_f4(int L, int nrb) {
          finish_warp_f4(L, nrb);
 }
 
+// the body of k_finish_one, for a CTA of kFinishOne threads with fsm its
+// finish_one_f4(L, nrb) float4 of shared memory
 template <bool GRAD, bool RECENTER, int DIEL, int IFORM>
-__global__ void __launch_bounds__(kFinishOne)
-    k_finish_one(DevLigand lig, PoseIO io, Scratch scr, int flags) {
-  extern __shared__ __align__(16) float4 fsm[];
+__device__ __forceinline__ void finish_one_cta(const DevLigand& lig, const PoseIO& io,
+                                               const Scratch& scr, int flags, float4* fsm) {
   const int L = lig.L, nrb = lig.nrb, tid = threadIdx.x;
   float4* sxh = fsm;
   float4* sxl = sxh + L;
@@ -756,6 +760,701 @@ __global__ void __launch_bounds__(kFinishOne)
       lig, scr.C, scr.Epart, GRAD ? scr.Gpart : nullptr, scr.X, GRAD ? scr.Y : nullptr,
       GRAD ? scr.rec : nullptr, GRAD ? scr.cen : nullptr, io.dofs, GRAD ? io.grad : nullptr,
       io.E, io.status, io.E_inter, flags, wsm, intra ? sred[kFinishOne / 32] : 0.0, stot);
+}
+
+template <bool GRAD, bool RECENTER, int DIEL, int IFORM>
+__global__ void __launch_bounds__(kFinishOne)
+    k_finish_one(DevLigand lig, PoseIO io, Scratch scr, int flags) {
+  extern __shared__ __align__(16) float4 fsm[];
+  finish_one_cta<GRAD, RECENTER, DIEL, IFORM>(lig, io, scr, flags, fsm);
+}
+
+// ---------------------------------------------------------------------------
+// k_one_pose: the one-pose path (the drop-in) in one launch.
+//   1. every CTA rebuilds the pose.  For nested rotation groups
+//      (DevLigand::nested: every two groups nested or disjoint, each axis
+//      inside the groups that contain its group or on their axes) the
+//      bond-order application of src/optim.ml:68-71 equals applying to each
+//      atom the rotations of its groups about their axes in the reference
+//      conformer, innermost group first: the rotations are built once (a
+//      thread per matrix entry) and every atom applies its own chain.  Other
+//      ligands take the torsions in bond order (the operations of
+//      rebuild_pose), recording what the reverse pass needs;
+//   2. CTA c stages protein atoms [c kOneChunk, (c + 1) kOneChunk) in shared
+//      memory and sums their pair terms against every ligand atom (kFinishOne
+//      / L threads per ligand atom) into per-CTA partials;
+//   3. the last CTA to arrive (an atomic count, nothing waits) adds the
+//      partials in CTA order and finishes the pose.  For nested groups the
+//      derivative of torsion t is a sum over its group in the posed frame,
+//        dE/dtheta_t = w_t . sum_{i in G_t} (X_i - C_t) x (dE/dX_i - F / L)
+//      (w_t the posed axis, C_t the posed centre atom, F the total force; F / L
+//      only with the centroid removed), one warp per torsion, plus the intra
+//      terms of the pairs that straddle the group; other ligands go through
+//      the work buffers and the one-pose finishing code (finish_one_cta).
+// ---------------------------------------------------------------------------
+// shared-memory layout of k_one_pose, byte offsets (16-byte aligned)
+struct OneLayout {
+  int xh, xl, yr, rec, tsc, x, y, z, bonds, gmask, rig, cen, status, rot, ord, gsize, amask, uax;
+  int sp, stype, pe, pg, qe, qg, sE, sG, saxis, sdt, sred, red, total;
+};
+
+__host__ __device__ inline int take16(int& off, int n) {
+  const int p = off;
+  off += (n + 15) / 16 * 16;
+  return p;
+}
+
+__host__ __device__ inline OneLayout one_layout(int L, int nrb) {
+  OneLayout o;
+  int off = 0;
+  o.xh = take16(off, 16 * L);
+  o.xl = take16(off, 16 * L);
+  o.yr = take16(off, 32 * L);
+  o.rec = take16(off, 48 * nrb);
+  o.tsc = take16(off, 16 * (3 + nrb));
+  o.x = take16(off, 8 * L);
+  o.y = take16(off, 8 * L);
+  o.z = take16(off, 8 * L);
+  o.bonds = take16(off, 8 * nrb);
+  o.gmask = take16(off, 4 * nrb * kSlots);
+  o.rig = take16(off, 8 * 12);
+  o.cen = take16(off, 8 * 3);
+  o.status = take16(off, 4);
+  o.rot = take16(off, 8 * 12 * nrb);
+  o.ord = take16(off, 4 * nrb);
+  o.gsize = take16(off, 4 * nrb);
+  o.amask = take16(off, 4 * L);
+  o.uax = take16(off, 8 * 3 * nrb);
+  o.sp = take16(off, 32 * kOneChunk);
+  o.stype = take16(off, 4 * kOneChunk);
+  o.pe = take16(off, 4 * kFinishOne);
+  o.pg = take16(off, 16 * kFinishOne);
+  o.qe = take16(off, 8 * kFinishOne);
+  o.qg = take16(off, 24 * kFinishOne);  // [3][kFinishOne] float2
+  o.sE = take16(off, 8 * L);
+  o.sG = take16(off, 16 * L);
+  o.saxis = take16(off, 32 * nrb);
+  o.sdt = take16(off, 4 * nrb * (kFinishOne + 1));
+  o.sred = take16(off, 8 * (kFinishOne / 32 + 1));
+  o.red = take16(off, 4 * 12);
+  o.total = off;
+  return o;
+}
+
+struct OneSmem {
+  float4 *Xh, *Xl;     // [L] posed coordinates hi, lo
+  float4* Y;           // [L][2] coordinates after the torsions hi, lo (bond-order path)
+  float4* rec;         // [nrb][3] torsion records (bond-order path)
+  float4* tsc;         // [3 + nrb] double-float (sin, cos) of the angles
+  float2 *x, *y, *z;   // [L] double-float coordinates
+  int2* bonds;         // [nrb]
+  uint32_t* gmask;     // [nrb][kSlots]
+  float2* G;           // [12] rigid map
+  float2* cen;         // [3] centroid
+  int* status;
+  float2* rot;         // [nrb][12] reference-frame rotation of each torsion: matrix, centre
+  int* ord;            // [nrb] torsions by group size, smallest first
+  int* gsize;          // [nrb] group sizes
+  uint32_t* amask;     // [L] the groups of each atom (bit t: group t)
+  float2* uax;         // [nrb][3] unit axis of each torsion in the reference conformer
+  float4* sp;          // [kOneChunk][2] the CTA's protein atoms hi (q in w), lo
+  int* stype;          // [kOneChunk] their types
+  float* pe;           // [kFinishOne] per-thread pair sums
+  float4* pg;
+  float2* qe;          // [kFinishOne] per-thread sums of the partials (double-float)
+  float2* qg;          // [3][kFinishOne]
+  float2* sE;          // [L] inter energy per ligand atom (double-float)
+  float4* sG;          // [L] dE/dX per ligand atom (inter terms)
+  float4* saxis;       // [2 nrb] posed axes and centres (torsion_frame)
+  float* sdt;          // [nrb][kFinishOne + 1] straddling intra terms per thread
+  float2* sred;        // [warps] intra energy per warp (double-float)
+  float* red;          // [12] total force and the rigid-map sums
+};
+
+__device__ __forceinline__ OneSmem one_smem(char* base, int L, int nrb) {
+  const OneLayout o = one_layout(L, nrb);
+  OneSmem m;
+  m.Xh = reinterpret_cast<float4*>(base + o.xh);
+  m.Xl = reinterpret_cast<float4*>(base + o.xl);
+  m.Y = reinterpret_cast<float4*>(base + o.yr);
+  m.rec = reinterpret_cast<float4*>(base + o.rec);
+  m.tsc = reinterpret_cast<float4*>(base + o.tsc);
+  m.x = reinterpret_cast<float2*>(base + o.x);
+  m.y = reinterpret_cast<float2*>(base + o.y);
+  m.z = reinterpret_cast<float2*>(base + o.z);
+  m.bonds = reinterpret_cast<int2*>(base + o.bonds);
+  m.gmask = reinterpret_cast<uint32_t*>(base + o.gmask);
+  m.G = reinterpret_cast<float2*>(base + o.rig);
+  m.cen = reinterpret_cast<float2*>(base + o.cen);
+  m.status = reinterpret_cast<int*>(base + o.status);
+  m.rot = reinterpret_cast<float2*>(base + o.rot);
+  m.ord = reinterpret_cast<int*>(base + o.ord);
+  m.gsize = reinterpret_cast<int*>(base + o.gsize);
+  m.amask = reinterpret_cast<uint32_t*>(base + o.amask);
+  m.uax = reinterpret_cast<float2*>(base + o.uax);
+  m.sp = reinterpret_cast<float4*>(base + o.sp);
+  m.stype = reinterpret_cast<int*>(base + o.stype);
+  m.pe = reinterpret_cast<float*>(base + o.pe);
+  m.pg = reinterpret_cast<float4*>(base + o.pg);
+  m.qe = reinterpret_cast<float2*>(base + o.qe);
+  m.qg = reinterpret_cast<float2*>(base + o.qg);
+  m.sE = reinterpret_cast<float2*>(base + o.sE);
+  m.sG = reinterpret_cast<float4*>(base + o.sG);
+  m.saxis = reinterpret_cast<float4*>(base + o.saxis);
+  m.sdt = reinterpret_cast<float*>(base + o.sdt);
+  m.sred = reinterpret_cast<float2*>(base + o.sred);
+  m.red = reinterpret_cast<float*>(base + o.red);
+  return m;
+}
+
+// unit vector (double-float) of the axis a = centre - left, with the inverse
+// length; the operations of rebuild_pose
+__device__ __forceinline__ void unit_axis(float2 ax, float2 ay, float2 az, float2& ux, float2& uy,
+                                          float2& uz, float2& inv) {
+  const float2 one = make_float2(1.f, 0.f);
+  const float2 n2 = dadd(dadd(dmul(ax, ax), dmul(ay, ay)), dmul(az, az));
+  const float r0 = rsqrtf(n2.x);
+  const float2 err = dsub(one, dmul(n2, dmul(make_float2(r0, 0.f), make_float2(r0, 0.f))));
+  inv = qts(r0, __fmul_rn(0.5f * r0, err.x));
+  ux = dmul(ax, inv);
+  uy = dmul(ay, inv);
+  uz = dmul(az, inv);
+}
+
+// unit axis of the bond (left, centre) from the coordinates in shared memory
+__device__ __forceinline__ void one_axis(const OneSmem& m, int2 bd, float2& ux, float2& uy,
+                                         float2& uz, float2& inv) {
+  unit_axis(dsub(m.x[bd.y], m.x[bd.x]), dsub(m.y[bd.y], m.y[bd.x]), dsub(m.z[bd.y], m.z[bd.x]),
+            ux, uy, uz, inv);
+}
+
+// Reference conformer, the angles' sines and cosines (FP64, as rebuild_pose),
+// the rigid map and the topology into shared memory.  For nested groups also
+// the group sizes and, in warps 2-3 while warp 0 takes the FP64 sines and
+// cosines, each torsion's unit axis and centre in the reference conformer.
+__device__ __forceinline__ void one_load(const DevLigand& lig, const float* dof, float orx,
+                                         float ory, float orz, const OneSmem& m) {
+  const int tid = threadIdx.x, L = lig.L, nrb = lig.nrb;
+  if (tid < 32) {
+    for (int a = tid; a < 3 + nrb; a += 32) {
+      float2 sn, cs;
+      df_sincos(dof[3 + a], sn, cs);
+      m.tsc[a] = make_float4(sn.x, sn.y, cs.x, cs.y);
+    }
+    __syncwarp();
+    // rigid map: twelve entries (rotation, translation)
+    if (tid < 12) m.G[tid] = rigid_entry_df(tid, m.tsc, dof, orx, ory, orz);
+  } else if (lig.nested && tid >= 64 && tid < 64 + nrb) {
+    const int t = tid - 64;
+    const int2 bd = lig.bonds[t];
+    const float2 cx = lig.ref2[3 * bd.y], cy = lig.ref2[3 * bd.y + 1], cz = lig.ref2[3 * bd.y + 2];
+    const float2 lx = lig.ref2[3 * bd.x], ly = lig.ref2[3 * bd.x + 1], lz = lig.ref2[3 * bd.x + 2];
+    float2 ux, uy, uz, inv;
+    unit_axis(dsub(cx, lx), dsub(cy, ly), dsub(cz, lz), ux, uy, uz, inv);
+    float2* r = m.rot + 12 * t;
+    r[9] = cx;
+    r[10] = cy;
+    r[11] = cz;
+    m.uax[3 * t] = ux;
+    m.uax[3 * t + 1] = uy;
+    m.uax[3 * t + 2] = uz;
+  }
+  if (tid < L) {
+    m.x[tid] = lig.ref2[3 * tid];
+    m.y[tid] = lig.ref2[3 * tid + 1];
+    m.z[tid] = lig.ref2[3 * tid + 2];
+    m.amask[tid] = lig.amask[tid];
+  }
+  for (int k = tid; k < nrb; k += blockDim.x) {
+    m.bonds[k] = lig.bonds[k];
+    if (lig.nested) {
+      int s = 0;
+      for (int w = 0; w < kSlots; ++w) s += __popc(lig.gmask[k * kSlots + w]);
+      m.gsize[k] = s;
+    }
+  }
+  for (int k = tid; k < nrb * kSlots; k += blockDim.x) m.gmask[k] = lig.gmask[k];
+}
+
+// posed coordinates of atom a from its coordinates after the torsions
+template <bool RECENTER>
+__device__ __forceinline__ void one_posed(const OneSmem& m, int a, float2 x, float2 y, float2 z) {
+  const float2 zero = make_float2(0.f, 0.f);
+  const float2 vx = RECENTER ? dsub(x, m.cen[0]) : x, vy = RECENTER ? dsub(y, m.cen[1]) : y,
+               vz = RECENTER ? dsub(z, m.cen[2]) : z;
+  (void)zero;
+  const float2 px = ddot3c(m.G[0], vx, m.G[1], vy, m.G[2], vz, m.G[9]);
+  const float2 py = ddot3c(m.G[3], vx, m.G[4], vy, m.G[5], vz, m.G[10]);
+  const float2 pz = ddot3c(m.G[6], vx, m.G[7], vy, m.G[8], vz, m.G[11]);
+  m.Xh[a] = make_float4(px.x, py.x, pz.x, 0.f);
+  m.Xl[a] = make_float4(px.y, py.y, pz.y, 0.f);
+}
+
+// warp 0: the centroid of the coordinates after the torsions (rebuild_pose's
+// order for a pose of 32 lanes: atom a on lane a % 32, then the xor tree)
+__device__ __forceinline__ void one_centroid(const DevLigand& lig, const OneSmem& m) {
+  const int lane = threadIdx.x & 31, L = lig.L;
+  float2 mx = make_float2(0.f, 0.f), my = mx, mz = mx;
+  for (int a = lane; a < L; a += 32) {
+    mx = dadd(mx, m.x[a]);
+    my = dadd(my, m.y[a]);
+    mz = dadd(mz, m.z[a]);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = dadd(mx, dshfl_xor(mx, o));
+    my = dadd(my, dshfl_xor(my, o));
+    mz = dadd(mz, dshfl_xor(mz, o));
+  }
+  const float2 iL = make_float2(lig.ilh, lig.ill);  // df_of(1.0 / L)
+  if (lane == 0) {
+    m.cen[0] = dmul(mx, iL);
+    m.cen[1] = dmul(my, iL);
+    m.cen[2] = dmul(mz, iL);
+  }
+}
+
+// warp 0, after one_centroid: the enclosing radius, max_i (0.01 + |c - y_i|)
+// > 12 (mol.ml:576-591), into the status
+__device__ __forceinline__ void one_radius(const DevLigand& lig, const OneSmem& m) {
+  const int lane = threadIdx.x & 31, L = lig.L;
+  __syncwarp();
+  const float2 mx = m.cen[0], my = m.cen[1], mz = m.cen[2];
+  float2 d2max = make_float2(0.f, 0.f);
+  for (int a = lane; a < L; a += 32) {
+    const float2 dx = dsub(mx, m.x[a]), dy = dsub(my, m.y[a]), dz = dsub(mz, m.z[a]);
+    const float2 d2 = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
+    if (dgt(d2, d2max)) d2max = d2;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float2 other = dshfl_xor(d2max, o);
+    if (dgt(other, d2max)) d2max = other;
+  }
+  if (lane == 0) *m.status = too_long_of(d2max);
+}
+
+// Nested groups: the rotation of each torsion about its reference-frame axis
+// (a thread per matrix entry), the group order, then each atom's chain of
+// rotations, innermost group first, and (without the centroid) its posed
+// coordinates.
+template <bool RECENTER>
+__device__ __forceinline__ void one_torsions_nested(const DevLigand& lig, const OneSmem& m) {
+  const int tid = threadIdx.x, L = lig.L, nrb = lig.nrb;
+  if (tid < nrb) {  // rank by group size (a contained group is smaller)
+    const int s = m.gsize[tid];
+    int r = 0;
+    for (int u = 0; u < nrb; ++u) {
+      const int su = m.gsize[u];
+      r += su < s || (su == s && u < tid);
+    }
+    m.ord[r] = tid;
+  }
+  for (int e = tid; e < 9 * nrb; e += blockDim.x) {
+    const int t = e / 9, k = e - 9 * t;
+    const float2 ux = m.uax[3 * t], uy = m.uax[3 * t + 1], uz = m.uax[3 * t + 2];
+    const float4 tsc = m.tsc[3 + t];
+    const float2 sn = make_float2(tsc.x, tsc.y), cs = make_float2(tsc.z, tsc.w);
+    const float2 o = dsub(make_float2(1.f, 0.f), cs);
+    m.rot[12 * t + k] =
+        rodrigues_entry(k, cs, ux, uy, uz, o, dmul(ux, sn), dmul(uy, sn), dmul(uz, sn));
+  }
+  __syncthreads();
+  if (tid < L) {
+    const uint32_t am = m.amask[tid];
+    float2 x = m.x[tid], y = m.y[tid], z = m.z[tid];
+    for (int k = 0; k < nrb; ++k) {
+      const int t = m.ord[k];
+      if ((am >> t) & 1u) {
+        const float2* R = m.rot + 12 * t;
+        const float2 vx = dsub(x, R[9]), vy = dsub(y, R[10]), vz = dsub(z, R[11]);
+        x = ddot3c(R[0], vx, R[1], vy, R[2], vz, R[9]);
+        y = ddot3c(R[3], vx, R[4], vy, R[5], vz, R[10]);
+        z = ddot3c(R[6], vx, R[7], vy, R[8], vz, R[11]);
+      }
+    }
+    m.x[tid] = x;
+    m.y[tid] = y;
+    m.z[tid] = z;
+    if (!RECENTER) one_posed<false>(m, tid, x, y, z);
+  }
+  __syncthreads();
+  if (RECENTER) {
+    if (tid < 32) one_centroid(lig, m);
+    __syncthreads();
+    if (tid < L) one_posed<true>(m, tid, m.x[tid], m.y[tid], m.z[tid]);
+    __syncthreads();
+  }
+}
+
+// Other ligands: the torsions in bond order, each rotating its group about
+// the current axis (every thread recomputes the axis and its atom's matrix),
+// with the records of the reverse pass when RECORD; then the centroid, the
+// status and the posed coordinates.
+template <bool RECENTER, bool RECORD>
+__device__ __forceinline__ void one_torsions_seq(const DevLigand& lig, const OneSmem& m) {
+  const int tid = threadIdx.x, L = lig.L, nrb = lig.nrb;
+  for (int t = 0; t < nrb; ++t) {
+    const int2 bd = m.bonds[t];
+    const bool mine = tid < L && ((m.gmask[t * kSlots + (tid >> 5)] >> (tid & 31)) & 1u);
+    if (mine || (RECORD && tid == 0)) {
+      const float2 cx = m.x[bd.y], cy = m.y[bd.y], cz = m.z[bd.y];
+      float2 ux, uy, uz, inv;
+      one_axis(m, bd, ux, uy, uz, inv);
+      const float4 tsc = m.tsc[3 + t];
+      const float2 sn = make_float2(tsc.x, tsc.y), cs = make_float2(tsc.z, tsc.w);
+      if (mine) {
+        const float2 o = dsub(make_float2(1.f, 0.f), cs);
+        const float2 xs = dmul(ux, sn), ys = dmul(uy, sn), zs = dmul(uz, sn);
+        float2 R[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) R[k] = rodrigues_entry(k, cs, ux, uy, uz, o, xs, ys, zs);
+        // the axis atoms are outside the group: no thread of the group reads a
+        // coordinate another one writes
+        const float2 vx = dsub(m.x[tid], cx), vy = dsub(m.y[tid], cy), vz = dsub(m.z[tid], cz);
+        m.x[tid] = ddot3c(R[0], vx, R[1], vy, R[2], vz, cx);
+        m.y[tid] = ddot3c(R[3], vx, R[4], vy, R[5], vz, cy);
+        m.z[tid] = ddot3c(R[6], vx, R[7], vy, R[8], vz, cz);
+      }
+      if (RECORD && tid == 0) {
+        m.rec[3 * t] = make_float4(cx.x, cy.x, cz.x, cs.x);
+        m.rec[3 * t + 1] = make_float4(ux.x, uy.x, uz.x, sn.x);
+        m.rec[3 * t + 2] = make_float4(inv.x, cx.y, cy.y, cz.y);
+      }
+    }
+    __syncthreads();  // the rotated group is visible before the next axis is read
+  }
+  if (RECORD && tid < L) {
+    m.Y[2 * tid] = make_float4(m.x[tid].x, m.y[tid].x, m.z[tid].x, 0.f);
+    m.Y[2 * tid + 1] = make_float4(m.x[tid].y, m.y[tid].y, m.z[tid].y, 0.f);
+  }
+  if (tid < 32) {
+    one_centroid(lig, m);
+    one_radius(lig, m);
+  }
+  __syncthreads();
+  if (tid < L) one_posed<RECENTER>(m, tid, m.x[tid], m.y[tid], m.z[tid]);
+  __syncthreads();
+}
+
+// kPairBatch interacting pairs of one thread (pairs p0, p0 + kFinishOne, ...),
+// loaded together so that their latencies overlap
+constexpr int kPairBatch = 4;
+struct PairBatch {
+  int2 ij[kPairBatch];
+  float4 par[kPairBatch];
+};
+
+__device__ __forceinline__ void load_pairs(const DevLigand& lig, int p0, PairBatch& b) {
+#pragma unroll
+  for (int u = 0; u < kPairBatch; ++u) {
+    const int p = p0 + u * kFinishOne;
+    b.ij[u] = p < lig.npairs ? lig.pair_ij[p] : make_int2(0, 0);
+    b.par[u] = p < lig.npairs ? lig.pair_par[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+// The finish of a pose with nested groups, from shared memory: energy,
+// status and (GRAD) the gradient with the torsion derivatives summed in the
+// posed frame.  pb: the thread's first batch of pairs, already loaded.
+template <bool GRAD, bool RECENTER, int DIEL, int IFORM>
+__device__ __forceinline__ void finish_one_nested(const DevLigand& lig, const PoseIO& io,
+                                                  const OneSmem& m, int flags, PairBatch& pb) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, L = lig.L, nrb = lig.nrb;
+  constexpr int kWarps = kFinishOne / 32;
+  const bool intra = flags & kFlagIntra;
+  const bool crossing = GRAD && intra && nrb > 0;
+  if (GRAD && tid < nrb) torsion_frame(lig, m.Xh, m.Xl, m.saxis, tid);
+  if (crossing)
+    for (int k = tid; k < nrb * (kFinishOne + 1); k += kFinishOne) m.sdt[k] = 0.f;
+  __syncthreads();
+  if (intra) {
+    float acc = 0.f;
+    for (int p0 = tid; p0 < lig.npairs; p0 += kPairBatch * kFinishOne) {
+      if (p0 != tid) load_pairs(lig, p0, pb);
+#pragma unroll
+      for (int u = 0; u < kPairBatch; ++u)
+        if (p0 + u * kFinishOne < lig.npairs)
+          intra_pair_terms_at<DIEL, IFORM>(m.Xh, m.Xl, m.saxis, pb.ij[u], pb.par[u], m.amask,
+                                           crossing, acc, m.sdt + tid, kFinishOne + 1);
+    }
+    float2 w = make_float2(acc, 0.f);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) w = dadd(w, dshfl_xor(w, o));
+    if (lane == 0) m.sred[warp] = w;
+  }
+  if (GRAD) {
+    // total force (q < 3) and M_rc = sum_i G_ir Yc_ic (q = 3 + 3 r + c), Yc
+    // the coordinates after the torsions less the rotation origin
+    for (int q = warp; q < 12; q += kWarps) {
+      float s = 0.f;
+      for (int a = lane; a < L; a += 32) {
+        const float4 g = m.sG[a];
+        if (q < 3) {
+          s += q == 0 ? g.x : (q == 1 ? g.y : g.z);
+        } else {
+          const int r = (q - 3) / 3, c = q - 3 - 3 * r;
+          const float gr = r == 0 ? g.x : (r == 1 ? g.y : g.z);
+          const float2 yv = c == 0 ? m.x[a] : (c == 1 ? m.y[a] : m.z[a]);
+          const float2 ce = RECENTER ? m.cen[c] : make_float2(0.f, 0.f);
+          s += gr * split_diff(yv.x, yv.y, ce.x, ce.y);
+        }
+      }
+      s = warp_sum(s);
+      if (lane == 0) m.red[q] = s;
+    }
+  }
+  __syncthreads();
+  if (warp == 0) {  // double-float sums; FP64 only for the outputs
+    float2 ei = make_float2(0.f, 0.f);
+    if (flags & kFlagInter)
+      for (int a = lane; a < L; a += 32) ei = dadd(ei, m.sE[a]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ei = dadd(ei, dshfl_xor(ei, o));
+    if (lane == 0) {
+      float2 t = ei;
+      if (intra)
+        for (int k = 0; k < kWarps; ++k) t = dadd(t, m.sred[k]);
+      const double e = (double)t.x + (double)t.y;
+      io.E[0] = e;
+      io.status[0] = *m.status | (isfinite(e) ? 0 : kStatusNonFinite);
+      if (io.E_inter) io.E_inter[0] = (double)ei.x + (double)ei.y;
+    }
+  }
+  if (!GRAD) return;
+  const float* M = m.red + 3;
+  if (tid == 32) {  // the rigid map: translation, then d R / d a, d b, d g of rot.ml:52-66
+    float sa, ca, sb, cb, sg, cg;
+    sincosf(io.dofs[3], &sa, &ca);
+    sincosf(io.dofs[4], &sb, &cb);
+    sincosf(io.dofs[5], &sg, &cg);
+    const float dA[9] = {0.f, cg * ca * sb + sa * sg, ca * sg - sa * cg * sb,
+                         0.f, -sa * cg + ca * sb * sg, -sa * sb * sg - cg * ca,
+                         0.f, cb * ca, -sa * cb};
+    const float dB[9] = {-sb * cg, cg * sa * cb, ca * cg * cb,
+                         -sb * sg, sa * cb * sg, ca * cb * sg,
+                         -cb, -sb * sa, -ca * sb};
+    const float dG[9] = {-cb * sg, -sg * sa * sb - ca * cg, sa * cg - ca * sg * sb,
+                         cb * cg, -ca * sg + sa * sb * cg, ca * sb * cg + sg * sa,
+                         0.f, 0.f, 0.f};
+    float ga = 0.f, gb = 0.f, gg = 0.f;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      ga += M[k] * dA[k];
+      gb += M[k] * dB[k];
+      gg += M[k] * dG[k];
+    }
+    io.grad[0] = m.red[0];
+    io.grad[1] = m.red[1];
+    io.grad[2] = m.red[2];
+    io.grad[3] = ga;
+    io.grad[4] = gb;
+    io.grad[5] = gg;
+  }
+  const float iL = 1.0f / (float)L;
+  const float fx = RECENTER ? m.red[0] * iL : 0.f, fy = RECENTER ? m.red[1] * iL : 0.f,
+              fz = RECENTER ? m.red[2] * iL : 0.f;
+  for (int t = warp; t < nrb; t += kWarps) {
+    float d = 0.f;  // the straddling intra terms, in a fixed order
+    if (crossing) {
+      for (int k = lane; k < kFinishOne; k += 32) d += m.sdt[t * (kFinishOne + 1) + k];
+      d = warp_sum(d);
+    }
+    const float4 w = m.saxis[t];
+    const int ci = __float_as_int(w.w);
+    const float4 ch = m.Xh[ci], cl = m.Xl[ci];
+    float tx = 0.f, ty = 0.f, tz = 0.f;
+    for (int a = lane; a < L; a += 32) {
+      if ((m.gmask[t * kSlots + (a >> 5)] >> (a & 31)) & 1u) {
+        const float4 g = m.sG[a];
+        const float gx = g.x - fx, gy = g.y - fy, gz = g.z - fz;
+        const float4 ah = m.Xh[a], al = m.Xl[a];
+        // the lever X_i - C_t from the hi/lo pairs
+        const float lx = split_diff(ah.x, al.x, ch.x, cl.x);
+        const float ly = split_diff(ah.y, al.y, ch.y, cl.y);
+        const float lz = split_diff(ah.z, al.z, ch.z, cl.z);
+        tx += ly * gz - lz * gy;
+        ty += lz * gx - lx * gz;
+        tz += lx * gy - ly * gx;
+      }
+    }
+    tx = warp_sum(tx);
+    ty = warp_sum(ty);
+    tz = warp_sum(tz);
+    if (lane == 0) io.grad[6 + t] = w.x * tx + w.y * ty + w.z * tz + d;
+  }
+}
+
+// static shared memory of k_one_pose (type table and flag), rounded up
+constexpr int kOneStatic = 2048;
+static_assert(sizeof(float2) * kNTypes * kNTypes + 16 <= kOneStatic, "k_one_pose static smem");
+
+template <bool GRAD, bool RECENTER, int DIEL, int FORM, int IFORM>
+__global__ void __launch_bounds__(kFinishOne)
+    k_one_pose(DevLigand lig, DevProtein prot, const float4* __restrict__ tab4, PoseIO io,
+               Scratch scr, OneScratch os, int flags) {
+  extern __shared__ __align__(16) float4 osm[];
+  __shared__ float2 stab[kNTypes * kNTypes];
+  __shared__ int s_last;
+  const int tid = threadIdx.x, L = lig.L, nrb = lig.nrb;
+  const bool nested = lig.nested;
+  const OneSmem m = one_smem(reinterpret_cast<char*>(osm), L, nrb);
+  if (blockIdx.x == 0 && tid == 0 && io.zero_err) *io.err = 0;
+  // this CTA's protein atoms and the pair table: their loads overlap the rebuild
+  const int c = blockIdx.x, c0 = c * kOneChunk, n = min(kOneChunk, prot.P - c0);
+  if (tid < n) {
+    m.sp[2 * tid] = prot.atoms[2 * (c0 + tid)];
+    m.sp[2 * tid + 1] = prot.atoms[2 * (c0 + tid) + 1];
+    m.stype[tid] = prot.type[c0 + tid];
+  }
+  for (int k = tid; k < kNTypes * kNTypes; k += blockDim.x) {
+    const float4 v = tab4[k];  // (X, 1 / D, x^2, D)
+    stab[k] = make_float2(v.z, v.w);
+  }
+  const int S = kFinishOne / L;  // threads per ligand atom in the pair sums
+  const int j = tid % L, g = tid / L;
+  const float qj = g < S ? lig.q[j] : 0.f;
+  const int lt = g < S ? lig.type[j] : 0;
+  one_load(lig, io.dofs, io.ox, io.oy, io.oz, m);
+  __syncthreads();
+  if (nested) {
+    one_torsions_nested<RECENTER>(lig, m);  // the status waits for the last CTA
+  } else {
+    one_torsions_seq<RECENTER, GRAD>(lig, m);
+  }
+  // the pair terms of this CTA's protein atoms
+  if (g < S) {
+    const float4 xh = m.Xh[j], xl = m.Xl[j];
+    float ae = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+    for (int i = g; i < n; i += S) {
+      const float4 p = m.sp[2 * i], pl = m.sp[2 * i + 1];
+      const float2 xd = stab[m.stype[i] * kNTypes + lt];
+      uff_pair<GRAD, DIEL, FORM>(split_diff(xh.x, xl.x, p.x, pl.x),
+                                 split_diff(xh.y, xl.y, p.y, pl.y),
+                                 split_diff(xh.z, xl.z, p.z, pl.z), xd.x, xd.y, p.w * qj, ae, gx,
+                                 gy, gz);
+    }
+    m.pe[tid] = ae;
+    m.pg[tid] = make_float4(gx, gy, gz, 0.f);
+  }
+  __syncthreads();
+  if (tid < L) {
+    float2 e = make_float2(0.f, 0.f);
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    for (int k = 0; k < S; ++k) {
+      acc2(e, m.pe[k * L + tid]);
+      if (GRAD) {
+        const float4 p = m.pg[k * L + tid];
+        sx += p.x;
+        sy += p.y;
+        sz += p.z;
+      }
+    }
+    os.E[(size_t)c * L + tid] = e;
+    if (GRAD) os.G[(size_t)c * L + tid] = make_float4(sx, sy, sz, 0.f);
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) s_last = atomicAdd(os.arrive, 1u) == (unsigned)gridDim.x - 1u;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  PairBatch pb;  // the first intra pairs of the finish, loaded ahead
+  if (nested && (flags & kFlagIntra)) load_pairs(lig, tid, pb);
+  // the last CTA: the partials of every CTA, thread (j, g) over CTAs g, g + S, ...
+  const int ncta = gridDim.x;
+  // (double-float sums on the FP32 pipe; loads in batches of kBatch)
+  constexpr int kBatch = 10;
+  const float2 z2 = make_float2(0.f, 0.f);
+  float2 e = z2, sx = z2, sy = z2, sz = z2;
+  float2 ev[kBatch];
+  float4 gv[kBatch];
+  // threads (jq, gq), gq < Sq, over CTAs gq, gq + Sq, ...; the last warp is
+  // left free for the status
+  const int Sq = (kFinishOne - 32) / L;
+  const int jq = tid % L, gq = tid / L;
+  const bool summing = gq < Sq;
+  int k0 = gq;
+  auto load_batch = [&]() {
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int k = k0 + u * Sq;
+      ev[u] = k < ncta ? __ldcg(os.E + (size_t)k * L + jq) : z2;
+      if (GRAD)
+        gv[u] = k < ncta ? __ldcg(os.G + (size_t)k * L + jq) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  };
+  if (summing) load_batch();
+  // nested groups: the last warp (whole) takes the status meanwhile
+  if (nested && tid >= kFinishOne - 32) {
+    if (!RECENTER) one_centroid(lig, m);
+    one_radius(lig, m);
+  }
+  if (summing) {
+    while (k0 < ncta) {
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        e = dadd(e, ev[u]);
+        if (GRAD) {
+          acc2(sx, gv[u].x);
+          acc2(sy, gv[u].y);
+          acc2(sz, gv[u].z);
+        }
+      }
+      k0 += kBatch * Sq;
+      if (k0 < ncta) load_batch();
+    }
+    m.qe[tid] = e;
+    if (GRAD) {
+      m.qg[tid] = sx;
+      m.qg[kFinishOne + tid] = sy;
+      m.qg[2 * kFinishOne + tid] = sz;
+    }
+  }
+  __syncthreads();
+  if (tid < L) {
+    const float2 z2 = make_float2(0.f, 0.f);
+    float2 e = z2, sx = z2, sy = z2, sz = z2;
+    for (int k = 0; k < Sq; ++k) {
+      e = dadd(e, m.qe[k * L + tid]);
+      if (GRAD) {
+        sx = dadd(sx, m.qg[k * L + tid]);
+        sy = dadd(sy, m.qg[kFinishOne + k * L + tid]);
+        sz = dadd(sz, m.qg[2 * kFinishOne + k * L + tid]);
+      }
+    }
+    m.sE[tid] = e;
+    if (GRAD)
+      m.sG[tid] = make_float4(__fadd_rn(sx.x, sx.y), __fadd_rn(sy.x, sy.y),
+                              __fadd_rn(sz.x, sz.y), 0.f);
+  }
+  if (tid == 0) *os.arrive = 0u;  // ready for the next launch
+  __syncthreads();
+  if (nested) {
+    finish_one_nested<GRAD, RECENTER, DIEL, IFORM>(lig, io, m, flags, pb);
+    return;
+  }
+  // other ligands: the work buffers of the one-pose finishing code
+  for (int a = tid; a < L; a += blockDim.x) {
+    scr.Epart[a] = (double)m.sE[a].x + (double)m.sE[a].y;
+    if (GRAD) scr.Gpart[a] = m.sG[a];
+    scr.X[2 * a] = m.Xh[a];
+    scr.X[2 * a + 1] = m.Xl[a];
+    if (GRAD) {
+      scr.Y[2 * a] = m.Y[2 * a];
+      scr.Y[2 * a + 1] = m.Y[2 * a + 1];
+    }
+  }
+  if (GRAD) {
+    for (int k = tid; k < 3 * nrb; k += blockDim.x) scr.rec[k] = m.rec[k];
+    if (tid == 0) {
+      scr.cen[0] = make_float4(m.cen[0].x, m.cen[1].x, m.cen[2].x, 0.f);
+      scr.cen[1] = make_float4(m.cen[0].y, m.cen[1].y, m.cen[2].y, 0.f);
+    }
+  }
+  if (tid == 0) io.status[0] = *m.status;
+  __syncthreads();  // the buffers above are written before the finish reads them
+  finish_one_cta<GRAD, RECENTER, DIEL, IFORM>(lig, io, scr, flags, osm);
 }
 
 // one warp: sum of n FP64 partials
@@ -904,7 +1603,7 @@ template <bool G, bool RC, int DIEL, int IFORM>
 cudaError_t sys_finish_t(const DevSystems& S, int nblk, const PoseIO& io, const Scratch& s,
                          int flags, cudaStream_t st) {
   const int smem = kWarpsPerBlock * finish_warp_f4(S.Lmax, S.nrbmax) * (int)sizeof(float4);
-  if (smem > 48 * 1024) {
+  if (smem + (int)sizeof(DevLigand) > 48 * 1024) {  // the opt-in counts the static slig
     const cudaError_t e = cudaFuncSetAttribute(k_sys_finish<G, RC, DIEL, IFORM>,
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
@@ -931,6 +1630,58 @@ cudaError_t launch_rebuild(const DevLigand& lig, const PoseIO& io, const Scratch
                      : rebuild_tpp<true, false>(tpp, lig, io, s, st);
   return rec ? rebuild_tpp<false, true>(tpp, lig, io, s, st)
              : rebuild_tpp<false, false>(tpp, lig, io, s, st);
+}
+
+namespace {
+
+template <bool G, bool RC, int D, int F, int IF>
+cudaError_t one_t(const DevLigand& lig, const DevProtein& prot, const float4* tab4,
+                  const PoseIO& io, const Scratch& s, const OneScratch& os, int flags, int smem,
+                  cudaStream_t st, int* stage) {
+  *stage = 1;
+  // the opt-in counts the static type table too (kOneStatic bytes)
+  if (smem + kOneStatic > 48 * 1024) {
+    const cudaError_t e = cudaFuncSetAttribute(k_one_pose<G, RC, D, F, IF>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+  }
+  *stage = 2;
+  k_one_pose<G, RC, D, F, IF><<<os.ncta, kFinishOne, smem, st>>>(lig, prot, tab4, io, s, os, flags);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+int one_pose_smem(int L, int nrb) {
+  return std::max(one_layout(L, nrb).total, finish_one_f4(L, nrb) * (int)sizeof(float4)) +
+         kOneStatic;
+}
+
+cudaError_t launch_one_pose(const DevLigand& lig, const DevProtein& prot, const float4* tab4,
+                            const PoseIO& io, const Scratch& s, const OneScratch& os, int flags,
+                            const Physics& ph, cudaStream_t st, int* stage) {
+  const bool g = (flags & kFlagGrad) && io.grad;
+  const bool rc = flags & kFlagRecenter;
+  const int d = ph.dielectric ? 1 : 0, f = ph.inter_form ? 1 : 0, i = ph.intra_form ? 0 : 1;
+  const int smem = one_pose_smem(lig.L, lig.nrb) - kOneStatic;  // dynamic part
+#define MMO_ONE(G, RC) \
+  if (d == 0) { \
+    if (f == 0) return i ? one_t<G, RC, 0, 0, 1>(lig, prot, tab4, io, s, os, flags, smem, st, stage) \
+                         : one_t<G, RC, 0, 0, 0>(lig, prot, tab4, io, s, os, flags, smem, st, stage); \
+    return i ? one_t<G, RC, 0, 1, 1>(lig, prot, tab4, io, s, os, flags, smem, st, stage) \
+             : one_t<G, RC, 0, 1, 0>(lig, prot, tab4, io, s, os, flags, smem, st, stage); \
+  } \
+  if (f == 0) return i ? one_t<G, RC, 1, 0, 1>(lig, prot, tab4, io, s, os, flags, smem, st, stage) \
+                       : one_t<G, RC, 1, 0, 0>(lig, prot, tab4, io, s, os, flags, smem, st, stage); \
+  return i ? one_t<G, RC, 1, 1, 1>(lig, prot, tab4, io, s, os, flags, smem, st, stage) \
+           : one_t<G, RC, 1, 1, 0>(lig, prot, tab4, io, s, os, flags, smem, st, stage);
+  if (g) {
+    if (rc) { MMO_ONE(true, true) }
+    MMO_ONE(true, false)
+  }
+  if (rc) { MMO_ONE(false, true) }
+  MMO_ONE(false, false)
+#undef MMO_ONE
 }
 
 // intra_form: 0 plain (IFORM 1), 1 shifted (IFORM 0)

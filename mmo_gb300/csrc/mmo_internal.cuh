@@ -55,6 +55,7 @@ struct DevLigand {
   // is rigid-invariant) enters the gradient only through pairs that straddle
   // a group boundary.
   int nested;
+  float ilh, ill;           // 1 / L as a double-float (hi, lo), rounded from FP64
   const float4* ref;        // [L] (x, y, z, q) centred conformer, rounded to float
   const double* ref64;      // [L][3] the same conformer in double
   const float2* ref2;       // [L][3] the same conformer as float pairs (hi, lo)
@@ -257,6 +258,17 @@ struct DevSystems {
   int Lmax, nrbmax, piece_pairs_max, piece_rows_max;
 };
 
+// ---- the one-pose path in one launch (kernels_pose.cu, k_one_pose) --------
+constexpr int kOneChunk = 128;  // protein atoms per CTA of the one-pose kernel
+
+struct OneScratch {
+  float2* E;          // [ncta][L] inter energy of each CTA's protein atoms per ligand atom
+                      // (double-float: hi, lo)
+  float4* G;          // [ncta][L] dE/dX of the same
+  unsigned* arrive;   // CTAs done; the last one clears it
+  int ncta, chunk;    // CTAs and protein atoms per CTA
+};
+
 // ---- Monte Carlo chains (kernels_mc.cu) ----------------------------------
 enum : int { kMcUniform = 0, kMcGaussian = 1 };
 constexpr int kMcCounts = 3;   // per chain: step, rigid frames, conformer frames
@@ -453,6 +465,11 @@ cudaError_t launch_pairs_plain(const DevProtein& prot, const PairTable& tab, con
                                const float* lig_q, const int* lig_type, int L, int C,
                                double* Epart, float4* Gpart, int grad, const Physics& ph,
                                cudaStream_t st);
+int one_pose_smem(int L, int nrb);  // static + dynamic shared memory of k_one_pose, bytes
+// *stage: 1 when the shared-memory attribute call failed, 2 the launch
+cudaError_t launch_one_pose(const DevLigand& lig, const DevProtein& prot, const float4* tab4,
+                            const PoseIO& io, const Scratch& s, const OneScratch& os, int flags,
+                            const Physics& ph, cudaStream_t st, int* stage);
 cudaError_t launch_finish(const DevLigand& lig, const PoseIO& io, const Scratch& s, int flags,
                           const Physics& ph, cudaStream_t st);
 cudaError_t launch_reduce_plain(const double* Epart, int n, double* out, cudaStream_t st);
@@ -488,6 +505,7 @@ cudaError_t launch_prot_desolv(const DevCull& cull, const DesolvBuild& db, doubl
                                cudaStream_t st);
 cudaError_t launch_desolv_pose(const DesolvPose& d, cudaStream_t st);
 cudaError_t launch_fma_peak(int sms, int iters, float* out, cudaStream_t st, double* flops);
+cudaError_t launch_df_sincos(const float* x, int n, float4* out, cudaStream_t st);
 
 // ---- device helpers ------------------------------------------------------
 #ifdef __CUDACC__
@@ -758,6 +776,134 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
     if (done) return true;
   }
   return false;
+}
+// Double-float arithmetic: a value is an unevaluated pair h + l of floats
+// (|l| <= ulp(h) / 2), about 48 significant bits, on the FP32 pipe (GB300's
+// FP64 rate is 1/64 of its FP32 rate).  ts / qts are the error-free sums
+// (TwoSum, and Fast2Sum for |a| >= |b|); the products take their error by FMA.
+__device__ __forceinline__ float2 df_of(double x) {
+  const float h = __double2float_rn(x);
+  return make_float2(h, __double2float_rn(x - (double)h));
+}
+__device__ __forceinline__ float2 qts(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ float2 ts(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bp = __fsub_rn(s, a);
+  return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp)));
+}
+__device__ __forceinline__ float2 dadd(float2 a, float2 b) {
+  const float2 s = ts(a.x, b.x);
+  return qts(s.x, __fadd_rn(s.y, __fadd_rn(a.y, b.y)));
+}
+__device__ __forceinline__ float2 dneg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 dsub(float2 a, float2 b) { return dadd(a, dneg(b)); }
+__device__ __forceinline__ float2 dmul(float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  return qts(p, fmaf(a.x, b.y, fmaf(a.y, b.x, fmaf(a.x, b.x, -p))));
+}
+// a0 b0 + a1 b1 + a2 b2 + c
+__device__ __forceinline__ float2 ddot3c(float2 a0, float2 b0, float2 a1, float2 b1, float2 a2,
+                                         float2 b2, float2 c) {
+  return dadd(dadd(dadd(dmul(a0, b0), dmul(a1, b1)), dmul(a2, b2)), c);
+}
+__device__ __forceinline__ float2 dshfl_xor(float2 a, int o) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, a.x, o), __shfl_xor_sync(0xffffffffu, a.y, o));
+}
+__device__ __forceinline__ bool dgt(float2 a, float2 b) {
+  return a.x > b.x || (a.x == b.x && a.y > b.y);
+}
+// s += x for a double-float running sum s (TwoSum on the high part)
+__device__ __forceinline__ void acc2(float2& s, float x) {
+  const float2 t = ts(s.x, x);
+  s.x = t.x;
+  s.y = __fadd_rn(s.y, t.y);
+}
+
+// sin and cos of a float angle x as double-floats, on the FP32 pipe (the FP64
+// library sincos runs at GB300's FP64 rate).  Cody-Waite reduction:
+// k = rint(2 x / pi), r = x - k pi/2 with pi/2 split in three floats (the
+// first with 8 significant bits, so k * kHalfPi1 is exact for |k| < 2^16);
+// then the Taylor series of sin r and cos r on |r| <= pi/4 + (rounding of k),
+//   sin r = r (1 - z/3! + z^2/5! - ...),  cos r = 1 - z/2! + z^2/4! - ...,
+// z = r^2, summed by Horner's scheme with the five leading steps in
+// double-float and the tail (below 3e-8 of the result from z^5 on) in FP32;
+// the last terms kept are z^8 / 17! and z^9 / 18! (the next ones are below
+// 1e-18).  Absolute error below 1e-14 (the double-float operations), plus
+// |k| 6e-17 from pi / 2 rounded to double (4e-13 at |x| = 1e4); |x| >= 1e5
+// takes the FP64 library function.
+constexpr double kHalfPi = 1.5707963267948966;  // pi / 2 rounded to double
+constexpr float kHalfPi1 = 1.5703125f;          // 201 / 128
+constexpr float kHalfPi2 = (float)(kHalfPi - 1.5703125);
+constexpr float kHalfPi3 = (float)(kHalfPi - 1.5703125 - (double)(float)(kHalfPi - 1.5703125));
+constexpr double inv_fact(int m) {
+  double f = 1.0;
+  for (int i = 2; i <= m; ++i) f *= i;
+  return 1.0 / f;
+}
+// 1 / m! rounded at compile time: hi, and the lo of the double-float
+#define MMO_INV_FACT(m)                                 \
+  constexpr float kIF##m##h = (float)inv_fact(m);       \
+  constexpr float kIF##m##l = (float)(inv_fact(m) - (double)(float)inv_fact(m));
+MMO_INV_FACT(2)
+MMO_INV_FACT(3)
+MMO_INV_FACT(4)
+MMO_INV_FACT(5)
+MMO_INV_FACT(6)
+MMO_INV_FACT(7)
+MMO_INV_FACT(8)
+MMO_INV_FACT(9)
+MMO_INV_FACT(10)
+MMO_INV_FACT(11)
+MMO_INV_FACT(12)
+MMO_INV_FACT(13)
+MMO_INV_FACT(14)
+MMO_INV_FACT(15)
+MMO_INV_FACT(16)
+MMO_INV_FACT(17)
+MMO_INV_FACT(18)
+#undef MMO_INV_FACT
+
+__device__ __forceinline__ void df_sincos(float x, float2& s, float2& c) {
+  if (!(fabsf(x) < 1e5f)) {  // (also NaN and infinities)
+    double sd, cd;
+    sincos((double)x, &sd, &cd);
+    s = df_of(sd);
+    c = df_of(cd);
+    return;
+  }
+  const float k = rintf(x * 0.63661977236758134f);  // 2 / pi
+  float2 r = ts(x, -k * kHalfPi1);                   // k kHalfPi1 exact
+  const float p2 = k * kHalfPi2;
+  r = dsub(r, make_float2(p2, fmaf(k, kHalfPi2, -p2)));
+  r = dsub(r, make_float2(k * kHalfPi3, 0.f));
+  const float2 z = dmul(r, r);
+  const float zf = z.x;
+  // sin: tail from z^5 in FP32, then z^4 / 9!, -z^3 / 7!, z^2 / 5!, -z / 3!, 1
+  const float ts5 = fmaf(fmaf(fmaf(kIF17h, zf, -kIF15h), zf, kIF13h), zf, -kIF11h);
+  float2 hs = make_float2(ts5, 0.f);
+  hs = dadd(dmul(hs, z), make_float2(kIF9h, kIF9l));
+  hs = dadd(dmul(hs, z), make_float2(-kIF7h, -kIF7l));
+  hs = dadd(dmul(hs, z), make_float2(kIF5h, kIF5l));
+  hs = dadd(dmul(hs, z), make_float2(-kIF3h, -kIF3l));
+  hs = dadd(dmul(hs, z), make_float2(1.f, 0.f));
+  const float2 sr = dmul(r, hs);
+  // cos: tail from z^5 in FP32, then z^4 / 8!, -z^3 / 6!, z^2 / 4!, -z / 2!, 1
+  const float tc5 = fmaf(fmaf(fmaf(fmaf(-kIF18h, zf, kIF16h), zf, -kIF14h), zf, kIF12h), zf, -kIF10h);
+  float2 hc = make_float2(tc5, 0.f);
+  hc = dadd(dmul(hc, z), make_float2(kIF8h, kIF8l));
+  hc = dadd(dmul(hc, z), make_float2(-kIF6h, -kIF6l));
+  hc = dadd(dmul(hc, z), make_float2(kIF4h, kIF4l));
+  hc = dadd(dmul(hc, z), make_float2(-kIF2h, -kIF2l));
+  const float2 cr = dadd(dmul(hc, z), make_float2(1.f, 0.f));
+  switch (((int)k) & 3) {
+    case 0: s = sr; c = cr; break;
+    case 1: s = cr; c = dneg(sr); break;
+    case 2: s = dneg(sr); c = dneg(cr); break;
+    default: s = dneg(cr); c = sr; break;
+  }
 }
 #endif
 

@@ -79,6 +79,33 @@ def test_single_pose_energy_gradient(oracle, scorer_factory, small, recenter):
     assert_ref(E, G, ref, st)
 
 
+@pytest.mark.parametrize("grad,recenter,phys", [(True, False, (0, 0, 0, 0)),
+                                                 (True, True, (1, 1, 1, 1)),
+                                                 (False, False, (0, 0, 1, 0)),
+                                                 (True, False, (1, 0, 0, 0)),
+                                                 (False, True, (0, 1, 1, 1))])
+def test_one_pose_is_one_launch(oracle, scorer_factory, batch, grad, recenter, phys):
+    """One pose with the pair terms is a single launch (k_one_pose: every CTA
+    rebuilds the pose and sums its protein atoms' pair terms, the last CTA to
+    arrive adds the partials in CTA order and finishes the pose).  Twenty-four
+    calls in a row, each held to the contract: every launch leaves the
+    arrival count at zero for the next."""
+    from mmo_gb300.ff import Physics
+
+    s = scorer_factory(batch.pocket, batch.ligand, Physics(*phys))
+    d = batch.poses[:24]
+    ref = ref_batch(oracle, batch, d, grad=grad, recenter=recenter, ph=oracle.physics(*phys))
+    E, G, st = [], [], []
+    for b in range(len(d)):
+        e, g, t = s.score_poses(d[b:b + 1], grad=grad, recenter=recenter)
+        assert s.last_launches() == 1
+        E.append(e[0])
+        st.append(t[0])
+        if grad:
+            G.append(g[0])
+    assert_ref(np.array(E), np.array(G) if grad else None, ref, np.array(st))
+
+
 # -- batched ------------------------------------------------------------------------
 
 def test_batched_energy(oracle, scorer_factory, batch):
