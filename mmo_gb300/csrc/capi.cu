@@ -354,6 +354,8 @@ DevLigand ligand_at(const LigBlob& B, char* b, size_t* bytes) {
   L.pair_ij = align_ptr<int2>(b, off, std::max(np, 1));
   L.pair_par = align_ptr<float4>(b, off, std::max(np, 1));
   L.amask = align_ptr<uint32_t>(b, off, n);
+  L.tax = align_ptr<float2>(b, off, 6 * (size_t)std::max(nrb, 1));
+  L.tord = align_ptr<int>(b, off, std::max(nrb, 1));
   L.grp_off = align_ptr<int>(b, off, nrb + 1);
   L.grp_atoms = align_ptr<int>(b, off, std::max(B.ngat, 1));
   L.nb_off = align_ptr<int>(b, off, n + 1);
@@ -466,6 +468,28 @@ void make_ligand_blob(int mixing, const LigIn& in, LigBlob* out) {
       const float h = (float)r64[d];
       r2[d] = make_float2(h, (float)(r64[d] - (double)h));
     }
+  }
+  // per torsion: the unit axis and centre in the reference conformer, and the
+  // order of the groups by size (inner groups first; the one-pose kernel's
+  // rotation chains for nested groups)
+  {
+    std::vector<int> gsz(nrb);
+    for (int t = 0; t < nrb; ++t) {
+      gsz[t] = in.goff[t + 1] - in.goff[t];
+      const int l = bonds[t].x, c = bonds[t].y;
+      double a[3] = {in.x[c] - in.x[l], in.y[c] - in.y[l], in.z[c] - in.z[l]};
+      const double len = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+      const double v[6] = {a[0] / len, a[1] / len, a[2] / len, in.x[c], in.y[c], in.z[c]};
+      float2* tx = const_cast<float2*>(H.tax) + 6 * t;
+      for (int d = 0; d < 6; ++d) {
+        const float h = (float)v[d];
+        tx[d] = make_float2(h, (float)(v[d] - (double)h));
+      }
+    }
+    std::vector<int> ord(nrb);
+    for (int t = 0; t < nrb; ++t) ord[t] = t;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return gsz[a] < gsz[b]; });
+    if (nrb) memcpy((void*)H.tord, ord.data(), sizeof(int) * nrb);
   }
   memcpy((void*)H.type, in.type.data(), sizeof(int) * n);
   for (int i = 0; i < n; ++i) const_cast<float*>(H.q)[i] = (float)in.q[i];
@@ -1078,22 +1102,23 @@ int check_dev_err(mmo_ctx* ctx, int flag) {
   return MMO_OK;
 }
 
-// the one-pose path's per-CTA partials: ncta CTAs of 64 protein atoms
+// the one-pose path's per-CTA partials: npair CTAs of kOneChunk protein atoms,
+// and the intra CTA's terms
 int ensure_one_scratch(mmo_ctx* ctx, int L) {
   OneScratch& o = ctx->one;
-  o.chunk = kOneChunk;
-  o.ncta = std::max(1, (ctx->prot.P + o.chunk - 1) / o.chunk);
+  o.npair = std::max(1, (ctx->prot.P + kOneChunk - 1) / kOneChunk);
   int r;
-  if ((r = grow(ctx, (void**)&o.E, &ctx->capOneE, sizeof(float2) * (size_t)o.ncta * L,
+  if ((r = grow(ctx, (void**)&o.E, &ctx->capOneE, sizeof(float2) * (size_t)o.npair * L,
                 "one-pose partials")))
     return r;
-  if ((r = grow(ctx, (void**)&o.G, &ctx->capOneG, sizeof(float4) * (size_t)o.ncta * L,
+  if ((r = grow(ctx, (void**)&o.G, &ctx->capOneG, sizeof(float4) * (size_t)o.npair * L,
                 "one-pose partials")))
     return r;
   if (!o.arrive) {
     MMO_CK(cudaMalloc((void**)&o.arrive, sizeof(unsigned)), "one-pose counter");
     MMO_CK(cudaMemset(o.arrive, 0, sizeof(unsigned)), "one-pose counter");
   }
+  if (!o.intra) MMO_CK(cudaMalloc((void**)&o.intra, sizeof(float) * (kMaxTors + 2)), "one-pose intra terms");
   return MMO_OK;
 }
 
@@ -1161,6 +1186,7 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
     MMO_CK(mark(1), "event");
     MMO_CK(mark(2), "event");
     int stage = 0;
+    ctx->one.with_intra = ctx->lig.nested && (fl & kFlagIntra) ? 1 : 0;
     const cudaError_t pending = cudaGetLastError();
     if (pending != cudaSuccess)
       return cuda_fail(ctx, pending, "error left by an earlier runtime call");
@@ -1726,6 +1752,7 @@ int mmo_ctx_destroy(mmo_ctx* ctx) {
   cudaFree(ctx->one.E);
   cudaFree(ctx->one.G);
   cudaFree(ctx->one.arrive);
+  cudaFree(ctx->one.intra);
   cudaFree(ctx->cs.gcount);
   cudaFree(ctx->cs.glist);
   cudaFree(ctx->cs.items);

@@ -777,25 +777,30 @@ __global__ void __launch_bounds__(kFinishOne)
 //      bond-order application of src/optim.ml:68-71 equals applying to each
 //      atom the rotations of its groups about their axes in the reference
 //      conformer, innermost group first: the rotations are built once (a
-//      thread per matrix entry) and every atom applies its own chain.  Other
-//      ligands take the torsions in bond order (the operations of
-//      rebuild_pose), recording what the reverse pass needs;
-//   2. CTA c stages protein atoms [c kOneChunk, (c + 1) kOneChunk) in shared
-//      memory and sums their pair terms against every ligand atom (kFinishOne
-//      / L threads per ligand atom) into per-CTA partials;
+//      thread per matrix entry; axes, centres and the group order come from
+//      the host) and every atom applies its own chain.  Other ligands take the
+//      torsions in bond order (the operations of rebuild_pose), recording what
+//      the reverse pass needs.  The angles' sines and cosines, the rigid map
+//      and all sums are double-float on the FP32 pipe;
+//   2. CTA 0, for nested groups with the intra term, sums the intra energy and
+//      the terms of each torsion from the pairs that straddle its group; every
+//      other CTA stages kOneChunk protein atoms in shared memory and sums their
+//      pair terms against every ligand atom (kFinishOne / L threads per ligand
+//      atom) into per-CTA partials;
 //   3. the last CTA to arrive (an atomic count, nothing waits) adds the
 //      partials in CTA order and finishes the pose.  For nested groups the
 //      derivative of torsion t is a sum over its group in the posed frame,
 //        dE/dtheta_t = w_t . sum_{i in G_t} (X_i - C_t) x (dE/dX_i - F / L)
 //      (w_t the posed axis, C_t the posed centre atom, F the total force; F / L
-//      only with the centroid removed), one warp per torsion, plus the intra
-//      terms of the pairs that straddle the group; other ligands go through
-//      the work buffers and the one-pose finishing code (finish_one_cta).
+//      only with the centroid removed), plus CTA 0's intra term, one warp per
+//      torsion; the radius check runs on a spare warp meanwhile.  Other
+//      ligands go through the work buffers and the one-pose finishing code
+//      (finish_one_cta).
 // ---------------------------------------------------------------------------
 // shared-memory layout of k_one_pose, byte offsets (16-byte aligned)
 struct OneLayout {
-  int xh, xl, yr, rec, tsc, x, y, z, bonds, gmask, rig, cen, status, rot, ord, gsize, amask, uax;
-  int sp, stype, pe, pg, qe, qg, sE, sG, saxis, sdt, sred, red, total;
+  int xh, xl, yr, rec, tsc, x, y, z, bonds, gmask, rig, cen, status, rot, ord, amask, uax;
+  int sp, stype, pe, pg, qe, qg, sE, sG, saxis, sdt, sred, red, tT, tV, total;
 };
 
 __host__ __device__ inline int take16(int& off, int n) {
@@ -822,7 +827,6 @@ __host__ __device__ inline OneLayout one_layout(int L, int nrb) {
   o.status = take16(off, 4);
   o.rot = take16(off, 8 * 12 * nrb);
   o.ord = take16(off, 4 * nrb);
-  o.gsize = take16(off, 4 * nrb);
   o.amask = take16(off, 4 * L);
   o.uax = take16(off, 8 * 3 * nrb);
   o.sp = take16(off, 32 * kOneChunk);
@@ -837,6 +841,8 @@ __host__ __device__ inline OneLayout one_layout(int L, int nrb) {
   o.sdt = take16(off, 4 * nrb * (kFinishOne + 1));
   o.sred = take16(off, 8 * (kFinishOne / 32 + 1));
   o.red = take16(off, 4 * 12);
+  o.tT = take16(off, 16 * nrb);
+  o.tV = take16(off, 16 * nrb);
   o.total = off;
   return o;
 }
@@ -854,7 +860,6 @@ struct OneSmem {
   int* status;
   float2* rot;         // [nrb][12] reference-frame rotation of each torsion: matrix, centre
   int* ord;            // [nrb] torsions by group size, smallest first
-  int* gsize;          // [nrb] group sizes
   uint32_t* amask;     // [L] the groups of each atom (bit t: group t)
   float2* uax;         // [nrb][3] unit axis of each torsion in the reference conformer
   float4* sp;          // [kOneChunk][2] the CTA's protein atoms hi (q in w), lo
@@ -869,6 +874,7 @@ struct OneSmem {
   float* sdt;          // [nrb][kFinishOne + 1] straddling intra terms per thread
   float2* sred;        // [warps] intra energy per warp (double-float)
   float* red;          // [12] total force and the rigid-map sums
+  float4 *tT, *tV;     // [nrb] per torsion: sum of lever x force, sum of levers
 };
 
 __device__ __forceinline__ OneSmem one_smem(char* base, int L, int nrb) {
@@ -889,7 +895,6 @@ __device__ __forceinline__ OneSmem one_smem(char* base, int L, int nrb) {
   m.status = reinterpret_cast<int*>(base + o.status);
   m.rot = reinterpret_cast<float2*>(base + o.rot);
   m.ord = reinterpret_cast<int*>(base + o.ord);
-  m.gsize = reinterpret_cast<int*>(base + o.gsize);
   m.amask = reinterpret_cast<uint32_t*>(base + o.amask);
   m.uax = reinterpret_cast<float2*>(base + o.uax);
   m.sp = reinterpret_cast<float4*>(base + o.sp);
@@ -904,6 +909,8 @@ __device__ __forceinline__ OneSmem one_smem(char* base, int L, int nrb) {
   m.sdt = reinterpret_cast<float*>(base + o.sdt);
   m.sred = reinterpret_cast<float2*>(base + o.sred);
   m.red = reinterpret_cast<float*>(base + o.red);
+  m.tT = reinterpret_cast<float4*>(base + o.tT);
+  m.tV = reinterpret_cast<float4*>(base + o.tV);
   return m;
 }
 
@@ -945,19 +952,18 @@ __device__ __forceinline__ void one_load(const DevLigand& lig, const float* dof,
     // rigid map: twelve entries (rotation, translation)
     if (tid < 12) m.G[tid] = rigid_entry_df(tid, m.tsc, dof, orx, ory, orz);
   } else if (lig.nested && tid >= 64 && tid < 64 + nrb) {
+    // the torsion's unit axis and centre in the reference conformer, and the
+    // group order (both from the host)
     const int t = tid - 64;
-    const int2 bd = lig.bonds[t];
-    const float2 cx = lig.ref2[3 * bd.y], cy = lig.ref2[3 * bd.y + 1], cz = lig.ref2[3 * bd.y + 2];
-    const float2 lx = lig.ref2[3 * bd.x], ly = lig.ref2[3 * bd.x + 1], lz = lig.ref2[3 * bd.x + 2];
-    float2 ux, uy, uz, inv;
-    unit_axis(dsub(cx, lx), dsub(cy, ly), dsub(cz, lz), ux, uy, uz, inv);
+    const float2* tx = lig.tax + 6 * t;
     float2* r = m.rot + 12 * t;
-    r[9] = cx;
-    r[10] = cy;
-    r[11] = cz;
-    m.uax[3 * t] = ux;
-    m.uax[3 * t + 1] = uy;
-    m.uax[3 * t + 2] = uz;
+    m.uax[3 * t] = tx[0];
+    m.uax[3 * t + 1] = tx[1];
+    m.uax[3 * t + 2] = tx[2];
+    r[9] = tx[3];
+    r[10] = tx[4];
+    r[11] = tx[5];
+    m.ord[t] = lig.tord[t];
   }
   if (tid < L) {
     m.x[tid] = lig.ref2[3 * tid];
@@ -965,14 +971,7 @@ __device__ __forceinline__ void one_load(const DevLigand& lig, const float* dof,
     m.z[tid] = lig.ref2[3 * tid + 2];
     m.amask[tid] = lig.amask[tid];
   }
-  for (int k = tid; k < nrb; k += blockDim.x) {
-    m.bonds[k] = lig.bonds[k];
-    if (lig.nested) {
-      int s = 0;
-      for (int w = 0; w < kSlots; ++w) s += __popc(lig.gmask[k * kSlots + w]);
-      m.gsize[k] = s;
-    }
-  }
+  for (int k = tid; k < nrb; k += blockDim.x) m.bonds[k] = lig.bonds[k];
   for (int k = tid; k < nrb * kSlots; k += blockDim.x) m.gmask[k] = lig.gmask[k];
 }
 
@@ -1041,15 +1040,6 @@ __device__ __forceinline__ void one_radius(const DevLigand& lig, const OneSmem& 
 template <bool RECENTER>
 __device__ __forceinline__ void one_torsions_nested(const DevLigand& lig, const OneSmem& m) {
   const int tid = threadIdx.x, L = lig.L, nrb = lig.nrb;
-  if (tid < nrb) {  // rank by group size (a contained group is smaller)
-    const int s = m.gsize[tid];
-    int r = 0;
-    for (int u = 0; u < nrb; ++u) {
-      const int su = m.gsize[u];
-      r += su < s || (su == s && u < tid);
-    }
-    m.ord[r] = tid;
-  }
   for (int e = tid; e < 9 * nrb; e += blockDim.x) {
     const int t = e / 9, k = e - 9 * t;
     const float2 ux = m.uax[3 * t], uy = m.uax[3 * t + 1], uz = m.uax[3 * t + 2];
@@ -1154,39 +1144,86 @@ __device__ __forceinline__ void load_pairs(const DevLigand& lig, int p0, PairBat
   }
 }
 
-// The finish of a pose with nested groups, from shared memory: energy,
-// status and (GRAD) the gradient with the torsion derivatives summed in the
-// posed frame.  pb: the thread's first batch of pairs, already loaded.
-template <bool GRAD, bool RECENTER, int DIEL, int IFORM>
+// The intra CTA (nested groups): the intra energy and, with the gradient, the
+// terms of each torsion from the pairs that straddle its group, from the
+// posed coordinates alone; out[t] (t < nrb) the torsion terms, out[nrb],
+// out[nrb + 1] the energy (double-float).
+template <bool GRAD, int DIEL, int IFORM>
+__device__ __forceinline__ void one_intra_terms(const DevLigand& lig, const OneSmem& m,
+                                                float* out) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nrb = lig.nrb;
+  constexpr int kWarps = kFinishOne / 32;
+  const bool crossing = GRAD && nrb > 0;
+  PairBatch pb;
+  load_pairs(lig, tid, pb);
+  if (crossing) {
+    if (tid < nrb) torsion_frame(lig, m.Xh, m.Xl, m.saxis, tid);
+    for (int k = tid; k < nrb * (kFinishOne + 1); k += kFinishOne) m.sdt[k] = 0.f;
+  }
+  __syncthreads();
+  float acc = 0.f;
+  for (int p0 = tid; p0 < lig.npairs; p0 += kPairBatch * kFinishOne) {
+    if (p0 != tid) load_pairs(lig, p0, pb);
+#pragma unroll
+    for (int u = 0; u < kPairBatch; ++u)
+      if (p0 + u * kFinishOne < lig.npairs)
+        intra_pair_terms_at<DIEL, IFORM>(m.Xh, m.Xl, m.saxis, pb.ij[u], pb.par[u], m.amask,
+                                         crossing, acc, m.sdt + tid, kFinishOne + 1);
+  }
+  float2 w = make_float2(acc, 0.f);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) w = dadd(w, dshfl_xor(w, o));
+  if (lane == 0) m.sred[warp] = w;
+  __syncthreads();
+  if (crossing)
+    for (int t = warp; t < nrb; t += kWarps) {  // each torsion's column, in a fixed order
+      float d = 0.f;
+      for (int k = lane; k < kFinishOne; k += 32) d += m.sdt[t * (kFinishOne + 1) + k];
+      d = warp_sum(d);
+      if (lane == 0) out[t] = d;
+    }
+  if (tid == 0) {
+    float2 e = m.sred[0];
+    for (int k = 1; k < kWarps; ++k) e = dadd(e, m.sred[k]);
+    out[nrb] = e.x;
+    out[nrb + 1] = e.y;
+  }
+}
+
+// The finish of a pose with nested groups in the last CTA, from shared memory
+// (the inter partials summed, the torsion frames, the status) and the intra
+// CTA's terms (intra_g; nullptr without the intra term): energy, status and
+// with the gradient the rigid-map sums and the torsion derivatives
+//   dE/dtheta_t = w_t . sum_{i in G_t} (X_i - C_t) x (dE/dX_i - F / L) + intra_t,
+// one warp per item (energy on warp 0; twelve rigid sums and the torsions on
+// warps 1, 2, ...).
+template <bool GRAD, bool RECENTER>
 __device__ __forceinline__ void finish_one_nested(const DevLigand& lig, const PoseIO& io,
-                                                  const OneSmem& m, int flags, PairBatch& pb) {
+                                                  const OneSmem& m, int flags,
+                                                  const float* intra_g) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, L = lig.L, nrb = lig.nrb;
   constexpr int kWarps = kFinishOne / 32;
-  const bool intra = flags & kFlagIntra;
-  const bool crossing = GRAD && intra && nrb > 0;
-  if (GRAD && tid < nrb) torsion_frame(lig, m.Xh, m.Xl, m.saxis, tid);
-  if (crossing)
-    for (int k = tid; k < nrb * (kFinishOne + 1); k += kFinishOne) m.sdt[k] = 0.f;
-  __syncthreads();
-  if (intra) {
-    float acc = 0.f;
-    for (int p0 = tid; p0 < lig.npairs; p0 += kPairBatch * kFinishOne) {
-      if (p0 != tid) load_pairs(lig, p0, pb);
+  if (warp == 0) {  // double-float sums; FP64 only for the outputs
+    float2 ei = make_float2(0.f, 0.f);
+    if (flags & kFlagInter)
+      for (int a = lane; a < L; a += 32) ei = dadd(ei, m.sE[a]);
 #pragma unroll
-      for (int u = 0; u < kPairBatch; ++u)
-        if (p0 + u * kFinishOne < lig.npairs)
-          intra_pair_terms_at<DIEL, IFORM>(m.Xh, m.Xl, m.saxis, pb.ij[u], pb.par[u], m.amask,
-                                           crossing, acc, m.sdt + tid, kFinishOne + 1);
+    for (int o = 16; o > 0; o >>= 1) ei = dadd(ei, dshfl_xor(ei, o));
+    if (lane == 0) {
+      float2 t = ei;
+      if (intra_g) t = dadd(t, make_float2(__ldcg(intra_g + nrb), __ldcg(intra_g + nrb + 1)));
+      const double e = (double)t.x + (double)t.y;
+      io.E[0] = e;
+      io.status[0] = *m.status | (isfinite(e) ? 0 : kStatusNonFinite);
+      if (io.E_inter) io.E_inter[0] = (double)ei.x + (double)ei.y;
     }
-    float2 w = make_float2(acc, 0.f);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) w = dadd(w, dshfl_xor(w, o));
-    if (lane == 0) m.sred[warp] = w;
   }
-  if (GRAD) {
-    // total force (q < 3) and M_rc = sum_i G_ir Yc_ic (q = 3 + 3 r + c), Yc
-    // the coordinates after the torsions less the rotation origin
-    for (int q = warp; q < 12; q += kWarps) {
+  if (!GRAD) return;
+  for (int it = (warp + kWarps - 1) % kWarps; it < 12 + nrb; it += kWarps) {
+    if (it < 12) {
+      // total force (q < 3) and M_rc = sum_i G_ir Yc_ic (q = 3 + 3 r + c), Yc
+      // the coordinates after the torsions less the rotation origin
+      const int q = it;
       float s = 0.f;
       for (int a = lane; a < L; a += 32) {
         const float4 g = m.sG[a];
@@ -1202,28 +1239,58 @@ __device__ __forceinline__ void finish_one_nested(const DevLigand& lig, const Po
       }
       s = warp_sum(s);
       if (lane == 0) m.red[q] = s;
+    } else {
+      const int t = it - 12;
+      const float4 w = m.saxis[t];
+      const int ci = __float_as_int(w.w);
+      const float4 ch = m.Xh[ci], cl = m.Xl[ci];
+      float tx = 0.f, ty = 0.f, tz = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
+      for (int a = lane; a < L; a += 32) {
+        if ((m.gmask[t * kSlots + (a >> 5)] >> (a & 31)) & 1u) {
+          const float4 g = m.sG[a];
+          const float4 ah = m.Xh[a], al = m.Xl[a];
+          // the lever X_i - C_t from the hi/lo pairs
+          const float lx = split_diff(ah.x, al.x, ch.x, cl.x);
+          const float ly = split_diff(ah.y, al.y, ch.y, cl.y);
+          const float lz = split_diff(ah.z, al.z, ch.z, cl.z);
+          tx += ly * g.z - lz * g.y;
+          ty += lz * g.x - lx * g.z;
+          tz += lx * g.y - ly * g.x;
+          if (RECENTER) {
+            vx += lx;
+            vy += ly;
+            vz += lz;
+          }
+        }
+      }
+      tx = warp_sum(tx);
+      ty = warp_sum(ty);
+      tz = warp_sum(tz);
+      if (RECENTER) {
+        vx = warp_sum(vx);
+        vy = warp_sum(vy);
+        vz = warp_sum(vz);
+        if (lane == 0) {
+          m.tT[t] = make_float4(tx, ty, tz, 0.f);
+          m.tV[t] = make_float4(vx, vy, vz, 0.f);
+        }
+      } else if (lane == 0) {
+        io.grad[6 + t] = w.x * tx + w.y * ty + w.z * tz + (intra_g ? __ldcg(intra_g + t) : 0.f);
+      }
     }
   }
   __syncthreads();
-  if (warp == 0) {  // double-float sums; FP64 only for the outputs
-    float2 ei = make_float2(0.f, 0.f);
-    if (flags & kFlagInter)
-      for (int a = lane; a < L; a += 32) ei = dadd(ei, m.sE[a]);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) ei = dadd(ei, dshfl_xor(ei, o));
-    if (lane == 0) {
-      float2 t = ei;
-      if (intra)
-        for (int k = 0; k < kWarps; ++k) t = dadd(t, m.sred[k]);
-      const double e = (double)t.x + (double)t.y;
-      io.E[0] = e;
-      io.status[0] = *m.status | (isfinite(e) ? 0 : kStatusNonFinite);
-      if (io.E_inter) io.E_inter[0] = (double)ei.x + (double)ei.y;
-    }
+  if (RECENTER && tid < nrb) {
+    // sum_i l_i x (G_i - F / L) = T - V x F / L
+    const float iL = 1.0f / (float)L;
+    const float fx = m.red[0] * iL, fy = m.red[1] * iL, fz = m.red[2] * iL;
+    const float4 T = m.tT[tid], V = m.tV[tid], w = m.saxis[tid];
+    const float cx = T.x - (V.y * fz - V.z * fy), cy = T.y - (V.z * fx - V.x * fz),
+                cz = T.z - (V.x * fy - V.y * fx);
+    io.grad[6 + tid] = w.x * cx + w.y * cy + w.z * cz + (intra_g ? __ldcg(intra_g + tid) : 0.f);
   }
-  if (!GRAD) return;
-  const float* M = m.red + 3;
-  if (tid == 32) {  // the rigid map: translation, then d R / d a, d b, d g of rot.ml:52-66
+  if (tid == kFinishOne - 32) {  // the rigid map: translation, then d R / d a, d b, d g of rot.ml:52-66
+    const float* M = m.red + 3;
     float sa, ca, sb, cb, sg, cg;
     sincosf(io.dofs[3], &sa, &ca);
     sincosf(io.dofs[4], &sb, &cb);
@@ -1251,38 +1318,6 @@ __device__ __forceinline__ void finish_one_nested(const DevLigand& lig, const Po
     io.grad[4] = gb;
     io.grad[5] = gg;
   }
-  const float iL = 1.0f / (float)L;
-  const float fx = RECENTER ? m.red[0] * iL : 0.f, fy = RECENTER ? m.red[1] * iL : 0.f,
-              fz = RECENTER ? m.red[2] * iL : 0.f;
-  for (int t = warp; t < nrb; t += kWarps) {
-    float d = 0.f;  // the straddling intra terms, in a fixed order
-    if (crossing) {
-      for (int k = lane; k < kFinishOne; k += 32) d += m.sdt[t * (kFinishOne + 1) + k];
-      d = warp_sum(d);
-    }
-    const float4 w = m.saxis[t];
-    const int ci = __float_as_int(w.w);
-    const float4 ch = m.Xh[ci], cl = m.Xl[ci];
-    float tx = 0.f, ty = 0.f, tz = 0.f;
-    for (int a = lane; a < L; a += 32) {
-      if ((m.gmask[t * kSlots + (a >> 5)] >> (a & 31)) & 1u) {
-        const float4 g = m.sG[a];
-        const float gx = g.x - fx, gy = g.y - fy, gz = g.z - fz;
-        const float4 ah = m.Xh[a], al = m.Xl[a];
-        // the lever X_i - C_t from the hi/lo pairs
-        const float lx = split_diff(ah.x, al.x, ch.x, cl.x);
-        const float ly = split_diff(ah.y, al.y, ch.y, cl.y);
-        const float lz = split_diff(ah.z, al.z, ch.z, cl.z);
-        tx += ly * gz - lz * gy;
-        ty += lz * gx - lx * gz;
-        tz += lx * gy - ly * gx;
-      }
-    }
-    tx = warp_sum(tx);
-    ty = warp_sum(ty);
-    tz = warp_sum(tz);
-    if (lane == 0) io.grad[6 + t] = w.x * tx + w.y * ty + w.z * tz + d;
-  }
 }
 
 // static shared memory of k_one_pose (type table and flag), rounded up
@@ -1300,8 +1335,11 @@ __global__ void __launch_bounds__(kFinishOne)
   const bool nested = lig.nested;
   const OneSmem m = one_smem(reinterpret_cast<char*>(osm), L, nrb);
   if (blockIdx.x == 0 && tid == 0 && io.zero_err) *io.err = 0;
-  // this CTA's protein atoms and the pair table: their loads overlap the rebuild
-  const int c = blockIdx.x, c0 = c * kOneChunk, n = min(kOneChunk, prot.P - c0);
+  // CTA 0 takes the intra terms when os.with_intra (nested groups), the others
+  // a chunk of protein atoms each; their loads overlap the rebuild
+  const bool intra_cta = os.with_intra && blockIdx.x == 0;
+  const int c = blockIdx.x - os.with_intra;  // the pair chunk
+  const int c0 = c * kOneChunk, n = intra_cta ? 0 : min(kOneChunk, prot.P - c0);
   if (tid < n) {
     m.sp[2 * tid] = prot.atoms[2 * (c0 + tid)];
     m.sp[2 * tid + 1] = prot.atoms[2 * (c0 + tid) + 1];
@@ -1322,36 +1360,40 @@ __global__ void __launch_bounds__(kFinishOne)
   } else {
     one_torsions_seq<RECENTER, GRAD>(lig, m);
   }
-  // the pair terms of this CTA's protein atoms
-  if (g < S) {
-    const float4 xh = m.Xh[j], xl = m.Xl[j];
-    float ae = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
-    for (int i = g; i < n; i += S) {
-      const float4 p = m.sp[2 * i], pl = m.sp[2 * i + 1];
-      const float2 xd = stab[m.stype[i] * kNTypes + lt];
-      uff_pair<GRAD, DIEL, FORM>(split_diff(xh.x, xl.x, p.x, pl.x),
-                                 split_diff(xh.y, xl.y, p.y, pl.y),
-                                 split_diff(xh.z, xl.z, p.z, pl.z), xd.x, xd.y, p.w * qj, ae, gx,
-                                 gy, gz);
-    }
-    m.pe[tid] = ae;
-    m.pg[tid] = make_float4(gx, gy, gz, 0.f);
-  }
-  __syncthreads();
-  if (tid < L) {
-    float2 e = make_float2(0.f, 0.f);
-    float sx = 0.f, sy = 0.f, sz = 0.f;
-    for (int k = 0; k < S; ++k) {
-      acc2(e, m.pe[k * L + tid]);
-      if (GRAD) {
-        const float4 p = m.pg[k * L + tid];
-        sx += p.x;
-        sy += p.y;
-        sz += p.z;
+  if (intra_cta) {
+    one_intra_terms<GRAD, DIEL, IFORM>(lig, m, os.intra);
+  } else {
+    // the pair terms of this CTA's protein atoms
+    if (g < S) {
+      const float4 xh = m.Xh[j], xl = m.Xl[j];
+      float ae = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+      for (int i = g; i < n; i += S) {
+        const float4 p = m.sp[2 * i], pl = m.sp[2 * i + 1];
+        const float2 xd = stab[m.stype[i] * kNTypes + lt];
+        uff_pair<GRAD, DIEL, FORM>(split_diff(xh.x, xl.x, p.x, pl.x),
+                                   split_diff(xh.y, xl.y, p.y, pl.y),
+                                   split_diff(xh.z, xl.z, p.z, pl.z), xd.x, xd.y, p.w * qj, ae,
+                                   gx, gy, gz);
       }
+      m.pe[tid] = ae;
+      m.pg[tid] = make_float4(gx, gy, gz, 0.f);
     }
-    os.E[(size_t)c * L + tid] = e;
-    if (GRAD) os.G[(size_t)c * L + tid] = make_float4(sx, sy, sz, 0.f);
+    __syncthreads();
+    if (tid < L) {
+      float2 e = make_float2(0.f, 0.f);
+      float sx = 0.f, sy = 0.f, sz = 0.f;
+      for (int k = 0; k < S; ++k) {
+        acc2(e, m.pe[k * L + tid]);
+        if (GRAD) {
+          const float4 p = m.pg[k * L + tid];
+          sx += p.x;
+          sy += p.y;
+          sz += p.z;
+        }
+      }
+      os.E[(size_t)c * L + tid] = e;
+      if (GRAD) os.G[(size_t)c * L + tid] = make_float4(sx, sy, sz, 0.f);
+    }
   }
   __threadfence();
   __syncthreads();
@@ -1359,18 +1401,17 @@ __global__ void __launch_bounds__(kFinishOne)
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  PairBatch pb;  // the first intra pairs of the finish, loaded ahead
-  if (nested && (flags & kFlagIntra)) load_pairs(lig, tid, pb);
-  // the last CTA: the partials of every CTA, thread (j, g) over CTAs g, g + S, ...
-  const int ncta = gridDim.x;
+  // the last CTA.  Nested groups with the gradient: the posed torsion frames
+  if (GRAD && nested && tid < nrb) torsion_frame(lig, m.Xh, m.Xl, m.saxis, tid);
+  // the partials of every pair CTA, thread (jq, gq) over chunks gq, gq + Sq, ...
   // (double-float sums on the FP32 pipe; loads in batches of kBatch)
+  const int npair = gridDim.x - os.with_intra;
   constexpr int kBatch = 10;
   const float2 z2 = make_float2(0.f, 0.f);
   float2 e = z2, sx = z2, sy = z2, sz = z2;
   float2 ev[kBatch];
   float4 gv[kBatch];
-  // threads (jq, gq), gq < Sq, over CTAs gq, gq + Sq, ...; the last warp is
-  // left free for the status
+  // the last warp is left free for the status
   const int Sq = (kFinishOne - 32) / L;
   const int jq = tid % L, gq = tid / L;
   const bool summing = gq < Sq;
@@ -1379,9 +1420,9 @@ __global__ void __launch_bounds__(kFinishOne)
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
       const int k = k0 + u * Sq;
-      ev[u] = k < ncta ? __ldcg(os.E + (size_t)k * L + jq) : z2;
+      ev[u] = k < npair ? __ldcg(os.E + (size_t)k * L + jq) : z2;
       if (GRAD)
-        gv[u] = k < ncta ? __ldcg(os.G + (size_t)k * L + jq) : make_float4(0.f, 0.f, 0.f, 0.f);
+        gv[u] = k < npair ? __ldcg(os.G + (size_t)k * L + jq) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
   };
   if (summing) load_batch();
@@ -1391,7 +1432,7 @@ __global__ void __launch_bounds__(kFinishOne)
     one_radius(lig, m);
   }
   if (summing) {
-    while (k0 < ncta) {
+    while (k0 < npair) {
 #pragma unroll
       for (int u = 0; u < kBatch; ++u) {
         e = dadd(e, ev[u]);
@@ -1402,7 +1443,7 @@ __global__ void __launch_bounds__(kFinishOne)
         }
       }
       k0 += kBatch * Sq;
-      if (k0 < ncta) load_batch();
+      if (k0 < npair) load_batch();
     }
     m.qe[tid] = e;
     if (GRAD) {
@@ -1413,7 +1454,6 @@ __global__ void __launch_bounds__(kFinishOne)
   }
   __syncthreads();
   if (tid < L) {
-    const float2 z2 = make_float2(0.f, 0.f);
     float2 e = z2, sx = z2, sy = z2, sz = z2;
     for (int k = 0; k < Sq; ++k) {
       e = dadd(e, m.qe[k * L + tid]);
@@ -1431,7 +1471,7 @@ __global__ void __launch_bounds__(kFinishOne)
   if (tid == 0) *os.arrive = 0u;  // ready for the next launch
   __syncthreads();
   if (nested) {
-    finish_one_nested<GRAD, RECENTER, DIEL, IFORM>(lig, io, m, flags, pb);
+    finish_one_nested<GRAD, RECENTER>(lig, io, m, flags, os.with_intra ? os.intra : nullptr);
     return;
   }
   // other ligands: the work buffers of the one-pose finishing code
@@ -1646,7 +1686,7 @@ cudaError_t one_t(const DevLigand& lig, const DevProtein& prot, const float4* ta
     if (e != cudaSuccess) return e;
   }
   *stage = 2;
-  k_one_pose<G, RC, D, F, IF><<<os.ncta, kFinishOne, smem, st>>>(lig, prot, tab4, io, s, os, flags);
+  k_one_pose<G, RC, D, F, IF><<<os.npair + os.with_intra, kFinishOne, smem, st>>>(lig, prot, tab4, io, s, os, flags);
   return cudaGetLastError();
 }
 

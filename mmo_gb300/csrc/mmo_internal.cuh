@@ -67,6 +67,9 @@ struct DevLigand {
   const float4* pair_par;   // [npairs] (x^2, D, K q_i q_j, the bits of the torsions whose
                             // group holds exactly one of the two atoms)
   const uint32_t* amask;    // [L] bit t set when the atom is in rotation group t
+  const float2* tax;        // [nrb][6] unit axis (centre - left) and centre of each
+                            // torsion in the reference conformer, double-float
+  const int* tord;          // [nrb] torsions by group size, smallest first
   const int* grp_off;       // [nrb + 1] rotation groups as CSR
   const int* grp_atoms;
   const int* nb_off;        // [L + 1] both-direction CSR of the same pairs
@@ -262,11 +265,13 @@ struct DevSystems {
 constexpr int kOneChunk = 128;  // protein atoms per CTA of the one-pose kernel
 
 struct OneScratch {
-  float2* E;          // [ncta][L] inter energy of each CTA's protein atoms per ligand atom
-                      // (double-float: hi, lo)
-  float4* G;          // [ncta][L] dE/dX of the same
+  float2* E;          // [npair][L] inter energy of each pair CTA's protein atoms per
+                      // ligand atom (double-float: hi, lo)
+  float4* G;          // [npair][L] dE/dX of the same
+  float* intra;       // [kMaxTors + 2] the intra CTA's torsion terms, then its energy
   unsigned* arrive;   // CTAs done; the last one clears it
-  int ncta, chunk;    // CTAs and protein atoms per CTA
+  int npair;          // pair CTAs (kOneChunk protein atoms each)
+  int with_intra;     // 1: CTA 0 takes the intra terms (nested groups with MMO_F_INTRA)
 };
 
 // ---- Monte Carlo chains (kernels_mc.cu) ----------------------------------
