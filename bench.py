@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-energy-only", action="store_true",
                     help="skip the 65,536-pose energy-only measurement of the main workload")
+    ap.add_argument("--no-large-pocket", action="store_true",
+                    help="skip the 4,096-pose line against the 12,000-atom pocket")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the default launch plan instead of the autotuner's")
     ap.add_argument("--workload", default="poses",
@@ -904,6 +906,71 @@ def energy_only_batch(args, torch, sc, L, dev, stream, flush):
             "E": E, "system": big}
 
 
+def large_pocket_batch(args, torch, L, dev, stream, flush):
+    """4,096 poses of the main line's 48-atom ligand with the gradient against a
+    12,000-atom pocket (22.7 A sphere: the 6,000-atom pocket's atom density),
+    above the sweep's shared-memory staging of the protein: device-resident
+    poses/s (L2 flushed before every step), the stage times and the sweep's cost
+    per evaluated pair, to set beside the main line's."""
+    from mmo_gb300 import synth
+    from mmo_gb300.ff import UFFScorer
+
+    sysm = synth.pose_batch(n_poses=4096, seed=1, n_pocket=12000, radius=22.7)
+    B = len(sysm.poses)
+    sc = UFFScorer(0)
+    sc.set_protein(sysm.pocket)
+    sc.set_ligand(sysm.ligand)
+    sp = stream.cuda_stream
+    d_dofs = torch.from_numpy(sysm.poses).to(dev)
+    d_E = torch.empty(B, dtype=torch.float64, device=dev)
+    d_G = torch.empty(sysm.poses.shape, dtype=torch.float32, device=dev)
+    d_st = torch.empty(B, dtype=torch.int32, device=dev)
+    flags = L.F_INTER | L.F_INTRA | L.F_GRAD
+
+    def step():
+        sc.score_poses_device(d_dofs.data_ptr(), B, d_E.data_ptr(), d_G.data_ptr(),
+                              d_st.data_ptr(), flags, sp)
+
+    tune_ms = None
+    if not args.no_tune:
+        tune_ms = sc.tune_device(d_dofs.data_ptr(), B, d_E.data_ptr(), d_G.data_ptr(),
+                                 d_st.data_ptr(), flags, sp)
+    for _ in range(3):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    steps = max(5, min(args.steps, 40))
+    sc.set_profiling(True)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    stage = []
+    for a, b in ev:
+        flush.zero_()
+        a.record(stream)
+        step()
+        b.record(stream)
+        stage.append(sc.stage_times())
+    torch.cuda.synchronize()
+    sc.set_profiling(False)
+    pairs_ev, pairs_all = sc.pair_count()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    st = np.mean(np.array(stage), axis=0)
+    out = {"metric": "poses/s (energy+grad)", "value": B * steps / (sum(ms) * 1e-3),
+           "unit": "poses/s", "ms_per_step": sum(ms) / steps, "steps": steps,
+           "config": {"workload": "energy+grad, 4096 poses/step, 48-atom ligand (8 torsions) vs "
+                                  "12000-atom pocket (22.7 A sphere)",
+                      "poses_per_step_per_gpu": B, "pocket_atoms": 12000,
+                      "l2": "flushed before every timed step",
+                      "plan": dict(sc.plan(), tuned_ms=tune_ms)},
+           "stages_ms": dict(zip(("rebuild", "sweep", "finish", "sort"), (float(v) for v in st))),
+           "pairs_evaluated": pairs_ev, "pairs_all": pairs_all,
+           "sweep_ns_per_evaluated_pair": float(st[1]) * 1e6 / pairs_ev,
+           "status_bits_set": int(np.count_nonzero(d_st.cpu().numpy())),
+           "E": d_E.cpu().numpy(), "G": d_G.cpu().numpy(), "system": sysm}
+    sc.close()
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -1053,6 +1120,10 @@ def main():
     cfg1 = None
     if not args.no_energy_only:
         cfg1 = energy_only_batch(args, torch, sc, L, dev, stream, flush)
+    # ---- 4,096 poses against a 12,000-atom pocket ----------------------------
+    big = None
+    if not args.no_large_pocket:
+        big = large_pocket_batch(args, torch, L, dev, stream, flush)
 
     # ---- roofline of the pair sweep -----------------------------------------
     peak = sc.fp32_peak_tflops()
@@ -1127,10 +1198,20 @@ def main():
             cfg1_sys = cfg1.pop("system")
             cfg1["errors"] = errors_vs_oracle(cfg1_sys, cfg1.pop("E")[idx], None, nthreads,
                                               poses=idx)
+        if big is not None:
+            idx = np.random.default_rng(8).choice(len(big["E"]), 256, replace=False)
+            big["errors"] = errors_vs_oracle(big["system"], big["E"][idx], big["G"][idx],
+                                             nthreads, poses=idx)
     if cfg1 is not None:
         cfg1.pop("E", None)
         cfg1.pop("system", None)
         line["energy_only_65536"] = cfg1
+    if big is not None:
+        for k in ("E", "G", "system"):
+            big.pop(k, None)
+        big["sweep_ns_per_evaluated_pair_main_line"] = (line["roofline"]["ms_per_launch"] * 1e6 /
+                                                        line["roofline"]["pairs_evaluated"])
+        line["pocket_12000"] = big
     if rank == 0:
         print(json.dumps(line), flush=True)
     sc.close()

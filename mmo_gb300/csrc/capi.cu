@@ -356,6 +356,7 @@ DevLigand ligand_at(const LigBlob& B, char* b, size_t* bytes) {
   L.amask = align_ptr<uint32_t>(b, off, n);
   L.tax = align_ptr<float2>(b, off, 6 * (size_t)std::max(nrb, 1));
   L.tord = align_ptr<int>(b, off, std::max(nrb, 1));
+  L.ramask = align_ptr<uint32_t>(b, off, n);
   L.grp_off = align_ptr<int>(b, off, nrb + 1);
   L.grp_atoms = align_ptr<int>(b, off, std::max(B.ngat, 1));
   L.nb_off = align_ptr<int>(b, off, n + 1);
@@ -490,6 +491,9 @@ void make_ligand_blob(int mixing, const LigIn& in, LigBlob* out) {
     for (int t = 0; t < nrb; ++t) ord[t] = t;
     std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return gsz[a] < gsz[b]; });
     if (nrb) memcpy((void*)H.tord, ord.data(), sizeof(int) * nrb);
+    for (int k = 0; k < nrb; ++k)
+      for (int g = in.goff[ord[k]]; g < in.goff[ord[k] + 1]; ++g)
+        const_cast<uint32_t*>(H.ramask)[in.gat[g]] |= 1u << k;
   }
   memcpy((void*)H.type, in.type.data(), sizeof(int) * n);
   for (int i = 0; i < n; ++i) const_cast<float*>(H.q)[i] = (float)in.q[i];
@@ -1144,9 +1148,9 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
   ctx->last_pairs = inter && !use_grid ? (double)B * L * ctx->prot.P : 0.0;
   // one pose with pair sums: the fused one-launch path (k_one_pose)
   const bool one = B == 1 && inter && !use_grid && ctx->one_ok;
-  // rebuild + finish, and the sweep: entry bin, scan, scatter, broad phase,
-  // sweep (or the grid lookup)
-  ctx->last_launches = one ? 1 : 2 + (cull ? 5 : (inter ? 1 : 0));
+  // rebuild (which bins the entries for the cut-off sweep) + finish, and the
+  // sweep: scan, scatter, broad phase, sweep (or the grid lookup)
+  ctx->last_launches = one ? 1 : 2 + (cull ? 4 : (inter ? 1 : 0));
   PairPlan plan{};
   int C = 1;
   int r;
@@ -1207,14 +1211,28 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
     }
     return MMO_OK;
   }
+  // with the cut-off sweep the rebuild also bins the entries (k_cull_bin's
+  // work), into the histogram reset just before it
+  Scratch sr = ctx->scr;
+  if (cull) {
+    sr.binning = 1;
+    sr.hist = ctx->cs.hist;
+    sr.bin = ctx->cs.bin;
+    sr.rank = ctx->cs.rank;
+    sr.seg_of_atom = ctx->cs.seg_of_atom;
+    for (int d = 0; d < 3; ++d) sr.glo[d] = ctx->cull.glo[d];
+    sr.ginv = ctx->cull.ginv;
+  }
   MMO_CK(mark(0), "event");
-  MMO_CK(launch_rebuild(ctx->lig, io, ctx->scr, fl, st), "rebuild kernel");
+  if (cull)
+    MMO_CK(cudaMemsetAsync(ctx->cs.hist, 0,
+                           sizeof(unsigned) * ctx->segs[grad ? 1 : 0].nseg * kCullBins, st),
+           "entry bin reset");
+  MMO_CK(launch_rebuild(ctx->lig, io, sr, fl, st), "rebuild kernel");
   MMO_CK(mark(1), "event");
   if (cull) {
     const CullSegs& sg = ctx->segs[grad ? 1 : 0];
-    MMO_CK(cudaMemsetAsync(ctx->cs.hist, 0, sizeof(unsigned) * sg.nseg * kCullBins, st),
-           "entry bin reset");
-    MMO_CK(launch_cull_sort(ctx->cull, ctx->scr, ctx->lig.q, B, L, sg, ctx->cs, st),
+    MMO_CK(launch_cull_sort(ctx->cull, ctx->scr, ctx->lig.q, B, L, sg, ctx->cs, true, st),
            "entry sort kernels");
     MMO_CK(mark(2), "event");
     MMO_CK(launch_pairs_cull(ctx->cull, ctx->d_tab4, sg, ctx->cs, fl, ctx->ph, ctx->cplan[grad], d_err,
@@ -1398,10 +1416,8 @@ int sys_build_static(mmo_ctx* ctx, SysBatch* S) {
   const int nv = (int)S->info.size();
   // threads per pose of the rebuild, as launch_rebuild chooses them
   int tpp = 32;
-  while (tpp > 1 && (long)S->B * (tpp / 2) >= 20000) tpp /= 2;
-  while (tpp < 32 && (sizeof(double) * (3.0 * S->Lmax + 2.0 * (3 + kMaxTors)) +
-                      sizeof(float4) * kMaxTors) * (128 / tpp) > 200.0 * 1024)
-    tpp *= 2;
+  while (tpp > 1 && (long)S->B * (tpp / 2) >= kRebuildThreadsInFlight) tpp /= 2;
+  while (tpp < 32 && rebuild_smem(S->Lmax, S->nrbmax, 128 / tpp) > 200 * 1024) tpp *= 2;
   S->tpp = tpp;
   const int ppb = 128 / tpp;
   std::vector<SysBlk> rblk, fblk;

@@ -41,45 +41,6 @@ __device__ __forceinline__ void stage_pair_table(const float4* __restrict__ tabv
   }
 }
 
-// Index of cell (x, y, z) of the 32^3 binning grid along a 3-D Hilbert curve
-// (J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc. 707, 2004:
-// axes to transposed index, then the bits interleaved).  Consecutive slots in
-// Hilbert order stay closer together than in Morton order, so the groups'
-// boxes are smaller.
-template <int kBits = 5>
-__device__ __forceinline__ uint32_t hilbert_cell(uint32_t x, uint32_t y, uint32_t z) {
-  uint32_t X[3] = {x, y, z};
-  for (uint32_t Q = 1u << (kBits - 1); Q > 1; Q >>= 1) {
-    const uint32_t P = Q - 1;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      if (X[i] & Q) {
-        X[0] ^= P;
-      } else {
-        const uint32_t t = (X[0] ^ X[i]) & P;
-        X[0] ^= t;
-        X[i] ^= t;
-      }
-    }
-  }
-  X[1] ^= X[0];
-  X[2] ^= X[1];
-  uint32_t t = 0;
-  for (uint32_t Q = 1u << (kBits - 1); Q > 1; Q >>= 1)
-    if (X[2] & Q) t ^= Q - 1;
-  uint32_t k = 0;
-#pragma unroll
-  for (int b = kBits - 1; b >= 0; --b)
-#pragma unroll
-    for (int i = 0; i < 3; ++i) k = (k << 1) | (((X[i] ^ t) >> b) & 1u);
-  return k;
-}
-
-__device__ __forceinline__ int grid_cell(float v, float lo, float inv) {
-  // NaN converts to 0; the clamp keeps infinities and far entries on the grid
-  return min(max(__float2int_rd((v - lo) * inv), 0), kCullGrid - 1);
-}
-
 __global__ void k_cull_bin(const float4* __restrict__ X, int n, int L,
                            const int* __restrict__ seg_of_atom, DevCull cull, unsigned* hist,
                            int* bin, int* rank) {
@@ -781,11 +742,13 @@ int cull_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_b
 }
 
 cudaError_t launch_cull_sort(const DevCull& cull, const Scratch& s, const float* lig_q, int B,
-                             int L, const CullSegs& seg, const CullScratch& cs, cudaStream_t st) {
+                             int L, const CullSegs& seg, const CullScratch& cs, bool binned,
+                             cudaStream_t st) {
   const int n = B * L;
   if (n <= 0) return cudaSuccess;
   const int tb = 256, nb = (n + tb - 1) / tb;
-  k_cull_bin<<<nb, tb, 0, st>>>(s.X, n, L, cs.seg_of_atom, cull, cs.hist, cs.bin, cs.rank);
+  if (!binned)  // (the rebuild bins the entries when it can)
+    k_cull_bin<<<nb, tb, 0, st>>>(s.X, n, L, cs.seg_of_atom, cull, cs.hist, cs.bin, cs.rank);
   cudaError_t e = cudaFuncSetAttribute(k_cull_scan, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        kScanSmem);
   if (e != cudaSuccess) return e;

@@ -70,27 +70,8 @@ __device__ __forceinline__ float2 rodrigues_entry(int k, float2 c, float2 ux, fl
 }
 
 // entry k of R = Rz(g) Ry(b) Rx(a) (rot.ml:52-66), k = 9..11 the translation
-__device__ __forceinline__ double rigid_entry(int k, const double* SC, const float* dof, float orx,
-                                              float ory, float orz) {
-  const double sa = SC[0], ca = SC[1], sb = SC[2], cb = SC[3], sg = SC[4], cg = SC[5];
-  switch (k) {
-    case 0: return cb * cg;
-    case 1: return cg * sa * sb - ca * sg;
-    case 2: return sa * sg + ca * cg * sb;
-    case 3: return cb * sg;
-    case 4: return ca * cg + sa * sb * sg;
-    case 5: return ca * sb * sg - cg * sa;
-    case 6: return -sb;
-    case 7: return cb * sa;
-    case 8: return ca * cb;
-    case 9: return (double)dof[0] - (double)orx;
-    case 10: return (double)dof[1] - (double)ory;
-    default: return (double)dof[2] - (double)orz;
-  }
-}
-
-// rigid_entry from the double-float sines and cosines t[0..2] = (sin hi, sin
-// lo, cos hi, cos lo) of a, b, g: the same products in double-float
+// (dof - origin), in double-float from the sines and cosines t[0..2] = (sin
+// hi, sin lo, cos hi, cos lo) of a, b, g
 __device__ __forceinline__ float2 rigid_entry_df(int k, const float4* t, const float* dof,
                                                  float orx, float ory, float orz) {
   const float2 sa = make_float2(t[0].x, t[0].y), ca = make_float2(t[0].z, t[0].w);
@@ -134,19 +115,21 @@ template <bool RECENTER, bool RECORD, int TPP>
 __device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof, bool live,
                                              float orx, float ory, float orz, float4* Xo,
                                              float4* Yo, float4* reco, float4* ceno,
-                                             int* statuso) {
+                                             int* statuso, const Scratch* sb, size_t e0) {
   constexpr int PPB = kRebuildThreads / TPP;  // poses per block
   constexpr int NANG = 3 + kMaxTors;
-  // [3][L][PPB] double-float coordinates, then [PPB][NANG] FP64 (sin, cos),
-  // then [PPB][kMaxTors] double-float (sin, cos) of the torsions
+  // rebuild_smem's layout: [3][L][PPB] double-float coordinates, then
+  // [PPB][NANG] double-float (sin, cos) of the angles, then (nested groups)
+  // [PPB][nrb][12] the torsions' rotations about their reference axes
   extern __shared__ double sz[];
   const int tid = threadIdx.x, p = tid / TPP, sub = tid % TPP;
   const int L = lig.L, nrb = lig.nrb;
   float2* X = reinterpret_cast<float2*>(sz);
   float2* Yc = X + L * PPB;
   float2* Zc = X + 2 * L * PPB;
-  double* SC = sz + 3 * L * PPB + p * NANG * 2;
-  float4* TSC = reinterpret_cast<float4*>(sz + 3 * L * PPB + PPB * NANG * 2) + p * kMaxTors;
+  float4* TSC = reinterpret_cast<float4*>(sz + 3 * L * PPB) + p * NANG;
+  float2* ROT = reinterpret_cast<float2*>(reinterpret_cast<float4*>(sz + 3 * L * PPB) + PPB * NANG) +
+                (size_t)p * nrb * 12;
 #define AT(arr, a) arr[(a) * PPB + p]
   for (int a = sub; a < L; a += TPP) {
     AT(X, a) = lig.ref2[3 * a];
@@ -154,15 +137,47 @@ __device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof
     AT(Zc, a) = lig.ref2[3 * a + 2];
   }
   for (int k = sub; k < 3 + nrb; k += TPP) {
-    sincos((double)dof[3 + k], &SC[2 * k], &SC[2 * k + 1]);
-    if (k >= 3) {
-      const float2 sn = df_of(SC[2 * k]), cs = df_of(SC[2 * k + 1]);
-      TSC[k - 3] = make_float4(sn.x, sn.y, cs.x, cs.y);
-    }
+    float2 sn, cs;
+    df_sincos(dof[3 + k], sn, cs);
+    TSC[k] = make_float4(sn.x, sn.y, cs.x, cs.y);
   }
   __syncwarp();
   const float2 one = make_float2(1.f, 0.f);
-  for (int t = 0; t < nrb; ++t) {
+  if (lig.nested) {
+    // nested groups: each atom's rotations about the reference-frame axes,
+    // innermost group first (equal to the bond-order application); the
+    // rotations' entries split over the pose's lanes
+    for (int e = sub; e < 12 * nrb; e += TPP) {
+      const int t = e / 12, k = e - 12 * t;
+      const float2* tx = lig.tax + 6 * t;
+      if (k >= 9) {
+        ROT[e] = tx[k - 6];
+      } else {
+        const float2 ux = tx[0], uy = tx[1], uz = tx[2];
+        const float4 tsc = TSC[3 + t];
+        const float2 sn = make_float2(tsc.x, tsc.y), cs = make_float2(tsc.z, tsc.w);
+        ROT[e] = rodrigues_entry(k, cs, ux, uy, uz, dsub(one, cs), dmul(ux, sn), dmul(uy, sn),
+                                 dmul(uz, sn));
+      }
+    }
+    __syncwarp();
+    for (int a = sub; a < L; a += TPP) {
+      float2 x = AT(X, a), y = AT(Yc, a), z = AT(Zc, a);
+      // the atom's own groups only, innermost first
+      for (uint32_t mk = lig.ramask[a]; mk; mk &= mk - 1) {
+        const float2* R = ROT + 12 * lig.tord[__ffs(mk) - 1];
+        const float2 vx = dsub(x, R[9]), vy = dsub(y, R[10]), vz = dsub(z, R[11]);
+        x = ddot3c(R[0], vx, R[1], vy, R[2], vz, R[9]);
+        y = ddot3c(R[3], vx, R[4], vy, R[5], vz, R[10]);
+        z = ddot3c(R[6], vx, R[7], vy, R[8], vz, R[11]);
+      }
+      AT(X, a) = x;
+      AT(Yc, a) = y;
+      AT(Zc, a) = z;
+    }
+    __syncwarp();
+  }
+  for (int t = 0; t < (lig.nested ? 0 : nrb); ++t) {
     const int2 bd = lig.bonds[t];
     const float2 cx = AT(X, bd.y), cy = AT(Yc, bd.y), cz = AT(Zc, bd.y);
     const float2 ax = dsub(cx, AT(X, bd.x)), ay = dsub(cy, AT(Yc, bd.x)),
@@ -173,7 +188,7 @@ __device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof
     const float2 err = dsub(one, dmul(n2, dmul(make_float2(r0, 0.f), make_float2(r0, 0.f))));
     const float2 inv = qts(r0, __fmul_rn(0.5f * r0, err.x));
     const float2 ux = dmul(ax, inv), uy = dmul(ay, inv), uz = dmul(az, inv);
-    const float4 tsc = TSC[t];
+    const float4 tsc = TSC[3 + t];
     const float2 sn = make_float2(tsc.x, tsc.y), cs = make_float2(tsc.z, tsc.w);
     const float2 o = dsub(one, cs);
     const float2 xs = dmul(ux, sn), ys = dmul(uy, sn), zs = dmul(uz, sn);
@@ -195,7 +210,7 @@ __device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof
       AT(Yc, i) = ddot3c(R[3], vx, R[4], vy, R[5], vz, cy);
       AT(Zc, i) = ddot3c(R[6], vx, R[7], vy, R[8], vz, cz);
     }
-    if (RECORD && live && sub == 0) {
+    if (RECORD && !lig.nested && live && sub == 0) {
       float4* r = reco + (size_t)t * 3;
       r[0] = make_float4(cx.x, cy.x, cz.x, cs.x);
       r[1] = make_float4(ux.x, uy.x, uz.x, sn.x);
@@ -237,7 +252,7 @@ __device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof
 #pragma unroll
   for (int q = 0; q < (12 + TPP - 1) / TPP; ++q) {
     const int k = sub + q * TPP;
-    rm[q] = k < 12 ? df_of(rigid_entry(k, SC, dof, orx, ory, orz)) : one;
+    rm[q] = k < 12 ? rigid_entry_df(k, TSC, dof, orx, ory, orz) : one;
   }
   float2 G[12];
 #pragma unroll
@@ -247,16 +262,25 @@ __device__ __noinline__ void rebuild_pose(const DevLigand& lig, const float* dof
   if (live) {
     for (int a = sub; a < L; a += TPP) {
       const float2 vx = dsub(AT(X, a), ox), vy = dsub(AT(Yc, a), oy), vz = dsub(AT(Zc, a), oz);
-      store_pair(Xo + (size_t)a * 2, ddot3c(G[0], vx, G[1], vy, G[2], vz, G[9]),
-                 ddot3c(G[3], vx, G[4], vy, G[5], vz, G[10]),
-                 ddot3c(G[6], vx, G[7], vy, G[8], vz, G[11]));
-      if (RECORD) {  // hi and lo parts: the reverse pass takes its lever arms from them
+      const float2 px = ddot3c(G[0], vx, G[1], vy, G[2], vz, G[9]);
+      const float2 py = ddot3c(G[3], vx, G[4], vy, G[5], vz, G[10]);
+      const float2 pz = ddot3c(G[6], vx, G[7], vy, G[8], vz, G[11]);
+      store_pair(Xo + (size_t)a * 2, px, py, pz);
+      if (sb) {  // the cut-off sweep's entry binning (k_cull_bin's operations)
+        const uint32_t cx = grid_cell(px.x, sb->glo[0], sb->ginv);
+        const uint32_t cy = grid_cell(py.x, sb->glo[1], sb->ginv);
+        const uint32_t cz = grid_cell(pz.x, sb->glo[2], sb->ginv);
+        const int bn = sb->seg_of_atom[a] * kCullBins + (int)hilbert_cell(cx, cy, cz);
+        sb->bin[e0 + a] = bn;
+        sb->rank[e0 + a] = (int)atomicAdd(&sb->hist[bn], 1u);
+      }
+      if (RECORD && !lig.nested) {  // hi and lo parts: the reverse pass's lever arms
         Yo[2 * a] = make_float4(AT(X, a).x, AT(Yc, a).x, AT(Zc, a).x, 0.f);
         Yo[2 * a + 1] = make_float4(AT(X, a).y, AT(Yc, a).y, AT(Zc, a).y, 0.f);
       }
     }
     if (sub == 0) {
-      if (RECORD) {
+      if (RECORD && !lig.nested) {
         ceno[0] = make_float4(mx.x, my.x, mz.x, 0.f);
         ceno[1] = make_float4(mx.y, my.y, mz.y, 0.f);
       }
@@ -276,7 +300,8 @@ __global__ void __launch_bounds__(kRebuildThreads) k_rebuild(DevLigand lig, Pose
   rebuild_pose<RECENTER, RECORD, TPP>(
       lig, io.dofs + bb * nd, live, io.ox, io.oy, io.oz, scr.X + bb * L * 2,
       RECORD ? scr.Y + bb * L * 2 : nullptr, RECORD ? scr.rec + bb * nrb * 3 : nullptr,
-      RECORD ? scr.cen + bb * 2 : nullptr, io.status + bb);
+      RECORD ? scr.cen + bb * 2 : nullptr, io.status + bb, scr.binning ? &scr : nullptr,
+      bb * L);
   if (live && b == 0 && threadIdx.x % TPP == 0 && io.zero_err) *io.err = 0;
 }
 
@@ -396,9 +421,9 @@ template <bool GRAD, bool RECENTER, int DIEL, int IFORM>
 __device__ __noinline__ void finish_pose(const DevLigand& lig, int C, const double* ep,
                                             const float4* gp, const float4* Xb, const float4* Yb,
                                             const float4* recb, const float4* cenp,
-                                            const float* dof, float* grad, double* Eo, int* sto,
-                                            double* Eio, int flags, float4* wsm,
-                                            double pre_e = 0.0,
+                                            const float* dof, float orx, float ory, float orz,
+                                            float* grad, double* Eo, int* sto, double* Eio,
+                                            int flags, float4* wsm, double pre_e = 0.0,
                                             const float* pre_dti = nullptr) {
   const bool pre = pre_dti != nullptr;
   const int lane = threadIdx.x & 31;
@@ -408,13 +433,13 @@ __device__ __noinline__ void finish_pose(const DevLigand& lig, int C, const doub
   float4* saxis = sxl + L;        // [nrb] final axes, then [nrb] centres
   float4* srec = saxis + 2 * nrb;  // [nrb][3] torsion records
   float* sdti = reinterpret_cast<float*>(srec + 3 * nrb);  // [nrb][33]
-  if (GRAD)  // the reverse pass reads them last: start the loads now
+  if (GRAD && !lig.nested)  // the reverse pass reads them last: start the loads now
     for (int k = lane; k < 3 * nrb; k += 32) srec[k] = recb[k];
   const bool intra = flags & kFlagIntra, inter = flags & kFlagInter;
   double e = 0.0;
   if (inter)
     for (int k = lane; k < C * L; k += 32) e += ep[k];
-  if (intra) {
+  if (intra || (GRAD && lig.nested)) {  // (nested groups: the levers of the torsion sums)
     for (int a = lane; a < L; a += 32) {
       sxh[a] = Xb[(size_t)a * 2];
       sxl[a] = Xb[(size_t)a * 2 + 1];
@@ -484,6 +509,121 @@ __device__ __noinline__ void finish_pose(const DevLigand& lig, int C, const doub
         }
       }
     }
+  }
+  if (lig.nested) {
+    // Nested groups: the gradient from the posed frame alone.  Rigid map:
+    // dE/dt = F = sum G; dE/dR_kc = M_kc = sum_i G_ik Yc_ic with
+    // Yc = R^T (X - t), so M = P R for P_rk = sum_i G_ir (X_i - t)_k.
+    // Torsion t: w_t . sum_{i in G_t} (X_i - C_t) x (G_i - F / L) (F / L only
+    // with the centroid removed) plus the straddling intra terms.
+    __syncwarp();
+    if (lane < nrb) torsion_frame(lig, sxh, sxl, saxis, lane);
+    __syncwarp();
+    float dti_mine = 0.f;
+    if (crossing && pre) {
+      if (lane < nrb) dti_mine = pre_dti[lane];
+    } else if (crossing) {
+      if (lane < nrb)
+        for (int k = 0; k < 32; ++k) dti_mine += sdti[lane * 33 + k];
+    }
+    const float2 tx2 = ts(dof[0], -orx), ty2 = ts(dof[1], -ory), tz2 = ts(dof[2], -orz);
+    float red[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) red[k] = 0.f;
+    // the total force in double-float: the atoms' forces can cancel by orders
+    // of magnitude in a clash
+    float2 fsum[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+    for (int s = 0; s < kSlots; ++s) {
+      const int a = lane + 32 * s;
+      if (a < L) {
+        const float4 ph = sxh[a], pl = sxl[a];
+        const float qx = split_diff(ph.x, pl.x, tx2.x, tx2.y);
+        const float qy = split_diff(ph.y, pl.y, ty2.x, ty2.y);
+        const float qz = split_diff(ph.z, pl.z, tz2.x, tz2.y);
+        acc2(fsum[0], gx[s]);
+        acc2(fsum[1], gy[s]);
+        acc2(fsum[2], gz[s]);
+        red[3] += gx[s] * qx; red[4] += gx[s] * qy; red[5] += gx[s] * qz;
+        red[6] += gy[s] * qx; red[7] += gy[s] * qy; red[8] += gy[s] * qz;
+        red[9] += gz[s] * qx; red[10] += gz[s] * qy; red[11] += gz[s] * qz;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) fsum[k] = dadd(fsum[k], dshfl_xor(fsum[k], o));
+      red[k] = __fadd_rn(fsum[k].x, fsum[k].y);
+    }
+#pragma unroll
+    for (int k = 3; k < 12; ++k) red[k] = warp_sum(red[k]);
+    float sa, ca, sb, cb, sg, cg;
+    sincosf(dof[3], &sa, &ca);
+    sincosf(dof[4], &sb, &cb);
+    sincosf(dof[5], &sg, &cg);
+    if (lane == 0) {
+      const float R[9] = {cb * cg, cg * sa * sb - ca * sg, sa * sg + ca * cg * sb,
+                          cb * sg, ca * cg + sa * sb * sg, ca * sb * sg - cg * sa,
+                          -sb,     cb * sa,                 ca * cb};
+      float M[9];
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          M[3 * r + c] = red[3 + 3 * r] * R[c] + red[4 + 3 * r] * R[3 + c] +
+                         red[5 + 3 * r] * R[6 + c];
+      // d R / d a, d b, d g of rot.ml:52-66, entry by entry
+      const float dA[9] = {0.f, cg * ca * sb + sa * sg, ca * sg - sa * cg * sb,
+                           0.f, -sa * cg + ca * sb * sg, -sa * sb * sg - cg * ca,
+                           0.f, cb * ca, -sa * cb};
+      const float dB[9] = {-sb * cg, cg * sa * cb, ca * cg * cb,
+                           -sb * sg, sa * cb * sg, ca * cb * sg,
+                           -cb, -sb * sa, -ca * sb};
+      const float dG[9] = {-cb * sg, -sg * sa * sb - ca * cg, sa * cg - ca * sg * sb,
+                           cb * cg, -ca * sg + sa * sb * cg, ca * sb * cg + sg * sa,
+                           0.f, 0.f, 0.f};
+      float ga = 0.f, gb = 0.f, gg = 0.f;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        ga += M[k] * dA[k];
+        gb += M[k] * dB[k];
+        gg += M[k] * dG[k];
+      }
+      grad[0] = red[0];
+      grad[1] = red[1];
+      grad[2] = red[2];
+      grad[3] = ga;
+      grad[4] = gb;
+      grad[5] = gg;
+    }
+    const float iL = 1.0f / (float)L;
+    const float fx = RECENTER ? red[0] * iL : 0.f, fy = RECENTER ? red[1] * iL : 0.f,
+                fz = RECENTER ? red[2] * iL : 0.f;
+    for (int t = 0; t < nrb; ++t) {
+      const float4 w = saxis[t];
+      const int ci = __float_as_int(w.w);
+      const float4 ch = sxh[ci], cl = sxl[ci];
+      float cx = 0.f, cy = 0.f, cz = 0.f;
+#pragma unroll
+      for (int s = 0; s < kSlots; ++s) {
+        if (32 * s >= L) break;  // uniform: no atoms in this slot
+        if ((lig.gmask[t * kSlots + s] >> lane) & 1u) {
+          const int a = lane + 32 * s;
+          const float4 ah = sxh[a], al = sxl[a];
+          const float lx = split_diff(ah.x, al.x, ch.x, cl.x);
+          const float ly = split_diff(ah.y, al.y, ch.y, cl.y);
+          const float lz = split_diff(ah.z, al.z, ch.z, cl.z);
+          const float hx = gx[s] - fx, hy = gy[s] - fy, hz = gz[s] - fz;
+          cx += ly * hz - lz * hy;
+          cy += lz * hx - lx * hz;
+          cz += lx * hy - ly * hx;
+        }
+      }
+      const float v = warp_sum(w.x * cx + w.y * cy + w.z * cz);
+      const float intra_t = __shfl_sync(kFull, dti_mine, t & 31);
+      if (lane == 0) grad[6 + t] = v + intra_t;
+    }
+    return;
   }
   // coordinates after the torsions (recorded by k_rebuild): hi parts in
   // registers, lo parts in the warp's shared memory (the slot of the posed
@@ -695,7 +835,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kFinishBlocksPerSM)
   finish_pose<GRAD, RECENTER, DIEL, IFORM>(
       lig, C, scr.Epart + ent * C, GRAD ? scr.Gpart + ent * C : nullptr, scr.X + ent * 2,
       GRAD ? scr.Y + ent * 2 : nullptr, GRAD ? scr.rec + (size_t)b * nrb * 3 : nullptr,
-      GRAD ? scr.cen + b * 2 : nullptr, io.dofs + (size_t)b * nd,
+      GRAD ? scr.cen + b * 2 : nullptr, io.dofs + (size_t)b * nd, io.ox, io.oy, io.oz,
       GRAD ? io.grad + (size_t)b * nd : nullptr, io.E + b, io.status + b,
       io.E_inter ? io.E_inter + b : nullptr, flags, fsm + wib * finish_warp_f4(L, nrb));
 }
@@ -758,8 +898,9 @@ __device__ __forceinline__ void finish_one_cta(const DevLigand& lig, const PoseI
   if (tid >= 32) return;  // warp 0 alone from here: no block-wide barrier follows
   finish_pose<GRAD, RECENTER, DIEL, IFORM>(
       lig, scr.C, scr.Epart, GRAD ? scr.Gpart : nullptr, scr.X, GRAD ? scr.Y : nullptr,
-      GRAD ? scr.rec : nullptr, GRAD ? scr.cen : nullptr, io.dofs, GRAD ? io.grad : nullptr,
-      io.E, io.status, io.E_inter, flags, wsm, intra ? sred[kFinishOne / 32] : 0.0, stot);
+      GRAD ? scr.rec : nullptr, GRAD ? scr.cen : nullptr, io.dofs, io.ox, io.oy, io.oz,
+      GRAD ? io.grad : nullptr, io.E, io.status, io.E_inter, flags, wsm,
+      intra ? sred[kFinishOne / 32] : 0.0, stot);
 }
 
 template <bool GRAD, bool RECENTER, int DIEL, int IFORM>
@@ -1051,17 +1192,14 @@ __device__ __forceinline__ void one_torsions_nested(const DevLigand& lig, const 
   }
   __syncthreads();
   if (tid < L) {
-    const uint32_t am = m.amask[tid];
     float2 x = m.x[tid], y = m.y[tid], z = m.z[tid];
-    for (int k = 0; k < nrb; ++k) {
-      const int t = m.ord[k];
-      if ((am >> t) & 1u) {
-        const float2* R = m.rot + 12 * t;
-        const float2 vx = dsub(x, R[9]), vy = dsub(y, R[10]), vz = dsub(z, R[11]);
-        x = ddot3c(R[0], vx, R[1], vy, R[2], vz, R[9]);
-        y = ddot3c(R[3], vx, R[4], vy, R[5], vz, R[10]);
-        z = ddot3c(R[6], vx, R[7], vy, R[8], vz, R[11]);
-      }
+    // the atom's own groups only, innermost first
+    for (uint32_t mk = lig.ramask[tid]; mk; mk &= mk - 1) {
+      const float2* R = m.rot + 12 * m.ord[__ffs(mk) - 1];
+      const float2 vx = dsub(x, R[9]), vy = dsub(y, R[10]), vz = dsub(z, R[11]);
+      x = ddot3c(R[0], vx, R[1], vy, R[2], vz, R[9]);
+      y = ddot3c(R[3], vx, R[4], vy, R[5], vz, R[10]);
+      z = ddot3c(R[6], vx, R[7], vy, R[8], vz, R[11]);
     }
     m.x[tid] = x;
     m.y[tid] = y;
@@ -1225,11 +1363,20 @@ __device__ __forceinline__ void finish_one_nested(const DevLigand& lig, const Po
       // the coordinates after the torsions less the rotation origin
       const int q = it;
       float s = 0.f;
+      if (q < 3) {  // the total force in double-float (clash forces cancel)
+        float2 f = make_float2(0.f, 0.f);
+        for (int a = lane; a < L; a += 32) {
+          const float4 g = m.sG[a];
+          acc2(f, q == 0 ? g.x : (q == 1 ? g.y : g.z));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) f = dadd(f, dshfl_xor(f, o));
+        if (lane == 0) m.red[q] = __fadd_rn(f.x, f.y);
+        continue;
+      }
       for (int a = lane; a < L; a += 32) {
         const float4 g = m.sG[a];
-        if (q < 3) {
-          s += q == 0 ? g.x : (q == 1 ? g.y : g.z);
-        } else {
+        {
           const int r = (q - 3) / 3, c = q - 3 - 3 * r;
           const float gr = r == 0 ? g.x : (r == 1 ? g.y : g.z);
           const float2 yv = c == 0 ? m.x[a] : (c == 1 ? m.y[a] : m.z[a]);
@@ -1527,8 +1674,7 @@ template <bool RC, bool REC, int TPP>
 cudaError_t rebuild_t(const DevLigand& lig, const PoseIO& io, const Scratch& s, cudaStream_t st) {
   constexpr int PPB = kRebuildThreads / TPP;
   const int blocks = (io.B + PPB - 1) / PPB;
-  const size_t smem = sizeof(double) * ((size_t)3 * lig.L * PPB + (size_t)PPB * (3 + kMaxTors) * 2) +
-                      sizeof(float4) * (size_t)PPB * kMaxTors;
+  const size_t smem = rebuild_smem(lig.L, lig.nrb, PPB);
   cudaError_t e = cudaFuncSetAttribute(k_rebuild<RC, REC, TPP>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -1593,7 +1739,7 @@ __global__ void __launch_bounds__(kRebuildThreads)
   rebuild_pose<RECENTER, RECORD, TPP>(
       slig, io.dofs + (size_t)inf.dof0 + (size_t)lp * (6 + nrb), live, inf.ox, inf.oy, inf.oz,
       scr.X + ent * 2, RECORD ? scr.Y + ent * 2 : nullptr, RECORD ? scr.rec + rec * 3 : nullptr,
-      RECORD ? scr.cen + b * 2 : nullptr, io.status + b);
+      RECORD ? scr.cen + b * 2 : nullptr, io.status + b, nullptr, 0);
 }
 
 template <bool GRAD, bool RECENTER, int DIEL, int IFORM>
@@ -1614,16 +1760,16 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, kFinishBlocksPerSM)
   finish_pose<GRAD, RECENTER, DIEL, IFORM>(
       slig, 1, scr.Epart + ent, GRAD ? scr.Gpart + ent : nullptr, scr.X + ent * 2,
       GRAD ? scr.Y + ent * 2 : nullptr, GRAD ? scr.rec + rec * 3 : nullptr,
-      GRAD ? scr.cen + b * 2 : nullptr, io.dofs + dof, GRAD ? io.grad + dof : nullptr, io.E + b,
-      io.status + b, nullptr, flags, fsm + wib * finish_warp_f4(S.Lmax, S.nrbmax));
+      GRAD ? scr.cen + b * 2 : nullptr, io.dofs + dof, inf.ox, inf.oy, inf.oz,
+      GRAD ? io.grad + dof : nullptr, io.E + b, io.status + b, nullptr, flags,
+      fsm + wib * finish_warp_f4(S.Lmax, S.nrbmax));
 }
 
 template <bool RC, bool REC>
 cudaError_t sys_rebuild_tpp(int tpp, const DevSystems& S, int nblk, const PoseIO& io,
                             const Scratch& s, cudaStream_t st) {
   const int ppb = kRebuildThreads / tpp;
-  const int smem = (int)(sizeof(double) * (3 * (size_t)S.Lmax * ppb + (size_t)ppb * (3 + kMaxTors) * 2) +
-                         sizeof(float4) * (size_t)ppb * kMaxTors);
+  const int smem = (int)rebuild_smem(S.Lmax, S.nrbmax, ppb);
 #define MMO_SR(T)                                                                          \
   case T: {                                                                                \
     cudaError_t e = cudaFuncSetAttribute(k_sys_rebuild<RC, REC, T>,                        \
@@ -1659,13 +1805,12 @@ cudaError_t launch_rebuild(const DevLigand& lig, const PoseIO& io, const Scratch
   if (io.B <= 0) return cudaSuccess;
   const bool rc = flags & kFlagRecenter;
   const bool rec = (flags & kFlagGrad) && io.grad;
-  // threads per pose: enough threads in flight to hide the latency (about
-  // 20,000), within 200 KB of shared memory
+  // threads per pose: up to a warp per pose while the batch keeps fewer than
+  // about 160,000 threads in flight (half of GB300's 152 x 2,048), within 200 KB
+  // of shared memory; more threads per pose shorten each pose's chain
   int tpp = 32;
-  while (tpp > 1 && (long)io.B * (tpp / 2) >= 20000) tpp /= 2;
-  while (tpp < 32 && (sizeof(double) * (3.0 * lig.L + 2.0 * (3 + kMaxTors)) +
-                      sizeof(float4) * kMaxTors) * (kRebuildThreads / tpp) > 200.0 * 1024)
-    tpp *= 2;
+  while (tpp > 1 && (long)io.B * (tpp / 2) >= kRebuildThreadsInFlight) tpp /= 2;
+  while (tpp < 32 && rebuild_smem(lig.L, lig.nrb, kRebuildThreads / tpp) > 200 * 1024) tpp *= 2;
   if (rc) return rec ? rebuild_tpp<true, true>(tpp, lig, io, s, st)
                      : rebuild_tpp<true, false>(tpp, lig, io, s, st);
   return rec ? rebuild_tpp<false, true>(tpp, lig, io, s, st)

@@ -70,6 +70,7 @@ struct DevLigand {
   const float2* tax;        // [nrb][6] unit axis (centre - left) and centre of each
                             // torsion in the reference conformer, double-float
   const int* tord;          // [nrb] torsions by group size, smallest first
+  const uint32_t* ramask;   // [L] bit k set when the atom is in the group of tord[k]
   const int* grp_off;       // [nrb + 1] rotation groups as CSR
   const int* grp_atoms;
   const int* nb_off;        // [L + 1] both-direction CSR of the same pairs
@@ -98,6 +99,16 @@ struct Scratch {
   float4* cen;     // [B][2] centroid of Y, hi then lo (gradient only)
   int C;
   uint32_t first_wait_polls = kWaitPollsDefault;  // polls of the full sweep's first TMA wait
+  // the cut-off sweep's entry binning, done by the rebuild when binning != 0:
+  // entry e = b L + j of pose b, ligand atom j goes to bin seg_of_atom[j]
+  // kCullBins + its Hilbert cell, rank[e] its place in the bin (hist counts)
+  int binning = 0;
+  unsigned* hist = nullptr;
+  int* bin = nullptr;
+  int* rank = nullptr;
+  const int* seg_of_atom = nullptr;
+  float glo[3] = {0.f, 0.f, 0.f};
+  float ginv = 0.f;
 };
 
 struct PoseIO {
@@ -263,6 +274,13 @@ struct DevSystems {
 
 // ---- the one-pose path in one launch (kernels_pose.cu, k_one_pose) --------
 constexpr int kOneChunk = 128;  // protein atoms per CTA of the one-pose kernel
+// threads in flight the pose rebuild aims for (threads per pose x poses)
+constexpr long kRebuildThreadsInFlight = 160000;
+// dynamic shared memory of a rebuild block of ppb poses (rebuild_pose's layout)
+inline size_t rebuild_smem(int L, int nrb, int ppb) {
+  return sizeof(float2) * 3 * (size_t)L * ppb + sizeof(float4) * (size_t)ppb * (3 + kMaxTors) +
+         sizeof(float2) * 12 * (size_t)ppb * nrb;
+}
 
 struct OneScratch {
   float2* E;          // [npair][L] inter energy of each pair CTA's protein atoms per
@@ -483,7 +501,7 @@ cudaError_t launch_intra_plain(const DevLigand& lig, const float4* X, int form, 
 int pairs_batched_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_bytes);
 // entry sort of the cut-off sweep: bin, scan, scatter (hist must be zeroed)
 cudaError_t launch_cull_sort(const DevCull& cull, const Scratch& s, const float* lig_q, int B,
-                             int L, const CullSegs& seg, const CullScratch& cs, cudaStream_t st);
+                             int L, const CullSegs& seg, const CullScratch& cs, bool binned, cudaStream_t st);
 cudaError_t launch_pairs_cull(const DevCull& cull, const float4* tab, const CullSegs& seg,
                               const CullScratch& cs, int flags, const Physics& ph,
                               const CullPlan& plan, int* d_err, cudaStream_t st);
@@ -782,6 +800,45 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
   }
   return false;
 }
+// Index of cell (x, y, z) of the 32^3 binning grid along a 3-D Hilbert curve
+// (J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc. 707, 2004:
+// axes to transposed index, then the bits interleaved).  Consecutive slots in
+// Hilbert order stay closer together than in Morton order, so the groups'
+// boxes are smaller.
+template <int kBits = 5>
+__device__ __forceinline__ uint32_t hilbert_cell(uint32_t x, uint32_t y, uint32_t z) {
+  uint32_t X[3] = {x, y, z};
+  for (uint32_t Q = 1u << (kBits - 1); Q > 1; Q >>= 1) {
+    const uint32_t P = Q - 1;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      if (X[i] & Q) {
+        X[0] ^= P;
+      } else {
+        const uint32_t t = (X[0] ^ X[i]) & P;
+        X[0] ^= t;
+        X[i] ^= t;
+      }
+    }
+  }
+  X[1] ^= X[0];
+  X[2] ^= X[1];
+  uint32_t t = 0;
+  for (uint32_t Q = 1u << (kBits - 1); Q > 1; Q >>= 1)
+    if (X[2] & Q) t ^= Q - 1;
+  uint32_t k = 0;
+#pragma unroll
+  for (int b = kBits - 1; b >= 0; --b)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) k = (k << 1) | (((X[i] ^ t) >> b) & 1u);
+  return k;
+}
+
+__device__ __forceinline__ int grid_cell(float v, float lo, float inv) {
+  // NaN converts to 0; the clamp keeps infinities and far entries on the grid
+  return min(max(__float2int_rd((v - lo) * inv), 0), kCullGrid - 1);
+}
+
 // Double-float arithmetic: a value is an unevaluated pair h + l of floats
 // (|l| <= ulp(h) / 2), about 48 significant bits, on the FP32 pipe (GB300's
 // FP64 rate is 1/64 of its FP32 rate).  ts / qts are the error-free sums
