@@ -164,6 +164,7 @@ struct mmo_ctx {
   uint32_t first_wait_polls = kWaitPollsDefault;  // mmo_diag_set_wait_polls
   // the one-pose path (k_one_pose): per-CTA partials and the arrival count
   OneScratch one{};
+  unsigned* d_plain_arrive = nullptr;  // mmo_ene_inter's arrival counter
   bool one_ok = false;       // its shared memory fits (set with the ligand)
   size_t capOneE = 0, capOneG = 0;
 
@@ -1769,6 +1770,7 @@ int mmo_ctx_destroy(mmo_ctx* ctx) {
   cudaFree(ctx->one.G);
   cudaFree(ctx->one.arrive);
   cudaFree(ctx->one.intra);
+  cudaFree(ctx->d_plain_arrive);
   cudaFree(ctx->cs.gcount);
   cudaFree(ctx->cs.glist);
   cudaFree(ctx->cs.items);
@@ -2083,10 +2085,15 @@ int mmo_ene_inter(mmo_ctx* ctx, int n, const double* xs, const double* ys, const
   double* dE = dEp + (size_t)C * n;
   MMO_CK(cudaMemcpyAsync(ctx->d_in, ctx->h_in, in_bytes, cudaMemcpyHostToDevice, ctx->stream),
          "H2D");
+  if (!ctx->d_plain_arrive) {
+    MMO_CK(cudaMalloc((void**)&ctx->d_plain_arrive, sizeof(unsigned)), "arrival counter");
+    MMO_CK(cudaMemset(ctx->d_plain_arrive, 0, sizeof(unsigned)), "arrival counter");
+  }
+  // one launch: the pair partials, and their total from the last block
   MMO_CK(launch_pairs_plain(ctx->prot, ctx->tab, dX, dq, dt, n, C, dEp, nullptr, 0, ctx->ph,
-                            ctx->stream),
+                            ctx->stream, dE, ctx->d_plain_arrive),
          "plain pair kernel");
-  MMO_CK(launch_reduce_plain(dEp, C * n, dE, ctx->stream), "reduce kernel");
+  ctx->last_launches = 1;
   MMO_CK(cudaMemcpyAsync(ctx->h_out, dE, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
          "D2H");
   MMO_CK(cudaStreamSynchronize(ctx->stream), "sync");
@@ -2111,6 +2118,7 @@ int mmo_ene_intra(mmo_ctx* ctx, const double* xs, const double* ys, const double
   MMO_CK(cudaMemcpyAsync(ctx->d_in, ctx->h_in, sizeof(float4) * 2 * n, cudaMemcpyHostToDevice,
                          ctx->stream),
          "H2D");
+  ctx->last_launches = 1;
   MMO_CK(launch_intra_plain(ctx->lig, reinterpret_cast<const float4*>(ctx->d_in),
                             ctx->ph.intra_form, ctx->ph.dielectric,
                             reinterpret_cast<double*>(ctx->d_out), ctx->stream),

@@ -165,35 +165,59 @@ template <bool GRAD, int DIEL, int FORM>
 __global__ void __launch_bounds__(256)
     k_pairs_plain(DevProtein prot, PairTable tab, const float4* X, const float* lig_q,
                   const int* lig_type, int L, int C, int chunk_len, double* Epart,
-                  float4* Gpart) {
+                  float4* Gpart, double* Eout, unsigned* arrive) {
   __shared__ float2 stab[kNTypes * kNTypes];
+  __shared__ double wsum[8];
+  __shared__ int s_last;
   for (int k = threadIdx.x; k < kNTypes * kNTypes; k += blockDim.x) stab[k] = tab.xd[k];
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (item >= C * L) return;
-  const int j = item % L, c = item / L;
-  const int c0 = c * chunk_len, c1 = min(c0 + chunk_len, prot.P);
-  const float4 xh = X[2 * j], xl = X[2 * j + 1];
-  const float qj = lig_q[j];
-  const int lt = lig_type[j];
-  float ae = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
-  for (int i = c0 + lane; i < c1; i += 32) {
-    const float4 p = prot.atoms[2 * i], pl = prot.atoms[2 * i + 1];
-    const float2 xd = stab[prot.type[i] * kNTypes + lt];
-    uff_pair<GRAD, DIEL, FORM>(split_diff(xh.x, xl.x, p.x, pl.x), split_diff(xh.y, xl.y, p.y, pl.y),
-                               split_diff(xh.z, xl.z, p.z, pl.z), xd.x, xd.y, p.w * qj, ae, gx,
-                               gy, gz);
+  if (item < C * L) {
+    const int j = item % L, c = item / L;
+    const int c0 = c * chunk_len, c1 = min(c0 + chunk_len, prot.P);
+    const float4 xh = X[2 * j], xl = X[2 * j + 1];
+    const float qj = lig_q[j];
+    const int lt = lig_type[j];
+    float ae = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+    for (int i = c0 + lane; i < c1; i += 32) {
+      const float4 p = prot.atoms[2 * i], pl = prot.atoms[2 * i + 1];
+      const float2 xd = stab[prot.type[i] * kNTypes + lt];
+      uff_pair<GRAD, DIEL, FORM>(split_diff(xh.x, xl.x, p.x, pl.x),
+                                 split_diff(xh.y, xl.y, p.y, pl.y),
+                                 split_diff(xh.z, xl.z, p.z, pl.z), xd.x, xd.y, p.w * qj, ae, gx,
+                                 gy, gz);
+    }
+    const double e = warp_sum((double)ae);
+    if (GRAD) {
+      gx = warp_sum(gx);
+      gy = warp_sum(gy);
+      gz = warp_sum(gz);
+    }
+    if (lane == 0) {
+      Epart[c * L + j] = e;
+      if (GRAD) Gpart[c * L + j] = make_float4(gx, gy, gz, 0.f);
+    }
   }
-  const double e = warp_sum((double)ae);
-  if (GRAD) {
-    gx = warp_sum(gx);
-    gy = warp_sum(gy);
-    gz = warp_sum(gz);
-  }
-  if (lane == 0) {
-    Epart[c * L + j] = e;
-    if (GRAD) Gpart[c * L + j] = make_float4(gx, gy, gz, 0.f);
+  if (!Eout) return;
+  // Eout: the last block to arrive adds every partial in a fixed order, so
+  // that one launch gives the total (an atomic count, nothing waits)
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(arrive, 1u) == gridDim.x - 1u;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  double s = 0.0;
+  for (int k = threadIdx.x; k < C * L; k += blockDim.x) s += __ldcg(Epart + k);
+  s = warp_sum(s);
+  if (lane == 0) wsum[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += wsum[w];
+    *Eout = t;
+    *arrive = 0u;  // ready for the next launch
   }
 }
 
@@ -258,13 +282,13 @@ cudaError_t launch_pairs_batched(const DevProtein& prot, const float4* tab,
 cudaError_t launch_pairs_plain(const DevProtein& prot, const PairTable& tab, const float4* X,
                                const float* lig_q, const int* lig_type, int L, int C,
                                double* Epart, float4* Gpart, int grad, const Physics& ph,
-                               cudaStream_t st) {
+                               cudaStream_t st, double* Eout, unsigned* arrive) {
   if (L <= 0 || C <= 0) return cudaSuccess;
   const int chunk_len = (prot.P + C - 1) / C;
   const int blocks = (C * L + 7) / 8;
   const int d = ph.dielectric ? 1 : 0, f = ph.inter_form ? 1 : 0;
 #define MMO_PL(G, D, F) \
-  k_pairs_plain<G, D, F><<<blocks, 256, 0, st>>>(prot, tab, X, lig_q, lig_type, L, C, chunk_len, Epart, Gpart)
+  k_pairs_plain<G, D, F><<<blocks, 256, 0, st>>>(prot, tab, X, lig_q, lig_type, L, C, chunk_len, Epart, Gpart, Eout, arrive)
   if (grad) {
     if (d) { if (f) MMO_PL(true, 1, 1); else MMO_PL(true, 1, 0); }
     else { if (f) MMO_PL(true, 0, 1); else MMO_PL(true, 0, 0); }

@@ -484,10 +484,12 @@ cudaError_t launch_pairs_batched(const DevProtein& prot, const float4* tab,
                                  const DevLigand& lig, const Scratch& s, int B, int flags,
                                  const Physics& ph, const PairPlan& plan, int* d_err,
                                  cudaStream_t st);
+// Eout (with its arrival counter): the total of all partials, by the last block
 cudaError_t launch_pairs_plain(const DevProtein& prot, const PairTable& tab, const float4* X,
                                const float* lig_q, const int* lig_type, int L, int C,
                                double* Epart, float4* Gpart, int grad, const Physics& ph,
-                               cudaStream_t st);
+                               cudaStream_t st, double* Eout = nullptr,
+                               unsigned* arrive = nullptr);
 int one_pose_smem(int L, int nrb);  // static + dynamic shared memory of k_one_pose, bytes
 // *stage: 1 when the shared-memory attribute call failed, 2 the launch
 cudaError_t launch_one_pose(const DevLigand& lig, const DevProtein& prot, const float4* tab4,

@@ -34,6 +34,9 @@ def main(argv=None) -> int:
                          "this margin, mask sphere of 34 A) --repeat times, then score the poses "
                          "from them")
     ap.add_argument("--grid-kp", type=int, default=0, help="lattice points per lane (1, 2)")
+    ap.add_argument("--plain", type=int, default=0,
+                    help="score the first N poses one per call (the one-pose kernel), "
+                         "--repeat times")
     ap.add_argument("--dock", action="store_true",
                     help="exhaustive docking of the 24-atom ligand in the 6,000-atom cavity site "
                          "(grids over the site's box + 6 A, masks, ROI r = 4 A at 0.5 A, 2,000 "
@@ -60,6 +63,14 @@ def main(argv=None) -> int:
         print("grids %s x %d types  build ms %s  E[0] %.6e  status bits %d" %
               (dims, len(types), " ".join("%.3f" % m for m in ms), E[0],
                int(np.count_nonzero(st))))
+        sc.close()
+        return 0
+    if args.plain:
+        for _ in range(args.repeat):
+            for b in range(args.plain):
+                E, G, st = sc.score_poses(s.poses[b:b + 1], grad=not args.energy_only)
+        print("plain: %d poses x %d, %d launch(es) per pose, E %.6e  status bits %d" %
+              (args.plain, args.repeat, sc.last_launches(), E[0], int(np.count_nonzero(st))))
         sc.close()
         return 0
     if args.sweep == "cut-off":

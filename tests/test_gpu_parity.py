@@ -42,11 +42,13 @@ def test_plain_ene_inter_and_intra(oracle, scorer_factory, small, phys):
     xyz, _ = _posed(oracle, small.ligand, small.poses[0])
     lig = small.ligand.with_xyz(xyz)
     e = s.ene_inter(lig)
+    assert s.last_launches() == 1  # the pair partials and their total in one launch
     e64 = oracle.ene_inter(small.pocket, small.ligand, xyz, ph=ph)
     scale = T.ene_inter(small.pocket.xyz(), small.pocket.q, small.pocket.anum, xyz, lig.q,
                         lig.anum, shifted=phys[2] == 0, dielectric=phys[0], absolute=True)
     assert_energy(np.array([e]), np.array([e64]), np.array([scale]))
     ei = s.ene_intra(lig)
+    assert s.last_launches() == 1
     ei64 = oracle.ene_intra(small.ligand, xyz, ph=ph)
     si = T.ene_intra(xyz, lig.q, lig.anum, lig.interacting, dielectric=phys[0], absolute=True)
     assert_energy(np.array([ei]), np.array([ei64]), np.array([si]))
