@@ -96,6 +96,14 @@ int mmo_set_ligand(mmo_ctx* ctx, int n, const double* xs, const double* ys, cons
 int mmo_ene_inter(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
                   const double* q, const int* anum, double* out);
 
+/* The same sum with its two parts kept apart, as
+ * Mol.ene_inter_UFF_shifted_bst_components (mol.ml:920-957) keeps them for
+ * rescoring functions: *elec the electrostatic part (elec_weight_protein
+ * applied), *vdw the van der Waals part; *elec + *vdw is mmo_ene_inter's
+ * energy up to rounding.  One launch. */
+int mmo_ene_inter_parts(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
+                        const double* q, const int* anum, double* elec, double* vdw);
+
 /* Plain drop-in for Mol.ene_intra_UFFNB_brute (mol.ml:881-903) on the ligand
  * of mmo_set_ligand, at the given coordinates. */
 int mmo_ene_intra(mmo_ctx* ctx, const double* xs, const double* ys, const double* zs,

@@ -2046,16 +2046,21 @@ int mmo_set_ligand(mmo_ctx* ctx, int n, const double* xs, const double* ys, cons
   return grid_map(ctx);
 }
 
-int mmo_ene_inter(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
-                  const double* q, const int* anum, double* out) {
+namespace {
+
+// mmo_ene_inter (parts = false: out[0] the energy) and mmo_ene_inter_parts
+// (out[0] electrostatic, out[1] van der Waals): one launch each
+int ene_inter_impl(mmo_ctx* ctx, const char* who, int n, const double* xs, const double* ys,
+                   const double* zs, const double* q, const int* anum, bool parts, double* out) {
   if (!ctx) return MMO_EINVAL;
   if (n < 0 || n > kMaxLig || !out || (n > 0 && (!xs || !ys || !zs || !q || !anum)))
-    return fail(ctx, MMO_EINVAL, "mmo_ene_inter: bad arguments (n <= %d)", kMaxLig);
+    return fail(ctx, MMO_EINVAL, "%s: bad arguments (n <= %d)", who, kMaxLig);
+  const int nout = parts ? 2 : 1;
   if (n == 0 || ctx->prot.P == 0) {
-    *out = 0.0;
+    for (int k = 0; k < nout; ++k) out[k] = 0.0;
     return MMO_OK;
   }
-  // staging: X[n] float4 | q[n] float | type[n] int ; output: C*n doubles | E
+  // staging: X[n] float4 | q[n] float | type[n] int ; output: nout C n partials | the totals
   const int C = std::max(1, (ctx->prot.P + 255) / 256);
   size_t off = 0;
   const size_t oX = take(off, sizeof(float4) * 2 * n);
@@ -2065,7 +2070,8 @@ int mmo_ene_inter(mmo_ctx* ctx, int n, const double* xs, const double* ys, const
   MMO_CK(cudaSetDevice(ctx->device), "set device");
   int r = grow_host(ctx, &ctx->h_in, &ctx->d_in, &ctx->cap_in, in_bytes);
   if (r) return r;
-  r = grow_host(ctx, &ctx->h_out, &ctx->d_out, &ctx->cap_out, sizeof(double) * ((size_t)C * n + 1));
+  r = grow_host(ctx, &ctx->h_out, &ctx->d_out, &ctx->cap_out,
+                sizeof(double) * ((size_t)nout * C * n + nout));
   if (r) return r;
   float4* hX = reinterpret_cast<float4*>(ctx->h_in + oX);
   float* hq = reinterpret_cast<float*>(ctx->h_in + oq);
@@ -2082,23 +2088,48 @@ int mmo_ene_inter(mmo_ctx* ctx, int n, const double* xs, const double* ys, const
   const float* dq = reinterpret_cast<const float*>(ctx->d_in + oq);
   const int* dt = reinterpret_cast<const int*>(ctx->d_in + ot);
   double* dEp = reinterpret_cast<double*>(ctx->d_out);
-  double* dE = dEp + (size_t)C * n;
+  double* dE = dEp + (size_t)nout * C * n;
   MMO_CK(cudaMemcpyAsync(ctx->d_in, ctx->h_in, in_bytes, cudaMemcpyHostToDevice, ctx->stream),
          "H2D");
   if (!ctx->d_plain_arrive) {
     MMO_CK(cudaMalloc((void**)&ctx->d_plain_arrive, sizeof(unsigned)), "arrival counter");
     MMO_CK(cudaMemset(ctx->d_plain_arrive, 0, sizeof(unsigned)), "arrival counter");
   }
-  // one launch: the pair partials, and their total from the last block
-  MMO_CK(launch_pairs_plain(ctx->prot, ctx->tab, dX, dq, dt, n, C, dEp, nullptr, 0, ctx->ph,
-                            ctx->stream, dE, ctx->d_plain_arrive),
-         "plain pair kernel");
+  // one launch: the pair partials, and their totals from the last block
+  if (parts)
+    MMO_CK(launch_pairs_parts(ctx->prot, ctx->tab, dX, dq, dt, n, C, dEp, ctx->ph, ctx->stream,
+                              dE, ctx->d_plain_arrive),
+           "plain pair-parts kernel");
+  else
+    MMO_CK(launch_pairs_plain(ctx->prot, ctx->tab, dX, dq, dt, n, C, dEp, nullptr, 0, ctx->ph,
+                              ctx->stream, dE, ctx->d_plain_arrive),
+           "plain pair kernel");
   ctx->last_launches = 1;
-  MMO_CK(cudaMemcpyAsync(ctx->h_out, dE, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+  MMO_CK(cudaMemcpyAsync(ctx->h_out, dE, sizeof(double) * nout, cudaMemcpyDeviceToHost,
+                         ctx->stream),
          "D2H");
   MMO_CK(cudaStreamSynchronize(ctx->stream), "sync");
-  memcpy(out, ctx->h_out, sizeof(double));
+  memcpy(out, ctx->h_out, sizeof(double) * nout);
   return MMO_OK;
+}
+
+}  // namespace
+
+int mmo_ene_inter(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
+                  const double* q, const int* anum, double* out) {
+  return ene_inter_impl(ctx, "mmo_ene_inter", n, xs, ys, zs, q, anum, false, out);
+}
+
+int mmo_ene_inter_parts(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
+                        const double* q, const int* anum, double* elec, double* vdw) {
+  if (ctx && (!elec || !vdw)) return fail(ctx, MMO_EINVAL, "mmo_ene_inter_parts: null output");
+  double two[2];
+  const int r = ene_inter_impl(ctx, "mmo_ene_inter_parts", n, xs, ys, zs, q, anum, true, two);
+  if (r == MMO_OK) {
+    *elec = two[0];
+    *vdw = two[1];
+  }
+  return r;
 }
 
 int mmo_ene_intra(mmo_ctx* ctx, const double* xs, const double* ys, const double* zs,

@@ -221,6 +221,64 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// The two parts of the inter energy for one ligand (mmo_ene_inter_parts): as
+// k_pairs_plain, with the electrostatic partials in Epart[0, C L) and the van
+// der Waals ones in Epart[C L, 2 C L); the last block to arrive adds each set
+// in a fixed order into Eout[0], Eout[1].
+template <int DIEL, int FORM>
+__global__ void __launch_bounds__(256)
+    k_pairs_parts(DevProtein prot, PairTable tab, const float4* X, const float* lig_q,
+                  const int* lig_type, int L, int C, int chunk_len, double* Epart, double* Eout,
+                  unsigned* arrive) {
+  __shared__ float2 stab[kNTypes * kNTypes];
+  __shared__ double wsum[2][8];
+  __shared__ int s_last;
+  for (int k = threadIdx.x; k < kNTypes * kNTypes; k += blockDim.x) stab[k] = tab.xd[k];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (item < C * L) {
+    const int j = item % L, c = item / L;
+    const int c0 = c * chunk_len, c1 = min(c0 + chunk_len, prot.P);
+    const float4 xh = X[2 * j], xl = X[2 * j + 1];
+    const float qj = lig_q[j];
+    const int lt = lig_type[j];
+    float ael = 0.f, alj = 0.f;
+    for (int i = c0 + lane; i < c1; i += 32) {
+      const float4 p = prot.atoms[2 * i], pl = prot.atoms[2 * i + 1];
+      const float2 xd = stab[prot.type[i] * kNTypes + lt];
+      uff_pair_parts<DIEL, FORM>(split_diff(xh.x, xl.x, p.x, pl.x),
+                                 split_diff(xh.y, xl.y, p.y, pl.y),
+                                 split_diff(xh.z, xl.z, p.z, pl.z), xd.x, xd.y, p.w * qj, ael,
+                                 alj);
+    }
+    const double el = warp_sum((double)ael), lj = warp_sum((double)alj);
+    if (lane == 0) {
+      Epart[c * L + j] = el;
+      Epart[C * L + c * L + j] = lj;
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(arrive, 1u) == gridDim.x - 1u;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int part = 0; part < 2; ++part) {
+    double s = 0.0;
+    for (int k = threadIdx.x; k < C * L; k += blockDim.x) s += __ldcg(Epart + part * C * L + k);
+    s = warp_sum(s);
+    if (lane == 0) wsum[part][threadIdx.x >> 5] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += wsum[threadIdx.x][w];
+    Eout[threadIdx.x] = t;
+  }
+  if (threadIdx.x == 0) *arrive = 0u;  // ready for the next launch
+}
+
 using PairsFn = void (*)(DevProtein, const float4*, DevLigand, Scratch, int, int, int, int, int,
                          int, int*);
 
@@ -277,6 +335,22 @@ cudaError_t launch_pairs_batched(const DevProtein& prot, const float4* tab,
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+cudaError_t launch_pairs_parts(const DevProtein& prot, const PairTable& tab, const float4* X,
+                               const float* lig_q, const int* lig_type, int L, int C,
+                               double* Epart, const Physics& ph, cudaStream_t st, double* Eout,
+                               unsigned* arrive) {
+  if (L <= 0 || C <= 0) return cudaSuccess;
+  const int chunk_len = (prot.P + C - 1) / C;
+  const int blocks = (C * L + 7) / 8;
+  const int d = ph.dielectric ? 1 : 0, f = ph.inter_form ? 1 : 0;
+#define MMO_PP(D, F) \
+  k_pairs_parts<D, F><<<blocks, 256, 0, st>>>(prot, tab, X, lig_q, lig_type, L, C, chunk_len, Epart, Eout, arrive)
+  if (d) { if (f) MMO_PP(1, 1); else MMO_PP(1, 0); }
+  else { if (f) MMO_PP(0, 1); else MMO_PP(0, 0); }
+#undef MMO_PP
+  return cudaGetLastError();
 }
 
 cudaError_t launch_pairs_plain(const DevProtein& prot, const PairTable& tab, const float4* X,

@@ -498,6 +498,12 @@ cudaError_t launch_one_pose(const DevLigand& lig, const DevProtein& prot, const 
 cudaError_t launch_finish(const DevLigand& lig, const PoseIO& io, const Scratch& s, int flags,
                           const Physics& ph, cudaStream_t st);
 cudaError_t launch_reduce_plain(const double* Epart, int n, double* out, cudaStream_t st);
+// the inter energy's two parts for one ligand: Eout[0] electrostatic, Eout[1]
+// van der Waals (Epart: 2 C L partials), one launch
+cudaError_t launch_pairs_parts(const DevProtein& prot, const PairTable& tab, const float4* X,
+                               const float* lig_q, const int* lig_type, int L, int C,
+                               double* Epart, const Physics& ph, cudaStream_t st, double* Eout,
+                               unsigned* arrive);
 cudaError_t launch_intra_plain(const DevLigand& lig, const float4* X, int form, int dielectric,
                                double* out, cudaStream_t st);
 int pairs_batched_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_bytes);
@@ -632,6 +638,27 @@ __device__ __forceinline__ void uff_pair(float dx, float dy, float dz, float x2,
     gy = fmaf(g, dy, gy);
     gz = fmaf(g, dz, gz);
   }
+}
+
+// The electrostatic and van der Waals parts of uff_pair's energy, each with
+// the switch weight, into el_acc and lj_acc (mol.ml:945-953)
+template <int DIEL, int FORM>
+__device__ __forceinline__ void uff_pair_parts(float dx, float dy, float dz, float x2, float D,
+                                               float qq, float& el_acc, float& lj_acc) {
+  const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  const float r2c = fmaxf(r2, kMinR2);
+  const float ir = rsqrtf(r2c);
+  const float ir2 = rcp_approx(r2c);
+  const float p2 = x2 * ir2;
+  const float p6 = p2 * p2 * p2;
+  const float el = DIEL == 0 ? qq * ir : qq * ir2;
+  float w = 1.0f;
+  if (FORM == 0) {
+    const float s = fmaxf(fmaf(r2c, -1.0f / 144.0f, 1.0f), 0.0f);
+    w = s * s;
+  }
+  el_acc = fmaf(w, el, el_acc);
+  lj_acc = fmaf(w, (D * p6) * (p6 - 2.0f), lj_acc);
 }
 
 // Energy e and the scalar g of one pair's gradient, dE_pair/dd = g d (the

@@ -273,6 +273,16 @@ class UFFScorer:
                                             _ip(an), C.byref(out)))
         return out.value
 
+    def ene_inter_parts(self, lig: Mol) -> tuple[float, float]:
+        """Mol.ene_inter_UFF_shifted_bst_components prot_bst prot lig
+        (src/mol.ml:920-957): (electrostatic, van der Waals)."""
+        x, y, z, q = (_f64(v) for v in (lig.x, lig.y, lig.z, lig.q))
+        an = np.ascontiguousarray(lig.anum, np.int32)
+        el, lj = C.c_double(), C.c_double()
+        self._check(self._lib.mmo_ene_inter_parts(self._h, lig.n, _dp(x), _dp(y), _dp(z), _dp(q),
+                                                  _ip(an), C.byref(el), C.byref(lj)))
+        return el.value, lj.value
+
     def ene_intra(self, lig: Mol) -> float:
         """Mol.ene_intra_UFFNB_brute lig (src/mol.ml:881-903) for the ligand of
         set_ligand at lig's coordinates."""

@@ -87,6 +87,8 @@ SIGNATURES = {
                             _P(_i), _P(_i), _P(_i)]),
     "mmo_ene_inter": (_i, [_vp, _i, _P(_d), _P(_d), _P(_d), _P(_d), _P(_i), _P(_d)]),
     "mmo_ene_intra": (_i, [_vp, _P(_d), _P(_d), _P(_d), _P(_d)]),
+    "mmo_ene_inter_parts": (_i, [_vp, _i, _P(_d), _P(_d), _P(_d), _P(_d), _P(_i), _P(_d),
+                                 _P(_d)]),
     "mmo_score_poses": (_i, [_vp, _i, _P(C.c_float), _i, _P(_d), _P(C.c_float), _P(_i)]),
     "mmo_score_poses_device": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp, _vp]),
     "mmo_posed_coords": (_i, [_vp, _i, _P(C.c_float), _i, _P(_d), _P(_i)]),

@@ -54,6 +54,30 @@ def test_plain_ene_inter_and_intra(oracle, scorer_factory, small, phys):
     assert_energy(np.array([ei]), np.array([ei64]), np.array([si]))
 
 
+@pytest.mark.parametrize("phys", [(0, 0, 0, 0), (1, 0, 1, 0), (0, 1, 0, 1)])
+def test_plain_ene_inter_parts(oracle, scorer_factory, small, phys):
+    """The electrostatic and van der Waals parts (ene_inter_UFF_shifted_bst_
+    components) against the oracle's, each within 1e-5 of its own sum of
+    |terms|; their sum is the energy of mmo_ene_inter; one launch."""
+    from mmo_gb300.ff import Physics
+    from oracle import np_twin as T
+
+    ph = oracle.physics(*phys)
+    s = scorer_factory(small.pocket, small.ligand, Physics(*phys))
+    for k in range(3):
+        xyz, _ = _posed(oracle, small.ligand, small.poses[0] if k == 0 else
+                        np.concatenate([np.full(3, 0.7 * k), small.poses[0][3:]]))
+        lig = small.ligand.with_xyz(xyz)
+        el, lj = s.ene_inter_parts(lig)
+        assert s.last_launches() == 1
+        el64, lj64 = oracle.ene_inter_parts(small.pocket, small.ligand, xyz, ph=ph)
+        scale = T.ene_inter(small.pocket.xyz(), small.pocket.q, small.pocket.anum, xyz, lig.q,
+                            lig.anum, shifted=phys[2] == 0, dielectric=phys[0], absolute=True)
+        assert abs(el - el64) <= E_TOL * scale and abs(lj - lj64) <= E_TOL * scale
+        e = s.ene_inter(lig)
+        assert abs((el + lj) - e) <= 1e-6 * scale
+
+
 def test_plain_closures_match_reference_call_shape(oracle, gpu_lib, small):
     from mmo_gb300.ff import ene_inter_builder, ene_intra_builder
 
