@@ -20,6 +20,9 @@ external set_ligand_raw :
 external ene_inter_raw :
   ctx -> float array -> float array -> float array -> float array -> int array -> float
   = "mmo_ocaml_ene_inter_byte" "mmo_ocaml_ene_inter"
+external ene_inter_parts_raw :
+  ctx -> float array -> float array -> float array -> float array -> int array -> float * float
+  = "mmo_ocaml_ene_inter_parts_byte" "mmo_ocaml_ene_inter_parts"
 external ene_intra_raw : ctx -> float array -> float array -> float array -> float
   = "mmo_ocaml_ene_intra"
 external score_poses_raw :
@@ -79,6 +82,17 @@ let ene_inter_builder (prot: Mol.t) =
     let c = get_ctx () in
     if not !ready then (set_protein c prot; ready := true);
     ene_inter_raw c lig.Mol.xs lig.Mol.ys lig.Mol.zs lig.Mol.q_a lig.Mol.elt_a
+
+(* drop-in for [Mol.ene_inter_UFF_shifted_bst_components prot_bst prot]:
+   Mol.t -> Mol.ele_vdW (mol.ml:920-957) *)
+let ene_inter_components_builder (prot: Mol.t) =
+  let ready = ref false in
+  fun (lig: Mol.t) ->
+    let c = get_ctx () in
+    if not !ready then (set_protein c prot; ready := true);
+    let el, vdw =
+      ene_inter_parts_raw c lig.Mol.xs lig.Mol.ys lig.Mol.zs lig.Mol.q_a lig.Mol.elt_a in
+    { Mol.sum_elec = el; sum_vdW = vdw }
 
 (* drop-in for [ene_intra_builder UFF_NB] *)
 let ene_intra_builder tweak_rbonds (centered_lig: Mol.t) =

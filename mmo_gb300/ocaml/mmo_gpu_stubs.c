@@ -132,6 +132,30 @@ CAMLprim value mmo_ocaml_ene_inter_byte(value *argv, int argn) {
   return mmo_ocaml_ene_inter(argv[0], argv[1], argv[2], argv[3], argv[4], argv[5]);
 }
 
+/* Mol.ene_inter_UFF_shifted_bst_components (mol.ml:920-957): (elec, vdW) */
+CAMLprim value mmo_ocaml_ene_inter_parts(value ctx, value xs, value ys, value zs, value q,
+                                         value anum) {
+  CAMLparam5(ctx, xs, ys, zs, q);
+  CAMLxparam1(anum);
+  CAMLlocal1(res);
+  mmo_ctx *c = Ctx_val(ctx);
+  double el = 0.0, vdw = 0.0;
+  int *an = c_ints(anum);
+  int rc = mmo_ene_inter_parts(c, n_floats(xs), Doubles(xs), Doubles(ys), Doubles(zs), Doubles(q),
+                               an, &el, &vdw);
+  free(an);
+  check(c, rc);
+  res = caml_alloc_tuple(2);
+  Store_field(res, 0, caml_copy_double(el));
+  Store_field(res, 1, caml_copy_double(vdw));
+  CAMLreturn(res);
+}
+
+CAMLprim value mmo_ocaml_ene_inter_parts_byte(value *argv, int argn) {
+  (void)argn;
+  return mmo_ocaml_ene_inter_parts(argv[0], argv[1], argv[2], argv[3], argv[4], argv[5]);
+}
+
 CAMLprim value mmo_ocaml_ene_intra(value ctx, value xs, value ys, value zs) {
   CAMLparam4(ctx, xs, ys, zs);
   mmo_ctx *c = Ctx_val(ctx);
