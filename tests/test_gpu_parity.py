@@ -132,6 +132,70 @@ def test_one_pose_is_one_launch(oracle, scorer_factory, batch, grad, recenter, p
     assert_ref(np.array(E), np.array(G) if grad else None, ref, np.array(st))
 
 
+def _nested(lig) -> bool:
+    """The nested-group rule of mmo_set_ligand: every two groups nested or
+    disjoint; an inner group's axis inside its outer group or on the outer
+    axis; no axis atom of one of two disjoint groups inside the other."""
+    G = [set(int(a) for a in g) for g in lig.rgroups]
+    B = [tuple(int(v) for v in b) for b in lig.rbonds]
+    for t in range(lig.nrb):
+        for u in range(lig.nrb):
+            if t == u:
+                continue
+            (tl, tr), (ul, ur) = B[t], B[u]
+            if not (G[t] & G[u]):
+                if ul in G[t] or ur in G[t]:
+                    return False
+            elif G[u] <= G[t]:
+                if not all(a in G[t] or a in (tl, tr) for a in (ul, ur)):
+                    return False
+            elif not G[t] <= G[u]:
+                return False
+    return True
+
+
+def _crossing_ligand(lig):
+    """The ligand with one rotatable bond's group moved to the bond's other
+    side (axis reversed): a valid MMO group assignment whose groups are no
+    longer nested, so the pose map takes the torsions in bond order and the
+    gradient the reverse pass."""
+    import dataclasses
+
+    n = lig.n
+    for t in sorted(range(lig.nrb), key=lambda k: len(lig.rgroups[k])):
+        left, right = (int(v) for v in lig.rbonds[t])
+        side = set(int(a) for a in lig.rgroups[t]) | {right}
+        rb = lig.rbonds.copy()
+        rb[t] = (right, left)
+        groups = list(lig.rgroups)
+        groups[t] = np.asarray(sorted(set(range(n)) - side - {left}), np.int32)
+        flipped = dataclasses.replace(lig, rbonds=rb, rgroups=groups)
+        if not _nested(flipped):
+            return flipped
+    raise AssertionError("no flip makes the groups cross")
+
+
+@pytest.mark.parametrize("recenter", [False, True])
+def test_groups_not_nested(oracle, scorer_factory, batch, recenter):
+    """A ligand whose rotation groups cross (one group moved to its bond's other
+    side): the batched path (bond-order rebuild with records, reverse pass) and
+    the one-pose kernel (finishing through the work buffers) against the oracle."""
+    assert _nested(batch.ligand)
+    lig = _crossing_ligand(batch.ligand)
+    d = batch.poses[:64]
+    sysm = synth.System("crossing", batch.pocket, lig, d)
+    s = scorer_factory(batch.pocket, lig)
+    ref = ref_batch(oracle, sysm, d, grad=True, recenter=recenter)
+    E, G, st = s.score_poses(d, grad=True, recenter=recenter)
+    assert_ref(E, G, ref, st)
+    for b in range(0, 64, 9):
+        E1, G1, st1 = s.score_poses(d[b:b + 1], grad=True, recenter=recenter)
+        assert s.last_launches() == 1
+        assert_energy(E1, ref.E[b:b + 1], ref.S[b:b + 1])
+        assert_grad(G1, ref.G[b:b + 1], ref.GA[b:b + 1])
+        assert st1[0] == ref.st[b]
+
+
 # -- batched ------------------------------------------------------------------------
 
 def test_batched_energy(oracle, scorer_factory, batch):
