@@ -1059,6 +1059,8 @@ def main():
     plan = sc.plan()
     launches = sc.last_launches()
     pairs_ev, pairs_all = sc.pair_count()
+    # the pairs within the 12 A cutoff of the same poses: the second roofline denominator
+    pairs_12 = sc.pairs_within(12.0)
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     tot_ms = float(sum(step_ms))
     if dist:
@@ -1169,7 +1171,9 @@ def main():
                      "peak_source": "measured FP32 FMA probe on this GPU (mmo_fp32_fma_peak)",
                      "flops_per_pair": FLOPS_PAIR_GRAD, "pairs_evaluated": pairs_ev,
                      "pairs_all": pairs_all, "flops_per_launch": flops,
-                     "ms_per_launch": pair_avg},
+                     "ms_per_launch": pair_avg,
+                     "pairs_within_12A": pairs_12,
+                     "frac_within_12A": FLOPS_PAIR_GRAD * pairs_12 / (pair_avg * 1e-3) * 1e-12 / peak},
         "stages_ms": dict(zip(("rebuild", "sweep", "finish", "sort"),
                               (float(v) for v in np.mean(np.array(stage_ms), axis=0)))),
         "clocks": clk,

@@ -46,6 +46,13 @@ int mmo_fp32_fma_peak(mmo_ctx* ctx, double* tflops, double* ms);
 int mmo_grid_build_stats(const mmo_ctx* ctx, double* points, double* pairs_evaluated,
                          double* pairs_within_cutoff);
 
+/* Pairs (posed ligand atom, protein atom) closer than r in the last scoring
+ * call that rebuilt its poses in the library's work buffers (a batched call,
+ * B > 1), counted by a brute kernel over the posed coordinates (hi + lo): the
+ * roofline's second denominator, the pairs within the 12 A cutoff.  No
+ * counterpart in the reference.  Synchronous. */
+int mmo_diag_pairs_within(mmo_ctx* ctx, double r, double* count);
+
 /* Accuracy check of the device's double-float sine and cosine (no
  * counterpart in the reference; the one-pose kernel takes the angles' sines
  * and cosines from it instead of the FP64 library): for n host floats x,

@@ -165,6 +165,7 @@ struct mmo_ctx {
   // the one-pose path (k_one_pose): per-CTA partials and the arrival count
   OneScratch one{};
   unsigned* d_plain_arrive = nullptr;  // mmo_ene_inter's arrival counter
+  int last_pose_entries = 0;           // B L posed entries in scr.X from the last call
   bool one_ok = false;       // its shared memory fits (set with the ligand)
   size_t capOneE = 0, capOneG = 0;
 
@@ -1147,6 +1148,7 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
   ctx->last_cull = cull;
   ctx->last_grad = grad ? 1 : 0;
   ctx->last_pairs = inter && !use_grid ? (double)B * L * ctx->prot.P : 0.0;
+  ctx->last_pose_entries = 0;  // set below once the rebuild has written X
   // one pose with pair sums: the fused one-launch path (k_one_pose)
   const bool one = B == 1 && inter && !use_grid && ctx->one_ok;
   // rebuild (which bins the entries for the cut-off sweep) + finish, and the
@@ -1230,6 +1232,7 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
                            sizeof(unsigned) * ctx->segs[grad ? 1 : 0].nseg * kCullBins, st),
            "entry bin reset");
   MMO_CK(launch_rebuild(ctx->lig, io, sr, fl, st), "rebuild kernel");
+  ctx->last_pose_entries = B * L;
   MMO_CK(mark(1), "event");
   if (cull) {
     const CullSegs& sg = ctx->segs[grad ? 1 : 0];
@@ -2732,6 +2735,28 @@ int mmo_diag_set_wait_polls(mmo_ctx* ctx, long long polls) {
     return fail(ctx, MMO_EINVAL, "mmo_diag_set_wait_polls: %lld polls above 2^32 - 1", polls);
   ctx->first_wait_polls = polls < 0 ? kWaitPollsDefault : (uint32_t)polls;
   ++ctx->epoch;  // graphs captured with the old limit are rebuilt
+  return MMO_OK;
+}
+
+int mmo_diag_pairs_within(mmo_ctx* ctx, double r, double* count) {
+  if (!ctx || !count) return MMO_EINVAL;
+  if (!(r > 0.0)) return fail(ctx, MMO_EINVAL, "mmo_diag_pairs_within: r = %g", r);
+  if (ctx->last_pose_entries <= 0 || ctx->prot.P <= 0)
+    return fail(ctx, MMO_ESTATE, "mmo_diag_pairs_within: no batched scoring call before it");
+  MMO_CK(cudaSetDevice(ctx->device), "set device");
+  unsigned long long* d = nullptr;
+  MMO_CK(cudaMalloc(&d, sizeof *d), "counter");
+  unsigned long long n = 0;
+  cudaError_t e = cudaMemsetAsync(d, 0, sizeof *d, ctx->stream);
+  if (e == cudaSuccess)
+    e = launch_count_within(ctx->scr.X, ctx->last_pose_entries, ctx->prot.atoms, ctx->prot.P,
+                            (float)(r * r), d, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&n, d, sizeof n, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "mmo_diag_pairs_within");
+  *count = (double)n;
   return MMO_OK;
 }
 

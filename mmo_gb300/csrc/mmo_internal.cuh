@@ -537,6 +537,8 @@ cudaError_t launch_prot_desolv(const DevCull& cull, const DesolvBuild& db, doubl
 cudaError_t launch_desolv_pose(const DesolvPose& d, cudaStream_t st);
 cudaError_t launch_fma_peak(int sms, int iters, float* out, cudaStream_t st, double* flops);
 cudaError_t launch_df_sincos(const float* x, int n, float4* out, cudaStream_t st);
+cudaError_t launch_count_within(const float4* X, int n, const float4* atoms, int P, float r2cut,
+                                unsigned long long* out, cudaStream_t st);
 
 // ---- device helpers ------------------------------------------------------
 #ifdef __CUDACC__

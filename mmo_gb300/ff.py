@@ -553,6 +553,13 @@ class UFFScorer:
         self._check(self._lib.mmo_pair_count(self._h, C.byref(ev), C.byref(al)))
         return ev.value, al.value
 
+    def pairs_within(self, r: float = 12.0) -> float:
+        """(posed ligand atom, protein atom) pairs closer than r in the last
+        batched scoring call (mmo_diag_pairs_within)."""
+        out = C.c_double()
+        self._check(self._lib.mmo_diag_pairs_within(self._h, float(r), C.byref(out)))
+        return out.value
+
     def last_launches(self) -> int:
         """Kernels the last scoring call launched."""
         n = C.c_int()

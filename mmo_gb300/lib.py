@@ -116,6 +116,7 @@ SIGNATURES = {
     "mmo_fp32_fma_peak": (_i, [_vp, _P(_d), _P(_d)]),
     "mmo_diag_set_wait_polls": (_i, [_vp, C.c_longlong]),
     "mmo_diag_sincos": (_i, [_vp, _i, _P(C.c_float), _P(C.c_float)]),
+    "mmo_diag_pairs_within": (_i, [_vp, C.c_double, _P(C.c_double)]),
     "mmo_build_grids": (_i, [_vp, _P(GridSpec), _P(_d)]),
     "mmo_load_grids": (_i, [_vp, _P(GridSpec), _P(C.c_float)]),
     "mmo_set_grid_build": (_i, [_vp, _i]),

@@ -220,6 +220,25 @@ def test_batched_terms_separately(oracle, scorer_factory, batch, inter, intra):
     assert_ref(E, G, ref_batch(oracle, batch, d, grad=True, inter=inter, intra=intra))
 
 
+def test_pairs_within_cutoff_count(oracle, scorer_factory, batch):
+    """mmo_diag_pairs_within (the roofline's pairs within 12 A) against a count
+    from the oracle's FP64 posed coordinates; the sweep's counted pairs are at
+    least as many (every pair within 12 A passes the box test)."""
+    s = scorer_factory(batch.pocket, batch.ligand)
+    d = batch.poses[:16]
+    s.score_poses(d, grad=True)
+    n12 = s.pairs_within(12.0)
+    p = batch.pocket.xyz()
+    want = 0
+    for conf in d:
+        xyz, _ = _posed(oracle, batch.ligand, conf)
+        d2 = ((xyz[:, None, :] - p[None, :, :]) ** 2).sum(-1)
+        want += int(np.count_nonzero(d2 < 144.0))
+    assert abs(n12 - want) <= 1e-6 * want + 2  # a pair at 12 A to within rounding
+    ev, al = s.pair_count()
+    assert n12 <= ev <= al
+
+
 @pytest.mark.parametrize("phys", [(1, 0, 0, 0), (0, 1, 1, 1), (1, 1, 1, 0)])
 def test_batched_physics_variants(oracle, scorer_factory, batch, phys):
     from mmo_gb300.ff import Physics
