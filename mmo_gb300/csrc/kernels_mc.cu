@@ -92,13 +92,27 @@ __global__ void k_mc_start(MCDev s, MCParams p) {
   for (int k = 0; k < p.nd; ++k) s.best[(size_t)b * p.nd + k] = s.cur[(size_t)b * p.nd + k];
 }
 
+// A quad of lanes per chain: the rigid move's random draws (Box-Muller) and the
+// sines and cosines of the current angles run on separate lanes, and each lane
+// then forms the same products; every FP64 operation is the one-thread
+// sequence's, on the same inputs, so the proposal keeps its bits.
+constexpr int kQuad = 4;
+
+// the quad's own lanes (quads leave the kernel independently)
+__device__ __forceinline__ unsigned quad_mask() { return 0xfu << (threadIdx.x & 28); }
+__device__ __forceinline__ double quad_get(double v, int src) {
+  return __shfl_sync(quad_mask(), v, src, kQuad);
+}
+
 __global__ void k_mc_propose(MCDev s, MCParams p) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = gt / kQuad, q = gt % kQuad;
+  // the whole quad leaves together (B kQuad threads run, a multiple of the quad)
   if (b >= p.B) return;
   const int nd = p.nd, nrb = p.nrb;
   const float* cur = s.cur + (size_t)b * nd;
   float* tr = s.trial + (size_t)b * nd;
-  for (int k = 0; k < nd; ++k) tr[k] = cur[k];
+  for (int k = q; k < nd; k += kQuad) tr[k] = cur[k];
   const int* c = chain_counts(s, b);
   const int step = c[0];
   const double* st = s.steps + (size_t)b * (2 + nrb);
@@ -106,19 +120,35 @@ __global__ void k_mc_propose(MCDev s, MCParams p) {
   if (s.stopped[b] || (!rigid && nrb == 0)) {
     // an ended chain stays; a ligand without rotatable bonds makes no
     // conformer move (its odd frames re-score the same pose, lds.ml:797-798)
-    s.moved[b] = -2;
+    if (q == 0) s.moved[b] = -2;
     return;
   }
-  const uint4 r0 = philox(make_uint4((uint32_t)b, (uint32_t)step, 0u, 0u), p.key0, p.key1);
-  const uint4 r1 = philox(make_uint4((uint32_t)b, (uint32_t)step, 1u, 0u), p.key0, p.key1);
   if (rigid) {
+    // lane q: Philox draw q (its two uniforms, or the normal pair from them)
+    // and, for q < 3, the sine and cosine of the current angle 3 + q
+    const uint4 rq = philox(make_uint4((uint32_t)b, (uint32_t)step, (uint32_t)q, 0u), p.key0,
+                            p.key1);
+    double nq0, nq1;
+    if (p.law == kMcGaussian) {
+      normal2(u01(rq.x, rq.y), u01(rq.z, rq.w), nq0, nq1);
+    } else {
+      nq0 = u01(rq.x, rq.y);
+      nq1 = u01(rq.z, rq.w);
+    }
+    double sq = 0.0, cq = 1.0;
+    if (q < 3) sincos((double)cur[3 + q], &sq, &cq);
+    __syncwarp(quad_mask());
+    double n[8];
+#pragma unroll
+    for (int k = 0; k < kQuad; ++k) {
+      n[2 * k] = quad_get(nq0, k);
+      n[2 * k + 1] = quad_get(nq1, k);
+    }
+    const double sa = quad_get(sq, 0), ca = quad_get(cq, 0);
+    const double sb = quad_get(sq, 1), cb = quad_get(cq, 1);
+    const double sg = quad_get(sq, 2), cg = quad_get(cq, 2);
     double ax = 0.0, ay = 0.0, az = 0.0, th, dt[3];
     if (p.law == kMcGaussian) {
-      double n[8];
-      normal2(u01(r0.x, r0.y), u01(r0.z, r0.w), n[0], n[1]);
-      normal2(u01(r1.x, r1.y), u01(r1.z, r1.w), n[2], n[3]);
-      const uint4 r2 = philox(make_uint4((uint32_t)b, (uint32_t)step, 2u, 0u), p.key0, p.key1);
-      normal2(u01(r2.x, r2.y), u01(r2.z, r2.w), n[4], n[5]);
       const double il = 1.0 / sqrt(fmax(n[0] * n[0] + n[1] * n[1] + n[2] * n[2], 1e-300));
       ax = n[0] * il;  // uniform direction
       ay = n[1] * il;
@@ -126,33 +156,26 @@ __global__ void k_mc_propose(MCDev s, MCParams p) {
       th = st[0] * n[3];
       dt[0] = st[1] * n[4];
       dt[1] = st[1] * n[5];
-      const uint4 r3 = philox(make_uint4((uint32_t)b, (uint32_t)step, 3u, 0u), p.key0, p.key1);
-      double n6, n7;
-      normal2(u01(r3.x, r3.y), u01(r3.z, r3.w), n6, n7);
-      dt[2] = st[1] * n6;
+      dt[2] = st[1] * n[6];
     } else {
       // Move.rand_rot: theta in [-dr, dr] about one of Ox, Oy, Oz; Move.rand_trans:
-      // a direction in [-1, 1]^3 times dt
-      th = (2.0 * u01(r0.x, r0.y) - 1.0) * st[0];
-      const int axis = min(2, (int)(u01(r0.z, r0.w) * 3.0));
+      // a direction in [-1, 1]^3 times dt (n[k]: the uniforms of draws 0, 1, 2)
+      th = (2.0 * n[0] - 1.0) * st[0];
+      const int axis = min(2, (int)(n[1] * 3.0));
       ax = axis == 0;
       ay = axis == 1;
       az = axis == 2;
-      dt[0] = (2.0 * u01(r1.x, r1.y) - 1.0) * st[1];
-      dt[1] = (2.0 * u01(r1.z, r1.w) - 1.0) * st[1];
-      const uint4 r2 = philox(make_uint4((uint32_t)b, (uint32_t)step, 2u, 0u), p.key0, p.key1);
-      dt[2] = (2.0 * u01(r2.x, r2.y) - 1.0) * st[1];
+      dt[0] = (2.0 * n[2] - 1.0) * st[1];
+      dt[1] = (2.0 * n[3] - 1.0) * st[1];
+      dt[2] = (2.0 * n[4] - 1.0) * st[1];
     }
     // R' = Rm R, Rm = rotation by th about (ax, ay, az) (rot.ml:121-146),
     // R = r_xyz(a, b, g) (rot.ml:52-66)
-    double sa, ca, sb, cb, sg, cg, sn, cs;
-    sincos((double)cur[3], &sa, &ca);
-    sincos((double)cur[4], &sb, &cb);
-    sincos((double)cur[5], &sg, &cg);
+    double sn, cs;
+    sincos(th, &sn, &cs);
     const double R[9] = {cb * cg, cg * sa * sb - ca * sg, sa * sg + ca * cg * sb,
                          cb * sg, ca * cg + sa * sb * sg, ca * sb * sg - cg * sa,
                          -sb,     cb * sa,                 ca * cb};
-    sincos(th, &sn, &cs);
     const double o = 1.0 - cs;
     const double M[9] = {cs + ax * ax * o,      ax * ay * o - az * sn, ax * az * o + ay * sn,
                          ax * ay * o + az * sn, cs + ay * ay * o,      ay * az * o - ax * sn,
@@ -163,15 +186,19 @@ __global__ void k_mc_propose(MCDev s, MCParams p) {
 #pragma unroll
       for (int j = 0; j < 3; ++j)
         Q[3 * i + j] = M[3 * i] * R[j] + M[3 * i + 1] * R[3 + j] + M[3 * i + 2] * R[6 + j];
-    // Rot.decompose (rot.ml:71-75)
+    // Rot.decompose (rot.ml:71-75): lane 0 the first angle, lane 1 the third
     const double beta = atan2(-Q[6], sqrt(Q[0] * Q[0] + Q[3] * Q[3]));
     const double icb = 1.0 / cos(beta);
-    tr[3] = (float)atan2(Q[7] * icb, Q[8] * icb);
-    tr[4] = (float)beta;
-    tr[5] = (float)atan2(Q[3] * icb, Q[0] * icb);
-    for (int k = 0; k < 3; ++k) tr[k] = (float)((double)cur[k] + dt[k]);
-    s.moved[b] = -1;
-  } else {
+    if (q == 0) tr[3] = (float)atan2(Q[7] * icb, Q[8] * icb);
+    if (q == 1) tr[5] = (float)atan2(Q[3] * icb, Q[0] * icb);
+    if (q == 2) {
+      tr[4] = (float)beta;
+      for (int k = 0; k < 3; ++k) tr[k] = (float)((double)cur[k] + dt[k]);
+    }
+    if (q == 3) s.moved[b] = -1;
+  } else if (q == 0) {
+    const uint4 r0 = philox(make_uint4((uint32_t)b, (uint32_t)step, 0u, 0u), p.key0, p.key1);
+    const uint4 r1 = philox(make_uint4((uint32_t)b, (uint32_t)step, 1u, 0u), p.key0, p.key1);
     // Mol.tweak_rbond: one bond, an angle in [-dr_i, dr_i] (or a Gaussian
     // step); Mol.flip_rbond in [-pi, pi] on conformer frames whose count of
     // earlier conformer frames is a positive multiple of flip_every
@@ -380,13 +407,19 @@ inline int nblk(int B) { return (B + 127) / 128; }
   }
 MMO_MC_LAUNCH(k_mc_init)
 MMO_MC_LAUNCH(k_mc_start)
-MMO_MC_LAUNCH(k_mc_propose)
 MMO_MC_LAUNCH(k_mc_accept)
 MMO_MC_LAUNCH(k_gd_begin)
 MMO_MC_LAUNCH(k_gd_propose)
 MMO_MC_LAUNCH(k_gd_accept)
 MMO_MC_LAUNCH(k_gd_take)
 #undef MMO_MC_LAUNCH
+
+// a quad of lanes per chain
+cudaError_t launch_k_mc_propose(const MCDev& s, const MCParams& p, cudaStream_t st) {
+  if (p.B <= 0) return cudaSuccess;
+  k_mc_propose<<<nblk(p.B * kQuad), 128, 0, st>>>(s, p);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_philox(uint32_t k0, uint32_t k1, uint32_t c1, uint32_t c2, int n, uint4* out,
                           cudaStream_t st) {
