@@ -92,7 +92,8 @@ int mmo_set_ligand(mmo_ctx* ctx, int n, const double* xs, const double* ys, cons
 
 /* Plain drop-in for Mol.ene_inter_UFF_shifted_bst / _shifted_brute /
  * _global_brute (mol.ml:796-849, 928-960) on the protein of mmo_set_protein:
- * one ligand (any n <= 128 atoms) per call, energy into *out. */
+ * one ligand (any n <= 128 atoms) per call, energy into *out; one launch (the
+ * pair partials, and their total from the last block). */
 int mmo_ene_inter(mmo_ctx* ctx, int n, const double* xs, const double* ys, const double* zs,
                   const double* q, const int* anum, double* out);
 
@@ -105,7 +106,7 @@ int mmo_ene_inter_parts(mmo_ctx* ctx, int n, const double* xs, const double* ys,
                         const double* q, const int* anum, double* elec, double* vdw);
 
 /* Plain drop-in for Mol.ene_intra_UFFNB_brute (mol.ml:881-903) on the ligand
- * of mmo_set_ligand, at the given coordinates. */
+ * of mmo_set_ligand, at the given coordinates.  One launch. */
 int mmo_ene_intra(mmo_ctx* ctx, const double* xs, const double* ys, const double* zs,
                   double* out);
 
@@ -116,7 +117,8 @@ int mmo_ene_intra(mmo_ctx* ctx, const double* xs, const double* ys, const double
  * E_out[B] (FP64): E_inter and/or E_intra as flags select.  grad_out (null
  * unless MMO_F_GRAD): B x (6 + nrb) floats, the analytic gradient replacing
  * approx_local_gradient (lds.ml:1118-1136).  status_out[B] (nullable):
- * MMO_S_* bits.  B = 1 runs the one-pose-per-launch plain path.  Page-locked
+ * MMO_S_* bits.  B = 1 with the inter term is one kernel launch (the
+ * one-pose path: rebuild, pair sums and finish fused).  Page-locked
  * buffers (cudaHostAlloc / cudaHostRegister) are read and written by DMA
  * directly; other host memory goes through the context's staging buffers. */
 int mmo_score_poses(mmo_ctx* ctx, int B, const float* dofs, int flags, double* E_out,
