@@ -436,6 +436,39 @@ def test_edge_single_atom_ligand(oracle, scorer_factory, small):
     assert E[1] == 0.0 and np.all(G[1] == 0.0)  # beyond the 12 A cutoff
 
 
+@pytest.mark.parametrize("case", ["one-atom ligand", "rigid ligand", "one-atom pocket"])
+def test_one_pose_edges(oracle, scorer_factory, small, case):
+    """The one-pose kernel at its edges, one pose per call against the oracle:
+    L = 1 (every thread of a CTA on one ligand atom), nrb = 0 (no torsions, no
+    intra terms to straddle), P = 1 (a single pair CTA)."""
+    rng = np.random.default_rng(12)
+    if case == "one-atom ligand":
+        lig = Mol("one", np.zeros(1), np.zeros(1), np.zeros(1), np.array([0.4]),
+                  np.array([8], np.int32), None, np.zeros((1, 1), np.int32))
+        pocket = small.pocket
+        d = np.array([[0.5, -1.0, 2.0, 0.1, 0.2, 0.3], [3.0, 2.0, -1.0, 1.0, 0.5, -2.0]],
+                     np.float32)
+    elif case == "rigid ligand":
+        lig = synth.random_ligand(rng, 20, 0)
+        pocket = small.pocket
+        d = synth.random_poses(rng, 6, 0, 2.0)
+    else:
+        lig = small.ligand
+        pocket = synth.random_pocket(rng, 1, 1.0)
+        d = small.poses[:1].repeat(3, axis=0)
+        d[1, :3] += 1.5
+        d[2, :3] -= 2.0
+    sysm = synth.System(case, pocket, lig, d)
+    s = scorer_factory(pocket, lig)
+    ref = ref_batch(oracle, sysm, d, grad=True)
+    for b in range(len(d)):
+        E1, G1, st1 = s.score_poses(d[b:b + 1], grad=True)
+        assert s.last_launches() == 1
+        assert_energy(E1, ref.E[b:b + 1], ref.S[b:b + 1])
+        assert_grad(G1, ref.G[b:b + 1], ref.GA[b:b + 1])
+        assert st1[0] == ref.st[b]
+
+
 def test_edge_max_ligand_and_two_slices(oracle, scorer_factory):
     rng = np.random.default_rng(4)
     lig = synth.random_ligand(rng, 128, 32)
