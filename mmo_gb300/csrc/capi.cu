@@ -3163,13 +3163,12 @@ int mmo_ene_inter_grid(mmo_ctx* ctx, int n, const double* xs, const double* ys, 
     *out = 0.0;
     return MMO_OK;
   }
-  // staging: X[n][2] float4 | type[n] int ; output: E parts [n] | E | status
+  // staging: X[n][2] float4 | type[n] int ; output: E | status
   size_t off = 0;
   const size_t oX = take(off, sizeof(float4) * 2 * n);
   const size_t ot = take(off, sizeof(int) * n);
   const size_t in_bytes = off;
   size_t ooff = 0;
-  const size_t oEp = take(ooff, sizeof(double) * n);
   const size_t oE = take(ooff, sizeof(double));
   const size_t oS = take(ooff, sizeof(int));
   MMO_CK(cudaSetDevice(ctx->device), "set device");
@@ -3190,17 +3189,14 @@ int mmo_ene_inter_grid(mmo_ctx* ctx, int n, const double* xs, const double* ys, 
                 zs[i] - ctx->origin[2], 0.f);
     ht[i] = t;
   }
-  double* dEp = reinterpret_cast<double*>(ctx->d_out + oEp);
   int* dS = reinterpret_cast<int*>(ctx->d_out + oS);
   MMO_CK(cudaMemcpyAsync(ctx->d_in, ctx->h_in, in_bytes, cudaMemcpyHostToDevice, ctx->stream),
          "H2D");
-  MMO_CK(cudaMemsetAsync(dS, 0, sizeof(int), ctx->stream), "status reset");
-  MMO_CK(launch_grid_inter(grid_look(ctx), reinterpret_cast<const float4*>(ctx->d_in + oX), n, n,
-                           reinterpret_cast<const int*>(ctx->d_in + ot), ctx->d_grid, dEp, nullptr,
-                           dS, 0, ctx->stream),
+  MMO_CK(launch_grid_inter_one(grid_look(ctx), reinterpret_cast<const float4*>(ctx->d_in + oX), n,
+                               reinterpret_cast<const int*>(ctx->d_in + ot), ctx->d_grid,
+                               reinterpret_cast<double*>(ctx->d_out + oE), dS, ctx->stream),
          "grid lookup kernel");
-  MMO_CK(launch_reduce_plain(dEp, n, reinterpret_cast<double*>(ctx->d_out + oE), ctx->stream),
-         "reduce kernel");
+  ctx->last_launches = 1;
   MMO_CK(cudaMemcpyAsync(ctx->h_out + oE, ctx->d_out + oE, ooff - oE, cudaMemcpyDeviceToHost,
                          ctx->stream),
          "D2H");

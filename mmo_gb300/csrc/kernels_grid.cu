@@ -565,24 +565,21 @@ __device__ __forceinline__ bool lattice_cell(float xh, float xl, float oh, float
 // in FP32 (the values are float32, as the reference's .ba1 grids).  A corner
 // off the lattice (the reference reads out of bounds) sets MMO_S_OFF_GRID and
 // the entry adds 0.
+// the trilinear value (and gradient) of the type grid `type` at the entry's
+// position; false when a corner is off the lattice (E = 0 then)
 template <bool GRAD>
-__global__ void k_grid_inter(GridLook g, const float4* __restrict__ X, int n, int L,
-                             const int* __restrict__ atom_type, const float* __restrict__ grids,
-                             double* Epart, float4* Gpart, int* status) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= n) return;
-  const float4 h = X[2 * (size_t)e], l = X[2 * (size_t)e + 1];
+__device__ __forceinline__ bool grid_entry(const GridLook& g, float4 h, float4 l, int type,
+                                           const float* __restrict__ grids, float& E, float& gx,
+                                           float& gy, float& gz) {
   int i0, j0, k0;
   float wx, wy, wz;
   const bool ok = lattice_cell(h.x, l.x, g.oh[0], g.ol[0], g.invh, g.invl, g.nx, i0, wx) &
                   lattice_cell(h.y, l.y, g.oh[1], g.ol[1], g.invh, g.invl, g.ny, j0, wy) &
                   lattice_cell(h.z, l.z, g.oh[2], g.ol[2], g.invh, g.invl, g.nz, k0, wz);
-  float E = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
-  if (!ok) {
-    atomicOr(&status[e / L], kStatusOffGrid);
-  } else {
+  E = gx = gy = gz = 0.f;
+  if (ok) {
     const size_t nx = g.nx, nxy = (size_t)g.nx * g.ny;
-    const float* v = grids + (size_t)atom_type[e % L] * nxy * g.nz + i0 + j0 * nx + k0 * nxy;
+    const float* v = grids + (size_t)type * nxy * g.nz + i0 + j0 * nx + k0 * nxy;
     const float a = v[0], b = v[1], c = v[1 + nx], d = v[nx];
     const float ee = v[nxy], f = v[1 + nxy], gg = v[1 + nx + nxy], hh = v[nx + nxy];
     const float hx = 1.f - wx, hy = 1.f - wy, hz = 1.f - wz;
@@ -597,8 +594,51 @@ __global__ void k_grid_inter(GridLook g, const float4* __restrict__ X, int n, in
       gz = inv * (c1 - c0);
     }
   }
+  return ok;
+}
+
+template <bool GRAD>
+__global__ void k_grid_inter(GridLook g, const float4* __restrict__ X, int n, int L,
+                             const int* __restrict__ atom_type, const float* __restrict__ grids,
+                             double* Epart, float4* Gpart, int* status) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  float E, gx, gy, gz;
+  if (!grid_entry<GRAD>(g, X[2 * (size_t)e], X[2 * (size_t)e + 1], atom_type[e % L], grids, E,
+                        gx, gy, gz))
+    atomicOr(&status[e / L], kStatusOffGrid);
   Epart[e] = (double)E;
   if (GRAD) Gpart[e] = make_float4(gx, gy, gz, 0.f);
+}
+
+// One ligand (the grid closure, mmo_ene_inter_grid) in one block of 128
+// threads, an atom each: the energy summed in a fixed order into *Eout and the
+// status (MMO_S_OFF_GRID when a corner is off the lattice) into *status.
+__global__ void __launch_bounds__(kMaxLig) k_grid_inter_one(GridLook g, const float4* X, int n,
+                                                          const int* atom_type,
+                                                          const float* grids, double* Eout,
+                                                          int* status) {
+  __shared__ double ws[kMaxLig / 32];
+  __shared__ int s_st;
+  const int e = threadIdx.x, lane = e & 31;
+  if (e == 0) s_st = 0;
+  __syncthreads();
+  double E = 0.0;
+  if (e < n) {
+    float ef, gx, gy, gz;
+    if (!grid_entry<false>(g, X[2 * e], X[2 * e + 1], atom_type[e], grids, ef, gx, gy, gz))
+      atomicOr(&s_st, kStatusOffGrid);
+    E = (double)ef;
+  }
+  E = warp_sum(E);
+  if (lane == 0) ws[e >> 5] = E;
+  __syncthreads();
+  if (e == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kMaxLig / 32; ++w) t += ws[w];
+    *Eout = t;
+    *status = s_st;
+  }
 }
 
 }  // namespace
@@ -676,6 +716,14 @@ cudaError_t launch_grid_build(const DevCull& cull, const GridBuild& gb, int diel
                  : grid_build_kp<1, false>(cull, gb, grids, st);
   return count ? grid_build_kp<0, true>(cull, gb, grids, st)
                : grid_build_kp<0, false>(cull, gb, grids, st);
+}
+
+cudaError_t launch_grid_inter_one(const GridLook& g, const float4* X, int n,
+                                  const int* atom_type, const float* grids, double* Eout,
+                                  int* status, cudaStream_t st) {
+  if (n <= 0 || n > kMaxLig) return cudaErrorInvalidValue;
+  k_grid_inter_one<<<1, kMaxLig, 0, st>>>(g, X, n, atom_type, grids, Eout, status);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_grid_inter(const GridLook& g, const float4* X, int n, int L,

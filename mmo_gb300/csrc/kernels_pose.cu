@@ -1644,13 +1644,6 @@ __global__ void __launch_bounds__(kFinishOne)
   finish_one_cta<GRAD, RECENTER, DIEL, IFORM>(lig, io, scr, flags, osm);
 }
 
-// one warp: sum of n FP64 partials
-__global__ void k_reduce_plain(const double* Epart, int n, double* out) {
-  double e = 0.0;
-  for (int k = threadIdx.x; k < n; k += 32) e += Epart[k];
-  e = warp_sum(e);
-  if (threadIdx.x == 0) out[0] = e;
-}
 
 // one warp: intra-ligand energy of one set of hi/lo coordinates X[L][2]
 // (mol.ml:881-903)
@@ -1892,10 +1885,6 @@ cudaError_t launch_finish(const DevLigand& lig, const PoseIO& io, const Scratch&
 #undef MMO_FN
 }
 
-cudaError_t launch_reduce_plain(const double* Epart, int n, double* out, cudaStream_t st) {
-  k_reduce_plain<<<1, 32, 0, st>>>(Epart, n, out);
-  return cudaGetLastError();
-}
 
 cudaError_t launch_intra_plain(const DevLigand& lig, const float4* X, int form, int dielectric,
                                double* out, cudaStream_t st) {

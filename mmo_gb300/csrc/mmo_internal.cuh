@@ -497,7 +497,6 @@ cudaError_t launch_one_pose(const DevLigand& lig, const DevProtein& prot, const 
                             const Physics& ph, cudaStream_t st, int* stage);
 cudaError_t launch_finish(const DevLigand& lig, const PoseIO& io, const Scratch& s, int flags,
                           const Physics& ph, cudaStream_t st);
-cudaError_t launch_reduce_plain(const double* Epart, int n, double* out, cudaStream_t st);
 // the inter energy's two parts for one ligand: Eout[0] electrostatic, Eout[1]
 // van der Waals (Epart: 2 C L partials), one launch
 cudaError_t launch_pairs_parts(const DevProtein& prot, const PairTable& tab, const float4* X,
@@ -518,6 +517,10 @@ int cull_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_b
 int cull_smem_bytes(int npairs, int nrows, int threads, bool glob, int kp);
 cudaError_t launch_grid_build(const DevCull& cull, const GridBuild& gb, int dielectric,
                               float* grids, cudaStream_t st);
+// one ligand of n <= kMaxLig atoms in one launch: its energy and status
+cudaError_t launch_grid_inter_one(const GridLook& g, const float4* X, int n,
+                                  const int* atom_type, const float* grids, double* Eout,
+                                  int* status, cudaStream_t st);
 cudaError_t launch_grid_inter(const GridLook& g, const float4* X, int n, int L,
                               const int* atom_type, const float* grids, double* Epart,
                               float4* Gpart, int* status, int grad, cudaStream_t st);

@@ -198,6 +198,11 @@ def test_off_lattice_atoms_flagged_and_skipped(oracle, scorer_factory, system, l
         e, off, _ = _interp_ref(oracle, system, g, lattice, lt, d[b])
         assert off and (st[b] & 4)
         assert abs(E[b] - e) <= I_TOL * max(abs(e), 100.0)
+        # the closure (one launch) flags it the same way
+        xyz, _ = oracle.apply_config(system.ligand, d[b].astype(np.float64), 0)
+        e1, st1 = s.ene_inter_grid(system.ligand.with_xyz(xyz))
+        assert st1 & 4
+        assert abs(e1 - e) <= I_TOL * max(abs(e), 100.0)
 
 
 def test_loaded_grids_score_like_built(scorer_factory, system, lattice, tmp_path):
@@ -283,6 +288,7 @@ def test_plain_interp_closure_matches_oracle(oracle, gpu_lib, system, lattice):
     for conf in system.poses[:6]:
         xyz, _ = oracle.apply_config(system.ligand, conf.astype(np.float64), 0)
         e = f(system.ligand.with_xyz(xyz))
+        assert s.last_launches() == 1  # lookup and sum in one block
         e64, off = oracle.ene_inter_interp(STEP, d2, g, xyz - o2, lt)
         assert not off
         assert abs(e - e64) <= I_TOL * _corner_scale(g, lt, (xyz - o2) / STEP)
