@@ -1110,9 +1110,9 @@ int check_dev_err(mmo_ctx* ctx, int flag) {
 
 // the one-pose path's per-CTA partials: npair CTAs of kOneChunk protein atoms,
 // and the intra CTA's terms
-int ensure_one_scratch(mmo_ctx* ctx, int L) {
+int ensure_one_scratch(mmo_ctx* ctx, int L, bool grid) {
   OneScratch& o = ctx->one;
-  o.npair = std::max(1, (ctx->prot.P + kOneChunk - 1) / kOneChunk);
+  o.npair = grid ? 1 : std::max(1, (ctx->prot.P + kOneChunk - 1) / kOneChunk);
   int r;
   if ((r = grow(ctx, (void**)&o.E, &ctx->capOneE, sizeof(float2) * (size_t)o.npair * L,
                 "one-pose partials")))
@@ -1125,6 +1125,7 @@ int ensure_one_scratch(mmo_ctx* ctx, int L) {
     MMO_CK(cudaMemset(o.arrive, 0, sizeof(unsigned)), "one-pose counter");
   }
   if (!o.intra) MMO_CK(cudaMalloc((void**)&o.intra, sizeof(float) * (kMaxTors + 2)), "one-pose intra terms");
+  if (!o.gstat) MMO_CK(cudaMalloc((void**)&o.gstat, sizeof(int)), "one-pose grid status");
   return MMO_OK;
 }
 
@@ -1149,8 +1150,9 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
   ctx->last_grad = grad ? 1 : 0;
   ctx->last_pairs = inter && !use_grid ? (double)B * L * ctx->prot.P : 0.0;
   ctx->last_pose_entries = 0;  // set below once the rebuild has written X
-  // one pose with pair sums: the fused one-launch path (k_one_pose)
-  const bool one = B == 1 && inter && !use_grid && ctx->one_ok;
+  // one pose with the inter term (pair sums or the grids): the fused one-launch
+  // path (k_one_pose)
+  const bool one = B == 1 && inter && ctx->one_ok;
   // rebuild (which bins the entries for the cut-off sweep) + finish, and the
   // sweep: scan, scatter, broad phase, sweep (or the grid lookup)
   ctx->last_launches = one ? 1 : 2 + (cull ? 4 : (inter ? 1 : 0));
@@ -1169,7 +1171,7 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
   }
   if ((r = ensure_scratch(ctx, B, L, C, grad))) return r;
   if (cull && (r = ensure_cull_scratch(ctx, B, L, grad))) return r;
-  if (one && (r = ensure_one_scratch(ctx, L))) return r;
+  if (one && (r = ensure_one_scratch(ctx, L, use_grid))) return r;
   PoseIO io{};
   io.dofs = d_dofs;
   io.E = d_E;
@@ -1194,6 +1196,12 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
     MMO_CK(mark(2), "event");
     int stage = 0;
     ctx->one.with_intra = ctx->lig.nested && (fl & kFlagIntra) ? 1 : 0;
+    ctx->one.grid = use_grid ? 1 : 0;
+    if (use_grid) {
+      ctx->one.gl = grid_look(ctx);
+      ctx->one.grids = ctx->d_grid;
+      ctx->one.grid_lt = ctx->d_grid_lt;
+    }
     const cudaError_t pending = cudaGetLastError();
     if (pending != cudaSuccess)
       return cuda_fail(ctx, pending, "error left by an earlier runtime call");
@@ -1773,6 +1781,7 @@ int mmo_ctx_destroy(mmo_ctx* ctx) {
   cudaFree(ctx->one.G);
   cudaFree(ctx->one.arrive);
   cudaFree(ctx->one.intra);
+  cudaFree(ctx->one.gstat);
   cudaFree(ctx->d_plain_arrive);
   cudaFree(ctx->cs.gcount);
   cudaFree(ctx->cs.glist);

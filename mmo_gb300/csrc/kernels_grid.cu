@@ -530,73 +530,6 @@ __global__ void __launch_bounds__(kGridWarps * 32) k_grid_build_pk(DevCull cull,
   grid_store<true, KP, ELEC>(gb, P, ad, grids);
 }
 
-// Lattice coordinate u = (x - o) / step of a float-pair coordinate on one axis,
-// as a cell i = floor(u) and a fraction w in [0, 1), in float-pair arithmetic
-// (TwoDiff of the high parts, the product's error by FMA); false unless the
-// cell's high corner is on the lattice (0 <= u < n - 1).
-__device__ __forceinline__ bool lattice_cell(float xh, float xl, float oh, float ol, float ih,
-                                             float il, int n, int& i, float& w) {
-  const float dh = __fsub_rn(xh, oh);
-  const float bp = __fsub_rn(dh, xh), ap = __fsub_rn(dh, bp);
-  const float de = __fadd_rn(__fsub_rn(xh, ap), __fsub_rn(-oh, bp));
-  const float dl = __fadd_rn(de, __fsub_rn(xl, ol));
-  const float uh = __fmul_rn(dh, ih);
-  const float ul = __fadd_rn(fmaf(dh, ih, -uh), fmaf(dh, il, __fmul_rn(dl, ih)));
-  if (!(uh > -2.0f && uh < (float)n + 1.0f)) return false;  // also NaN
-  const float f = floorf(uh);
-  float frac = __fadd_rn(__fsub_rn(uh, f), ul);
-  int k = (int)f;
-  if (frac < 0.f) {
-    frac = __fadd_rn(frac, 1.f);
-    --k;
-  } else if (frac >= 1.f) {
-    frac = __fsub_rn(frac, 1.f);
-    ++k;
-  }
-  if (frac >= 1.f) frac = 0.99999994f;
-  i = k;
-  w = frac;
-  return k >= 0 && k <= n - 2;
-}
-
-// One thread per entry: E = trilin of the atom's type grid at the atom, and
-// dE/dx (the derivative of the trilinear form), into Epart / Gpart.  The
-// lattice coordinate in float pairs; weights, values and the interpolation
-// in FP32 (the values are float32, as the reference's .ba1 grids).  A corner
-// off the lattice (the reference reads out of bounds) sets MMO_S_OFF_GRID and
-// the entry adds 0.
-// the trilinear value (and gradient) of the type grid `type` at the entry's
-// position; false when a corner is off the lattice (E = 0 then)
-template <bool GRAD>
-__device__ __forceinline__ bool grid_entry(const GridLook& g, float4 h, float4 l, int type,
-                                           const float* __restrict__ grids, float& E, float& gx,
-                                           float& gy, float& gz) {
-  int i0, j0, k0;
-  float wx, wy, wz;
-  const bool ok = lattice_cell(h.x, l.x, g.oh[0], g.ol[0], g.invh, g.invl, g.nx, i0, wx) &
-                  lattice_cell(h.y, l.y, g.oh[1], g.ol[1], g.invh, g.invl, g.ny, j0, wy) &
-                  lattice_cell(h.z, l.z, g.oh[2], g.ol[2], g.invh, g.invl, g.nz, k0, wz);
-  E = gx = gy = gz = 0.f;
-  if (ok) {
-    const size_t nx = g.nx, nxy = (size_t)g.nx * g.ny;
-    const float* v = grids + (size_t)type * nxy * g.nz + i0 + j0 * nx + k0 * nxy;
-    const float a = v[0], b = v[1], c = v[1 + nx], d = v[nx];
-    const float ee = v[nxy], f = v[1 + nxy], gg = v[1 + nx + nxy], hh = v[nx + nxy];
-    const float hx = 1.f - wx, hy = 1.f - wy, hz = 1.f - wz;
-    const float c00 = fmaf(b, wx, a * hx), c10 = fmaf(c, wx, d * hx);
-    const float c01 = fmaf(f, wx, ee * hx), c11 = fmaf(gg, wx, hh * hx);
-    const float c0 = fmaf(c10, wy, c00 * hy), c1 = fmaf(c11, wy, c01 * hy);
-    E = fmaf(c1, wz, c0 * hz);
-    if (GRAD) {
-      const float inv = g.invh;
-      gx = inv * (hz * fmaf(c - d, wy, (b - a) * hy) + wz * fmaf(gg - hh, wy, (f - ee) * hy));
-      gy = inv * (hz * (c10 - c00) + wz * (c11 - c01));
-      gz = inv * (c1 - c0);
-    }
-  }
-  return ok;
-}
-
 template <bool GRAD>
 __global__ void k_grid_inter(GridLook g, const float4* __restrict__ X, int n, int L,
                              const int* __restrict__ atom_type, const float* __restrict__ grids,

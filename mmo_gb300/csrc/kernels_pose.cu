@@ -1338,7 +1338,7 @@ __device__ __forceinline__ void one_intra_terms(const DevLigand& lig, const OneS
 template <bool GRAD, bool RECENTER>
 __device__ __forceinline__ void finish_one_nested(const DevLigand& lig, const PoseIO& io,
                                                   const OneSmem& m, int flags,
-                                                  const float* intra_g) {
+                                                  const float* intra_g, int extra_status) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, L = lig.L, nrb = lig.nrb;
   constexpr int kWarps = kFinishOne / 32;
   if (warp == 0) {  // double-float sums; FP64 only for the outputs
@@ -1352,7 +1352,7 @@ __device__ __forceinline__ void finish_one_nested(const DevLigand& lig, const Po
       if (intra_g) t = dadd(t, make_float2(__ldcg(intra_g + nrb), __ldcg(intra_g + nrb + 1)));
       const double e = (double)t.x + (double)t.y;
       io.E[0] = e;
-      io.status[0] = *m.status | (isfinite(e) ? 0 : kStatusNonFinite);
+      io.status[0] = *m.status | extra_status | (isfinite(e) ? 0 : kStatusNonFinite);
       if (io.E_inter) io.E_inter[0] = (double)ei.x + (double)ei.y;
     }
   }
@@ -1486,7 +1486,7 @@ __global__ void __launch_bounds__(kFinishOne)
   // a chunk of protein atoms each; their loads overlap the rebuild
   const bool intra_cta = os.with_intra && blockIdx.x == 0;
   const int c = blockIdx.x - os.with_intra;  // the pair chunk
-  const int c0 = c * kOneChunk, n = intra_cta ? 0 : min(kOneChunk, prot.P - c0);
+  const int c0 = c * kOneChunk, n = intra_cta || os.grid ? 0 : min(kOneChunk, prot.P - c0);
   if (tid < n) {
     m.sp[2 * tid] = prot.atoms[2 * (c0 + tid)];
     m.sp[2 * tid + 1] = prot.atoms[2 * (c0 + tid) + 1];
@@ -1509,6 +1509,21 @@ __global__ void __launch_bounds__(kFinishOne)
   }
   if (intra_cta) {
     one_intra_terms<GRAD, DIEL, IFORM>(lig, m, os.intra);
+  } else if (os.grid) {
+    // MMO_F_GRID: the inter terms of every ligand atom from its type's grid
+    // (k_grid_inter's lookup), a thread per atom
+    if (tid == 0) s_last = 0;  // (the off-lattice flag until the arrival below)
+    __syncthreads();
+    if (tid < L) {
+      float e, gx, gy, gz;
+      if (!grid_entry<GRAD>(os.gl, m.Xh[tid], m.Xl[tid], os.grid_lt[tid], os.grids, e, gx, gy,
+                            gz))
+        atomicOr(&s_last, kStatusOffGrid);
+      os.E[tid] = make_float2(e, 0.f);
+      if (GRAD) os.G[tid] = make_float4(gx, gy, gz, 0.f);
+    }
+    __syncthreads();
+    if (tid == 0) *os.gstat = s_last;
   } else {
     // the pair terms of this CTA's protein atoms
     if (g < S) {
@@ -1616,9 +1631,11 @@ __global__ void __launch_bounds__(kFinishOne)
                               __fadd_rn(sz.x, sz.y), 0.f);
   }
   if (tid == 0) *os.arrive = 0u;  // ready for the next launch
+  const int gst = os.grid ? __ldcg(os.gstat) : 0;  // the lookup CTA's off-lattice bit
   __syncthreads();
   if (nested) {
-    finish_one_nested<GRAD, RECENTER>(lig, io, m, flags, os.with_intra ? os.intra : nullptr);
+    finish_one_nested<GRAD, RECENTER>(lig, io, m, flags, os.with_intra ? os.intra : nullptr,
+                                      gst);
     return;
   }
   // other ligands: the work buffers of the one-pose finishing code
@@ -1639,7 +1656,7 @@ __global__ void __launch_bounds__(kFinishOne)
       scr.cen[1] = make_float4(m.cen[0].y, m.cen[1].y, m.cen[2].y, 0.f);
     }
   }
-  if (tid == 0) io.status[0] = *m.status;
+  if (tid == 0) io.status[0] = *m.status | gst;
   __syncthreads();  // the buffers above are written before the finish reads them
   finish_one_cta<GRAD, RECENTER, DIEL, IFORM>(lig, io, scr, flags, osm);
 }

@@ -167,6 +167,35 @@ def test_interpolated_energy_matches_oracle(oracle, scorer_factory, system, latt
     assert np.allclose(Et, E + Ei, rtol=1e-12, atol=1e-9)
 
 
+@pytest.mark.parametrize("recenter", [False, True])
+def test_one_pose_on_grids_is_one_launch(oracle, scorer_factory, system, lattice, recenter):
+    """One pose per call with MMO_F_GRID runs the one-pose kernel (a lookup CTA
+    beside the intra CTA): one launch, the energy against the oracle's
+    interpolation plus intra term, the gradient as the batched grid path's, and
+    the off-lattice bit."""
+    s, types, lt = _built(scorer_factory, system, lattice)
+    g = s.grid_values()
+    d = system.poses[:8]
+    Eb, Gb, stb = s.score_poses(d, grad=True, grid=True, recenter=recenter)
+    Ei, _, _ = s.score_poses(d, inter=False, recenter=recenter)
+    origin, dims = lattice
+    for b in range(len(d)):
+        E1, G1, st1 = s.score_poses(d[b:b + 1], grad=True, grid=True, recenter=recenter)
+        assert s.last_launches() == 1
+        assert st1[0] == stb[b]
+        e, off, xyz = _interp_ref(oracle, system, g, lattice, lt, d[b], recenter)
+        sc = _corner_scale(g, lt, (xyz - origin) / STEP)
+        # (E1 - Ei: the inter part, up to the intra sums' FP32 rounding)
+        assert abs((E1[0] - Ei[b]) - e) <= I_TOL * max(sc, 1e-300) + 1e-6 * abs(Ei[b])
+        # the intra sums round differently (FP32 terms in another order)
+        assert abs(E1[0] - Eb[b]) <= 1e-7 * max(abs(Eb[b]), sc, abs(Ei[b]))
+        assert np.abs(G1[0] - Gb[b]).max() <= 1e-5 * np.abs(Gb[b]).max()
+    far = d[:1].copy()
+    far[0, 0] = 16.0  # the ligand's far side leaves the lattice
+    _, _, stf = s.score_poses(far, grad=True, grid=True, recenter=recenter)
+    assert stf[0] & 4
+
+
 def test_interpolated_gradient_matches_differences(oracle, scorer_factory, system, lattice):
     s, types, lt = _built(scorer_factory, system, lattice)
     g = s.grid_values()
