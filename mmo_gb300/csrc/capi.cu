@@ -2417,9 +2417,9 @@ int mmo_tune(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_E, f
     if (ctx->ph.inter_form == 0 && ctx->cull_ok)
       for (int mem : {1, 2}) {
         if (mem == 1 && !ctx->cull_fits) continue;  // the staged copy needs shared memory
-        for (double h : {2.0, 3.0, 4.0})
+        for (double h : {2.0, 3.0, 4.0, 5.0})
           for (int kp : {1, 2, 4})
-            for (int piece : {256, 512}) {
+            for (int piece : {256, 512, 1024}) {
               // the register budget's thread count, and fewer warps with more shared
               // memory left to the L1
               const int th = cull_max_threads(kp);
