@@ -1467,9 +1467,9 @@ __device__ __forceinline__ void finish_one_nested(const DevLigand& lig, const Po
   }
 }
 
-// static shared memory of k_one_pose (type table and flag), rounded up
+// static shared memory of k_one_pose (type table and flags), rounded up
 constexpr int kOneStatic = 2048;
-static_assert(sizeof(float2) * kNTypes * kNTypes + 16 <= kOneStatic, "k_one_pose static smem");
+static_assert(sizeof(float2) * kNTypes * kNTypes + 32 <= kOneStatic, "k_one_pose static smem");
 
 template <bool GRAD, bool RECENTER, int DIEL, int FORM, int IFORM>
 __global__ void __launch_bounds__(kFinishOne)
@@ -1477,7 +1477,7 @@ __global__ void __launch_bounds__(kFinishOne)
                Scratch scr, OneScratch os, int flags) {
   extern __shared__ __align__(16) float4 osm[];
   __shared__ float2 stab[kNTypes * kNTypes];
-  __shared__ int s_last;
+  __shared__ int s_last, s_offgrid;
   const int tid = threadIdx.x, L = lig.L, nrb = lig.nrb;
   const bool nested = lig.nested;
   const OneSmem m = one_smem(reinterpret_cast<char*>(osm), L, nrb);
@@ -1512,18 +1512,18 @@ __global__ void __launch_bounds__(kFinishOne)
   } else if (os.grid) {
     // MMO_F_GRID: the inter terms of every ligand atom from its type's grid
     // (k_grid_inter's lookup), a thread per atom
-    if (tid == 0) s_last = 0;  // (the off-lattice flag until the arrival below)
+    if (tid == 0) s_offgrid = 0;
     __syncthreads();
     if (tid < L) {
       float e, gx, gy, gz;
       if (!grid_entry<GRAD>(os.gl, m.Xh[tid], m.Xl[tid], os.grid_lt[tid], os.grids, e, gx, gy,
                             gz))
-        atomicOr(&s_last, kStatusOffGrid);
+        atomicOr(&s_offgrid, kStatusOffGrid);
       os.E[tid] = make_float2(e, 0.f);
       if (GRAD) os.G[tid] = make_float4(gx, gy, gz, 0.f);
     }
     __syncthreads();
-    if (tid == 0) *os.gstat = s_last;
+    if (tid == 0) *os.gstat = s_offgrid;
   } else {
     // the pair terms of this CTA's protein atoms
     if (g < S) {
