@@ -453,9 +453,24 @@ __device__ __noinline__ void finish_pose(const DevLigand& lig, int C, const doub
     __syncwarp();
   }
   if (intra && !pre) {
+    // pairs lane, lane + 32, ... in that order, their records loaded four at a
+    // time so that the loads' latencies overlap
     float acc = 0.f;
-    for (int p = lane; p < lig.npairs; p += 32)
-      intra_pair_terms<DIEL, IFORM>(lig, sxh, sxl, saxis, p, crossing, acc, sdti + lane, 33);
+    for (int p0 = lane; p0 < lig.npairs; p0 += 4 * 32) {
+      int2 ij[4];
+      float4 par[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int p = p0 + 32 * u;
+        ij[u] = p < lig.npairs ? lig.pair_ij[p] : make_int2(0, 0);
+        par[u] = p < lig.npairs ? lig.pair_par[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (p0 + 32 * u < lig.npairs)
+          intra_pair_terms_at<DIEL, IFORM>(sxh, sxl, saxis, ij[u], par[u], lig.amask, crossing,
+                                           acc, sdti + lane, 33);
+    }
     e += (double)acc;
   }
   if (intra && pre && lane == 0) e += pre_e;
