@@ -4,15 +4,17 @@
 // bisector-tree neighbour query returns within 12 A).  Here the query is made for a
 // group of 32 * KP (pose, ligand atom) entries at once:
 //
-//   k_cull_bin      entry -> (ligand type segment, Hilbert cell of its position)
+//   (the pose rebuild bins the entries: ligand type segment, Hilbert cell of
+//   each entry's position, count and rank)
 //   k_cull_scan     bin counts -> first slot of each bin (one CTA per segment)
 //   k_cull_scatter  entries copied into slot order
-//   k_pairs_cull    persistent CTAs, protein resident in shared memory (TMA
-//                   bulk copy); a warp takes (group, protein piece) items from
-//                   a work counter, bounds its group by a box and sweeps the
-//                   rows of the piece that come within 12 A of the box
-//                   and the last piece of a group to finish sums the group's
-//                   pieces in piece order
+//   k_cull_items    broad phase: the (group, protein piece) items within 12 A
+//   k_pairs_cull    persistent CTAs, protein staged in shared memory (TMA bulk
+//                   copy) or read from global memory; a warp takes (group,
+//                   piece) items from a work counter, bounds its group by a box
+//                   and sweeps the rows of the piece that come within 12 A of
+//                   the box, and the last piece of a group to finish sums the
+//                   group's pieces in piece order
 //
 // Slot order only decides which entries share a warp.  Skipped pairs add
 // exact zeros and the FP32 partials are flushed at fixed rows, so the result
@@ -41,19 +43,6 @@ __device__ __forceinline__ void stage_pair_table(const float4* __restrict__ tabv
   }
 }
 
-__global__ void k_cull_bin(const float4* __restrict__ X, int n, int L,
-                           const int* __restrict__ seg_of_atom, DevCull cull, unsigned* hist,
-                           int* bin, int* rank) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= n) return;
-  const float4 h = X[2 * (size_t)e];
-  const uint32_t cx = grid_cell(h.x, cull.glo[0], cull.ginv);
-  const uint32_t cy = grid_cell(h.y, cull.glo[1], cull.ginv);
-  const uint32_t cz = grid_cell(h.z, cull.glo[2], cull.ginv);
-  const int b = seg_of_atom[e % L] * kCullBins + (int)hilbert_cell(cx, cy, cz);
-  bin[e] = b;
-  rank[e] = (int)atomicAdd(&hist[b], 1u);
-}
 
 constexpr int kScanThreads = 1024;
 constexpr int kScanPer = kCullBins / kScanThreads;  // 32 consecutive bins per thread
@@ -742,13 +731,11 @@ int cull_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_b
 }
 
 cudaError_t launch_cull_sort(const DevCull& cull, const Scratch& s, const float* lig_q, int B,
-                             int L, const CullSegs& seg, const CullScratch& cs, bool binned,
-                             cudaStream_t st) {
+                             int L, const CullSegs& seg, const CullScratch& cs, cudaStream_t st) {
   const int n = B * L;
   if (n <= 0) return cudaSuccess;
   const int tb = 256, nb = (n + tb - 1) / tb;
-  if (!binned)  // (the rebuild bins the entries when it can)
-    k_cull_bin<<<nb, tb, 0, st>>>(s.X, n, L, cs.seg_of_atom, cull, cs.hist, cs.bin, cs.rank);
+  (void)cull;  // the entries were binned by the rebuild (rebuild_pose)
   cudaError_t e = cudaFuncSetAttribute(k_cull_scan, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        kScanSmem);
   if (e != cudaSuccess) return e;
