@@ -1244,7 +1244,7 @@ int score_device(mmo_ctx* ctx, int B, const float* d_dofs, int flags, double* d_
   MMO_CK(mark(1), "event");
   if (cull) {
     const CullSegs& sg = ctx->segs[grad ? 1 : 0];
-    MMO_CK(launch_cull_sort(ctx->cull, ctx->scr, ctx->lig.q, B, L, sg, ctx->cs, st),
+    MMO_CK(launch_cull_sort(ctx->scr, ctx->lig.q, B, L, sg, ctx->cs, st),
            "entry sort kernels");
     MMO_CK(mark(2), "event");
     MMO_CK(launch_pairs_cull(ctx->cull, ctx->d_tab4, sg, ctx->cs, fl, ctx->ph, ctx->cplan[grad], d_err,

@@ -730,12 +730,12 @@ int cull_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_b
   return nb;
 }
 
-cudaError_t launch_cull_sort(const DevCull& cull, const Scratch& s, const float* lig_q, int B,
-                             int L, const CullSegs& seg, const CullScratch& cs, cudaStream_t st) {
+// (the entries were binned by the rebuild, rebuild_pose)
+cudaError_t launch_cull_sort(const Scratch& s, const float* lig_q, int B, int L,
+                             const CullSegs& seg, const CullScratch& cs, cudaStream_t st) {
   const int n = B * L;
   if (n <= 0) return cudaSuccess;
   const int tb = 256, nb = (n + tb - 1) / tb;
-  (void)cull;  // the entries were binned by the rebuild (rebuild_pose)
   cudaError_t e = cudaFuncSetAttribute(k_cull_scan, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        kScanSmem);
   if (e != cudaSuccess) return e;

@@ -514,8 +514,8 @@ cudaError_t launch_intra_plain(const DevLigand& lig, const float4* X, int form, 
                                double* out, cudaStream_t st);
 int pairs_batched_max_blocks(int kp, int threads, int grad, const Physics& ph, int smem_bytes);
 // entry sort of the cut-off sweep: bin, scan, scatter (hist must be zeroed)
-cudaError_t launch_cull_sort(const DevCull& cull, const Scratch& s, const float* lig_q, int B,
-                             int L, const CullSegs& seg, const CullScratch& cs, cudaStream_t st);
+cudaError_t launch_cull_sort(const Scratch& s, const float* lig_q, int B, int L,
+                             const CullSegs& seg, const CullScratch& cs, cudaStream_t st);
 cudaError_t launch_pairs_cull(const DevCull& cull, const float4* tab, const CullSegs& seg,
                               const CullScratch& cs, int flags, const Physics& ph,
                               const CullPlan& plan, int* d_err, cudaStream_t st);
