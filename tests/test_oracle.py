@@ -141,6 +141,35 @@ def test_c_vs_numpy_inter(oracle, ph):
             e_c, rel=1e-12)
 
 
+@pytest.mark.parametrize("ph", [dict(), dict(inter_form=1), dict(dielectric=1)])
+def test_c_vs_numpy_inter_parts(oracle, ph):
+    """orc_ene_inter_parts (the electrostatic and van der Waals parts of
+    Mol.ene_inter_UFF_shifted_bst_components, mol.ml:920-957) against the same
+    parts summed in NumPy; their sum is the oracle's ene_inter."""
+    from oracle import np_twin as T
+
+    s = synth.single_pose(seed=7)
+    xyz, _ = oracle.apply_config(s.ligand, s.poses[0].astype(np.float64))
+    p, l = s.pocket, s.ligand
+    el, lj = oracle.ene_inter_parts(p, l, xyz, ph=oracle.physics(**ph))
+    xp, dp = T.params(p.anum)
+    xl, dl = T.params(l.anum)
+    d = np.linalg.norm(p.xyz()[:, None, :] - xyz[None, :, :], axis=2)
+    r = np.maximum(d, 0.01)
+    if ph.get("inter_form", 0) == 0:
+        w = np.where(d * d < 144.0, (1.0 - (r / 12.0) ** 2) ** 2, 0.0)
+    else:
+        w = np.ones_like(r)
+    qq = p.q[:, None] * l.q[None, :]
+    el_n = (w * T.ELEC * (qq / r if ph.get("dielectric", 0) == 0 else qq / (r * r))).sum()
+    p6 = (np.sqrt(xp[:, None] * xl[None, :]) / r) ** 6
+    lj_n = (w * np.sqrt(dp[:, None] * dl[None, :]) * (p6 * p6 - 2.0 * p6)).sum()
+    assert el == pytest.approx(el_n, rel=1e-12, abs=1e-12)
+    assert lj == pytest.approx(lj_n, rel=1e-12, abs=1e-12)
+    assert el + lj == pytest.approx(oracle.ene_inter(p, l, xyz, ph=oracle.physics(**ph)),
+                                    rel=1e-12)
+
+
 def test_c_vs_numpy_intra_and_pose(oracle, rng):
     from oracle import np_twin as T
 
